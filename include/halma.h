@@ -1,0 +1,217 @@
+/*
+ * halma.h — C ABI of the GB300 (sm_103a) halo-finding hot path.
+ *
+ * Every entry point returns an int status (HALMA_OK = 0, negative on error) and never
+ * throws.  Array arguments are plain pointers that may live in host memory (pageable or
+ * pinned) or in device memory of the current CUDA device; the library detects which.
+ *   - device pointers: work is queued on `stream` (a cudaStream_t, NULL = legacy default
+ *     stream) and the call returns without synchronising unless a count must be returned;
+ *   - host pointers: inputs are copied in and outputs copied back on `stream`, and the call
+ *     synchronises the stream before returning.
+ * The caller owns every buffer it passes.  The library keeps one cached device workspace
+ * per device (grown on demand, released by halma_release_workspace) and serialises calls
+ * that use it with a mutex.  A human-readable reason for the last failure on the calling
+ * thread is returned by halma_last_error().
+ *
+ * Reference interfaces replaced (pyHALMA, paths inside its repository):
+ *   halma_fof / halma_fof_groups  <- python_scripts/fof.py:18-79 friends_of_friends
+ *                                    (+ fof.py:87-89 serial wrapper, pyHALMA.py:148-149
+ *                                    good_groups for the min-member filter)
+ *   halma_bf_potential_f32        <- fortran_modules/particle_subroutines.f90:466-514
+ *                                    brute_force_binding_energy, bound by f2py as
+ *                                    particle.particle.brute_force_binding_energy(ncores,
+ *                                    ntotal, total_mass, total_x, total_y, total_z, ntest,
+ *                                    test_x, test_y, test_z) (halo_gas.py:182-186)
+ *   halma_potential_f64           <- same loop in FP64 (the plain per-halo GPU comparator)
+ *   halma_halo_reductions         <- python_scripts/halo_properties.py:16-60 total_mass,
+ *                                    center_of_mass, CM_velocity; :98-111
+ *                                    furthest_particle; :365-392 half_mass_radius;
+ *                                    :607-625 sigma_effective
+ *   halma_unbind_batched          <- halo_properties.py:282-361
+ *                                    escape_velocity_unbinding_fortran (single pass),
+ *                                    iterated until no particle is removed
+ *   halma_potential_grad_f32      <- no reference counterpart (adjoint of the potential)
+ */
+#ifndef HALMA_H
+#define HALMA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define HALMA_ABI_VERSION 1
+
+#define HALMA_OK                 0
+#define HALMA_ERR_INVALID       -1   /* bad argument (size, NaN input, null pointer)   */
+#define HALMA_ERR_NOMEM         -2   /* device or pinned allocation failed              */
+#define HALMA_ERR_CUDA          -3   /* a CUDA runtime call failed                      */
+#define HALMA_ERR_NOT_CONVERGED -4   /* iteration cap reached (union-find, unbinding)   */
+#define HALMA_ERR_TIMEOUT       -5   /* a bounded device-side wait ran out              */
+#define HALMA_ERR_CAPACITY      -6   /* input exceeds a documented capacity             */
+#define HALMA_ERR_NO_DEVICE     -7   /* no CUDA device visible                          */
+
+typedef void *halma_stream_t;        /* cudaStream_t */
+
+int         halma_abi_version(void);
+const char *halma_status_string(int status);
+const char *halma_last_error(void);
+int         halma_release_workspace(void);
+/* Number of kernels this library launched since load (all entry points, all devices). */
+int64_t     halma_kernel_launch_count(void);
+
+/* ------------------------------------------------------------------------------------ */
+/* Friends-of-friends                                                                   */
+/* ------------------------------------------------------------------------------------ */
+/* labels[i] = smallest index of i's FoF component, or -1 if i has no friend.  Pair rule:
+ * ((dx*dx + dy*dy) + dz*dz) <= ll*ll in IEEE double (inclusive, non-periodic), exactly the
+ * predicate of scipy's KDTree.query_ball_point used by fof.py:40,61.
+ * n_groups (optional) receives the number of components with >= 2 members. */
+int halma_fof(int64_t n, const double *x, const double *y, const double *z,
+              double linking_length, int32_t *labels, int64_t *n_groups,
+              halma_stream_t stream);
+
+/* Groups in the reference's output order (fof.py:76-77): groups ordered by smallest member,
+ * members ascending, only groups with >= min_members members (pyHALMA.py:148-149).
+ * members must hold n entries and offsets n+1 entries.  On return *n_groups groups are
+ * stored: members[offsets[g] .. offsets[g+1]). */
+int halma_fof_groups(int64_t n, const int32_t *labels, int32_t min_members,
+                     int64_t *offsets, int32_t *members, int64_t *n_groups,
+                     halma_stream_t stream);
+
+/* ------------------------------------------------------------------------------------ */
+/* Brute-force potential                                                                */
+/* ------------------------------------------------------------------------------------ */
+#define HALMA_POT_REFERENCE 0   /* per target, float32 sequential sum in source order:
+                                   bit-identical to particle_subroutines.f90:497-510
+                                   (each operation rounded, no FMA); eps2 must be 0     */
+#define HALMA_POT_FAST      1   /* float32 pair terms (rsqrt), compensated summation    */
+
+/* phi_i = sum_j m_j / sqrt(r_ij^2 + eps2), skipping source j unless its x, y and z all
+ * differ from target i's (f90:499-501).  Inputs are float32 as the f2py wrapper casts them
+ * (halo_gas.py:172-178). */
+int halma_bf_potential_f32(int64_t ntotal, const float *total_mass, const float *total_x,
+                           const float *total_y, const float *total_z, int64_t ntest,
+                           const float *test_x, const float *test_y, const float *test_z,
+                           float *binding_energy, int32_t mode, double eps2,
+                           halma_stream_t stream);
+
+#define HALMA_MASK_COORD 0   /* the reference's coordinate-inequality mask              */
+#define HALMA_MASK_SELF  1   /* skip source j == i + self_offset only                   */
+#define HALMA_MASK_NONE  2
+
+/* float32 pair terms (rsqrt) with compensated sums and a selectable mask: the smooth
+ * (differentiable) forward of halma_potential_grad_f32 when mask is SELF or NONE.
+ * No reference counterpart beyond the potential above. */
+int halma_potential_f32(int64_t ns, const float *m, const float *sx, const float *sy,
+                        const float *sz, int64_t nt, const float *tx, const float *ty,
+                        const float *tz, double eps2, int32_t mask, int64_t self_offset,
+                        float *phi, halma_stream_t stream);
+
+/* FP64 pairs and FP64 sum, one thread per target (the plain comparator path). */
+int halma_potential_f64(int64_t ns, const double *m, const double *sx, const double *sy,
+                        const double *sz, int64_t nt, const double *tx, const double *ty,
+                        const double *tz, double eps2, int32_t mask, int64_t self_offset,
+                        double *phi, halma_stream_t stream);
+
+/* Adjoint of phi_i = sum_j m_j (r_ij^2 + eps2)^-1/2 (mask SELF or NONE) for an upstream
+ * gradient g_i = dL/dphi_i.  Outputs (any may be NULL):
+ *   grad_m[j]          = sum_i g_i (r^2+eps2)^-1/2
+ *   grad_src[3j+k]     = m_j sum_i g_i (t_i - s_j)_k (r^2+eps2)^-3/2
+ *   grad_tgt[3i+k]     = g_i sum_j m_j (s_j - t_i)_k (r^2+eps2)^-3/2
+ * float32 pair terms with compensated sums. */
+int halma_potential_grad_f32(int64_t ns, const float *m, const float *sx, const float *sy,
+                             const float *sz, int64_t nt, const float *tx, const float *ty,
+                             const float *tz, const float *g, double eps2, int32_t mask,
+                             int64_t self_offset, float *grad_m, float *grad_src,
+                             float *grad_tgt, halma_stream_t stream);
+
+/* ------------------------------------------------------------------------------------ */
+/* Per-halo reductions (FP64)                                                           */
+/* ------------------------------------------------------------------------------------ */
+/* Haloes are CSR segments: halo h owns rows offsets[h] .. offsets[h+1] of the particle
+ * arrays (halo-contiguous order).  mask (optional, uint8) selects the particles that take
+ * part.  out is n_haloes x HALMA_RED_NFIELDS doubles, row-major. */
+enum {
+    HALMA_RED_MASS = 0,  /* total_mass                                  */
+    HALMA_RED_CX, HALMA_RED_CY, HALMA_RED_CZ,      /* center_of_mass    */
+    HALMA_RED_VX, HALMA_RED_VY, HALMA_RED_VZ,      /* CM_velocity       */
+    HALMA_RED_RMAX,      /* furthest_particle from the centre of mass  */
+    HALMA_RED_R05,       /* half_mass_radius                           */
+    HALMA_RED_SIGMA,     /* sigma_effective inside R05                 */
+    HALMA_RED_N,         /* members taking part                        */
+    HALMA_RED_NFIELDS
+};
+/* about (optional, n_haloes x HALMA_ABOUT_NFIELDS): per-halo values supplied by the caller
+ * in place of the computed ones, as the reference functions take them as arguments
+ * (furthest_particle and half_mass_radius take the centre and M, sigma_effective the
+ * centre, bulk velocity and R05).  A NaN entry means "use the computed value". */
+enum {
+    HALMA_ABOUT_CX = 0, HALMA_ABOUT_CY, HALMA_ABOUT_CZ, HALMA_ABOUT_VX, HALMA_ABOUT_VY,
+    HALMA_ABOUT_VZ, HALMA_ABOUT_MASS, HALMA_ABOUT_R05, HALMA_ABOUT_NFIELDS
+};
+int halma_halo_reductions(int64_t n, int64_t n_haloes, const int64_t *offsets,
+                          const double *x, const double *y, const double *z,
+                          const double *vx, const double *vy, const double *vz,
+                          const double *m, const uint8_t *mask, const double *about,
+                          double *out, halma_stream_t stream);
+
+/* ------------------------------------------------------------------------------------ */
+/* Batched iterative unbinding                                                          */
+/* ------------------------------------------------------------------------------------ */
+#define HALMA_UNBIND_FP32C 0   /* float32 pair terms, compensated sums, FP64 reductions */
+#define HALMA_UNBIND_FP64  1   /* plain FP64 per-halo path: one launch per halo         */
+
+typedef struct {
+    double  eps;        /* softening length (position units), must be > 0               */
+    double  G;          /* gravitational constant: velocity^2 * length / mass           */
+    double  factor_v;   /* potential multiplied by factor_v^2 (halo_properties.py:353)  */
+    int32_t max_iter;   /* passes at most (>= 1)                                        */
+    int32_t precision;  /* HALMA_UNBIND_FP32C or HALMA_UNBIND_FP64                      */
+    int32_t use_graph;  /* FP32C: replay all passes as one captured CUDA graph          */
+    int32_t reserved;
+} halma_unbind_params;
+
+enum {
+    HALMA_UB_MASS = 0, HALMA_UB_CX, HALMA_UB_CY, HALMA_UB_CZ, HALMA_UB_VX, HALMA_UB_VY,
+    HALMA_UB_VZ, HALMA_UB_NBOUND, HALMA_UB_ITER, HALMA_UB_EKIN, HALMA_UB_EPOT,
+    HALMA_UB_NFIELDS
+};
+
+/* Particles in halo-contiguous order (CSR offsets, n_haloes+1 entries).  Every pass
+ * recomputes each halo's FP64 bound mass, centre and bulk velocity, the potential of the
+ * bound particles due to the bound particles (self pair excluded), and removes particles
+ * with 1/2|v - v_bulk|^2 - G * factor_v^2 * phi > 0.  Outputs: bound[n] (1 = bound),
+ * phi[n] (optional, last pass, FP64; 0 for removed particles), halo_out (n_haloes x
+ * HALMA_UB_NFIELDS, row-major; EKIN = sum 1/2 m |v - v_bulk|^2 and EPOT = -1/2 G
+ * factor_v^2 sum m phi over the bound particles of the last pass). */
+int halma_unbind_batched(int64_t n, int64_t n_haloes, const int64_t *offsets,
+                         const double *x, const double *y, const double *z,
+                         const double *vx, const double *vy, const double *vz,
+                         const double *m, const halma_unbind_params *params,
+                         uint8_t *bound, double *phi, double *halo_out,
+                         halma_stream_t stream);
+
+/* ------------------------------------------------------------------------------------ */
+/* One snapshot end to end                                                              */
+/* ------------------------------------------------------------------------------------ */
+/* The driver's star-particle path (pyHALMA.py:543-592 FoF + good_groups, then the per-halo
+ * unbinding above) in one call: halma_fof -> groups with >= min_members members in the
+ * reference order -> halma_unbind_batched over those groups.  Outputs (each optional except
+ * n_haloes): labels[n] (FoF labels), bound[n] (1 = member of a kept group that survived the
+ * unbinding), halo_offsets[cap+1] / members[n] (the groups as CSR over particle indices) and
+ * halo_out[cap x HALMA_UB_NFIELDS].  Returns HALMA_ERR_CAPACITY (with *n_haloes set) when
+ * more than halo_capacity groups were found and halo_offsets or halo_out was requested. */
+int halma_find_haloes(int64_t n, const double *x, const double *y, const double *z,
+                      const double *vx, const double *vy, const double *vz, const double *m,
+                      double linking_length, int32_t min_members,
+                      const halma_unbind_params *params, int32_t *labels, uint8_t *bound,
+                      int64_t *n_haloes, int64_t halo_capacity, int64_t *halo_offsets,
+                      int32_t *members, double *halo_out, halma_stream_t stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* HALMA_H */

@@ -1,0 +1,152 @@
+"""ctypes binding of libhalma_gb300.so (the C ABI declared in include/halma.h).
+
+The library is loaded from the package directory only.  There is no CPU fallback: if the
+shared library is missing the import of any compute function fails with ``ImportError``
+telling the user to build it (``python -c "import pyhalma_gb300.build as b; b.build()"``).
+Arrays cross the boundary as raw pointers: NumPy arrays (host memory; the library copies them
+to the device and back) or CUDA torch tensors (device memory, used in place on the current
+torch stream).
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import threading
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libhalma_gb300.so")
+
+OK = 0
+ERR_INVALID = -1
+ERR_NOMEM = -2
+ERR_CUDA = -3
+ERR_NOT_CONVERGED = -4
+ERR_TIMEOUT = -5
+ERR_CAPACITY = -6
+ERR_NO_DEVICE = -7
+
+POT_REFERENCE = 0
+POT_FAST = 1
+MASK_COORD, MASK_SELF, MASK_NONE = 0, 1, 2
+UNBIND_FP32C, UNBIND_FP64 = 0, 1
+
+RED_FIELDS = ["mass", "cx", "cy", "cz", "vx", "vy", "vz", "rmax", "r05", "sigma", "n"]
+UB_FIELDS = ["mass", "cx", "cy", "cz", "vx", "vy", "vz", "n_bound", "iterations", "e_kin", "e_pot"]
+
+
+class HalmaError(RuntimeError):
+    def __init__(self, status, where, detail):
+        self.status = status
+        super().__init__(f"{where}: {detail} (status {status})")
+
+
+class UnbindParams(ctypes.Structure):
+    _fields_ = [("eps", ctypes.c_double), ("G", ctypes.c_double), ("factor_v", ctypes.c_double),
+                ("max_iter", ctypes.c_int32), ("precision", ctypes.c_int32),
+                ("use_graph", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+
+
+_lock = threading.Lock()
+_lib = None
+
+_P = ctypes.c_void_p
+_I64 = ctypes.c_int64
+_I32 = ctypes.c_int32
+_F64 = ctypes.c_double
+
+SIGNATURES = {
+    "halma_abi_version": ([], ctypes.c_int),
+    "halma_status_string": ([ctypes.c_int], ctypes.c_char_p),
+    "halma_last_error": ([], ctypes.c_char_p),
+    "halma_release_workspace": ([], ctypes.c_int),
+    "halma_kernel_launch_count": ([], ctypes.c_int64),
+    "halma_fof": ([_I64, _P, _P, _P, _F64, _P, _P, _P], ctypes.c_int),
+    "halma_fof_groups": ([_I64, _P, _I32, _P, _P, _P, _P], ctypes.c_int),
+    "halma_bf_potential_f32": ([_I64, _P, _P, _P, _P, _I64, _P, _P, _P, _P, _I32, _F64, _P], ctypes.c_int),
+    "halma_potential_f64": ([_I64, _P, _P, _P, _P, _I64, _P, _P, _P, _F64, _I32, _I64, _P, _P], ctypes.c_int),
+    "halma_potential_f32": ([_I64, _P, _P, _P, _P, _I64, _P, _P, _P, _F64, _I32, _I64, _P, _P], ctypes.c_int),
+    "halma_potential_grad_f32": ([_I64, _P, _P, _P, _P, _I64, _P, _P, _P, _P, _F64, _I32, _I64, _P, _P, _P, _P],
+                                 ctypes.c_int),
+    "halma_halo_reductions": ([_I64, _I64, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P], ctypes.c_int),
+    "halma_unbind_batched": ([_I64, _I64, _P, _P, _P, _P, _P, _P, _P, _P, ctypes.POINTER(UnbindParams), _P, _P, _P,
+                              _P], ctypes.c_int),
+    "halma_find_haloes": ([_I64, _P, _P, _P, _P, _P, _P, _P, _F64, _I32, ctypes.POINTER(UnbindParams), _P, _P, _P,
+                           _I64, _P, _P, _P, _P], ctypes.c_int),
+}
+
+
+def lib():
+    """The loaded library; raises ImportError if it has not been built."""
+    global _lib
+    with _lock:
+        if _lib is None:
+            if not os.path.exists(LIB_PATH):
+                raise ImportError(
+                    f"{LIB_PATH} is missing: build the CUDA extension first "
+                    "(python -c 'import pyhalma_gb300.build as b; b.build()'); there is no CPU fallback")
+            L = ctypes.CDLL(LIB_PATH)
+            for name, (args, res) in SIGNATURES.items():
+                fn = getattr(L, name)
+                fn.argtypes = args
+                fn.restype = res
+            _lib = L
+    return _lib
+
+
+def check(status, where):
+    if status == OK:
+        return
+    detail = lib().halma_last_error().decode(errors="replace")
+    if status == ERR_INVALID:
+        raise ValueError(f"{where}: {detail}")
+    raise HalmaError(status, where, detail)
+
+
+def launch_count() -> int:
+    return int(lib().halma_kernel_launch_count())
+
+
+# ---------------------------------------------------------------------------------------
+# array plumbing
+# ---------------------------------------------------------------------------------------
+def _is_torch(a):
+    return type(a).__module__.startswith("torch")
+
+
+def ptr(a):
+    """Raw pointer of a contiguous NumPy array or torch tensor (None -> NULL)."""
+    if a is None:
+        return None
+    if _is_torch(a):
+        if not a.is_contiguous():
+            raise ValueError("torch tensors passed to the library must be contiguous")
+        return ctypes.c_void_p(a.data_ptr())
+    if not a.flags["C_CONTIGUOUS"]:
+        raise ValueError("arrays passed to the library must be C-contiguous")
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def stream_of(*arrays):
+    """The current torch stream if any argument lives on a CUDA device, else NULL."""
+    for a in arrays:
+        if a is not None and _is_torch(a) and a.is_cuda:
+            import torch
+            return ctypes.c_void_p(torch.cuda.current_stream(a.device).cuda_stream)
+    return None
+
+
+def as_host(a, dtype):
+    """Contiguous NumPy array of the given dtype (copy only when needed)."""
+    return np.ascontiguousarray(a, dtype=dtype)
+
+
+def like(a, shape, dtype):
+    """An output buffer on the same side (host NumPy / device torch) as `a`."""
+    if _is_torch(a):
+        import torch
+        tmap = {np.float32: torch.float32, np.float64: torch.float64, np.int32: torch.int32,
+                np.int64: torch.int64, np.uint8: torch.uint8}
+        return torch.empty(shape, dtype=tmap[np.dtype(dtype).type], device=a.device)
+    return np.empty(shape, dtype=dtype)

@@ -1,0 +1,660 @@
+// Friends-of-friends on the GPU: the C ABI that replaces python_scripts/fof.py:18-79.
+//
+// Pipeline (all on one stream):
+//   1. bounding box (FP64) -> host picks the cell geometry (cell side = ll * (1 + 2^-20));
+//   2. each particle gets a row-major cell key; keys are radix-sorted with their indices;
+//   3. per sorted particle: a float4 record (position inside its cell in units of ll, and
+//      the original index), run heads of equal keys -> cell table + open-addressing hash
+//      from cell key to cell id;
+//   4. work items = 32-particle chunks of a cell; one warp per item tests its particles
+//      against the same cell and the 13 neighbour cells that sort after it, staging each
+//      neighbour chunk in shared memory (coalesced float4 loads, broadcast reads);
+//   5. a pair whose float32 distance is clearly inside (outside) the linking length is
+//      accepted (rejected); pairs in a +-1e-5 band are re-tested with the exact FP64
+//      predicate ((dx*dx + dy*dy) + dz*dz) <= ll*ll, every operation rounded on its own;
+//   6. accepted pairs join a lock-free union-find over sorted positions (atomicCAS hooks
+//      the larger root under the smaller one, path halving on every find);
+//   7. each component's label = the smallest ORIGINAL index among its members
+//      (atomicMin), -1 for particles that never linked.
+// The result is the reference's partition exactly: same components, same canonical labels.
+#include <math.h>
+#include <limits.h>
+
+#include "common.cuh"
+#include "sort.cuh"
+
+namespace halma {
+
+namespace {
+
+constexpr int kFofWarps = 8;
+constexpr uint64_t kEmptyKey = ~0ull;
+constexpr int kUfCap = 1 << 26;      // bound on any union-find loop (never reached in practice)
+
+struct FofGeom {
+    double xmin, ymin, zmin;
+    double cell, inv_cell, inv_scale, r2;
+    float cs, lo, hi;
+    long long ncx, ncy, ncz;
+};
+
+__device__ __forceinline__ uint64_t mix64(uint64_t k) {
+    // MurmurHash3 64-bit finaliser
+    k ^= k >> 33;
+    k *= 0xff51afd7ed558ccdull;
+    k ^= k >> 33;
+    k *= 0xc4ceb9fe1a85ec53ull;
+    k ^= k >> 33;
+    return k;
+}
+
+__device__ __forceinline__ int uf_find(int *parent, int v, int *err) {
+    int p = __ldcg(parent + v);
+    int guard = 0;
+    while (p != v) {
+        const int gp = __ldcg(parent + p);
+        if (gp != p) __stcg(parent + v, gp);   // path halving: gp is an ancestor of v
+        v = p;
+        p = gp;
+        if (++guard > kUfCap) {
+            atomicOr(err, 1);
+            break;
+        }
+    }
+    return v;
+}
+
+// Hooks the larger of two roots under the smaller; retries from the new parent when the
+// CAS loses a race.  Every root of a tree is its smallest sorted position.
+__device__ __forceinline__ void uf_union(int *parent, int a, int b, int *err) {
+    int guard = 0;
+    while (a != b) {
+        if (a < b) {
+            const int t = a;
+            a = b;
+            b = t;
+        }
+        const int old = atomicCAS(parent + a, a, b);
+        if (old == a) return;
+        a = uf_find(parent, old, err);
+        b = uf_find(parent, b, err);
+        if (++guard > kUfCap) {
+            atomicOr(err, 1);
+            return;
+        }
+    }
+}
+
+__global__ void bbox_partial_kernel(const double *__restrict__ x, const double *__restrict__ y,
+                                    const double *__restrict__ z, int n, double *__restrict__ part) {
+    double mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
+    double bad = 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const double v[3] = {x[i], y[i], z[i]};
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            if (!isfinite(v[d])) bad = 1.0;
+            mn[d] = fmin(mn[d], v[d]);
+            mx[d] = fmax(mx[d], v[d]);
+        }
+    }
+    __shared__ double sh[7][32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    double vals[7] = {mn[0], mn[1], mn[2], mx[0], mx[1], mx[2], bad};
+#pragma unroll
+    for (int q = 0; q < 7; ++q) {
+        double v = vals[q];
+        for (int o = 16; o > 0; o >>= 1) {
+            const double u = __shfl_down_sync(0xffffffffu, v, o);
+            v = (q < 3) ? fmin(v, u) : fmax(v, u);
+        }
+        if (lane == 0) sh[q][w] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < 7) {
+        const int q = threadIdx.x;
+        double v = sh[q][0];
+        for (int k = 1; k < (int)(blockDim.x >> 5); ++k) v = (q < 3) ? fmin(v, sh[q][k]) : fmax(v, sh[q][k]);
+        part[blockIdx.x * 7 + q] = v;
+    }
+}
+
+__global__ void bbox_final_kernel(const double *__restrict__ part, int g, double *__restrict__ out) {
+    if (threadIdx.x < 7) {
+        const int q = threadIdx.x;
+        double v = part[q];
+        for (int k = 1; k < g; ++k) v = (q < 3) ? fmin(v, part[k * 7 + q]) : fmax(v, part[k * 7 + q]);
+        out[q] = v;
+    }
+}
+
+__global__ void keys_kernel(const double *__restrict__ x, const double *__restrict__ y,
+                            const double *__restrict__ z, int n, FofGeom g,
+                            uint64_t *__restrict__ keys, int *__restrict__ vals) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        long long cx = (long long)floor((x[i] - g.xmin) * g.inv_cell);
+        long long cy = (long long)floor((y[i] - g.ymin) * g.inv_cell);
+        long long cz = (long long)floor((z[i] - g.zmin) * g.inv_cell);
+        cx = min(max(cx, 0ll), g.ncx - 1);
+        cy = min(max(cy, 0ll), g.ncy - 1);
+        cz = min(max(cz, 0ll), g.ncz - 1);
+        keys[i] = ((uint64_t)cx * (uint64_t)g.ncy + (uint64_t)cy) * (uint64_t)g.ncz + (uint64_t)cz;
+        vals[i] = i;
+    }
+}
+
+__device__ __forceinline__ void decode_key(uint64_t key, const FofGeom &g, long long &cx, long long &cy,
+                                           long long &cz) {
+    cz = (long long)(key % (uint64_t)g.ncz);
+    const uint64_t t = key / (uint64_t)g.ncz;
+    cy = (long long)(t % (uint64_t)g.ncy);
+    cx = (long long)(t / (uint64_t)g.ncy);
+}
+
+// Sorted records, run heads, union-find / label initialisation.
+__global__ void prep_kernel(const double *__restrict__ x, const double *__restrict__ y,
+                            const double *__restrict__ z, int n, FofGeom g,
+                            const uint64_t *__restrict__ keys, const int *__restrict__ idx,
+                            float4 *__restrict__ rec, int *__restrict__ head, int *__restrict__ parent,
+                            unsigned char *__restrict__ has, int *__restrict__ minidx) {
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        const uint64_t key = keys[k];
+        long long cx, cy, cz;
+        decode_key(key, g, cx, cy, cz);
+        const int i = idx[k];
+        const double ox = g.xmin + (double)cx * g.cell;
+        const double oy = g.ymin + (double)cy * g.cell;
+        const double oz = g.zmin + (double)cz * g.cell;
+        rec[k] = make_float4((float)((x[i] - ox) * g.inv_scale), (float)((y[i] - oy) * g.inv_scale),
+                             (float)((z[i] - oz) * g.inv_scale), __int_as_float(i));
+        head[k] = (k == 0 || keys[k - 1] != key) ? 1 : 0;
+        parent[k] = k;
+        has[k] = 0;
+        minidx[k] = INT_MAX;
+    }
+}
+
+// Cell table + hash insert, from the exclusive scan of the run heads.
+__global__ void cells_kernel(int n, const uint64_t *__restrict__ keys, const int *__restrict__ head,
+                             const int *__restrict__ cellpos, int *__restrict__ cell_start,
+                             uint64_t *__restrict__ cell_key, uint64_t *__restrict__ hkeys,
+                             int *__restrict__ hvals, uint64_t hmask, int *__restrict__ ncell) {
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        if (head[k]) {
+            const int c = cellpos[k];
+            const uint64_t key = keys[k];
+            cell_start[c] = k;
+            cell_key[c] = key;
+            uint64_t h = mix64(key) & hmask;
+            for (uint64_t probe = 0; probe <= hmask; ++probe) {
+                const unsigned long long prev =
+                    atomicCAS((unsigned long long *)(hkeys + h), (unsigned long long)kEmptyKey,
+                              (unsigned long long)key);
+                if (prev == kEmptyKey || prev == key) {
+                    hvals[h] = c;
+                    break;
+                }
+                h = (h + 1) & hmask;
+            }
+        }
+        if (k == n - 1) {
+            const int m = cellpos[k] + head[k];
+            *ncell = m;
+            cell_start[m] = n;
+        }
+    }
+}
+
+// Marks the first particle of every 32-particle chunk of every cell.
+__global__ void itemflag_kernel(int n, const int *__restrict__ head, const int *__restrict__ cellpos,
+                                const int *__restrict__ cell_start, int *__restrict__ flag) {
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        const int c = cellpos[k] + head[k] - 1;
+        flag[k] = ((k - cell_start[c]) & 31) == 0 ? 1 : 0;
+    }
+}
+
+__global__ void items_kernel(int n, const int *__restrict__ head, const int *__restrict__ cellpos,
+                             const int *__restrict__ flag, const int *__restrict__ itempos,
+                             int *__restrict__ item_k0, int *__restrict__ item_cell, int *__restrict__ nitems) {
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        if (flag[k]) {
+            item_k0[itempos[k]] = k;
+            item_cell[itempos[k]] = cellpos[k] + head[k] - 1;
+        }
+        if (k == n - 1) *nitems = itempos[k] + flag[k];
+    }
+}
+
+__device__ __forceinline__ int hash_lookup(const uint64_t *__restrict__ hkeys, const int *__restrict__ hvals,
+                                           uint64_t hmask, uint64_t key) {
+    uint64_t h = mix64(key) & hmask;
+    for (uint64_t probe = 0; probe <= hmask; ++probe) {
+        const uint64_t k = hkeys[h];
+        if (k == key) return hvals[h];
+        if (k == kEmptyKey) return -1;
+        h = (h + 1) & hmask;
+    }
+    return -1;
+}
+
+__device__ __forceinline__ bool exact_link(const double *__restrict__ x, const double *__restrict__ y,
+                                           const double *__restrict__ z, int i, int j, double r2) {
+    // scipy's p = 2 distance: ((dx*dx + dy*dy) + dz*dz) <= r*r, each operation rounded
+    const double dx = __dsub_rn(x[i], x[j]);
+    const double dy = __dsub_rn(y[i], y[j]);
+    const double dz = __dsub_rn(z[i], z[j]);
+    double s = __dmul_rn(dx, dx);
+    s = __dadd_rn(s, __dmul_rn(dy, dy));
+    s = __dadd_rn(s, __dmul_rn(dz, dz));
+    return s <= r2;
+}
+
+__constant__ int c_stencil[13][3] = {{0, 0, 1},  {0, 1, -1}, {0, 1, 0},  {0, 1, 1},  {1, -1, -1},
+                                     {1, -1, 0}, {1, -1, 1}, {1, 0, -1}, {1, 0, 0},  {1, 0, 1},
+                                     {1, 1, -1}, {1, 1, 0},  {1, 1, 1}};
+
+__global__ void __launch_bounds__(256) link_kernel(
+    const float4 *__restrict__ rec, const int *__restrict__ cell_start, const uint64_t *__restrict__ cell_key,
+    const int *__restrict__ item_k0, const int *__restrict__ item_cell, const int *__restrict__ nitems_p,
+    const uint64_t *__restrict__ hkeys, const int *__restrict__ hvals, uint64_t hmask, FofGeom g,
+    const double *__restrict__ x, const double *__restrict__ y, const double *__restrict__ z,
+    int *parent, unsigned char *has, int *err) {
+    __shared__ float4 buf[kFofWarps][32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int nitems = *nitems_p;
+    for (int item = blockIdx.x * kFofWarps + w; item < nitems; item += gridDim.x * kFofWarps) {
+        const int c = item_cell[item];
+        const int k0 = item_k0[item];
+        const int ce = cell_start[c + 1];
+        const int k = k0 + lane;
+        const bool hv = k < ce;
+        const float4 hp = hv ? rec[k] : make_float4(0.f, 0.f, 0.f, 0.f);
+        const int hidx = __float_as_int(hp.w);
+        int myroot = hv ? uf_find(parent, k, err) : -1;
+        long long cx, cy, cz;
+        decode_key(cell_key[c], g, cx, cy, cz);
+        for (int nb = -1; nb < 13; ++nb) {
+            int js, je, ox = 0, oy = 0, oz = 0;
+            if (nb < 0) {
+                js = cell_start[c];
+                je = ce;
+            } else {
+                ox = c_stencil[nb][0];
+                oy = c_stencil[nb][1];
+                oz = c_stencil[nb][2];
+                const long long nx = cx + ox, ny = cy + oy, nz = cz + oz;
+                if (nx >= g.ncx || ny < 0 || ny >= g.ncy || nz < 0 || nz >= g.ncz) continue;
+                const uint64_t nkey = ((uint64_t)nx * (uint64_t)g.ncy + (uint64_t)ny) * (uint64_t)g.ncz + (uint64_t)nz;
+                const int cc = hash_lookup(hkeys, hvals, hmask, nkey);
+                if (cc < 0) continue;
+                js = cell_start[cc];
+                je = cell_start[cc + 1];
+            }
+            // home position expressed in the neighbour cell's frame
+            const float hx = hp.x - (float)ox * g.cs;
+            const float hy = hp.y - (float)oy * g.cs;
+            const float hz = hp.z - (float)oz * g.cs;
+            for (int j0 = js; j0 < je; j0 += 32) {
+                const int jl = j0 + lane;
+                const float4 q = jl < je ? rec[jl] : make_float4(0.f, 0.f, 0.f, 0.f);
+                __syncwarp();
+                buf[w][lane] = q;
+                __syncwarp();
+                const int cnt = min(32, je - j0);
+                for (int t = 0; t < cnt; ++t) {
+                    const float4 qq = buf[w][t];
+                    const int jj = j0 + t;
+                    const float dx = qq.x - hx, dy = qq.y - hy, dz = qq.z - hz;
+                    const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                    bool hit = hv && d2 <= g.hi && (nb >= 0 || jj > k);
+                    if (hit && d2 >= g.lo) hit = exact_link(x, y, z, hidx, __float_as_int(qq.w), g.r2);
+                    if (hit) {
+                        const int rq = uf_find(parent, jj, err);
+                        if (rq != myroot) {
+                            uf_union(parent, myroot, rq, err);
+                            has[k] = 1;
+                            has[jj] = 1;
+                            myroot = uf_find(parent, k, err);
+                        }
+                    }
+                }
+            }
+        }
+    }
+}
+
+__global__ void root_kernel(int n, const float4 *__restrict__ rec, int *parent,
+                            const unsigned char *__restrict__ has, int *__restrict__ root,
+                            int *__restrict__ minidx, int *err) {
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        const int r = uf_find(parent, k, err);
+        root[k] = r;
+        if (has[k]) atomicMin(minidx + r, __float_as_int(rec[k].w));
+    }
+}
+
+__global__ void label_kernel(int n, const float4 *__restrict__ rec, const unsigned char *__restrict__ has,
+                             const int *__restrict__ root, const int *__restrict__ minidx,
+                             int *__restrict__ labels, int *__restrict__ ngroups) {
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        const int i = __float_as_int(rec[k].w);
+        const int r = root[k];
+        labels[i] = has[k] ? minidx[r] : -1;
+        if (has[k] && r == k) atomicAdd(ngroups, 1);
+    }
+}
+
+int bits_for(uint64_t v) {
+    int b = 0;
+    while (b < 64 && (v >> b) != 0) ++b;
+    return b < 1 ? 1 : b;
+}
+
+}  // namespace
+
+// Full FoF on device arrays (no staging, no locking); used by halma_fof and the pipeline.
+int fof_device(int n, const double *x, const double *y, const double *z, double ll, int *labels,
+               int64_t *n_groups, cudaStream_t st) {
+    if (n == 0) {
+        if (n_groups) *n_groups = 0;
+        return HALMA_OK;
+    }
+    const int sms = device_sm_count();
+    const int gb = std::min(sms * 4, grid_for(n, 256));
+    // pass 1: bounding box
+    {
+        Layout L;
+        const size_t o_part = L.add(sizeof(double) * 7 * gb);
+        const size_t o_out = L.add(sizeof(double) * 8);
+        void *base = nullptr;
+        HALMA_TRY(workspace(L.total, &base, st));
+        HALMA_LAUNCH(bbox_partial_kernel, gb, 256, 0, st, x, y, z, n, at<double>(base, o_part));
+        HALMA_LAUNCH(bbox_final_kernel, 1, 32, 0, st, at<double>(base, o_part), gb, at<double>(base, o_out));
+        double bb[7];
+        HALMA_CUDA(cudaMemcpyAsync(bb, at<double>(base, o_out), sizeof(bb), cudaMemcpyDeviceToHost, st));
+        HALMA_CUDA(cudaStreamSynchronize(st));
+        if (bb[6] != 0.0) return fail(HALMA_ERR_INVALID, "non-finite particle position");
+        FofGeom g{};
+        g.xmin = bb[0];
+        g.ymin = bb[1];
+        g.zmin = bb[2];
+        const double ext = std::max(bb[3] - bb[0], std::max(bb[4] - bb[1], bb[5] - bb[2]));
+        if (ll > 0.0) {
+            g.cell = ll * (1.0 + 0x1p-20);
+            g.inv_scale = 1.0 / ll;
+            g.lo = 1.0f - 1e-5f;
+            g.hi = 1.0f + 1e-5f;
+        } else {
+            // ll == 0 links coincident points only: every float candidate is re-tested exactly
+            g.cell = ext > 0.0 ? ext * 0x1p-16 : 1.0;
+            g.inv_scale = 1.0 / g.cell;
+            g.lo = -1.0f;
+            g.hi = 1e-6f;
+        }
+        g.inv_cell = 1.0 / g.cell;
+        g.cs = (float)(g.cell * g.inv_scale);
+        g.r2 = ll * ll;
+        g.ncx = (long long)floor((bb[3] - bb[0]) * g.inv_cell) + 1;
+        g.ncy = (long long)floor((bb[4] - bb[1]) * g.inv_cell) + 1;
+        g.ncz = (long long)floor((bb[5] - bb[2]) * g.inv_cell) + 1;
+        const long double cells = (long double)g.ncx * g.ncy * g.ncz;
+        if (cells > 4.0e18L)
+            return fail(HALMA_ERR_CAPACITY, "cell grid too large (%lld x %lld x %lld cells)", g.ncx, g.ncy, g.ncz);
+        const int end_bit = bits_for((uint64_t)(g.ncx * g.ncy * g.ncz - 1));
+
+        // pass 2: everything else, one workspace layout sized by n
+        uint64_t hcap = 1;
+        while (hcap < 2ull * (uint64_t)n) hcap <<= 1;
+        const size_t sort_b = sort_pairs_u64_i32_bytes(n, end_bit);
+        const size_t scan_b = exclusive_sum_i32_bytes(n);
+        Layout M;
+        const size_t o_kin = M.add(8ull * n), o_kout = M.add(8ull * n);
+        const size_t o_vin = M.add(4ull * n), o_vout = M.add(4ull * n);
+        const size_t o_rec = M.add(16ull * n);
+        const size_t o_head = M.add(4ull * n), o_cpos = M.add(4ull * n);
+        const size_t o_par = M.add(4ull * n), o_has = M.add(1ull * n), o_root = M.add(4ull * n);
+        const size_t o_min = M.add(4ull * n);
+        const size_t o_cst = M.add(4ull * (n + 1)), o_ckey = M.add(8ull * n);
+        const size_t o_hk = M.add(8ull * hcap), o_hv = M.add(4ull * hcap);
+        const size_t o_flag = M.add(4ull * n), o_ipos = M.add(4ull * n);
+        const size_t o_ik0 = M.add(4ull * n), o_icell = M.add(4ull * n);
+        const size_t o_cnt = M.add(64);
+        const size_t o_tmp = M.add(std::max(sort_b, scan_b));
+        HALMA_TRY(workspace(M.total, &base, st));
+        auto *kin = at<uint64_t>(base, o_kin), *kout = at<uint64_t>(base, o_kout);
+        auto *vin = at<int>(base, o_vin), *vout = at<int>(base, o_vout);
+        auto *rec = at<float4>(base, o_rec);
+        auto *head = at<int>(base, o_head), *cpos = at<int>(base, o_cpos);
+        auto *parent = at<int>(base, o_par), *root = at<int>(base, o_root), *minidx = at<int>(base, o_min);
+        auto *has = at<unsigned char>(base, o_has);
+        auto *cst = at<int>(base, o_cst);
+        auto *ckey = at<uint64_t>(base, o_ckey);
+        auto *hk = at<uint64_t>(base, o_hk);
+        auto *hv = at<int>(base, o_hv);
+        auto *flag = at<int>(base, o_flag), *ipos = at<int>(base, o_ipos);
+        auto *ik0 = at<int>(base, o_ik0), *icell = at<int>(base, o_icell);
+        int *cnt = at<int>(base, o_cnt);   // [0] ncell [1] nitems [2] ngroups [3] err
+        void *tmp = at<void>(base, o_tmp);
+        const int g1 = std::min(sms * 8, grid_for(n, 256));
+
+        HALMA_CUDA(cudaMemsetAsync(cnt, 0, 64, st));
+        HALMA_CUDA(cudaMemsetAsync(hk, 0xff, 8ull * hcap, st));
+        HALMA_LAUNCH(keys_kernel, g1, 256, 0, st, x, y, z, n, g, kin, vin);
+        HALMA_TRY(sort_pairs_u64_i32(tmp, sort_b, kin, kout, vin, vout, n, end_bit, st));
+        HALMA_LAUNCH(prep_kernel, g1, 256, 0, st, x, y, z, n, g, kout, vout, rec, head, parent, has, minidx);
+        HALMA_TRY(exclusive_sum_i32(tmp, scan_b, head, cpos, n, st));
+        HALMA_LAUNCH(cells_kernel, g1, 256, 0, st, n, kout, head, cpos, cst, ckey, hk, hv, hcap - 1, cnt + 0);
+        HALMA_LAUNCH(itemflag_kernel, g1, 256, 0, st, n, head, cpos, cst, flag);
+        HALMA_TRY(exclusive_sum_i32(tmp, scan_b, flag, ipos, n, st));
+        HALMA_LAUNCH(items_kernel, g1, 256, 0, st, n, head, cpos, flag, ipos, ik0, icell, cnt + 1);
+        HALMA_LAUNCH(link_kernel, sms * 8, 32 * kFofWarps, 0, st, rec, cst, ckey, ik0, icell, cnt + 1, hk, hv,
+                     hcap - 1, g, x, y, z, parent, has, cnt + 3);
+        HALMA_LAUNCH(root_kernel, g1, 256, 0, st, n, rec, parent, has, root, minidx, cnt + 3);
+        HALMA_LAUNCH(label_kernel, g1, 256, 0, st, n, rec, has, root, minidx, labels, cnt + 2);
+        int hc[4];
+        HALMA_CUDA(cudaMemcpyAsync(hc, cnt, sizeof(hc), cudaMemcpyDeviceToHost, st));
+        HALMA_CUDA(cudaStreamSynchronize(st));
+        if (hc[3]) return fail(HALMA_ERR_NOT_CONVERGED, "union-find iteration cap reached");
+        if (n_groups) *n_groups = hc[2];
+    }
+    return HALMA_OK;
+}
+
+}  // namespace halma
+
+using namespace halma;
+
+extern "C" int halma_fof(int64_t n, const double *x, const double *y, const double *z, double linking_length,
+                         int32_t *labels, int64_t *n_groups, halma_stream_t stream) {
+    if (n < 0) return fail(HALMA_ERR_INVALID, "negative particle count");
+    if (n >= INT_MAX) return fail(HALMA_ERR_CAPACITY, "at most 2^31-2 particles per call");
+    if (!(linking_length >= 0.0) || !isfinite(linking_length))
+        return fail(HALMA_ERR_INVALID, "linking length must be finite and >= 0");
+    if (n > 0 && (!x || !y || !z || !labels)) return fail(HALMA_ERR_INVALID, "null pointer");
+    if (n == 0) {
+        if (n_groups) *n_groups = 0;
+        return HALMA_OK;
+    }
+    std::lock_guard<std::mutex> guard(api_mutex());
+    cudaStream_t st = (cudaStream_t)stream;
+    Stager sg;
+    const double *dx = nullptr, *dy = nullptr, *dz = nullptr;
+    int32_t *dl = nullptr;
+    sg.add(x, n, true, false, &dx);
+    sg.add(y, n, true, false, &dy);
+    sg.add(z, n, true, false, &dz);
+    sg.add((const int32_t *)labels, n, false, true, &dl);
+    if (sg.any_host) {
+        // host arrays live in their own allocation so the FoF scratch can reuse the workspace
+        std::vector<void *> owned;
+        Layout L;
+        sg.plan(L);
+        void *stage = nullptr;
+        HALMA_CUDA(cudaMallocAsync(&stage, L.total, st));
+        int s = sg.bind_and_upload(stage, st);
+        if (s == HALMA_OK) s = fof_device((int)n, dx, dy, dz, linking_length, dl, n_groups, st);
+        if (s == HALMA_OK) s = sg.download(st);
+        cudaFreeAsync(stage, st);
+        cudaStreamSynchronize(st);
+        return s;
+    }
+    HALMA_TRY(sg.bind_and_upload(nullptr, st));
+    return fof_device((int)n, dx, dy, dz, linking_length, dl, n_groups, st);
+}
+
+namespace halma {
+namespace {
+
+__global__ void group_keys_kernel(int n, const int *__restrict__ labels, uint32_t *__restrict__ keys,
+                                  int *__restrict__ vals) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int l = labels[i];
+        keys[i] = l < 0 ? 0xffffffffu : (uint32_t)l;
+        vals[i] = i;
+    }
+}
+
+__global__ void group_heads_kernel(int n, const uint32_t *__restrict__ keys, int *__restrict__ head) {
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x)
+        head[k] = (keys[k] != 0xffffffffu && (k == 0 || keys[k] != keys[k - 1])) ? 1 : 0;
+}
+
+// gstart[gid] = first sorted position of group gid; cnt[0] = groups, cnt[1] = members
+__global__ void group_starts_kernel(int n, const uint32_t *__restrict__ keys, const int *__restrict__ head,
+                                    const int *__restrict__ gid, int *__restrict__ gstart, int *__restrict__ cnt) {
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        if (head[k]) gstart[gid[k]] = k;
+        const bool valid = keys[k] != 0xffffffffu;
+        const bool last_valid = valid && (k == n - 1 || keys[k + 1] == 0xffffffffu);
+        if (last_valid) {
+            cnt[0] = gid[k] + head[k];
+            cnt[1] = k + 1;
+            gstart[gid[k] + head[k]] = k + 1;
+        }
+    }
+}
+
+__global__ void group_keep_kernel(int n, const uint32_t *__restrict__ keys, const int *__restrict__ head,
+                                  const int *__restrict__ gid, const int *__restrict__ gstart,
+                                  const int *__restrict__ cnt, int minp, int *__restrict__ keep,
+                                  int *__restrict__ keepg) {
+    const int ng = cnt[0];
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        int kp = 0;
+        if (keys[k] != 0xffffffffu) {
+            const int g = gid[k] + head[k] - 1;
+            kp = (gstart[g + 1] - gstart[g]) >= minp;
+        }
+        keep[k] = kp;
+        keepg[k] = (k < ng) ? ((gstart[k + 1] - gstart[k]) >= minp) : 0;
+    }
+}
+
+__global__ void group_emit_kernel(int n, const uint32_t *__restrict__ keys, const int *__restrict__ head,
+                                  const int *__restrict__ gid, const int *__restrict__ vals,
+                                  const int *__restrict__ keep, const int *__restrict__ pos,
+                                  const int *__restrict__ keepg, const int *__restrict__ gpos,
+                                  int *__restrict__ members, int64_t *__restrict__ offsets,
+                                  int *__restrict__ cnt) {
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        if (keep[k]) {
+            members[pos[k]] = vals[k];
+            if (head[k]) offsets[gpos[gid[k]]] = pos[k];
+        }
+        if (k == n - 1) {
+            const int kept_members = pos[k] + keep[k];
+            const int kept_groups = gpos[k] + keepg[k];
+            offsets[kept_groups] = kept_members;
+            cnt[2] = kept_groups;
+            cnt[3] = kept_members;
+        }
+    }
+}
+
+}  // namespace
+
+// Groups of >= minp members in the reference order, on device arrays; the counts are
+// returned on the host (one synchronisation).
+int fof_groups_device(int n, const int *labels, int minp, int64_t *offsets, int *members,
+                      int64_t *n_groups, int64_t *n_members, cudaStream_t st) {
+    const size_t sort_b = sort_pairs_u32_i32_bytes(n);
+    const size_t scan_b = exclusive_sum_i32_bytes(n);
+    Layout L;
+    const size_t o_kin = L.add(4ull * n), o_kout = L.add(4ull * n), o_vin = L.add(4ull * n), o_vout = L.add(4ull * n);
+    const size_t o_head = L.add(4ull * n), o_gid = L.add(4ull * n), o_gst = L.add(4ull * (n + 2));
+    const size_t o_keep = L.add(4ull * n), o_pos = L.add(4ull * n), o_keepg = L.add(4ull * n), o_gpos = L.add(4ull * n);
+    const size_t o_cnt = L.add(64), o_tmp = L.add(std::max(sort_b, scan_b));
+    void *base = nullptr;
+    HALMA_TRY(workspace(L.total, &base, st));
+    auto *kin = at<uint32_t>(base, o_kin), *kout = at<uint32_t>(base, o_kout);
+    auto *vin = at<int>(base, o_vin), *vout = at<int>(base, o_vout);
+    auto *head = at<int>(base, o_head), *gid = at<int>(base, o_gid), *gst = at<int>(base, o_gst);
+    auto *keep = at<int>(base, o_keep), *pos = at<int>(base, o_pos), *keepg = at<int>(base, o_keepg), *gpos = at<int>(base, o_gpos);
+    int *cnt = at<int>(base, o_cnt);
+    void *tmp = at<void>(base, o_tmp);
+    const int g1 = std::min(device_sm_count() * 8, grid_for(n, 256));
+    HALMA_CUDA(cudaMemsetAsync(cnt, 0, 64, st));
+    HALMA_CUDA(cudaMemsetAsync(offsets, 0, sizeof(int64_t), st));
+    HALMA_LAUNCH(group_keys_kernel, g1, 256, 0, st, n, labels, kin, vin);
+    HALMA_TRY(sort_pairs_u32_i32(tmp, sort_b, kin, kout, vin, vout, n, 32, st));
+    HALMA_LAUNCH(group_heads_kernel, g1, 256, 0, st, n, kout, head);
+    HALMA_TRY(exclusive_sum_i32(tmp, scan_b, head, gid, n, st));
+    HALMA_LAUNCH(group_starts_kernel, g1, 256, 0, st, n, kout, head, gid, gst, cnt);
+    HALMA_LAUNCH(group_keep_kernel, g1, 256, 0, st, n, kout, head, gid, gst, cnt, minp, keep, keepg);
+    HALMA_TRY(exclusive_sum_i32(tmp, scan_b, keep, pos, n, st));
+    HALMA_TRY(exclusive_sum_i32(tmp, scan_b, keepg, gpos, n, st));
+    HALMA_LAUNCH(group_emit_kernel, g1, 256, 0, st, n, kout, head, gid, vout, keep, pos, keepg, gpos, members,
+                 offsets, cnt);
+    int hc[4];
+    HALMA_CUDA(cudaMemcpyAsync(hc, cnt, sizeof(hc), cudaMemcpyDeviceToHost, st));
+    HALMA_CUDA(cudaStreamSynchronize(st));
+    *n_groups = hc[2];
+    if (n_members) *n_members = hc[3];
+    return HALMA_OK;
+}
+
+}  // namespace halma
+
+extern "C" int halma_fof_groups(int64_t n, const int32_t *labels, int32_t min_members, int64_t *offsets,
+                                int32_t *members, int64_t *n_groups, halma_stream_t stream) {
+    if (n < 0) return fail(HALMA_ERR_INVALID, "negative particle count");
+    if (n >= INT_MAX) return fail(HALMA_ERR_CAPACITY, "at most 2^31-2 particles per call");
+    if (!offsets || !n_groups || (n > 0 && (!labels || !members))) return fail(HALMA_ERR_INVALID, "null pointer");
+    if (n == 0) {
+        *n_groups = 0;
+        int64_t zero = 0;
+        if (is_device_pointer(offsets)) HALMA_CUDA(cudaMemcpy(offsets, &zero, 8, cudaMemcpyHostToDevice));
+        else offsets[0] = 0;
+        return HALMA_OK;
+    }
+    std::lock_guard<std::mutex> guard(api_mutex());
+    cudaStream_t st = (cudaStream_t)stream;
+    const bool h_lab = !is_device_pointer(labels), h_off = !is_device_pointer(offsets),
+               h_mem = !is_device_pointer(members);
+    void *stage = nullptr;
+    const int *dl = labels;
+    int64_t *doff = offsets;
+    int *dmem = members;
+    if (h_lab || h_off || h_mem) {
+        Layout L;
+        const size_t a = L.add(4ull * n), b = L.add(8ull * (n + 1)), c = L.add(4ull * n);
+        HALMA_CUDA(cudaMallocAsync(&stage, L.total, st));
+        if (h_lab) {
+            dl = at<int>(stage, a);
+            HALMA_CUDA(cudaMemcpyAsync((void *)dl, labels, 4ull * n, cudaMemcpyHostToDevice, st));
+        }
+        if (h_off) doff = at<int64_t>(stage, b);
+        if (h_mem) dmem = at<int>(stage, c);
+    }
+    int64_t ng = 0, nm = 0;
+    int s = fof_groups_device((int)n, dl, min_members, doff, dmem, &ng, &nm, st);
+    if (s == HALMA_OK) {
+        if (h_off) s = cudaMemcpyAsync(offsets, doff, 8ull * (ng + 1), cudaMemcpyDeviceToHost, st) == cudaSuccess ? s : fail(HALMA_ERR_CUDA, "copy of group offsets failed");
+        if (h_mem && nm > 0) s = cudaMemcpyAsync(members, dmem, 4ull * nm, cudaMemcpyDeviceToHost, st) == cudaSuccess ? s : fail(HALMA_ERR_CUDA, "copy of group members failed");
+        *n_groups = ng;
+    }
+    if (stage) cudaFreeAsync(stage, st);
+    cudaStreamSynchronize(st);
+    return s;
+}

@@ -1,0 +1,58 @@
+// Per-pair arithmetic shared by the potential, unbinding and gradient kernels.
+#pragma once
+#include <cuda_runtime.h>
+
+namespace halma {
+
+// Error-free transformation of s + v (Knuth's TwoSum); the rounding error goes into c.
+// Six additions, no fused operations, valid for any magnitudes.
+__device__ __forceinline__ void two_sum_acc(float &s, float &c, float v) {
+    float t = s + v;
+    float bp = t - s;
+    float err = (s - (t - bp)) + (v - bp);
+    s = t;
+    c += err;
+}
+
+// One softened pair term m / sqrt(r^2 + eps2) with the FP32 special-function rsqrt.
+__device__ __forceinline__ float pair_term_fast(float4 q, float px, float py, float pz, float eps2,
+                                                float acc) {
+    float dx = q.x - px;
+    float dy = q.y - py;
+    float dz = q.z - pz;
+    float r2 = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, eps2)));
+    return fmaf(q.w, rsqrtf(r2), acc);
+}
+
+// Same, with the reference's pair mask: the term counts only when the source's x, y and z
+// all differ from the target's (particle_subroutines.f90:499-501).
+__device__ __forceinline__ float pair_term_fast_masked(float4 q, float px, float py, float pz,
+                                                       float eps2, float acc) {
+    float dx = q.x - px;
+    float dy = q.y - py;
+    float dz = q.z - pz;
+    float r2 = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, eps2)));
+    float ri = rsqrtf(r2);
+    bool keep = (q.x != px) & (q.y != py) & (q.z != pz);
+    return fmaf(q.w, keep ? ri : 0.0f, acc);
+}
+
+// The reference's float32 statement, each operation rounded on its own (no FMA):
+//   r = sqrt((xj-xi)**2 + (yj-yi)**2 + (zj-zi)**2); phi = phi + m / r
+// (particle_subroutines.f90:502-505), guarded by the mask of f90:499-501.
+__device__ __forceinline__ float pair_term_reference(float4 q, float px, float py, float pz,
+                                                     float acc) {
+    if (q.x != px && q.y != py && q.z != pz) {
+        float dx = __fsub_rn(q.x, px);
+        float dy = __fsub_rn(q.y, py);
+        float dz = __fsub_rn(q.z, pz);
+        float s = __fmul_rn(dx, dx);
+        s = __fadd_rn(s, __fmul_rn(dy, dy));
+        s = __fadd_rn(s, __fmul_rn(dz, dz));
+        float r = __fsqrt_rn(s);
+        acc = __fadd_rn(acc, __fdiv_rn(q.w, r));
+    }
+    return acc;
+}
+
+}  // namespace halma

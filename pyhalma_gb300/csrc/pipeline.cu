@@ -1,0 +1,135 @@
+// End-to-end halo finding for one snapshot: FoF -> groups with >= min_members members in the
+// reference order (pyHALMA.py:555-592) -> members gathered into halo-contiguous FP64 arrays
+// -> batched iterative unbinding -> bound flags scattered back to the snapshot order.
+#include <math.h>
+#include <string.h>
+
+#include "common.cuh"
+#include "unbind.cuh"
+
+namespace halma {
+namespace {
+
+__global__ void gather7_kernel(int64_t nm, const int *__restrict__ members, const double *__restrict__ x,
+                               const double *__restrict__ y, const double *__restrict__ z,
+                               const double *__restrict__ vx, const double *__restrict__ vy,
+                               const double *__restrict__ vz, const double *__restrict__ m,
+                               double *__restrict__ out /* 7 x nm */) {
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < nm; k += (int64_t)gridDim.x * blockDim.x) {
+        const int i = members[k];
+        out[k] = x[i];
+        out[nm + k] = y[i];
+        out[2 * nm + k] = z[i];
+        out[3 * nm + k] = vx[i];
+        out[4 * nm + k] = vy[i];
+        out[5 * nm + k] = vz[i];
+        out[6 * nm + k] = m[i];
+    }
+}
+
+__global__ void scatter_bound_kernel(int64_t nm, const int *__restrict__ members, const unsigned char *__restrict__ bs,
+                                     unsigned char *__restrict__ bound) {
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < nm; k += (int64_t)gridDim.x * blockDim.x)
+        bound[members[k]] = bs[k];
+}
+
+struct DevBuf {
+    void *p = nullptr;
+    cudaStream_t s = nullptr;
+    ~DevBuf() {
+        if (p) cudaFreeAsync(p, s);
+    }
+};
+
+}  // namespace
+}  // namespace halma
+
+using namespace halma;
+
+extern "C" int halma_find_haloes(int64_t n, const double *x, const double *y, const double *z, const double *vx,
+                                 const double *vy, const double *vz, const double *m, double linking_length,
+                                 int32_t min_members, const halma_unbind_params *params, int32_t *labels,
+                                 uint8_t *bound, int64_t *n_haloes, int64_t halo_capacity, int64_t *halo_offsets,
+                                 int32_t *members, double *halo_out, halma_stream_t stream) {
+    if (!params || !n_haloes) return fail(HALMA_ERR_INVALID, "params and n_haloes must not be NULL");
+    if (n < 0 || halo_capacity < 0) return fail(HALMA_ERR_INVALID, "negative size");
+    if (n >= (1ll << 31) - 64) return fail(HALMA_ERR_CAPACITY, "at most 2^31-65 particles per call");
+    if (!(linking_length >= 0.0) || !isfinite(linking_length))
+        return fail(HALMA_ERR_INVALID, "linking length must be finite and >= 0");
+    const halma_unbind_params p = *params;
+    if (!(p.eps > 0.0) || !isfinite(p.eps)) return fail(HALMA_ERR_INVALID, "eps must be finite and > 0");
+    if (p.max_iter < 1 || p.max_iter > 1000) return fail(HALMA_ERR_INVALID, "max_iter must be in [1, 1000]");
+    if (p.precision != HALMA_UNBIND_FP32C && p.precision != HALMA_UNBIND_FP64)
+        return fail(HALMA_ERR_INVALID, "unknown precision %d", p.precision);
+    if (n > 0 && (!x || !y || !z || !vx || !vy || !vz || !m)) return fail(HALMA_ERR_INVALID, "null input pointer");
+    *n_haloes = 0;
+    if (n == 0) {
+        if (halo_offsets) {
+            int64_t zero = 0;
+            if (is_device_pointer(halo_offsets)) HALMA_CUDA(cudaMemcpy(halo_offsets, &zero, 8, cudaMemcpyHostToDevice));
+            else halo_offsets[0] = 0;
+        }
+        return HALMA_OK;
+    }
+    std::lock_guard<std::mutex> guard(api_mutex());
+    cudaStream_t st = (cudaStream_t)stream;
+    Stager sg;
+    const double *dx = nullptr, *dy = nullptr, *dz = nullptr, *dvx = nullptr, *dvy = nullptr, *dvz = nullptr,
+                 *dm = nullptr;
+    sg.add(x, n, true, false, &dx);
+    sg.add(y, n, true, false, &dy);
+    sg.add(z, n, true, false, &dz);
+    sg.add(vx, n, true, false, &dvx);
+    sg.add(vy, n, true, false, &dvy);
+    sg.add(vz, n, true, false, &dvz);
+    sg.add(m, n, true, false, &dm);
+    // private scratch for everything that must outlive the individual stages
+    Layout L;
+    sg.plan(L);
+    const size_t o_lab = L.add(4ull * n), o_off = L.add(8ull * (n + 1)), o_mem = L.add(4ull * n);
+    const size_t o_g7 = L.add(8ull * 7 * n), o_bs = L.add(1ull * n), o_bnd = L.add(1ull * n);
+    const size_t o_halo = L.add(8ull * HALMA_UB_NFIELDS * (size_t)std::max<int64_t>(n / 2 + 1, 1));
+    DevBuf buf;
+    buf.s = st;
+    HALMA_CUDA(cudaMallocAsync(&buf.p, L.total, st));
+    HALMA_TRY(sg.bind_and_upload(buf.p, st));
+    int *dlab = at<int>(buf.p, o_lab);
+    int64_t *doff = at<int64_t>(buf.p, o_off);
+    int *dmem = at<int>(buf.p, o_mem);
+    double *g7 = at<double>(buf.p, o_g7);
+    unsigned char *bs = at<unsigned char>(buf.p, o_bs), *dbnd = at<unsigned char>(buf.p, o_bnd);
+    double *dhalo = at<double>(buf.p, o_halo);
+
+    HALMA_TRY(fof_device((int)n, dx, dy, dz, linking_length, dlab, nullptr, st));
+    int64_t ng = 0, nm = 0;
+    HALMA_TRY(fof_groups_device((int)n, dlab, std::max(min_members, 1), doff, dmem, &ng, &nm, st));
+    *n_haloes = ng;
+    HALMA_CUDA(cudaMemsetAsync(dbnd, 0, n, st));
+    if (ng > 0) {
+        const int g = std::min(device_sm_count() * 8, grid_for(nm, 256));
+        HALMA_LAUNCH(gather7_kernel, g, 256, 0, st, nm, dmem, dx, dy, dz, dvx, dvy, dvz, dm, g7);
+        std::vector<int64_t> h_off(ng + 1);
+        HALMA_CUDA(cudaMemcpyAsync(h_off.data(), doff, 8ull * (ng + 1), cudaMemcpyDeviceToHost, st));
+        HALMA_CUDA(cudaStreamSynchronize(st));
+        HALMA_TRY(unbind_device(nm, (int)ng, doff, h_off.data(), g7, g7 + nm, g7 + 2 * nm, g7 + 3 * nm, g7 + 4 * nm,
+                                g7 + 5 * nm, g7 + 6 * nm, p, bs, nullptr, dhalo, st));
+        HALMA_LAUNCH(scatter_bound_kernel, g, 256, 0, st, nm, dmem, bs, dbnd);
+    }
+    // outputs (host or device)
+    auto put = [&](void *user, const void *dev, size_t bytes) -> int {
+        if (!user || bytes == 0) return HALMA_OK;
+        HALMA_CUDA(cudaMemcpyAsync(user, dev, bytes, cudaMemcpyDefault, st));
+        return HALMA_OK;
+    };
+    HALMA_TRY(put(labels, dlab, 4ull * n));
+    HALMA_TRY(put(bound, dbnd, 1ull * n));
+    if (ng > halo_capacity && (halo_offsets || halo_out)) {
+        HALMA_CUDA(cudaStreamSynchronize(st));
+        return fail(HALMA_ERR_CAPACITY, "%lld haloes found, capacity %lld", (long long)ng, (long long)halo_capacity);
+    }
+    HALMA_TRY(put(halo_offsets, doff, 8ull * (ng + 1)));
+    HALMA_TRY(put(members, dmem, 4ull * nm));
+    HALMA_TRY(put(halo_out, dhalo, 8ull * HALMA_UB_NFIELDS * ng));
+    HALMA_CUDA(cudaStreamSynchronize(st));
+    return HALMA_OK;
+}

@@ -1,0 +1,346 @@
+// Brute-force potential kernels and the C ABI that replaces the f2py symbol
+// particle.particle.brute_force_binding_energy (particle_subroutines.f90:466-514).
+//
+// Layout: sources are read as float32 SoA (m, x, y, z) and staged per warp in shared memory
+// as float4 chunks of 32; each lane owns T targets, so one shared-memory broadcast feeds T
+// pair terms.  Work items are (target tile of 32*T, source slice); warps stride over items.
+#include <math.h>
+
+#include "common.cuh"
+#include "pair_math.cuh"
+
+namespace halma {
+
+constexpr int kWarpsPerBlock = 8;
+constexpr float kPadCoord = 3.0e30f;   // pad sources: m = 0 at a far point -> exact +0 term
+
+__device__ __forceinline__ float4 load_source(const float *__restrict__ m, const float *__restrict__ x,
+                                              const float *__restrict__ y, const float *__restrict__ z,
+                                              int64_t j, int64_t end) {
+    if (j < end) return make_float4(__ldg(x + j), __ldg(y + j), __ldg(z + j), __ldg(m + j));
+    return make_float4(kPadCoord, kPadCoord, kPadCoord, 0.0f);
+}
+
+// HALMA_POT_REFERENCE: one target per lane, sources in order, bit-identical to the
+// Fortran loop body (f90:497-510).
+__global__ void __launch_bounds__(256) bf_potential_reference_kernel(
+    const float *__restrict__ m, const float *__restrict__ x, const float *__restrict__ y,
+    const float *__restrict__ z, int64_t ns, const float *__restrict__ tx,
+    const float *__restrict__ ty, const float *__restrict__ tz, int64_t nt, float *__restrict__ out) {
+    __shared__ float4 buf[kWarpsPerBlock][32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int64_t gwarp = (int64_t)blockIdx.x * kWarpsPerBlock + w;
+    const int64_t nwarps = (int64_t)gridDim.x * kWarpsPerBlock;
+    const int64_t ntiles = (nt + 31) / 32;
+    for (int64_t tile = gwarp; tile < ntiles; tile += nwarps) {
+        const int64_t i = tile * 32 + lane;
+        const bool valid = i < nt;
+        const float px = valid ? tx[i] : 0.f, py = valid ? ty[i] : 0.f, pz = valid ? tz[i] : 0.f;
+        float acc = 0.0f;
+        float4 nxt = load_source(m, x, y, z, lane, ns);
+        for (int64_t j0 = 0; j0 < ns; j0 += 32) {
+            __syncwarp();
+            buf[w][lane] = nxt;
+            __syncwarp();
+            nxt = load_source(m, x, y, z, j0 + 32 + lane, ns);
+            const int cnt = (int)min((int64_t)32, ns - j0);
+            for (int k = 0; k < cnt; ++k) acc = pair_term_reference(buf[w][k], px, py, pz, acc);
+        }
+        if (valid) out[i] = acc;
+    }
+}
+
+// HALMA_POT_FAST: T targets per lane, FP32 rsqrt pair terms with the reference mask, each
+// 32-source chunk summed in FP32 and folded into a TwoSum-compensated accumulator.
+// MASK: HALMA_MASK_COORD (reference mask), HALMA_MASK_SELF (skip j == i + self_offset) or
+// HALMA_MASK_NONE.
+template <int T, int MASK>
+__global__ void __launch_bounds__(256) bf_potential_fast_kernel(
+    const float *__restrict__ m, const float *__restrict__ x, const float *__restrict__ y,
+    const float *__restrict__ z, int64_t ns, const float *__restrict__ tx,
+    const float *__restrict__ ty, const float *__restrict__ tz, int64_t nt, float eps2,
+    int n_split, int64_t split_len, int64_t self_offset, float *__restrict__ out,
+    double *__restrict__ partial) {
+    __shared__ float4 buf[kWarpsPerBlock][32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int64_t gwarp = (int64_t)blockIdx.x * kWarpsPerBlock + w;
+    const int64_t nwarps = (int64_t)gridDim.x * kWarpsPerBlock;
+    const int64_t ntiles = (nt + 32 * T - 1) / (32 * T);
+    const int64_t nitems = ntiles * n_split;
+    for (int64_t item = gwarp; item < nitems; item += nwarps) {
+        const int64_t tile = item / n_split;
+        const int s = (int)(item - tile * n_split);
+        const int64_t jb = (int64_t)s * split_len;
+        const int64_t je = min(ns, jb + split_len);
+        float px[T], py[T], pz[T], sum[T], comp[T];
+#pragma unroll
+        for (int t = 0; t < T; ++t) {
+            const int64_t i = tile * 32 * T + t * 32 + lane;
+            const bool v = i < nt;
+            px[t] = v ? tx[i] : kPadCoord;
+            py[t] = v ? ty[i] : kPadCoord;
+            pz[t] = v ? tz[i] : kPadCoord;
+            sum[t] = 0.f;
+            comp[t] = 0.f;
+        }
+        float4 nxt = load_source(m, x, y, z, jb + lane, je);
+        for (int64_t j0 = jb; j0 < je; j0 += 32) {
+            __syncwarp();
+            buf[w][lane] = nxt;
+            __syncwarp();
+            nxt = load_source(m, x, y, z, j0 + 32 + lane, je);
+            float part[T];
+#pragma unroll
+            for (int t = 0; t < T; ++t) part[t] = 0.f;
+            if (MASK == HALMA_MASK_COORD) {
+#pragma unroll 8
+                for (int k = 0; k < 32; ++k) {
+                    const float4 q = buf[w][k];
+#pragma unroll
+                    for (int t = 0; t < T; ++t) part[t] = pair_term_fast_masked(q, px[t], py[t], pz[t], eps2, part[t]);
+                }
+            } else if (MASK == HALMA_MASK_NONE) {
+#pragma unroll 8
+                for (int k = 0; k < 32; ++k) {
+                    const float4 q = buf[w][k];
+#pragma unroll
+                    for (int t = 0; t < T; ++t) part[t] = pair_term_fast(q, px[t], py[t], pz[t], eps2, part[t]);
+                }
+            } else {
+                // source index of target t's self pair relative to this chunk
+                int64_t rel[T];
+#pragma unroll
+                for (int t = 0; t < T; ++t) rel[t] = tile * 32 * T + t * 32 + lane + self_offset - j0;
+#pragma unroll 4
+                for (int k = 0; k < 32; ++k) {
+                    const float4 q = buf[w][k];
+#pragma unroll
+                    for (int t = 0; t < T; ++t) {
+                        const float v = pair_term_fast(q, px[t], py[t], pz[t], eps2, part[t]);
+                        part[t] = (rel[t] == k) ? part[t] : v;
+                    }
+                }
+            }
+#pragma unroll
+            for (int t = 0; t < T; ++t) two_sum_acc(sum[t], comp[t], part[t]);
+        }
+#pragma unroll
+        for (int t = 0; t < T; ++t) {
+            const int64_t i = tile * 32 * T + t * 32 + lane;
+            if (i < nt) {
+                if (n_split == 1) out[i] = sum[t] + comp[t];
+                else partial[(int64_t)s * nt + i] = (double)sum[t] + (double)comp[t];
+            }
+        }
+    }
+}
+
+// Deterministic combine of the per-slice partial sums (fixed slice order, FP64).
+__global__ void reduce_partials_kernel(const double *__restrict__ partial, int n_split, int64_t nt,
+                                       float *__restrict__ out) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nt;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        double acc = 0.0;
+        for (int s = 0; s < n_split; ++s) acc += partial[(int64_t)s * nt + i];
+        out[i] = (float)acc;
+    }
+}
+
+// Plain FP64 path: one target per thread, FP64 pair terms and FP64 sum.
+__global__ void __launch_bounds__(256) potential_f64_kernel(
+    const double *__restrict__ m, const double *__restrict__ sx, const double *__restrict__ sy,
+    const double *__restrict__ sz, int64_t ns, const double *__restrict__ tx,
+    const double *__restrict__ ty, const double *__restrict__ tz, int64_t nt, double eps2,
+    int mask, int64_t self_offset, double *__restrict__ phi) {
+    __shared__ double4 buf[256];
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const bool valid = i < nt;
+    const double px = valid ? tx[i] : 0.0, py = valid ? ty[i] : 0.0, pz = valid ? tz[i] : 0.0;
+    const int64_t self = valid ? i + self_offset : -1;
+    double acc = 0.0;
+    for (int64_t j0 = 0; j0 < ns; j0 += 256) {
+        const int64_t j = j0 + threadIdx.x;
+        __syncthreads();
+        buf[threadIdx.x] = (j < ns) ? make_double4(sx[j], sy[j], sz[j], m[j]) : make_double4(0, 0, 0, 0);
+        __syncthreads();
+        const int cnt = (int)min((int64_t)256, ns - j0);
+        for (int k = 0; k < cnt; ++k) {
+            const double4 q = buf[k];
+            const double dx = q.x - px, dy = q.y - py, dz = q.z - pz;
+            bool keep = true;
+            if (mask == HALMA_MASK_COORD) keep = (q.x != px) && (q.y != py) && (q.z != pz);
+            else if (mask == HALMA_MASK_SELF) keep = (j0 + k) != self;
+            const double r2 = fma(dx, dx, fma(dy, dy, fma(dz, dz, eps2)));
+            if (keep) acc = fma(q.w, rsqrt(r2), acc);
+        }
+    }
+    if (valid) phi[i] = acc;
+}
+
+// Number of source slices so that (target tiles x slices) keeps every SM busy.
+static void choose_split(int64_t ns, int64_t nt, int T, int *n_split, int64_t *split_len) {
+    const int sms = device_sm_count();
+    const int64_t ntiles = (nt + 32 * T - 1) / (32 * T);
+    const int64_t want_items = (int64_t)sms * 64;   // ~2 waves of resident warps
+    int64_t s = 1;
+    if (ntiles < want_items) s = (want_items + ntiles - 1) / ntiles;
+    const int64_t max_s = std::max<int64_t>(1, ns / 2048);   // keep slices >= 2048 sources
+    s = std::min(s, max_s);
+    s = std::min<int64_t>(s, 1024);
+    int64_t len = (ns + s - 1) / s;
+    len = (len + 31) / 32 * 32;
+    s = std::max<int64_t>(1, (ns + len - 1) / len);
+    *n_split = (int)s;
+    *split_len = std::max<int64_t>(len, 32);
+}
+
+template <int T>
+static int launch_fast(const float *m, const float *x, const float *y, const float *z, int64_t ns,
+                       const float *tx, const float *ty, const float *tz, int64_t nt, float eps2,
+                       int n_split, int64_t split_len, int mask, int64_t self_offset, float *out,
+                       double *partial, cudaStream_t st) {
+    const int64_t ntiles = (nt + 32 * T - 1) / (32 * T);
+    const int64_t nitems = ntiles * n_split;
+    const int sms = device_sm_count();
+    const int grid = (int)std::min<int64_t>((nitems + kWarpsPerBlock - 1) / kWarpsPerBlock, (int64_t)sms * 8);
+    if (mask == HALMA_MASK_COORD)
+        HALMA_LAUNCH((bf_potential_fast_kernel<T, HALMA_MASK_COORD>), grid, 256, 0, st, m, x, y, z, ns, tx, ty, tz,
+                     nt, eps2, n_split, split_len, self_offset, out, partial);
+    else if (mask == HALMA_MASK_SELF)
+        HALMA_LAUNCH((bf_potential_fast_kernel<T, HALMA_MASK_SELF>), grid, 256, 0, st, m, x, y, z, ns, tx, ty, tz,
+                     nt, eps2, n_split, split_len, self_offset, out, partial);
+    else
+        HALMA_LAUNCH((bf_potential_fast_kernel<T, HALMA_MASK_NONE>), grid, 256, 0, st, m, x, y, z, ns, tx, ty, tz,
+                     nt, eps2, n_split, split_len, self_offset, out, partial);
+    return HALMA_OK;
+}
+
+// Stages the caller's arrays and runs the FP32-compensated kernel with the given mask.
+static int potential_fast_api(int64_t ns, const float *mm, const float *sx_, const float *sy_, const float *sz_,
+                              int64_t nt, const float *tx_, const float *ty_, const float *tz_, double eps2,
+                              int mask, int64_t self_offset, float *out_, cudaStream_t st) {
+    constexpr int T = 4;
+    int n_split = 1;
+    int64_t split_len = ns;
+    if (ns > 0) choose_split(ns, nt, T, &n_split, &split_len);
+    Stager sg;
+    const float *m = nullptr, *x = nullptr, *y = nullptr, *z = nullptr, *tx = nullptr, *ty = nullptr, *tz = nullptr;
+    float *out = nullptr;
+    sg.add(mm, ns, true, false, &m);
+    sg.add(sx_, ns, true, false, &x);
+    sg.add(sy_, ns, true, false, &y);
+    sg.add(sz_, ns, true, false, &z);
+    sg.add(tx_, nt, true, false, &tx);
+    sg.add(ty_, nt, true, false, &ty);
+    sg.add(tz_, nt, true, false, &tz);
+    sg.add((const float *)out_, nt, false, true, &out);
+    Layout L;
+    sg.plan(L);
+    const size_t off_part = (n_split > 1) ? L.add(sizeof(double) * (size_t)n_split * nt) : 0;
+    void *base = nullptr;
+    HALMA_TRY(workspace(L.total, &base, st));
+    HALMA_TRY(sg.bind_and_upload(base, st));
+    if (ns == 0) {
+        HALMA_CUDA(cudaMemsetAsync(out, 0, sizeof(float) * nt, st));
+    } else {
+        double *partial = n_split > 1 ? at<double>(base, off_part) : nullptr;
+        HALMA_TRY(launch_fast<T>(m, x, y, z, ns, tx, ty, tz, nt, (float)eps2, n_split, split_len, mask, self_offset,
+                                 out, partial, st));
+        if (n_split > 1)
+            HALMA_LAUNCH(reduce_partials_kernel, grid_for(nt, 256, 4096), 256, 0, st, partial, n_split, nt, out);
+    }
+    return sg.download(st);
+}
+
+}  // namespace halma
+
+using namespace halma;
+
+extern "C" int halma_bf_potential_f32(int64_t ntotal, const float *total_mass, const float *total_x,
+                                      const float *total_y, const float *total_z, int64_t ntest,
+                                      const float *test_x, const float *test_y, const float *test_z,
+                                      float *binding_energy, int32_t mode, double eps2,
+                                      halma_stream_t stream) {
+    if (ntotal < 0 || ntest < 0) return fail(HALMA_ERR_INVALID, "negative size (ntotal=%lld ntest=%lld)", (long long)ntotal, (long long)ntest);
+    if (ntest == 0) return HALMA_OK;
+    if (!binding_energy || !test_x || !test_y || !test_z) return fail(HALMA_ERR_INVALID, "null target/output pointer");
+    if (ntotal > 0 && (!total_mass || !total_x || !total_y || !total_z)) return fail(HALMA_ERR_INVALID, "null source pointer");
+    if (mode != HALMA_POT_REFERENCE && mode != HALMA_POT_FAST) return fail(HALMA_ERR_INVALID, "unknown mode %d", mode);
+    if (!(eps2 >= 0.0) || !isfinite(eps2)) return fail(HALMA_ERR_INVALID, "eps2 must be finite and >= 0");
+    if (mode == HALMA_POT_REFERENCE && eps2 != 0.0) return fail(HALMA_ERR_INVALID, "reference mode has no softening (eps2 must be 0)");
+    std::lock_guard<std::mutex> guard(api_mutex());
+    cudaStream_t st = (cudaStream_t)stream;
+    if (mode == HALMA_POT_FAST)
+        return potential_fast_api(ntotal, total_mass, total_x, total_y, total_z, ntest, test_x, test_y, test_z, eps2,
+                                  HALMA_MASK_COORD, 0, binding_energy, st);
+    Stager sg;
+    const float *m = nullptr, *x = nullptr, *y = nullptr, *z = nullptr, *tx = nullptr, *ty = nullptr, *tz = nullptr;
+    float *out = nullptr;
+    sg.add(total_mass, ntotal, true, false, &m);
+    sg.add(total_x, ntotal, true, false, &x);
+    sg.add(total_y, ntotal, true, false, &y);
+    sg.add(total_z, ntotal, true, false, &z);
+    sg.add(test_x, ntest, true, false, &tx);
+    sg.add(test_y, ntest, true, false, &ty);
+    sg.add(test_z, ntest, true, false, &tz);
+    sg.add((const float *)binding_energy, ntest, false, true, &out);
+    Layout L;
+    sg.plan(L);
+    void *base = nullptr;
+    HALMA_TRY(workspace(L.total, &base, st));
+    HALMA_TRY(sg.bind_and_upload(base, st));
+    if (ntotal == 0) {
+        HALMA_CUDA(cudaMemsetAsync(out, 0, sizeof(float) * ntest, st));
+    } else {
+        const int64_t ntiles = (ntest + 31) / 32;
+        const int grid = (int)std::min<int64_t>((ntiles + kWarpsPerBlock - 1) / kWarpsPerBlock, (int64_t)device_sm_count() * 16);
+        HALMA_LAUNCH(bf_potential_reference_kernel, grid, 256, 0, st, m, x, y, z, ntotal, tx, ty, tz, ntest, out);
+    }
+    return sg.download(st);
+}
+
+extern "C" int halma_potential_f32(int64_t ns, const float *m, const float *sx, const float *sy, const float *sz,
+                                   int64_t nt, const float *tx, const float *ty, const float *tz, double eps2,
+                                   int32_t mask, int64_t self_offset, float *phi, halma_stream_t stream) {
+    if (ns < 0 || nt < 0) return fail(HALMA_ERR_INVALID, "negative size");
+    if (nt == 0) return HALMA_OK;
+    if (!phi || !tx || !ty || !tz) return fail(HALMA_ERR_INVALID, "null target/output pointer");
+    if (ns > 0 && (!m || !sx || !sy || !sz)) return fail(HALMA_ERR_INVALID, "null source pointer");
+    if (mask < HALMA_MASK_COORD || mask > HALMA_MASK_NONE) return fail(HALMA_ERR_INVALID, "unknown mask %d", mask);
+    if (!(eps2 >= 0.0) || !isfinite(eps2)) return fail(HALMA_ERR_INVALID, "eps2 must be finite and >= 0");
+    std::lock_guard<std::mutex> guard(api_mutex());
+    return potential_fast_api(ns, m, sx, sy, sz, nt, tx, ty, tz, eps2, mask, self_offset, phi, (cudaStream_t)stream);
+}
+
+extern "C" int halma_potential_f64(int64_t ns, const double *mm, const double *sx_, const double *sy_,
+                                   const double *sz_, int64_t nt, const double *tx_, const double *ty_,
+                                   const double *tz_, double eps2, int32_t mask, int64_t self_offset,
+                                   double *phi, halma_stream_t stream) {
+    if (ns < 0 || nt < 0) return fail(HALMA_ERR_INVALID, "negative size");
+    if (nt == 0) return HALMA_OK;
+    if (!phi || !tx_ || !ty_ || !tz_) return fail(HALMA_ERR_INVALID, "null target/output pointer");
+    if (ns > 0 && (!mm || !sx_ || !sy_ || !sz_)) return fail(HALMA_ERR_INVALID, "null source pointer");
+    if (mask < HALMA_MASK_COORD || mask > HALMA_MASK_NONE) return fail(HALMA_ERR_INVALID, "unknown mask %d", mask);
+    if (!(eps2 >= 0.0) || !isfinite(eps2)) return fail(HALMA_ERR_INVALID, "eps2 must be finite and >= 0");
+    std::lock_guard<std::mutex> guard(api_mutex());
+    cudaStream_t st = (cudaStream_t)stream;
+    Stager sg;
+    const double *m = nullptr, *sx = nullptr, *sy = nullptr, *sz = nullptr, *tx = nullptr, *ty = nullptr, *tz = nullptr;
+    double *out = nullptr;
+    sg.add(mm, ns, true, false, &m);
+    sg.add(sx_, ns, true, false, &sx);
+    sg.add(sy_, ns, true, false, &sy);
+    sg.add(sz_, ns, true, false, &sz);
+    sg.add(tx_, nt, true, false, &tx);
+    sg.add(ty_, nt, true, false, &ty);
+    sg.add(tz_, nt, true, false, &tz);
+    sg.add((const double *)phi, nt, false, true, &out);
+    Layout L;
+    sg.plan(L);
+    void *base = nullptr;
+    HALMA_TRY(workspace(L.total, &base, st));
+    HALMA_TRY(sg.bind_and_upload(base, st));
+    HALMA_LAUNCH(potential_f64_kernel, grid_for(nt, 256), 256, 0, st, m, sx, sy, sz, ns, tx, ty, tz, nt,
+                 eps2, (int)mask, self_offset, out);
+    return sg.download(st);
+}

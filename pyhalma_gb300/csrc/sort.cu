@@ -1,0 +1,47 @@
+// Radix sorts and scans (CUB device primitives) used by FoF, groups and reductions.
+#include <cub/device/device_radix_sort.cuh>
+#include <cub/device/device_scan.cuh>
+
+#include "sort.cuh"
+
+namespace halma {
+
+size_t sort_pairs_u64_i32_bytes(int n, int end_bit) {
+    size_t b = 0;
+    cub::DeviceRadixSort::SortPairs(nullptr, b, (const uint64_t *)nullptr, (uint64_t *)nullptr,
+                                    (const int32_t *)nullptr, (int32_t *)nullptr, n, 0, end_bit);
+    return b;
+}
+
+int sort_pairs_u64_i32(void *tmp, size_t tmp_bytes, const uint64_t *kin, uint64_t *kout,
+                       const int32_t *vin, int32_t *vout, int n, int end_bit, cudaStream_t s) {
+    HALMA_CUDA(cub::DeviceRadixSort::SortPairs(tmp, tmp_bytes, kin, kout, vin, vout, n, 0, end_bit, s));
+    return HALMA_OK;
+}
+
+size_t sort_pairs_u32_i32_bytes(int n) {
+    size_t b = 0;
+    cub::DeviceRadixSort::SortPairs(nullptr, b, (const uint32_t *)nullptr, (uint32_t *)nullptr,
+                                    (const int32_t *)nullptr, (int32_t *)nullptr, n, 0, 32);
+    return b;
+}
+
+int sort_pairs_u32_i32(void *tmp, size_t tmp_bytes, const uint32_t *kin, uint32_t *kout,
+                       const int32_t *vin, int32_t *vout, int n, int end_bit, cudaStream_t s) {
+    HALMA_CUDA(cub::DeviceRadixSort::SortPairs(tmp, tmp_bytes, kin, kout, vin, vout, n, 0, end_bit, s));
+    return HALMA_OK;
+}
+
+size_t exclusive_sum_i32_bytes(int n) {
+    size_t b = 0;
+    cub::DeviceScan::ExclusiveSum(nullptr, b, (const int32_t *)nullptr, (int32_t *)nullptr, n);
+    return b;
+}
+
+int exclusive_sum_i32(void *tmp, size_t tmp_bytes, const int32_t *in, int32_t *out, int n,
+                      cudaStream_t s) {
+    HALMA_CUDA(cub::DeviceScan::ExclusiveSum(tmp, tmp_bytes, in, out, n, s));
+    return HALMA_OK;
+}
+
+}  // namespace halma

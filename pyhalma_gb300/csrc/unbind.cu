@@ -1,0 +1,576 @@
+// Batched iterative unbinding of thousands of haloes, and the plain FP64 per-halo path.
+//
+// The single pass is pyHALMA's escape cut (python_scripts/halo_properties.py:282-361):
+//     E_i = 1/2 |v_i - v_bulk|^2 - G * factor_v^2 * phi_i,   bound iff E_i <= 0
+// repeated until a pass removes nothing.  One pass over all haloes is five kernels:
+//   reduce  - per active halo, FP64 bound mass, centre of mass and bulk velocity;
+//   pack    - bound particles re-centred on their halo's centre, float4 (x, y, z, m),
+//             padded to a multiple of 32 with zero-mass far points (halo-contiguous);
+//   items   - one work item per (halo, tile of 32*T targets), biggest haloes first;
+//   pairs   - persistent kernel: warps take items from an atomic counter, stream the
+//             halo's sources through a per-warp shared-memory chunk, FP32 rsqrt pair terms,
+//             32-term FP32 partials folded into a TwoSum-compensated accumulator; the self
+//             pair is skipped by slot index;
+//   energy  - FP64 energy and sign test per bound particle, removals counted per halo;
+//             a halo whose pass removed nothing becomes inactive and costs nothing later.
+// All passes are captured once into a CUDA graph and replayed (cached by shape).
+#include <math.h>
+#include <string.h>
+
+#include <algorithm>
+#include <numeric>
+#include <vector>
+
+#include "common.cuh"
+#include "pair_math.cuh"
+#include "unbind.cuh"
+
+namespace halma {
+
+namespace {
+
+constexpr int kUbWarps = 8;
+constexpr float kFar = 3.0e30f;
+
+struct HaloState {   // per halo, FP64 unless stated
+    double M, cx, cy, cz, vx, vy, vz, ekin, epot;
+    int nb, active, iter, removed;
+};
+
+__device__ __forceinline__ double warp_sum(double v) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Block-wide FP64 sum of NV values (fixed association: warp tree, then warps in order).
+template <int NV>
+__device__ __forceinline__ void block_sum(double (&v)[NV], double (*sh)[32]) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+    for (int q = 0; q < NV; ++q) {
+        double s = warp_sum(v[q]);
+        if (lane == 0) sh[q][w] = s;
+    }
+    __syncthreads();
+    if (threadIdx.x < 32) {
+#pragma unroll
+        for (int q = 0; q < NV; ++q) {
+            double s = lane < nw ? sh[q][lane] : 0.0;
+            s = warp_sum(s);
+            if (lane == 0) sh[q][0] = s;
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < NV; ++q) v[q] = sh[q][0];
+    __syncthreads();
+}
+
+__global__ void ub_init_kernel(int64_t n, unsigned char *bound, int nh, HaloState *hs) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        bound[i] = 1;
+    for (int64_t h = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; h < nh; h += (int64_t)gridDim.x * blockDim.x) {
+        HaloState s{};
+        s.active = 1;
+        hs[h] = s;
+    }
+}
+
+// Per active halo: FP64 bound mass, centre and bulk velocity (one block per halo).
+__global__ void __launch_bounds__(256) ub_reduce_kernel(const int64_t *__restrict__ off, const double *__restrict__ x,
+                                                        const double *__restrict__ y, const double *__restrict__ z,
+                                                        const double *__restrict__ vx, const double *__restrict__ vy,
+                                                        const double *__restrict__ vz, const double *__restrict__ m,
+                                                        const unsigned char *__restrict__ bound, HaloState *hs,
+                                                        int force) {
+    const int h = blockIdx.x;
+    if (!force && !hs[h].active) return;
+    __shared__ double sh[8][32];
+    double v[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    for (int64_t i = off[h] + threadIdx.x; i < off[h + 1]; i += blockDim.x) {
+        if (!bound[i]) continue;
+        const double mi = m[i];
+        v[0] += mi;
+        v[1] += mi * x[i];
+        v[2] += mi * y[i];
+        v[3] += mi * z[i];
+        v[4] += mi * vx[i];
+        v[5] += mi * vy[i];
+        v[6] += mi * vz[i];
+        v[7] += 1.0;
+    }
+    block_sum<8>(v, sh);
+    if (threadIdx.x == 0) {
+        HaloState &s = hs[h];
+        const double M = v[0];
+        s.M = M;
+        s.nb = (int)v[7];
+        if (M > 0) {
+            s.cx = v[1] / M; s.cy = v[2] / M; s.cz = v[3] / M;
+            s.vx = v[4] / M; s.vy = v[5] / M; s.vz = v[6] / M;
+        } else {
+            s.cx = s.cy = s.cz = s.vx = s.vy = s.vz = 0.0;
+        }
+    }
+}
+
+// Stable compaction of the bound members of each active halo into its padded slot range.
+template <class V>
+__global__ void __launch_bounds__(256) ub_pack_kernel(const int64_t *__restrict__ off, const int64_t *__restrict__ poff,
+                                                      const double *__restrict__ x, const double *__restrict__ y,
+                                                      const double *__restrict__ z, const double *__restrict__ m,
+                                                      const unsigned char *__restrict__ bound, const HaloState *hs,
+                                                      V *__restrict__ pk, int *__restrict__ pidx) {
+    const int h = blockIdx.x;
+    if (!hs[h].active) return;
+    __shared__ int wcount[8];
+    __shared__ int running;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const double cx = hs[h].cx, cy = hs[h].cy, cz = hs[h].cz;
+    const int64_t b = off[h], e = off[h + 1], pb = poff[h];
+    if (threadIdx.x == 0) running = 0;
+    __syncthreads();
+    for (int64_t i0 = b; i0 < e; i0 += blockDim.x) {
+        const int64_t i = i0 + threadIdx.x;
+        const bool keep = i < e && bound[i];
+        const unsigned bal = __ballot_sync(0xffffffffu, keep);
+        if (lane == 0) wcount[w] = __popc(bal);
+        __syncthreads();
+        int before = running;
+        for (int q = 0; q < w; ++q) before += wcount[q];
+        const int rank = before + __popc(bal & ((1u << lane) - 1u));
+        if (keep) {
+            V r;
+            r.x = x[i] - cx; r.y = y[i] - cy; r.z = z[i] - cz; r.w = m[i];
+            pk[pb + rank] = r;
+            pidx[pb + rank] = (int)(i);
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            int tot = 0;
+            for (int q = 0; q < (int)(blockDim.x >> 5); ++q) tot += wcount[q];
+            running += tot;
+        }
+        __syncthreads();
+    }
+    const int nb = running;
+    const int npad = (nb + 31) & ~31;
+    for (int r = nb + threadIdx.x; r < npad; r += blockDim.x) {
+        V f;
+        f.x = f.y = f.z = kFar; f.w = 0;
+        pk[pb + r] = f;
+        pidx[pb + r] = -1;
+    }
+}
+
+// Work list for the pair kernel: haloes in decreasing initial size, tiles of 32*T targets.
+__global__ void __launch_bounds__(1024) ub_items_kernel(int nh, const int *__restrict__ order, const HaloState *hs,
+                                                        int tt, int2 *__restrict__ items, int *__restrict__ nitems,
+                                                        int *__restrict__ counter) {
+    __shared__ int wsum[32];
+    __shared__ int base;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (threadIdx.x == 0) base = 0;
+    __syncthreads();
+    for (int h0 = 0; h0 < nh; h0 += blockDim.x) {
+        const int q = h0 + threadIdx.x;
+        int h = -1, cnt = 0;
+        if (q < nh) {
+            h = order[q];
+            if (hs[h].active) cnt = (hs[h].nb + tt - 1) / tt;
+        }
+        int incl = cnt;
+        for (int o = 1; o < 32; o <<= 1) {
+            const int u = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += u;
+        }
+        if (lane == 31) wsum[w] = incl;
+        __syncthreads();
+        int pre = base;
+        for (int k = 0; k < w; ++k) pre += wsum[k];
+        const int start = pre + incl - cnt;
+        for (int t = 0; t < cnt; ++t) items[start + t] = make_int2(h, t);
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            int tot = 0;
+            for (int k = 0; k < (int)(blockDim.x >> 5); ++k) tot += wsum[k];
+            base += tot;
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        *nitems = base;
+        *counter = 0;
+    }
+}
+
+// Persistent all-pairs kernel over the work list (FP32 pair terms, compensated sums).
+template <int T>
+__global__ void __launch_bounds__(256) ub_pair_kernel(const float4 *__restrict__ pk, const int64_t *__restrict__ poff,
+                                                      const HaloState *__restrict__ hs, const int2 *__restrict__ items,
+                                                      const int *__restrict__ nitems_p, int *counter, float eps2,
+                                                      double *__restrict__ phi) {
+    __shared__ float4 buf[kUbWarps][32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int nitems = *nitems_p;
+    for (;;) {
+        int item = 0;
+        if (lane == 0) item = atomicAdd(counter, 1);
+        item = __shfl_sync(0xffffffffu, item, 0);
+        if (item >= nitems) break;
+        const int2 it = items[item];
+        const int h = it.x, tile = it.y;
+        const int64_t base = poff[h];
+        const int nb = hs[h].nb;
+        const int nchunk = (nb + 31) >> 5;
+        float px[T], py[T], pz[T], sum[T], comp[T];
+#pragma unroll
+        for (int t = 0; t < T; ++t) {
+            const int r = tile * 32 * T + t * 32 + lane;
+            const float4 p = r < nb ? pk[base + r] : make_float4(kFar, kFar, kFar, 0.f);
+            px[t] = p.x; py[t] = p.y; pz[t] = p.z;
+            sum[t] = 0.f; comp[t] = 0.f;
+        }
+        const int self0 = tile * T;   // chunk c holds the self slot of target t = c - self0
+        float4 nxt = pk[base + lane];
+        for (int c = 0; c < nchunk; ++c) {
+            __syncwarp();
+            buf[w][lane] = nxt;
+            __syncwarp();
+            if (c + 1 < nchunk) nxt = pk[base + (int64_t)(c + 1) * 32 + lane];
+            float part[T];
+#pragma unroll
+            for (int t = 0; t < T; ++t) part[t] = 0.f;
+            const int ts = c - self0;
+            if (ts >= 0 && ts < T) {
+                for (int k = 0; k < 32; ++k) {
+                    const float4 q = buf[w][k];
+#pragma unroll
+                    for (int t = 0; t < T; ++t) {
+                        const float v = pair_term_fast(q, px[t], py[t], pz[t], eps2, part[t]);
+                        part[t] = (t == ts && k == lane) ? part[t] : v;
+                    }
+                }
+            } else {
+#pragma unroll 8
+                for (int k = 0; k < 32; ++k) {
+                    const float4 q = buf[w][k];
+#pragma unroll
+                    for (int t = 0; t < T; ++t) part[t] = pair_term_fast(q, px[t], py[t], pz[t], eps2, part[t]);
+                }
+            }
+#pragma unroll
+            for (int t = 0; t < T; ++t) two_sum_acc(sum[t], comp[t], part[t]);
+        }
+#pragma unroll
+        for (int t = 0; t < T; ++t) {
+            const int r = tile * 32 * T + t * 32 + lane;
+            if (r < nb) phi[base + r] = (double)sum[t] + (double)comp[t];
+        }
+    }
+}
+
+// FP64 energies, sign test and removal counts (one block per active halo).
+__global__ void __launch_bounds__(256) ub_energy_kernel(const int64_t *__restrict__ poff, const int *__restrict__ pidx,
+                                                        const double *__restrict__ phi, const double *__restrict__ vx,
+                                                        const double *__restrict__ vy, const double *__restrict__ vz,
+                                                        const double *__restrict__ m, double gfac,
+                                                        unsigned char *__restrict__ bound, double *__restrict__ phi_out,
+                                                        HaloState *hs) {
+    const int h = blockIdx.x;
+    if (!hs[h].active) return;
+    __shared__ double sh[3][32];
+    const HaloState s = hs[h];
+    const int64_t pb = poff[h];
+    double v[3] = {0, 0, 0};   // removed, ekin (kept), epot (kept)
+    for (int r = threadIdx.x; r < s.nb; r += blockDim.x) {
+        const int i = pidx[pb + r];
+        const double dvx = vx[i] - s.vx, dvy = vy[i] - s.vy, dvz = vz[i] - s.vz;
+        const double ek = 0.5 * (dvx * dvx + dvy * dvy + dvz * dvz);
+        const double p = phi[pb + r];
+        const double e = ek - gfac * p;
+        const double mi = m[i];
+        if (e > 0.0) {
+            bound[i] = 0;
+            v[0] += 1.0;
+            if (phi_out) phi_out[i] = 0.0;
+        } else {
+            v[1] += mi * ek;
+            v[2] += mi * p;
+            if (phi_out) phi_out[i] = p;
+        }
+    }
+    block_sum<3>(v, sh);
+    if (threadIdx.x == 0) {
+        HaloState &o = hs[h];
+        o.removed = (int)v[0];
+        o.iter += 1;
+        o.ekin = v[1];
+        o.epot = -0.5 * gfac * v[2];
+        if (v[0] == 0.0) o.active = 0;
+    }
+}
+
+// Plain FP64 pair kernel for one halo (targets = sources = its packed slots).
+__global__ void __launch_bounds__(256) ub_pair_f64_kernel(const double4 *__restrict__ pk, int nb, double eps2,
+                                                          double *__restrict__ phi) {
+    __shared__ double4 sb[256];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const double4 p = i < nb ? pk[i] : make_double4(0, 0, 0, 0);
+    double acc = 0.0;
+    for (int j0 = 0; j0 < nb; j0 += 256) {
+        __syncthreads();
+        if (j0 + threadIdx.x < nb) sb[threadIdx.x] = pk[j0 + threadIdx.x];
+        __syncthreads();
+        const int cnt = min(256, nb - j0);
+        for (int k = 0; k < cnt; ++k) {
+            if (j0 + k == i) continue;
+            const double4 q = sb[k];
+            const double dx = q.x - p.x, dy = q.y - p.y, dz = q.z - p.z;
+            acc = fma(q.w, rsqrt(fma(dx, dx, fma(dy, dy, fma(dz, dz, eps2)))), acc);
+        }
+    }
+    if (i < nb) phi[i] = acc;
+}
+
+__global__ void ub_output_kernel(int nh, const HaloState *__restrict__ hs, double *__restrict__ out) {
+    for (int h = blockIdx.x * blockDim.x + threadIdx.x; h < nh; h += gridDim.x * blockDim.x) {
+        const HaloState s = hs[h];
+        double *o = out + (int64_t)h * HALMA_UB_NFIELDS;
+        o[HALMA_UB_MASS] = s.M;
+        o[HALMA_UB_CX] = s.cx; o[HALMA_UB_CY] = s.cy; o[HALMA_UB_CZ] = s.cz;
+        o[HALMA_UB_VX] = s.vx; o[HALMA_UB_VY] = s.vy; o[HALMA_UB_VZ] = s.vz;
+        o[HALMA_UB_NBOUND] = (double)s.nb;
+        o[HALMA_UB_ITER] = (double)s.iter;
+        o[HALMA_UB_EKIN] = s.ekin;
+        o[HALMA_UB_EPOT] = s.epot;
+    }
+}
+
+struct GraphCache {
+    cudaGraphExec_t exec = nullptr;
+    std::vector<uintptr_t> key;
+    cudaStream_t capture_stream = nullptr;
+    int capture_device = -1;
+    int64_t nodes = 0;
+};
+GraphCache &graph_cache() {
+    static GraphCache g;
+    return g;
+}
+
+}  // namespace
+
+int unbind_targets_per_item() { return 32 * 4; }
+
+// Device-array implementation shared by halma_unbind_batched and the pipeline.
+int unbind_device(int64_t n, int nh, const int64_t *d_off, const int64_t *h_off, const double *x, const double *y,
+                  const double *z, const double *vx, const double *vy, const double *vz, const double *m,
+                  const halma_unbind_params &p, unsigned char *bound, double *phi_out, double *halo_out,
+                  cudaStream_t st) {
+    constexpr int T = 4;
+    const int TT = 32 * T;
+    // host-side plan: padded slot offsets, work-list capacity, size order
+    std::vector<int64_t> poff(nh + 1);
+    std::vector<int> order(nh);
+    int64_t max_items = 0;
+    poff[0] = 0;
+    for (int h = 0; h < nh; ++h) {
+        const int64_t c = h_off[h + 1] - h_off[h];
+        poff[h + 1] = poff[h] + ((c + 31) / 32) * 32;
+        max_items += (c + TT - 1) / TT;
+    }
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+        return (h_off[a + 1] - h_off[a]) > (h_off[b + 1] - h_off[b]);
+    });
+    const int64_t P = std::max<int64_t>(poff[nh], 32);
+    const bool f64 = p.precision == HALMA_UNBIND_FP64;
+    Layout L;
+    const size_t o_hs = L.add(sizeof(HaloState) * (size_t)std::max(nh, 1));
+    const size_t o_poff = L.add(sizeof(int64_t) * (nh + 1));
+    const size_t o_order = L.add(sizeof(int) * std::max(nh, 1));
+    const size_t o_pk = L.add((f64 ? sizeof(double4) : sizeof(float4)) * P);
+    const size_t o_pidx = L.add(sizeof(int) * P);
+    const size_t o_phi = L.add(sizeof(double) * P);
+    const size_t o_items = L.add(sizeof(int2) * std::max<int64_t>(max_items, 1));
+    const size_t o_cnt = L.add(64);
+    const size_t o_off = d_off ? 0 : L.add(sizeof(int64_t) * (nh + 1));
+    void *base = nullptr;
+    HALMA_TRY(workspace(L.total, &base, st));
+    auto *hs = at<HaloState>(base, o_hs);
+    auto *dpoff = at<int64_t>(base, o_poff);
+    auto *dorder = at<int>(base, o_order);
+    auto *pidx = at<int>(base, o_pidx);
+    auto *phi = at<double>(base, o_phi);
+    auto *items = at<int2>(base, o_items);
+    int *cnt = at<int>(base, o_cnt);   // [0] nitems [1] counter
+    const int64_t *off = d_off;
+    if (!d_off) {
+        int64_t *o = at<int64_t>(base, o_off);
+        HALMA_CUDA(cudaMemcpyAsync(o, h_off, sizeof(int64_t) * (nh + 1), cudaMemcpyHostToDevice, st));
+        off = o;
+    }
+    HALMA_CUDA(cudaMemcpyAsync(dpoff, poff.data(), sizeof(int64_t) * (nh + 1), cudaMemcpyHostToDevice, st));
+    HALMA_CUDA(cudaMemcpyAsync(dorder, order.data(), sizeof(int) * nh, cudaMemcpyHostToDevice, st));
+    const double gfac = p.G * p.factor_v * p.factor_v;
+    const float eps2 = (float)(p.eps * p.eps);
+    HALMA_LAUNCH(ub_init_kernel, std::min(device_sm_count() * 8, grid_for(std::max<int64_t>(n, nh), 256)), 256, 0, st,
+                 n, bound, nh, hs);
+    if (phi_out) HALMA_CUDA(cudaMemsetAsync(phi_out, 0, sizeof(double) * n, st));
+
+    if (!f64) {
+        auto *pk = at<float4>(base, o_pk);
+        int bps = 0;
+        HALMA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, ub_pair_kernel<T>, 256, 0));
+        const int pgrid = device_sm_count() * std::max(bps, 1);
+        auto record = [&](cudaStream_t rs) -> int {
+            for (int it = 0; it < p.max_iter; ++it) {
+                HALMA_LAUNCH(ub_reduce_kernel, nh, 256, 0, rs, off, x, y, z, vx, vy, vz, m, bound, hs, 0);
+                HALMA_LAUNCH(ub_pack_kernel<float4>, nh, 256, 0, rs, off, dpoff, x, y, z, m, bound, hs, pk, pidx);
+                HALMA_LAUNCH(ub_items_kernel, 1, 1024, 0, rs, nh, dorder, hs, TT, items, cnt, cnt + 1);
+                HALMA_LAUNCH(ub_pair_kernel<T>, pgrid, 256, 0, rs, pk, dpoff, hs, items, cnt, cnt + 1, eps2, phi);
+                HALMA_LAUNCH(ub_energy_kernel, nh, 256, 0, rs, dpoff, pidx, phi, vx, vy, vz, m, gfac, bound, phi_out,
+                             hs);
+            }
+            return HALMA_OK;
+        };
+        if (p.use_graph) {
+            std::vector<uintptr_t> key = {(uintptr_t)base, (uintptr_t)off, (uintptr_t)x, (uintptr_t)y, (uintptr_t)z,
+                                          (uintptr_t)vx, (uintptr_t)vy, (uintptr_t)vz, (uintptr_t)m,
+                                          (uintptr_t)bound, (uintptr_t)phi_out, (uintptr_t)n, (uintptr_t)nh,
+                                          (uintptr_t)p.max_iter, (uintptr_t)st};
+            uint64_t eb, gb;
+            memcpy(&eb, &eps2, sizeof(float));
+            memcpy(&gb, &gfac, sizeof(double));
+            key.push_back((uintptr_t)eb);
+            key.push_back((uintptr_t)gb);
+            key.insert(key.end(), poff.begin(), poff.end());
+            key.push_back((uintptr_t)current_device());
+            GraphCache &gc = graph_cache();
+            if (!gc.exec || gc.key != key) {
+                if (gc.exec) {
+                    cudaGraphExecDestroy(gc.exec);
+                    gc.exec = nullptr;
+                }
+                // capture on a private stream (the legacy default stream cannot be captured)
+                if (!gc.capture_stream || gc.capture_device != current_device()) {
+                    HALMA_CUDA(cudaStreamCreateWithFlags(&gc.capture_stream, cudaStreamNonBlocking));
+                    gc.capture_device = current_device();
+                }
+                cudaGraph_t graph = nullptr;
+                HALMA_CUDA(cudaStreamBeginCapture(gc.capture_stream, cudaStreamCaptureModeThreadLocal));
+                const int64_t before = halma_kernel_launch_count();
+                int s = record(gc.capture_stream);
+                cudaError_t ce = cudaStreamEndCapture(gc.capture_stream, &graph);
+                if (s != HALMA_OK) {
+                    if (graph) cudaGraphDestroy(graph);
+                    return s;
+                }
+                HALMA_CUDA(ce);
+                cudaError_t ie = cudaGraphInstantiate(&gc.exec, graph, 0);
+                cudaGraphDestroy(graph);
+                HALMA_CUDA(ie);
+                gc.key = key;
+                gc.nodes = halma_kernel_launch_count() - before;
+                add_launches(-gc.nodes);   // counted again at every replay below
+            }
+            HALMA_CUDA(cudaGraphLaunch(gc.exec, st));
+            add_launches(gc.nodes);
+        } else {
+            HALMA_TRY(record(st));
+        }
+        // final bound mass, centre and bulk velocity over the final bound sets
+        HALMA_LAUNCH(ub_reduce_kernel, nh, 256, 0, st, off, x, y, z, vx, vy, vz, m, bound, hs, 1);
+    } else {
+        // plain FP64 path: per pass, one pair launch per active halo, host checks convergence
+        auto *pk = at<double4>(base, o_pk);
+        std::vector<HaloState> hh(nh);
+        for (int it = 0; it < p.max_iter; ++it) {
+            HALMA_LAUNCH(ub_reduce_kernel, nh, 256, 0, st, off, x, y, z, vx, vy, vz, m, bound, hs, 0);
+            HALMA_LAUNCH(ub_pack_kernel<double4>, nh, 256, 0, st, off, dpoff, x, y, z, m, bound, hs, pk, pidx);
+            HALMA_CUDA(cudaMemcpyAsync(hh.data(), hs, sizeof(HaloState) * nh, cudaMemcpyDeviceToHost, st));
+            HALMA_CUDA(cudaStreamSynchronize(st));
+            int any = 0;
+            for (int h = 0; h < nh; ++h) {
+                if (!hh[h].active || hh[h].nb == 0) continue;
+                any = 1;
+                HALMA_LAUNCH(ub_pair_f64_kernel, grid_for(hh[h].nb, 256), 256, 0, st, pk + poff[h], hh[h].nb,
+                             p.eps * p.eps, phi + poff[h]);
+            }
+            HALMA_LAUNCH(ub_energy_kernel, nh, 256, 0, st, dpoff, pidx, phi, vx, vy, vz, m, gfac, bound, phi_out, hs);
+            if (!any) break;
+        }
+        HALMA_LAUNCH(ub_reduce_kernel, nh, 256, 0, st, off, x, y, z, vx, vy, vz, m, bound, hs, 1);
+    }
+    if (halo_out) HALMA_LAUNCH(ub_output_kernel, grid_for(nh, 256), 256, 0, st, nh, hs, halo_out);
+    return HALMA_OK;
+}
+
+}  // namespace halma
+
+using namespace halma;
+
+extern "C" int halma_unbind_batched(int64_t n, int64_t n_haloes, const int64_t *offsets, const double *x,
+                                    const double *y, const double *z, const double *vx, const double *vy,
+                                    const double *vz, const double *m, const halma_unbind_params *params,
+                                    uint8_t *bound, double *phi, double *halo_out, halma_stream_t stream) {
+    if (!params) return fail(HALMA_ERR_INVALID, "params is NULL");
+    const halma_unbind_params p = *params;
+    if (n < 0 || n_haloes < 0) return fail(HALMA_ERR_INVALID, "negative size");
+    if (n >= (1ll << 31) - 64) return fail(HALMA_ERR_CAPACITY, "at most 2^31-65 particles per call");
+    if (n_haloes >= (1ll << 31) - 1) return fail(HALMA_ERR_CAPACITY, "too many haloes");
+    if (!(p.eps > 0.0) || !isfinite(p.eps)) return fail(HALMA_ERR_INVALID, "eps must be finite and > 0");
+    if (!isfinite(p.G) || !isfinite(p.factor_v)) return fail(HALMA_ERR_INVALID, "G and factor_v must be finite");
+    if (p.max_iter < 1 || p.max_iter > 1000) return fail(HALMA_ERR_INVALID, "max_iter must be in [1, 1000]");
+    if (p.precision != HALMA_UNBIND_FP32C && p.precision != HALMA_UNBIND_FP64)
+        return fail(HALMA_ERR_INVALID, "unknown precision %d", p.precision);
+    if (!offsets || (n > 0 && (!x || !y || !z || !vx || !vy || !vz || !m || !bound)))
+        return fail(HALMA_ERR_INVALID, "null pointer");
+    if (n_haloes == 0) return HALMA_OK;
+    std::lock_guard<std::mutex> guard(api_mutex());
+    cudaStream_t st = (cudaStream_t)stream;
+    // the plan needs the offsets on the host
+    std::vector<int64_t> h_off(n_haloes + 1);
+    const bool dev_off = is_device_pointer(offsets);
+    if (dev_off) {
+        HALMA_CUDA(cudaMemcpyAsync(h_off.data(), offsets, sizeof(int64_t) * (n_haloes + 1), cudaMemcpyDeviceToHost, st));
+        HALMA_CUDA(cudaStreamSynchronize(st));
+    } else {
+        memcpy(h_off.data(), offsets, sizeof(int64_t) * (n_haloes + 1));
+    }
+    if (h_off[0] != 0 || h_off[n_haloes] != n) return fail(HALMA_ERR_INVALID, "offsets must start at 0 and end at n");
+    for (int64_t h = 0; h < n_haloes; ++h)
+        if (h_off[h + 1] < h_off[h]) return fail(HALMA_ERR_INVALID, "offsets must be non-decreasing");
+    Stager sg;
+    const double *dx = nullptr, *dy = nullptr, *dz = nullptr, *dvx = nullptr, *dvy = nullptr, *dvz = nullptr,
+                 *dm = nullptr;
+    unsigned char *db = nullptr;
+    double *dphi = nullptr, *dout = nullptr;
+    sg.add(x, n, true, false, &dx);
+    sg.add(y, n, true, false, &dy);
+    sg.add(z, n, true, false, &dz);
+    sg.add(vx, n, true, false, &dvx);
+    sg.add(vy, n, true, false, &dvy);
+    sg.add(vz, n, true, false, &dvz);
+    sg.add(m, n, true, false, &dm);
+    sg.add((const unsigned char *)bound, n, false, true, &db);
+    sg.add((const double *)phi, phi ? n : 0, false, true, &dphi);
+    sg.add((const double *)halo_out, halo_out ? n_haloes * HALMA_UB_NFIELDS : 0, false, true, &dout);
+    void *stage = nullptr;
+    if (sg.any_host) {
+        Layout L;
+        sg.plan(L);
+        HALMA_CUDA(cudaMallocAsync(&stage, L.total, st));
+    }
+    int s = sg.bind_and_upload(stage, st);
+    if (s == HALMA_OK)
+        s = unbind_device(n, (int)n_haloes, dev_off ? offsets : nullptr, h_off.data(), dx, dy, dz, dvx, dvy, dvz, dm,
+                          p, db, dphi, dout, st);
+    if (s == HALMA_OK) s = sg.download(st);
+    if (stage) {
+        cudaFreeAsync(stage, st);
+        cudaStreamSynchronize(st);
+    }
+    return s;
+}

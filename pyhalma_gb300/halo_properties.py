@@ -1,0 +1,144 @@
+"""Per-halo FP64 reductions of python_scripts/halo_properties.py on the GPU.
+
+Batched form (the one the pipeline uses): ``halo_reductions(offsets, x, y, z, vx, vy, vz, m,
+mask=None, about=None)`` returns one row per CSR halo segment with the fields of
+``halma_halo_reductions``: mass, centre of mass, bulk velocity, R_max, R_1/2, sigma_eff, n.
+``about`` (n_haloes x 8: cx, cy, cz, vx, vy, vz, M, R05; NaN = computed) supplies the values
+the reference functions take as arguments instead of computing them.
+
+Drop-in single-halo functions with the reference signatures, each one launch of the same
+kernel over the halo's members:
+
+* ``total_mass(part_list, st_mass)``                                   :16-24
+* ``center_of_mass(part_list, st_x, st_y, st_z, st_mass)``             :26-43
+* ``CM_velocity(M, part_list, st_vx, st_vy, st_vz, st_mass)``          :45-60
+* ``furthest_particle(cx, cy, cz, part_list, st_x, st_y, st_z)``       :98-111
+* ``half_mass_radius(cx, cy, cz, M, part_list, st_x, st_y, st_z, st_mass)`` :365-392
+* ``sigma_effective(part_list, R05, st_x, ..., vx, vy, vz)``           :607-625
+
+``escape_velocity_unbinding_particles`` is the single-pass stellar escape cut of
+halo_properties.py:282-361 with the gas and dark-matter particles supplied by the caller
+(the reference builds them from MASCLET AMR grids, which this package does not read).
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from . import _lib
+from .halo_gas import bf_potential
+
+RED = {k: i for i, k in enumerate(_lib.RED_FIELDS)}
+N_ABOUT = 8
+NAN = float("nan")
+
+
+def halo_reductions(offsets, x, y, z, vx, vy, vz, m, mask=None, about=None):
+    """FP64 reductions per CSR segment; returns an (n_haloes, 11) array (or device tensor)."""
+    dev = _lib._is_torch(x)
+    if dev:
+        nh = int(offsets.shape[0]) - 1
+        n = int(x.shape[0])
+        out = _lib.like(x, (max(nh, 0), len(_lib.RED_FIELDS)), np.float64)
+        arrs = (offsets, x, y, z, vx, vy, vz, m)
+    else:
+        offsets = _lib.as_host(offsets, np.int64)
+        arrs = (offsets,) + tuple(_lib.as_host(a, np.float64) for a in (x, y, z, vx, vy, vz, m))
+        nh = offsets.shape[0] - 1
+        n = arrs[1].shape[0]
+        out = np.zeros((max(nh, 0), len(_lib.RED_FIELDS)), dtype=np.float64)
+        if mask is not None:
+            mask = _lib.as_host(mask, np.uint8)
+        if about is not None:
+            about = _lib.as_host(about, np.float64).reshape(nh, N_ABOUT)
+    if nh <= 0:
+        return out
+    st = _lib.lib().halma_halo_reductions(n, nh, *[_lib.ptr(a) for a in arrs], _lib.ptr(mask), _lib.ptr(about),
+                                          _lib.ptr(out), _lib.stream_of(*arrs))
+    _lib.check(st, "halma_halo_reductions")
+    return out
+
+
+def _one(part_list, st_x=None, st_y=None, st_z=None, st_vx=None, st_vy=None, st_vz=None, st_mass=None,
+         about=None):
+    pl = np.asarray(part_list, dtype=np.int64)
+
+    def g(a, fill):
+        if a is None:
+            return np.full(len(pl), fill)
+        return np.ascontiguousarray(np.asarray(a, dtype=np.float64)[pl])
+
+    ab = None if about is None else np.array([about], dtype=np.float64)
+    row = halo_reductions(np.array([0, len(pl)], dtype=np.int64), g(st_x, 0.0), g(st_y, 0.0), g(st_z, 0.0),
+                          g(st_vx, 0.0), g(st_vy, 0.0), g(st_vz, 0.0), g(st_mass, 1.0), about=ab)
+    return row[0]
+
+
+def total_mass(part_list, st_mass):
+    return float(_one(part_list, st_mass=st_mass)[RED["mass"]])
+
+
+def center_of_mass(part_list, st_x, st_y, st_z, st_mass):
+    r = _one(part_list, st_x, st_y, st_z, st_mass=st_mass)
+    if r[RED["mass"]] > 0:
+        return float(r[RED["cx"]]), float(r[RED["cy"]]), float(r[RED["cz"]]), float(r[RED["mass"]])
+    return 0., 0., 0., 0.
+
+
+def CM_velocity(M, part_list, st_vx, st_vy, st_vz, st_mass):
+    if not M > 0.:
+        return 0., 0., 0.
+    r = _one(part_list, st_vx=st_vx, st_vy=st_vy, st_vz=st_vz, st_mass=st_mass)
+    # the kernel divides by its own sum of masses; the reference divides by the caller's M
+    s = r[RED["mass"]] / M
+    return float(r[RED["vx"]] * s), float(r[RED["vy"]] * s), float(r[RED["vz"]] * s)
+
+
+def furthest_particle(cx, cy, cz, part_list, st_x, st_y, st_z):
+    if len(part_list) == 0:
+        return 0.
+    r = _one(part_list, st_x, st_y, st_z, about=[cx, cy, cz, NAN, NAN, NAN, NAN, NAN])
+    return float(r[RED["rmax"]])
+
+
+def half_mass_radius(cx, cy, cz, M, part_list, st_x, st_y, st_z, st_mass):
+    r = _one(part_list, st_x, st_y, st_z, st_mass=st_mass, about=[cx, cy, cz, NAN, NAN, NAN, M, NAN])
+    return float(r[RED["r05"]])
+
+
+def sigma_effective(part_list, R05, st_x, st_y, st_z, st_vx, st_vy, st_vz, cx, cy, cz, vx, vy, vz):
+    if len(part_list) == 0:
+        return 0.
+    r = _one(part_list, st_x, st_y, st_z, st_vx, st_vy, st_vz, about=[cx, cy, cz, vx, vy, vz, NAN, R05])
+    return float(r[RED["sigma"]])
+
+
+def escape_velocity_unbinding_particles(cx, cy, cz, vx, vy, vz, Rmax, part_list, st_x, st_y, st_z, st_vx, st_vy,
+                                        st_vz, st_mass, factor_v, gas_x=(), gas_y=(), gas_z=(), gas_mass=(),
+                                        dm_x=(), dm_y=(), dm_z=(), dm_mass=()):
+    """Single-pass escape cut (halo_properties.py:320-361): sources are the gas cells, the
+    halo's stars and the DM particles inside Rmax (concatenated in that order, :333-336);
+    E = 1/2 |v - v_bulk|^2 - G phi factor_v^2; returns ``E <= 0`` per halo star.  The
+    selection of gas and DM inside Rmax is host bookkeeping; the potential runs on the GPU."""
+    gx, gy, gz, gm = (np.asarray(a, dtype=np.float64) for a in (gas_x, gas_y, gas_z, gas_mass))
+    dmx, dmy, dmz, dmm = (np.asarray(a, dtype=np.float64) for a in (dm_x, dm_y, dm_z, dm_mass))
+    if dmx.size:
+        inside = np.sqrt((dmx - cx) ** 2 + (dmy - cy) ** 2 + (dmz - cz) ** 2) < Rmax
+        dmx, dmy, dmz, dmm = dmx[inside], dmy[inside], dmz[inside], dmm[inside]
+    if gx.size:
+        inside = np.sqrt((gx - cx) ** 2 + (gy - cy) ** 2 + (gz - cz) ** 2) < Rmax
+        gx, gy, gz, gm = gx[inside], gy[inside], gz[inside], gm[inside]
+    pl = np.asarray(part_list)
+    sx, sy, sz = st_x[pl], st_y[pl], st_z[pl]
+    if len(sx) == 0:
+        return np.array([], dtype=bool)
+    tx = np.concatenate((gx, sx, dmx))
+    ty = np.concatenate((gy, sy, dmy))
+    tz = np.concatenate((gz, sz, dmz))
+    tm = np.concatenate((gm, st_mass[pl], dmm))
+    e = -bf_potential(tm, tx, ty, tz, sx, sy, sz)
+    G_const = 4.3 * 1e-3
+    G_const *= 1e-6
+    e *= G_const
+    e *= factor_v ** 2
+    ek = 0.5 * ((st_vx[pl] - vx) ** 2 + (st_vy[pl] - vy) ** 2 + (st_vz[pl] - vz) ** 2)
+    return (ek + e) <= 0.

@@ -1,0 +1,257 @@
+"""Generate golden fixtures by running pyHALMA's own Python code in this container.
+
+Run from the repository root:  python tests/golden/make_golden.py [--reference DIR]
+
+The reference tree is read in place (default /root/reference) and never modified.  Modules
+that are absent here are replaced by stubs in ``sys.modules`` before the import:
+
+* ``numba``: ``njit`` returns the function unchanged, ``prange`` is ``range`` and
+  ``get_num_threads`` returns 1, so the numba kernels run as plain Python;
+* ``masclet_framework``, ``matplotlib``: empty namespaces (only ``units.mass_to_sun`` is
+  read on the paths used here);
+* ``fortran_modules.particle``: ``particle.brute_force_binding_energy`` maps onto the
+  oracle's float32 restatement of particle_subroutines.f90:466-514 (gfortran is absent).
+
+Fixtures written to tests/golden/ (all seeds fixed):
+
+* fof_cases.npz   — reference ``fof.friends_of_friends_serial`` on small synthetic and
+  adversarial inputs (positions stored exactly; canonical labels = min index, -1 alone);
+* fof_config1.npz — the same on the 1e5-particle Plummer snapshot; inputs are regenerated
+  from the seed by ``pyhalma_gb300.synth`` and checked against the stored SHA-256;
+* predicate.npz   — adversarial two-point pairs at nextafter distances and whether the
+  reference's KDTree links them (pins the pair predicate);
+* halo_props.npz  — reference reductions (halo_properties.py) on a few haloes;
+* rps.npz         — reference ``halo_gas.RPS`` / ``most_bound_particle`` outputs with
+  ``np.random.seed`` fixed before each call (pins the sub-sampling and energy logic).
+"""
+from __future__ import annotations
+
+import argparse
+import hashlib
+import os
+import sys
+import types
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+import oracle  # noqa: E402
+from pyhalma_gb300 import synth  # noqa: E402
+
+
+def install_stubs():
+    nb = types.ModuleType("numba")
+
+    def njit(*a, **k):
+        if a and callable(a[0]) and not k:
+            return a[0]
+        return lambda f: f
+
+    nb.njit = njit
+    nb.jit = njit
+    nb.prange = range
+    nb.get_num_threads = lambda: 1
+    nb.set_num_threads = lambda n: None
+    sys.modules["numba"] = nb
+
+    mf = types.ModuleType("masclet_framework")
+    for sub in ("units", "tools", "particles", "particle2grid", "read_masclet", "read_asohf",
+                "cosmo_tools"):
+        m = types.ModuleType("masclet_framework." + sub)
+        setattr(mf, sub, m)
+        sys.modules["masclet_framework." + sub] = m
+    mf.units.mass_to_sun = 1.0
+    sys.modules["masclet_framework"] = mf
+
+    mpl = types.ModuleType("matplotlib")
+    plt = types.ModuleType("matplotlib.pyplot")
+    mpl.pyplot = plt
+    sys.modules["matplotlib"] = mpl
+    sys.modules["matplotlib.pyplot"] = plt
+
+    fm = types.ModuleType("fortran_modules")
+    part = types.ModuleType("fortran_modules.particle")
+
+    class _P:
+        @staticmethod
+        def brute_force_binding_energy(ncores, ntotal, m, x, y, z, ntest, tx, ty, tz):
+            assert m.dtype == np.float32 and tx.dtype == np.float32
+            assert int(ntotal) == len(m) and int(ntest) == len(tx)
+            return oracle.bf_potential_f32(m, x, y, z, tx, ty, tz, ncores=max(int(ncores), 1))
+
+        serial_brute_force_binding_energy = None
+
+    part.particle = _P
+    fm.particle = part
+    sys.modules["fortran_modules"] = fm
+    sys.modules["fortran_modules.particle"] = part
+
+
+def import_reference(refdir):
+    install_stubs()
+    sys.path.insert(0, refdir)
+    from python_scripts import fof, halo_gas, halo_properties  # noqa
+    return fof, halo_gas, halo_properties
+
+
+def sha(*arrays):
+    h = hashlib.sha256()
+    for a in arrays:
+        h.update(np.ascontiguousarray(a).tobytes())
+    return h.hexdigest()
+
+
+def fof_cases(fof):
+    cases = {}
+    rng = np.random.default_rng(11)
+    # 1) small clustered snapshot
+    s = synth.plummer_snapshot(4000, 8, seed=3, box_mpc=0.5)
+    cases["plummer4k"] = (np.stack([s.x, s.y, s.z], 1), 0.0015)
+    # 2) lattice with spacing exactly the linking length (ties at d == r), jittered by ulps
+    cases["lattice_tie"] = (synth.lattice_points(9, 0.0015, origin=(0.3, -0.2, 0.1)), 0.0015)
+    cases["lattice_jitter"] = (synth.lattice_points(9, 0.0015, origin=(1.7, 2.3, -4.1),
+                                                    jitter_ulps=2, seed=5), 0.0015)
+    # 3) duplicates, chains and isolated points
+    base = rng.uniform(0, 0.05, (600, 3))
+    dup = np.concatenate([base, base[:100], base[50:60]])
+    cases["duplicates"] = (dup, 0.002)
+    chain = np.zeros((400, 3))
+    chain[:, 0] = np.arange(400) * 0.0015
+    chain[:, 1] = 0.25
+    cases["chain"] = (chain, 0.0015)
+    cases["sparse"] = (rng.uniform(-1, 1, (500, 3)), 0.01)
+    cases["single"] = (np.array([[0.1, 0.2, 0.3]]), 0.0015)
+    cases["pair_at_r"] = (np.array([[0.0, 0.0, 0.0], [0.0015, 0.0, 0.0]]), 0.0015)
+    big = rng.normal(0, 0.004, (3000, 3))
+    cases["blob"] = (big, 0.0004)
+    out = {}
+    for name, (data, ll) in cases.items():
+        groups = fof.friends_of_friends_serial(data[:, 0], data[:, 1], data[:, 2], ll)
+        lab = oracle.groups_to_labels(groups, data.shape[0])
+        out[f"{name}__xyz"] = data
+        out[f"{name}__ll"] = np.float64(ll)
+        out[f"{name}__labels"] = lab
+        out[f"{name}__ngroups"] = np.int64(len(groups))
+        print(f"  fof {name}: n={data.shape[0]} groups={len(groups)}")
+    np.savez_compressed(os.path.join(HERE, "fof_cases.npz"), **out)
+
+
+def fof_config1(fof):
+    s = synth.plummer_snapshot(100_000, 50, seed=0, box_mpc=10.0)
+    groups = fof.friends_of_friends_serial(s.x, s.y, s.z, 0.0015)
+    lab = oracle.groups_to_labels(groups, s.n)
+    np.savez_compressed(os.path.join(HERE, "fof_config1.npz"), labels=lab,
+                        sha256=np.array(sha(s.x, s.y, s.z)), ll=np.float64(0.0015),
+                        n=np.int64(s.n), seed=np.int64(0), n_spheres=np.int64(50),
+                        box_mpc=np.float64(10.0), ngroups=np.int64(len(groups)))
+    print(f"  fof config1: n={s.n} groups={len(groups)}")
+
+
+def predicate_pairs(fof):
+    from scipy.spatial import KDTree
+    rng = np.random.default_rng(7)
+    a_all, b_all, r_all, hit_all = [], [], [], []
+    for r in (0.0015, 1.5, 0.7):
+        found, tries = 0, 0
+        while found < 400 and tries < 200_000:
+            tries += 1
+            a = rng.uniform(-4 * r, 4 * r, 3)
+            d = rng.normal(size=3)
+            d /= np.linalg.norm(d)
+            b = a + d * r
+            for k in range(3):
+                for _ in range(rng.integers(0, 3)):
+                    b[k] = np.nextafter(b[k], np.inf if rng.random() < 0.5 else -np.inf)
+            dx, dy, dz = a - b
+            seq = (dx * dx + dy * dy) + dz * dz <= r * r
+            alt = np.sqrt(dx * dx + dy * dy + dz * dz) <= r
+            alt2 = dx * dx + (dy * dy + dz * dz) <= r * r
+            if seq == alt and seq == alt2:
+                continue  # keep only pairs where plausible predicates disagree
+            hit = 1 in KDTree(np.array([a, b])).query_ball_point(a, r)
+            found += 1
+            a_all.append(a); b_all.append(b); r_all.append(r); hit_all.append(hit)
+    np.savez_compressed(os.path.join(HERE, "predicate.npz"), a=np.array(a_all),
+                        b=np.array(b_all), r=np.array(r_all), hit=np.array(hit_all))
+    print(f"  predicate pairs: {len(r_all)}")
+
+
+def halo_props(hp):
+    s = synth.plummer_snapshot(20_000, 6, seed=4, box_mpc=1.0)
+    out = {"x": s.x, "y": s.y, "z": s.z, "vx": s.vx, "vy": s.vy, "vz": s.vz, "m": s.mass}
+    res = []
+    for h in range(6):
+        pl = np.nonzero(s.sphere == h)[0].astype(np.int64)
+        cx, cy, cz, M = hp.center_of_mass(pl, s.x, s.y, s.z, s.mass)
+        tm = hp.total_mass(pl, s.mass)
+        vx, vy, vz = hp.CM_velocity(M, pl, s.vx, s.vy, s.vz, s.mass)
+        rmax = hp.furthest_particle(cx, cy, cz, pl, s.x, s.y, s.z)
+        r05 = hp.half_mass_radius(cx, cy, cz, M, pl, s.x, s.y, s.z, s.mass)
+        sig = hp.sigma_effective(pl, r05, s.x, s.y, s.z, s.vx, s.vy, s.vz, cx, cy, cz, vx, vy, vz)
+        res.append([tm, cx, cy, cz, M, vx, vy, vz, rmax, r05, sig])
+        out[f"pl{h}"] = pl
+    out["results"] = np.array(res)
+    np.savez_compressed(os.path.join(HERE, "halo_props.npz"), **out)
+    print("  halo properties: 6 haloes")
+
+
+def rps_cases(hg):
+    out = {}
+    n = 0
+    for k, (ngas, ndm, nst, lim) in enumerate([(800, 300, 400, 5000), (7000, 6000, 5500, 5000),
+                                               (1200, 9000, 300, 1000)]):
+        g = synth.nfw_gas_halo(ngas, nst, seed=20 + k, r_vir_kpc=60.0)
+        rng = np.random.default_rng(40 + k)
+        dm = rng.normal(0, 0.02, (ndm, 3))
+        mass_dm_part = 1e7
+        dm_m = np.where(rng.random(ndm) < 0.3, mass_dm_part / 8, mass_dm_part / 64)
+        vb = g.bulk
+        gas = [g.gas_x.astype(np.float64), g.gas_y.astype(np.float64), g.gas_z.astype(np.float64),
+               g.gas_vx, g.gas_vy, g.gas_vz, g.gas_mass, g.gas_temp]
+        oripa = np.arange(nst) + 1000 * k
+        for nspec in (1, 2):
+            np.random.seed(1234 + k)
+            r = hg.RPS(*gas, dm[:, 0], dm[:, 1], dm[:, 2], dm_m, g.st_x, g.st_y, g.st_z,
+                       g.st_mass, vb[0], vb[1], vb[2], lim, mass_dm_part, nspec)
+            out[f"c{k}_rps{nspec}"] = np.array(r, dtype=np.float64)
+        np.random.seed(999 + k)
+        mb = hg.most_bound_particle(gas[0], gas[1], gas[2], gas[6], dm[:, 0], dm[:, 1], dm[:, 2],
+                                    dm_m, g.st_x, g.st_y, g.st_z, g.st_mass, oripa, lim,
+                                    mass_dm_part)
+        out[f"c{k}_mb"] = np.array(mb, dtype=np.float64)
+        for name, arr in (("gx", gas[0]), ("gy", gas[1]), ("gz", gas[2]), ("gvx", gas[3]),
+                          ("gvy", gas[4]), ("gvz", gas[5]), ("gm", gas[6]), ("gt", gas[7]),
+                          ("dx", dm[:, 0]), ("dy", dm[:, 1]), ("dz", dm[:, 2]), ("dm", dm_m),
+                          ("sx", g.st_x), ("sy", g.st_y), ("sz", g.st_z), ("sm", g.st_mass),
+                          ("oripa", oripa), ("bulk", vb)):
+            out[f"c{k}_{name}"] = arr
+        out[f"c{k}_params"] = np.array([lim, mass_dm_part], dtype=np.float64)
+        n += 1
+    np.savez_compressed(os.path.join(HERE, "rps.npz"), ncase=np.int64(n), **out)
+    print(f"  rps/most-bound: {n} cases")
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--only", default="")
+    args = ap.parse_args()
+    fof, hg, hp = import_reference(args.reference)
+    todo = args.only.split(",") if args.only else ["fof", "config1", "pred", "props", "rps"]
+    if "fof" in todo:
+        fof_cases(fof)
+    if "config1" in todo:
+        fof_config1(fof)
+    if "pred" in todo:
+        predicate_pairs(fof)
+    if "props" in todo:
+        halo_props(hp)
+    if "rps" in todo:
+        rps_cases(hg)
+
+
+if __name__ == "__main__":
+    main()

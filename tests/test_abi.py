@@ -1,0 +1,86 @@
+"""C ABI: the library loads, exports every function include/halma.h declares, and rejects bad
+arguments with the documented status before touching a GPU (CPU only)."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+from pyhalma_gb300 import _lib
+
+HEADER = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include", "halma.h")
+
+
+def declared_functions():
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"^\s*(?:int|int64_t|const char \*)\s*\*?\s*(halma_\w+)\s*\(", text, flags=re.M)))
+
+
+def test_header_declares_the_boundary():
+    names = declared_functions()
+    for must in ("halma_fof", "halma_fof_groups", "halma_bf_potential_f32", "halma_potential_f64",
+                 "halma_potential_f32", "halma_potential_grad_f32", "halma_halo_reductions",
+                 "halma_unbind_batched", "halma_find_haloes"):
+        assert must in names
+
+
+def test_library_exports_every_declared_symbol():
+    L = _lib.lib()
+    for name in declared_functions():
+        assert hasattr(L, name), name
+        assert name in _lib.SIGNATURES, f"{name} has no ctypes signature"
+
+
+def test_status_strings_and_version():
+    L = _lib.lib()
+    assert L.halma_abi_version() == 1
+    assert L.halma_status_string(0) == b"ok"
+    assert L.halma_status_string(-1) == b"invalid argument"
+
+
+def test_invalid_arguments_are_rejected_before_any_device_work():
+    L = _lib.lib()
+    x = np.zeros(4)
+    lab = np.zeros(4, dtype=np.int32)
+    assert L.halma_fof(-1, _lib.ptr(x), _lib.ptr(x), _lib.ptr(x), 1.0, _lib.ptr(lab), None, None) == _lib.ERR_INVALID
+    assert L.halma_fof(4, _lib.ptr(x), _lib.ptr(x), _lib.ptr(x), -1.0, _lib.ptr(lab), None, None) == _lib.ERR_INVALID
+    assert b"linking length" in L.halma_last_error()
+    assert L.halma_fof(4, _lib.ptr(x), _lib.ptr(x), _lib.ptr(x), float("nan"), _lib.ptr(lab), None, None) == \
+        _lib.ERR_INVALID
+    assert L.halma_fof(4, None, _lib.ptr(x), _lib.ptr(x), 1.0, _lib.ptr(lab), None, None) == _lib.ERR_INVALID
+    f = np.zeros(3, dtype=np.float32)
+    assert L.halma_bf_potential_f32(3, *[_lib.ptr(f)] * 4, 3, *[_lib.ptr(f)] * 3, _lib.ptr(f), 7, 0.0, None) == \
+        _lib.ERR_INVALID
+    assert L.halma_bf_potential_f32(3, *[_lib.ptr(f)] * 4, 3, *[_lib.ptr(f)] * 3, _lib.ptr(f),
+                                    _lib.POT_REFERENCE, 0.5, None) == _lib.ERR_INVALID
+    # no targets: nothing to do, success without a device
+    assert L.halma_bf_potential_f32(3, *[_lib.ptr(f)] * 4, 0, *[_lib.ptr(f)] * 3, _lib.ptr(f),
+                                    _lib.POT_FAST, 0.0, None) == _lib.OK
+    p = _lib.UnbindParams(0.0, 4.3e-9, 1.0, 10, 0, 1, 0)
+    off = np.array([0, 4], dtype=np.int64)
+    b = np.zeros(4, dtype=np.uint8)
+    assert L.halma_unbind_batched(4, 1, _lib.ptr(off), *[_lib.ptr(x)] * 7, ctypes.byref(p), _lib.ptr(b), None,
+                                  None, None) == _lib.ERR_INVALID          # eps must be > 0
+    p = _lib.UnbindParams(1e-4, 4.3e-9, 1.0, 0, 0, 1, 0)
+    assert L.halma_unbind_batched(4, 1, _lib.ptr(off), *[_lib.ptr(x)] * 7, ctypes.byref(p), _lib.ptr(b), None,
+                                  None, None) == _lib.ERR_INVALID          # max_iter >= 1
+    p = _lib.UnbindParams(1e-4, 4.3e-9, 1.0, 5, 9, 1, 0)
+    assert L.halma_unbind_batched(4, 1, _lib.ptr(off), *[_lib.ptr(x)] * 7, ctypes.byref(p), _lib.ptr(b), None,
+                                  None, None) == _lib.ERR_INVALID          # unknown precision
+    assert L.halma_potential_grad_f32(3, *[_lib.ptr(f)] * 4, 3, *[_lib.ptr(f)] * 4, 0.0, _lib.MASK_COORD, 0,
+                                      None, None, None, None) == _lib.ERR_INVALID
+
+
+def test_python_layer_raises_value_error():
+    from pyhalma_gb300 import fof
+    with pytest.raises(ValueError):
+        fof.fof_labels(np.zeros(3), np.zeros(2), np.zeros(3), 1.0)
+    with pytest.raises(ValueError):
+        fof.friends_of_friends(np.zeros((3, 2)), 1.0)
+
+
+def test_unbind_params_layout():
+    # the C struct: 3 doubles + 4 int32
+    assert ctypes.sizeof(_lib.UnbindParams) == 40

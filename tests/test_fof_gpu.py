@@ -1,0 +1,100 @@
+"""GPU FoF parity: bit-exact partition and labels against the reference (golden fixtures)
+and against the exact C oracle at the single-GPU workload size."""
+import hashlib
+
+import numpy as np
+import pytest
+
+import oracle
+from pyhalma_gb300 import fof, synth
+
+pytestmark = pytest.mark.gpu
+
+
+def _cases(d):
+    return sorted(set(k.split("__")[0] for k in d.files))
+
+
+def test_reference_cases_bit_exact(golden, cuda):
+    d = golden("fof_cases.npz")
+    for name in _cases(d):
+        xyz = d[name + "__xyz"]
+        ll = float(d[name + "__ll"])
+        lab = fof.fof_labels(xyz[:, 0].copy(), xyz[:, 1].copy(), xyz[:, 2].copy(), ll)
+        assert np.array_equal(lab, d[name + "__labels"]), name
+        groups = fof.friends_of_friends(xyz, ll)
+        assert groups == oracle.labels_to_groups(d[name + "__labels"]), name
+
+
+def test_reference_config1_bit_exact(golden, cuda):
+    c = golden("fof_config1.npz")
+    s = synth.plummer_snapshot(int(c["n"]), int(c["n_spheres"]), seed=int(c["seed"]), box_mpc=float(c["box_mpc"]))
+    h = hashlib.sha256()
+    for a in (s.x, s.y, s.z):
+        h.update(np.ascontiguousarray(a).tobytes())
+    if h.hexdigest() != str(c["sha256"]):
+        pytest.skip("this NumPy regenerates a different snapshot from the seed")
+    groups = fof.friends_of_friends_serial(s.x, s.y, s.z, float(c["ll"]))
+    assert len(groups) == int(c["ngroups"])
+    assert np.array_equal(oracle.groups_to_labels(groups, s.n), c["labels"])
+
+
+def test_two_million_particles_match_oracle(cuda):
+    s = synth.plummer_snapshot(2_000_000, 500, seed=1, box_mpc=10.0, contaminant_frac=0.15)
+    lab = fof.fof_labels(s.x, s.y, s.z, 0.0015)
+    ref = oracle.fof_labels(s.x, s.y, s.z, 0.0015)
+    assert np.array_equal(lab, ref)
+    # CSR groups: reference order, strict minp filter of the "parallel" variant
+    off, mem = fof.fof_groups(lab, 50)
+    ref_groups = [g for g in oracle.labels_to_groups(ref) if len(g) >= 50]
+    assert len(off) - 1 == len(ref_groups)
+    for g in (0, len(ref_groups) // 2, len(ref_groups) - 1):
+        assert mem[off[g]:off[g + 1]].tolist() == ref_groups[g]
+
+
+def test_device_tensors_in_place(cuda):
+    import torch
+    s = synth.plummer_snapshot(50_000, 20, seed=9, box_mpc=2.0)
+    x, y, z = (torch.from_numpy(a).to(cuda) for a in (s.x, s.y, s.z))
+    lab = fof.fof_labels(x, y, z, 0.0015)
+    assert lab.is_cuda and lab.dtype == torch.int32
+    assert np.array_equal(lab.cpu().numpy(), oracle.fof_labels(s.x, s.y, s.z, 0.0015))
+
+
+def test_edge_cases(cuda):
+    e = np.zeros(0)
+    assert fof.friends_of_friends_serial(e, e, e, 0.0015) == []
+    assert fof.friends_of_friends_serial(np.array([1.0]), np.array([2.0]), np.array([3.0]), 0.0015) == []
+    # zero linking length links coincident points only
+    p = np.array([[0.0, 0.0, 0.0], [0.0, 0.0, 0.0], [1e-12, 0.0, 0.0], [5.0, 5.0, 5.0], [5.0, 5.0, 5.0]])
+    assert fof.friends_of_friends(p, 0.0) == [[0, 1], [3, 4]]
+    # a linking length larger than the box puts everything in one group
+    rng = np.random.default_rng(3)
+    q = rng.uniform(0, 1, (1000, 3))
+    assert fof.friends_of_friends(q, 10.0) == [list(range(1000))]
+    with pytest.raises(ValueError):
+        fof.friends_of_friends(np.array([[0.0, np.nan, 0.0], [0.0, 0.0, 0.0]]), 1.0)
+    with pytest.raises(ValueError):
+        fof.friends_of_friends(q, -1.0)
+
+
+def test_parallel_variants_filter_strictly(cuda):
+    s = synth.plummer_snapshot(30_000, 12, seed=2, box_mpc=1.0)
+    groups = fof.friends_of_friends_parallel(s.x, s.y, s.z, 0.0015, 1.0, 50, s.mass)
+    ref = [g for g in oracle.labels_to_groups(oracle.fof_labels(s.x, s.y, s.z, 0.0015)) if len(g) > 50]
+    assert [g.tolist() for g in groups] == ref
+    assert [g.tolist() for g in fof.pyfof_friends_of_friends_parallel(s.x, s.y, s.z, 0.0015, 1.0, 50, s.mass)] == ref
+
+
+def test_dense_lattices_and_random_clusters_property(cuda):
+    rng = np.random.default_rng(17)
+    for trial in range(6):
+        n = int(rng.integers(2_000, 40_000))
+        pts = rng.normal(0, rng.uniform(0.001, 0.02), (n, 3)) + rng.uniform(-50, 50, 3)
+        ll = float(rng.uniform(0.0002, 0.002))
+        lab = fof.fof_labels(pts[:, 0].copy(), pts[:, 1].copy(), pts[:, 2].copy(), ll)
+        assert np.array_equal(lab, oracle.fof_labels(pts[:, 0], pts[:, 1], pts[:, 2], ll)), trial
+    # ties: lattice spacing equal to the linking length at large coordinates
+    pts = synth.lattice_points(24, 0.0015, origin=(37.1, -12.3, 4.4), jitter_ulps=1, seed=4)
+    lab = fof.fof_labels(pts[:, 0].copy(), pts[:, 1].copy(), pts[:, 2].copy(), 0.0015)
+    assert np.array_equal(lab, oracle.fof_labels(pts[:, 0], pts[:, 1], pts[:, 2], 0.0015))

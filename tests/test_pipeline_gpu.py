@@ -1,0 +1,34 @@
+"""One-call snapshot pipeline (FoF -> groups >= minp -> batched unbinding) against the
+oracle composition on the 1e5-particle Plummer snapshot."""
+import numpy as np
+import pytest
+
+import oracle
+from oracle.unbind import unbind_halo
+from pyhalma_gb300 import synth
+from pyhalma_gb300.unbinding import G_MPC, UnbindOptions, find_haloes
+
+pytestmark = pytest.mark.gpu
+
+
+def test_find_haloes_matches_oracle_composition(cuda):
+    s = synth.plummer_snapshot(100_000, 50, seed=0, box_mpc=10.0, contaminant_frac=0.15)
+    cat = find_haloes(s.x, s.y, s.z, s.vx, s.vy, s.vz, s.mass, 0.0015, minp=50,
+                      options=UnbindOptions(eps=1e-4, max_iter=50))
+    lab = oracle.fof_labels(s.x, s.y, s.z, 0.0015)
+    assert np.array_equal(cat.labels, lab)
+    groups = [g for g in oracle.labels_to_groups(lab) if len(g) >= 50]
+    assert cat.n_haloes == len(groups)
+    expect = np.zeros(s.n, dtype=np.uint8)
+    for h, g in enumerate(groups):
+        g = np.array(g)
+        assert np.array_equal(cat.members[cat.offsets[h]:cat.offsets[h + 1]], g)
+        b, it, e, phi = unbind_halo(s.x[g], s.y[g], s.z[g], s.vx[g], s.vy[g], s.vz[g], s.mass[g], eps=1e-4,
+                                    max_iter=50, return_energy=True)
+        diff = cat.bound[g].astype(bool) != b
+        if diff.any():
+            scale = np.abs(e) / (np.abs(e) + G_MPC * np.abs(phi))
+            assert np.all(scale[diff] <= 1e-5)
+        expect[g] = b
+    assert (cat.bound != expect).sum() <= 5
+    assert cat.haloes.shape == (cat.n_haloes, 11)

@@ -1,0 +1,115 @@
+"""Batched unbinding parity against the FP64 oracle (oracle/unbind.py).
+
+Tolerances written here:
+* potential: |phi_gpu / phi_fp64 - 1| <= RTOL_PHI = 1e-6 per particle (FP32-compensated path);
+* membership: a particle may end on the other side of the cut only if its FP64 energy lies
+  within BAND = 1e-5 * (E_kin + G*phi) of zero (the FP32 error band, with margin);
+* halo table: FP64 mass / centre / bulk velocity of the bound set at 1e-12 relative.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from oracle.unbind import unbind_halo
+from pyhalma_gb300 import synth
+from pyhalma_gb300.unbinding import G_MPC, UnbindOptions, unbind_batched
+
+pytestmark = pytest.mark.gpu
+RTOL_PHI = 1e-6
+BAND = 1e-5
+EPS = 1e-4
+
+
+@pytest.fixture(scope="module")
+def catalogue():
+    return synth.powerlaw_catalogue(80, seed=3, n_min=50, n_max=6000, contaminant_frac=0.15, alpha=0.6)
+
+
+def _arrays(cat):
+    return cat.offsets, cat.x, cat.y, cat.z, cat.vx, cat.vy, cat.vz, cat.mass
+
+
+def _check_against_oracle(cat, bound, phi, halo, rtol_phi):
+    flips = 0
+    for h in range(cat.n_haloes):
+        sl = slice(cat.offsets[h], cat.offsets[h + 1])
+        b_ref, it, e_ref, phi_ref = unbind_halo(cat.x[sl], cat.y[sl], cat.z[sl], cat.vx[sl], cat.vy[sl],
+                                                cat.vz[sl], cat.mass[sl], eps=EPS, max_iter=50,
+                                                return_energy=True)
+        b = bound[sl].astype(bool)
+        diff = b != b_ref
+        if diff.any():
+            scale = np.abs(e_ref) / (np.abs(e_ref) + G_MPC * np.abs(phi_ref))
+            assert np.all(scale[diff] <= BAND), (h, scale[diff])
+            flips += int(diff.sum())
+            continue
+        # same final set: the GPU's last-pass potential is the potential of that set
+        p = phi[sl][b]
+        assert np.max(np.abs(p / phi_ref[b] - 1.0)) <= rtol_phi, h
+        m = cat.mass[sl][b]
+        M = m.sum()
+        row = halo[h]
+        assert row[7] == b.sum()
+        assert abs(row[0] / M - 1) < 1e-12
+        for k, a in ((1, cat.x), (2, cat.y), (3, cat.z), (4, cat.vx), (5, cat.vy), (6, cat.vz)):
+            ref = (m * a[sl][b]).sum() / M
+            assert abs(row[k] - ref) <= 1e-12 * max(1.0, abs(ref)), (h, k)
+    return flips
+
+
+def test_fp32c_matches_fp64_oracle(catalogue, cuda):
+    bound, halo, phi = unbind_batched(*_arrays(catalogue), UnbindOptions(eps=EPS, max_iter=50), want_phi=True)
+    flips = _check_against_oracle(catalogue, bound, phi, halo, RTOL_PHI)
+    assert flips <= 5
+    cont = catalogue.contaminant
+    assert not bound[cont].any()
+
+
+def test_fp64_path_matches_oracle(catalogue, cuda):
+    bound, halo, phi = unbind_batched(*_arrays(catalogue), UnbindOptions(eps=EPS, max_iter=50, precision="fp64"),
+                                      want_phi=True)
+    assert _check_against_oracle(catalogue, bound, phi, halo, 1e-12) == 0
+
+
+def test_graph_replay_is_identical_and_deterministic(catalogue, cuda):
+    a = unbind_batched(*_arrays(catalogue), UnbindOptions(eps=EPS, max_iter=12, use_graph=True), want_phi=True)
+    b = unbind_batched(*_arrays(catalogue), UnbindOptions(eps=EPS, max_iter=12, use_graph=False), want_phi=True)
+    c = unbind_batched(*_arrays(catalogue), UnbindOptions(eps=EPS, max_iter=12, use_graph=True), want_phi=True)
+    for x, y in ((a, b), (a, c)):
+        assert np.array_equal(x[0], y[0])
+        assert np.array_equal(x[1], y[1])
+        assert np.array_equal(x[2], y[2])
+
+
+def test_iteration_cap_and_pass_count(catalogue, cuda):
+    bound1, halo1, _ = unbind_batched(*_arrays(catalogue), UnbindOptions(eps=EPS, max_iter=1))
+    assert np.all(halo1[:, 8] == 1)
+    bound, halo, _ = unbind_batched(*_arrays(catalogue), UnbindOptions(eps=EPS, max_iter=50))
+    assert halo[:, 8].max() >= 2
+    # one pass removes a subset of what the converged cut removes
+    assert np.all(bound <= bound1)
+
+
+def test_edge_cases(cuda):
+    # empty haloes and single-particle haloes
+    off = np.array([0, 0, 1, 3], dtype=np.int64)
+    x = np.array([0.0, 1.0, 1.0001])
+    v = np.zeros(3)
+    m = np.full(3, 1e8)
+    bound, halo, phi = unbind_batched(off, x, v, v, v, v, v, m, UnbindOptions(eps=EPS), want_phi=True)
+    assert bound.tolist() == [1, 1, 1]     # at rest: every particle is bound (E = -G phi <= 0)
+    assert halo[0, 7] == 0 and halo[1, 7] == 1 and halo[2, 7] == 2
+    assert phi[0] == 0.0
+    assert abs(phi[1] / (1e8 / np.sqrt(1e-8 + EPS ** 2)) - 1) < 1e-6
+    # no haloes at all
+    b2, h2, _ = unbind_batched(np.array([0], dtype=np.int64), np.zeros(0), *[np.zeros(0)] * 6)
+    assert b2.shape == (0,) and h2.shape[0] == 0
+
+
+def test_device_tensors(catalogue, cuda):
+    import torch
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(cuda)
+    bound_d, halo_d, _ = unbind_batched(*[t(a) for a in _arrays(catalogue)], UnbindOptions(eps=EPS, max_iter=50))
+    bound_h, halo_h, _ = unbind_batched(*_arrays(catalogue), UnbindOptions(eps=EPS, max_iter=50))
+    assert np.array_equal(bound_d.cpu().numpy(), bound_h)
+    assert np.array_equal(halo_d.cpu().numpy(), halo_h)
