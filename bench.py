@@ -1,0 +1,376 @@
+#!/usr/bin/env python
+"""FoF + batched unbinding throughput of one synthetic snapshot (single-GPU workload).
+
+Workload (one "step"): 2,000,000 star particles in a 10 Mpc box, 500 Plummer spheres with
+log-uniform masses 1e8-1e11 Msun, 15 % contaminants per sphere at 3 v_esc, 10 % uniform
+background; FoF at LL = 1.5 kpc (exact reference partition), groups >= 50 members, then
+iterative unbinding of every group (FP32 pair terms, compensated sums, FP64 reductions,
+softening 0.1 kpc) until no particle is removed.  Inputs are seeded synthetic data.
+
+Arms:
+  default           the GB300 path; `value` = particles/s with inputs resident in HBM,
+                    `e2e` = the same through the C ABI from pinned host buffers.
+  --impl reference  the reference's CPU algorithm on this host (the oracle port: the KDTree
+                    flood fill of fof.py and the float32 potential loop of
+                    particle_subroutines.f90 with OpenMP), timed on bounded samples and
+                    extrapolated to the full snapshot.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "particles/sec FoF+unbinding and pair-interactions/sec, batched FP32 vs FP64 at ≤1e-6"
+WORKLOAD = dict(workload="plummer-2M-500sph-15pc-contaminants", particles=2_000_000, spheres=500, box_mpc=10.0,
+                contaminant_frac=0.15, background_frac=0.10, linking_length_kpc=1.5, min_members=50,
+                softening_kpc=0.1, max_passes=30)
+FLOPS_PER_PAIR = 20          # conventional N-body count (rsqrt counted as several flops)
+MUFU_PAIRS_PER_CLK_SM = 16   # one rsqrt per pair; 16 special-function results / clock / SM
+FOF_BYTES_PER_PARTICLE = 28  # FP64 xyz read once + int32 label written once
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return d.get("hbm_gbs", 6800.0), d.get("sm_max_mhz", 2070.0), "measured"
+    return 6800.0, 2070.0, "fallback"
+
+
+def snapshot(seed):
+    from pyhalma_gb300 import synth
+    w = WORKLOAD
+    return synth.plummer_snapshot(w["particles"], w["spheres"], seed=seed, box_mpc=w["box_mpc"],
+                                  bg_frac=w["background_frac"], contaminant_frac=w["contaminant_frac"])
+
+
+# ---------------------------------------------------------------------------------------
+# clocks during the timed region
+# ---------------------------------------------------------------------------------------
+class ClockSampler:
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        rows = []
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 7:
+                try:
+                    rows.append((float(parts[0]), float(parts[1]), parts[3:7]))
+                except ValueError:
+                    pass
+        os.unlink(self.path)
+        if not rows:
+            return None
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for _, _, r in rows for i, v in enumerate(r) if v.lower() == "active"})
+        return {"sm_mhz": statistics.median(r[0] for r in rows), "sm_max_mhz": max(r[1] for r in rows),
+                "samples": len(rows), "reasons": reasons}
+
+
+# ---------------------------------------------------------------------------------------
+# CPU leg: the reference algorithm on bounded samples of the same snapshot
+# ---------------------------------------------------------------------------------------
+def cpu_measure(s, every=20, ncores=None):
+    """Returns (particles/s estimate for the full snapshot, details).
+
+    FoF: the KDTree flood fill (fof.py:18-79 restated) on every `every`-th sphere plus the same
+    share of background, single-threaded like the reference's serial FoF.  Unbinding: the
+    iterative cut with the float32 potential loop (particle_subroutines.f90:466-514 restated,
+    OpenMP over all cores) on the sample's groups; the full snapshot's pair count is scaled by
+    the sum of squared group sizes (full FoF from the exact C oracle)."""
+    import oracle
+    from oracle import fof_kdtree
+    ncores = ncores or oracle.ncores_default()
+    w = WORKLOAD
+    ll = w["linking_length_kpc"] * 1e-3
+    rng = np.random.default_rng(7)
+    take = (s.sphere >= 0) & (s.sphere % every == 0)
+    take |= (s.sphere < 0) & (rng.random(s.n) < 1.0 / every)
+    idx = np.nonzero(take)[0]
+    t0 = time.perf_counter()
+    groups = fof_kdtree.friends_of_friends_serial(s.x[idx], s.y[idx], s.z[idx], ll)
+    t_fof = time.perf_counter() - t0
+    groups = [np.asarray(g) for g in groups if len(g) >= w["min_members"]]
+    pairs = 0.0
+    G = 4.3e-9
+    eps = w["softening_kpc"] * 1e-3  # the float32 reference loop has no softening; eps only shapes the cut
+    t0 = time.perf_counter()
+    for g in groups:
+        gi = idx[g]
+        bound = np.ones(len(gi), dtype=bool)
+        for _ in range(w["max_passes"]):
+            b = gi[bound]
+            m = s.mass[b]
+            M = m.sum()
+            v = [(m * a[b]).sum() / M for a in (s.vx, s.vy, s.vz)]
+            c = [(m * a[b]).sum() / M for a in (s.x, s.y, s.z)]
+            px, py, pz = (np.float32(a[b] - cc) for a, cc in zip((s.x, s.y, s.z), c))
+            phi = oracle.bf_potential_f32(m, px, py, pz, px, py, pz, ncores=ncores)
+            pairs += float(len(b)) ** 2
+            e = 0.5 * ((s.vx[b] - v[0]) ** 2 + (s.vy[b] - v[1]) ** 2 + (s.vz[b] - v[2]) ** 2) - G * phi
+            drop = e > 0
+            if not drop.any():
+                break
+            sel = np.nonzero(bound)[0]
+            bound[sel[drop]] = False
+    t_unb = time.perf_counter() - t0
+    # full snapshot: pair count scaled by sum N^2 of all groups vs the sample's groups
+    lab = oracle.fof_labels(s.x, s.y, s.z, ll)
+    _, cnt = np.unique(lab[lab >= 0], return_counts=True)
+    full_n2 = float((cnt[cnt >= w["min_members"]].astype(np.float64) ** 2).sum())
+    samp_n2 = float(sum(float(len(g)) ** 2 for g in groups)) or 1.0
+    pairs_full = pairs * full_n2 / samp_n2
+    fof_rate = len(idx) / t_fof
+    pair_rate = pairs / max(t_unb, 1e-9)
+    t_full = s.n / fof_rate + pairs_full / pair_rate
+    return s.n / t_full, dict(t_fof=t_fof, n_fof=len(idx), t_unbind=t_unb, pairs=pairs, pairs_full=pairs_full,
+                              fof_rate=fof_rate, pair_rate=pair_rate, cores=ncores, groups=len(groups))
+
+
+def cpu_sample_text(d, every):
+    return (f"FoF: KDTree flood fill, 1 thread, on every {every}th sphere + 1/{every} of the background "
+            f"({d['n_fof']} particles, {d['t_fof']:.2f} s); unbinding: float32 reference loop with OpenMP on "
+            f"{d['cores']} threads over the sample's {d['groups']} groups ({d['pairs']:.3g} pairs, "
+            f"{d['t_unbind']:.2f} s); extrapolated to the full snapshot ({d['pairs_full']:.3g} pairs)")
+
+
+# ---------------------------------------------------------------------------------------
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def run_reference(args):
+    world, rank, local = dist_env()
+    if rank != 0:
+        return 0
+    import oracle
+    oracle.build()
+    s = snapshot(seed=1)
+    every = 20
+    vals = []
+    for _ in range(args.warmup):
+        cpu_measure(s, every)
+    last = None
+    for _ in range(args.steps):
+        v, last = cpu_measure(s, every)
+        vals.append(v)
+    value = statistics.median(vals)
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "particles/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": s.n / value * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic", "config": dict(WORKLOAD),
+            "cpu_baseline": {"value": value, "unit": "particles/s", "cores": last["cores"], "kind": "port",
+                             "sample": cpu_sample_text(last, every)},
+            "e2e": {"value": value, "unit": "particles/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "pair_interactions_per_s": last["pair_rate"]}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_gpu(args):
+    import torch
+    world, rank, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    from pyhalma_gb300 import _lib
+    from pyhalma_gb300.unbinding import UnbindOptions, find_haloes
+    w = WORKLOAD
+    s = snapshot(seed=1 + rank)
+    n = s.n
+    ll = w["linking_length_kpc"] * 1e-3
+    opt = UnbindOptions(eps=w["softening_kpc"] * 1e-3, max_iter=w["max_passes"], precision="fp32c")
+    host = [np.ascontiguousarray(a) for a in (s.x, s.y, s.z, s.vx, s.vy, s.vz, s.mass)]
+    dev_in = [torch.from_numpy(a).to(dev) for a in host]
+    pinned = [torch.from_numpy(a).pin_memory() for a in host]
+    pinned_np = [t.numpy() for t in pinned]
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)   # > 129 MB L2
+    stream = torch.cuda.current_stream()
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+
+    _lib.set_profiling(True)
+    for _ in range(args.warmup):
+        find_haloes(*dev_in, ll, w["min_members"], options=opt)
+    torch.cuda.synchronize()
+
+    # timed region: inputs resident in HBM, L2 flushed before every step
+    ms, pairs, pair_ms, fof_ms, unbind_ms, passes = [], 0.0, 0.0, [], [], []
+    sampler = ClockSampler(local)
+    sampler.start()
+    launches0 = _lib.launch_count()
+    barrier()
+    wall0 = time.perf_counter()
+    for _ in range(args.steps):
+        flush.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        cat = find_haloes(*dev_in, ll, w["min_members"], options=opt)
+        e1.record(stream)
+        e1.synchronize()
+        ms.append(e0.elapsed_time(e1))
+        st = _lib.profile_stats()
+        fof_ms.append(st["fof_ms"])
+        unbind_ms.append(st["unbind_ms"])
+        for p, t in st["passes"]:
+            if p > 0:
+                pairs += p
+                pair_ms += t
+        passes.append(sum(1 for p, _ in st["passes"] if p > 0))
+    barrier()
+    wall = time.perf_counter() - wall0
+    launches = _lib.launch_count() - launches0
+    clocks = sampler.stop()
+    n_haloes = cat.n_haloes
+    step_ms = statistics.mean(ms)
+    if world > 1:
+        t = torch.tensor([step_ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        step_ms = float(t.item())
+    value = n * world / (step_ms * 1e-3)
+
+    # end to end through the C ABI from pinned host buffers (copies inside the timed region)
+    e2e_ms = []
+    for k in range(args.warmup + args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        hc = find_haloes(*pinned_np, ll, w["min_members"], options=opt)
+        e1.record(stream)
+        e1.synchronize()
+        if k >= args.warmup:
+            e2e_ms.append(e0.elapsed_time(e1))
+    ng = hc.n_haloes
+    nm = int(hc.offsets[-1]) if ng else 0
+    h2d = 7 * 8 * n
+    d2h = 4 * n + n + 8 * (ng + 1) + 4 * nm + 8 * 11 * ng
+    e2e_step = statistics.mean(e2e_ms)
+    if world > 1:
+        t = torch.tensor([e2e_step], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_step = float(t.item())
+
+    # plain FP64 per-halo path on the same snapshot (the comparator of the batched path)
+    fp64 = None
+    if not args.skip_fp64:
+        _lib.set_profiling(False)
+        o64 = UnbindOptions(eps=opt.eps, max_iter=opt.max_iter, precision="fp64")
+        find_haloes(*dev_in, ll, w["min_members"], options=o64)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        find_haloes(*dev_in, ll, w["min_members"], options=o64)
+        e1.record(stream)
+        e1.synchronize()
+        t64 = e0.elapsed_time(e1)
+        fp64 = {"value": n / (t64 * 1e-3), "unit": "particles/s", "ms_per_step": t64,
+                "speedup_fp32c_vs_fp64": t64 / statistics.mean(ms)}
+
+    hbm, sm_max, src = peaks()
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    pair_peak = MUFU_PAIRS_PER_CLK_SM * sms * sm_max * 1e6 * FLOPS_PER_PAIR / 1e12
+    n_pair_launches = sum(passes)
+    achieved = FLOPS_PER_PAIR * pairs / (pair_ms * 1e-3) / 1e12 if pair_ms > 0 else 0.0
+    traffic = None
+    tp = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tp):
+        traffic = json.load(open(tp)).get("ub_pair_kernel_bytes_per_launch")
+    roofline = {"bound": "sfu", "kernel": "ub_pair_kernel", "achieved": achieved, "peak": pair_peak,
+                "unit": "TFLOP/s", "frac": achieved / pair_peak if pair_peak else None, "traffic": traffic,
+                "peak_source": f"{MUFU_PAIRS_PER_CLK_SM} rsqrt/clk/SM x {sms} SMs x {sm_max:.0f} MHz "
+                               f"(sm_max_mhz {src}) x {FLOPS_PER_PAIR} flops/pair",
+                "pairs_per_launch": pairs / max(n_pair_launches, 1), "ms_per_launch": pair_ms / max(n_pair_launches, 1),
+                "launches_timed": n_pair_launches}
+    fof_gbs = FOF_BYTES_PER_PARTICLE * n / (statistics.mean(fof_ms) * 1e-3) / 1e9
+    roofline_fof = {"bound": "hbm", "achieved": fof_gbs, "peak": hbm, "unit": "GB/s", "frac": fof_gbs / hbm,
+                    "traffic": None, "ms": statistics.mean(fof_ms),
+                    "note": f"{FOF_BYTES_PER_PARTICLE} algorithmic B/particle over the whole FoF stage "
+                            f"(bbox, keys, sort, cells, links, labels, groups); hbm_gbs {src}"}
+
+    line = {"metric": METRIC, "value": value, "unit": "particles/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": dict(WORKLOAD, l2="flushed before every step (256 MB device write)", haloes=n_haloes,
+                           passes_mean=statistics.mean(passes), fof_ms=statistics.mean(fof_ms),
+                           unbind_ms=statistics.mean(unbind_ms), reductions="FP64",
+                           parallelism=f"snapshot-per-rank x{world}"),
+            "pair_interactions_per_s": pairs / (sum(ms) * 1e-3) * world,
+            "roofline": roofline, "roofline_fof": roofline_fof,
+            "e2e": {"value": n * world / (e2e_step * 1e-3), "unit": "particles/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h, "ms_per_step": e2e_step},
+            "gpu_launches": launches, "clocks": clocks, "fp64_path": fp64, "wall_s_timed": wall}
+    if rank == 0 and world == 1 and not args.skip_cpu:
+        every = 20
+        v, d = cpu_measure(s, every)
+        line["cpu_baseline"] = {"value": v, "unit": "particles/s", "cores": d["cores"], "kind": "port",
+                                "sample": cpu_sample_text(d, every)}
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--skip-fp64", action="store_true")
+    ap.add_argument("--skip-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    from pyhalma_gb300 import build
+    build.build()
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -62,6 +62,8 @@ SIGNATURES = {
     "halma_last_error": ([], ctypes.c_char_p),
     "halma_release_workspace": ([], ctypes.c_int),
     "halma_kernel_launch_count": ([], ctypes.c_int64),
+    "halma_set_profiling": ([_I32], ctypes.c_int),
+    "halma_profile_stats": ([_P, _I32], ctypes.c_int),
     "halma_fof": ([_I64, _P, _P, _P, _F64, _P, _P, _P], ctypes.c_int),
     "halma_fof_groups": ([_I64, _P, _I32, _P, _P, _P, _P], ctypes.c_int),
     "halma_bf_potential_f32": ([_I64, _P, _P, _P, _P, _I64, _P, _P, _P, _P, _I32, _F64, _P], ctypes.c_int),
@@ -106,6 +108,20 @@ def check(status, where):
 
 def launch_count() -> int:
     return int(lib().halma_kernel_launch_count())
+
+
+def set_profiling(on: bool):
+    lib().halma_set_profiling(1 if on else 0)
+
+
+def profile_stats():
+    """Last call's measurements: dict(fof_ms, unbind_ms, passes=[(pairs, pair_kernel_ms), ...])."""
+    n = lib().halma_profile_stats(None, 0)
+    buf = np.zeros(max(n, 3))
+    lib().halma_profile_stats(buf.ctypes.data_as(ctypes.c_void_p), len(buf))
+    k = int(buf[2])
+    passes = [(float(buf[3 + 2 * i]), float(buf[4 + 2 * i])) for i in range(k)]
+    return {"fof_ms": float(buf[0]), "unbind_ms": float(buf[1]), "passes": passes}
 
 
 # ---------------------------------------------------------------------------------------

@@ -100,9 +100,16 @@ extern "C" int halma_find_haloes(int64_t n, const double *x, const double *y, co
     unsigned char *bs = at<unsigned char>(buf.p, o_bs), *dbnd = at<unsigned char>(buf.p, o_bnd);
     double *dhalo = at<double>(buf.p, o_halo);
 
+    Profile &prof = profile();
+    cudaEvent_t ev[4] = {};
+    if (prof.enabled) {
+        for (auto &e : ev) HALMA_CUDA(cudaEventCreate(&e));
+        HALMA_CUDA(cudaEventRecord(ev[0], st));
+    }
     HALMA_TRY(fof_device((int)n, dx, dy, dz, linking_length, dlab, nullptr, st));
     int64_t ng = 0, nm = 0;
     HALMA_TRY(fof_groups_device((int)n, dlab, std::max(min_members, 1), doff, dmem, &ng, &nm, st));
+    if (prof.enabled) HALMA_CUDA(cudaEventRecord(ev[1], st));
     *n_haloes = ng;
     HALMA_CUDA(cudaMemsetAsync(dbnd, 0, n, st));
     if (ng > 0) {
@@ -111,9 +118,20 @@ extern "C" int halma_find_haloes(int64_t n, const double *x, const double *y, co
         std::vector<int64_t> h_off(ng + 1);
         HALMA_CUDA(cudaMemcpyAsync(h_off.data(), doff, 8ull * (ng + 1), cudaMemcpyDeviceToHost, st));
         HALMA_CUDA(cudaStreamSynchronize(st));
+        if (prof.enabled) HALMA_CUDA(cudaEventRecord(ev[2], st));
         HALMA_TRY(unbind_device(nm, (int)ng, doff, h_off.data(), g7, g7 + nm, g7 + 2 * nm, g7 + 3 * nm, g7 + 4 * nm,
                                 g7 + 5 * nm, g7 + 6 * nm, p, bs, nullptr, dhalo, st));
+        if (prof.enabled) HALMA_CUDA(cudaEventRecord(ev[3], st));
         HALMA_LAUNCH(scatter_bound_kernel, g, 256, 0, st, nm, dmem, bs, dbnd);
+    }
+    if (prof.enabled) {
+        HALMA_CUDA(cudaStreamSynchronize(st));
+        float a = 0.f, b = 0.f;
+        HALMA_CUDA(cudaEventElapsedTime(&a, ev[0], ev[1]));
+        if (ng > 0) HALMA_CUDA(cudaEventElapsedTime(&b, ev[2], ev[3]));
+        prof.fof_ms = a;
+        prof.unbind_ms = b;
+        for (auto &e : ev) cudaEventDestroy(e);
     }
     // outputs (host or device)
     auto put = [&](void *user, const void *dev, size_t bytes) -> int {
@@ -132,4 +150,23 @@ extern "C" int halma_find_haloes(int64_t n, const double *x, const double *y, co
     HALMA_TRY(put(halo_out, dhalo, 8ull * HALMA_UB_NFIELDS * ng));
     HALMA_CUDA(cudaStreamSynchronize(st));
     return HALMA_OK;
+}
+
+extern "C" int halma_set_profiling(int32_t on) {
+    std::lock_guard<std::mutex> guard(api_mutex());
+    profile().enabled = on != 0;
+    return HALMA_OK;
+}
+
+extern "C" int halma_profile_stats(double *out, int32_t cap) {
+    std::lock_guard<std::mutex> guard(api_mutex());
+    const Profile &p = profile();
+    std::vector<double> v = {p.fof_ms, p.unbind_ms, (double)p.passes.size()};
+    for (const auto &q : p.passes) {
+        v.push_back(q.pairs);
+        v.push_back(q.ms);
+    }
+    if (out)
+        for (int i = 0; i < cap && i < (int)v.size(); ++i) out[i] = v[i];
+    return (int)v.size();
 }

@@ -4,6 +4,7 @@
 // One block per halo for the sums; the half-mass radius needs the members in increasing
 // distance from the centre, obtained with two stable radix sorts over all particles (by the
 // FP64 distance bits, then by halo id), after which each halo walks its own segment.
+#include <limits.h>
 #include <math.h>
 
 #include "common.cuh"
@@ -141,7 +142,7 @@ __global__ void __launch_bounds__(256) red_r05_kernel(const int64_t *__restrict_
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
     if (threadIdx.x == 0) {
         running = 0.0;
-        first = -1;
+        first = LLONG_MAX;   // atomicMin target: no crossing yet
     }
     __syncthreads();
     const double half = 0.5 * r.mref;
@@ -167,7 +168,7 @@ __global__ void __launch_bounds__(256) red_r05_kernel(const int64_t *__restrict_
             running += t;
         }
         __syncthreads();
-        if (first >= 0) break;
+        if (first != LLONG_MAX) break;
     }
     __shared__ double r05s;
     if (threadIdx.x == 0) {
@@ -175,7 +176,7 @@ __global__ void __launch_bounds__(256) red_r05_kernel(const int64_t *__restrict_
         if (given) {
             r05 = r.r05;
         } else if (nmem > 0) {
-            const long long f = first;
+            const long long f = first == LLONG_MAX ? -1 : first;
             if (f > 0) r05 = dist[order[b + f - 1]];
             else if (f == 0) r05 = dist[order[b]];
             else r05 = dist[order[b + nmem - 1]];

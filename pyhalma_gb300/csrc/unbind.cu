@@ -164,20 +164,30 @@ __global__ void __launch_bounds__(256) ub_pack_kernel(const int64_t *__restrict_
 }
 
 // Work list for the pair kernel: haloes in decreasing initial size, tiles of 32*T targets.
+// Also records the pass's pair count (sum of nb^2 over active haloes) in pairs_out.
 __global__ void __launch_bounds__(1024) ub_items_kernel(int nh, const int *__restrict__ order, const HaloState *hs,
                                                         int tt, int2 *__restrict__ items, int *__restrict__ nitems,
-                                                        int *__restrict__ counter) {
+                                                        int *__restrict__ counter,
+                                                        unsigned long long *__restrict__ pairs_out) {
     __shared__ int wsum[32];
     __shared__ int base;
+    __shared__ unsigned long long pairs;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    if (threadIdx.x == 0) base = 0;
+    if (threadIdx.x == 0) {
+        base = 0;
+        pairs = 0;
+    }
     __syncthreads();
     for (int h0 = 0; h0 < nh; h0 += blockDim.x) {
         const int q = h0 + threadIdx.x;
         int h = -1, cnt = 0;
         if (q < nh) {
             h = order[q];
-            if (hs[h].active) cnt = (hs[h].nb + tt - 1) / tt;
+            if (hs[h].active) {
+                const int nb = hs[h].nb;
+                cnt = (nb + tt - 1) / tt;
+                if (nb > 0) atomicAdd(&pairs, (unsigned long long)nb * (unsigned long long)nb);
+            }
         }
         int incl = cnt;
         for (int o = 1; o < 32; o <<= 1) {
@@ -201,6 +211,7 @@ __global__ void __launch_bounds__(1024) ub_items_kernel(int nh, const int *__res
     if (threadIdx.x == 0) {
         *nitems = base;
         *counter = 0;
+        if (pairs_out) *pairs_out = pairs;
     }
 }
 
@@ -361,7 +372,21 @@ GraphCache &graph_cache() {
 
 }  // namespace
 
-int unbind_targets_per_item() { return 32 * 4; }
+Profile &profile() {
+    static Profile p;
+    return p;
+}
+
+int Profile::ensure_events(int k) {
+    while ((int)ev0.size() < k) {
+        cudaEvent_t a, b;
+        HALMA_CUDA(cudaEventCreate(&a));
+        HALMA_CUDA(cudaEventCreate(&b));
+        ev0.push_back(a);
+        ev1.push_back(b);
+    }
+    return HALMA_OK;
+}
 
 // Device-array implementation shared by halma_unbind_batched and the pipeline.
 int unbind_device(int64_t n, int nh, const int64_t *d_off, const int64_t *h_off, const double *x, const double *y,
@@ -395,6 +420,7 @@ int unbind_device(int64_t n, int nh, const int64_t *d_off, const int64_t *h_off,
     const size_t o_phi = L.add(sizeof(double) * P);
     const size_t o_items = L.add(sizeof(int2) * std::max<int64_t>(max_items, 1));
     const size_t o_cnt = L.add(64);
+    const size_t o_pairs = L.add(sizeof(unsigned long long) * p.max_iter);
     const size_t o_off = d_off ? 0 : L.add(sizeof(int64_t) * (nh + 1));
     void *base = nullptr;
     HALMA_TRY(workspace(L.total, &base, st));
@@ -405,6 +431,13 @@ int unbind_device(int64_t n, int nh, const int64_t *d_off, const int64_t *h_off,
     auto *phi = at<double>(base, o_phi);
     auto *items = at<int2>(base, o_items);
     int *cnt = at<int>(base, o_cnt);   // [0] nitems [1] counter
+    auto *dpairs = at<unsigned long long>(base, o_pairs);
+    Profile &prof = profile();
+    const bool profiling = prof.enabled;
+    if (profiling) {
+        HALMA_TRY(prof.ensure_events(p.max_iter));
+        HALMA_CUDA(cudaMemsetAsync(dpairs, 0, sizeof(unsigned long long) * p.max_iter, st));
+    }
     const int64_t *off = d_off;
     if (!d_off) {
         int64_t *o = at<int64_t>(base, o_off);
@@ -428,8 +461,11 @@ int unbind_device(int64_t n, int nh, const int64_t *d_off, const int64_t *h_off,
             for (int it = 0; it < p.max_iter; ++it) {
                 HALMA_LAUNCH(ub_reduce_kernel, nh, 256, 0, rs, off, x, y, z, vx, vy, vz, m, bound, hs, 0);
                 HALMA_LAUNCH(ub_pack_kernel<float4>, nh, 256, 0, rs, off, dpoff, x, y, z, m, bound, hs, pk, pidx);
-                HALMA_LAUNCH(ub_items_kernel, 1, 1024, 0, rs, nh, dorder, hs, TT, items, cnt, cnt + 1);
+                HALMA_LAUNCH(ub_items_kernel, 1, 1024, 0, rs, nh, dorder, hs, TT, items, cnt, cnt + 1,
+                             profiling ? dpairs + it : nullptr);
+                if (profiling) HALMA_CUDA(cudaEventRecord(prof.ev0[it], rs));
                 HALMA_LAUNCH(ub_pair_kernel<T>, pgrid, 256, 0, rs, pk, dpoff, hs, items, cnt, cnt + 1, eps2, phi);
+                if (profiling) HALMA_CUDA(cudaEventRecord(prof.ev1[it], rs));
                 HALMA_LAUNCH(ub_energy_kernel, nh, 256, 0, rs, dpoff, pidx, phi, vx, vy, vz, m, gfac, bound, phi_out,
                              hs);
             }
@@ -447,6 +483,8 @@ int unbind_device(int64_t n, int nh, const int64_t *d_off, const int64_t *h_off,
             key.push_back((uintptr_t)gb);
             key.insert(key.end(), poff.begin(), poff.end());
             key.push_back((uintptr_t)current_device());
+            key.push_back((uintptr_t)profiling);
+            key.push_back((uintptr_t)dpairs);
             GraphCache &gc = graph_cache();
             if (!gc.exec || gc.key != key) {
                 if (gc.exec) {
@@ -482,6 +520,18 @@ int unbind_device(int64_t n, int nh, const int64_t *d_off, const int64_t *h_off,
         }
         // final bound mass, centre and bulk velocity over the final bound sets
         HALMA_LAUNCH(ub_reduce_kernel, nh, 256, 0, st, off, x, y, z, vx, vy, vz, m, bound, hs, 1);
+        if (profiling) {
+            std::vector<unsigned long long> hp(p.max_iter);
+            HALMA_CUDA(cudaMemcpyAsync(hp.data(), dpairs, sizeof(unsigned long long) * p.max_iter,
+                                       cudaMemcpyDeviceToHost, st));
+            HALMA_CUDA(cudaStreamSynchronize(st));
+            prof.passes.clear();
+            for (int it = 0; it < p.max_iter; ++it) {
+                float ms = 0.f;
+                HALMA_CUDA(cudaEventElapsedTime(&ms, prof.ev0[it], prof.ev1[it]));
+                prof.passes.push_back({(double)hp[it], (double)ms});
+            }
+        }
     } else {
         // plain FP64 path: per pass, one pair launch per active halo, host checks convergence
         auto *pk = at<double4>(base, o_pk);

@@ -4,6 +4,21 @@
 
 namespace halma {
 
+// Optional measurement state (halma_set_profiling): CUDA events recorded on the launching
+// stream around every pair-kernel launch (captured into the pass graph as event nodes) and
+// the pair count of each pass, read back at the end of the call.
+struct Profile {
+    bool enabled = false;
+    std::vector<cudaEvent_t> ev0, ev1;
+    struct Pass {
+        double pairs, ms;
+    };
+    std::vector<Pass> passes;
+    double fof_ms = 0, unbind_ms = 0;
+    int ensure_events(int k);
+};
+Profile &profile();
+
 int fof_device(int n, const double *x, const double *y, const double *z, double ll, int *labels,
                int64_t *n_groups, cudaStream_t st);
 int fof_groups_device(int n, const int *labels, int minp, int64_t *offsets, int *members,
