@@ -97,7 +97,9 @@ __global__ void __launch_bounds__(256) red_sums_kernel(const int64_t *__restrict
     for (int64_t i = b + threadIdx.x; i < e; i += blockDim.x) {
         const bool in = !mask || mask[i];
         const double dx = cx - x[i], dy = cy - y[i], dz = cz - z[i];
-        const double d = sqrt(dx * dx + dy * dy + dz * dz);
+        // (dx**2 + dy**2 + dz**2)**0.5 as the reference evaluates it (halo_properties.py:104-107),
+        // each operation rounded on its own so that d < R05 splits members the same way
+        const double d = sqrt(__dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz)));
         dist[i] = d;
         if (in) rmax = fmax(rmax, d);
         // excluded particles sort after every member (+inf)

@@ -463,9 +463,10 @@ int unbind_device(int64_t n, int nh, const int64_t *d_off, const int64_t *h_off,
                 HALMA_LAUNCH(ub_pack_kernel<float4>, nh, 256, 0, rs, off, dpoff, x, y, z, m, bound, hs, pk, pidx);
                 HALMA_LAUNCH(ub_items_kernel, 1, 1024, 0, rs, nh, dorder, hs, TT, items, cnt, cnt + 1,
                              profiling ? dpairs + it : nullptr);
-                if (profiling) HALMA_CUDA(cudaEventRecord(prof.ev0[it], rs));
+                // External: captured as an event-record node, so the replay records it
+                if (profiling) HALMA_CUDA(cudaEventRecordWithFlags(prof.ev0[it], rs, cudaEventRecordExternal));
                 HALMA_LAUNCH(ub_pair_kernel<T>, pgrid, 256, 0, rs, pk, dpoff, hs, items, cnt, cnt + 1, eps2, phi);
-                if (profiling) HALMA_CUDA(cudaEventRecord(prof.ev1[it], rs));
+                if (profiling) HALMA_CUDA(cudaEventRecordWithFlags(prof.ev1[it], rs, cudaEventRecordExternal));
                 HALMA_LAUNCH(ub_energy_kernel, nh, 256, 0, rs, dpoff, pidx, phi, vx, vy, vz, m, gfac, bound, phi_out,
                              hs);
             }

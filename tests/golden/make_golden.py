@@ -16,8 +16,8 @@ Fixtures written to tests/golden/ (all seeds fixed):
 
 * fof_cases.npz   — reference ``fof.friends_of_friends_serial`` on small synthetic and
   adversarial inputs (positions stored exactly; canonical labels = min index, -1 alone);
-* fof_config1.npz — the same on the 1e5-particle Plummer snapshot; inputs are regenerated
-  from the seed by ``pyhalma_gb300.synth`` and checked against the stored SHA-256;
+* fof_config1.npz — the same on the 1e5-particle Plummer snapshot (positions stored; the
+  SHA-256 of the positions regenerated from the seed here is stored as well);
 * predicate.npz   — adversarial two-point pairs at nextafter distances and whether the
   reference's KDTree links them (pins the pair predicate);
 * halo_props.npz  — reference reductions (halo_properties.py) on a few haloes;
@@ -143,7 +143,9 @@ def fof_config1(fof):
     s = synth.plummer_snapshot(100_000, 50, seed=0, box_mpc=10.0)
     groups = fof.friends_of_friends_serial(s.x, s.y, s.z, 0.0015)
     lab = oracle.groups_to_labels(groups, s.n)
-    np.savez_compressed(os.path.join(HERE, "fof_config1.npz"), labels=lab,
+    # positions are stored too: NumPy's transcendental kernels differ across platforms, so
+    # another machine may regenerate a slightly different snapshot from the same seed
+    np.savez_compressed(os.path.join(HERE, "fof_config1.npz"), labels=lab, x=s.x, y=s.y, z=s.z,
                         sha256=np.array(sha(s.x, s.y, s.z)), ll=np.float64(0.0015),
                         n=np.int64(s.n), seed=np.int64(0), n_spheres=np.int64(50),
                         box_mpc=np.float64(10.0), ngroups=np.int64(len(groups)))

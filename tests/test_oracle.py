@@ -62,10 +62,15 @@ def _config1(golden):
 
 
 def test_fof_oracle_matches_reference_config1(golden):
-    s, c = _config1(golden)
-    lab = oracle.fof_labels(s.x, s.y, s.z, float(c["ll"]))
+    c = golden("fof_config1.npz")
+    lab = oracle.fof_labels(c["x"], c["y"], c["z"], float(c["ll"]))
     assert np.array_equal(lab, c["labels"])
     assert len(oracle.labels_to_groups(lab)) == int(c["ngroups"])
+
+
+def test_config1_generator_reproduces_stored_positions(golden):
+    s, c = _config1(golden)     # skips where NumPy's transcendental kernels differ
+    assert np.array_equal(s.x, c["x"]) and np.array_equal(s.z, c["z"])
 
 
 def test_potential_oracle_known_answers():
