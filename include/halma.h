@@ -187,6 +187,13 @@ enum {
     HALMA_UB_NFIELDS
 };
 
+/* Tile shapes of the FP32C pair kernel per halo size class (no reference counterpart):
+ * a halo with nb bound particles uses T = t_per_class[c] targets per lane (1, 2, 4 or 8) for
+ * the first class c with nb <= upper[c] (increasing bounds, at most 8 classes).  Written by
+ * the autotuner (pyhalma_gb300.autotune); the default is {32:1, 64:2, inf:4}. */
+int halma_set_tile_table(int32_t n_classes, const int32_t *upper, const int32_t *t_per_class);
+int halma_get_tile_table(int32_t *n_classes, int32_t *upper, int32_t *t_per_class);
+
 /* Particles in halo-contiguous order (CSR offsets, n_haloes+1 entries).  Every pass
  * recomputes each halo's FP64 bound mass, centre and bulk velocity, the potential of the
  * bound particles due to the bound particles (self pair excluded), and removes particles

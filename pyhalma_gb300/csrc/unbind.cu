@@ -165,9 +165,15 @@ __global__ void __launch_bounds__(256) ub_pack_kernel(const int64_t *__restrict_
 
 // Work list for the pair kernel: haloes in decreasing initial size, tiles of 32*T targets.
 // Also records the pass's pair count (sum of nb^2 over active haloes) in pairs_out.
+__device__ __forceinline__ int tile_t_for(const TileTable &tab, int nb) {
+    for (int c = 0; c < tab.n; ++c)
+        if (nb <= tab.upper[c]) return tab.t[c];
+    return 4;
+}
+
 __global__ void __launch_bounds__(1024) ub_items_kernel(int nh, const int *__restrict__ order, const HaloState *hs,
-                                                        int tt, int2 *__restrict__ items, int *__restrict__ nitems,
-                                                        int *__restrict__ counter,
+                                                        TileTable tab, int4 *__restrict__ items,
+                                                        int *__restrict__ nitems, int *__restrict__ counter,
                                                         unsigned long long *__restrict__ pairs_out) {
     __shared__ int wsum[32];
     __shared__ int base;
@@ -180,12 +186,13 @@ __global__ void __launch_bounds__(1024) ub_items_kernel(int nh, const int *__res
     __syncthreads();
     for (int h0 = 0; h0 < nh; h0 += blockDim.x) {
         const int q = h0 + threadIdx.x;
-        int h = -1, cnt = 0;
+        int h = -1, cnt = 0, T = 4;
         if (q < nh) {
             h = order[q];
             if (hs[h].active) {
                 const int nb = hs[h].nb;
-                cnt = (nb + tt - 1) / tt;
+                T = tile_t_for(tab, nb);
+                cnt = (nb + 32 * T - 1) / (32 * T);
                 if (nb > 0) atomicAdd(&pairs, (unsigned long long)nb * (unsigned long long)nb);
             }
         }
@@ -199,7 +206,7 @@ __global__ void __launch_bounds__(1024) ub_items_kernel(int nh, const int *__res
         int pre = base;
         for (int k = 0; k < w; ++k) pre += wsum[k];
         const int start = pre + incl - cnt;
-        for (int t = 0; t < cnt; ++t) items[start + t] = make_int2(h, t);
+        for (int t = 0; t < cnt; ++t) items[start + t] = make_int4(h, t, T, 0);
         __syncthreads();
         if (threadIdx.x == 0) {
             int tot = 0;
@@ -215,24 +222,11 @@ __global__ void __launch_bounds__(1024) ub_items_kernel(int nh, const int *__res
     }
 }
 
-// Persistent all-pairs kernel over the work list (FP32 pair terms, compensated sums).
+// One work item: 32*T target slots of one halo against all of its source slots.
 template <int T>
-__global__ void __launch_bounds__(256) ub_pair_kernel(const float4 *__restrict__ pk, const int64_t *__restrict__ poff,
-                                                      const HaloState *__restrict__ hs, const int2 *__restrict__ items,
-                                                      const int *__restrict__ nitems_p, int *counter, float eps2,
-                                                      double *__restrict__ phi) {
-    __shared__ float4 buf[kUbWarps][32];
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const int nitems = *nitems_p;
-    for (;;) {
-        int item = 0;
-        if (lane == 0) item = atomicAdd(counter, 1);
-        item = __shfl_sync(0xffffffffu, item, 0);
-        if (item >= nitems) break;
-        const int2 it = items[item];
-        const int h = it.x, tile = it.y;
-        const int64_t base = poff[h];
-        const int nb = hs[h].nb;
+__device__ __forceinline__ void pair_item(const float4 *__restrict__ pk, int64_t base, int nb, int tile, float eps2,
+                                          double *__restrict__ phi, float4 *buf, int lane) {
+    {
         const int nchunk = (nb + 31) >> 5;
         float px[T], py[T], pz[T], sum[T], comp[T];
 #pragma unroll
@@ -246,7 +240,7 @@ __global__ void __launch_bounds__(256) ub_pair_kernel(const float4 *__restrict__
         float4 nxt = pk[base + lane];
         for (int c = 0; c < nchunk; ++c) {
             __syncwarp();
-            buf[w][lane] = nxt;
+            buf[lane] = nxt;
             __syncwarp();
             if (c + 1 < nchunk) nxt = pk[base + (int64_t)(c + 1) * 32 + lane];
             float part[T];
@@ -255,7 +249,7 @@ __global__ void __launch_bounds__(256) ub_pair_kernel(const float4 *__restrict__
             const int ts = c - self0;
             if (ts >= 0 && ts < T) {
                 for (int k = 0; k < 32; ++k) {
-                    const float4 q = buf[w][k];
+                    const float4 q = buf[k];
 #pragma unroll
                     for (int t = 0; t < T; ++t) {
                         const float v = pair_term_fast(q, px[t], py[t], pz[t], eps2, part[t]);
@@ -265,7 +259,7 @@ __global__ void __launch_bounds__(256) ub_pair_kernel(const float4 *__restrict__
             } else {
 #pragma unroll 8
                 for (int k = 0; k < 32; ++k) {
-                    const float4 q = buf[w][k];
+                    const float4 q = buf[k];
 #pragma unroll
                     for (int t = 0; t < T; ++t) part[t] = pair_term_fast(q, px[t], py[t], pz[t], eps2, part[t]);
                 }
@@ -277,6 +271,33 @@ __global__ void __launch_bounds__(256) ub_pair_kernel(const float4 *__restrict__
         for (int t = 0; t < T; ++t) {
             const int r = tile * 32 * T + t * 32 + lane;
             if (r < nb) phi[base + r] = (double)sum[t] + (double)comp[t];
+        }
+    }
+}
+
+// Persistent all-pairs kernel over the work list (FP32 pair terms, compensated sums).  Each
+// item carries its tile shape T (targets per lane) chosen per halo size class.
+__global__ void __launch_bounds__(256) ub_pair_kernel(const float4 *__restrict__ pk, const int64_t *__restrict__ poff,
+                                                      const HaloState *__restrict__ hs, const int4 *__restrict__ items,
+                                                      const int *__restrict__ nitems_p, int *counter, float eps2,
+                                                      double *__restrict__ phi) {
+    __shared__ float4 buf[kUbWarps][32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int nitems = *nitems_p;
+    for (;;) {
+        int item = 0;
+        if (lane == 0) item = atomicAdd(counter, 1);
+        item = __shfl_sync(0xffffffffu, item, 0);
+        if (item >= nitems) break;
+        const int4 it = items[item];
+        const int h = it.x, tile = it.y;
+        const int64_t base = poff[h];
+        const int nb = hs[h].nb;
+        switch (it.z) {
+            case 1: pair_item<1>(pk, base, nb, tile, eps2, phi, buf[w], lane); break;
+            case 2: pair_item<2>(pk, base, nb, tile, eps2, phi, buf[w], lane); break;
+            case 8: pair_item<8>(pk, base, nb, tile, eps2, phi, buf[w], lane); break;
+            default: pair_item<4>(pk, base, nb, tile, eps2, phi, buf[w], lane); break;
         }
     }
 }
@@ -377,6 +398,15 @@ Profile &profile() {
     return p;
 }
 
+static TileTable &tile_table_ref() {
+    // default until the autotuner's table is loaded: 1 chunk of targets for haloes of up to
+    // 32 bound particles, 2 up to 64, 4 above
+    static TileTable t = {3, {32, 64, 0x7fffffff}, {1, 2, 4}};
+    return t;
+}
+
+TileTable tile_table() { return tile_table_ref(); }
+
 int Profile::ensure_events(int k) {
     while ((int)ev0.size() < k) {
         cudaEvent_t a, b;
@@ -393,9 +423,9 @@ int unbind_device(int64_t n, int nh, const int64_t *d_off, const int64_t *h_off,
                   const double *z, const double *vx, const double *vy, const double *vz, const double *m,
                   const halma_unbind_params &p, unsigned char *bound, double *phi_out, double *halo_out,
                   cudaStream_t st) {
-    constexpr int T = 4;
-    const int TT = 32 * T;
-    // host-side plan: padded slot offsets, work-list capacity, size order
+    const TileTable tab = tile_table();
+    // host-side plan: padded slot offsets, work-list capacity (one item per 32 slots at
+    // most, the smallest tile), size order
     std::vector<int64_t> poff(nh + 1);
     std::vector<int> order(nh);
     int64_t max_items = 0;
@@ -403,7 +433,7 @@ int unbind_device(int64_t n, int nh, const int64_t *d_off, const int64_t *h_off,
     for (int h = 0; h < nh; ++h) {
         const int64_t c = h_off[h + 1] - h_off[h];
         poff[h + 1] = poff[h] + ((c + 31) / 32) * 32;
-        max_items += (c + TT - 1) / TT;
+        max_items += (c + 31) / 32;
     }
     std::iota(order.begin(), order.end(), 0);
     std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
@@ -418,7 +448,7 @@ int unbind_device(int64_t n, int nh, const int64_t *d_off, const int64_t *h_off,
     const size_t o_pk = L.add((f64 ? sizeof(double4) : sizeof(float4)) * P);
     const size_t o_pidx = L.add(sizeof(int) * P);
     const size_t o_phi = L.add(sizeof(double) * P);
-    const size_t o_items = L.add(sizeof(int2) * std::max<int64_t>(max_items, 1));
+    const size_t o_items = L.add(sizeof(int4) * std::max<int64_t>(max_items, 1));
     const size_t o_cnt = L.add(64);
     const size_t o_pairs = L.add(sizeof(unsigned long long) * p.max_iter);
     const size_t o_off = d_off ? 0 : L.add(sizeof(int64_t) * (nh + 1));
@@ -429,7 +459,7 @@ int unbind_device(int64_t n, int nh, const int64_t *d_off, const int64_t *h_off,
     auto *dorder = at<int>(base, o_order);
     auto *pidx = at<int>(base, o_pidx);
     auto *phi = at<double>(base, o_phi);
-    auto *items = at<int2>(base, o_items);
+    auto *items = at<int4>(base, o_items);
     int *cnt = at<int>(base, o_cnt);   // [0] nitems [1] counter
     auto *dpairs = at<unsigned long long>(base, o_pairs);
     Profile &prof = profile();
@@ -455,17 +485,17 @@ int unbind_device(int64_t n, int nh, const int64_t *d_off, const int64_t *h_off,
     if (!f64) {
         auto *pk = at<float4>(base, o_pk);
         int bps = 0;
-        HALMA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, ub_pair_kernel<T>, 256, 0));
+        HALMA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, ub_pair_kernel, 256, 0));
         const int pgrid = device_sm_count() * std::max(bps, 1);
         auto record = [&](cudaStream_t rs) -> int {
             for (int it = 0; it < p.max_iter; ++it) {
                 HALMA_LAUNCH(ub_reduce_kernel, nh, 256, 0, rs, off, x, y, z, vx, vy, vz, m, bound, hs, 0);
                 HALMA_LAUNCH(ub_pack_kernel<float4>, nh, 256, 0, rs, off, dpoff, x, y, z, m, bound, hs, pk, pidx);
-                HALMA_LAUNCH(ub_items_kernel, 1, 1024, 0, rs, nh, dorder, hs, TT, items, cnt, cnt + 1,
+                HALMA_LAUNCH(ub_items_kernel, 1, 1024, 0, rs, nh, dorder, hs, tab, items, cnt, cnt + 1,
                              profiling ? dpairs + it : nullptr);
                 // External: captured as an event-record node, so the replay records it
                 if (profiling) HALMA_CUDA(cudaEventRecordWithFlags(prof.ev0[it], rs, cudaEventRecordExternal));
-                HALMA_LAUNCH(ub_pair_kernel<T>, pgrid, 256, 0, rs, pk, dpoff, hs, items, cnt, cnt + 1, eps2, phi);
+                HALMA_LAUNCH(ub_pair_kernel, pgrid, 256, 0, rs, pk, dpoff, hs, items, cnt, cnt + 1, eps2, phi);
                 if (profiling) HALMA_CUDA(cudaEventRecordWithFlags(prof.ev1[it], rs, cudaEventRecordExternal));
                 HALMA_LAUNCH(ub_energy_kernel, nh, 256, 0, rs, dpoff, pidx, phi, vx, vy, vz, m, gfac, bound, phi_out,
                              hs);
@@ -486,6 +516,11 @@ int unbind_device(int64_t n, int nh, const int64_t *d_off, const int64_t *h_off,
             key.push_back((uintptr_t)current_device());
             key.push_back((uintptr_t)profiling);
             key.push_back((uintptr_t)dpairs);
+            key.push_back((uintptr_t)tab.n);
+            for (int c = 0; c < tab.n; ++c) {
+                key.push_back((uintptr_t)tab.upper[c]);
+                key.push_back((uintptr_t)tab.t[c]);
+            }
             GraphCache &gc = graph_cache();
             if (!gc.exec || gc.key != key) {
                 if (gc.exec) {
@@ -624,4 +659,34 @@ extern "C" int halma_unbind_batched(int64_t n, int64_t n_haloes, const int64_t *
         cudaStreamSynchronize(st);
     }
     return s;
+}
+
+extern "C" int halma_set_tile_table(int32_t n_classes, const int32_t *upper, const int32_t *t_per_class) {
+    if (n_classes < 1 || n_classes > kMaxTileClasses || !upper || !t_per_class)
+        return fail(HALMA_ERR_INVALID, "tile table needs 1..%d classes", kMaxTileClasses);
+    TileTable t{};
+    t.n = n_classes;
+    for (int c = 0; c < n_classes; ++c) {
+        const int v = t_per_class[c];
+        if (v != 1 && v != 2 && v != 4 && v != 8) return fail(HALMA_ERR_INVALID, "tile shape must be 1, 2, 4 or 8");
+        if (upper[c] < 1 || (c > 0 && upper[c] <= upper[c - 1]))
+            return fail(HALMA_ERR_INVALID, "class bounds must be positive and increasing");
+        t.upper[c] = upper[c];
+        t.t[c] = v;
+    }
+    std::lock_guard<std::mutex> guard(api_mutex());
+    tile_table_ref() = t;
+    return HALMA_OK;
+}
+
+extern "C" int halma_get_tile_table(int32_t *n_classes, int32_t *upper, int32_t *t_per_class) {
+    if (!n_classes || !upper || !t_per_class) return fail(HALMA_ERR_INVALID, "null pointer");
+    std::lock_guard<std::mutex> guard(api_mutex());
+    const TileTable &t = tile_table_ref();
+    *n_classes = t.n;
+    for (int c = 0; c < t.n; ++c) {
+        upper[c] = t.upper[c];
+        t_per_class[c] = t.t[c];
+    }
+    return HALMA_OK;
 }

@@ -19,6 +19,16 @@ struct Profile {
 };
 Profile &profile();
 
+// Tile shape per halo size class for the batched pair kernel: a halo with nb bound
+// particles uses T = t[c] targets per lane for the first class c with nb <= upper[c].
+constexpr int kMaxTileClasses = 8;
+struct TileTable {
+    int n;
+    int upper[kMaxTileClasses];
+    int t[kMaxTileClasses];
+};
+TileTable tile_table();
+
 int fof_device(int n, const double *x, const double *y, const double *z, double ll, int *labels,
                int64_t *n_groups, cudaStream_t st);
 int fof_groups_device(int n, const int *labels, int minp, int64_t *offsets, int *members,

@@ -26,6 +26,16 @@ from . import _lib
 
 G_MPC = 4.3e-9   # (km/s)^2 Mpc / Msun, halo_gas.py:459-460
 _PREC = {"fp32c": _lib.UNBIND_FP32C, "fp64": _lib.UNBIND_FP64}
+_table_loaded = False
+
+
+def _ensure_tile_table():
+    """Loads the autotuner's saved tile table once per process (if one was saved)."""
+    global _table_loaded
+    if not _table_loaded:
+        from . import autotune
+        autotune.apply()
+        _table_loaded = True
 
 
 @dataclass
@@ -48,6 +58,7 @@ def unbind_batched(offsets, x, y, z, vx, vy, vz, m, options: UnbindOptions | Non
     Arrays are host NumPy (copied in and out) or CUDA torch tensors (used in place).
     """
     opt = options or UnbindOptions(**kw)
+    _ensure_tile_table()
     dev = _lib._is_torch(x)
     if dev:
         n = int(x.shape[0])
@@ -87,6 +98,7 @@ def find_haloes(st_x, st_y, st_z, st_vx, st_vy, st_vz, st_mass, linking_length, 
                 options: UnbindOptions | None = None, **kw):
     """FoF (fof.py:18-79) + good_groups (pyHALMA.py:148-149) + batched unbinding, one call."""
     opt = options or UnbindOptions(**kw)
+    _ensure_tile_table()
     dev = _lib._is_torch(st_x)
     if dev:
         arrs = (st_x, st_y, st_z, st_vx, st_vy, st_vz, st_mass)

@@ -81,6 +81,20 @@ def test_python_layer_raises_value_error():
         fof.friends_of_friends(np.zeros((3, 2)), 1.0)
 
 
+def test_tile_table_validation_and_roundtrip():
+    from pyhalma_gb300 import autotune
+    saved = autotune.get_table()
+    try:
+        autotune.set_table([100, 5000, 2 ** 31 - 1], [1, 4, 8])
+        assert autotune.get_table() == ([100, 5000, 2 ** 31 - 1], [1, 4, 8])
+        with pytest.raises(ValueError):
+            autotune.set_table([100], [3])            # tile shape must be 1, 2, 4 or 8
+        with pytest.raises(ValueError):
+            autotune.set_table([100, 50], [1, 2])     # bounds must increase
+    finally:
+        autotune.set_table(*saved)
+
+
 def test_unbind_params_layout():
     # the C struct: 3 doubles + 4 int32
     assert ctypes.sizeof(_lib.UnbindParams) == 40

@@ -81,6 +81,22 @@ def test_graph_replay_is_identical_and_deterministic(catalogue, cuda):
         assert np.array_equal(x[2], y[2])
 
 
+def test_tile_shapes_give_identical_results(catalogue, cuda):
+    # every tile shape sums each target's sources in the same chunk order: bit-identical
+    from pyhalma_gb300 import autotune
+    saved = autotune.get_table()
+    try:
+        out = []
+        for t in (1, 2, 4, 8):
+            autotune.set_table([2 ** 31 - 1], [t])
+            out.append(unbind_batched(*_arrays(catalogue), UnbindOptions(eps=EPS, max_iter=50), want_phi=True))
+        for o in out[1:]:
+            assert np.array_equal(o[0], out[0][0])
+            assert np.array_equal(o[2], out[0][2])
+    finally:
+        autotune.set_table(*saved)
+
+
 def test_iteration_cap_and_pass_count(catalogue, cuda):
     bound1, halo1, _ = unbind_batched(*_arrays(catalogue), UnbindOptions(eps=EPS, max_iter=1))
     assert np.all(halo1[:, 8] == 1)
