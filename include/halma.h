@@ -188,11 +188,15 @@ enum {
 };
 
 /* Tile shapes of the FP32C pair kernel per halo size class (no reference counterpart):
- * a halo with nb bound particles uses T = t_per_class[c] targets per lane (1, 2, 4 or 8) for
- * the first class c with nb <= upper[c] (increasing bounds, at most 8 classes).  Written by
- * the autotuner (pyhalma_gb300.autotune); the default is {32:1, 64:2, inf:4}. */
-int halma_set_tile_table(int32_t n_classes, const int32_t *upper, const int32_t *t_per_class);
-int halma_get_tile_table(int32_t *n_classes, int32_t *upper, int32_t *t_per_class);
+ * a halo with nb bound particles uses T = t_per_class[c] targets per lane (1, 2 or 4) for
+ * the first class c with nb <= upper[c] (increasing bounds, at most 8 classes), and every
+ * work item covers slice_len source slots (a multiple of 32): big haloes are split into
+ * (target tile x source slice) items whose partial sums are added in slice order.  Written
+ * by the autotuner (pyhalma_gb300.autotune); the default is {32:1, 64:2, inf:4}, 4096. */
+int halma_set_tile_table(int32_t n_classes, const int32_t *upper, const int32_t *t_per_class,
+                         int32_t slice_len);
+int halma_get_tile_table(int32_t *n_classes, int32_t *upper, int32_t *t_per_class,
+                         int32_t *slice_len);
 
 /* Particles in halo-contiguous order (CSR offsets, n_haloes+1 entries).  Every pass
  * recomputes each halo's FP64 bound mass, centre and bulk velocity, the potential of the

@@ -63,8 +63,8 @@ SIGNATURES = {
     "halma_release_workspace": ([], ctypes.c_int),
     "halma_kernel_launch_count": ([], ctypes.c_int64),
     "halma_set_profiling": ([_I32], ctypes.c_int),
-    "halma_set_tile_table": ([_I32, _P, _P], ctypes.c_int),
-    "halma_get_tile_table": ([_P, _P, _P], ctypes.c_int),
+    "halma_set_tile_table": ([_I32, _P, _P, _I32], ctypes.c_int),
+    "halma_get_tile_table": ([_P, _P, _P, _P], ctypes.c_int),
     "halma_profile_stats": ([_P, _I32], ctypes.c_int),
     "halma_fof": ([_I64, _P, _P, _P, _F64, _P, _P, _P], ctypes.c_int),
     "halma_fof_groups": ([_I64, _P, _I32, _P, _P, _P, _P], ctypes.c_int),

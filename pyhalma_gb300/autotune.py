@@ -1,12 +1,14 @@
 """Tile-shape autotuner for the batched unbinding pair kernel.
 
-The pair kernel processes a work item of 32*T target slots of one halo (T targets per lane,
-T in {1, 2, 4, 8}).  Small T wastes fewer lanes on small haloes and gives more items for load
-balance; large T reuses each shared-memory source read for more targets.  For each halo size
-class the tuner times one unbinding pass (pair-kernel CUDA events, ``halma_set_profiling``)
-over a synthetic catalogue of haloes drawn from that class with every candidate T, keeps the
-fastest, and writes the table to ``tile_table.json`` beside this file; ``apply()`` loads a
-saved table into the library (``halma_set_tile_table``).
+A work item of the pair kernel is 32*T target slots of one halo (T targets per lane,
+T in {1, 2, 4}) against one slice of ``slice`` source slots.  Small T wastes fewer lanes on
+small haloes and gives more items for load balance; large T reuses each shared-memory source
+read for more targets; shorter slices split the biggest haloes into more items so that no
+single item outlasts a pass.  The tuner times one unbinding pass (pair-kernel CUDA events,
+``halma_set_profiling``) per candidate: first T per halo size class on catalogues drawn from
+that class, then the slice length on a power-law catalogue.  The table is written to
+``tile_table.json`` beside this file; ``apply()`` loads a saved table into the library
+(``halma_set_tile_table``).
 """
 from __future__ import annotations
 
@@ -20,22 +22,27 @@ from . import _lib
 HERE = os.path.dirname(os.path.abspath(__file__))
 TABLE_PATH = os.path.join(HERE, "tile_table.json")
 CLASS_UPPER = [32, 64, 128, 512, 2048, 8192, 2 ** 31 - 1]
-CANDIDATES = [1, 2, 4, 8]
+CANDIDATES = [1, 2, 4]
+SLICES = [1024, 2048, 4096, 8192, 16384, 1 << 20]
 
 
-def set_table(upper, tvals):
+def set_table(upper, tvals, slice_len=4096):
     u = np.ascontiguousarray(upper, dtype=np.int32)
     t = np.ascontiguousarray(tvals, dtype=np.int32)
-    _lib.check(_lib.lib().halma_set_tile_table(len(u), _lib.ptr(u), _lib.ptr(t)), "halma_set_tile_table")
+    _lib.check(_lib.lib().halma_set_tile_table(len(u), _lib.ptr(u), _lib.ptr(t), int(slice_len)),
+               "halma_set_tile_table")
 
 
 def get_table():
+    """(upper bounds, tile shapes, slice length) currently used by the library."""
     n = np.zeros(1, dtype=np.int32)
     u = np.zeros(8, dtype=np.int32)
     t = np.zeros(8, dtype=np.int32)
-    _lib.check(_lib.lib().halma_get_tile_table(_lib.ptr(n), _lib.ptr(u), _lib.ptr(t)), "halma_get_tile_table")
+    s = np.zeros(1, dtype=np.int32)
+    _lib.check(_lib.lib().halma_get_tile_table(_lib.ptr(n), _lib.ptr(u), _lib.ptr(t), _lib.ptr(s)),
+               "halma_get_tile_table")
     k = int(n[0])
-    return u[:k].tolist(), t[:k].tolist()
+    return u[:k].tolist(), t[:k].tolist(), int(s[0])
 
 
 def apply(path=TABLE_PATH):
@@ -43,57 +50,71 @@ def apply(path=TABLE_PATH):
     if not os.path.exists(path):
         return None
     d = json.load(open(path))
-    set_table(d["upper"], d["t"])
+    set_table(d["upper"], d["t"], d.get("slice", 4096))
     return d
 
 
-def _class_catalogue(lo, hi, target_pairs, seed):
+def _catalogue(lo, hi, target_pairs, seed, alpha=0.0):
     from .synth import powerlaw_catalogue
     mean_n2 = ((lo + hi) / 2.0) ** 2
     nh = int(np.clip(target_pairs / mean_n2, 8, 40_000))
-    return powerlaw_catalogue(nh, seed=seed, alpha=0.0, n_min=lo, n_max=hi, contaminant_frac=0.0)
+    return powerlaw_catalogue(nh, seed=seed, alpha=alpha, n_min=lo, n_max=hi, contaminant_frac=0.0)
+
+
+def _time_pass(arrs, repeats):
+    from .unbinding import UnbindOptions, unbind_batched
+    opt = UnbindOptions(eps=1e-4, max_iter=1)
+    unbind_batched(*arrs, opt)          # warm-up (graph capture for this shape)
+    ms = []
+    pairs = 0.0
+    for _ in range(repeats):
+        unbind_batched(*arrs, opt)
+        pairs, t_ms = _lib.profile_stats()["passes"][0]
+        ms.append(t_ms)
+    return float(np.median(ms)), pairs
 
 
 def tune(target_pairs=4e9, repeats=3, seed=0, save_path=TABLE_PATH, verbose=True):
-    """Times every candidate T on every size class; returns and saves the table."""
+    """Times every candidate; returns and saves the table."""
     import torch
-    from .unbinding import UnbindOptions, unbind_batched
     dev = torch.device("cuda", torch.cuda.current_device())
+    to_dev = lambda cat: [torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+                          for a in (cat.offsets, cat.x, cat.y, cat.z, cat.vx, cat.vy, cat.vz, cat.mass)]
     best_t, report = [], []
     lo = 1
-    for c, hi in enumerate(CLASS_UPPER):
-        hi_eff = min(hi, 200_000)
-        lo_eff = max(lo, 8)
-        cat = _class_catalogue(lo_eff, hi_eff, target_pairs, seed + c)
-        arrs = [torch.from_numpy(np.ascontiguousarray(a)).to(dev)
-                for a in (cat.offsets, cat.x, cat.y, cat.z, cat.vx, cat.vy, cat.vz, cat.mass)]
-        opt = UnbindOptions(eps=1e-4, max_iter=1)
-        times = {}
-        _lib.set_profiling(True)
-        try:
+    _lib.set_profiling(True)
+    try:
+        for c, hi in enumerate(CLASS_UPPER):
+            hi_eff, lo_eff = min(hi, 200_000), max(lo, 8)
+            arrs = to_dev(_catalogue(lo_eff, hi_eff, target_pairs, seed + c))
+            times = {}
             for t in CANDIDATES:
-                set_table([2 ** 31 - 1], [t])
-                unbind_batched(*arrs, opt)          # warm-up (graph capture for this shape)
-                ms = []
-                for _ in range(repeats):
-                    unbind_batched(*arrs, opt)
-                    st = _lib.profile_stats()
-                    pairs, t_ms = st["passes"][0]
-                    ms.append(t_ms)
-                times[t] = (float(np.median(ms)), pairs)
-        finally:
-            _lib.set_profiling(False)
-        tbest = min(times, key=lambda k: times[k][0])
-        best_t.append(tbest)
-        report.append({"class_upper": hi, "haloes": cat.n_haloes, "sizes": [lo_eff, hi_eff],
-                       "ms": {str(k): v[0] for k, v in times.items()}, "pairs": times[tbest][1],
-                       "gpairs_per_s": {str(k): v[1] / v[0] / 1e6 for k, v in times.items()}, "best": tbest})
+                set_table([2 ** 31 - 1], [t], 1 << 20)
+                times[t] = _time_pass(arrs, repeats)
+            tbest = min(times, key=lambda k: times[k][0])
+            best_t.append(tbest)
+            report.append({"class_upper": hi, "sizes": [lo_eff, hi_eff],
+                           "ms": {str(k): v[0] for k, v in times.items()},
+                           "gpairs_per_s": {str(k): v[1] / v[0] / 1e6 for k, v in times.items()}, "best": tbest})
+            if verbose:
+                print(f"class <= {hi}: " + ", ".join(f"T={k}: {v[0]:.3f} ms" for k, v in times.items())
+                      + f" -> T={tbest}", flush=True)
+            lo = hi + 1
+        # slice length on a power-law catalogue with the chosen shapes
+        arrs = to_dev(_catalogue(50, 200_000, 4 * target_pairs, seed + 99, alpha=0.6))
+        stimes = {}
+        for s in SLICES:
+            set_table(CLASS_UPPER, best_t, s)
+            stimes[s] = _time_pass(arrs, repeats)
+        sbest = min(stimes, key=lambda k: stimes[k][0])
         if verbose:
-            print(f"class <= {hi}: " + ", ".join(f"T={k}: {v[0]:.3f} ms" for k, v in times.items())
-                  + f" -> T={tbest}", flush=True)
-        lo = hi + 1
-    table = {"upper": CLASS_UPPER, "t": best_t, "device": torch.cuda.get_device_name(dev), "report": report}
-    set_table(CLASS_UPPER, best_t)
+            print("slices: " + ", ".join(f"{k}: {v[0]:.3f} ms" for k, v in stimes.items()) + f" -> {sbest}",
+                  flush=True)
+    finally:
+        _lib.set_profiling(False)
+    table = {"upper": CLASS_UPPER, "t": best_t, "slice": sbest, "device": torch.cuda.get_device_name(dev),
+             "report": report, "slice_ms": {str(k): v[0] for k, v in stimes.items()}}
+    set_table(CLASS_UPPER, best_t, sbest)
     if save_path:
         with open(save_path, "w") as f:
             json.dump(table, f, indent=1)

@@ -172,7 +172,7 @@ __device__ __forceinline__ int tile_t_for(const TileTable &tab, int nb) {
 }
 
 __global__ void __launch_bounds__(1024) ub_items_kernel(int nh, const int *__restrict__ order, const HaloState *hs,
-                                                        TileTable tab, int4 *__restrict__ items,
+                                                        TileTable tab, int slice_len, int4 *__restrict__ items,
                                                         int *__restrict__ nitems, int *__restrict__ counter,
                                                         unsigned long long *__restrict__ pairs_out) {
     __shared__ int wsum[32];
@@ -186,13 +186,14 @@ __global__ void __launch_bounds__(1024) ub_items_kernel(int nh, const int *__res
     __syncthreads();
     for (int h0 = 0; h0 < nh; h0 += blockDim.x) {
         const int q = h0 + threadIdx.x;
-        int h = -1, cnt = 0, T = 4;
+        int h = -1, cnt = 0, T = 4, nsl = 1;
         if (q < nh) {
             h = order[q];
             if (hs[h].active) {
                 const int nb = hs[h].nb;
                 T = tile_t_for(tab, nb);
-                cnt = (nb + 32 * T - 1) / (32 * T);
+                nsl = (nb + slice_len - 1) / slice_len;
+                cnt = ((nb + 32 * T - 1) / (32 * T)) * nsl;
                 if (nb > 0) atomicAdd(&pairs, (unsigned long long)nb * (unsigned long long)nb);
             }
         }
@@ -206,7 +207,7 @@ __global__ void __launch_bounds__(1024) ub_items_kernel(int nh, const int *__res
         int pre = base;
         for (int k = 0; k < w; ++k) pre += wsum[k];
         const int start = pre + incl - cnt;
-        for (int t = 0; t < cnt; ++t) items[start + t] = make_int4(h, t, T, 0);
+        for (int t = 0; t < cnt; ++t) items[start + t] = make_int4(h, t / nsl, T, t % nsl);
         __syncthreads();
         if (threadIdx.x == 0) {
             int tot = 0;
@@ -225,9 +226,8 @@ __global__ void __launch_bounds__(1024) ub_items_kernel(int nh, const int *__res
 // One work item: 32*T target slots of one halo against all of its source slots.
 template <int T>
 __device__ __forceinline__ void pair_item(const float4 *__restrict__ pk, int64_t base, int nb, int tile, float eps2,
-                                          double *__restrict__ phi, float4 *buf, int lane) {
+                                          int c_begin, int c_end, double *__restrict__ out, float4 *buf, int lane) {
     {
-        const int nchunk = (nb + 31) >> 5;
         float px[T], py[T], pz[T], sum[T], comp[T];
 #pragma unroll
         for (int t = 0; t < T; ++t) {
@@ -237,12 +237,12 @@ __device__ __forceinline__ void pair_item(const float4 *__restrict__ pk, int64_t
             sum[t] = 0.f; comp[t] = 0.f;
         }
         const int self0 = tile * T;   // chunk c holds the self slot of target t = c - self0
-        float4 nxt = pk[base + lane];
-        for (int c = 0; c < nchunk; ++c) {
+        float4 nxt = pk[base + (int64_t)c_begin * 32 + lane];
+        for (int c = c_begin; c < c_end; ++c) {
             __syncwarp();
             buf[lane] = nxt;
             __syncwarp();
-            if (c + 1 < nchunk) nxt = pk[base + (int64_t)(c + 1) * 32 + lane];
+            if (c + 1 < c_end) nxt = pk[base + (int64_t)(c + 1) * 32 + lane];
             float part[T];
 #pragma unroll
             for (int t = 0; t < T; ++t) part[t] = 0.f;
@@ -270,17 +270,21 @@ __device__ __forceinline__ void pair_item(const float4 *__restrict__ pk, int64_t
 #pragma unroll
         for (int t = 0; t < T; ++t) {
             const int r = tile * 32 * T + t * 32 + lane;
-            if (r < nb) phi[base + r] = (double)sum[t] + (double)comp[t];
+            if (r < nb) out[r] = (double)sum[t] + (double)comp[t];
         }
     }
 }
 
-// Persistent all-pairs kernel over the work list (FP32 pair terms, compensated sums).  Each
-// item carries its tile shape T (targets per lane) chosen per halo size class.
+// Persistent all-pairs kernel over the work list (FP32 pair terms, compensated sums).  An
+// item is (halo, target tile, tile shape T, source slice): 32*T targets against one slice of
+// slice_chunks*32 source slots.  Each slice writes its own partial sums
+// (part[qoff[h] + slice * npad_h + r]); the energy kernel adds the slices in order, so the
+// result does not depend on which warp ran which item.
 __global__ void __launch_bounds__(256) ub_pair_kernel(const float4 *__restrict__ pk, const int64_t *__restrict__ poff,
-                                                      const HaloState *__restrict__ hs, const int4 *__restrict__ items,
-                                                      const int *__restrict__ nitems_p, int *counter, float eps2,
-                                                      double *__restrict__ phi) {
+                                                      const int64_t *__restrict__ qoff, const HaloState *__restrict__ hs,
+                                                      const int4 *__restrict__ items, const int *__restrict__ nitems_p,
+                                                      int *counter, float eps2, int slice_chunks,
+                                                      double *__restrict__ part) {
     __shared__ float4 buf[kUbWarps][32];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int nitems = *nitems_p;
@@ -290,21 +294,25 @@ __global__ void __launch_bounds__(256) ub_pair_kernel(const float4 *__restrict__
         item = __shfl_sync(0xffffffffu, item, 0);
         if (item >= nitems) break;
         const int4 it = items[item];
-        const int h = it.x, tile = it.y;
+        const int h = it.x, tile = it.y, slice = it.w;
         const int64_t base = poff[h];
+        const int64_t npad = poff[h + 1] - base;
         const int nb = hs[h].nb;
+        const int c0 = slice * slice_chunks;
+        const int c1 = min((nb + 31) >> 5, c0 + slice_chunks);
+        double *out = part + qoff[h] + (int64_t)slice * npad;
         switch (it.z) {
-            case 1: pair_item<1>(pk, base, nb, tile, eps2, phi, buf[w], lane); break;
-            case 2: pair_item<2>(pk, base, nb, tile, eps2, phi, buf[w], lane); break;
-            case 8: pair_item<8>(pk, base, nb, tile, eps2, phi, buf[w], lane); break;
-            default: pair_item<4>(pk, base, nb, tile, eps2, phi, buf[w], lane); break;
+            case 1: pair_item<1>(pk, base, nb, tile, eps2, c0, c1, out, buf[w], lane); break;
+            case 2: pair_item<2>(pk, base, nb, tile, eps2, c0, c1, out, buf[w], lane); break;
+            default: pair_item<4>(pk, base, nb, tile, eps2, c0, c1, out, buf[w], lane); break;
         }
     }
 }
 
 // FP64 energies, sign test and removal counts (one block per active halo).
-__global__ void __launch_bounds__(256) ub_energy_kernel(const int64_t *__restrict__ poff, const int *__restrict__ pidx,
-                                                        const double *__restrict__ phi, const double *__restrict__ vx,
+__global__ void __launch_bounds__(256) ub_energy_kernel(const int64_t *__restrict__ poff, const int64_t *__restrict__ qoff,
+                                                        int slice_len, const int *__restrict__ pidx,
+                                                        const double *__restrict__ part, const double *__restrict__ vx,
                                                         const double *__restrict__ vy, const double *__restrict__ vz,
                                                         const double *__restrict__ m, double gfac,
                                                         unsigned char *__restrict__ bound, double *__restrict__ phi_out,
@@ -313,13 +321,15 @@ __global__ void __launch_bounds__(256) ub_energy_kernel(const int64_t *__restric
     if (!hs[h].active) return;
     __shared__ double sh[3][32];
     const HaloState s = hs[h];
-    const int64_t pb = poff[h];
+    const int64_t pb = poff[h], npad = poff[h + 1] - pb, qb = qoff[h];
+    const int nsl = (s.nb + slice_len - 1) / slice_len;
     double v[3] = {0, 0, 0};   // removed, ekin (kept), epot (kept)
     for (int r = threadIdx.x; r < s.nb; r += blockDim.x) {
         const int i = pidx[pb + r];
         const double dvx = vx[i] - s.vx, dvy = vy[i] - s.vy, dvz = vz[i] - s.vz;
         const double ek = 0.5 * (dvx * dvx + dvy * dvy + dvz * dvz);
-        const double p = phi[pb + r];
+        double p = 0.0;
+        for (int q = 0; q < nsl; ++q) p += part[qb + (int64_t)q * npad + r];   // slices in order
         const double e = ek - gfac * p;
         const double mi = m[i];
         if (e > 0.0) {
@@ -401,7 +411,7 @@ Profile &profile() {
 static TileTable &tile_table_ref() {
     // default until the autotuner's table is loaded: 1 chunk of targets for haloes of up to
     // 32 bound particles, 2 up to 64, 4 above
-    static TileTable t = {3, {32, 64, 0x7fffffff}, {1, 2, 4}};
+    static TileTable t = {3, {32, 64, 0x7fffffff}, {1, 2, 4}, 4096};
     return t;
 }
 
@@ -424,30 +434,38 @@ int unbind_device(int64_t n, int nh, const int64_t *d_off, const int64_t *h_off,
                   const halma_unbind_params &p, unsigned char *bound, double *phi_out, double *halo_out,
                   cudaStream_t st) {
     const TileTable tab = tile_table();
-    // host-side plan: padded slot offsets, work-list capacity (one item per 32 slots at
-    // most, the smallest tile), size order
-    std::vector<int64_t> poff(nh + 1);
+    const bool f64 = p.precision == HALMA_UNBIND_FP64;
+    // source slice length (a multiple of 32); the FP64 path sums a halo in one piece
+    const int slice_len = f64 ? 0x7fffffe0 : tab.slice;
+    // host-side plan: padded slot offsets, per-slice partial-sum offsets, work-list capacity
+    // (one item per 32 targets and slice at most, the smallest tile), size order
+    std::vector<int64_t> poff(nh + 1), qoff(nh + 1);
     std::vector<int> order(nh);
     int64_t max_items = 0;
     poff[0] = 0;
+    qoff[0] = 0;
     for (int h = 0; h < nh; ++h) {
         const int64_t c = h_off[h + 1] - h_off[h];
-        poff[h + 1] = poff[h] + ((c + 31) / 32) * 32;
-        max_items += (c + 31) / 32;
+        const int64_t npad = ((c + 31) / 32) * 32;
+        const int64_t nsl = std::max<int64_t>(1, (c + slice_len - 1) / slice_len);
+        poff[h + 1] = poff[h] + npad;
+        qoff[h + 1] = qoff[h] + npad * nsl;
+        max_items += ((c + 31) / 32) * nsl;
     }
     std::iota(order.begin(), order.end(), 0);
     std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
         return (h_off[a + 1] - h_off[a]) > (h_off[b + 1] - h_off[b]);
     });
     const int64_t P = std::max<int64_t>(poff[nh], 32);
-    const bool f64 = p.precision == HALMA_UNBIND_FP64;
+    const int64_t Q = std::max<int64_t>(qoff[nh], 32);
     Layout L;
     const size_t o_hs = L.add(sizeof(HaloState) * (size_t)std::max(nh, 1));
     const size_t o_poff = L.add(sizeof(int64_t) * (nh + 1));
+    const size_t o_qoff = L.add(sizeof(int64_t) * (nh + 1));
     const size_t o_order = L.add(sizeof(int) * std::max(nh, 1));
     const size_t o_pk = L.add((f64 ? sizeof(double4) : sizeof(float4)) * P);
     const size_t o_pidx = L.add(sizeof(int) * P);
-    const size_t o_phi = L.add(sizeof(double) * P);
+    const size_t o_phi = L.add(sizeof(double) * Q);
     const size_t o_items = L.add(sizeof(int4) * std::max<int64_t>(max_items, 1));
     const size_t o_cnt = L.add(64);
     const size_t o_pairs = L.add(sizeof(unsigned long long) * p.max_iter);
@@ -456,6 +474,7 @@ int unbind_device(int64_t n, int nh, const int64_t *d_off, const int64_t *h_off,
     HALMA_TRY(workspace(L.total, &base, st));
     auto *hs = at<HaloState>(base, o_hs);
     auto *dpoff = at<int64_t>(base, o_poff);
+    auto *dqoff = at<int64_t>(base, o_qoff);
     auto *dorder = at<int>(base, o_order);
     auto *pidx = at<int>(base, o_pidx);
     auto *phi = at<double>(base, o_phi);
@@ -475,6 +494,7 @@ int unbind_device(int64_t n, int nh, const int64_t *d_off, const int64_t *h_off,
         off = o;
     }
     HALMA_CUDA(cudaMemcpyAsync(dpoff, poff.data(), sizeof(int64_t) * (nh + 1), cudaMemcpyHostToDevice, st));
+    HALMA_CUDA(cudaMemcpyAsync(dqoff, qoff.data(), sizeof(int64_t) * (nh + 1), cudaMemcpyHostToDevice, st));
     HALMA_CUDA(cudaMemcpyAsync(dorder, order.data(), sizeof(int) * nh, cudaMemcpyHostToDevice, st));
     const double gfac = p.G * p.factor_v * p.factor_v;
     const float eps2 = (float)(p.eps * p.eps);
@@ -491,14 +511,15 @@ int unbind_device(int64_t n, int nh, const int64_t *d_off, const int64_t *h_off,
             for (int it = 0; it < p.max_iter; ++it) {
                 HALMA_LAUNCH(ub_reduce_kernel, nh, 256, 0, rs, off, x, y, z, vx, vy, vz, m, bound, hs, 0);
                 HALMA_LAUNCH(ub_pack_kernel<float4>, nh, 256, 0, rs, off, dpoff, x, y, z, m, bound, hs, pk, pidx);
-                HALMA_LAUNCH(ub_items_kernel, 1, 1024, 0, rs, nh, dorder, hs, tab, items, cnt, cnt + 1,
+                HALMA_LAUNCH(ub_items_kernel, 1, 1024, 0, rs, nh, dorder, hs, tab, slice_len, items, cnt, cnt + 1,
                              profiling ? dpairs + it : nullptr);
                 // External: captured as an event-record node, so the replay records it
                 if (profiling) HALMA_CUDA(cudaEventRecordWithFlags(prof.ev0[it], rs, cudaEventRecordExternal));
-                HALMA_LAUNCH(ub_pair_kernel, pgrid, 256, 0, rs, pk, dpoff, hs, items, cnt, cnt + 1, eps2, phi);
+                HALMA_LAUNCH(ub_pair_kernel, pgrid, 256, 0, rs, pk, dpoff, dqoff, hs, items, cnt, cnt + 1, eps2,
+                             slice_len / 32, phi);
                 if (profiling) HALMA_CUDA(cudaEventRecordWithFlags(prof.ev1[it], rs, cudaEventRecordExternal));
-                HALMA_LAUNCH(ub_energy_kernel, nh, 256, 0, rs, dpoff, pidx, phi, vx, vy, vz, m, gfac, bound, phi_out,
-                             hs);
+                HALMA_LAUNCH(ub_energy_kernel, nh, 256, 0, rs, dpoff, dqoff, slice_len, pidx, phi, vx, vy, vz, m, gfac,
+                             bound, phi_out, hs);
             }
             return HALMA_OK;
         };
@@ -517,6 +538,7 @@ int unbind_device(int64_t n, int nh, const int64_t *d_off, const int64_t *h_off,
             key.push_back((uintptr_t)profiling);
             key.push_back((uintptr_t)dpairs);
             key.push_back((uintptr_t)tab.n);
+            key.push_back((uintptr_t)slice_len);
             for (int c = 0; c < tab.n; ++c) {
                 key.push_back((uintptr_t)tab.upper[c]);
                 key.push_back((uintptr_t)tab.t[c]);
@@ -584,7 +606,8 @@ int unbind_device(int64_t n, int nh, const int64_t *d_off, const int64_t *h_off,
                 HALMA_LAUNCH(ub_pair_f64_kernel, grid_for(hh[h].nb, 256), 256, 0, st, pk + poff[h], hh[h].nb,
                              p.eps * p.eps, phi + poff[h]);
             }
-            HALMA_LAUNCH(ub_energy_kernel, nh, 256, 0, st, dpoff, pidx, phi, vx, vy, vz, m, gfac, bound, phi_out, hs);
+            HALMA_LAUNCH(ub_energy_kernel, nh, 256, 0, st, dpoff, dqoff, slice_len, pidx, phi, vx, vy, vz, m, gfac,
+                         bound, phi_out, hs);
             if (!any) break;
         }
         HALMA_LAUNCH(ub_reduce_kernel, nh, 256, 0, st, off, x, y, z, vx, vy, vz, m, bound, hs, 1);
@@ -661,14 +684,18 @@ extern "C" int halma_unbind_batched(int64_t n, int64_t n_haloes, const int64_t *
     return s;
 }
 
-extern "C" int halma_set_tile_table(int32_t n_classes, const int32_t *upper, const int32_t *t_per_class) {
+extern "C" int halma_set_tile_table(int32_t n_classes, const int32_t *upper, const int32_t *t_per_class,
+                                    int32_t slice_len) {
     if (n_classes < 1 || n_classes > kMaxTileClasses || !upper || !t_per_class)
         return fail(HALMA_ERR_INVALID, "tile table needs 1..%d classes", kMaxTileClasses);
+    if (slice_len < 32 || slice_len % 32 != 0 || slice_len > (1 << 26))
+        return fail(HALMA_ERR_INVALID, "source slice must be a positive multiple of 32 (at most 2^26)");
     TileTable t{};
     t.n = n_classes;
+    t.slice = slice_len;
     for (int c = 0; c < n_classes; ++c) {
         const int v = t_per_class[c];
-        if (v != 1 && v != 2 && v != 4 && v != 8) return fail(HALMA_ERR_INVALID, "tile shape must be 1, 2, 4 or 8");
+        if (v != 1 && v != 2 && v != 4) return fail(HALMA_ERR_INVALID, "tile shape must be 1, 2 or 4");
         if (upper[c] < 1 || (c > 0 && upper[c] <= upper[c - 1]))
             return fail(HALMA_ERR_INVALID, "class bounds must be positive and increasing");
         t.upper[c] = upper[c];
@@ -679,11 +706,13 @@ extern "C" int halma_set_tile_table(int32_t n_classes, const int32_t *upper, con
     return HALMA_OK;
 }
 
-extern "C" int halma_get_tile_table(int32_t *n_classes, int32_t *upper, int32_t *t_per_class) {
-    if (!n_classes || !upper || !t_per_class) return fail(HALMA_ERR_INVALID, "null pointer");
+extern "C" int halma_get_tile_table(int32_t *n_classes, int32_t *upper, int32_t *t_per_class,
+                                    int32_t *slice_len) {
+    if (!n_classes || !upper || !t_per_class || !slice_len) return fail(HALMA_ERR_INVALID, "null pointer");
     std::lock_guard<std::mutex> guard(api_mutex());
     const TileTable &t = tile_table_ref();
     *n_classes = t.n;
+    *slice_len = t.slice;
     for (int c = 0; c < t.n; ++c) {
         upper[c] = t.upper[c];
         t_per_class[c] = t.t[c];

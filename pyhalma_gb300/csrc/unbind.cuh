@@ -26,6 +26,7 @@ struct TileTable {
     int n;
     int upper[kMaxTileClasses];
     int t[kMaxTileClasses];
+    int slice;   // source slots per work item (multiple of 32)
 };
 TileTable tile_table();
 

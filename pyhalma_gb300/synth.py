@@ -201,6 +201,81 @@ def powerlaw_catalogue(n_haloes, *, seed=0, alpha=1.0, n_min=50, n_max=200_000,
                               total=int(counts.sum()), sum_n2=float((counts.astype(np.float64) ** 2).sum())))
 
 
+def powerlaw_mean(alpha, n_min=50, n_max=200_000):
+    """Mean halo size of dN/dlogN ∝ N^-alpha on [n_min, n_max] (closed form)."""
+    a = float(alpha)
+    if abs(a) < 1e-9:
+        return (n_max - n_min) / np.log(n_max / n_min)
+    if abs(a - 1.0) < 1e-9:
+        return np.log(n_max / n_min) / (1.0 / n_min - 1.0 / n_max)
+    return (a / (a - 1.0)) * (n_min ** (1 - a) - n_max ** (1 - a)) / (n_min ** (-a) - n_max ** (-a))
+
+
+def alpha_for_mean(mean, n_min=50, n_max=200_000):
+    """The slope whose mean halo size is `mean` (bisection; the mean falls as alpha grows)."""
+    lo, hi = -1.0, 3.0
+    for _ in range(100):
+        mid = 0.5 * (lo + hi)
+        if powerlaw_mean(mid, n_min, n_max) > mean:
+            lo = mid
+        else:
+            hi = mid
+    return 0.5 * (lo + hi)
+
+
+def full_snapshot(n_total=200_000_000, n_haloes=200_000, *, seed=0, box_mpc=100.0, bg_frac=0.20,
+                  bridge_frac=0.05, alpha=None, n_min=50, n_max=200_000, particle_mass=1e6,
+                  bulk_sigma=200.0, bg_sigma=300.0, chunk=20_000):
+    """Large snapshot: power-law Plummer haloes (a fraction placed in pairs within 2a of a
+    partner to form FoF bridges) plus a uniform background.  With alpha=None the slope is
+    chosen so that haloes hold (1 - bg_frac) of n_total on average.  Returns float64 arrays
+    in Mpc, km/s, Msun and the per-particle generating halo id (-1 background)."""
+    rng = np.random.default_rng(seed)
+    n_bg_target = int(round(bg_frac * n_total))
+    if alpha is None:
+        alpha = alpha_for_mean((n_total - n_bg_target) / n_haloes, n_min, n_max)
+    counts = powerlaw_counts(rng, n_haloes, alpha, n_min, n_max)
+    masses = counts * particle_mass
+    a = plummer_scale_radius_kpc(masses)
+    box_kpc = box_mpc * 1e3
+    centres = rng.uniform(-box_kpc / 2, box_kpc / 2, (n_haloes, 3))
+    n_pair = int(bridge_frac * n_haloes) // 2 * 2
+    pick = rng.choice(n_haloes, n_pair, replace=False)
+    first, second = pick[: n_pair // 2], pick[n_pair // 2:]
+    offs = _unit_vectors(rng, len(first)) * (rng.uniform(0, 2.0, len(first)) * a[first])[:, None]
+    centres[second] = np.clip(centres[first] + offs, -box_kpc / 2, box_kpc / 2)
+    bulk = rng.normal(0.0, bulk_sigma, (n_haloes, 3))
+    n_halo = int(counts.sum())
+    n_bg = max(n_total - n_halo, 0)
+    n = n_halo + n_bg
+    out = {k: np.empty(n) for k in ("x", "y", "z", "vx", "vy", "vz")}
+    hid = np.empty(n, dtype=np.int32)
+    pos = 0
+    for h0 in range(0, n_haloes, chunk):
+        sl = slice(h0, min(h0 + chunk, n_haloes))
+        p, v, sid, _ = _spheres(rng, counts[sl], masses[sl], centres[sl], bulk[sl], 0.0)
+        k = p.shape[0]
+        for d, key in enumerate(("x", "y", "z")):
+            out[key][pos:pos + k] = p[:, d] / 1e3
+        for d, key in enumerate(("vx", "vy", "vz")):
+            out[key][pos:pos + k] = v[:, d]
+        hid[pos:pos + k] = sid + h0
+        pos += k
+    for q0 in range(0, n_bg, 10_000_000):
+        k = min(10_000_000, n_bg - q0)
+        for key in ("x", "y", "z"):
+            out[key][pos:pos + k] = rng.uniform(-box_kpc / 2, box_kpc / 2, k) / 1e3
+        for key in ("vx", "vy", "vz"):
+            out[key][pos:pos + k] = rng.normal(0.0, bg_sigma, k)
+        hid[pos:pos + k] = -1
+        pos += k
+    mass = np.full(n, particle_mass)
+    return Snapshot(out["x"], out["y"], out["z"], out["vx"], out["vy"], out["vz"], mass, hid,
+                    np.zeros(n, dtype=bool), box_mpc,
+                    dict(seed=seed, alpha=alpha, n_haloes=n_haloes, halo_particles=n_halo, background=n_bg,
+                         bridged_pairs=n_pair // 2))
+
+
 def _nfw_radius(rng, n, c, r_vir):
     """Inverse-CDF sampling of the NFW enclosed-mass profile inside r_vir (tabulated)."""
     rs = r_vir / c

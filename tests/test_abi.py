@@ -85,12 +85,14 @@ def test_tile_table_validation_and_roundtrip():
     from pyhalma_gb300 import autotune
     saved = autotune.get_table()
     try:
-        autotune.set_table([100, 5000, 2 ** 31 - 1], [1, 4, 8])
-        assert autotune.get_table() == ([100, 5000, 2 ** 31 - 1], [1, 4, 8])
+        autotune.set_table([100, 5000, 2 ** 31 - 1], [1, 2, 4], 2048)
+        assert autotune.get_table() == ([100, 5000, 2 ** 31 - 1], [1, 2, 4], 2048)
         with pytest.raises(ValueError):
-            autotune.set_table([100], [3])            # tile shape must be 1, 2, 4 or 8
+            autotune.set_table([100], [3])            # tile shape must be 1, 2 or 4
         with pytest.raises(ValueError):
             autotune.set_table([100, 50], [1, 2])     # bounds must increase
+        with pytest.raises(ValueError):
+            autotune.set_table([100], [2], 100)       # slice must be a multiple of 32
     finally:
         autotune.set_table(*saved)
 

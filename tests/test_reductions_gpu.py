@@ -38,7 +38,8 @@ def test_batched_reductions_with_mask(cuda):
         assert np.allclose(row[:7], (M, cx, cy, cz, ux, uy, uz), rtol=1e-12, atol=1e-12)
         assert np.isclose(row[7], ref.furthest_particle(cx, cy, cz, pl, cat.x, cat.y, cat.z), rtol=1e-12)
         assert np.isclose(row[8], r05, rtol=1e-12)
-        sig = ref.sigma_effective(pl, row[8], cat.x, cat.y, cat.z, cat.vx, cat.vy, cat.vz, cx, cy, cz, ux, uy, uz)
+        # same centre as the GPU: members at d == R05 split identically (d < R05 is strict)
+        sig = ref.sigma_effective(pl, row[8], cat.x, cat.y, cat.z, cat.vx, cat.vy, cat.vz, *row[1:7])
         assert np.isclose(row[9], sig, rtol=1e-11)
         assert row[10] == len(pl)
 
