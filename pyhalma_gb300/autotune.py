@@ -80,16 +80,29 @@ def tune(target_pairs=4e9, repeats=3, seed=0, save_path=TABLE_PATH, verbose=True
     dev = torch.device("cuda", torch.cuda.current_device())
     to_dev = lambda cat: [torch.from_numpy(np.ascontiguousarray(a)).to(dev)
                           for a in (cat.offsets, cat.x, cat.y, cat.z, cat.vx, cat.vy, cat.vz, cat.mass)]
+    from .synth import powerlaw_catalogue
     best_t, report = [], []
-    lo = 1
     _lib.set_profiling(True)
     try:
+        # 1) slice length on the batched workload's size distribution (dN/dlogN ∝ N^-1 on
+        #    [50, 2e5], 20 000 haloes) with the default shapes
+        big = to_dev(powerlaw_catalogue(20_000, seed=seed + 99, alpha=1.0, contaminant_frac=0.0))
+        stimes = {}
+        for s in SLICES:
+            set_table([32, 64, 2 ** 31 - 1], [1, 2, 4], s)
+            stimes[s] = _time_pass(big, repeats)
+        sbest = min(stimes, key=lambda k: stimes[k][0])
+        if verbose:
+            print("slices: " + ", ".join(f"{k}: {v[0]:.3f} ms" for k, v in stimes.items()) + f" -> {sbest}",
+                  flush=True)
+        # 2) tile shape per size class with that slice
+        lo = 1
         for c, hi in enumerate(CLASS_UPPER):
             hi_eff, lo_eff = min(hi, 200_000), max(lo, 8)
             arrs = to_dev(_catalogue(lo_eff, hi_eff, target_pairs, seed + c))
             times = {}
             for t in CANDIDATES:
-                set_table([2 ** 31 - 1], [t], 1 << 20)
+                set_table([2 ** 31 - 1], [t], sbest)
                 times[t] = _time_pass(arrs, repeats)
             tbest = min(times, key=lambda k: times[k][0])
             best_t.append(tbest)
@@ -100,20 +113,16 @@ def tune(target_pairs=4e9, repeats=3, seed=0, save_path=TABLE_PATH, verbose=True
                 print(f"class <= {hi}: " + ", ".join(f"T={k}: {v[0]:.3f} ms" for k, v in times.items())
                       + f" -> T={tbest}", flush=True)
             lo = hi + 1
-        # slice length on a power-law catalogue with the chosen shapes
-        arrs = to_dev(_catalogue(50, 200_000, 4 * target_pairs, seed + 99, alpha=0.6))
-        stimes = {}
-        for s in SLICES:
-            set_table(CLASS_UPPER, best_t, s)
-            stimes[s] = _time_pass(arrs, repeats)
-        sbest = min(stimes, key=lambda k: stimes[k][0])
+        # 3) the tuned table on the batched workload
+        set_table(CLASS_UPPER, best_t, sbest)
+        final_ms, final_pairs = _time_pass(big, repeats)
         if verbose:
-            print("slices: " + ", ".join(f"{k}: {v[0]:.3f} ms" for k, v in stimes.items()) + f" -> {sbest}",
-                  flush=True)
+            print(f"tuned table: {final_ms:.3f} ms per pass ({final_pairs / final_ms / 1e9:.3f} Tpairs/s)", flush=True)
     finally:
         _lib.set_profiling(False)
     table = {"upper": CLASS_UPPER, "t": best_t, "slice": sbest, "device": torch.cuda.get_device_name(dev),
-             "report": report, "slice_ms": {str(k): v[0] for k, v in stimes.items()}}
+             "report": report, "slice_ms": {str(k): v[0] for k, v in stimes.items()},
+             "batched_pass_ms": final_ms, "batched_pass_pairs": final_pairs}
     set_table(CLASS_UPPER, best_t, sbest)
     if save_path:
         with open(save_path, "w") as f:

@@ -261,6 +261,7 @@ __global__ void __launch_bounds__(256) link_kernel(
     const double *__restrict__ x, const double *__restrict__ y, const double *__restrict__ z,
     int *parent, unsigned char *has, int *err) {
     __shared__ float4 buf[kFofWarps][32];
+    __shared__ int rbuf[kFofWarps][32];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int nitems = *nitems_p;
     for (int item = blockIdx.x * kFofWarps + w; item < nitems; item += gridDim.x * kFofWarps) {
@@ -298,8 +299,13 @@ __global__ void __launch_bounds__(256) link_kernel(
             for (int j0 = js; j0 < je; j0 += 32) {
                 const int jl = j0 + lane;
                 const float4 q = jl < je ? rec[jl] : make_float4(0.f, 0.f, 0.f, 0.f);
+                // roots of the chunk, found once per chunk instead of once per hit; a root
+                // read here may be outdated by later unions, which is safe: equal roots
+                // prove the same set, unequal ones are re-checked by uf_union
+                const int rql = jl < je ? uf_find(parent, jl, err) : -1;
                 __syncwarp();
                 buf[w][lane] = q;
+                rbuf[w][lane] = rql;
                 __syncwarp();
                 const int cnt = min(32, je - j0);
                 for (int t = 0; t < cnt; ++t) {
@@ -310,7 +316,7 @@ __global__ void __launch_bounds__(256) link_kernel(
                     bool hit = hv && d2 <= g.hi && (nb >= 0 || jj > k);
                     if (hit && d2 >= g.lo) hit = exact_link(x, y, z, hidx, __float_as_int(qq.w), g.r2);
                     if (hit) {
-                        const int rq = uf_find(parent, jj, err);
+                        const int rq = rbuf[w][t];
                         if (rq != myroot) {
                             uf_union(parent, myroot, rq, err);
                             has[k] = 1;

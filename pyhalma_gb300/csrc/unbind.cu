@@ -171,9 +171,13 @@ __device__ __forceinline__ int tile_t_for(const TileTable &tab, int nb) {
     return 4;
 }
 
+// The work list is implicit: ordered halo q owns items istart[q] .. istart[q+1]-1, described
+// by idesc[q] = (halo, T, slices, unused); item i of that halo is (tile i / slices,
+// slice i % slices).  Only nh+1 prefix counts are written per pass.
 __global__ void __launch_bounds__(1024) ub_items_kernel(int nh, const int *__restrict__ order, const HaloState *hs,
-                                                        TileTable tab, int slice_len, int4 *__restrict__ items,
-                                                        int *__restrict__ nitems, int *__restrict__ counter,
+                                                        TileTable tab, int slice_len, int *__restrict__ istart,
+                                                        int4 *__restrict__ idesc, int *__restrict__ nitems,
+                                                        int *__restrict__ counter,
                                                         unsigned long long *__restrict__ pairs_out) {
     __shared__ int wsum[32];
     __shared__ int base;
@@ -192,7 +196,7 @@ __global__ void __launch_bounds__(1024) ub_items_kernel(int nh, const int *__res
             if (hs[h].active) {
                 const int nb = hs[h].nb;
                 T = tile_t_for(tab, nb);
-                nsl = (nb + slice_len - 1) / slice_len;
+                nsl = (int)(((int64_t)nb + slice_len - 1) / slice_len);
                 cnt = ((nb + 32 * T - 1) / (32 * T)) * nsl;
                 if (nb > 0) atomicAdd(&pairs, (unsigned long long)nb * (unsigned long long)nb);
             }
@@ -206,8 +210,10 @@ __global__ void __launch_bounds__(1024) ub_items_kernel(int nh, const int *__res
         __syncthreads();
         int pre = base;
         for (int k = 0; k < w; ++k) pre += wsum[k];
-        const int start = pre + incl - cnt;
-        for (int t = 0; t < cnt; ++t) items[start + t] = make_int4(h, t / nsl, T, t % nsl);
+        if (q < nh) {
+            istart[q] = pre + incl - cnt;
+            idesc[q] = make_int4(h, T, max(nsl, 1), 0);
+        }
         __syncthreads();
         if (threadIdx.x == 0) {
             int tot = 0;
@@ -217,6 +223,7 @@ __global__ void __launch_bounds__(1024) ub_items_kernel(int nh, const int *__res
         __syncthreads();
     }
     if (threadIdx.x == 0) {
+        istart[nh] = base;
         *nitems = base;
         *counter = 0;
         if (pairs_out) *pairs_out = pairs;
@@ -282,7 +289,8 @@ __device__ __forceinline__ void pair_item(const float4 *__restrict__ pk, int64_t
 // result does not depend on which warp ran which item.
 __global__ void __launch_bounds__(256) ub_pair_kernel(const float4 *__restrict__ pk, const int64_t *__restrict__ poff,
                                                       const int64_t *__restrict__ qoff, const HaloState *__restrict__ hs,
-                                                      const int4 *__restrict__ items, const int *__restrict__ nitems_p,
+                                                      int nh, const int *__restrict__ istart,
+                                                      const int4 *__restrict__ idesc, const int *__restrict__ nitems_p,
                                                       int *counter, float eps2, int slice_chunks,
                                                       double *__restrict__ part) {
     __shared__ float4 buf[kUbWarps][32];
@@ -293,7 +301,16 @@ __global__ void __launch_bounds__(256) ub_pair_kernel(const float4 *__restrict__
         if (lane == 0) item = atomicAdd(counter, 1);
         item = __shfl_sync(0xffffffffu, item, 0);
         if (item >= nitems) break;
-        const int4 it = items[item];
+        // ordered halo owning the item: last q with istart[q] <= item
+        int lo = 0, hi = nh - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (istart[mid] <= item) lo = mid;
+            else hi = mid - 1;
+        }
+        const int4 d = idesc[lo];
+        const int local = item - istart[lo];
+        const int4 it = make_int4(d.x, local / d.z, d.y, local % d.z);
         const int h = it.x, tile = it.y, slice = it.w;
         const int64_t base = poff[h];
         const int64_t npad = poff[h + 1] - base;
@@ -322,7 +339,7 @@ __global__ void __launch_bounds__(256) ub_energy_kernel(const int64_t *__restric
     __shared__ double sh[3][32];
     const HaloState s = hs[h];
     const int64_t pb = poff[h], npad = poff[h + 1] - pb, qb = qoff[h];
-    const int nsl = (s.nb + slice_len - 1) / slice_len;
+    const int nsl = (int)(((int64_t)s.nb + slice_len - 1) / slice_len);
     double v[3] = {0, 0, 0};   // removed, ekin (kept), epot (kept)
     for (int r = threadIdx.x; r < s.nb; r += blockDim.x) {
         const int i = pidx[pb + r];
@@ -436,12 +453,10 @@ int unbind_device(int64_t n, int nh, const int64_t *d_off, const int64_t *h_off,
     const TileTable tab = tile_table();
     const bool f64 = p.precision == HALMA_UNBIND_FP64;
     // source slice length (a multiple of 32); the FP64 path sums a halo in one piece
-    const int slice_len = f64 ? 0x7fffffe0 : tab.slice;
-    // host-side plan: padded slot offsets, per-slice partial-sum offsets, work-list capacity
-    // (one item per 32 targets and slice at most, the smallest tile), size order
+    const int slice_len = f64 ? (1 << 30) : tab.slice;
+    // host-side plan: padded slot offsets, per-slice partial-sum offsets, size order
     std::vector<int64_t> poff(nh + 1), qoff(nh + 1);
     std::vector<int> order(nh);
-    int64_t max_items = 0;
     poff[0] = 0;
     qoff[0] = 0;
     for (int h = 0; h < nh; ++h) {
@@ -450,7 +465,6 @@ int unbind_device(int64_t n, int nh, const int64_t *d_off, const int64_t *h_off,
         const int64_t nsl = std::max<int64_t>(1, (c + slice_len - 1) / slice_len);
         poff[h + 1] = poff[h] + npad;
         qoff[h + 1] = qoff[h] + npad * nsl;
-        max_items += ((c + 31) / 32) * nsl;
     }
     std::iota(order.begin(), order.end(), 0);
     std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
@@ -466,7 +480,8 @@ int unbind_device(int64_t n, int nh, const int64_t *d_off, const int64_t *h_off,
     const size_t o_pk = L.add((f64 ? sizeof(double4) : sizeof(float4)) * P);
     const size_t o_pidx = L.add(sizeof(int) * P);
     const size_t o_phi = L.add(sizeof(double) * Q);
-    const size_t o_items = L.add(sizeof(int4) * std::max<int64_t>(max_items, 1));
+    const size_t o_istart = L.add(sizeof(int) * (nh + 1));
+    const size_t o_idesc = L.add(sizeof(int4) * std::max(nh, 1));
     const size_t o_cnt = L.add(64);
     const size_t o_pairs = L.add(sizeof(unsigned long long) * p.max_iter);
     const size_t o_off = d_off ? 0 : L.add(sizeof(int64_t) * (nh + 1));
@@ -478,7 +493,8 @@ int unbind_device(int64_t n, int nh, const int64_t *d_off, const int64_t *h_off,
     auto *dorder = at<int>(base, o_order);
     auto *pidx = at<int>(base, o_pidx);
     auto *phi = at<double>(base, o_phi);
-    auto *items = at<int4>(base, o_items);
+    auto *istart = at<int>(base, o_istart);
+    auto *idesc = at<int4>(base, o_idesc);
     int *cnt = at<int>(base, o_cnt);   // [0] nitems [1] counter
     auto *dpairs = at<unsigned long long>(base, o_pairs);
     Profile &prof = profile();
@@ -511,12 +527,12 @@ int unbind_device(int64_t n, int nh, const int64_t *d_off, const int64_t *h_off,
             for (int it = 0; it < p.max_iter; ++it) {
                 HALMA_LAUNCH(ub_reduce_kernel, nh, 256, 0, rs, off, x, y, z, vx, vy, vz, m, bound, hs, 0);
                 HALMA_LAUNCH(ub_pack_kernel<float4>, nh, 256, 0, rs, off, dpoff, x, y, z, m, bound, hs, pk, pidx);
-                HALMA_LAUNCH(ub_items_kernel, 1, 1024, 0, rs, nh, dorder, hs, tab, slice_len, items, cnt, cnt + 1,
-                             profiling ? dpairs + it : nullptr);
+                HALMA_LAUNCH(ub_items_kernel, 1, 1024, 0, rs, nh, dorder, hs, tab, slice_len, istart, idesc, cnt,
+                             cnt + 1, profiling ? dpairs + it : nullptr);
                 // External: captured as an event-record node, so the replay records it
                 if (profiling) HALMA_CUDA(cudaEventRecordWithFlags(prof.ev0[it], rs, cudaEventRecordExternal));
-                HALMA_LAUNCH(ub_pair_kernel, pgrid, 256, 0, rs, pk, dpoff, dqoff, hs, items, cnt, cnt + 1, eps2,
-                             slice_len / 32, phi);
+                HALMA_LAUNCH(ub_pair_kernel, pgrid, 256, 0, rs, pk, dpoff, dqoff, hs, nh, istart, idesc, cnt, cnt + 1,
+                             eps2, slice_len / 32, phi);
                 if (profiling) HALMA_CUDA(cudaEventRecordWithFlags(prof.ev1[it], rs, cudaEventRecordExternal));
                 HALMA_LAUNCH(ub_energy_kernel, nh, 256, 0, rs, dpoff, dqoff, slice_len, pidx, phi, vx, vy, vz, m, gfac,
                              bound, phi_out, hs);
