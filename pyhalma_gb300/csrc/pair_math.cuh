@@ -4,6 +4,35 @@
 
 namespace halma {
 
+// ---- packed FP32 pairs (sm_100+ f32x2 instructions: two FP32 lanes per instruction) -------
+typedef unsigned long long f2x;   // {lo, hi} float pair in one 64-bit register
+
+__device__ __forceinline__ f2x pack2(float lo, float hi) {
+    f2x r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+    return r;
+}
+__device__ __forceinline__ void unpack2(f2x r, float &lo, float &hi) {
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(r));
+}
+__device__ __forceinline__ f2x sub2(f2x a, f2x b) {
+    f2x d;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ f2x fma2(f2x a, f2x b, f2x c) {
+    f2x d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
+// Hardware reciprocal square root, subnormal inputs and outputs flushed to zero (the
+// softened r^2 >= eps^2 is never subnormal); one special-function instruction.
+__device__ __forceinline__ float rsqrt_ftz(float x) {
+    float y;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
 // Error-free transformation of s + v (Knuth's TwoSum); the rounding error goes into c.
 // Six additions, no fused operations, valid for any magnitudes.
 __device__ __forceinline__ void two_sum_acc(float &s, float &c, float v) {

@@ -230,49 +230,79 @@ __global__ void __launch_bounds__(1024) ub_items_kernel(int nh, const int *__res
     }
 }
 
-// One work item: 32*T target slots of one halo against all of its source slots.
+// 32 sources of the staged chunk against T targets, two sources per f32x2 instruction.
+// sa[kp] = {x_2kp, x_2kp+1, y_2kp, y_2kp+1}, sb[kp] = {z.., z.., m.., m..}.  Each target keeps
+// an {even, odd} pair of partial sums.  SELF: target ts skips the source in its own lane slot.
+template <int T, bool SELF>
+__device__ __forceinline__ void chunk_pairs(const float4 *sa, const float4 *sb, const f2x (&tx)[T], const f2x (&ty)[T],
+                                            const f2x (&tz)[T], f2x e2, f2x (&acc)[T], int ts, int lane) {
+#pragma unroll 4
+    for (int kp = 0; kp < 16; ++kp) {
+        const float4 a = sa[kp], b = sb[kp];
+        const f2x X = pack2(a.x, a.y), Y = pack2(a.z, a.w), Z = pack2(b.x, b.y), M = pack2(b.z, b.w);
+#pragma unroll
+        for (int t = 0; t < T; ++t) {
+            const f2x dx = sub2(X, tx[t]), dy = sub2(Y, ty[t]), dz = sub2(Z, tz[t]);
+            f2x r2 = fma2(dz, dz, e2);
+            r2 = fma2(dy, dy, r2);
+            r2 = fma2(dx, dx, r2);
+            float r0, r1;
+            unpack2(r2, r0, r1);
+            float i0 = rsqrt_ftz(r0), i1 = rsqrt_ftz(r1);
+            if (SELF && t == ts && kp == (lane >> 1)) {
+                if (lane & 1) i1 = 0.f;
+                else i0 = 0.f;
+            }
+            acc[t] = fma2(M, pack2(i0, i1), acc[t]);
+        }
+    }
+}
+
+// One work item: 32*T target slots of one halo against source chunks [c_begin, c_end).
 template <int T>
 __device__ __forceinline__ void pair_item(const float4 *__restrict__ pk, int64_t base, int nb, int tile, float eps2,
                                           int c_begin, int c_end, double *__restrict__ out, float4 *buf, int lane) {
     {
-        float px[T], py[T], pz[T], sum[T], comp[T];
+        f2x tx[T], ty[T], tz[T];
+        float sum[T], comp[T];
 #pragma unroll
         for (int t = 0; t < T; ++t) {
             const int r = tile * 32 * T + t * 32 + lane;
             const float4 p = r < nb ? pk[base + r] : make_float4(kFar, kFar, kFar, 0.f);
-            px[t] = p.x; py[t] = p.y; pz[t] = p.z;
-            sum[t] = 0.f; comp[t] = 0.f;
+            tx[t] = pack2(p.x, p.x);
+            ty[t] = pack2(p.y, p.y);
+            tz[t] = pack2(p.z, p.z);
+            sum[t] = 0.f;
+            comp[t] = 0.f;
         }
+        const f2x e2 = pack2(eps2, eps2);
+        float *sa = reinterpret_cast<float *>(buf);        // 16 float4: x/y pairs
+        float *sb = reinterpret_cast<float *>(buf + 16);   // 16 float4: z/m pairs
+        const int kp = lane >> 1, hf = lane & 1;
         const int self0 = tile * T;   // chunk c holds the self slot of target t = c - self0
         float4 nxt = pk[base + (int64_t)c_begin * 32 + lane];
         for (int c = c_begin; c < c_end; ++c) {
             __syncwarp();
-            buf[lane] = nxt;
+            sa[kp * 4 + hf] = nxt.x;
+            sa[kp * 4 + 2 + hf] = nxt.y;
+            sb[kp * 4 + hf] = nxt.z;
+            sb[kp * 4 + 2 + hf] = nxt.w;
             __syncwarp();
             if (c + 1 < c_end) nxt = pk[base + (int64_t)(c + 1) * 32 + lane];
-            float part[T];
+            f2x acc[T];
 #pragma unroll
-            for (int t = 0; t < T; ++t) part[t] = 0.f;
+            for (int t = 0; t < T; ++t) acc[t] = pack2(0.f, 0.f);
             const int ts = c - self0;
-            if (ts >= 0 && ts < T) {
-                for (int k = 0; k < 32; ++k) {
-                    const float4 q = buf[k];
+            if (ts >= 0 && ts < T)
+                chunk_pairs<T, true>(buf, buf + 16, tx, ty, tz, e2, acc, ts, lane);
+            else
+                chunk_pairs<T, false>(buf, buf + 16, tx, ty, tz, e2, acc, ts, lane);
 #pragma unroll
-                    for (int t = 0; t < T; ++t) {
-                        const float v = pair_term_fast(q, px[t], py[t], pz[t], eps2, part[t]);
-                        part[t] = (t == ts && k == lane) ? part[t] : v;
-                    }
-                }
-            } else {
-#pragma unroll 8
-                for (int k = 0; k < 32; ++k) {
-                    const float4 q = buf[k];
-#pragma unroll
-                    for (int t = 0; t < T; ++t) part[t] = pair_term_fast(q, px[t], py[t], pz[t], eps2, part[t]);
-                }
+            for (int t = 0; t < T; ++t) {
+                float a0, a1;
+                unpack2(acc[t], a0, a1);
+                two_sum_acc(sum[t], comp[t], a0 + a1);
             }
-#pragma unroll
-            for (int t = 0; t < T; ++t) two_sum_acc(sum[t], comp[t], part[t]);
         }
 #pragma unroll
         for (int t = 0; t < T; ++t) {
