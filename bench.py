@@ -36,7 +36,10 @@ WORKLOAD = dict(workload="plummer-2M-500sph-15pc-contaminants", particles=2_000_
                 contaminant_frac=0.15, background_frac=0.10, linking_length_kpc=1.5, min_members=50,
                 softening_kpc=0.1, max_passes=30)
 FLOPS_PER_PAIR = 20          # conventional N-body count (rsqrt counted as several flops)
-MUFU_PAIRS_PER_CLK_SM = 16   # one rsqrt per pair; 16 special-function results / clock / SM
+# The pair term needs 7 FP32 lane-operations (3 sub, 3 fma for r^2, 1 fma to accumulate) and one
+# rsqrt.  The FP32 pipe does 128 lane-operations per clock per SM; ncu shows the special-
+# function pipe at 42 % when the FP32 pipe is at 76 %, so the FP32 pipe binds:
+FP32_PAIRS_PER_CLK_SM = 128.0 / 7.0
 FOF_BYTES_PER_PARTICLE = 28  # FP64 xyz read once + int32 label written once
 
 
@@ -313,17 +316,17 @@ def run_gpu(args):
 
     hbm, sm_max, src = peaks()
     sms = torch.cuda.get_device_properties(dev).multi_processor_count
-    pair_peak = MUFU_PAIRS_PER_CLK_SM * sms * sm_max * 1e6 * FLOPS_PER_PAIR / 1e12
+    pair_peak = FP32_PAIRS_PER_CLK_SM * sms * sm_max * 1e6 * FLOPS_PER_PAIR / 1e12
     n_pair_launches = sum(passes)
     achieved = FLOPS_PER_PAIR * pairs / (pair_ms * 1e-3) / 1e12 if pair_ms > 0 else 0.0
     traffic = None
     tp = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(tp):
         traffic = json.load(open(tp)).get("ub_pair_kernel_bytes_per_launch")
-    roofline = {"bound": "sfu", "kernel": "ub_pair_kernel", "achieved": achieved, "peak": pair_peak,
+    roofline = {"bound": "fp32", "kernel": "ub_pair_kernel", "achieved": achieved, "peak": pair_peak,
                 "unit": "TFLOP/s", "frac": achieved / pair_peak if pair_peak else None, "traffic": traffic,
-                "peak_source": f"{MUFU_PAIRS_PER_CLK_SM} rsqrt/clk/SM x {sms} SMs x {sm_max:.0f} MHz "
-                               f"(sm_max_mhz {src}) x {FLOPS_PER_PAIR} flops/pair",
+                "peak_source": f"FP32 pipe: 128 lane-ops/clk/SM / 7 per pair x {sms} SMs x {sm_max:.0f} MHz "
+                               f"(sm_max_mhz {src}) x {FLOPS_PER_PAIR} flops/pair (conventional count)",
                 "pairs_per_launch": pairs / max(n_pair_launches, 1), "ms_per_launch": pair_ms / max(n_pair_launches, 1),
                 "launches_timed": n_pair_launches}
     fof_gbs = FOF_BYTES_PER_PARTICLE * n / (statistics.mean(fof_ms) * 1e-3) / 1e9
