@@ -109,6 +109,21 @@ int halma_bf_potential_f32(int64_t ntotal, const float *total_mass, const float 
 #define HALMA_MASK_SELF  1   /* skip source j == i + self_offset only                   */
 #define HALMA_MASK_NONE  2
 
+/* Allocation-free twin of halma_bf_potential_f32 in HALMA_POT_FAST mode (no counterpart in
+ * the reference).  For callers that cannot allocate device memory when they need the
+ * potential — code running while its stream is captured into a CUDA graph (cudaMalloc is not
+ * allowed during capture) and host applications whose own pool owns all device memory.  It
+ * takes device arrays only, calls no cudaMalloc/cudaFree, and keeps its scratch (the partial
+ * sums of the source slices) in a 16 MiB static device array held by every GPU that loads the
+ * library.  Same source split and same results as halma_bf_potential_f32(HALMA_POT_FAST);
+ * returns HALMA_ERR_CAPACITY when the split needs more than 2,097,152 partial sums (source
+ * slices x targets).  The first call on a device looks up the array's address: make it before
+ * any stream capture.  Calls share the array: calls that overlap on the GPU race. */
+int halma_bf_potential_f32_noalloc(int64_t ntotal, const float *total_mass, const float *total_x,
+                                   const float *total_y, const float *total_z, int64_t ntest,
+                                   const float *test_x, const float *test_y, const float *test_z,
+                                   float *binding_energy, double eps2, halma_stream_t stream);
+
 /* float32 pair terms (rsqrt) with compensated sums and a selectable mask: the smooth
  * (differentiable) forward of halma_potential_grad_f32 when mask is SELF or NONE.
  * No reference counterpart beyond the potential above. */

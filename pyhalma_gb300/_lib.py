@@ -71,6 +71,7 @@ SIGNATURES = {
     "halma_bf_potential_f32": ([_I64, _P, _P, _P, _P, _I64, _P, _P, _P, _P, _I32, _F64, _P], ctypes.c_int),
     "halma_potential_f64": ([_I64, _P, _P, _P, _P, _I64, _P, _P, _P, _F64, _I32, _I64, _P, _P], ctypes.c_int),
     "halma_potential_f32": ([_I64, _P, _P, _P, _P, _I64, _P, _P, _P, _F64, _I32, _I64, _P, _P], ctypes.c_int),
+    "halma_bf_potential_f32_noalloc": ([_I64, _P, _P, _P, _P, _I64, _P, _P, _P, _P, _F64, _P], ctypes.c_int),
     "halma_potential_grad_f32": ([_I64, _P, _P, _P, _P, _I64, _P, _P, _P, _P, _F64, _I32, _I64, _P, _P, _P, _P],
                                  ctypes.c_int),
     "halma_halo_reductions": ([_I64, _I64, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P], ctypes.c_int),

@@ -344,3 +344,86 @@ extern "C" int halma_potential_f64(int64_t ns, const double *mm, const double *s
                  eps2, (int)mask, self_offset, out);
     return sg.download(st);
 }
+
+// ---------------------------------------------------------------------------------------
+// Allocation-free variant of the fast (compensated FP32) potential.
+//
+// Some callers cannot allocate device memory at the moment they need the potential: code
+// that runs while its stream is being captured into a CUDA graph (cudaMalloc is not allowed
+// during capture), and host applications that own every byte of device memory through their
+// own pool and forbid libraries from calling cudaMalloc/cudaFree behind their back.  This
+// entry point serves them: it takes device arrays only and keeps its scratch — the per-slice
+// partial sums of the source-split kernel — in the fixed array below instead of the library's
+// cached workspace.
+//
+// Limit: the scratch holds kNoAllocScratchDoubles = 2,097,152 partial sums (16 MiB).  The call
+// splits the sources exactly as halma_bf_potential_f32 does in HALMA_POT_FAST mode (so the two
+// return the same values); when that split needs more than 2,097,152 partial sums
+// (source slices x targets) the call is rejected with HALMA_ERR_CAPACITY.
+//
+// Every GPU that loads this library holds the 16 MiB array until the process exits.  All calls
+// share it and it keeps the previous call's contents; each partial sum a call reads is written
+// by the same call first, so nothing needs clearing.  Calls that overlap on the GPU (two
+// streams, or two host threads without ordering) race on the array and give wrong results.
+// The first call on each device looks up the array's device address (cudaGetSymbolAddress with
+// that device current); make that first call before any stream capture begins.
+constexpr int64_t kNoAllocScratchDoubles = 1ll << 21;
+static __device__ __align__(256) double g_noalloc_scratch[kNoAllocScratchDoubles];
+
+namespace {
+constexpr int kMaxDevices = 64;
+std::mutex g_noalloc_mutex;
+double *g_noalloc_ptr[kMaxDevices] = {};
+
+// Device address of g_noalloc_scratch on the current device (looked up once per device).
+int noalloc_scratch(double **out) {
+    const int dev = current_device();
+    if (dev < 0 || dev >= kMaxDevices) return fail(HALMA_ERR_CAPACITY, "device ordinal %d out of range", dev);
+    std::lock_guard<std::mutex> g(g_noalloc_mutex);
+    if (!g_noalloc_ptr[dev]) {
+        void *p = nullptr;
+        HALMA_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+        g_noalloc_ptr[dev] = static_cast<double *>(p);
+    }
+    *out = g_noalloc_ptr[dev];
+    return HALMA_OK;
+}
+}  // namespace
+
+extern "C" int halma_bf_potential_f32_noalloc(int64_t ntotal, const float *total_mass, const float *total_x,
+                                              const float *total_y, const float *total_z, int64_t ntest,
+                                              const float *test_x, const float *test_y, const float *test_z,
+                                              float *binding_energy, double eps2, halma_stream_t stream) {
+    if (ntotal < 0 || ntest < 0) return fail(HALMA_ERR_INVALID, "negative size");
+    if (ntest == 0) return HALMA_OK;
+    if (!binding_energy || !test_x || !test_y || !test_z) return fail(HALMA_ERR_INVALID, "null target/output pointer");
+    if (ntotal > 0 && (!total_mass || !total_x || !total_y || !total_z)) return fail(HALMA_ERR_INVALID, "null source pointer");
+    if (!(eps2 >= 0.0) || !isfinite(eps2)) return fail(HALMA_ERR_INVALID, "eps2 must be finite and >= 0");
+    const void *arrays[8] = {test_x, test_y, test_z, binding_energy, total_mass, total_x, total_y, total_z};
+    for (int k = 0; k < (ntotal > 0 ? 8 : 4); ++k)
+        if (!is_device_pointer(arrays[k]))
+            return fail(HALMA_ERR_INVALID, "the allocation-free entry point takes device arrays only");
+    cudaStream_t st = (cudaStream_t)stream;
+    if (ntotal == 0) {
+        HALMA_CUDA(cudaMemsetAsync(binding_energy, 0, sizeof(float) * ntest, st));
+        return HALMA_OK;
+    }
+    constexpr int T = 4;
+    int n_split = 1;
+    int64_t split_len = ntotal;
+    choose_split(ntotal, ntest, T, &n_split, &split_len);
+    if (n_split > 1 && (int64_t)n_split * ntest > kNoAllocScratchDoubles)
+        return fail(HALMA_ERR_CAPACITY,
+                    "this call needs %lld partial sums (%d source slices x %lld targets); the allocation-free "
+                    "scratch holds %lld — use halma_bf_potential_f32",
+                    (long long)n_split * ntest, n_split, (long long)ntest, (long long)kNoAllocScratchDoubles);
+    double *scratch = nullptr;
+    HALMA_TRY(noalloc_scratch(&scratch));
+    double *partial = n_split > 1 ? scratch : nullptr;
+    HALMA_TRY(launch_fast<T>(total_mass, total_x, total_y, total_z, ntotal, test_x, test_y, test_z, ntest,
+                             (float)eps2, n_split, split_len, HALMA_MASK_COORD, 0, binding_energy, partial, st));
+    if (n_split > 1)
+        HALMA_LAUNCH(reduce_partials_kernel, grid_for(ntest, 256, 4096), 256, 0, st, partial, n_split, ntest,
+                     binding_energy);
+    return HALMA_OK;
+}
