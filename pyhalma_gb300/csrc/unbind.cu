@@ -356,47 +356,114 @@ __global__ void __launch_bounds__(256) ub_pair_kernel(const float4 *__restrict__
     }
 }
 
-// FP64 energies, sign test and removal counts (one block per active halo).
+// FP64 energies and sign test of one pass (one block per active halo), fused with the
+// bookkeeping of the next pass: the survivors are compacted in place, in their order, in the
+// packed slots (positions stay re-centred on the first pass's centre), the padding after them
+// is rewritten, and their FP64 mass, centre of mass and bulk velocity become the halo state of
+// the next pass.  A halo whose pass removed nothing becomes inactive.
+template <class V>
 __global__ void __launch_bounds__(256) ub_energy_kernel(const int64_t *__restrict__ poff, const int64_t *__restrict__ qoff,
-                                                        int slice_len, const int *__restrict__ pidx,
-                                                        const double *__restrict__ part, const double *__restrict__ vx,
-                                                        const double *__restrict__ vy, const double *__restrict__ vz,
-                                                        const double *__restrict__ m, double gfac,
-                                                        unsigned char *__restrict__ bound, double *__restrict__ phi_out,
-                                                        HaloState *hs) {
+                                                        int slice_len, V *pk, int *pidx,
+                                                        const double *__restrict__ part, const double *__restrict__ x,
+                                                        const double *__restrict__ y, const double *__restrict__ z,
+                                                        const double *__restrict__ vx, const double *__restrict__ vy,
+                                                        const double *__restrict__ vz, const double *__restrict__ m,
+                                                        double gfac, unsigned char *__restrict__ bound,
+                                                        double *__restrict__ phi_out, HaloState *hs) {
     const int h = blockIdx.x;
     if (!hs[h].active) return;
-    __shared__ double sh[3][32];
+    __shared__ double sh[11][32];
+    __shared__ int wcount[8];
+    __shared__ int running;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const HaloState s = hs[h];
     const int64_t pb = poff[h], npad = poff[h + 1] - pb, qb = qoff[h];
     const int nsl = (int)(((int64_t)s.nb + slice_len - 1) / slice_len);
-    double v[3] = {0, 0, 0};   // removed, ekin (kept), epot (kept)
-    for (int r = threadIdx.x; r < s.nb; r += blockDim.x) {
-        const int i = pidx[pb + r];
-        const double dvx = vx[i] - s.vx, dvy = vy[i] - s.vy, dvz = vz[i] - s.vz;
-        const double ek = 0.5 * (dvx * dvx + dvy * dvy + dvz * dvz);
-        double p = 0.0;
-        for (int q = 0; q < nsl; ++q) p += part[qb + (int64_t)q * npad + r];   // slices in order
-        const double e = ek - gfac * p;
-        const double mi = m[i];
-        if (e > 0.0) {
-            bound[i] = 0;
-            v[0] += 1.0;
-            if (phi_out) phi_out[i] = 0.0;
-        } else {
-            v[1] += mi * ek;
-            v[2] += mi * p;
-            if (phi_out) phi_out[i] = p;
+    // removed, ekin, epot | next pass: M, Mx, My, Mz, Mvx, Mvy, Mvz, n
+    double v[11] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+    if (threadIdx.x == 0) running = 0;
+    __syncthreads();
+    for (int r0 = 0; r0 < s.nb; r0 += blockDim.x) {
+        const int r = r0 + threadIdx.x;
+        bool keep = false;
+        V slot;
+        int i = -1;
+        if (r < s.nb) {
+            i = pidx[pb + r];
+            slot = pk[pb + r];
+            const double dvx = vx[i] - s.vx, dvy = vy[i] - s.vy, dvz = vz[i] - s.vz;
+            const double ek = 0.5 * (dvx * dvx + dvy * dvy + dvz * dvz);
+            double p = 0.0;
+            for (int q = 0; q < nsl; ++q) p += part[qb + (int64_t)q * npad + r];   // slices in order
+            const double e = ek - gfac * p;
+            const double mi = m[i];
+            keep = !(e > 0.0);
+            if (!keep) {
+                bound[i] = 0;
+                v[0] += 1.0;
+                if (phi_out) phi_out[i] = 0.0;
+            } else {
+                v[1] += mi * ek;
+                v[2] += mi * p;
+                if (phi_out) phi_out[i] = p;
+                v[3] += mi;
+                v[4] += mi * x[i];
+                v[5] += mi * y[i];
+                v[6] += mi * z[i];
+                v[7] += mi * vx[i];
+                v[8] += mi * vy[i];
+                v[9] += mi * vz[i];
+                v[10] += 1.0;
+            }
         }
+        // stable in-place compaction of the survivors (every read of this chunk happens
+        // before any write: writes land at ranks <= the positions being read)
+        const unsigned bal = __ballot_sync(0xffffffffu, keep);
+        if (lane == 0) wcount[w] = __popc(bal);
+        __syncthreads();
+        int rank = running;
+        for (int q = 0; q < w; ++q) rank += wcount[q];
+        rank += __popc(bal & ((1u << lane) - 1u));
+        __syncthreads();
+        if (keep) {
+            pk[pb + rank] = slot;
+            pidx[pb + rank] = i;
+        }
+        if (threadIdx.x == 0) {
+            int tot = 0;
+            for (int q = 0; q < (int)(blockDim.x >> 5); ++q) tot += wcount[q];
+            running += tot;
+        }
+        __syncthreads();
     }
-    block_sum<3>(v, sh);
+    const int nkeep = running;
+    for (int r = nkeep + threadIdx.x; r < ((nkeep + 31) & ~31); r += blockDim.x) {
+        V f;
+        f.x = f.y = f.z = kFar;
+        f.w = 0;
+        pk[pb + r] = f;
+        pidx[pb + r] = -1;
+    }
+    block_sum<11>(v, sh);
     if (threadIdx.x == 0) {
         HaloState &o = hs[h];
         o.removed = (int)v[0];
         o.iter += 1;
         o.ekin = v[1];
         o.epot = -0.5 * gfac * v[2];
-        if (v[0] == 0.0) o.active = 0;
+        if (v[0] == 0.0) {
+            o.active = 0;
+        } else {
+            const double M = v[3];
+            o.M = M;
+            o.nb = nkeep;
+            if (M > 0) {
+                o.cx = v[4] / M; o.cy = v[5] / M; o.cz = v[6] / M;
+                o.vx = v[7] / M; o.vy = v[8] / M; o.vz = v[9] / M;
+            } else {
+                o.cx = o.cy = o.cz = o.vx = o.vy = o.vz = 0.0;
+            }
+        }
     }
 }
 
@@ -554,9 +621,11 @@ int unbind_device(int64_t n, int nh, const int64_t *d_off, const int64_t *h_off,
         HALMA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, ub_pair_kernel, 256, 0));
         const int pgrid = device_sm_count() * std::max(bps, 1);
         auto record = [&](cudaStream_t rs) -> int {
+            // first pass: centre of mass and packing; later passes are kept up to date by the
+            // energy kernel (compaction + next-pass sums)
+            HALMA_LAUNCH(ub_reduce_kernel, nh, 256, 0, rs, off, x, y, z, vx, vy, vz, m, bound, hs, 0);
+            HALMA_LAUNCH(ub_pack_kernel<float4>, nh, 256, 0, rs, off, dpoff, x, y, z, m, bound, hs, pk, pidx);
             for (int it = 0; it < p.max_iter; ++it) {
-                HALMA_LAUNCH(ub_reduce_kernel, nh, 256, 0, rs, off, x, y, z, vx, vy, vz, m, bound, hs, 0);
-                HALMA_LAUNCH(ub_pack_kernel<float4>, nh, 256, 0, rs, off, dpoff, x, y, z, m, bound, hs, pk, pidx);
                 HALMA_LAUNCH(ub_items_kernel, 1, 1024, 0, rs, nh, dorder, hs, tab, slice_len, istart, idesc, cnt,
                              cnt + 1, profiling ? dpairs + it : nullptr);
                 // External: captured as an event-record node, so the replay records it
@@ -564,8 +633,8 @@ int unbind_device(int64_t n, int nh, const int64_t *d_off, const int64_t *h_off,
                 HALMA_LAUNCH(ub_pair_kernel, pgrid, 256, 0, rs, pk, dpoff, dqoff, hs, nh, istart, idesc, cnt, cnt + 1,
                              eps2, slice_len / 32, phi);
                 if (profiling) HALMA_CUDA(cudaEventRecordWithFlags(prof.ev1[it], rs, cudaEventRecordExternal));
-                HALMA_LAUNCH(ub_energy_kernel, nh, 256, 0, rs, dpoff, dqoff, slice_len, pidx, phi, vx, vy, vz, m, gfac,
-                             bound, phi_out, hs);
+                HALMA_LAUNCH(ub_energy_kernel<float4>, nh, 256, 0, rs, dpoff, dqoff, slice_len, pk, pidx, phi, x, y, z,
+                             vx, vy, vz, m, gfac, bound, phi_out, hs);
             }
             return HALMA_OK;
         };
@@ -640,9 +709,9 @@ int unbind_device(int64_t n, int nh, const int64_t *d_off, const int64_t *h_off,
         // plain FP64 path: per pass, one pair launch per active halo, host checks convergence
         auto *pk = at<double4>(base, o_pk);
         std::vector<HaloState> hh(nh);
+        HALMA_LAUNCH(ub_reduce_kernel, nh, 256, 0, st, off, x, y, z, vx, vy, vz, m, bound, hs, 0);
+        HALMA_LAUNCH(ub_pack_kernel<double4>, nh, 256, 0, st, off, dpoff, x, y, z, m, bound, hs, pk, pidx);
         for (int it = 0; it < p.max_iter; ++it) {
-            HALMA_LAUNCH(ub_reduce_kernel, nh, 256, 0, st, off, x, y, z, vx, vy, vz, m, bound, hs, 0);
-            HALMA_LAUNCH(ub_pack_kernel<double4>, nh, 256, 0, st, off, dpoff, x, y, z, m, bound, hs, pk, pidx);
             HALMA_CUDA(cudaMemcpyAsync(hh.data(), hs, sizeof(HaloState) * nh, cudaMemcpyDeviceToHost, st));
             HALMA_CUDA(cudaStreamSynchronize(st));
             int any = 0;
@@ -652,9 +721,9 @@ int unbind_device(int64_t n, int nh, const int64_t *d_off, const int64_t *h_off,
                 HALMA_LAUNCH(ub_pair_f64_kernel, grid_for(hh[h].nb, 256), 256, 0, st, pk + poff[h], hh[h].nb,
                              p.eps * p.eps, phi + poff[h]);
             }
-            HALMA_LAUNCH(ub_energy_kernel, nh, 256, 0, st, dpoff, dqoff, slice_len, pidx, phi, vx, vy, vz, m, gfac,
-                         bound, phi_out, hs);
             if (!any) break;
+            HALMA_LAUNCH(ub_energy_kernel<double4>, nh, 256, 0, st, dpoff, dqoff, slice_len, pk, pidx, phi, x, y, z, vx,
+                         vy, vz, m, gfac, bound, phi_out, hs);
         }
         HALMA_LAUNCH(ub_reduce_kernel, nh, 256, 0, st, off, x, y, z, vx, vy, vz, m, bound, hs, 1);
     }
