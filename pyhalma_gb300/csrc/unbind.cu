@@ -2,17 +2,20 @@
 //
 // The single pass is pyHALMA's escape cut (python_scripts/halo_properties.py:282-361):
 //     E_i = 1/2 |v_i - v_bulk|^2 - G * factor_v^2 * phi_i,   bound iff E_i <= 0
-// repeated until a pass removes nothing.  One pass over all haloes is five kernels:
-//   reduce  - per active halo, FP64 bound mass, centre of mass and bulk velocity;
-//   pack    - bound particles re-centred on their halo's centre, float4 (x, y, z, m),
-//             padded to a multiple of 32 with zero-mass far points (halo-contiguous);
-//   items   - one work item per (halo, tile of 32*T targets), biggest haloes first;
-//   pairs   - persistent kernel: warps take items from an atomic counter, stream the
-//             halo's sources through a per-warp shared-memory chunk, FP32 rsqrt pair terms,
-//             32-term FP32 partials folded into a TwoSum-compensated accumulator; the self
-//             pair is skipped by slot index;
-//   energy  - FP64 energy and sign test per bound particle, removals counted per halo;
-//             a halo whose pass removed nothing becomes inactive and costs nothing later.
+// repeated until a pass removes nothing.  Before the first pass:
+//   reduce  - per halo, FP64 mass, centre of mass and bulk velocity;
+//   pack    - members re-centred on their halo's centre, float4 (x, y, z, m), padded to a
+//             multiple of 32 with zero-mass far points (halo-contiguous slots).
+// Every pass over all active haloes is then five kernels:
+//   items   - the implicit work list: per halo, (target tile of 32*T) x (source slice) items,
+//             biggest haloes first, and the energy segments of the pass;
+//   pairs   - persistent kernel: warps take items from an atomic counter, stream the slice's
+//             sources through a per-warp shared-memory chunk, two sources per f32x2
+//             instruction, 32-term FP32 partials folded into a TwoSum-compensated
+//             accumulator; the self pair is skipped by slot index;
+//   energy / compact / finalize - FP64 energy and sign test, survivors compacted into the
+//             other packed buffer, next pass's FP64 centre and bulk velocity; a halo whose pass
+//             removed nothing becomes inactive and costs nothing later.
 // All passes are captured once into a CUDA graph and replayed (cached by shape).
 #include <math.h>
 #include <string.h>
@@ -174,23 +177,37 @@ __device__ __forceinline__ int tile_t_for(const TileTable &tab, int nb) {
 // The work list is implicit: ordered halo q owns items istart[q] .. istart[q+1]-1, described
 // by idesc[q] = (halo, T, slices, unused); item i of that halo is (tile i / slices,
 // slice i % slices).  Only nh+1 prefix counts are written per pass.
+// The same pass also lays out the energy segments: active ordered halo q owns segments
+// sstart[q] .. sstart[q+1]-1 of kSeg slots each.
+constexpr int kSeg = 1024;
+
+__device__ __forceinline__ int warp_incl_scan(int v, int lane) {
+    for (int o = 1; o < 32; o <<= 1) {
+        const int u = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o) v += u;
+    }
+    return v;
+}
+
 __global__ void __launch_bounds__(1024) ub_items_kernel(int nh, const int *__restrict__ order, const HaloState *hs,
                                                         TileTable tab, int slice_len, int *__restrict__ istart,
-                                                        int4 *__restrict__ idesc, int *__restrict__ nitems,
-                                                        int *__restrict__ counter,
+                                                        int4 *__restrict__ idesc, int *__restrict__ sstart,
+                                                        int *__restrict__ nitems, int *__restrict__ counter,
+                                                        int *__restrict__ nsegs,
                                                         unsigned long long *__restrict__ pairs_out) {
-    __shared__ int wsum[32];
-    __shared__ int base;
+    __shared__ int wsum[32], wseg[32];
+    __shared__ int base, sbase;
     __shared__ unsigned long long pairs;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     if (threadIdx.x == 0) {
         base = 0;
+        sbase = 0;
         pairs = 0;
     }
     __syncthreads();
     for (int h0 = 0; h0 < nh; h0 += blockDim.x) {
         const int q = h0 + threadIdx.x;
-        int h = -1, cnt = 0, T = 4, nsl = 1;
+        int h = -1, cnt = 0, T = 4, nsl = 1, nseg = 0;
         if (q < nh) {
             h = order[q];
             if (hs[h].active) {
@@ -198,36 +215,58 @@ __global__ void __launch_bounds__(1024) ub_items_kernel(int nh, const int *__res
                 T = tile_t_for(tab, nb);
                 nsl = (int)(((int64_t)nb + slice_len - 1) / slice_len);
                 cnt = ((nb + 32 * T - 1) / (32 * T)) * nsl;
+                nseg = max(1, (nb + kSeg - 1) / kSeg);
                 if (nb > 0) atomicAdd(&pairs, (unsigned long long)nb * (unsigned long long)nb);
             }
         }
-        int incl = cnt;
-        for (int o = 1; o < 32; o <<= 1) {
-            const int u = __shfl_up_sync(0xffffffffu, incl, o);
-            if (lane >= o) incl += u;
+        const int incl = warp_incl_scan(cnt, lane);
+        const int sincl = warp_incl_scan(nseg, lane);
+        if (lane == 31) {
+            wsum[w] = incl;
+            wseg[w] = sincl;
         }
-        if (lane == 31) wsum[w] = incl;
         __syncthreads();
-        int pre = base;
-        for (int k = 0; k < w; ++k) pre += wsum[k];
+        int pre = base, spre = sbase;
+        for (int k = 0; k < w; ++k) {
+            pre += wsum[k];
+            spre += wseg[k];
+        }
         if (q < nh) {
             istart[q] = pre + incl - cnt;
             idesc[q] = make_int4(h, T, max(nsl, 1), 0);
+            sstart[q] = spre + sincl - nseg;
         }
         __syncthreads();
         if (threadIdx.x == 0) {
-            int tot = 0;
-            for (int k = 0; k < (int)(blockDim.x >> 5); ++k) tot += wsum[k];
+            int tot = 0, stot = 0;
+            for (int k = 0; k < (int)(blockDim.x >> 5); ++k) {
+                tot += wsum[k];
+                stot += wseg[k];
+            }
             base += tot;
+            sbase += stot;
         }
         __syncthreads();
     }
     if (threadIdx.x == 0) {
         istart[nh] = base;
+        sstart[nh] = sbase;
         *nitems = base;
         *counter = 0;
+        *nsegs = sbase;
         if (pairs_out) *pairs_out = pairs;
     }
+}
+
+// Ordered halo owning work unit u: the last q with start[q] <= u.
+__device__ __forceinline__ int owner_of(const int *__restrict__ start, int nh, int u) {
+    int lo = 0, hi = nh - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (start[mid] <= u) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
 }
 
 // 32 sources of the staged chunk against T targets, two sources per f32x2 instruction.
@@ -356,110 +395,155 @@ __global__ void __launch_bounds__(256) ub_pair_kernel(const float4 *__restrict__
     }
 }
 
-// FP64 energies and sign test of one pass (one block per active halo), fused with the
-// bookkeeping of the next pass: the survivors are compacted in place, in their order, in the
-// packed slots (positions stay re-centred on the first pass's centre), the padding after them
-// is rewritten, and their FP64 mass, centre of mass and bulk velocity become the halo state of
-// the next pass.  A halo whose pass removed nothing becomes inactive.
+// The end of a pass runs in three wide kernels over energy segments (kSeg packed slots of one
+// halo each), so a big halo is spread over many blocks:
+//   energy  - FP64 energy and sign test of every slot of the segment; removed particles are
+//             marked; per-segment FP64 sums of the survivors (mass, mass-weighted position and
+//             velocity, count) and of the pass's kinetic / potential energy;
+//   compact - survivors copied, in order, into the other packed buffer at the halo's running
+//             offset (positions stay re-centred on the first pass's centre); padding rewritten;
+//   finalize- per halo, segment sums added in segment order (deterministic): removals, pass
+//             count, energies, and the next pass's mass, centre and bulk velocity.  A halo whose
+//             pass removed nothing becomes inactive.
+constexpr int kSegSums = 12;   // removed, kept, ekin, epot, M, Mx, My, Mz, Mvx, Mvy, Mvz, unused
+
 template <class V>
-__global__ void __launch_bounds__(256) ub_energy_kernel(const int64_t *__restrict__ poff, const int64_t *__restrict__ qoff,
-                                                        int slice_len, V *pk, int *pidx,
-                                                        const double *__restrict__ part, const double *__restrict__ x,
-                                                        const double *__restrict__ y, const double *__restrict__ z,
-                                                        const double *__restrict__ vx, const double *__restrict__ vy,
-                                                        const double *__restrict__ vz, const double *__restrict__ m,
-                                                        double gfac, unsigned char *__restrict__ bound,
-                                                        double *__restrict__ phi_out, HaloState *hs) {
-    const int h = blockIdx.x;
-    if (!hs[h].active) return;
-    __shared__ double sh[11][32];
-    __shared__ int wcount[8];
-    __shared__ int running;
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+__global__ void __launch_bounds__(256) ub_energy_seg_kernel(int nh, const int *__restrict__ sstart,
+                                                            const int4 *__restrict__ idesc, const int *__restrict__ nsegs,
+                                                            const int64_t *__restrict__ poff, const int64_t *__restrict__ qoff,
+                                                            int slice_len, const int *__restrict__ pidx,
+                                                            const double *__restrict__ part, const double *__restrict__ x,
+                                                            const double *__restrict__ y, const double *__restrict__ z,
+                                                            const double *__restrict__ vx, const double *__restrict__ vy,
+                                                            const double *__restrict__ vz, const double *__restrict__ m,
+                                                            double gfac, const HaloState *__restrict__ hs,
+                                                            unsigned char *__restrict__ bound, double *__restrict__ phi_out,
+                                                            unsigned char *__restrict__ keepf,
+                                                            double *__restrict__ seg_sums) {
+    const int seg = blockIdx.x;
+    if (seg >= *nsegs) return;
+    __shared__ double sh[kSegSums][32];
+    const int q = owner_of(sstart, nh, seg);
+    const int h = idesc[q].x;
+    const int sl = seg - sstart[q];
     const HaloState s = hs[h];
     const int64_t pb = poff[h], npad = poff[h + 1] - pb, qb = qoff[h];
     const int nsl = (int)(((int64_t)s.nb + slice_len - 1) / slice_len);
-    // removed, ekin, epot | next pass: M, Mx, My, Mz, Mvx, Mvy, Mvz, n
-    double v[11] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
-    if (threadIdx.x == 0) running = 0;
-    __syncthreads();
-    for (int r0 = 0; r0 < s.nb; r0 += blockDim.x) {
-        const int r = r0 + threadIdx.x;
-        bool keep = false;
-        V slot;
-        int i = -1;
-        if (r < s.nb) {
-            i = pidx[pb + r];
-            slot = pk[pb + r];
-            const double dvx = vx[i] - s.vx, dvy = vy[i] - s.vy, dvz = vz[i] - s.vz;
-            const double ek = 0.5 * (dvx * dvx + dvy * dvy + dvz * dvz);
-            double p = 0.0;
-            for (int q = 0; q < nsl; ++q) p += part[qb + (int64_t)q * npad + r];   // slices in order
-            const double e = ek - gfac * p;
+    double v[kSegSums] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+    const int rend = min(s.nb, (sl + 1) * kSeg);
+    for (int r = sl * kSeg + threadIdx.x; r < rend; r += blockDim.x) {
+        const int i = pidx[pb + r];
+        const double dvx = vx[i] - s.vx, dvy = vy[i] - s.vy, dvz = vz[i] - s.vz;
+        const double ek = 0.5 * (dvx * dvx + dvy * dvy + dvz * dvz);
+        double p = 0.0;
+        for (int k = 0; k < nsl; ++k) p += part[qb + (int64_t)k * npad + r];   // slices in order
+        const double e = ek - gfac * p;
+        const bool keep = !(e > 0.0);
+        keepf[pb + r] = keep ? 1 : 0;
+        if (!keep) {
+            bound[i] = 0;
+            v[0] += 1.0;
+            if (phi_out) phi_out[i] = 0.0;
+        } else {
             const double mi = m[i];
-            keep = !(e > 0.0);
-            if (!keep) {
-                bound[i] = 0;
-                v[0] += 1.0;
-                if (phi_out) phi_out[i] = 0.0;
-            } else {
-                v[1] += mi * ek;
-                v[2] += mi * p;
-                if (phi_out) phi_out[i] = p;
-                v[3] += mi;
-                v[4] += mi * x[i];
-                v[5] += mi * y[i];
-                v[6] += mi * z[i];
-                v[7] += mi * vx[i];
-                v[8] += mi * vy[i];
-                v[9] += mi * vz[i];
-                v[10] += 1.0;
-            }
+            v[1] += 1.0;
+            v[2] += mi * ek;
+            v[3] += mi * p;
+            v[4] += mi;
+            v[5] += mi * x[i];
+            v[6] += mi * y[i];
+            v[7] += mi * z[i];
+            v[8] += mi * vx[i];
+            v[9] += mi * vy[i];
+            v[10] += mi * vz[i];
+            if (phi_out) phi_out[i] = p;
         }
-        // stable in-place compaction of the survivors (every read of this chunk happens
-        // before any write: writes land at ranks <= the positions being read)
+    }
+    block_sum<kSegSums>(v, sh);
+    if (threadIdx.x < kSegSums) seg_sums[(int64_t)seg * kSegSums + threadIdx.x] = v[threadIdx.x];
+}
+
+template <class V>
+__global__ void __launch_bounds__(256) ub_compact_seg_kernel(int nh, const int *__restrict__ sstart,
+                                                             const int4 *__restrict__ idesc, const int *__restrict__ nsegs,
+                                                             const int64_t *__restrict__ poff,
+                                                             const HaloState *__restrict__ hs,
+                                                             const unsigned char *__restrict__ keepf,
+                                                             const double *__restrict__ seg_sums,
+                                                             const V *__restrict__ pk_in, const int *__restrict__ pidx_in,
+                                                             V *__restrict__ pk_out, int *__restrict__ pidx_out) {
+    const int seg = blockIdx.x;
+    if (seg >= *nsegs) return;
+    __shared__ int wcount[8];
+    __shared__ int running;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int q = owner_of(sstart, nh, seg);
+    const int h = idesc[q].x;
+    const int s0 = sstart[q], sl = seg - s0, nseg = sstart[q + 1] - s0;
+    const int nb = hs[h].nb;
+    const int64_t pb = poff[h];
+    if (threadIdx.x == 0) {
+        int o = 0;   // survivors of the earlier segments of this halo
+        for (int k = 0; k < sl; ++k) o += (int)seg_sums[(int64_t)(s0 + k) * kSegSums + 1];
+        running = o;
+    }
+    __syncthreads();
+    const int rend = min(nb, (sl + 1) * kSeg);
+    for (int r0 = sl * kSeg; r0 < rend; r0 += blockDim.x) {
+        const int r = r0 + threadIdx.x;
+        const bool keep = r < rend && keepf[pb + r];
         const unsigned bal = __ballot_sync(0xffffffffu, keep);
         if (lane == 0) wcount[w] = __popc(bal);
         __syncthreads();
         int rank = running;
-        for (int q = 0; q < w; ++q) rank += wcount[q];
+        for (int k = 0; k < w; ++k) rank += wcount[k];
         rank += __popc(bal & ((1u << lane) - 1u));
-        __syncthreads();
         if (keep) {
-            pk[pb + rank] = slot;
-            pidx[pb + rank] = i;
+            pk_out[pb + rank] = pk_in[pb + r];
+            pidx_out[pb + rank] = pidx_in[pb + r];
         }
+        __syncthreads();
         if (threadIdx.x == 0) {
             int tot = 0;
-            for (int q = 0; q < (int)(blockDim.x >> 5); ++q) tot += wcount[q];
+            for (int k = 0; k < (int)(blockDim.x >> 5); ++k) tot += wcount[k];
             running += tot;
         }
         __syncthreads();
     }
-    const int nkeep = running;
-    for (int r = nkeep + threadIdx.x; r < ((nkeep + 31) & ~31); r += blockDim.x) {
-        V f;
-        f.x = f.y = f.z = kFar;
-        f.w = 0;
-        pk[pb + r] = f;
-        pidx[pb + r] = -1;
+    if (sl == nseg - 1) {   // the halo's last segment pads after the survivors
+        const int nkeep = running;
+        for (int r = nkeep + threadIdx.x; r < ((nkeep + 31) & ~31); r += blockDim.x) {
+            V f;
+            f.x = f.y = f.z = kFar;
+            f.w = 0;
+            pk_out[pb + r] = f;
+            pidx_out[pb + r] = -1;
+        }
     }
-    block_sum<11>(v, sh);
-    if (threadIdx.x == 0) {
+}
+
+__global__ void ub_finalize_kernel(int nh, const int *__restrict__ order, const int *__restrict__ sstart,
+                                   const double *__restrict__ seg_sums, double gfac, HaloState *hs) {
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < nh; q += gridDim.x * blockDim.x) {
+        const int h = order[q];
         HaloState &o = hs[h];
+        if (!o.active) continue;
+        double v[kSegSums] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+        for (int sg = sstart[q]; sg < sstart[q + 1]; ++sg)
+            for (int k = 0; k < kSegSums; ++k) v[k] += seg_sums[(int64_t)sg * kSegSums + k];
         o.removed = (int)v[0];
         o.iter += 1;
-        o.ekin = v[1];
-        o.epot = -0.5 * gfac * v[2];
+        o.ekin = v[2];
+        o.epot = -0.5 * gfac * v[3];
         if (v[0] == 0.0) {
             o.active = 0;
         } else {
-            const double M = v[3];
+            const double M = v[4];
             o.M = M;
-            o.nb = nkeep;
+            o.nb = (int)v[1];
             if (M > 0) {
-                o.cx = v[4] / M; o.cy = v[5] / M; o.cz = v[6] / M;
-                o.vx = v[7] / M; o.vy = v[8] / M; o.vz = v[9] / M;
+                o.cx = v[5] / M; o.cy = v[6] / M; o.cz = v[7] / M;
+                o.vx = v[8] / M; o.vy = v[9] / M; o.vz = v[10] / M;
             } else {
                 o.cx = o.cy = o.cz = o.vx = o.vy = o.vz = 0.0;
             }
@@ -556,13 +640,16 @@ int unbind_device(int64_t n, int nh, const int64_t *d_off, const int64_t *h_off,
     std::vector<int> order(nh);
     poff[0] = 0;
     qoff[0] = 0;
+    int64_t segcap = 0;   // energy segments at most (initial sizes)
     for (int h = 0; h < nh; ++h) {
         const int64_t c = h_off[h + 1] - h_off[h];
         const int64_t npad = ((c + 31) / 32) * 32;
         const int64_t nsl = std::max<int64_t>(1, (c + slice_len - 1) / slice_len);
         poff[h + 1] = poff[h] + npad;
         qoff[h + 1] = qoff[h] + npad * nsl;
+        segcap += std::max<int64_t>(1, (c + kSeg - 1) / kSeg);
     }
+    if (segcap >= (1ll << 31)) return fail(HALMA_ERR_CAPACITY, "too many energy segments");
     std::iota(order.begin(), order.end(), 0);
     std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
         return (h_off[a + 1] - h_off[a]) > (h_off[b + 1] - h_off[b]);
@@ -574,11 +661,15 @@ int unbind_device(int64_t n, int nh, const int64_t *d_off, const int64_t *h_off,
     const size_t o_poff = L.add(sizeof(int64_t) * (nh + 1));
     const size_t o_qoff = L.add(sizeof(int64_t) * (nh + 1));
     const size_t o_order = L.add(sizeof(int) * std::max(nh, 1));
-    const size_t o_pk = L.add((f64 ? sizeof(double4) : sizeof(float4)) * P);
-    const size_t o_pidx = L.add(sizeof(int) * P);
+    const size_t vsz = f64 ? sizeof(double4) : sizeof(float4);
+    const size_t o_pk = L.add(vsz * P), o_pk2 = L.add(vsz * P);       // packed slots, double-buffered
+    const size_t o_pidx = L.add(sizeof(int) * P), o_pidx2 = L.add(sizeof(int) * P);
+    const size_t o_keep = L.add(P);
     const size_t o_phi = L.add(sizeof(double) * Q);
     const size_t o_istart = L.add(sizeof(int) * (nh + 1));
+    const size_t o_sstart = L.add(sizeof(int) * (nh + 1));
     const size_t o_idesc = L.add(sizeof(int4) * std::max(nh, 1));
+    const size_t o_ssum = L.add(sizeof(double) * kSegSums * segcap);
     const size_t o_cnt = L.add(64);
     const size_t o_pairs = L.add(sizeof(unsigned long long) * p.max_iter);
     const size_t o_off = d_off ? 0 : L.add(sizeof(int64_t) * (nh + 1));
@@ -588,11 +679,15 @@ int unbind_device(int64_t n, int nh, const int64_t *d_off, const int64_t *h_off,
     auto *dpoff = at<int64_t>(base, o_poff);
     auto *dqoff = at<int64_t>(base, o_qoff);
     auto *dorder = at<int>(base, o_order);
-    auto *pidx = at<int>(base, o_pidx);
+    int *pidxb[2] = {at<int>(base, o_pidx), at<int>(base, o_pidx2)};
+    auto *keepf = at<unsigned char>(base, o_keep);
     auto *phi = at<double>(base, o_phi);
     auto *istart = at<int>(base, o_istart);
+    auto *sstart = at<int>(base, o_sstart);
     auto *idesc = at<int4>(base, o_idesc);
-    int *cnt = at<int>(base, o_cnt);   // [0] nitems [1] counter
+    auto *ssum = at<double>(base, o_ssum);
+    int *cnt = at<int>(base, o_cnt);   // [0] nitems [1] counter [2] energy segments
+    const int sgrid = (int)segcap;
     auto *dpairs = at<unsigned long long>(base, o_pairs);
     Profile &prof = profile();
     const bool profiling = prof.enabled;
@@ -616,25 +711,29 @@ int unbind_device(int64_t n, int nh, const int64_t *d_off, const int64_t *h_off,
     if (phi_out) HALMA_CUDA(cudaMemsetAsync(phi_out, 0, sizeof(double) * n, st));
 
     if (!f64) {
-        auto *pk = at<float4>(base, o_pk);
+        float4 *pkb[2] = {at<float4>(base, o_pk), at<float4>(base, o_pk2)};
         int bps = 0;
         HALMA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, ub_pair_kernel, 256, 0));
         const int pgrid = device_sm_count() * std::max(bps, 1);
         auto record = [&](cudaStream_t rs) -> int {
-            // first pass: centre of mass and packing; later passes are kept up to date by the
-            // energy kernel (compaction + next-pass sums)
+            // first pass: centre of mass and packing into buffer 0; every pass then compacts
+            // its survivors into the other buffer and sets the next pass's halo state
             HALMA_LAUNCH(ub_reduce_kernel, nh, 256, 0, rs, off, x, y, z, vx, vy, vz, m, bound, hs, 0);
-            HALMA_LAUNCH(ub_pack_kernel<float4>, nh, 256, 0, rs, off, dpoff, x, y, z, m, bound, hs, pk, pidx);
+            HALMA_LAUNCH(ub_pack_kernel<float4>, nh, 256, 0, rs, off, dpoff, x, y, z, m, bound, hs, pkb[0], pidxb[0]);
             for (int it = 0; it < p.max_iter; ++it) {
-                HALMA_LAUNCH(ub_items_kernel, 1, 1024, 0, rs, nh, dorder, hs, tab, slice_len, istart, idesc, cnt,
-                             cnt + 1, profiling ? dpairs + it : nullptr);
+                const int a = it & 1, b = a ^ 1;
+                HALMA_LAUNCH(ub_items_kernel, 1, 1024, 0, rs, nh, dorder, hs, tab, slice_len, istart, idesc, sstart,
+                             cnt, cnt + 1, cnt + 2, profiling ? dpairs + it : nullptr);
                 // External: captured as an event-record node, so the replay records it
                 if (profiling) HALMA_CUDA(cudaEventRecordWithFlags(prof.ev0[it], rs, cudaEventRecordExternal));
-                HALMA_LAUNCH(ub_pair_kernel, pgrid, 256, 0, rs, pk, dpoff, dqoff, hs, nh, istart, idesc, cnt, cnt + 1,
-                             eps2, slice_len / 32, phi);
+                HALMA_LAUNCH(ub_pair_kernel, pgrid, 256, 0, rs, pkb[a], dpoff, dqoff, hs, nh, istart, idesc, cnt,
+                             cnt + 1, eps2, slice_len / 32, phi);
                 if (profiling) HALMA_CUDA(cudaEventRecordWithFlags(prof.ev1[it], rs, cudaEventRecordExternal));
-                HALMA_LAUNCH(ub_energy_kernel<float4>, nh, 256, 0, rs, dpoff, dqoff, slice_len, pk, pidx, phi, x, y, z,
-                             vx, vy, vz, m, gfac, bound, phi_out, hs);
+                HALMA_LAUNCH(ub_energy_seg_kernel<float4>, sgrid, 256, 0, rs, nh, sstart, idesc, cnt + 2, dpoff, dqoff,
+                             slice_len, pidxb[a], phi, x, y, z, vx, vy, vz, m, gfac, hs, bound, phi_out, keepf, ssum);
+                HALMA_LAUNCH(ub_compact_seg_kernel<float4>, sgrid, 256, 0, rs, nh, sstart, idesc, cnt + 2, dpoff, hs,
+                             keepf, ssum, pkb[a], pidxb[a], pkb[b], pidxb[b]);
+                HALMA_LAUNCH(ub_finalize_kernel, grid_for(nh, 256), 256, 0, rs, nh, dorder, sstart, ssum, gfac, hs);
             }
             return HALMA_OK;
         };
@@ -707,23 +806,29 @@ int unbind_device(int64_t n, int nh, const int64_t *d_off, const int64_t *h_off,
         }
     } else {
         // plain FP64 path: per pass, one pair launch per active halo, host checks convergence
-        auto *pk = at<double4>(base, o_pk);
+        double4 *pkb[2] = {at<double4>(base, o_pk), at<double4>(base, o_pk2)};
         std::vector<HaloState> hh(nh);
         HALMA_LAUNCH(ub_reduce_kernel, nh, 256, 0, st, off, x, y, z, vx, vy, vz, m, bound, hs, 0);
-        HALMA_LAUNCH(ub_pack_kernel<double4>, nh, 256, 0, st, off, dpoff, x, y, z, m, bound, hs, pk, pidx);
+        HALMA_LAUNCH(ub_pack_kernel<double4>, nh, 256, 0, st, off, dpoff, x, y, z, m, bound, hs, pkb[0], pidxb[0]);
         for (int it = 0; it < p.max_iter; ++it) {
+            const int a = it & 1, b = a ^ 1;
+            HALMA_LAUNCH(ub_items_kernel, 1, 1024, 0, st, nh, dorder, hs, tab, slice_len, istart, idesc, sstart, cnt,
+                         cnt + 1, cnt + 2, nullptr);
             HALMA_CUDA(cudaMemcpyAsync(hh.data(), hs, sizeof(HaloState) * nh, cudaMemcpyDeviceToHost, st));
             HALMA_CUDA(cudaStreamSynchronize(st));
             int any = 0;
             for (int h = 0; h < nh; ++h) {
                 if (!hh[h].active || hh[h].nb == 0) continue;
                 any = 1;
-                HALMA_LAUNCH(ub_pair_f64_kernel, grid_for(hh[h].nb, 256), 256, 0, st, pk + poff[h], hh[h].nb,
+                HALMA_LAUNCH(ub_pair_f64_kernel, grid_for(hh[h].nb, 256), 256, 0, st, pkb[a] + poff[h], hh[h].nb,
                              p.eps * p.eps, phi + poff[h]);
             }
             if (!any) break;
-            HALMA_LAUNCH(ub_energy_kernel<double4>, nh, 256, 0, st, dpoff, dqoff, slice_len, pk, pidx, phi, x, y, z, vx,
-                         vy, vz, m, gfac, bound, phi_out, hs);
+            HALMA_LAUNCH(ub_energy_seg_kernel<double4>, sgrid, 256, 0, st, nh, sstart, idesc, cnt + 2, dpoff, dqoff,
+                         slice_len, pidxb[a], phi, x, y, z, vx, vy, vz, m, gfac, hs, bound, phi_out, keepf, ssum);
+            HALMA_LAUNCH(ub_compact_seg_kernel<double4>, sgrid, 256, 0, st, nh, sstart, idesc, cnt + 2, dpoff, hs, keepf,
+                         ssum, pkb[a], pidxb[a], pkb[b], pidxb[b]);
+            HALMA_LAUNCH(ub_finalize_kernel, grid_for(nh, 256), 256, 0, st, nh, dorder, sstart, ssum, gfac, hs);
         }
         HALMA_LAUNCH(ub_reduce_kernel, nh, 256, 0, st, off, x, y, z, vx, vy, vz, m, bound, hs, 1);
     }
