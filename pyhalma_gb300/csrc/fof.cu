@@ -291,6 +291,8 @@ __global__ void __launch_bounds__(256) link_kernel(
                 if (cc < 0) continue;
                 js = cell_start[cc];
                 je = cell_start[cc + 1];
+                // pick up unions made by other warps since the last look (helps the skip below)
+                if (hv) myroot = uf_find(parent, k, err);
             }
             // home position expressed in the neighbour cell's frame
             const float hx = hp.x - (float)ox * g.cs;
@@ -303,6 +305,10 @@ __global__ void __launch_bounds__(256) link_kernel(
                 // read here may be outdated by later unions, which is safe: equal roots
                 // prove the same set, unequal ones are re-checked by uf_union
                 const int rql = jl < je ? uf_find(parent, jl, err) : -1;
+                // every home particle and every particle of this chunk already in one set: no
+                // test here can join anything new, skip the 32 x 32 block
+                const int r0 = __shfl_sync(0xffffffffu, myroot, 0);   // lane 0 is always a home particle
+                if (__all_sync(0xffffffffu, (!hv || myroot == r0) && (jl >= je || rql == r0))) continue;
                 __syncwarp();
                 buf[w][lane] = q;
                 rbuf[w][lane] = rql;
