@@ -193,8 +193,14 @@ typedef struct {
     int32_t max_iter;   /* passes at most (>= 1)                                        */
     int32_t precision;  /* HALMA_UNBIND_FP32C or HALMA_UNBIND_FP64                      */
     int32_t use_graph;  /* FP32C: replay all passes as one captured CUDA graph          */
-    int32_t reserved;
+    int32_t flags;      /* HALMA_UNBIND_FULL_RECOMPUTE or 0                             */
 } halma_unbind_params;
+
+/* FP32C passes after the first normally update the potential of the survivors by
+ * subtracting the contribution of the particles the previous pass removed (the potential is
+ * linear in the sources): O(bound x removed) pairs per pass instead of O(bound^2).  This flag
+ * recomputes the full sum every pass instead. */
+#define HALMA_UNBIND_FULL_RECOMPUTE 1
 
 enum {
     HALMA_UB_MASS = 0, HALMA_UB_CX, HALMA_UB_CY, HALMA_UB_CZ, HALMA_UB_VX, HALMA_UB_VY,

@@ -45,7 +45,10 @@ class HalmaError(RuntimeError):
 class UnbindParams(ctypes.Structure):
     _fields_ = [("eps", ctypes.c_double), ("G", ctypes.c_double), ("factor_v", ctypes.c_double),
                 ("max_iter", ctypes.c_int32), ("precision", ctypes.c_int32),
-                ("use_graph", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+                ("use_graph", ctypes.c_int32), ("flags", ctypes.c_int32)]
+
+
+UNBIND_FULL_RECOMPUTE = 1
 
 
 _lock = threading.Lock()

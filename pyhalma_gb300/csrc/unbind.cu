@@ -37,7 +37,7 @@ constexpr float kFar = 3.0e30f;
 
 struct HaloState {   // per halo, FP64 unless stated
     double M, cx, cy, cz, vx, vy, vz, ekin, epot;
-    int nb, active, iter, removed;
+    int nb, active, iter, removed, nrem;   // nrem: removed by the last pass (next pass's sources)
 };
 
 __device__ __forceinline__ double warp_sum(double v) {
@@ -190,10 +190,10 @@ __device__ __forceinline__ int warp_incl_scan(int v, int lane) {
 }
 
 __global__ void __launch_bounds__(1024) ub_items_kernel(int nh, const int *__restrict__ order, const HaloState *hs,
-                                                        TileTable tab, int slice_len, int *__restrict__ istart,
-                                                        int4 *__restrict__ idesc, int *__restrict__ sstart,
-                                                        int *__restrict__ nitems, int *__restrict__ counter,
-                                                        int *__restrict__ nsegs,
+                                                        TileTable tab, int slice_len, int inc,
+                                                        int *__restrict__ istart, int4 *__restrict__ idesc,
+                                                        int *__restrict__ sstart, int *__restrict__ nitems,
+                                                        int *__restrict__ counter, int *__restrict__ nsegs,
                                                         unsigned long long *__restrict__ pairs_out) {
     __shared__ int wsum[32], wseg[32];
     __shared__ int base, sbase;
@@ -212,11 +212,12 @@ __global__ void __launch_bounds__(1024) ub_items_kernel(int nh, const int *__res
             h = order[q];
             if (hs[h].active) {
                 const int nb = hs[h].nb;
+                const int ns = inc ? hs[h].nrem : nb;   // sources: removed particles or the halo itself
                 T = tile_t_for(tab, nb);
-                nsl = (int)(((int64_t)nb + slice_len - 1) / slice_len);
-                cnt = ((nb + 32 * T - 1) / (32 * T)) * nsl;
+                nsl = (int)(((int64_t)ns + slice_len - 1) / slice_len);
+                cnt = ns > 0 ? ((nb + 32 * T - 1) / (32 * T)) * nsl : 0;
                 nseg = max(1, (nb + kSeg - 1) / kSeg);
-                if (nb > 0) atomicAdd(&pairs, (unsigned long long)nb * (unsigned long long)nb);
+                if (nb > 0) atomicAdd(&pairs, (unsigned long long)nb * (unsigned long long)ns);
             }
         }
         const int incl = warp_incl_scan(cnt, lane);
@@ -297,17 +298,19 @@ __device__ __forceinline__ void chunk_pairs(const float4 *sa, const float4 *sb, 
     }
 }
 
-// One work item: 32*T target slots of one halo against source chunks [c_begin, c_end).
+// One work item: 32*T target slots of one halo (tpk) against source chunks [c_begin, c_end)
+// of spk.  self_ok: targets and sources are the same slots, so the self pair is skipped.
 template <int T>
-__device__ __forceinline__ void pair_item(const float4 *__restrict__ pk, int64_t base, int nb, int tile, float eps2,
-                                          int c_begin, int c_end, double *__restrict__ out, float4 *buf, int lane) {
+__device__ __forceinline__ void pair_item(const float4 *__restrict__ tpk, const float4 *__restrict__ pk, int64_t base,
+                                          int nb, int tile, float eps2, int c_begin, int c_end, bool self_ok,
+                                          double *__restrict__ out, float4 *buf, int lane) {
     {
         f2x tx[T], ty[T], tz[T];
         float sum[T], comp[T];
 #pragma unroll
         for (int t = 0; t < T; ++t) {
             const int r = tile * 32 * T + t * 32 + lane;
-            const float4 p = r < nb ? pk[base + r] : make_float4(kFar, kFar, kFar, 0.f);
+            const float4 p = r < nb ? tpk[base + r] : make_float4(kFar, kFar, kFar, 0.f);
             tx[t] = pack2(p.x, p.x);
             ty[t] = pack2(p.y, p.y);
             tz[t] = pack2(p.z, p.z);
@@ -332,7 +335,7 @@ __device__ __forceinline__ void pair_item(const float4 *__restrict__ pk, int64_t
 #pragma unroll
             for (int t = 0; t < T; ++t) acc[t] = pack2(0.f, 0.f);
             const int ts = c - self0;
-            if (ts >= 0 && ts < T)
+            if (self_ok && ts >= 0 && ts < T)
                 chunk_pairs<T, true>(buf, buf + 16, tx, ty, tz, e2, acc, ts, lane);
             else
                 chunk_pairs<T, false>(buf, buf + 16, tx, ty, tz, e2, acc, ts, lane);
@@ -355,8 +358,12 @@ __device__ __forceinline__ void pair_item(const float4 *__restrict__ pk, int64_t
 // item is (halo, target tile, tile shape T, source slice): 32*T targets against one slice of
 // slice_chunks*32 source slots.  Each slice writes its own partial sums
 // (part[qoff[h] + slice * npad_h + r]); the energy kernel adds the slices in order, so the
-// result does not depend on which warp ran which item.
-__global__ void __launch_bounds__(256) ub_pair_kernel(const float4 *__restrict__ pk, const int64_t *__restrict__ poff,
+// result does not depend on which warp ran which item.  Full passes take the sources from the
+// targets' own slots (self pair skipped); incremental passes (inc) take them from the slots of
+// the particles removed by the previous pass (spk, hs.nrem of them), whose contribution the
+// energy kernel then subtracts from the previous potential.
+__global__ void __launch_bounds__(256) ub_pair_kernel(const float4 *__restrict__ pk, const float4 *__restrict__ spk,
+                                                      int inc, const int64_t *__restrict__ poff,
                                                       const int64_t *__restrict__ qoff, const HaloState *__restrict__ hs,
                                                       int nh, const int *__restrict__ istart,
                                                       const int4 *__restrict__ idesc, const int *__restrict__ nitems_p,
@@ -384,13 +391,15 @@ __global__ void __launch_bounds__(256) ub_pair_kernel(const float4 *__restrict__
         const int64_t base = poff[h];
         const int64_t npad = poff[h + 1] - base;
         const int nb = hs[h].nb;
+        const int ns = inc ? hs[h].nrem : nb;
+        const float4 *src = inc ? spk : pk;
         const int c0 = slice * slice_chunks;
-        const int c1 = min((nb + 31) >> 5, c0 + slice_chunks);
+        const int c1 = min((ns + 31) >> 5, c0 + slice_chunks);
         double *out = part + qoff[h] + (int64_t)slice * npad;
         switch (it.z) {
-            case 1: pair_item<1>(pk, base, nb, tile, eps2, c0, c1, out, buf[w], lane); break;
-            case 2: pair_item<2>(pk, base, nb, tile, eps2, c0, c1, out, buf[w], lane); break;
-            default: pair_item<4>(pk, base, nb, tile, eps2, c0, c1, out, buf[w], lane); break;
+            case 1: pair_item<1>(pk, src, base, nb, tile, eps2, c0, c1, !inc, out, buf[w], lane); break;
+            case 2: pair_item<2>(pk, src, base, nb, tile, eps2, c0, c1, !inc, out, buf[w], lane); break;
+            default: pair_item<4>(pk, src, base, nb, tile, eps2, c0, c1, !inc, out, buf[w], lane); break;
         }
     }
 }
@@ -411,8 +420,10 @@ template <class V>
 __global__ void __launch_bounds__(256) ub_energy_seg_kernel(int nh, const int *__restrict__ sstart,
                                                             const int4 *__restrict__ idesc, const int *__restrict__ nsegs,
                                                             const int64_t *__restrict__ poff, const int64_t *__restrict__ qoff,
-                                                            int slice_len, const int *__restrict__ pidx,
-                                                            const double *__restrict__ part, const double *__restrict__ x,
+                                                            int slice_len, int inc, const int *__restrict__ pidx,
+                                                            const double *__restrict__ part,
+                                                            const double *__restrict__ phi_prev, double *__restrict__ phi_cur,
+                                                            const double *__restrict__ x,
                                                             const double *__restrict__ y, const double *__restrict__ z,
                                                             const double *__restrict__ vx, const double *__restrict__ vy,
                                                             const double *__restrict__ vz, const double *__restrict__ m,
@@ -428,15 +439,20 @@ __global__ void __launch_bounds__(256) ub_energy_seg_kernel(int nh, const int *_
     const int sl = seg - sstart[q];
     const HaloState s = hs[h];
     const int64_t pb = poff[h], npad = poff[h + 1] - pb, qb = qoff[h];
-    const int nsl = (int)(((int64_t)s.nb + slice_len - 1) / slice_len);
+    const int ns = inc ? s.nrem : s.nb;
+    const int nsl = (int)(((int64_t)ns + slice_len - 1) / slice_len);
     double v[kSegSums] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
     const int rend = min(s.nb, (sl + 1) * kSeg);
     for (int r = sl * kSeg + threadIdx.x; r < rend; r += blockDim.x) {
         const int i = pidx[pb + r];
         const double dvx = vx[i] - s.vx, dvy = vy[i] - s.vy, dvz = vz[i] - s.vz;
         const double ek = 0.5 * (dvx * dvx + dvy * dvy + dvz * dvz);
-        double p = 0.0;
-        for (int k = 0; k < nsl; ++k) p += part[qb + (int64_t)k * npad + r];   // slices in order
+        double d = 0.0;
+        for (int k = 0; k < nsl; ++k) d += part[qb + (int64_t)k * npad + r];   // slices in order
+        // full pass: the sum itself; incremental pass: previous potential minus the removed
+        // particles' contribution
+        const double p = inc ? phi_prev[pb + r] - d : d;
+        phi_cur[pb + r] = p;
         const double e = ek - gfac * p;
         const bool keep = !(e > 0.0);
         keepf[pb + r] = keep ? 1 : 0;
@@ -471,11 +487,13 @@ __global__ void __launch_bounds__(256) ub_compact_seg_kernel(int nh, const int *
                                                              const unsigned char *__restrict__ keepf,
                                                              const double *__restrict__ seg_sums,
                                                              const V *__restrict__ pk_in, const int *__restrict__ pidx_in,
-                                                             V *__restrict__ pk_out, int *__restrict__ pidx_out) {
+                                                             const double *__restrict__ phi_cur,
+                                                             V *__restrict__ pk_out, int *__restrict__ pidx_out,
+                                                             double *__restrict__ phi_next, V *__restrict__ removed) {
     const int seg = blockIdx.x;
     if (seg >= *nsegs) return;
-    __shared__ int wcount[8];
-    __shared__ int running;
+    __shared__ int wcount[8], wrem[8];
+    __shared__ int running, rrunning;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int q = owner_of(sstart, nh, seg);
     const int h = idesc[q].x;
@@ -483,42 +501,64 @@ __global__ void __launch_bounds__(256) ub_compact_seg_kernel(int nh, const int *
     const int nb = hs[h].nb;
     const int64_t pb = poff[h];
     if (threadIdx.x == 0) {
-        int o = 0;   // survivors of the earlier segments of this halo
-        for (int k = 0; k < sl; ++k) o += (int)seg_sums[(int64_t)(s0 + k) * kSegSums + 1];
+        int o = 0, orem = 0;   // survivors / removed of the earlier segments of this halo
+        for (int k = 0; k < sl; ++k) {
+            orem += (int)seg_sums[(int64_t)(s0 + k) * kSegSums + 0];
+            o += (int)seg_sums[(int64_t)(s0 + k) * kSegSums + 1];
+        }
         running = o;
+        rrunning = orem;
     }
     __syncthreads();
     const int rend = min(nb, (sl + 1) * kSeg);
     for (int r0 = sl * kSeg; r0 < rend; r0 += blockDim.x) {
         const int r = r0 + threadIdx.x;
-        const bool keep = r < rend && keepf[pb + r];
+        const bool valid = r < rend;
+        const bool keep = valid && keepf[pb + r];
+        const bool gone = valid && !keep;
         const unsigned bal = __ballot_sync(0xffffffffu, keep);
-        if (lane == 0) wcount[w] = __popc(bal);
+        const unsigned bgone = __ballot_sync(0xffffffffu, gone);
+        if (lane == 0) {
+            wcount[w] = __popc(bal);
+            wrem[w] = __popc(bgone);
+        }
         __syncthreads();
-        int rank = running;
-        for (int k = 0; k < w; ++k) rank += wcount[k];
+        int rank = running, rrank = rrunning;
+        for (int k = 0; k < w; ++k) {
+            rank += wcount[k];
+            rrank += wrem[k];
+        }
         rank += __popc(bal & ((1u << lane) - 1u));
+        rrank += __popc(bgone & ((1u << lane) - 1u));
         if (keep) {
             pk_out[pb + rank] = pk_in[pb + r];
             pidx_out[pb + rank] = pidx_in[pb + r];
+            phi_next[pb + rank] = phi_cur[pb + r];
+        } else if (gone) {
+            removed[pb + rrank] = pk_in[pb + r];   // sources of the next incremental pass
         }
         __syncthreads();
         if (threadIdx.x == 0) {
-            int tot = 0;
-            for (int k = 0; k < (int)(blockDim.x >> 5); ++k) tot += wcount[k];
+            int tot = 0, trem = 0;
+            for (int k = 0; k < (int)(blockDim.x >> 5); ++k) {
+                tot += wcount[k];
+                trem += wrem[k];
+            }
             running += tot;
+            rrunning += trem;
         }
         __syncthreads();
     }
-    if (sl == nseg - 1) {   // the halo's last segment pads after the survivors
-        const int nkeep = running;
+    if (sl == nseg - 1) {   // the halo's last segment pads after the survivors and the removed
+        V f;
+        f.x = f.y = f.z = kFar;
+        f.w = 0;
+        const int nkeep = running, nrem = rrunning;
         for (int r = nkeep + threadIdx.x; r < ((nkeep + 31) & ~31); r += blockDim.x) {
-            V f;
-            f.x = f.y = f.z = kFar;
-            f.w = 0;
             pk_out[pb + r] = f;
             pidx_out[pb + r] = -1;
         }
+        for (int r = nrem + threadIdx.x; r < ((nrem + 31) & ~31); r += blockDim.x) removed[pb + r] = f;
     }
 }
 
@@ -532,6 +572,7 @@ __global__ void ub_finalize_kernel(int nh, const int *__restrict__ order, const 
         for (int sg = sstart[q]; sg < sstart[q + 1]; ++sg)
             for (int k = 0; k < kSegSums; ++k) v[k] += seg_sums[(int64_t)sg * kSegSums + k];
         o.removed = (int)v[0];
+        o.nrem = (int)v[0];
         o.iter += 1;
         o.ekin = v[2];
         o.epot = -0.5 * gfac * v[3];
@@ -665,6 +706,8 @@ int unbind_device(int64_t n, int nh, const int64_t *d_off, const int64_t *h_off,
     const size_t o_pk = L.add(vsz * P), o_pk2 = L.add(vsz * P);       // packed slots, double-buffered
     const size_t o_pidx = L.add(sizeof(int) * P), o_pidx2 = L.add(sizeof(int) * P);
     const size_t o_keep = L.add(P);
+    const size_t o_rk = L.add(vsz * P);                               // removed particles' slots
+    const size_t o_phic = L.add(sizeof(double) * P), o_phin = L.add(sizeof(double) * P);
     const size_t o_phi = L.add(sizeof(double) * Q);
     const size_t o_istart = L.add(sizeof(int) * (nh + 1));
     const size_t o_sstart = L.add(sizeof(int) * (nh + 1));
@@ -681,6 +724,9 @@ int unbind_device(int64_t n, int nh, const int64_t *d_off, const int64_t *h_off,
     auto *dorder = at<int>(base, o_order);
     int *pidxb[2] = {at<int>(base, o_pidx), at<int>(base, o_pidx2)};
     auto *keepf = at<unsigned char>(base, o_keep);
+    auto *phic = at<double>(base, o_phic), *phin = at<double>(base, o_phin);
+    // incremental passes subtract the removed particles' potential instead of recomputing
+    const bool incremental = !(p.flags & HALMA_UNBIND_FULL_RECOMPUTE);
     auto *phi = at<double>(base, o_phi);
     auto *istart = at<int>(base, o_istart);
     auto *sstart = at<int>(base, o_sstart);
@@ -720,19 +766,22 @@ int unbind_device(int64_t n, int nh, const int64_t *d_off, const int64_t *h_off,
             // its survivors into the other buffer and sets the next pass's halo state
             HALMA_LAUNCH(ub_reduce_kernel, nh, 256, 0, rs, off, x, y, z, vx, vy, vz, m, bound, hs, 0);
             HALMA_LAUNCH(ub_pack_kernel<float4>, nh, 256, 0, rs, off, dpoff, x, y, z, m, bound, hs, pkb[0], pidxb[0]);
+            float4 *rk = at<float4>(base, o_rk);
             for (int it = 0; it < p.max_iter; ++it) {
                 const int a = it & 1, b = a ^ 1;
-                HALMA_LAUNCH(ub_items_kernel, 1, 1024, 0, rs, nh, dorder, hs, tab, slice_len, istart, idesc, sstart,
-                             cnt, cnt + 1, cnt + 2, profiling ? dpairs + it : nullptr);
+                const int inc = (it > 0 && incremental) ? 1 : 0;
+                HALMA_LAUNCH(ub_items_kernel, 1, 1024, 0, rs, nh, dorder, hs, tab, slice_len, inc, istart, idesc,
+                             sstart, cnt, cnt + 1, cnt + 2, profiling ? dpairs + it : nullptr);
                 // External: captured as an event-record node, so the replay records it
                 if (profiling) HALMA_CUDA(cudaEventRecordWithFlags(prof.ev0[it], rs, cudaEventRecordExternal));
-                HALMA_LAUNCH(ub_pair_kernel, pgrid, 256, 0, rs, pkb[a], dpoff, dqoff, hs, nh, istart, idesc, cnt,
-                             cnt + 1, eps2, slice_len / 32, phi);
+                HALMA_LAUNCH(ub_pair_kernel, pgrid, 256, 0, rs, pkb[a], rk, inc, dpoff, dqoff, hs, nh, istart, idesc,
+                             cnt, cnt + 1, eps2, slice_len / 32, phi);
                 if (profiling) HALMA_CUDA(cudaEventRecordWithFlags(prof.ev1[it], rs, cudaEventRecordExternal));
                 HALMA_LAUNCH(ub_energy_seg_kernel<float4>, sgrid, 256, 0, rs, nh, sstart, idesc, cnt + 2, dpoff, dqoff,
-                             slice_len, pidxb[a], phi, x, y, z, vx, vy, vz, m, gfac, hs, bound, phi_out, keepf, ssum);
+                             slice_len, inc, pidxb[a], phi, phin, phic, x, y, z, vx, vy, vz, m, gfac, hs, bound,
+                             phi_out, keepf, ssum);
                 HALMA_LAUNCH(ub_compact_seg_kernel<float4>, sgrid, 256, 0, rs, nh, sstart, idesc, cnt + 2, dpoff, hs,
-                             keepf, ssum, pkb[a], pidxb[a], pkb[b], pidxb[b]);
+                             keepf, ssum, pkb[a], pidxb[a], phic, pkb[b], pidxb[b], phin, rk);
                 HALMA_LAUNCH(ub_finalize_kernel, grid_for(nh, 256), 256, 0, rs, nh, dorder, sstart, ssum, gfac, hs);
             }
             return HALMA_OK;
@@ -753,6 +802,7 @@ int unbind_device(int64_t n, int nh, const int64_t *d_off, const int64_t *h_off,
             key.push_back((uintptr_t)dpairs);
             key.push_back((uintptr_t)tab.n);
             key.push_back((uintptr_t)slice_len);
+            key.push_back((uintptr_t)incremental);
             for (int c = 0; c < tab.n; ++c) {
                 key.push_back((uintptr_t)tab.upper[c]);
                 key.push_back((uintptr_t)tab.t[c]);
@@ -810,10 +860,11 @@ int unbind_device(int64_t n, int nh, const int64_t *d_off, const int64_t *h_off,
         std::vector<HaloState> hh(nh);
         HALMA_LAUNCH(ub_reduce_kernel, nh, 256, 0, st, off, x, y, z, vx, vy, vz, m, bound, hs, 0);
         HALMA_LAUNCH(ub_pack_kernel<double4>, nh, 256, 0, st, off, dpoff, x, y, z, m, bound, hs, pkb[0], pidxb[0]);
+        double4 *rk = at<double4>(base, o_rk);
         for (int it = 0; it < p.max_iter; ++it) {
             const int a = it & 1, b = a ^ 1;
-            HALMA_LAUNCH(ub_items_kernel, 1, 1024, 0, st, nh, dorder, hs, tab, slice_len, istart, idesc, sstart, cnt,
-                         cnt + 1, cnt + 2, nullptr);
+            HALMA_LAUNCH(ub_items_kernel, 1, 1024, 0, st, nh, dorder, hs, tab, slice_len, 0, istart, idesc, sstart,
+                         cnt, cnt + 1, cnt + 2, nullptr);
             HALMA_CUDA(cudaMemcpyAsync(hh.data(), hs, sizeof(HaloState) * nh, cudaMemcpyDeviceToHost, st));
             HALMA_CUDA(cudaStreamSynchronize(st));
             int any = 0;
@@ -825,9 +876,10 @@ int unbind_device(int64_t n, int nh, const int64_t *d_off, const int64_t *h_off,
             }
             if (!any) break;
             HALMA_LAUNCH(ub_energy_seg_kernel<double4>, sgrid, 256, 0, st, nh, sstart, idesc, cnt + 2, dpoff, dqoff,
-                         slice_len, pidxb[a], phi, x, y, z, vx, vy, vz, m, gfac, hs, bound, phi_out, keepf, ssum);
+                         slice_len, 0, pidxb[a], phi, phin, phic, x, y, z, vx, vy, vz, m, gfac, hs, bound, phi_out,
+                         keepf, ssum);
             HALMA_LAUNCH(ub_compact_seg_kernel<double4>, sgrid, 256, 0, st, nh, sstart, idesc, cnt + 2, dpoff, hs, keepf,
-                         ssum, pkb[a], pidxb[a], pkb[b], pidxb[b]);
+                         ssum, pkb[a], pidxb[a], phic, pkb[b], pidxb[b], phin, rk);
             HALMA_LAUNCH(ub_finalize_kernel, grid_for(nh, 256), 256, 0, st, nh, dorder, sstart, ssum, gfac, hs);
         }
         HALMA_LAUNCH(ub_reduce_kernel, nh, 256, 0, st, off, x, y, z, vx, vy, vz, m, bound, hs, 1);

@@ -46,10 +46,12 @@ class UnbindOptions:
     max_iter: int = 20
     precision: str = "fp32c"
     use_graph: bool = True
+    incremental: bool = True   # later passes subtract the removed particles' potential
 
     def params(self):
+        flags = 0 if self.incremental else _lib.UNBIND_FULL_RECOMPUTE
         return _lib.UnbindParams(float(self.eps), float(self.G), float(self.factor_v), int(self.max_iter),
-                                 _PREC[self.precision], int(bool(self.use_graph)), 0)
+                                 _PREC[self.precision], int(bool(self.use_graph)), flags)
 
 
 def unbind_batched(offsets, x, y, z, vx, vy, vz, m, options: UnbindOptions | None = None, want_phi=False, **kw):

@@ -65,6 +65,21 @@ def test_fp32c_matches_fp64_oracle(catalogue, cuda):
     assert not bound[cont].any()
 
 
+def test_full_recompute_matches_fp64_oracle(catalogue, cuda):
+    # every pass recomputes the full potential (no subtraction of the removed particles)
+    bound, halo, phi = unbind_batched(*_arrays(catalogue), UnbindOptions(eps=EPS, max_iter=50, incremental=False),
+                                      want_phi=True)
+    assert _check_against_oracle(catalogue, bound, phi, halo, RTOL_PHI) <= 5
+
+
+def test_incremental_equals_full_recompute(catalogue, cuda):
+    inc = unbind_batched(*_arrays(catalogue), UnbindOptions(eps=EPS, max_iter=50), want_phi=True)
+    full = unbind_batched(*_arrays(catalogue), UnbindOptions(eps=EPS, max_iter=50, incremental=False), want_phi=True)
+    assert (inc[0] != full[0]).sum() <= 2
+    both = (inc[0] == 1) & (full[0] == 1)
+    assert np.max(np.abs(inc[2][both] / full[2][both] - 1.0)) < 2e-7
+
+
 def test_fp64_path_matches_oracle(catalogue, cuda):
     bound, halo, phi = unbind_batched(*_arrays(catalogue), UnbindOptions(eps=EPS, max_iter=50, precision="fp64"),
                                       want_phi=True)
