@@ -77,7 +77,8 @@ def test_incremental_equals_full_recompute(catalogue, cuda):
     full = unbind_batched(*_arrays(catalogue), UnbindOptions(eps=EPS, max_iter=50, incremental=False), want_phi=True)
     assert (inc[0] != full[0]).sum() <= 2
     both = (inc[0] == 1) & (full[0] == 1)
-    assert np.max(np.abs(inc[2][both] / full[2][both] - 1.0)) < 2e-7
+    # each is within RTOL_PHI of FP64 (checked above); against each other likewise
+    assert np.max(np.abs(inc[2][both] / full[2][both] - 1.0)) < RTOL_PHI
 
 
 def test_fp64_path_matches_oracle(catalogue, cuda):
