@@ -64,6 +64,28 @@ __device__ __forceinline__ int uf_find(int *parent, int v, int *err) {
     return v;
 }
 
+// Same walk with L1-cached loads, for the linking kernel.  A value read from L1 may be older
+// than the one in L2 (another SM hooked or compressed since), which is harmless there: an
+// older parent is still an ancestor (parents only move toward the root, and every value in a
+// chain is smaller than the last), equal roots still prove the same set, and any hook goes
+// through an atomicCAS on L2 that sees the current value.  The final labels are read by a
+// later kernel.
+__device__ __forceinline__ int uf_find_cached(int *parent, int v, int *err) {
+    int p = parent[v];
+    int guard = 0;
+    while (p != v) {
+        const int gp = parent[p];
+        if (gp != p) __stcg(parent + v, gp);
+        v = p;
+        p = gp;
+        if (++guard > kUfCap) {
+            atomicOr(err, 1);
+            break;
+        }
+    }
+    return v;
+}
+
 // Hooks the larger of two roots under the smaller; retries from the new parent when the
 // CAS loses a race.  Every root of a tree is its smallest sorted position.
 __device__ __forceinline__ void uf_union(int *parent, int a, int b, int *err) {
@@ -272,27 +294,37 @@ __global__ void __launch_bounds__(256) link_kernel(
         const bool hv = k < ce;
         const float4 hp = hv ? rec[k] : make_float4(0.f, 0.f, 0.f, 0.f);
         const int hidx = __float_as_int(hp.w);
-        int myroot = hv ? uf_find(parent, k, err) : -1;
+        int myroot = hv ? uf_find_cached(parent, k, err) : -1;
         long long cx, cy, cz;
         decode_key(cell_key[c], g, cx, cy, cz);
+        // the 13 forward neighbour cells are looked up at once, lane nb finding cell nb, so
+        // the hash probes and cell bounds of one item cost one round of loads, not thirteen
+        int njs = 0, nje = 0;
+        if (lane < 13) {
+            const long long nx = cx + c_stencil[lane][0], ny = cy + c_stencil[lane][1], nz = cz + c_stencil[lane][2];
+            if (nx < g.ncx && ny >= 0 && ny < g.ncy && nz >= 0 && nz < g.ncz) {
+                const uint64_t nkey = ((uint64_t)nx * (uint64_t)g.ncy + (uint64_t)ny) * (uint64_t)g.ncz + (uint64_t)nz;
+                const int cc = hash_lookup(hkeys, hvals, hmask, nkey);
+                if (cc >= 0) {
+                    njs = cell_start[cc];
+                    nje = cell_start[cc + 1];
+                }
+            }
+        }
         for (int nb = -1; nb < 13; ++nb) {
             int js, je, ox = 0, oy = 0, oz = 0;
             if (nb < 0) {
                 js = cell_start[c];
                 je = ce;
             } else {
+                js = __shfl_sync(0xffffffffu, njs, nb);
+                je = __shfl_sync(0xffffffffu, nje, nb);
+                if (je <= js) continue;   // outside the grid or no particles there
                 ox = c_stencil[nb][0];
                 oy = c_stencil[nb][1];
                 oz = c_stencil[nb][2];
-                const long long nx = cx + ox, ny = cy + oy, nz = cz + oz;
-                if (nx >= g.ncx || ny < 0 || ny >= g.ncy || nz < 0 || nz >= g.ncz) continue;
-                const uint64_t nkey = ((uint64_t)nx * (uint64_t)g.ncy + (uint64_t)ny) * (uint64_t)g.ncz + (uint64_t)nz;
-                const int cc = hash_lookup(hkeys, hvals, hmask, nkey);
-                if (cc < 0) continue;
-                js = cell_start[cc];
-                je = cell_start[cc + 1];
                 // pick up unions made by other warps since the last look (helps the skip below)
-                if (hv) myroot = uf_find(parent, k, err);
+                if (hv) myroot = uf_find_cached(parent, k, err);
             }
             // home position expressed in the neighbour cell's frame
             const float hx = hp.x - (float)ox * g.cs;
@@ -304,7 +336,7 @@ __global__ void __launch_bounds__(256) link_kernel(
                 // roots of the chunk, found once per chunk instead of once per hit; a root
                 // read here may be outdated by later unions, which is safe: equal roots
                 // prove the same set, unequal ones are re-checked by uf_union
-                const int rql = jl < je ? uf_find(parent, jl, err) : -1;
+                const int rql = jl < je ? uf_find_cached(parent, jl, err) : -1;
                 // every home particle and every particle of this chunk already in one set: no
                 // test here can join anything new, skip the 32 x 32 block
                 const int r0 = __shfl_sync(0xffffffffu, myroot, 0);   // lane 0 is always a home particle
@@ -327,7 +359,7 @@ __global__ void __launch_bounds__(256) link_kernel(
                             uf_union(parent, myroot, rq, err);
                             has[k] = 1;
                             has[jj] = 1;
-                            myroot = uf_find(parent, k, err);
+                            myroot = uf_find_cached(parent, k, err);
                         }
                     }
                 }
