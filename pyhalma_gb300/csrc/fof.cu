@@ -276,6 +276,14 @@ __constant__ int c_stencil[13][3] = {{0, 0, 1},  {0, 1, -1}, {0, 1, 0},  {0, 1, 
                                      {1, -1, 0}, {1, -1, 1}, {1, 0, -1}, {1, 0, 0},  {1, 0, 1},
                                      {1, 1, -1}, {1, 1, 0},  {1, 1, 1}};
 
+// One warp per item (a chunk of up to 32 particles of one cell).  The candidates of the item
+// are the later particles of its own cell (j > k) and every particle of the 13 forward
+// neighbour cells; they are concatenated into one list ("segments" 0..12 = stencil cells, 13 =
+// the home cell from the chunk start) and walked 32 at a time, so a sparse region costs one
+// or two rounds of loads per item instead of one per neighbour cell.  Each candidate is moved
+// into the home cell's frame when it is loaded.
+constexpr int kHomeSeg = 13;
+
 __global__ void __launch_bounds__(256) link_kernel(
     const float4 *__restrict__ rec, const int *__restrict__ cell_start, const uint64_t *__restrict__ cell_key,
     const int *__restrict__ item_k0, const int *__restrict__ item_cell, const int *__restrict__ nitems_p,
@@ -284,6 +292,7 @@ __global__ void __launch_bounds__(256) link_kernel(
     int *parent, unsigned char *has, int *err) {
     __shared__ float4 buf[kFofWarps][32];
     __shared__ int rbuf[kFofWarps][32];
+    __shared__ int jbuf[kFofWarps][32];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int nitems = *nitems_p;
     for (int item = blockIdx.x * kFofWarps + w; item < nitems; item += gridDim.x * kFofWarps) {
@@ -294,73 +303,83 @@ __global__ void __launch_bounds__(256) link_kernel(
         const bool hv = k < ce;
         const float4 hp = hv ? rec[k] : make_float4(0.f, 0.f, 0.f, 0.f);
         const int hidx = __float_as_int(hp.w);
-        int myroot = hv ? uf_find_cached(parent, k, err) : -1;
         long long cx, cy, cz;
         decode_key(cell_key[c], g, cx, cy, cz);
-        // the 13 forward neighbour cells are looked up at once, lane nb finding cell nb, so
-        // the hash probes and cell bounds of one item cost one round of loads, not thirteen
-        int njs = 0, nje = 0;
+        // lane s < 13 owns stencil cell s, lane 13 the rest of the home cell
+        int sjs = 0, sn = 0, soff = 0x15;   // soff: stencil offset + 1 per axis, 2 bits each
         if (lane < 13) {
+            soff = (c_stencil[lane][0] + 1) | (c_stencil[lane][1] + 1) << 2 | (c_stencil[lane][2] + 1) << 4;
             const long long nx = cx + c_stencil[lane][0], ny = cy + c_stencil[lane][1], nz = cz + c_stencil[lane][2];
             if (nx < g.ncx && ny >= 0 && ny < g.ncy && nz >= 0 && nz < g.ncz) {
                 const uint64_t nkey = ((uint64_t)nx * (uint64_t)g.ncy + (uint64_t)ny) * (uint64_t)g.ncz + (uint64_t)nz;
                 const int cc = hash_lookup(hkeys, hvals, hmask, nkey);
                 if (cc >= 0) {
-                    njs = cell_start[cc];
-                    nje = cell_start[cc + 1];
+                    sjs = cell_start[cc];
+                    sn = cell_start[cc + 1] - sjs;
                 }
             }
+        } else if (lane == kHomeSeg) {
+            sjs = k0 + 1;
+            sn = ce - sjs;
         }
-        for (int nb = -1; nb < 13; ++nb) {
-            int js, je, ox = 0, oy = 0, oz = 0;
-            if (nb < 0) {
-                js = cell_start[c];
-                je = ce;
-            } else {
-                js = __shfl_sync(0xffffffffu, njs, nb);
-                je = __shfl_sync(0xffffffffu, nje, nb);
-                if (je <= js) continue;   // outside the grid or no particles there
-                ox = c_stencil[nb][0];
-                oy = c_stencil[nb][1];
-                oz = c_stencil[nb][2];
-                // pick up unions made by other warps since the last look (helps the skip below)
-                if (hv) myroot = uf_find_cached(parent, k, err);
-            }
-            // home position expressed in the neighbour cell's frame
-            const float hx = hp.x - (float)ox * g.cs;
-            const float hy = hp.y - (float)oy * g.cs;
-            const float hz = hp.z - (float)oz * g.cs;
-            for (int j0 = js; j0 < je; j0 += 32) {
-                const int jl = j0 + lane;
-                const float4 q = jl < je ? rec[jl] : make_float4(0.f, 0.f, 0.f, 0.f);
-                // roots of the chunk, found once per chunk instead of once per hit; a root
-                // read here may be outdated by later unions, which is safe: equal roots
+        // exclusive prefix of the segment lengths over lanes 0..13
+        int incl = sn;
+        for (int o = 1; o < 16; o <<= 1) {
+            const int u = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += u;
+        }
+        const int spre = incl - sn;
+        const int total = __shfl_sync(0xffffffffu, incl, kHomeSeg);
+        int myroot = hv ? uf_find_cached(parent, k, err) : -1;
+        for (int v0 = 0; v0 < total; v0 += 32) {
+            const int v = v0 + lane;
+            const bool cv = v < total;
+            // segment of candidate v: the last segment starting at or before v (empty
+            // segments share their successor's start and are passed over)
+            int seg = 0;
+#pragma unroll
+            for (int s = 0; s <= kHomeSeg; ++s)
+                if (__shfl_sync(0xffffffffu, spre, s) <= v) seg = s;
+            const int jl = __shfl_sync(0xffffffffu, sjs, seg) + v - __shfl_sync(0xffffffffu, spre, seg);
+            const int off = __shfl_sync(0xffffffffu, soff, seg);
+            float4 q = make_float4(0.f, 0.f, 0.f, 0.f);
+            int rql = -1;
+            if (cv) {
+                q = rec[jl];
+                q.x += (float)((off & 3) - 1) * g.cs;
+                q.y += (float)(((off >> 2) & 3) - 1) * g.cs;
+                q.z += (float)(((off >> 4) & 3) - 1) * g.cs;
+                // roots of the candidates, found once per round instead of once per hit; a
+                // root read here may be outdated by later unions, which is safe: equal roots
                 // prove the same set, unequal ones are re-checked by uf_union
-                const int rql = jl < je ? uf_find_cached(parent, jl, err) : -1;
-                // every home particle and every particle of this chunk already in one set: no
-                // test here can join anything new, skip the 32 x 32 block
-                const int r0 = __shfl_sync(0xffffffffu, myroot, 0);   // lane 0 is always a home particle
-                if (__all_sync(0xffffffffu, (!hv || myroot == r0) && (jl >= je || rql == r0))) continue;
-                __syncwarp();
-                buf[w][lane] = q;
-                rbuf[w][lane] = rql;
-                __syncwarp();
-                const int cnt = min(32, je - j0);
-                for (int t = 0; t < cnt; ++t) {
-                    const float4 qq = buf[w][t];
-                    const int jj = j0 + t;
-                    const float dx = qq.x - hx, dy = qq.y - hy, dz = qq.z - hz;
-                    const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-                    bool hit = hv && d2 <= g.hi && (nb >= 0 || jj > k);
-                    if (hit && d2 >= g.lo) hit = exact_link(x, y, z, hidx, __float_as_int(qq.w), g.r2);
-                    if (hit) {
-                        const int rq = rbuf[w][t];
-                        if (rq != myroot) {
-                            uf_union(parent, myroot, rq, err);
-                            has[k] = 1;
-                            has[jj] = 1;
-                            myroot = uf_find_cached(parent, k, err);
-                        }
+                rql = uf_find_cached(parent, jl, err);
+            }
+            // pick up unions made by other warps since the last look (helps the skip below)
+            if (v0 > 0 && hv) myroot = uf_find_cached(parent, k, err);
+            // every home particle and every candidate of this round already in one set: no
+            // test here can join anything new, skip the 32 x 32 block
+            const int r0 = __shfl_sync(0xffffffffu, myroot, 0);   // lane 0 is always a home particle
+            if (__all_sync(0xffffffffu, (!hv || myroot == r0) && (!cv || rql == r0))) continue;
+            __syncwarp();
+            buf[w][lane] = q;
+            rbuf[w][lane] = rql;
+            jbuf[w][lane] = seg == kHomeSeg ? jl : ~jl;   // home-cell candidates keep the j > k test
+            __syncwarp();
+            const int cnt = min(32, total - v0);
+            for (int t = 0; t < cnt; ++t) {
+                const float4 qq = buf[w][t];
+                const int jb = jbuf[w][t];
+                const float dx = qq.x - hp.x, dy = qq.y - hp.y, dz = qq.z - hp.z;
+                const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                bool hit = hv && d2 <= g.hi && (jb < 0 || jb > k);
+                if (hit && d2 >= g.lo) hit = exact_link(x, y, z, hidx, __float_as_int(qq.w), g.r2);
+                if (hit) {
+                    const int rq = rbuf[w][t];
+                    if (rq != myroot) {
+                        uf_union(parent, myroot, rq, err);
+                        has[k] = 1;
+                        has[jb < 0 ? ~jb : jb] = 1;
+                        myroot = uf_find_cached(parent, k, err);
                     }
                 }
             }
