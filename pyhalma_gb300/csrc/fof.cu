@@ -36,6 +36,7 @@ struct FofGeom {
     double cell, inv_cell, inv_scale, r2;
     float cs, lo, hi;
     long long ncx, ncy, ncz;
+    int sb;   // low key bits holding the 4 x 4 x 4 sub-cell (Morton order) within the cell: 6 or 0
 };
 
 __device__ __forceinline__ uint64_t mix64(uint64_t k) {
@@ -150,17 +151,30 @@ __global__ void bbox_final_kernel(const double *__restrict__ part, int g, double
     }
 }
 
+// Sort key: row-major cell index, then (when there is room) the particle's 4 x 4 x 4 sub-cell in
+// Morton order, so that each 32-particle chunk of a crowded cell is spatially compact.  The
+// order of particles inside a cell does not change the partition.
 __global__ void keys_kernel(const double *__restrict__ x, const double *__restrict__ y,
                             const double *__restrict__ z, int n, FofGeom g,
                             uint64_t *__restrict__ keys, int *__restrict__ vals) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        long long cx = (long long)floor((x[i] - g.xmin) * g.inv_cell);
-        long long cy = (long long)floor((y[i] - g.ymin) * g.inv_cell);
-        long long cz = (long long)floor((z[i] - g.zmin) * g.inv_cell);
+        const double tx = (x[i] - g.xmin) * g.inv_cell;
+        const double ty = (y[i] - g.ymin) * g.inv_cell;
+        const double tz = (z[i] - g.zmin) * g.inv_cell;
+        long long cx = (long long)floor(tx), cy = (long long)floor(ty), cz = (long long)floor(tz);
         cx = min(max(cx, 0ll), g.ncx - 1);
         cy = min(max(cy, 0ll), g.ncy - 1);
         cz = min(max(cz, 0ll), g.ncz - 1);
-        keys[i] = ((uint64_t)cx * (uint64_t)g.ncy + (uint64_t)cy) * (uint64_t)g.ncz + (uint64_t)cz;
+        uint64_t key = ((uint64_t)cx * (uint64_t)g.ncy + (uint64_t)cy) * (uint64_t)g.ncz + (uint64_t)cz;
+        if (g.sb) {
+            const int sx = min(3, max(0, (int)((tx - (double)cx) * 4.0)));
+            const int sy = min(3, max(0, (int)((ty - (double)cy) * 4.0)));
+            const int sz = min(3, max(0, (int)((tz - (double)cz) * 4.0)));
+            const int mort = ((sx >> 1) << 5) | ((sy >> 1) << 4) | ((sz >> 1) << 3) | ((sx & 1) << 2) |
+                             ((sy & 1) << 1) | (sz & 1);
+            key = (key << 6) | (uint64_t)mort;
+        }
+        keys[i] = key;
         vals[i] = i;
     }
 }
@@ -180,7 +194,7 @@ __global__ void prep_kernel(const double *__restrict__ x, const double *__restri
                             float4 *__restrict__ rec, int *__restrict__ head, int *__restrict__ parent,
                             unsigned char *__restrict__ has, int *__restrict__ minidx) {
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
-        const uint64_t key = keys[k];
+        const uint64_t key = keys[k] >> g.sb;
         long long cx, cy, cz;
         decode_key(key, g, cx, cy, cz);
         const int i = idx[k];
@@ -189,7 +203,7 @@ __global__ void prep_kernel(const double *__restrict__ x, const double *__restri
         const double oz = g.zmin + (double)cz * g.cell;
         rec[k] = make_float4((float)((x[i] - ox) * g.inv_scale), (float)((y[i] - oy) * g.inv_scale),
                              (float)((z[i] - oz) * g.inv_scale), __int_as_float(i));
-        head[k] = (k == 0 || keys[k - 1] != key) ? 1 : 0;
+        head[k] = (k == 0 || (keys[k - 1] >> g.sb) != key) ? 1 : 0;
         parent[k] = k;
         has[k] = 0;
         minidx[k] = INT_MAX;
@@ -197,14 +211,14 @@ __global__ void prep_kernel(const double *__restrict__ x, const double *__restri
 }
 
 // Cell table + hash insert, from the exclusive scan of the run heads.
-__global__ void cells_kernel(int n, const uint64_t *__restrict__ keys, const int *__restrict__ head,
+__global__ void cells_kernel(int n, int sb, const uint64_t *__restrict__ keys, const int *__restrict__ head,
                              const int *__restrict__ cellpos, int *__restrict__ cell_start,
                              uint64_t *__restrict__ cell_key, uint64_t *__restrict__ hkeys,
                              int *__restrict__ hvals, uint64_t hmask, int *__restrict__ ncell) {
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
         if (head[k]) {
             const int c = cellpos[k];
-            const uint64_t key = keys[k];
+            const uint64_t key = keys[k] >> sb;
             cell_start[c] = k;
             cell_key[c] = key;
             uint64_t h = mix64(key) & hmask;
@@ -330,10 +344,22 @@ __global__ void __launch_bounds__(256) link_kernel(
         }
         const int spre = incl - sn;
         const int total = __shfl_sync(0xffffffffu, incl, kHomeSeg);
+        // bounding box of the home chunk: a candidate farther than the linking length from it
+        // cannot link to any home particle
+        float bl[3] = {hv ? hp.x : INFINITY, hv ? hp.y : INFINITY, hv ? hp.z : INFINITY};
+        float bh[3] = {hv ? hp.x : -INFINITY, hv ? hp.y : -INFINITY, hv ? hp.z : -INFINITY};
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                bl[d] = fminf(bl[d], __shfl_xor_sync(0xffffffffu, bl[d], o));
+                bh[d] = fmaxf(bh[d], __shfl_xor_sync(0xffffffffu, bh[d], o));
+            }
+        }
         int myroot = hv ? uf_find_cached(parent, k, err) : -1;
         for (int v0 = 0; v0 < total; v0 += 32) {
             const int v = v0 + lane;
-            const bool cv = v < total;
+            bool cv = v < total;
             // segment of candidate v: the last segment starting at or before v (empty
             // segments share their successor's start and are passed over)
             int seg = 0;
@@ -349,24 +375,31 @@ __global__ void __launch_bounds__(256) link_kernel(
                 q.x += (float)((off & 3) - 1) * g.cs;
                 q.y += (float)(((off >> 2) & 3) - 1) * g.cs;
                 q.z += (float)(((off >> 4) & 3) - 1) * g.cs;
-                // roots of the candidates, found once per round instead of once per hit; a
-                // root read here may be outdated by later unions, which is safe: equal roots
-                // prove the same set, unequal ones are re-checked by uf_union
-                rql = uf_find_cached(parent, jl, err);
+                const float ex = fmaxf(0.f, fmaxf(bl[0] - q.x, q.x - bh[0]));
+                const float ey = fmaxf(0.f, fmaxf(bl[1] - q.y, q.y - bh[1]));
+                const float ez = fmaxf(0.f, fmaxf(bl[2] - q.z, q.z - bh[2]));
+                cv = fmaf(ex, ex, fmaf(ey, ey, ez * ez)) <= g.hi;
             }
-            // pick up unions made by other warps since the last look (helps the skip below)
+            if (!__any_sync(0xffffffffu, cv)) continue;
+            // roots of the candidates, found once per round instead of once per hit; a root
+            // read here may be outdated by later unions, which is safe: equal roots prove the
+            // same set, unequal ones are re-checked by uf_union
+            if (cv) rql = uf_find_cached(parent, jl, err);
+            // pick up unions made by other warps since the last look
             if (v0 > 0 && hv) myroot = uf_find_cached(parent, k, err);
-            // every home particle and every candidate of this round already in one set: no
-            // test here can join anything new, skip the 32 x 32 block
+            // when every home particle is in one set, candidates already in it need no test
             const int r0 = __shfl_sync(0xffffffffu, myroot, 0);   // lane 0 is always a home particle
-            if (__all_sync(0xffffffffu, (!hv || myroot == r0) && (!cv || rql == r0))) continue;
+            const bool uniform = __all_sync(0xffffffffu, !hv || myroot == r0);
+            unsigned todo = __ballot_sync(0xffffffffu, cv && !(uniform && rql == r0));
+            if (!todo) continue;
             __syncwarp();
             buf[w][lane] = q;
             rbuf[w][lane] = rql;
             jbuf[w][lane] = seg == kHomeSeg ? jl : ~jl;   // home-cell candidates keep the j > k test
             __syncwarp();
-            const int cnt = min(32, total - v0);
-            for (int t = 0; t < cnt; ++t) {
+            while (todo) {
+                const int t = __ffs(todo) - 1;
+                todo &= todo - 1;
                 const float4 qq = buf[w][t];
                 const int jb = jbuf[w][t];
                 const float dx = qq.x - hp.x, dy = qq.y - hp.y, dz = qq.z - hp.z;
@@ -464,7 +497,9 @@ int fof_device(int n, const double *x, const double *y, const double *z, double 
         const long double cells = (long double)g.ncx * g.ncy * g.ncz;
         if (cells > 4.0e18L)
             return fail(HALMA_ERR_CAPACITY, "cell grid too large (%lld x %lld x %lld cells)", g.ncx, g.ncy, g.ncz);
-        const int end_bit = bits_for((uint64_t)(g.ncx * g.ncy * g.ncz - 1));
+        const int cell_bits = bits_for((uint64_t)(g.ncx * g.ncy * g.ncz - 1));
+        g.sb = cell_bits <= 58 ? 6 : 0;
+        const int end_bit = cell_bits + g.sb;
 
         // pass 2: everything else, one workspace layout sized by n
         uint64_t hcap = 1;
@@ -507,7 +542,7 @@ int fof_device(int n, const double *x, const double *y, const double *z, double 
         HALMA_TRY(sort_pairs_u64_i32(tmp, sort_b, kin, kout, vin, vout, n, end_bit, st));
         HALMA_LAUNCH(prep_kernel, g1, 256, 0, st, x, y, z, n, g, kout, vout, rec, head, parent, has, minidx);
         HALMA_TRY(exclusive_sum_i32(tmp, scan_b, head, cpos, n, st));
-        HALMA_LAUNCH(cells_kernel, g1, 256, 0, st, n, kout, head, cpos, cst, ckey, hk, hv, hcap - 1, cnt + 0);
+        HALMA_LAUNCH(cells_kernel, g1, 256, 0, st, n, g.sb, kout, head, cpos, cst, ckey, hk, hv, hcap - 1, cnt + 0);
         HALMA_LAUNCH(itemflag_kernel, g1, 256, 0, st, n, head, cpos, cst, flag);
         HALMA_TRY(exclusive_sum_i32(tmp, scan_b, flag, ipos, n, st));
         HALMA_LAUNCH(items_kernel, g1, 256, 0, st, n, head, cpos, flag, ipos, ik0, icell, cnt + 1);
