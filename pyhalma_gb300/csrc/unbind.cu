@@ -38,6 +38,7 @@ constexpr float kFar = 3.0e30f;
 struct HaloState {   // per halo, FP64 unless stated
     double M, cx, cy, cz, vx, vy, vz, ekin, epot;
     int nb, active, iter, removed, nrem;   // nrem: removed by the last pass (next pass's sources)
+    int nprev;                             // slots the last pass examined (nb before its cut)
 };
 
 __device__ __forceinline__ double warp_sum(double v) {
@@ -45,9 +46,10 @@ __device__ __forceinline__ double warp_sum(double v) {
     return v;
 }
 
-// Block-wide FP64 sum of NV values (fixed association: warp tree, then warps in order).
+// Block-wide FP64 sums of NV values written to out[0..NV) (fixed association: warp tree,
+// then the warps in order).
 template <int NV>
-__device__ __forceinline__ void block_sum(double (&v)[NV], double (*sh)[32]) {
+__device__ __forceinline__ void block_sum_store(const double (&v)[NV], double (*sh)[32], double *out) {
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
 #pragma unroll
     for (int q = 0; q < NV; ++q) {
@@ -60,13 +62,9 @@ __device__ __forceinline__ void block_sum(double (&v)[NV], double (*sh)[32]) {
         for (int q = 0; q < NV; ++q) {
             double s = lane < nw ? sh[q][lane] : 0.0;
             s = warp_sum(s);
-            if (lane == 0) sh[q][0] = s;
+            if (lane == 0) out[q] = s;
         }
     }
-    __syncthreads();
-#pragma unroll
-    for (int q = 0; q < NV; ++q) v[q] = sh[q][0];
-    __syncthreads();
 }
 
 __global__ void ub_init_kernel(int64_t n, unsigned char *bound, int nh, HaloState *hs) {
@@ -79,31 +77,62 @@ __global__ void ub_init_kernel(int64_t n, unsigned char *bound, int nh, HaloStat
     }
 }
 
-// Per active halo: FP64 bound mass, centre and bulk velocity (one block per halo).
-__global__ void __launch_bounds__(256) ub_reduce_kernel(const int64_t *__restrict__ off, const double *__restrict__ x,
-                                                        const double *__restrict__ y, const double *__restrict__ z,
-                                                        const double *__restrict__ vx, const double *__restrict__ vy,
-                                                        const double *__restrict__ vz, const double *__restrict__ m,
-                                                        const unsigned char *__restrict__ bound, HaloState *hs,
-                                                        int force) {
-    const int h = blockIdx.x;
+// Member chunks: every halo's CSR range is cut into chunks of kSeg members, chunk c covering
+// members off[h] + (c - cstart[h]) * kSeg onward of halo h = chunk_h[c] (laid out on the host),
+// so a large halo is spread over many blocks.
+constexpr int kSeg = 1024;
+constexpr int kSegThreads = 256;
+constexpr int kSegPer = kSeg / kSegThreads;
+constexpr int kRedSums = 8;   // M, Mx, My, Mz, Mvx, Mvy, Mvz, count
+
+// Per member chunk of an active halo (or of every halo with force): FP64 sums over its bound
+// members (fixed association: per thread in member order, then the block tree).
+__global__ void __launch_bounds__(kSegThreads) ub_reduce_seg_kernel(
+    const int64_t *__restrict__ off, const int *__restrict__ cstart, const int *__restrict__ chunk_h,
+    const double *__restrict__ x, const double *__restrict__ y, const double *__restrict__ z,
+    const double *__restrict__ vx, const double *__restrict__ vy, const double *__restrict__ vz,
+    const double *__restrict__ m, const unsigned char *__restrict__ bound, const HaloState *__restrict__ hs,
+    int force, double *__restrict__ part) {
+    const int c = blockIdx.x;
+    const int h = chunk_h[c];
     if (!force && !hs[h].active) return;
-    __shared__ double sh[8][32];
-    double v[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-    for (int64_t i = off[h] + threadIdx.x; i < off[h + 1]; i += blockDim.x) {
-        if (!bound[i]) continue;
-        const double mi = m[i];
-        v[0] += mi;
-        v[1] += mi * x[i];
-        v[2] += mi * y[i];
-        v[3] += mi * z[i];
-        v[4] += mi * vx[i];
-        v[5] += mi * vy[i];
-        v[6] += mi * vz[i];
-        v[7] += 1.0;
+    __shared__ double sh[kRedSums][32];
+    const int64_t b = off[h] + (int64_t)(c - cstart[h]) * kSeg;
+    const int64_t e = min(off[h + 1], b + kSeg);
+    double v[kRedSums] = {0, 0, 0, 0, 0, 0, 0, 0};
+#pragma unroll
+    for (int j = 0; j < kSegPer; ++j) {
+        const int64_t i = b + j * kSegThreads + threadIdx.x;
+        if (i < e && bound[i]) {
+            const double mi = m[i];
+            v[0] += mi;
+            v[1] += mi * x[i];
+            v[2] += mi * y[i];
+            v[3] += mi * z[i];
+            v[4] += mi * vx[i];
+            v[5] += mi * vy[i];
+            v[6] += mi * vz[i];
+            v[7] += 1.0;
+        }
     }
-    block_sum<8>(v, sh);
-    if (threadIdx.x == 0) {
+    block_sum_store<kRedSums>(v, sh, part + (int64_t)c * kRedSums);
+}
+
+// One warp per halo: chunk sums added in a fixed order (lane-strided, then the warp tree);
+// sets the bound mass, centre of mass, bulk velocity and bound count.
+__global__ void ub_reduce_fin_kernel(int nh, const int *__restrict__ cstart, const double *__restrict__ part,
+                                     int force, HaloState *hs) {
+    const int h = (int)((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5);
+    const int lane = threadIdx.x & 31;
+    if (h >= nh) return;
+    if (!force && !hs[h].active) return;
+    double v[kRedSums] = {0, 0, 0, 0, 0, 0, 0, 0};
+    for (int c = cstart[h] + lane; c < cstart[h + 1]; c += 32)
+#pragma unroll
+        for (int k = 0; k < kRedSums; ++k) v[k] += part[(int64_t)c * kRedSums + k];
+#pragma unroll
+    for (int k = 0; k < kRedSums; ++k) v[k] = warp_sum(v[k]);
+    if (lane == 0) {
         HaloState &s = hs[h];
         const double M = v[0];
         s.M = M;
@@ -117,52 +146,36 @@ __global__ void __launch_bounds__(256) ub_reduce_kernel(const int64_t *__restric
     }
 }
 
-// Stable compaction of the bound members of each active halo into its padded slot range.
+// First packing, per member chunk: every member is bound before the first pass, so member
+// i of halo h goes to slot i - off[h] of the halo's padded range, re-centred on the halo's
+// centre of mass; the chunk holding the halo's end also writes the padding (zero-mass far
+// points up to the next multiple of 32).
 template <class V>
-__global__ void __launch_bounds__(256) ub_pack_kernel(const int64_t *__restrict__ off, const int64_t *__restrict__ poff,
-                                                      const double *__restrict__ x, const double *__restrict__ y,
-                                                      const double *__restrict__ z, const double *__restrict__ m,
-                                                      const unsigned char *__restrict__ bound, const HaloState *hs,
-                                                      V *__restrict__ pk, int *__restrict__ pidx) {
-    const int h = blockIdx.x;
-    if (!hs[h].active) return;
-    __shared__ int wcount[8];
-    __shared__ int running;
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+__global__ void __launch_bounds__(kSegThreads) ub_pack_kernel(
+    const int64_t *__restrict__ off, const int64_t *__restrict__ poff, const int *__restrict__ cstart,
+    const int *__restrict__ chunk_h, const double *__restrict__ x, const double *__restrict__ y,
+    const double *__restrict__ z, const double *__restrict__ m, const HaloState *__restrict__ hs,
+    V *__restrict__ pk, int *__restrict__ pidx) {
+    const int c = blockIdx.x;
+    const int h = chunk_h[c];
     const double cx = hs[h].cx, cy = hs[h].cy, cz = hs[h].cz;
-    const int64_t b = off[h], e = off[h + 1], pb = poff[h];
-    if (threadIdx.x == 0) running = 0;
-    __syncthreads();
-    for (int64_t i0 = b; i0 < e; i0 += blockDim.x) {
-        const int64_t i = i0 + threadIdx.x;
-        const bool keep = i < e && bound[i];
-        const unsigned bal = __ballot_sync(0xffffffffu, keep);
-        if (lane == 0) wcount[w] = __popc(bal);
-        __syncthreads();
-        int before = running;
-        for (int q = 0; q < w; ++q) before += wcount[q];
-        const int rank = before + __popc(bal & ((1u << lane) - 1u));
-        if (keep) {
-            V r;
-            r.x = x[i] - cx; r.y = y[i] - cy; r.z = z[i] - cz; r.w = m[i];
-            pk[pb + rank] = r;
-            pidx[pb + rank] = (int)(i);
-        }
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            int tot = 0;
-            for (int q = 0; q < (int)(blockDim.x >> 5); ++q) tot += wcount[q];
-            running += tot;
-        }
-        __syncthreads();
+    const int64_t hb = off[h], he = off[h + 1], pb = poff[h];
+    const int64_t b = hb + (int64_t)(c - cstart[h]) * kSeg;
+    const int64_t e = min(he, b + kSeg);
+    for (int64_t i = b + threadIdx.x; i < e; i += kSegThreads) {
+        V r;
+        r.x = x[i] - cx; r.y = y[i] - cy; r.z = z[i] - cz; r.w = m[i];
+        pk[pb + (i - hb)] = r;
+        pidx[pb + (i - hb)] = (int)i;
     }
-    const int nb = running;
-    const int npad = (nb + 31) & ~31;
-    for (int r = nb + threadIdx.x; r < npad; r += blockDim.x) {
-        V f;
-        f.x = f.y = f.z = kFar; f.w = 0;
-        pk[pb + r] = f;
-        pidx[pb + r] = -1;
+    if (e == he) {
+        const int64_t nb = he - hb, npad = (nb + 31) & ~31ll;
+        for (int64_t r = nb + threadIdx.x; r < npad; r += kSegThreads) {
+            V f;
+            f.x = f.y = f.z = kFar; f.w = 0;
+            pk[pb + r] = f;
+            pidx[pb + r] = -1;
+        }
     }
 }
 
@@ -178,8 +191,7 @@ __device__ __forceinline__ int tile_t_for(const TileTable &tab, int nb) {
 // by idesc[q] = (halo, T, slices, unused); item i of that halo is (tile i / slices,
 // slice i % slices).  Only nh+1 prefix counts are written per pass.
 // The same pass also lays out the energy segments: active ordered halo q owns segments
-// sstart[q] .. sstart[q+1]-1 of kSeg slots each.
-constexpr int kSeg = 1024;
+// sstart[q] .. sstart[q+1]-1 of kSeg slots each; sown[seg] names the segment's ordered halo.
 
 __device__ __forceinline__ int warp_incl_scan(int v, int lane) {
     for (int o = 1; o < 32; o <<= 1) {
@@ -192,7 +204,8 @@ __device__ __forceinline__ int warp_incl_scan(int v, int lane) {
 __global__ void __launch_bounds__(1024) ub_items_kernel(int nh, const int *__restrict__ order, const HaloState *hs,
                                                         TileTable tab, int slice_len, int inc,
                                                         int *__restrict__ istart, int4 *__restrict__ idesc,
-                                                        int *__restrict__ sstart, int *__restrict__ nitems,
+                                                        int *__restrict__ sstart, int *__restrict__ sown,
+                                                        int *__restrict__ nitems,
                                                         int *__restrict__ counter, int *__restrict__ nsegs,
                                                         unsigned long long *__restrict__ pairs_out) {
     __shared__ int wsum[32], wseg[32];
@@ -235,7 +248,9 @@ __global__ void __launch_bounds__(1024) ub_items_kernel(int nh, const int *__res
         if (q < nh) {
             istart[q] = pre + incl - cnt;
             idesc[q] = make_int4(h, T, max(nsl, 1), 0);
-            sstart[q] = spre + sincl - nseg;
+            const int s0 = spre + sincl - nseg;
+            sstart[q] = s0;
+            for (int sg = 0; sg < nseg; ++sg) sown[s0 + sg] = q;
         }
         __syncthreads();
         if (threadIdx.x == 0) {
@@ -257,17 +272,6 @@ __global__ void __launch_bounds__(1024) ub_items_kernel(int nh, const int *__res
         *nsegs = sbase;
         if (pairs_out) *pairs_out = pairs;
     }
-}
-
-// Ordered halo owning work unit u: the last q with start[q] <= u.
-__device__ __forceinline__ int owner_of(const int *__restrict__ start, int nh, int u) {
-    int lo = 0, hi = nh - 1;
-    while (lo < hi) {
-        const int mid = (lo + hi + 1) >> 1;
-        if (start[mid] <= u) lo = mid;
-        else hi = mid - 1;
-    }
-    return lo;
 }
 
 // 32 sources of the staged chunk against T targets, two sources per f32x2 instruction.
@@ -417,45 +421,54 @@ __global__ void __launch_bounds__(256) ub_pair_kernel(const float4 *__restrict__
 constexpr int kSegSums = 12;   // removed, kept, ekin, epot, M, Mx, My, Mz, Mvx, Mvy, Mvz, unused
 
 template <class V>
-__global__ void __launch_bounds__(256) ub_energy_seg_kernel(int nh, const int *__restrict__ sstart,
-                                                            const int4 *__restrict__ idesc, const int *__restrict__ nsegs,
-                                                            const int64_t *__restrict__ poff, const int64_t *__restrict__ qoff,
-                                                            int slice_len, int inc, const int *__restrict__ pidx,
-                                                            const double *__restrict__ part,
-                                                            const double *__restrict__ phi_prev, double *__restrict__ phi_cur,
-                                                            const double *__restrict__ x,
-                                                            const double *__restrict__ y, const double *__restrict__ z,
-                                                            const double *__restrict__ vx, const double *__restrict__ vy,
-                                                            const double *__restrict__ vz, const double *__restrict__ m,
-                                                            double gfac, const HaloState *__restrict__ hs,
-                                                            unsigned char *__restrict__ bound, double *__restrict__ phi_out,
-                                                            unsigned char *__restrict__ keepf,
-                                                            double *__restrict__ seg_sums) {
+__global__ void __launch_bounds__(kSegThreads) ub_energy_seg_kernel(
+    const int *__restrict__ sstart, const int *__restrict__ sown, const int4 *__restrict__ idesc,
+    const int *__restrict__ nsegs, const int64_t *__restrict__ poff, const int64_t *__restrict__ qoff,
+    int slice_len, int inc, const int *__restrict__ pidx, const double *__restrict__ part,
+    const double *__restrict__ phi_prev, double *__restrict__ phi_cur, const double *__restrict__ x,
+    const double *__restrict__ y, const double *__restrict__ z, const double *__restrict__ vx,
+    const double *__restrict__ vy, const double *__restrict__ vz, const double *__restrict__ m, double gfac,
+    const HaloState *__restrict__ hs, unsigned char *__restrict__ bound, double *__restrict__ phi_out,
+    unsigned char *__restrict__ keepf, double *__restrict__ seg_sums) {
     const int seg = blockIdx.x;
     if (seg >= *nsegs) return;
     __shared__ double sh[kSegSums][32];
-    const int q = owner_of(sstart, nh, seg);
+    const int q = sown[seg];
     const int h = idesc[q].x;
     const int sl = seg - sstart[q];
     const HaloState s = hs[h];
     const int64_t pb = poff[h], npad = poff[h + 1] - pb, qb = qoff[h];
     const int ns = inc ? s.nrem : s.nb;
     const int nsl = (int)(((int64_t)ns + slice_len - 1) / slice_len);
-    double v[kSegSums] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
     const int rend = min(s.nb, (sl + 1) * kSeg);
-    for (int r = sl * kSeg + threadIdx.x; r < rend; r += blockDim.x) {
-        const int i = pidx[pb + r];
+    // the segment's kSegPer slots per thread are loaded together (independent gathers in
+    // flight), then evaluated in slot order
+    int r[kSegPer], ii[kSegPer];
+    double d[kSegPer];
+#pragma unroll
+    for (int j = 0; j < kSegPer; ++j) {
+        r[j] = sl * kSeg + j * kSegThreads + threadIdx.x;
+        ii[j] = r[j] < rend ? pidx[pb + r[j]] : -1;
+        d[j] = 0.0;
+    }
+    for (int k = 0; k < nsl; ++k)   // slices in order
+#pragma unroll
+        for (int j = 0; j < kSegPer; ++j)
+            if (ii[j] >= 0) d[j] += part[qb + (int64_t)k * npad + r[j]];
+    double v[kSegSums] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+#pragma unroll
+    for (int j = 0; j < kSegPer; ++j) {
+        const int i = ii[j];
+        if (i < 0) continue;
         const double dvx = vx[i] - s.vx, dvy = vy[i] - s.vy, dvz = vz[i] - s.vz;
         const double ek = 0.5 * (dvx * dvx + dvy * dvy + dvz * dvz);
-        double d = 0.0;
-        for (int k = 0; k < nsl; ++k) d += part[qb + (int64_t)k * npad + r];   // slices in order
         // full pass: the sum itself; incremental pass: previous potential minus the removed
         // particles' contribution
-        const double p = inc ? phi_prev[pb + r] - d : d;
-        phi_cur[pb + r] = p;
+        const double p = inc ? phi_prev[pb + r[j]] - d[j] : d[j];
+        phi_cur[pb + r[j]] = p;
         const double e = ek - gfac * p;
         const bool keep = !(e > 0.0);
-        keepf[pb + r] = keep ? 1 : 0;
+        keepf[pb + r[j]] = keep ? 1 : 0;
         if (!keep) {
             bound[i] = 0;
             v[0] += 1.0;
@@ -475,102 +488,43 @@ __global__ void __launch_bounds__(256) ub_energy_seg_kernel(int nh, const int *_
             if (phi_out) phi_out[i] = p;
         }
     }
-    block_sum<kSegSums>(v, sh);
-    if (threadIdx.x < kSegSums) seg_sums[(int64_t)seg * kSegSums + threadIdx.x] = v[threadIdx.x];
+    block_sum_store<kSegSums>(v, sh, seg_sums + (int64_t)seg * kSegSums);
 }
 
-template <class V>
-__global__ void __launch_bounds__(256) ub_compact_seg_kernel(int nh, const int *__restrict__ sstart,
-                                                             const int4 *__restrict__ idesc, const int *__restrict__ nsegs,
-                                                             const int64_t *__restrict__ poff,
-                                                             const HaloState *__restrict__ hs,
-                                                             const unsigned char *__restrict__ keepf,
-                                                             const double *__restrict__ seg_sums,
-                                                             const V *__restrict__ pk_in, const int *__restrict__ pidx_in,
-                                                             const double *__restrict__ phi_cur,
-                                                             V *__restrict__ pk_out, int *__restrict__ pidx_out,
-                                                             double *__restrict__ phi_next, V *__restrict__ removed) {
-    const int seg = blockIdx.x;
-    if (seg >= *nsegs) return;
-    __shared__ int wcount[8], wrem[8];
-    __shared__ int running, rrunning;
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const int q = owner_of(sstart, nh, seg);
-    const int h = idesc[q].x;
-    const int s0 = sstart[q], sl = seg - s0, nseg = sstart[q + 1] - s0;
-    const int nb = hs[h].nb;
-    const int64_t pb = poff[h];
-    if (threadIdx.x == 0) {
-        int o = 0, orem = 0;   // survivors / removed of the earlier segments of this halo
-        for (int k = 0; k < sl; ++k) {
-            orem += (int)seg_sums[(int64_t)(s0 + k) * kSegSums + 0];
-            o += (int)seg_sums[(int64_t)(s0 + k) * kSegSums + 1];
-        }
-        running = o;
-        rrunning = orem;
-    }
-    __syncthreads();
-    const int rend = min(nb, (sl + 1) * kSeg);
-    for (int r0 = sl * kSeg; r0 < rend; r0 += blockDim.x) {
-        const int r = r0 + threadIdx.x;
-        const bool valid = r < rend;
-        const bool keep = valid && keepf[pb + r];
-        const bool gone = valid && !keep;
-        const unsigned bal = __ballot_sync(0xffffffffu, keep);
-        const unsigned bgone = __ballot_sync(0xffffffffu, gone);
-        if (lane == 0) {
-            wcount[w] = __popc(bal);
-            wrem[w] = __popc(bgone);
-        }
-        __syncthreads();
-        int rank = running, rrank = rrunning;
-        for (int k = 0; k < w; ++k) {
-            rank += wcount[k];
-            rrank += wrem[k];
-        }
-        rank += __popc(bal & ((1u << lane) - 1u));
-        rrank += __popc(bgone & ((1u << lane) - 1u));
-        if (keep) {
-            pk_out[pb + rank] = pk_in[pb + r];
-            pidx_out[pb + rank] = pidx_in[pb + r];
-            phi_next[pb + rank] = phi_cur[pb + r];
-        } else if (gone) {
-            removed[pb + rrank] = pk_in[pb + r];   // sources of the next incremental pass
-        }
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            int tot = 0, trem = 0;
-            for (int k = 0; k < (int)(blockDim.x >> 5); ++k) {
-                tot += wcount[k];
-                trem += wrem[k];
-            }
-            running += tot;
-            rrunning += trem;
-        }
-        __syncthreads();
-    }
-    if (sl == nseg - 1) {   // the halo's last segment pads after the survivors and the removed
-        V f;
-        f.x = f.y = f.z = kFar;
-        f.w = 0;
-        const int nkeep = running, nrem = rrunning;
-        for (int r = nkeep + threadIdx.x; r < ((nkeep + 31) & ~31); r += blockDim.x) {
-            pk_out[pb + r] = f;
-            pidx_out[pb + r] = -1;
-        }
-        for (int r = nrem + threadIdx.x; r < ((nrem + 31) & ~31); r += blockDim.x) removed[pb + r] = f;
-    }
-}
-
+// One warp per active ordered halo, after the energy pass: the halo's segment sums added in a
+// fixed order (lane-strided, then the warp tree), so the result does not depend on timing;
+// removals, pass count, energies and the next pass's mass, centre and bulk velocity.  A halo
+// whose pass removed nothing becomes inactive.  Also writes, per segment, the survivors and
+// removed particles of the halo's earlier segments (seg_pre), where compaction starts writing.
 __global__ void ub_finalize_kernel(int nh, const int *__restrict__ order, const int *__restrict__ sstart,
-                                   const double *__restrict__ seg_sums, double gfac, HaloState *hs) {
-    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < nh; q += gridDim.x * blockDim.x) {
-        const int h = order[q];
-        HaloState &o = hs[h];
-        if (!o.active) continue;
-        double v[kSegSums] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
-        for (int sg = sstart[q]; sg < sstart[q + 1]; ++sg)
+                                   const double *__restrict__ seg_sums, double gfac, HaloState *hs,
+                                   int2 *__restrict__ seg_pre) {
+    const int q = (int)((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5);
+    const int lane = threadIdx.x & 31;
+    if (q >= nh) return;
+    const int h = order[q];
+    if (!hs[h].active) return;
+    const int s0 = sstart[q], s1 = sstart[q + 1];
+    double v[kSegSums] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+    int keep_run = 0, rem_run = 0;
+    for (int b0 = s0; b0 < s1; b0 += 32) {
+        const int sg = b0 + lane;
+        const bool ok = sg < s1;
+        const int nrem = ok ? (int)seg_sums[(int64_t)sg * kSegSums + 0] : 0;
+        const int nkeep = ok ? (int)seg_sums[(int64_t)sg * kSegSums + 1] : 0;
+        const int ri = warp_incl_scan(nrem, lane), ki = warp_incl_scan(nkeep, lane);
+        if (ok) seg_pre[sg] = make_int2(keep_run + ki - nkeep, rem_run + ri - nrem);
+        keep_run += __shfl_sync(0xffffffffu, ki, 31);
+        rem_run += __shfl_sync(0xffffffffu, ri, 31);
+        if (ok)
+#pragma unroll
             for (int k = 0; k < kSegSums; ++k) v[k] += seg_sums[(int64_t)sg * kSegSums + k];
+    }
+#pragma unroll
+    for (int k = 0; k < kSegSums; ++k) v[k] = warp_sum(v[k]);
+    if (lane == 0) {
+        HaloState &o = hs[h];
+        o.nprev = o.nb;
         o.removed = (int)v[0];
         o.nrem = (int)v[0];
         o.iter += 1;
@@ -589,6 +543,78 @@ __global__ void ub_finalize_kernel(int nh, const int *__restrict__ order, const 
                 o.cx = o.cy = o.cz = o.vx = o.vy = o.vz = 0.0;
             }
         }
+    }
+}
+
+// Per segment of a halo that stays active: survivors copied in order into the other packed
+// buffer (with their potential, the next incremental pass's starting point), removed
+// particles into the removed list (the next pass's sources); the halo's last segment pads
+// both to a multiple of 32 with zero-mass far points.
+template <class V>
+__global__ void __launch_bounds__(kSegThreads) ub_compact_seg_kernel(
+    const int *__restrict__ sstart, const int *__restrict__ sown, const int4 *__restrict__ idesc,
+    const int *__restrict__ nsegs, const int64_t *__restrict__ poff, const HaloState *__restrict__ hs,
+    const unsigned char *__restrict__ keepf, const int2 *__restrict__ seg_pre, const V *__restrict__ pk_in,
+    const int *__restrict__ pidx_in, const double *__restrict__ phi_cur, V *__restrict__ pk_out,
+    int *__restrict__ pidx_out, double *__restrict__ phi_next, V *__restrict__ removed) {
+    const int seg = blockIdx.x;
+    if (seg >= *nsegs) return;
+    __shared__ int wcount[kSegThreads / 32], wrem[kSegThreads / 32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int q = sown[seg];
+    const int h = idesc[q].x;
+    if (!hs[h].active) return;   // converged this pass: its packed slots are not read again
+    const int s0 = sstart[q], sl = seg - s0, nseg = sstart[q + 1] - s0;
+    const int nb = hs[h].nprev;
+    const int64_t pb = poff[h];
+    const int2 pre = seg_pre[seg];
+    int running = pre.x, rrunning = pre.y;
+    const int rend = min(nb, (sl + 1) * kSeg);
+    for (int r0 = sl * kSeg; r0 < rend; r0 += kSegThreads) {
+        const int r = r0 + threadIdx.x;
+        const bool valid = r < rend;
+        const bool keep = valid && keepf[pb + r];
+        const bool gone = valid && !keep;
+        const unsigned bal = __ballot_sync(0xffffffffu, keep);
+        const unsigned bgone = __ballot_sync(0xffffffffu, gone);
+        if (lane == 0) {
+            wcount[w] = __popc(bal);
+            wrem[w] = __popc(bgone);
+        }
+        __syncthreads();
+        int rank = running, rrank = rrunning, tot = 0, trem = 0;
+#pragma unroll
+        for (int k = 0; k < kSegThreads / 32; ++k) {
+            if (k < w) {
+                rank += wcount[k];
+                rrank += wrem[k];
+            }
+            tot += wcount[k];
+            trem += wrem[k];
+        }
+        rank += __popc(bal & ((1u << lane) - 1u));
+        rrank += __popc(bgone & ((1u << lane) - 1u));
+        if (keep) {
+            pk_out[pb + rank] = pk_in[pb + r];
+            pidx_out[pb + rank] = pidx_in[pb + r];
+            phi_next[pb + rank] = phi_cur[pb + r];
+        } else if (gone) {
+            removed[pb + rrank] = pk_in[pb + r];
+        }
+        running += tot;
+        rrunning += trem;
+        __syncthreads();
+    }
+    if (sl == nseg - 1) {   // the halo's last segment pads after the survivors and the removed
+        V f;
+        f.x = f.y = f.z = kFar;
+        f.w = 0;
+        const int nkeep = running, nrem = rrunning;
+        for (int r = nkeep + threadIdx.x; r < ((nkeep + 31) & ~31); r += kSegThreads) {
+            pk_out[pb + r] = f;
+            pidx_out[pb + r] = -1;
+        }
+        for (int r = nrem + threadIdx.x; r < ((nrem + 31) & ~31); r += kSegThreads) removed[pb + r] = f;
     }
 }
 
@@ -682,14 +708,19 @@ int unbind_device(int64_t n, int nh, const int64_t *d_off, const int64_t *h_off,
     poff[0] = 0;
     qoff[0] = 0;
     int64_t segcap = 0;   // energy segments at most (initial sizes)
+    std::vector<int> cstart(nh + 1), chunk_h;   // member chunks of kSeg (reduce and first pack)
     for (int h = 0; h < nh; ++h) {
         const int64_t c = h_off[h + 1] - h_off[h];
+        cstart[h] = (int)chunk_h.size();
+        for (int64_t k = 0; k < (c + kSeg - 1) / kSeg; ++k) chunk_h.push_back(h);
         const int64_t npad = ((c + 31) / 32) * 32;
         const int64_t nsl = std::max<int64_t>(1, (c + slice_len - 1) / slice_len);
         poff[h + 1] = poff[h] + npad;
         qoff[h + 1] = qoff[h] + npad * nsl;
         segcap += std::max<int64_t>(1, (c + kSeg - 1) / kSeg);
     }
+    cstart[nh] = (int)chunk_h.size();
+    const int nchunks = (int)chunk_h.size();
     if (segcap >= (1ll << 31)) return fail(HALMA_ERR_CAPACITY, "too many energy segments");
     std::iota(order.begin(), order.end(), 0);
     std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
@@ -713,6 +744,11 @@ int unbind_device(int64_t n, int nh, const int64_t *d_off, const int64_t *h_off,
     const size_t o_sstart = L.add(sizeof(int) * (nh + 1));
     const size_t o_idesc = L.add(sizeof(int4) * std::max(nh, 1));
     const size_t o_ssum = L.add(sizeof(double) * kSegSums * segcap);
+    const size_t o_sown = L.add(sizeof(int) * segcap);
+    const size_t o_spre = L.add(sizeof(int2) * segcap);
+    const size_t o_cst = L.add(sizeof(int) * (nh + 1));
+    const size_t o_chh = L.add(sizeof(int) * std::max(nchunks, 1));
+    const size_t o_rpart = L.add(sizeof(double) * kRedSums * std::max(nchunks, 1));
     const size_t o_cnt = L.add(64);
     const size_t o_pairs = L.add(sizeof(unsigned long long) * p.max_iter);
     const size_t o_off = d_off ? 0 : L.add(sizeof(int64_t) * (nh + 1));
@@ -732,6 +768,11 @@ int unbind_device(int64_t n, int nh, const int64_t *d_off, const int64_t *h_off,
     auto *sstart = at<int>(base, o_sstart);
     auto *idesc = at<int4>(base, o_idesc);
     auto *ssum = at<double>(base, o_ssum);
+    auto *sown = at<int>(base, o_sown);
+    auto *segpre = at<int2>(base, o_spre);
+    auto *dcst = at<int>(base, o_cst);
+    auto *dchh = at<int>(base, o_chh);
+    auto *rpart = at<double>(base, o_rpart);
     int *cnt = at<int>(base, o_cnt);   // [0] nitems [1] counter [2] energy segments
     const int sgrid = (int)segcap;
     auto *dpairs = at<unsigned long long>(base, o_pairs);
@@ -750,6 +791,18 @@ int unbind_device(int64_t n, int nh, const int64_t *d_off, const int64_t *h_off,
     HALMA_CUDA(cudaMemcpyAsync(dpoff, poff.data(), sizeof(int64_t) * (nh + 1), cudaMemcpyHostToDevice, st));
     HALMA_CUDA(cudaMemcpyAsync(dqoff, qoff.data(), sizeof(int64_t) * (nh + 1), cudaMemcpyHostToDevice, st));
     HALMA_CUDA(cudaMemcpyAsync(dorder, order.data(), sizeof(int) * nh, cudaMemcpyHostToDevice, st));
+    HALMA_CUDA(cudaMemcpyAsync(dcst, cstart.data(), sizeof(int) * (nh + 1), cudaMemcpyHostToDevice, st));
+    if (nchunks > 0)
+        HALMA_CUDA(cudaMemcpyAsync(dchh, chunk_h.data(), sizeof(int) * nchunks, cudaMemcpyHostToDevice, st));
+    const int fgrid = grid_for((int64_t)nh * 32, 256);   // one warp per halo
+    // FP64 bound mass, centre and bulk velocity per halo (active ones, or all with force)
+    auto reduce = [&](cudaStream_t rs, int force) -> int {
+        if (nchunks > 0)
+            HALMA_LAUNCH(ub_reduce_seg_kernel, nchunks, kSegThreads, 0, rs, off, dcst, dchh, x, y, z, vx, vy, vz, m,
+                         bound, hs, force, rpart);
+        HALMA_LAUNCH(ub_reduce_fin_kernel, fgrid, 256, 0, rs, nh, dcst, rpart, force, hs);
+        return HALMA_OK;
+    };
     const double gfac = p.G * p.factor_v * p.factor_v;
     const float eps2 = (float)(p.eps * p.eps);
     HALMA_LAUNCH(ub_init_kernel, std::min(device_sm_count() * 8, grid_for(std::max<int64_t>(n, nh), 256)), 256, 0, st,
@@ -764,25 +817,27 @@ int unbind_device(int64_t n, int nh, const int64_t *d_off, const int64_t *h_off,
         auto record = [&](cudaStream_t rs) -> int {
             // first pass: centre of mass and packing into buffer 0; every pass then compacts
             // its survivors into the other buffer and sets the next pass's halo state
-            HALMA_LAUNCH(ub_reduce_kernel, nh, 256, 0, rs, off, x, y, z, vx, vy, vz, m, bound, hs, 0);
-            HALMA_LAUNCH(ub_pack_kernel<float4>, nh, 256, 0, rs, off, dpoff, x, y, z, m, bound, hs, pkb[0], pidxb[0]);
+            HALMA_TRY(reduce(rs, 0));
+            if (nchunks > 0)
+                HALMA_LAUNCH(ub_pack_kernel<float4>, nchunks, kSegThreads, 0, rs, off, dpoff, dcst, dchh, x, y, z, m,
+                             hs, pkb[0], pidxb[0]);
             float4 *rk = at<float4>(base, o_rk);
             for (int it = 0; it < p.max_iter; ++it) {
                 const int a = it & 1, b = a ^ 1;
                 const int inc = (it > 0 && incremental) ? 1 : 0;
                 HALMA_LAUNCH(ub_items_kernel, 1, 1024, 0, rs, nh, dorder, hs, tab, slice_len, inc, istart, idesc,
-                             sstart, cnt, cnt + 1, cnt + 2, profiling ? dpairs + it : nullptr);
+                             sstart, sown, cnt, cnt + 1, cnt + 2, profiling ? dpairs + it : nullptr);
                 // External: captured as an event-record node, so the replay records it
                 if (profiling) HALMA_CUDA(cudaEventRecordWithFlags(prof.ev0[it], rs, cudaEventRecordExternal));
                 HALMA_LAUNCH(ub_pair_kernel, pgrid, 256, 0, rs, pkb[a], rk, inc, dpoff, dqoff, hs, nh, istart, idesc,
                              cnt, cnt + 1, eps2, slice_len / 32, phi);
                 if (profiling) HALMA_CUDA(cudaEventRecordWithFlags(prof.ev1[it], rs, cudaEventRecordExternal));
-                HALMA_LAUNCH(ub_energy_seg_kernel<float4>, sgrid, 256, 0, rs, nh, sstart, idesc, cnt + 2, dpoff, dqoff,
-                             slice_len, inc, pidxb[a], phi, phin, phic, x, y, z, vx, vy, vz, m, gfac, hs, bound,
-                             phi_out, keepf, ssum);
-                HALMA_LAUNCH(ub_compact_seg_kernel<float4>, sgrid, 256, 0, rs, nh, sstart, idesc, cnt + 2, dpoff, hs,
-                             keepf, ssum, pkb[a], pidxb[a], phic, pkb[b], pidxb[b], phin, rk);
-                HALMA_LAUNCH(ub_finalize_kernel, grid_for(nh, 256), 256, 0, rs, nh, dorder, sstart, ssum, gfac, hs);
+                HALMA_LAUNCH(ub_energy_seg_kernel<float4>, sgrid, kSegThreads, 0, rs, sstart, sown, idesc, cnt + 2,
+                             dpoff, dqoff, slice_len, inc, pidxb[a], phi, phin, phic, x, y, z, vx, vy, vz, m, gfac, hs,
+                             bound, phi_out, keepf, ssum);
+                HALMA_LAUNCH(ub_finalize_kernel, fgrid, 256, 0, rs, nh, dorder, sstart, ssum, gfac, hs, segpre);
+                HALMA_LAUNCH(ub_compact_seg_kernel<float4>, sgrid, kSegThreads, 0, rs, sstart, sown, idesc, cnt + 2,
+                             dpoff, hs, keepf, segpre, pkb[a], pidxb[a], phic, pkb[b], pidxb[b], phin, rk);
             }
             return HALMA_OK;
         };
@@ -803,6 +858,7 @@ int unbind_device(int64_t n, int nh, const int64_t *d_off, const int64_t *h_off,
             key.push_back((uintptr_t)tab.n);
             key.push_back((uintptr_t)slice_len);
             key.push_back((uintptr_t)incremental);
+            key.push_back((uintptr_t)nchunks);
             for (int c = 0; c < tab.n; ++c) {
                 key.push_back((uintptr_t)tab.upper[c]);
                 key.push_back((uintptr_t)tab.t[c]);
@@ -841,7 +897,7 @@ int unbind_device(int64_t n, int nh, const int64_t *d_off, const int64_t *h_off,
             HALMA_TRY(record(st));
         }
         // final bound mass, centre and bulk velocity over the final bound sets
-        HALMA_LAUNCH(ub_reduce_kernel, nh, 256, 0, st, off, x, y, z, vx, vy, vz, m, bound, hs, 1);
+        HALMA_TRY(reduce(st, 1));
         if (profiling) {
             std::vector<unsigned long long> hp(p.max_iter);
             HALMA_CUDA(cudaMemcpyAsync(hp.data(), dpairs, sizeof(unsigned long long) * p.max_iter,
@@ -858,13 +914,15 @@ int unbind_device(int64_t n, int nh, const int64_t *d_off, const int64_t *h_off,
         // plain FP64 path: per pass, one pair launch per active halo, host checks convergence
         double4 *pkb[2] = {at<double4>(base, o_pk), at<double4>(base, o_pk2)};
         std::vector<HaloState> hh(nh);
-        HALMA_LAUNCH(ub_reduce_kernel, nh, 256, 0, st, off, x, y, z, vx, vy, vz, m, bound, hs, 0);
-        HALMA_LAUNCH(ub_pack_kernel<double4>, nh, 256, 0, st, off, dpoff, x, y, z, m, bound, hs, pkb[0], pidxb[0]);
+        HALMA_TRY(reduce(st, 0));
+        if (nchunks > 0)
+            HALMA_LAUNCH(ub_pack_kernel<double4>, nchunks, kSegThreads, 0, st, off, dpoff, dcst, dchh, x, y, z, m, hs,
+                         pkb[0], pidxb[0]);
         double4 *rk = at<double4>(base, o_rk);
         for (int it = 0; it < p.max_iter; ++it) {
             const int a = it & 1, b = a ^ 1;
             HALMA_LAUNCH(ub_items_kernel, 1, 1024, 0, st, nh, dorder, hs, tab, slice_len, 0, istart, idesc, sstart,
-                         cnt, cnt + 1, cnt + 2, nullptr);
+                         sown, cnt, cnt + 1, cnt + 2, nullptr);
             HALMA_CUDA(cudaMemcpyAsync(hh.data(), hs, sizeof(HaloState) * nh, cudaMemcpyDeviceToHost, st));
             HALMA_CUDA(cudaStreamSynchronize(st));
             int any = 0;
@@ -875,14 +933,14 @@ int unbind_device(int64_t n, int nh, const int64_t *d_off, const int64_t *h_off,
                              p.eps * p.eps, phi + poff[h]);
             }
             if (!any) break;
-            HALMA_LAUNCH(ub_energy_seg_kernel<double4>, sgrid, 256, 0, st, nh, sstart, idesc, cnt + 2, dpoff, dqoff,
-                         slice_len, 0, pidxb[a], phi, phin, phic, x, y, z, vx, vy, vz, m, gfac, hs, bound, phi_out,
-                         keepf, ssum);
-            HALMA_LAUNCH(ub_compact_seg_kernel<double4>, sgrid, 256, 0, st, nh, sstart, idesc, cnt + 2, dpoff, hs, keepf,
-                         ssum, pkb[a], pidxb[a], phic, pkb[b], pidxb[b], phin, rk);
-            HALMA_LAUNCH(ub_finalize_kernel, grid_for(nh, 256), 256, 0, st, nh, dorder, sstart, ssum, gfac, hs);
+            HALMA_LAUNCH(ub_energy_seg_kernel<double4>, sgrid, kSegThreads, 0, st, sstart, sown, idesc, cnt + 2, dpoff,
+                         dqoff, slice_len, 0, pidxb[a], phi, phin, phic, x, y, z, vx, vy, vz, m, gfac, hs, bound,
+                         phi_out, keepf, ssum);
+            HALMA_LAUNCH(ub_finalize_kernel, fgrid, 256, 0, st, nh, dorder, sstart, ssum, gfac, hs, segpre);
+            HALMA_LAUNCH(ub_compact_seg_kernel<double4>, sgrid, kSegThreads, 0, st, sstart, sown, idesc, cnt + 2, dpoff,
+                         hs, keepf, segpre, pkb[a], pidxb[a], phic, pkb[b], pidxb[b], phin, rk);
         }
-        HALMA_LAUNCH(ub_reduce_kernel, nh, 256, 0, st, off, x, y, z, vx, vy, vz, m, bound, hs, 1);
+        HALMA_TRY(reduce(st, 1));
     }
     if (halo_out) HALMA_LAUNCH(ub_output_kernel, grid_for(nh, 256), 256, 0, st, nh, hs, halo_out);
     return HALMA_OK;
