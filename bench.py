@@ -253,6 +253,7 @@ def run_gpu(args):
 
     # timed region: inputs resident in HBM, L2 flushed before every step
     ms, pairs, pair_ms, fof_ms, unbind_ms, passes = [], 0.0, 0.0, [], [], []
+    per_pass = []
     sampler = ClockSampler(local)
     sampler.start()
     launches0 = _lib.launch_count()
@@ -274,6 +275,7 @@ def run_gpu(args):
                 pairs += p
                 pair_ms += t
         passes.append(sum(1 for p, _ in st["passes"] if p > 0))
+        per_pass = [[int(p), round(t, 4)] for p, t in st["passes"] if p > 0]
     barrier()
     wall = time.perf_counter() - wall0
     launches = _lib.launch_count() - launches0
@@ -338,7 +340,7 @@ def run_gpu(args):
                 "peak_source": f"FP32 pipe: 128 lane-ops/clk/SM / 7 per pair x {sms} SMs x {sm_max:.0f} MHz "
                                f"(sm_max_mhz {src}) x {FLOPS_PER_PAIR} flops/pair (conventional count)",
                 "pairs_per_launch": pairs / max(n_pair_launches, 1), "ms_per_launch": pair_ms / max(n_pair_launches, 1),
-                "launches_timed": n_pair_launches}
+                "launches_timed": n_pair_launches, "last_step_passes_pairs_ms": per_pass}
     fof_gbs = FOF_BYTES_PER_PARTICLE * n / (statistics.mean(fof_ms) * 1e-3) / 1e9
     roofline_fof = {"bound": "hbm", "achieved": fof_gbs, "peak": hbm, "unit": "GB/s", "frac": fof_gbs / hbm,
                     "traffic": None, "ms": statistics.mean(fof_ms),

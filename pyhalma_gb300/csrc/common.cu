@@ -59,14 +59,14 @@ struct WsEntry {
     void *ptr = nullptr;
     size_t bytes = 0;
 };
-static std::map<int, WsEntry> &ws_map() {
-    static std::map<int, WsEntry> m;
+static std::map<std::pair<int, int>, WsEntry> &ws_map() {   // (device, slot)
+    static std::map<std::pair<int, int>, WsEntry> m;
     return m;
 }
 
-int workspace(size_t bytes, void **ptr, cudaStream_t stream) {
+int workspace(size_t bytes, void **ptr, cudaStream_t stream, int slot) {
     int d = current_device();
-    WsEntry &e = ws_map()[d];
+    WsEntry &e = ws_map()[{d, slot}];
     if (bytes == 0) bytes = 256;
     if (e.bytes < bytes) {
         if (e.ptr) {
@@ -131,7 +131,7 @@ int halma_release_workspace(void) {
     std::lock_guard<std::mutex> g(halma::api_mutex());
     for (auto &kv : halma::ws_map()) {
         if (kv.second.ptr) {
-            cudaSetDevice(kv.first);
+            cudaSetDevice(kv.first.first);
             cudaDeviceSynchronize();
             cudaFree(kv.second.ptr);
         }

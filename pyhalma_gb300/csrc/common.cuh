@@ -58,8 +58,10 @@ struct Layout {
     }
 };
 
-// Returns a device buffer of at least `bytes` (cached per device, grown on demand).
-int workspace(size_t bytes, void **ptr, cudaStream_t stream);
+// Returns a device buffer of at least `bytes`, cached per device and slot and grown on
+// demand.  Slot 0 is the scratch of one stage (FoF, unbinding, potentials); slot 1 holds what
+// the one-call pipeline keeps across its stages.
+int workspace(size_t bytes, void **ptr, cudaStream_t stream, int slot = 0);
 
 template <class T>
 inline T *at(void *base, size_t off) { return reinterpret_cast<T *>(static_cast<char *>(base) + off); }

@@ -33,14 +33,6 @@ __global__ void scatter_bound_kernel(int64_t nm, const int *__restrict__ members
         bound[members[k]] = bs[k];
 }
 
-struct DevBuf {
-    void *p = nullptr;
-    cudaStream_t s = nullptr;
-    ~DevBuf() {
-        if (p) cudaFreeAsync(p, s);
-    }
-};
-
 }  // namespace
 }  // namespace halma
 
@@ -89,9 +81,12 @@ extern "C" int halma_find_haloes(int64_t n, const double *x, const double *y, co
     const size_t o_lab = L.add(4ull * n), o_off = L.add(8ull * (n + 1)), o_mem = L.add(4ull * n);
     const size_t o_g7 = L.add(8ull * 7 * n), o_bs = L.add(1ull * n), o_bnd = L.add(1ull * n);
     const size_t o_halo = L.add(8ull * HALMA_UB_NFIELDS * (size_t)std::max<int64_t>(n / 2 + 1, 1));
-    DevBuf buf;
-    buf.s = st;
-    HALMA_CUDA(cudaMallocAsync(&buf.p, L.total, st));
+    // cached across calls: no allocation in the steady state, and stable addresses let the
+    // unbinding stage replay its captured graph
+    struct {
+        void *p = nullptr;
+    } buf;
+    HALMA_TRY(workspace(L.total, &buf.p, st, 1));
     HALMA_TRY(sg.bind_and_upload(buf.p, st));
     int *dlab = at<int>(buf.p, o_lab);
     int64_t *doff = at<int64_t>(buf.p, o_off);

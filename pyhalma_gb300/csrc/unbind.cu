@@ -100,20 +100,31 @@ __global__ void __launch_bounds__(kSegThreads) ub_reduce_seg_kernel(
     const int64_t b = off[h] + (int64_t)(c - cstart[h]) * kSeg;
     const int64_t e = min(off[h + 1], b + kSeg);
     double v[kRedSums] = {0, 0, 0, 0, 0, 0, 0, 0};
+    // all loads of the thread's members are issued before any is used; members outside the
+    // chunk or unbound read member b and count with weight 0
+    double w[kSegPer], f[kSegPer][7];
 #pragma unroll
     for (int j = 0; j < kSegPer; ++j) {
         const int64_t i = b + j * kSegThreads + threadIdx.x;
-        if (i < e && bound[i]) {
-            const double mi = m[i];
-            v[0] += mi;
-            v[1] += mi * x[i];
-            v[2] += mi * y[i];
-            v[3] += mi * z[i];
-            v[4] += mi * vx[i];
-            v[5] += mi * vy[i];
-            v[6] += mi * vz[i];
-            v[7] += 1.0;
-        }
+        const bool in = i < e;
+        const int64_t s = in ? i : b;
+        w[j] = (in && bound[s]) ? 1.0 : 0.0;
+        f[j][0] = m[s];
+        f[j][1] = x[s];
+        f[j][2] = y[s];
+        f[j][3] = z[s];
+        f[j][4] = vx[s];
+        f[j][5] = vy[s];
+        f[j][6] = vz[s];
+    }
+#pragma unroll
+    for (int j = 0; j < kSegPer; ++j) {
+        if (w[j] == 0.0) continue;
+        const double mi = f[j][0];
+        v[0] += mi;
+#pragma unroll
+        for (int k = 1; k < 7; ++k) v[k] += mi * f[j][k];
+        v[7] += 1.0;
     }
     block_sum_store<kRedSums>(v, sh, part + (int64_t)c * kRedSums);
 }
@@ -408,25 +419,27 @@ __global__ void __launch_bounds__(256) ub_pair_kernel(const float4 *__restrict__
     }
 }
 
-// The end of a pass runs in three wide kernels over energy segments (kSeg packed slots of one
-// halo each), so a big halo is spread over many blocks:
-//   energy  - FP64 energy and sign test of every slot of the segment; removed particles are
-//             marked; per-segment FP64 sums of the survivors (mass, mass-weighted position and
-//             velocity, count) and of the pass's kinetic / potential energy;
-//   compact - survivors copied, in order, into the other packed buffer at the halo's running
-//             offset (positions stay re-centred on the first pass's centre); padding rewritten;
-//   finalize- per halo, segment sums added in segment order (deterministic): removals, pass
-//             count, energies, and the next pass's mass, centre and bulk velocity.  A halo whose
-//             pass removed nothing becomes inactive.
-constexpr int kSegSums = 12;   // removed, kept, ekin, epot, M, Mx, My, Mz, Mvx, Mvy, Mvz, unused
+// The end of a pass runs in three kernels:
+//   energy  - per energy segment (kSeg packed slots of one halo, so a big halo is spread over
+//             many blocks): FP64 energy and sign test of every slot; removed particles are
+//             marked; per-segment FP64 sums of the survivors (count, mass, mass-weighted
+//             velocity) and of the pass's kinetic / potential energy.  The centre of mass is
+//             not needed between passes (positions stay re-centred on the first pass's
+//             centre) and is recomputed over the final bound set after the last pass;
+//   finalize- one warp per halo: segment sums added in a fixed order (deterministic):
+//             removals, pass count, energies, the next pass's mass and bulk velocity, and the
+//             survivors / removed particles before each segment.  A halo whose pass removed
+//             nothing becomes inactive;
+//   compact - per segment of a halo still active: survivors copied, in order, into the other
+//             packed buffer, removed particles into the next pass's source list.
+constexpr int kSegSums = 8;   // removed, kept, ekin, epot, M, Mvx, Mvy, Mvz
 
 template <class V>
 __global__ void __launch_bounds__(kSegThreads) ub_energy_seg_kernel(
     const int *__restrict__ sstart, const int *__restrict__ sown, const int4 *__restrict__ idesc,
     const int *__restrict__ nsegs, const int64_t *__restrict__ poff, const int64_t *__restrict__ qoff,
     int slice_len, int inc, const int *__restrict__ pidx, const double *__restrict__ part,
-    const double *__restrict__ phi_prev, double *__restrict__ phi_cur, const double *__restrict__ x,
-    const double *__restrict__ y, const double *__restrict__ z, const double *__restrict__ vx,
+    const double *__restrict__ phi_prev, double *__restrict__ phi_cur, const double *__restrict__ vx,
     const double *__restrict__ vy, const double *__restrict__ vz, const double *__restrict__ m, double gfac,
     const HaloState *__restrict__ hs, unsigned char *__restrict__ bound, double *__restrict__ phi_out,
     unsigned char *__restrict__ keepf, double *__restrict__ seg_sums) {
@@ -455,16 +468,28 @@ __global__ void __launch_bounds__(kSegThreads) ub_energy_seg_kernel(
 #pragma unroll
         for (int j = 0; j < kSegPer; ++j)
             if (ii[j] >= 0) d[j] += part[qb + (int64_t)k * npad + r[j]];
-    double v[kSegSums] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+    // gathers of all the thread's slots issued together (predicated, no branch between them)
+    double gv[kSegPer][4], pprev[kSegPer];
+#pragma unroll
+    for (int j = 0; j < kSegPer; ++j) {
+        const int i = ii[j];
+        const bool ok = i >= 0;
+        gv[j][0] = ok ? vx[i] : 0.0;
+        gv[j][1] = ok ? vy[i] : 0.0;
+        gv[j][2] = ok ? vz[i] : 0.0;
+        gv[j][3] = ok ? m[i] : 0.0;
+        pprev[j] = (ok && inc) ? phi_prev[pb + r[j]] : 0.0;
+    }
+    double v[kSegSums] = {0, 0, 0, 0, 0, 0, 0, 0};
 #pragma unroll
     for (int j = 0; j < kSegPer; ++j) {
         const int i = ii[j];
         if (i < 0) continue;
-        const double dvx = vx[i] - s.vx, dvy = vy[i] - s.vy, dvz = vz[i] - s.vz;
+        const double dvx = gv[j][0] - s.vx, dvy = gv[j][1] - s.vy, dvz = gv[j][2] - s.vz;
         const double ek = 0.5 * (dvx * dvx + dvy * dvy + dvz * dvz);
         // full pass: the sum itself; incremental pass: previous potential minus the removed
         // particles' contribution
-        const double p = inc ? phi_prev[pb + r[j]] - d[j] : d[j];
+        const double p = inc ? pprev[j] - d[j] : d[j];
         phi_cur[pb + r[j]] = p;
         const double e = ek - gfac * p;
         const bool keep = !(e > 0.0);
@@ -474,17 +499,14 @@ __global__ void __launch_bounds__(kSegThreads) ub_energy_seg_kernel(
             v[0] += 1.0;
             if (phi_out) phi_out[i] = 0.0;
         } else {
-            const double mi = m[i];
+            const double mi = gv[j][3];
             v[1] += 1.0;
             v[2] += mi * ek;
             v[3] += mi * p;
             v[4] += mi;
-            v[5] += mi * x[i];
-            v[6] += mi * y[i];
-            v[7] += mi * z[i];
-            v[8] += mi * vx[i];
-            v[9] += mi * vy[i];
-            v[10] += mi * vz[i];
+            v[5] += mi * gv[j][0];
+            v[6] += mi * gv[j][1];
+            v[7] += mi * gv[j][2];
             if (phi_out) phi_out[i] = p;
         }
     }
@@ -505,7 +527,7 @@ __global__ void ub_finalize_kernel(int nh, const int *__restrict__ order, const 
     const int h = order[q];
     if (!hs[h].active) return;
     const int s0 = sstart[q], s1 = sstart[q + 1];
-    double v[kSegSums] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+    double v[kSegSums] = {0, 0, 0, 0, 0, 0, 0, 0};
     int keep_run = 0, rem_run = 0;
     for (int b0 = s0; b0 < s1; b0 += 32) {
         const int sg = b0 + lane;
@@ -537,10 +559,9 @@ __global__ void ub_finalize_kernel(int nh, const int *__restrict__ order, const 
             o.M = M;
             o.nb = (int)v[1];
             if (M > 0) {
-                o.cx = v[5] / M; o.cy = v[6] / M; o.cz = v[7] / M;
-                o.vx = v[8] / M; o.vy = v[9] / M; o.vz = v[10] / M;
+                o.vx = v[5] / M; o.vy = v[6] / M; o.vz = v[7] / M;
             } else {
-                o.cx = o.cy = o.cz = o.vx = o.vy = o.vz = 0.0;
+                o.vx = o.vy = o.vz = 0.0;
             }
         }
     }
@@ -833,7 +854,7 @@ int unbind_device(int64_t n, int nh, const int64_t *d_off, const int64_t *h_off,
                              cnt, cnt + 1, eps2, slice_len / 32, phi);
                 if (profiling) HALMA_CUDA(cudaEventRecordWithFlags(prof.ev1[it], rs, cudaEventRecordExternal));
                 HALMA_LAUNCH(ub_energy_seg_kernel<float4>, sgrid, kSegThreads, 0, rs, sstart, sown, idesc, cnt + 2,
-                             dpoff, dqoff, slice_len, inc, pidxb[a], phi, phin, phic, x, y, z, vx, vy, vz, m, gfac, hs,
+                             dpoff, dqoff, slice_len, inc, pidxb[a], phi, phin, phic, vx, vy, vz, m, gfac, hs,
                              bound, phi_out, keepf, ssum);
                 HALMA_LAUNCH(ub_finalize_kernel, fgrid, 256, 0, rs, nh, dorder, sstart, ssum, gfac, hs, segpre);
                 HALMA_LAUNCH(ub_compact_seg_kernel<float4>, sgrid, kSegThreads, 0, rs, sstart, sown, idesc, cnt + 2,
@@ -934,7 +955,7 @@ int unbind_device(int64_t n, int nh, const int64_t *d_off, const int64_t *h_off,
             }
             if (!any) break;
             HALMA_LAUNCH(ub_energy_seg_kernel<double4>, sgrid, kSegThreads, 0, st, sstart, sown, idesc, cnt + 2, dpoff,
-                         dqoff, slice_len, 0, pidxb[a], phi, phin, phic, x, y, z, vx, vy, vz, m, gfac, hs, bound,
+                         dqoff, slice_len, 0, pidxb[a], phi, phin, phic, vx, vy, vz, m, gfac, hs, bound,
                          phi_out, keepf, ssum);
             HALMA_LAUNCH(ub_finalize_kernel, fgrid, 256, 0, st, nh, dorder, sstart, ssum, gfac, hs, segpre);
             HALMA_LAUNCH(ub_compact_seg_kernel<double4>, sgrid, kSegThreads, 0, st, sstart, sown, idesc, cnt + 2, dpoff,
