@@ -35,11 +35,18 @@ METRIC = "particles/sec FoF+unbinding and pair-interactions/sec, batched FP32 vs
 WORKLOAD = dict(workload="plummer-2M-500sph-15pc-contaminants", particles=2_000_000, spheres=500, box_mpc=10.0,
                 contaminant_frac=0.15, background_frac=0.10, linking_length_kpc=1.5, min_members=50,
                 softening_kpc=0.1, max_passes=30)
-FLOPS_PER_PAIR = 20          # conventional N-body count (rsqrt counted as several flops)
-# The pair term needs 7 FP32 lane-operations (3 sub, 3 fma for r^2, 1 fma to accumulate) and one
-# rsqrt.  The FP32 pipe does 128 lane-operations per clock per SM; ncu shows the special-
-# function pipe at 42 % when the FP32 pipe is at 76 %, so the FP32 pipe binds:
-FP32_PAIRS_PER_CLK_SM = 128.0 / 7.0
+# FP32-pipe work of the pair kernels, counted from the instruction mix (an FMA is 2 flops):
+#   a pair term evaluated for one particle (tiles, incremental passes): 3 sub + 3 fma for
+#   r^2 + 1 fma to accumulate = 7 lane-operations, 11 flops, and one rsqrt;
+#   a pair evaluated once for both particles (symmetric block kernel, full passes over the
+#   haloes above 1024 particles): 3 sub + 3 fma + 2 fma = 8 lane-operations, 13 flops, one
+#   rsqrt -- per pair term of the pass (each pair is two terms) 4 lane-operations, 6.5 flops
+#   (the diagonal blocks, evaluated per particle, are counted the same way).
+# The FP32 pipe does 128 lane-operations per clock per SM; ncu shows the special-function
+# pipe at 42 % when the FP32 pipe is at 76 %, so the FP32 pipe binds.
+FLOPS_PER_TERM, OPS_PER_TERM = 11.0, 7.0
+FLOPS_PER_SYM_TERM, OPS_PER_SYM_TERM = 6.5, 4.0
+FP32_OPS_PER_CLK_SM = 128.0
 FOF_BYTES_PER_PARTICLE = 28  # FP64 xyz read once + int32 label written once
 
 
@@ -253,7 +260,7 @@ def run_gpu(args):
 
     # timed region: inputs resident in HBM, L2 flushed before every step
     ms, pairs, pair_ms, fof_ms, unbind_ms, passes = [], 0.0, 0.0, [], [], []
-    per_pass = []
+    sym_pairs, per_pass = 0.0, []
     sampler = ClockSampler(local)
     sampler.start()
     launches0 = _lib.launch_count()
@@ -270,12 +277,13 @@ def run_gpu(args):
         st = _lib.profile_stats()
         fof_ms.append(st["fof_ms"])
         unbind_ms.append(st["unbind_ms"])
-        for p, t in st["passes"]:
+        for (p, t), sp in zip(st["passes"], st["sym_pairs"]):
             if p > 0:
                 pairs += p
                 pair_ms += t
+                sym_pairs += sp
         passes.append(sum(1 for p, _ in st["passes"] if p > 0))
-        per_pass = [[int(p), round(t, 4)] for p, t in st["passes"] if p > 0]
+        per_pass = [[int(p), round(t, 4), int(sp)] for (p, t), sp in zip(st["passes"], st["sym_pairs"]) if p > 0]
     barrier()
     wall = time.perf_counter() - wall0
     launches = _lib.launch_count() - launches0
@@ -328,17 +336,24 @@ def run_gpu(args):
 
     hbm, sm_max, src = peaks()
     sms = torch.cuda.get_device_properties(dev).multi_processor_count
-    pair_peak = FP32_PAIRS_PER_CLK_SM * sms * sm_max * 1e6 * FLOPS_PER_PAIR / 1e12
+    pair_peak = 2.0 * FP32_OPS_PER_CLK_SM * sms * sm_max * 1e6 / 1e12   # FP32 TFLOP/s, FMA = 2
     n_pair_launches = sum(passes)
-    achieved = FLOPS_PER_PAIR * pairs / (pair_ms * 1e-3) / 1e12 if pair_ms > 0 else 0.0
+    flops = FLOPS_PER_TERM * (pairs - sym_pairs) + FLOPS_PER_SYM_TERM * sym_pairs
+    lane_ops = OPS_PER_TERM * (pairs - sym_pairs) + OPS_PER_SYM_TERM * sym_pairs
+    achieved = flops / (pair_ms * 1e-3) / 1e12 if pair_ms > 0 else 0.0
+    pipe = lane_ops / (pair_ms * 1e-3) / (FP32_OPS_PER_CLK_SM * sms * sm_max * 1e6) if pair_ms > 0 else 0.0
     traffic = None
     tp = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(tp):
         traffic = json.load(open(tp)).get("ub_pair_kernel_bytes_per_launch")
     roofline = {"bound": "fp32", "kernel": "ub_pair_kernel", "achieved": achieved, "peak": pair_peak,
                 "unit": "TFLOP/s", "frac": achieved / pair_peak if pair_peak else None, "traffic": traffic,
-                "peak_source": f"FP32 pipe: 128 lane-ops/clk/SM / 7 per pair x {sms} SMs x {sm_max:.0f} MHz "
-                               f"(sm_max_mhz {src}) x {FLOPS_PER_PAIR} flops/pair (conventional count)",
+                "peak_source": f"FP32 peak: 128 lanes x 2 flops (FMA) x {sms} SMs x {sm_max:.0f} MHz (sm_max_mhz "
+                               f"{src}); flops from the instruction mix: 11 per pair term, 6.5 per term "
+                               f"on the symmetric block kernel (3 of every 7 or 8 lane-operations are "
+                               f"1-flop subtractions, so frac <= 0.79 at a full FP32 pipe)",
+                "fp32_pipe_frac": pipe,
+                "sym_pair_terms": sym_pairs,
                 "pairs_per_launch": pairs / max(n_pair_launches, 1), "ms_per_launch": pair_ms / max(n_pair_launches, 1),
                 "launches_timed": n_pair_launches, "last_step_passes_pairs_ms": per_pass}
     fof_gbs = FOF_BYTES_PER_PARTICLE * n / (statistics.mean(fof_ms) * 1e-3) / 1e9

@@ -64,8 +64,10 @@ int64_t     halma_kernel_launch_count(void);
 /* Measurement hooks (no reference counterpart).  With profiling on, the unbinding records
  * CUDA events around every pair-kernel launch on the launching stream and the pair count of
  * every pass, and halma_find_haloes times its FoF and unbinding stages.  halma_profile_stats
- * fills out[] with [fof_ms, unbind_ms, n_passes, pairs_0, ms_0, pairs_1, ms_1, ...] for the
- * last call and returns the number of values available. */
+ * fills out[] with [fof_ms, unbind_ms, n_passes, pairs_0, ms_0, sym_pairs_0, pairs_1, ...]
+ * for the last call (per pass: pair terms, pair-kernel milliseconds, and the pair terms of
+ * the haloes that ran on the symmetric block kernel, where each pair is evaluated once for
+ * both particles) and returns the number of values available. */
 int         halma_set_profiling(int32_t on);
 int         halma_profile_stats(double *out, int32_t cap);
 

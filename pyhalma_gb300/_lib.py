@@ -121,13 +121,15 @@ def set_profiling(on: bool):
 
 
 def profile_stats():
-    """Last call's measurements: dict(fof_ms, unbind_ms, passes=[(pairs, pair_kernel_ms), ...])."""
+    """Last call's measurements: dict(fof_ms, unbind_ms, passes=[(pairs, pair_kernel_ms), ...],
+    sym_pairs=[pairs of each pass evaluated by the symmetric block kernel])."""
     n = lib().halma_profile_stats(None, 0)
     buf = np.zeros(max(n, 3))
     lib().halma_profile_stats(buf.ctypes.data_as(ctypes.c_void_p), len(buf))
     k = int(buf[2])
-    passes = [(float(buf[3 + 2 * i]), float(buf[4 + 2 * i])) for i in range(k)]
-    return {"fof_ms": float(buf[0]), "unbind_ms": float(buf[1]), "passes": passes}
+    passes = [(float(buf[3 + 3 * i]), float(buf[4 + 3 * i])) for i in range(k)]
+    sym = [float(buf[5 + 3 * i]) for i in range(k)]
+    return {"fof_ms": float(buf[0]), "unbind_ms": float(buf[1]), "passes": passes, "sym_pairs": sym}
 
 
 # ---------------------------------------------------------------------------------------

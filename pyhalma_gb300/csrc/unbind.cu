@@ -212,26 +212,34 @@ __device__ __forceinline__ int warp_incl_scan(int v, int lane) {
     return v;
 }
 
+// Full passes over a halo of more than kSymBlock bound particles use the symmetric block
+// kernel instead: blocks of kSymBlock slots, one item per block pair (tb <= sb), B(B+1)/2
+// items for B blocks, listed from ystart[q]; the partial sums are then kept per block
+// (B slices of kSymBlock).  idesc[q].w is the number of partial slices the energy kernel adds.
+constexpr int kSymWarps = 8, kSymT = 4;
+constexpr int kSymBlock = kSymWarps * 32 * kSymT;   // 1024 slots
+
 __global__ void __launch_bounds__(1024) ub_items_kernel(int nh, const int *__restrict__ order, const HaloState *hs,
-                                                        TileTable tab, int slice_len, int inc,
-                                                        int *__restrict__ istart, int4 *__restrict__ idesc,
-                                                        int *__restrict__ sstart, int *__restrict__ sown,
-                                                        int *__restrict__ nitems,
-                                                        int *__restrict__ counter, int *__restrict__ nsegs,
+                                                        TileTable tab, int slice_len, int inc, int sym_ok,
+                                                        int *__restrict__ istart, int *__restrict__ ystart,
+                                                        int4 *__restrict__ idesc, int *__restrict__ sstart,
+                                                        int *__restrict__ sown, int *__restrict__ cnt,
                                                         unsigned long long *__restrict__ pairs_out) {
-    __shared__ int wsum[32], wseg[32];
-    __shared__ int base, sbase;
-    __shared__ unsigned long long pairs;
+    __shared__ int wsum[32], wseg[32], wsym[32];
+    __shared__ int base, sbase, ybase;
+    __shared__ unsigned long long pairs, spairs;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     if (threadIdx.x == 0) {
         base = 0;
         sbase = 0;
+        ybase = 0;
         pairs = 0;
+        spairs = 0;
     }
     __syncthreads();
     for (int h0 = 0; h0 < nh; h0 += blockDim.x) {
         const int q = h0 + threadIdx.x;
-        int h = -1, cnt = 0, T = 4, nsl = 1, nseg = 0;
+        int h = -1, n = 0, T = 4, nsl = 1, nseg = 0, ny = 0, nsl_e = 0;
         if (q < nh) {
             h = order[q];
             if (hs[h].active) {
@@ -239,49 +247,69 @@ __global__ void __launch_bounds__(1024) ub_items_kernel(int nh, const int *__res
                 const int ns = inc ? hs[h].nrem : nb;   // sources: removed particles or the halo itself
                 T = tile_t_for(tab, nb);
                 nsl = (int)(((int64_t)ns + slice_len - 1) / slice_len);
-                cnt = ns > 0 ? ((nb + 32 * T - 1) / (32 * T)) * nsl : 0;
+                if (!inc && sym_ok && nb > kSymBlock && nb <= 65535 * kSymBlock) {
+                    const int B = (nb + kSymBlock - 1) / kSymBlock;   // B <= 65535: B(B+1)/2 < 2^31
+                    ny = (int)((int64_t)B * (B + 1) / 2);
+                    nsl_e = B;
+                    atomicAdd(&spairs, (unsigned long long)nb * (unsigned long long)nb);
+                } else {
+                    n = ns > 0 ? ((nb + 32 * T - 1) / (32 * T)) * nsl : 0;
+                    nsl_e = nsl;
+                }
                 nseg = max(1, (nb + kSeg - 1) / kSeg);
                 if (nb > 0) atomicAdd(&pairs, (unsigned long long)nb * (unsigned long long)ns);
             }
         }
-        const int incl = warp_incl_scan(cnt, lane);
+        const int incl = warp_incl_scan(n, lane);
         const int sincl = warp_incl_scan(nseg, lane);
+        const int yincl = warp_incl_scan(ny, lane);
         if (lane == 31) {
             wsum[w] = incl;
             wseg[w] = sincl;
+            wsym[w] = yincl;
         }
         __syncthreads();
-        int pre = base, spre = sbase;
+        int pre = base, spre = sbase, ypre = ybase;
         for (int k = 0; k < w; ++k) {
             pre += wsum[k];
             spre += wseg[k];
+            ypre += wsym[k];
         }
         if (q < nh) {
-            istart[q] = pre + incl - cnt;
-            idesc[q] = make_int4(h, T, max(nsl, 1), 0);
+            istart[q] = pre + incl - n;
+            ystart[q] = ypre + yincl - ny;
+            idesc[q] = make_int4(h, T, max(nsl, 1), nsl_e);
             const int s0 = spre + sincl - nseg;
             sstart[q] = s0;
             for (int sg = 0; sg < nseg; ++sg) sown[s0 + sg] = q;
         }
         __syncthreads();
         if (threadIdx.x == 0) {
-            int tot = 0, stot = 0;
+            int tot = 0, stot = 0, ytot = 0;
             for (int k = 0; k < (int)(blockDim.x >> 5); ++k) {
                 tot += wsum[k];
                 stot += wseg[k];
+                ytot += wsym[k];
             }
             base += tot;
             sbase += stot;
+            ybase += ytot;
         }
         __syncthreads();
     }
     if (threadIdx.x == 0) {
         istart[nh] = base;
         sstart[nh] = sbase;
-        *nitems = base;
-        *counter = 0;
-        *nsegs = sbase;
-        if (pairs_out) *pairs_out = pairs;
+        ystart[nh] = ybase;
+        cnt[0] = base;    // warp items
+        cnt[1] = 0;       // their counter
+        cnt[2] = sbase;   // energy segments
+        cnt[3] = ybase;   // symmetric block items
+        cnt[4] = 0;       // their counter
+        if (pairs_out) {
+            pairs_out[0] = pairs;    // pair terms of the pass (nb x sources, every halo)
+            pairs_out[1] = spairs;   // of which in haloes on the symmetric block kernel
+        }
     }
 }
 
@@ -419,6 +447,211 @@ __global__ void __launch_bounds__(256) ub_pair_kernel(const float4 *__restrict__
     }
 }
 
+// Reduce-scatter of 16 per-lane values across the warp: lanes l and l^1 end with the warp's
+// total of value (l >> 1) & 15 (fixed association: halving steps over lane bits 4..1, then
+// the pair l, l^1).
+__device__ __forceinline__ float warp_reduce_scatter16(float (&v)[16], int lane) {
+    float a[8], b[4], c[2];
+    {
+        const bool up = lane & 16;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            const float send = up ? v[k] : v[k + 8], keep = up ? v[k + 8] : v[k];
+            a[k] = keep + __shfl_xor_sync(0xffffffffu, send, 16);
+        }
+    }
+    {
+        const bool up = lane & 8;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const float send = up ? a[k] : a[k + 4], keep = up ? a[k + 4] : a[k];
+            b[k] = keep + __shfl_xor_sync(0xffffffffu, send, 8);
+        }
+    }
+    {
+        const bool up = lane & 4;
+#pragma unroll
+        for (int k = 0; k < 2; ++k) {
+            const float send = up ? b[k] : b[k + 2], keep = up ? b[k + 2] : b[k];
+            c[k] = keep + __shfl_xor_sync(0xffffffffu, send, 4);
+        }
+    }
+    const bool up = lane & 2;
+    const float send = up ? c[0] : c[1], keep = up ? c[1] : c[0];
+    const float d = keep + __shfl_xor_sync(0xffffffffu, send, 2);
+    return d + __shfl_xor_sync(0xffffffffu, d, 1);
+}
+
+// Symmetric form of chunk_pairs: every pair term 1/r is used twice, m_source / r for the
+// lane's targets (acc, as in chunk_pairs) and m_target / r for the chunk's sources.  The
+// source side is summed over the lane's T targets, then over the warp (reduce-scatter), and
+// the warp's 32 * T-target sums of the chunk's 32 sources go to sout[0..32).
+template <int T>
+__device__ __forceinline__ void chunk_pairs_sym(const float4 *sa, const float4 *sb, const f2x (&tx)[T],
+                                                const f2x (&ty)[T], const f2x (&tz)[T], const f2x (&tm)[T], f2x e2,
+                                                f2x (&acc)[T], float *sout, int lane) {
+#pragma unroll
+    for (int half = 0; half < 2; ++half) {
+        f2x sacc[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) sacc[k] = pack2(0.f, 0.f);
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            const float4 a = sa[half * 8 + k], b = sb[half * 8 + k];
+            const f2x X = pack2(a.x, a.y), Y = pack2(a.z, a.w), Z = pack2(b.x, b.y), M = pack2(b.z, b.w);
+#pragma unroll
+            for (int t = 0; t < T; ++t) {
+                const f2x dx = sub2(X, tx[t]), dy = sub2(Y, ty[t]), dz = sub2(Z, tz[t]);
+                f2x r2 = fma2(dz, dz, e2);
+                r2 = fma2(dy, dy, r2);
+                r2 = fma2(dx, dx, r2);
+                float r0, r1;
+                unpack2(r2, r0, r1);
+                const f2x ri = pack2(rsqrt_ftz(r0), rsqrt_ftz(r1));
+                acc[t] = fma2(M, ri, acc[t]);
+                sacc[k] = fma2(tm[t], ri, sacc[k]);
+            }
+        }
+        float v[16];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) unpack2(sacc[k], v[2 * k], v[2 * k + 1]);
+        const float s = warp_reduce_scatter16(v, lane);
+        if ((lane & 1) == 0) sout[half * 16 + (lane >> 1)] = s;
+    }
+}
+
+// Full passes over the haloes of more than kSymBlock bound particles.  The halo's slots are
+// cut into blocks of kSymBlock; an item is a block pair (tb, sb), tb <= sb, taken by one CTA
+// from an atomic counter.  The CTA stages the source block in shared memory; warp w holds
+// targets tb*kSymBlock + w*128 + t*32 + lane.  Diagonal items (tb == sb) are plain (self pair
+// skipped) and write the targets' partial for slice sb.  Off-diagonal items compute each pair
+// once: the targets' partial goes to slice sb (part[qoff + sb*npad + r]) and the sources'
+// partial -- per source, the 8 warps' sums added in warp order in FP64 -- to slice tb.  So
+// slot r of block b receives slice k from item (b, k) for k >= b and from item (k, b) for
+// k < b: every slice exactly once, and the energy kernel adds slices 0..B-1 in order.
+__global__ void __launch_bounds__(256) ub_pair_sym_kernel(const float4 *__restrict__ pk,
+                                                          const int64_t *__restrict__ poff,
+                                                          const int64_t *__restrict__ qoff,
+                                                          const HaloState *__restrict__ hs, int nh,
+                                                          const int *__restrict__ ystart,
+                                                          const int4 *__restrict__ idesc, const int *__restrict__ cnt,
+                                                          int *counter, float eps2, double *__restrict__ part) {
+    extern __shared__ float4 sym_smem[];
+    float4 *ssrc = sym_smem;                                            // 32 chunks x (16 + 16) float4
+    float *spart = reinterpret_cast<float *>(sym_smem + kSymBlock);     // [kSymWarps][kSymBlock]
+    __shared__ int4 job;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int nitems = cnt[3];
+    const f2x e2 = pack2(eps2, eps2);
+    for (;;) {
+        if (threadIdx.x == 0) {
+            const int item = atomicAdd(counter, 1);
+            int4 jb = make_int4(-1, 0, 0, 0);
+            if (item < nitems) {
+                int lo = 0, hi = nh - 1;   // ordered halo owning the item: last q with ystart[q] <= item
+                while (lo < hi) {
+                    const int mid = (lo + hi + 1) >> 1;
+                    if (ystart[mid] <= item) lo = mid;
+                    else hi = mid - 1;
+                }
+                const int h = idesc[lo].x;
+                const int64_t u = item - ystart[lo];
+                const int64_t B = (hs[h].nb + kSymBlock - 1) / kSymBlock;
+                // row tb of the upper triangle starts at tb*B - tb*(tb-1)/2
+                int64_t tb = (int64_t)(((double)(2 * B + 1) - sqrt((double)(2 * B + 1) * (double)(2 * B + 1) -
+                                                                     8.0 * (double)u)) * 0.5);
+                tb = tb < 0 ? 0 : (tb > B - 1 ? B - 1 : tb);
+                while (tb + 1 < B && (tb + 1) * B - (tb + 1) * tb / 2 <= u) ++tb;
+                while (tb > 0 && tb * B - tb * (tb - 1) / 2 > u) --tb;
+                const int64_t sb = tb + (u - (tb * B - tb * (tb - 1) / 2));
+                jb = make_int4(h, (int)tb, (int)sb, 0);
+            }
+            job = jb;
+        }
+        __syncthreads();
+        const int4 jb = job;
+        if (jb.x < 0) break;
+        const int h = jb.x, tb = jb.y, sb = jb.z;
+        const bool sym = tb != sb;
+        const int64_t base = poff[h], npad = poff[h + 1] - base;
+        const int nb = hs[h].nb;
+        const int s0 = sb * kSymBlock;
+        const int nch = min(kSymBlock / 32, (nb - s0 + 31) >> 5);   // chunks holding sources
+        // stage the source block (slots past nb: zero mass, far away)
+        for (int k = threadIdx.x; k < nch * 32; k += blockDim.x) {
+            const int s = s0 + k;
+            const float4 p = s < nb ? pk[base + s] : make_float4(kFar, kFar, kFar, 0.f);
+            float *ca = reinterpret_cast<float *>(ssrc + (k >> 5) * 32);
+            const int li = k & 31, kp = li >> 1, hf = li & 1;
+            ca[kp * 4 + hf] = p.x;
+            ca[kp * 4 + 2 + hf] = p.y;
+            ca[64 + kp * 4 + hf] = p.z;
+            ca[64 + kp * 4 + 2 + hf] = p.w;
+        }
+        __syncthreads();
+        const int t0 = tb * kSymBlock + w * 32 * kSymT;   // the warp's first target slot
+        float *sp = spart + w * kSymBlock;
+        if (t0 < nb) {
+            f2x tx[kSymT], ty[kSymT], tz[kSymT], tm[kSymT];
+            float sum[kSymT], comp[kSymT];
+#pragma unroll
+            for (int t = 0; t < kSymT; ++t) {
+                const int r = t0 + t * 32 + lane;
+                const float4 p = r < nb ? pk[base + r] : make_float4(kFar, kFar, kFar, 0.f);
+                tx[t] = pack2(p.x, p.x);
+                ty[t] = pack2(p.y, p.y);
+                tz[t] = pack2(p.z, p.z);
+                tm[t] = pack2(p.w, p.w);
+                sum[t] = 0.f;
+                comp[t] = 0.f;
+            }
+            for (int c = 0; c < nch; ++c) {
+                const float4 *ca = ssrc + c * 32;
+                f2x acc[kSymT];
+#pragma unroll
+                for (int t = 0; t < kSymT; ++t) acc[t] = pack2(0.f, 0.f);
+                if (sym) {
+                    chunk_pairs_sym<kSymT>(ca, ca + 16, tx, ty, tz, tm, e2, acc, sp + c * 32, lane);
+                } else {
+                    const int ts = c - w * kSymT;   // chunk c holds the self slot of target ts
+                    if (ts >= 0 && ts < kSymT)
+                        chunk_pairs<kSymT, true>(ca, ca + 16, tx, ty, tz, e2, acc, ts, lane);
+                    else
+                        chunk_pairs<kSymT, false>(ca, ca + 16, tx, ty, tz, e2, acc, ts, lane);
+                }
+#pragma unroll
+                for (int t = 0; t < kSymT; ++t) {
+                    float a0, a1;
+                    unpack2(acc[t], a0, a1);
+                    two_sum_acc(sum[t], comp[t], a0 + a1);
+                }
+            }
+            double *out = part + qoff[h] + (int64_t)sb * npad;
+#pragma unroll
+            for (int t = 0; t < kSymT; ++t) {
+                const int r = t0 + t * 32 + lane;
+                if (r < nb) out[r] = (double)sum[t] + (double)comp[t];
+            }
+        } else if (sym) {
+            for (int k = lane; k < nch * 32; k += 32) sp[k] = 0.f;   // no targets here: no terms
+        }
+        if (sym) {
+            __syncthreads();
+            double *out = part + qoff[h] + (int64_t)tb * npad;
+            for (int k = threadIdx.x; k < nch * 32; k += blockDim.x) {
+                const int s = s0 + k;
+                if (s < nb) {
+                    double v = 0.0;
+#pragma unroll
+                    for (int ww = 0; ww < kSymWarps; ++ww) v += (double)spart[ww * kSymBlock + k];
+                    out[s] = v;
+                }
+            }
+        }
+        __syncthreads();   // shared memory is restaged by the next item
+    }
+}
+
 // The end of a pass runs in three kernels:
 //   energy  - per energy segment (kSeg packed slots of one halo, so a big halo is spread over
 //             many blocks): FP64 energy and sign test of every slot; removed particles are
@@ -438,7 +671,7 @@ template <class V>
 __global__ void __launch_bounds__(kSegThreads) ub_energy_seg_kernel(
     const int *__restrict__ sstart, const int *__restrict__ sown, const int4 *__restrict__ idesc,
     const int *__restrict__ nsegs, const int64_t *__restrict__ poff, const int64_t *__restrict__ qoff,
-    int slice_len, int inc, const int *__restrict__ pidx, const double *__restrict__ part,
+    int inc, const int *__restrict__ pidx, const double *__restrict__ part,
     const double *__restrict__ phi_prev, double *__restrict__ phi_cur, const double *__restrict__ vx,
     const double *__restrict__ vy, const double *__restrict__ vz, const double *__restrict__ m, double gfac,
     const HaloState *__restrict__ hs, unsigned char *__restrict__ bound, double *__restrict__ phi_out,
@@ -451,8 +684,7 @@ __global__ void __launch_bounds__(kSegThreads) ub_energy_seg_kernel(
     const int sl = seg - sstart[q];
     const HaloState s = hs[h];
     const int64_t pb = poff[h], npad = poff[h + 1] - pb, qb = qoff[h];
-    const int ns = inc ? s.nrem : s.nb;
-    const int nsl = (int)(((int64_t)ns + slice_len - 1) / slice_len);
+    const int nsl = idesc[q].w;   // partial-sum slices written by this pass's pair kernels
     const int rend = min(s.nb, (sl + 1) * kSeg);
     // the segment's kSegPer slots per thread are loaded together (independent gathers in
     // flight), then evaluated in slot order
@@ -735,7 +967,8 @@ int unbind_device(int64_t n, int nh, const int64_t *d_off, const int64_t *h_off,
         cstart[h] = (int)chunk_h.size();
         for (int64_t k = 0; k < (c + kSeg - 1) / kSeg; ++k) chunk_h.push_back(h);
         const int64_t npad = ((c + 31) / 32) * 32;
-        const int64_t nsl = std::max<int64_t>(1, (c + slice_len - 1) / slice_len);
+        int64_t nsl = std::max<int64_t>(1, (c + slice_len - 1) / slice_len);
+        if (!f64 && c > kSymBlock) nsl = std::max<int64_t>(nsl, (c + kSymBlock - 1) / kSymBlock);   // symmetric
         poff[h + 1] = poff[h] + npad;
         qoff[h + 1] = qoff[h] + npad * nsl;
         segcap += std::max<int64_t>(1, (c + kSeg - 1) / kSeg);
@@ -771,7 +1004,8 @@ int unbind_device(int64_t n, int nh, const int64_t *d_off, const int64_t *h_off,
     const size_t o_chh = L.add(sizeof(int) * std::max(nchunks, 1));
     const size_t o_rpart = L.add(sizeof(double) * kRedSums * std::max(nchunks, 1));
     const size_t o_cnt = L.add(64);
-    const size_t o_pairs = L.add(sizeof(unsigned long long) * p.max_iter);
+    const size_t o_pairs = L.add(sizeof(unsigned long long) * 2 * p.max_iter);
+    const size_t o_ystart = L.add(sizeof(int) * (nh + 1));
     const size_t o_off = d_off ? 0 : L.add(sizeof(int64_t) * (nh + 1));
     void *base = nullptr;
     HALMA_TRY(workspace(L.total, &base, st));
@@ -797,11 +1031,12 @@ int unbind_device(int64_t n, int nh, const int64_t *d_off, const int64_t *h_off,
     int *cnt = at<int>(base, o_cnt);   // [0] nitems [1] counter [2] energy segments
     const int sgrid = (int)segcap;
     auto *dpairs = at<unsigned long long>(base, o_pairs);
+    auto *ystart = at<int>(base, o_ystart);
     Profile &prof = profile();
     const bool profiling = prof.enabled;
     if (profiling) {
         HALMA_TRY(prof.ensure_events(p.max_iter));
-        HALMA_CUDA(cudaMemsetAsync(dpairs, 0, sizeof(unsigned long long) * p.max_iter, st));
+        HALMA_CUDA(cudaMemsetAsync(dpairs, 0, sizeof(unsigned long long) * 2 * p.max_iter, st));
     }
     const int64_t *off = d_off;
     if (!d_off) {
@@ -835,6 +1070,10 @@ int unbind_device(int64_t n, int nh, const int64_t *d_off, const int64_t *h_off,
         int bps = 0;
         HALMA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, ub_pair_kernel, 256, 0));
         const int pgrid = device_sm_count() * std::max(bps, 1);
+        constexpr int kSymSmem = kSymBlock * (int)sizeof(float4) + kSymWarps * kSymBlock * (int)sizeof(float);
+        HALMA_CUDA(cudaFuncSetAttribute(ub_pair_sym_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSymSmem));
+        HALMA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, ub_pair_sym_kernel, 256, kSymSmem));
+        const int ygrid = device_sm_count() * std::max(bps, 1);
         auto record = [&](cudaStream_t rs) -> int {
             // first pass: centre of mass and packing into buffer 0; every pass then compacts
             // its survivors into the other buffer and sets the next pass's halo state
@@ -846,16 +1085,21 @@ int unbind_device(int64_t n, int nh, const int64_t *d_off, const int64_t *h_off,
             for (int it = 0; it < p.max_iter; ++it) {
                 const int a = it & 1, b = a ^ 1;
                 const int inc = (it > 0 && incremental) ? 1 : 0;
-                HALMA_LAUNCH(ub_items_kernel, 1, 1024, 0, rs, nh, dorder, hs, tab, slice_len, inc, istart, idesc,
-                             sstart, sown, cnt, cnt + 1, cnt + 2, profiling ? dpairs + it : nullptr);
+                HALMA_LAUNCH(ub_items_kernel, 1, 1024, 0, rs, nh, dorder, hs, tab, slice_len, inc, 1, istart, ystart,
+                             idesc, sstart, sown, cnt, profiling ? dpairs + 2 * it : nullptr);
                 // External: captured as an event-record node, so the replay records it
                 if (profiling) HALMA_CUDA(cudaEventRecordWithFlags(prof.ev0[it], rs, cudaEventRecordExternal));
+                // full passes: the big haloes' block pairs first (the longest items), then the
+                // tiles of the small ones; incremental passes have only tiles
+                if (!inc)
+                    HALMA_LAUNCH(ub_pair_sym_kernel, ygrid, 256, kSymSmem, rs, pkb[a], dpoff, dqoff, hs, nh, ystart,
+                                 idesc, cnt, cnt + 4, eps2, phi);
                 HALMA_LAUNCH(ub_pair_kernel, pgrid, 256, 0, rs, pkb[a], rk, inc, dpoff, dqoff, hs, nh, istart, idesc,
                              cnt, cnt + 1, eps2, slice_len / 32, phi);
                 if (profiling) HALMA_CUDA(cudaEventRecordWithFlags(prof.ev1[it], rs, cudaEventRecordExternal));
                 HALMA_LAUNCH(ub_energy_seg_kernel<float4>, sgrid, kSegThreads, 0, rs, sstart, sown, idesc, cnt + 2,
-                             dpoff, dqoff, slice_len, inc, pidxb[a], phi, phin, phic, vx, vy, vz, m, gfac, hs,
-                             bound, phi_out, keepf, ssum);
+                             dpoff, dqoff, inc, pidxb[a], phi, phin, phic, vx, vy, vz, m, gfac, hs, bound, phi_out,
+                             keepf, ssum);
                 HALMA_LAUNCH(ub_finalize_kernel, fgrid, 256, 0, rs, nh, dorder, sstart, ssum, gfac, hs, segpre);
                 HALMA_LAUNCH(ub_compact_seg_kernel<float4>, sgrid, kSegThreads, 0, rs, sstart, sown, idesc, cnt + 2,
                              dpoff, hs, keepf, segpre, pkb[a], pidxb[a], phic, pkb[b], pidxb[b], phin, rk);
@@ -920,15 +1164,15 @@ int unbind_device(int64_t n, int nh, const int64_t *d_off, const int64_t *h_off,
         // final bound mass, centre and bulk velocity over the final bound sets
         HALMA_TRY(reduce(st, 1));
         if (profiling) {
-            std::vector<unsigned long long> hp(p.max_iter);
-            HALMA_CUDA(cudaMemcpyAsync(hp.data(), dpairs, sizeof(unsigned long long) * p.max_iter,
+            std::vector<unsigned long long> hp(2 * p.max_iter);
+            HALMA_CUDA(cudaMemcpyAsync(hp.data(), dpairs, sizeof(unsigned long long) * 2 * p.max_iter,
                                        cudaMemcpyDeviceToHost, st));
             HALMA_CUDA(cudaStreamSynchronize(st));
             prof.passes.clear();
             for (int it = 0; it < p.max_iter; ++it) {
                 float ms = 0.f;
                 HALMA_CUDA(cudaEventElapsedTime(&ms, prof.ev0[it], prof.ev1[it]));
-                prof.passes.push_back({(double)hp[it], (double)ms});
+                prof.passes.push_back({(double)hp[2 * it], (double)ms, (double)hp[2 * it + 1]});
             }
         }
     } else {
@@ -942,8 +1186,8 @@ int unbind_device(int64_t n, int nh, const int64_t *d_off, const int64_t *h_off,
         double4 *rk = at<double4>(base, o_rk);
         for (int it = 0; it < p.max_iter; ++it) {
             const int a = it & 1, b = a ^ 1;
-            HALMA_LAUNCH(ub_items_kernel, 1, 1024, 0, st, nh, dorder, hs, tab, slice_len, 0, istart, idesc, sstart,
-                         sown, cnt, cnt + 1, cnt + 2, nullptr);
+            HALMA_LAUNCH(ub_items_kernel, 1, 1024, 0, st, nh, dorder, hs, tab, slice_len, 0, 0, istart, ystart, idesc,
+                         sstart, sown, cnt, nullptr);
             HALMA_CUDA(cudaMemcpyAsync(hh.data(), hs, sizeof(HaloState) * nh, cudaMemcpyDeviceToHost, st));
             HALMA_CUDA(cudaStreamSynchronize(st));
             int any = 0;
@@ -955,8 +1199,8 @@ int unbind_device(int64_t n, int nh, const int64_t *d_off, const int64_t *h_off,
             }
             if (!any) break;
             HALMA_LAUNCH(ub_energy_seg_kernel<double4>, sgrid, kSegThreads, 0, st, sstart, sown, idesc, cnt + 2, dpoff,
-                         dqoff, slice_len, 0, pidxb[a], phi, phin, phic, vx, vy, vz, m, gfac, hs, bound,
-                         phi_out, keepf, ssum);
+                         dqoff, 0, pidxb[a], phi, phin, phic, vx, vy, vz, m, gfac, hs, bound, phi_out, keepf,
+                         ssum);
             HALMA_LAUNCH(ub_finalize_kernel, fgrid, 256, 0, st, nh, dorder, sstart, ssum, gfac, hs, segpre);
             HALMA_LAUNCH(ub_compact_seg_kernel<double4>, sgrid, kSegThreads, 0, st, sstart, sown, idesc, cnt + 2, dpoff,
                          hs, keepf, segpre, pkb[a], pidxb[a], phic, pkb[b], pidxb[b], phin, rk);

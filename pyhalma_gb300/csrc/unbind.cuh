@@ -11,7 +11,7 @@ struct Profile {
     bool enabled = false;
     std::vector<cudaEvent_t> ev0, ev1;
     struct Pass {
-        double pairs, ms;
+        double pairs, ms, sym_pairs;   // sym_pairs: the part done by the symmetric block kernel
     };
     std::vector<Pass> passes;
     double fof_ms = 0, unbind_ms = 0;
