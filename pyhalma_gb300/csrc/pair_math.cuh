@@ -43,6 +43,39 @@ __device__ __forceinline__ void two_sum_acc(float &s, float &c, float v) {
     c += err;
 }
 
+// Double-float numbers: a value held as the unevaluated sum hi + lo of two FP32 numbers
+// (float2 {hi, lo}), about 48 significant bits, computed with FP32 operations only -- on a GPU
+// whose FP64 rate is a small fraction of its FP32 rate, this carries FP64-like accuracy
+// through per-particle code.  Error-free transformations of Knuth (TwoSum) and Dekker
+// (FastTwoSum, |a| >= |b|); neither contains a product, so FMA contraction cannot alter them.
+__device__ __forceinline__ float2 df_two_sum(float a, float b) {
+    const float s = a + b;
+    const float bp = s - a;
+    return make_float2(s, (a - (s - bp)) + (b - bp));
+}
+
+__device__ __forceinline__ float2 df_fast_two_sum(float a, float b) {
+    const float s = a + b;
+    return make_float2(s, b - (s - a));
+}
+
+// The accurate double-float sum (both parts added with TwoSum, renormalised twice), valid
+// under cancellation, as in an incremental update phi - delta with delta close to phi.
+__device__ __forceinline__ float2 df_add(float2 a, float2 b) {
+    float2 s = df_two_sum(a.x, b.x);
+    const float2 t = df_two_sum(a.y, b.y);
+    s = df_fast_two_sum(s.x, s.y + t.x);
+    return df_fast_two_sum(s.x, s.y + t.y);
+}
+
+__device__ __forceinline__ float2 df_sub(float2 a, float2 b) { return df_add(a, make_float2(-b.x, -b.y)); }
+
+// A compensated FP32 accumulator (sum s, accumulated rounding errors c, |c| << |s|) as a
+// normalised double-float.
+__device__ __forceinline__ float2 df_from_acc(float s, float c) { return df_fast_two_sum(s, c); }
+
+__device__ __forceinline__ double df_to_double(float2 a) { return (double)a.x + (double)a.y; }
+
 // One softened pair term m / sqrt(r^2 + eps2) with the FP32 special-function rsqrt.
 __device__ __forceinline__ float pair_term_fast(float4 q, float px, float py, float pz, float eps2,
                                                 float acc) {

@@ -37,6 +37,11 @@ constexpr float kFar = 3.0e30f;
 
 struct HaloState {   // per halo, FP64 unless stated
     double M, cx, cy, cz, vx, vy, vz, ekin, epot;
+    // FP32 path: sums of m x and m v over the bound set, kept up to date by subtracting each
+    // pass's removed particles; the bulk velocity at packing (packed velocities are relative
+    // to it) and the current bulk velocity relative to it in FP32
+    double sx, sy, sz, px, py, pz, v0x, v0y, v0z;
+    float wx, wy, wz;
     int nb, active, iter, removed, nrem;   // nrem: removed by the last pass (next pass's sources)
     int nprev;                             // slots the last pass examined (nb before its cut)
 };
@@ -86,7 +91,9 @@ constexpr int kSegPer = kSeg / kSegThreads;
 constexpr int kRedSums = 8;   // M, Mx, My, Mz, Mvx, Mvy, Mvz, count
 
 // Per member chunk of an active halo (or of every halo with force): FP64 sums over its bound
-// members (fixed association: per thread in member order, then the block tree).
+// members.  FP64 is slow on this GPU, so the block's partials are combined by a few threads
+// in shared memory rather than by warp trees (fixed association: per thread in member order,
+// then per value four runs of 64 threads, then the four runs in order).
 __global__ void __launch_bounds__(kSegThreads) ub_reduce_seg_kernel(
     const int64_t *__restrict__ off, const int *__restrict__ cstart, const int *__restrict__ chunk_h,
     const double *__restrict__ x, const double *__restrict__ y, const double *__restrict__ z,
@@ -96,19 +103,22 @@ __global__ void __launch_bounds__(kSegThreads) ub_reduce_seg_kernel(
     const int c = blockIdx.x;
     const int h = chunk_h[c];
     if (!force && !hs[h].active) return;
-    __shared__ double sh[kRedSums][32];
+    __shared__ double sh[kRedSums - 1][kSegThreads];
+    __shared__ double q4[kRedSums - 1][4];
     const int64_t b = off[h] + (int64_t)(c - cstart[h]) * kSeg;
     const int64_t e = min(off[h + 1], b + kSeg);
-    double v[kRedSums] = {0, 0, 0, 0, 0, 0, 0, 0};
+    double v[kRedSums - 1] = {0, 0, 0, 0, 0, 0, 0};
+    int count = 0;
     // all loads of the thread's members are issued before any is used; members outside the
-    // chunk or unbound read member b and count with weight 0
-    double w[kSegPer], f[kSegPer][7];
+    // chunk read member b and are skipped
+    bool use[kSegPer];
+    double f[kSegPer][7];
 #pragma unroll
     for (int j = 0; j < kSegPer; ++j) {
         const int64_t i = b + j * kSegThreads + threadIdx.x;
         const bool in = i < e;
         const int64_t s = in ? i : b;
-        w[j] = (in && bound[s]) ? 1.0 : 0.0;
+        use[j] = in && bound[s];
         f[j][0] = m[s];
         f[j][1] = x[s];
         f[j][2] = y[s];
@@ -119,14 +129,35 @@ __global__ void __launch_bounds__(kSegThreads) ub_reduce_seg_kernel(
     }
 #pragma unroll
     for (int j = 0; j < kSegPer; ++j) {
-        if (w[j] == 0.0) continue;
+        if (!use[j]) continue;
         const double mi = f[j][0];
         v[0] += mi;
 #pragma unroll
         for (int k = 1; k < 7; ++k) v[k] += mi * f[j][k];
-        v[7] += 1.0;
+        ++count;
     }
-    block_sum_store<kRedSums>(v, sh, part + (int64_t)c * kRedSums);
+#pragma unroll
+    for (int k = 0; k < kRedSums - 1; ++k) sh[k][threadIdx.x] = v[k];
+    __shared__ int wcount[kSegThreads / 32];
+    int wc = count;
+    for (int o = 16; o > 0; o >>= 1) wc += __shfl_down_sync(0xffffffffu, wc, o);
+    if ((threadIdx.x & 31) == 0) wcount[threadIdx.x >> 5] = wc;
+    __syncthreads();
+    if (threadIdx.x < 4 * (kRedSums - 1)) {
+        const int k = threadIdx.x % (kRedSums - 1), run = threadIdx.x / (kRedSums - 1);
+        double t = 0.0;
+        for (int u = run * (kSegThreads / 4); u < (run + 1) * (kSegThreads / 4); ++u) t += sh[k][u];
+        q4[k][run] = t;
+    }
+    __syncthreads();
+    if (threadIdx.x < kRedSums - 1) {
+        const int k = threadIdx.x;
+        part[(int64_t)c * kRedSums + k] = ((q4[k][0] + q4[k][1]) + q4[k][2]) + q4[k][3];
+    } else if (threadIdx.x == kRedSums - 1) {
+        int tot = 0;
+        for (int w = 0; w < kSegThreads / 32; ++w) tot += wcount[w];
+        part[(int64_t)c * kRedSums + kRedSums - 1] = (double)tot;
+    }
 }
 
 // One warp per halo: chunk sums added in a fixed order (lane-strided, then the warp tree);
@@ -148,11 +179,17 @@ __global__ void ub_reduce_fin_kernel(int nh, const int *__restrict__ cstart, con
         const double M = v[0];
         s.M = M;
         s.nb = (int)v[7];
+        s.sx = v[1]; s.sy = v[2]; s.sz = v[3];
+        s.px = v[4]; s.py = v[5]; s.pz = v[6];
         if (M > 0) {
             s.cx = v[1] / M; s.cy = v[2] / M; s.cz = v[3] / M;
             s.vx = v[4] / M; s.vy = v[5] / M; s.vz = v[6] / M;
         } else {
             s.cx = s.cy = s.cz = s.vx = s.vy = s.vz = 0.0;
+        }
+        if (!force) {   // before the first pass: the reference velocity of the packed velocities
+            s.v0x = s.vx; s.v0y = s.vy; s.v0z = s.vz;
+            s.wx = s.wy = s.wz = 0.f;
         }
     }
 }
@@ -165,11 +202,13 @@ template <class V>
 __global__ void __launch_bounds__(kSegThreads) ub_pack_kernel(
     const int64_t *__restrict__ off, const int64_t *__restrict__ poff, const int *__restrict__ cstart,
     const int *__restrict__ chunk_h, const double *__restrict__ x, const double *__restrict__ y,
-    const double *__restrict__ z, const double *__restrict__ m, const HaloState *__restrict__ hs,
-    V *__restrict__ pk, int *__restrict__ pidx) {
+    const double *__restrict__ z, const double *__restrict__ m, const double *__restrict__ vx,
+    const double *__restrict__ vy, const double *__restrict__ vz, const HaloState *__restrict__ hs,
+    V *__restrict__ pk, float4 *__restrict__ pv, int *__restrict__ pidx) {
     const int c = blockIdx.x;
     const int h = chunk_h[c];
     const double cx = hs[h].cx, cy = hs[h].cy, cz = hs[h].cz;
+    const double v0x = hs[h].v0x, v0y = hs[h].v0y, v0z = hs[h].v0z;
     const int64_t hb = off[h], he = off[h + 1], pb = poff[h];
     const int64_t b = hb + (int64_t)(c - cstart[h]) * kSeg;
     const int64_t e = min(he, b + kSeg);
@@ -178,6 +217,9 @@ __global__ void __launch_bounds__(kSegThreads) ub_pack_kernel(
         r.x = x[i] - cx; r.y = y[i] - cy; r.z = z[i] - cz; r.w = m[i];
         pk[pb + (i - hb)] = r;
         pidx[pb + (i - hb)] = (int)i;
+        // FP32 path: velocity relative to the bulk velocity at packing, and the mass
+        if (pv) pv[pb + (i - hb)] = make_float4((float)(vx[i] - v0x), (float)(vy[i] - v0y), (float)(vz[i] - v0z),
+                                                 (float)m[i]);
     }
     if (e == he) {
         const int64_t nb = he - hb, npad = (nb + 31) & ~31ll;
@@ -186,6 +228,7 @@ __global__ void __launch_bounds__(kSegThreads) ub_pack_kernel(
             f.x = f.y = f.z = kFar; f.w = 0;
             pk[pb + r] = f;
             pidx[pb + r] = -1;
+            if (pv) pv[pb + r] = make_float4(0.f, 0.f, 0.f, 0.f);
         }
     }
 }
@@ -346,7 +389,7 @@ __device__ __forceinline__ void chunk_pairs(const float4 *sa, const float4 *sb, 
 template <int T>
 __device__ __forceinline__ void pair_item(const float4 *__restrict__ tpk, const float4 *__restrict__ pk, int64_t base,
                                           int nb, int tile, float eps2, int c_begin, int c_end, bool self_ok,
-                                          double *__restrict__ out, float4 *buf, int lane) {
+                                          float2 *__restrict__ out, float4 *buf, int lane) {
     {
         f2x tx[T], ty[T], tz[T];
         float sum[T], comp[T];
@@ -392,7 +435,7 @@ __device__ __forceinline__ void pair_item(const float4 *__restrict__ tpk, const 
 #pragma unroll
         for (int t = 0; t < T; ++t) {
             const int r = tile * 32 * T + t * 32 + lane;
-            if (r < nb) out[r] = (double)sum[t] + (double)comp[t];
+            if (r < nb) out[r] = df_from_acc(sum[t], comp[t]);
         }
     }
 }
@@ -411,7 +454,7 @@ __global__ void __launch_bounds__(256) ub_pair_kernel(const float4 *__restrict__
                                                       int nh, const int *__restrict__ istart,
                                                       const int4 *__restrict__ idesc, const int *__restrict__ nitems_p,
                                                       int *counter, float eps2, int slice_chunks,
-                                                      double *__restrict__ part) {
+                                                      float2 *__restrict__ part) {
     __shared__ float4 buf[kUbWarps][32];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int nitems = *nitems_p;
@@ -438,7 +481,7 @@ __global__ void __launch_bounds__(256) ub_pair_kernel(const float4 *__restrict__
         const float4 *src = inc ? spk : pk;
         const int c0 = slice * slice_chunks;
         const int c1 = min((ns + 31) >> 5, c0 + slice_chunks);
-        double *out = part + qoff[h] + (int64_t)slice * npad;
+        float2 *out = part + qoff[h] + (int64_t)slice * npad;
         switch (it.z) {
             case 1: pair_item<1>(pk, src, base, nb, tile, eps2, c0, c1, !inc, out, buf[w], lane); break;
             case 2: pair_item<2>(pk, src, base, nb, tile, eps2, c0, c1, !inc, out, buf[w], lane); break;
@@ -526,7 +569,7 @@ __device__ __forceinline__ void chunk_pairs_sym(const float4 *sa, const float4 *
 // targets tb*kSymBlock + w*128 + t*32 + lane.  Diagonal items (tb == sb) are plain (self pair
 // skipped) and write the targets' partial for slice sb.  Off-diagonal items compute each pair
 // once: the targets' partial goes to slice sb (part[qoff + sb*npad + r]) and the sources'
-// partial -- per source, the 8 warps' sums added in warp order in FP64 -- to slice tb.  So
+// partial -- per source, the 8 warps' sums added in warp order, compensated -- to slice tb.  So
 // slot r of block b receives slice k from item (b, k) for k >= b and from item (k, b) for
 // k < b: every slice exactly once, and the energy kernel adds slices 0..B-1 in order.
 __global__ void __launch_bounds__(256) ub_pair_sym_kernel(const float4 *__restrict__ pk,
@@ -535,7 +578,7 @@ __global__ void __launch_bounds__(256) ub_pair_sym_kernel(const float4 *__restri
                                                           const HaloState *__restrict__ hs, int nh,
                                                           const int *__restrict__ ystart,
                                                           const int4 *__restrict__ idesc, const int *__restrict__ cnt,
-                                                          int *counter, float eps2, double *__restrict__ part) {
+                                                          int *counter, float eps2, float2 *__restrict__ part) {
     extern __shared__ float4 sym_smem[];
     float4 *ssrc = sym_smem;                                            // 32 chunks x (16 + 16) float4
     float *spart = reinterpret_cast<float *>(sym_smem + kSymBlock);     // [kSymWarps][kSymBlock]
@@ -626,25 +669,25 @@ __global__ void __launch_bounds__(256) ub_pair_sym_kernel(const float4 *__restri
                     two_sum_acc(sum[t], comp[t], a0 + a1);
                 }
             }
-            double *out = part + qoff[h] + (int64_t)sb * npad;
+            float2 *out = part + qoff[h] + (int64_t)sb * npad;
 #pragma unroll
             for (int t = 0; t < kSymT; ++t) {
                 const int r = t0 + t * 32 + lane;
-                if (r < nb) out[r] = (double)sum[t] + (double)comp[t];
+                if (r < nb) out[r] = df_from_acc(sum[t], comp[t]);
             }
         } else if (sym) {
             for (int k = lane; k < nch * 32; k += 32) sp[k] = 0.f;   // no targets here: no terms
         }
         if (sym) {
             __syncthreads();
-            double *out = part + qoff[h] + (int64_t)tb * npad;
+            float2 *out = part + qoff[h] + (int64_t)tb * npad;
             for (int k = threadIdx.x; k < nch * 32; k += blockDim.x) {
                 const int s = s0 + k;
                 if (s < nb) {
-                    double v = 0.0;
+                    float sum = 0.f, comp = 0.f;   // the 8 warps' sums in warp order, compensated
 #pragma unroll
-                    for (int ww = 0; ww < kSymWarps; ++ww) v += (double)spart[ww * kSymBlock + k];
-                    out[s] = v;
+                    for (int ww = 0; ww < kSymWarps; ++ww) two_sum_acc(sum, comp, spart[ww * kSymBlock + k]);
+                    out[s] = df_from_acc(sum, comp);
                 }
             }
         }
@@ -871,6 +914,310 @@ __global__ void __launch_bounds__(kSegThreads) ub_compact_seg_kernel(
     }
 }
 
+// ---- end of a pass, FP32 path: per-particle work in FP32 and double-float only ----
+// This GPU's FP64 rate is a small fraction of its FP32 rate, so the per-particle work of the
+// FP32 path runs without FP64: the potential is a double-float (about 48 bits) carried from
+// pass to pass, the energy and its sign test are FP32 (relative error ~1e-7, far inside the
+// 1e-5 band where FP32 pair sums already leave the cut undecided), and the packed velocities
+// are FP32 offsets from the bulk velocity at packing.  The halo's FP64 mass and sums of m x
+// and m v are not re-summed over the survivors: each pass subtracts the FP64 sums over the
+// particles it removed (gathered from the caller's FP64 arrays), usually a few per cent.
+struct SegDF {
+    int removed, kept;
+    float2 ekin, epot;                            // double-float sums over the survivors: m ek, m phi
+    double rm, rmx, rmy, rmz, rmvx, rmvy, rmvz;   // FP64 sums over the removed particles
+};
+
+__device__ __forceinline__ float2 df_warp_sum(float2 v) {
+    for (int o = 16; o > 0; o >>= 1)
+        v = df_add(v, make_float2(__shfl_down_sync(0xffffffffu, v.x, o), __shfl_down_sync(0xffffffffu, v.y, o)));
+    return v;
+}
+
+// Per energy segment: potential phi (double-float: the slices' partials added in order, or,
+// in an incremental pass, the previous potential minus them), FP32 energy
+// E = 1/2 |u - w|^2 - G factor_v^2 phi with u the packed velocity offset and w the halo's
+// current bulk-velocity offset, sign test; survivors' sums of m ek and m phi in double-float;
+// the removed particles are listed in slot order and their FP64 mass, m x and m v summed by
+// warp 0 from the caller's arrays.
+__global__ void __launch_bounds__(kSegThreads) ub_energy_df_kernel(
+    const int *__restrict__ sstart, const int *__restrict__ sown, const int4 *__restrict__ idesc,
+    const int *__restrict__ nsegs, const int64_t *__restrict__ poff, const int64_t *__restrict__ qoff, int inc,
+    const int *__restrict__ pidx, const float4 *__restrict__ pv, const float2 *__restrict__ part,
+    const float2 *__restrict__ phi_prev, float2 *__restrict__ phi_cur, const double *__restrict__ x,
+    const double *__restrict__ y, const double *__restrict__ z, const double *__restrict__ vx,
+    const double *__restrict__ vy, const double *__restrict__ vz, const double *__restrict__ m, float gfac,
+    const HaloState *__restrict__ hs, unsigned char *__restrict__ bound, double *__restrict__ phi_out,
+    unsigned char *__restrict__ keepf, SegDF *__restrict__ seg_sums) {
+    const int seg = blockIdx.x;
+    if (seg >= *nsegs) return;
+    __shared__ unsigned char gone[kSeg];
+    __shared__ int rlist[kSeg];
+    __shared__ float2 se[2][kSegThreads / 32];
+    __shared__ int sc[2][kSegThreads / 32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int q = sown[seg];
+    const int h = idesc[q].x;
+    const int nsl = idesc[q].w;   // partial-sum slices written by this pass's pair kernels
+    const int sl = seg - sstart[q];
+    const int nb = hs[h].nb;
+    const float wx = hs[h].wx, wy = hs[h].wy, wz = hs[h].wz;
+    const int64_t pb = poff[h], npad = poff[h + 1] - pb, qb = qoff[h];
+    const int rend = min(nb, (sl + 1) * kSeg);
+    int r[kSegPer];
+    bool ok[kSegPer];
+    float4 u[kSegPer];
+    float2 d[kSegPer];
+#pragma unroll
+    for (int j = 0; j < kSegPer; ++j) {
+        r[j] = sl * kSeg + j * kSegThreads + threadIdx.x;
+        ok[j] = r[j] < rend;
+        u[j] = ok[j] ? pv[pb + r[j]] : make_float4(0.f, 0.f, 0.f, 0.f);
+        d[j] = make_float2(0.f, 0.f);
+    }
+    for (int k = 0; k < nsl; ++k)   // slices in order
+#pragma unroll
+        for (int j = 0; j < kSegPer; ++j)
+            if (ok[j]) d[j] = df_add(d[j], part[qb + (int64_t)k * npad + r[j]]);
+    float ek_s = 0.f, ek_c = 0.f, ep_s = 0.f, ep_c = 0.f;
+    int kept = 0, removed = 0;
+#pragma unroll
+    for (int j = 0; j < kSegPer; ++j) {
+        const int slot = j * kSegThreads + threadIdx.x;   // within the segment
+        if (!ok[j]) {
+            gone[slot] = 0;
+            continue;
+        }
+        // full pass: the sum itself; incremental pass: previous potential minus the removed
+        // particles' contribution
+        const float2 p = inc ? df_sub(phi_prev[pb + r[j]], d[j]) : d[j];
+        phi_cur[pb + r[j]] = p;
+        const float pf = p.x + p.y;
+        const float dx = u[j].x - wx, dy = u[j].y - wy, dz = u[j].z - wz;
+        const float ek = 0.5f * (dx * dx + dy * dy + dz * dz);
+        const float e = ek - gfac * pf;
+        const bool keep = !(e > 0.f);
+        keepf[pb + r[j]] = keep ? 1 : 0;
+        gone[slot] = keep ? 0 : 1;
+        if (keep) {
+            ++kept;
+            two_sum_acc(ek_s, ek_c, u[j].w * ek);
+            two_sum_acc(ep_s, ep_c, u[j].w * pf);
+            if (phi_out) phi_out[pidx[pb + r[j]]] = df_to_double(p);
+        } else {
+            ++removed;
+            const int i = pidx[pb + r[j]];
+            bound[i] = 0;
+            if (phi_out) phi_out[i] = 0.0;
+        }
+    }
+    // block sums: counts exactly, energies in double-float (warp tree, then warps in order)
+    float2 ekv = df_warp_sum(df_from_acc(ek_s, ek_c));
+    float2 epv = df_warp_sum(df_from_acc(ep_s, ep_c));
+    int kc = kept, rc = removed;
+    for (int o = 16; o > 0; o >>= 1) {
+        kc += __shfl_down_sync(0xffffffffu, kc, o);
+        rc += __shfl_down_sync(0xffffffffu, rc, o);
+    }
+    if (lane == 0) {
+        se[0][w] = ekv;
+        se[1][w] = epv;
+        sc[0][w] = kc;
+        sc[1][w] = rc;
+    }
+    __syncthreads();
+    int nrem = 0;
+    for (int k = 0; k < kSegThreads / 32; ++k) nrem += sc[1][k];
+    if (w == 0) {
+        // the removed particles in slot order (32 slots per step)
+        int base = 0;
+        if (nrem > 0)
+            for (int s0 = 0; s0 < kSeg; s0 += 32) {
+                const bool g = gone[s0 + lane];
+                const unsigned bal = __ballot_sync(0xffffffffu, g);
+                if (g) rlist[base + __popc(bal & ((1u << lane) - 1u))] = pidx[pb + sl * kSeg + s0 + lane];
+                base += __popc(bal);
+            }
+        __syncwarp();
+        double a[7] = {0, 0, 0, 0, 0, 0, 0};
+        for (int k = lane; k < nrem; k += 32) {
+            const int i = rlist[k];
+            const double mi = m[i];
+            a[0] += mi;
+            a[1] += mi * x[i];
+            a[2] += mi * y[i];
+            a[3] += mi * z[i];
+            a[4] += mi * vx[i];
+            a[5] += mi * vy[i];
+            a[6] += mi * vz[i];
+        }
+        if (nrem > 0)
+#pragma unroll
+            for (int k = 0; k < 7; ++k) a[k] = warp_sum(a[k]);
+        if (lane == 0) {
+            SegDF o;
+            o.removed = nrem;
+            o.kept = 0;
+            float2 e0 = make_float2(0.f, 0.f), e1 = make_float2(0.f, 0.f);
+            for (int k = 0; k < kSegThreads / 32; ++k) {
+                o.kept += sc[0][k];
+                e0 = df_add(e0, se[0][k]);
+                e1 = df_add(e1, se[1][k]);
+            }
+            o.ekin = e0;
+            o.epot = e1;
+            o.rm = a[0]; o.rmx = a[1]; o.rmy = a[2]; o.rmz = a[3];
+            o.rmvx = a[4]; o.rmvy = a[5]; o.rmvz = a[6];
+            seg_sums[seg] = o;
+        }
+    }
+}
+
+// One warp per active ordered halo after the energy pass (FP32 path): segment sums in a fixed
+// order; survivors / removed before each segment (seg_pre); removals, pass count, energies;
+// the halo's FP64 mass and sums of m x, m v less the removed particles' (a halo left empty
+// is set to zero exactly), its centre, bulk velocity and the FP32 bulk-velocity offset for
+// the next pass.  A halo whose pass removed nothing becomes inactive.
+__global__ void ub_finalize_df_kernel(int nh, const int *__restrict__ order, const int *__restrict__ sstart,
+                                      const SegDF *__restrict__ seg_sums, double gfac, HaloState *hs,
+                                      int2 *__restrict__ seg_pre) {
+    const int q = (int)((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5);
+    const int lane = threadIdx.x & 31;
+    if (q >= nh) return;
+    const int h = order[q];
+    if (!hs[h].active) return;
+    const int s0 = sstart[q], s1 = sstart[q + 1];
+    float2 ek = make_float2(0.f, 0.f), ep = make_float2(0.f, 0.f);
+    double a[7] = {0, 0, 0, 0, 0, 0, 0};
+    int keep_run = 0, rem_run = 0;
+    for (int b0 = s0; b0 < s1; b0 += 32) {
+        const int sg = b0 + lane;
+        const bool ok = sg < s1;
+        const int nrem = ok ? seg_sums[sg].removed : 0;
+        const int nkeep = ok ? seg_sums[sg].kept : 0;
+        const int ri = warp_incl_scan(nrem, lane), ki = warp_incl_scan(nkeep, lane);
+        if (ok) seg_pre[sg] = make_int2(keep_run + ki - nkeep, rem_run + ri - nrem);
+        keep_run += __shfl_sync(0xffffffffu, ki, 31);
+        rem_run += __shfl_sync(0xffffffffu, ri, 31);
+        if (ok) {
+            const SegDF &g = seg_sums[sg];
+            ek = df_add(ek, g.ekin);
+            ep = df_add(ep, g.epot);
+            if (g.removed > 0) {
+                a[0] += g.rm; a[1] += g.rmx; a[2] += g.rmy; a[3] += g.rmz;
+                a[4] += g.rmvx; a[5] += g.rmvy; a[6] += g.rmvz;
+            }
+        }
+    }
+    ek = df_warp_sum(ek);
+    ep = df_warp_sum(ep);
+    if (rem_run > 0)
+#pragma unroll
+        for (int k = 0; k < 7; ++k) a[k] = warp_sum(a[k]);
+    if (lane == 0) {
+        HaloState &o = hs[h];
+        o.nprev = o.nb;
+        o.removed = rem_run;
+        o.nrem = rem_run;
+        o.iter += 1;
+        o.ekin = df_to_double(ek);
+        o.epot = -0.5 * gfac * df_to_double(ep);
+        if (rem_run == 0) {
+            o.active = 0;
+        } else {
+            o.nb = keep_run;
+            if (keep_run == 0) {
+                o.M = o.sx = o.sy = o.sz = o.px = o.py = o.pz = 0.0;
+            } else {
+                o.M -= a[0];
+                o.sx -= a[1]; o.sy -= a[2]; o.sz -= a[3];
+                o.px -= a[4]; o.py -= a[5]; o.pz -= a[6];
+            }
+            const double M = o.M;
+            if (M > 0) {
+                o.cx = o.sx / M; o.cy = o.sy / M; o.cz = o.sz / M;
+                o.vx = o.px / M; o.vy = o.py / M; o.vz = o.pz / M;
+            } else {
+                o.cx = o.cy = o.cz = o.vx = o.vy = o.vz = 0.0;
+            }
+            o.wx = (float)(o.vx - o.v0x);
+            o.wy = (float)(o.vy - o.v0y);
+            o.wz = (float)(o.vz - o.v0z);
+        }
+    }
+}
+
+// Per segment of a halo that stays active (FP32 path): survivors' packed position, velocity
+// offset, index and potential copied in order into the other buffers, removed particles'
+// packed positions into the next pass's source list; the halo's last segment pads both.
+__global__ void __launch_bounds__(kSegThreads) ub_compact_df_kernel(
+    const int *__restrict__ sstart, const int *__restrict__ sown, const int4 *__restrict__ idesc,
+    const int *__restrict__ nsegs, const int64_t *__restrict__ poff, const HaloState *__restrict__ hs,
+    const unsigned char *__restrict__ keepf, const int2 *__restrict__ seg_pre, const float4 *__restrict__ pk_in,
+    const float4 *__restrict__ pv_in, const int *__restrict__ pidx_in, const float2 *__restrict__ phi_cur,
+    float4 *__restrict__ pk_out, float4 *__restrict__ pv_out, int *__restrict__ pidx_out,
+    float2 *__restrict__ phi_next, float4 *__restrict__ removed) {
+    const int seg = blockIdx.x;
+    if (seg >= *nsegs) return;
+    __shared__ int wcount[kSegThreads / 32], wrem[kSegThreads / 32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int q = sown[seg];
+    const int h = idesc[q].x;
+    if (!hs[h].active) return;   // converged this pass: its packed slots are not read again
+    const int s0 = sstart[q], sl = seg - s0, nseg = sstart[q + 1] - s0;
+    const int nb = hs[h].nprev;
+    const int64_t pb = poff[h];
+    const int2 pre = seg_pre[seg];
+    int running = pre.x, rrunning = pre.y;
+    const int rend = min(nb, (sl + 1) * kSeg);
+    for (int r0 = sl * kSeg; r0 < rend; r0 += kSegThreads) {
+        const int r = r0 + threadIdx.x;
+        const bool valid = r < rend;
+        const bool keep = valid && keepf[pb + r];
+        const bool gone = valid && !keep;
+        const unsigned bal = __ballot_sync(0xffffffffu, keep);
+        const unsigned bgone = __ballot_sync(0xffffffffu, gone);
+        if (lane == 0) {
+            wcount[w] = __popc(bal);
+            wrem[w] = __popc(bgone);
+        }
+        __syncthreads();
+        int rank = running, rrank = rrunning, tot = 0, trem = 0;
+#pragma unroll
+        for (int k = 0; k < kSegThreads / 32; ++k) {
+            if (k < w) {
+                rank += wcount[k];
+                rrank += wrem[k];
+            }
+            tot += wcount[k];
+            trem += wrem[k];
+        }
+        rank += __popc(bal & ((1u << lane) - 1u));
+        rrank += __popc(bgone & ((1u << lane) - 1u));
+        if (keep) {
+            pk_out[pb + rank] = pk_in[pb + r];
+            pv_out[pb + rank] = pv_in[pb + r];
+            pidx_out[pb + rank] = pidx_in[pb + r];
+            phi_next[pb + rank] = phi_cur[pb + r];
+        } else if (gone) {
+            removed[pb + rrank] = pk_in[pb + r];
+        }
+        running += tot;
+        rrunning += trem;
+        __syncthreads();
+    }
+    if (sl == nseg - 1) {   // the halo's last segment pads after the survivors and the removed
+        const float4 f = make_float4(kFar, kFar, kFar, 0.f);
+        const int nkeep = running, nrem = rrunning;
+        for (int r = nkeep + threadIdx.x; r < ((nkeep + 31) & ~31); r += kSegThreads) {
+            pk_out[pb + r] = f;
+            pv_out[pb + r] = make_float4(0.f, 0.f, 0.f, 0.f);
+            pidx_out[pb + r] = -1;
+        }
+        for (int r = nrem + threadIdx.x; r < ((nrem + 31) & ~31); r += kSegThreads) removed[pb + r] = f;
+    }
+}
+
 // Plain FP64 pair kernel for one halo (targets = sources = its packed slots).
 __global__ void __launch_bounds__(256) ub_pair_f64_kernel(const double4 *__restrict__ pk, int nb, double eps2,
                                                           double *__restrict__ phi) {
@@ -997,7 +1344,8 @@ int unbind_device(int64_t n, int nh, const int64_t *d_off, const int64_t *h_off,
     const size_t o_istart = L.add(sizeof(int) * (nh + 1));
     const size_t o_sstart = L.add(sizeof(int) * (nh + 1));
     const size_t o_idesc = L.add(sizeof(int4) * std::max(nh, 1));
-    const size_t o_ssum = L.add(sizeof(double) * kSegSums * segcap);
+    const size_t o_ssum = L.add(std::max(sizeof(double) * kSegSums, sizeof(SegDF)) * segcap);
+    const size_t o_pv = L.add(f64 ? 0 : sizeof(float4) * P), o_pv2 = L.add(f64 ? 0 : sizeof(float4) * P);
     const size_t o_sown = L.add(sizeof(int) * segcap);
     const size_t o_spre = L.add(sizeof(int2) * segcap);
     const size_t o_cst = L.add(sizeof(int) * (nh + 1));
@@ -1067,6 +1415,11 @@ int unbind_device(int64_t n, int nh, const int64_t *d_off, const int64_t *h_off,
 
     if (!f64) {
         float4 *pkb[2] = {at<float4>(base, o_pk), at<float4>(base, o_pk2)};
+        float4 *pvb[2] = {at<float4>(base, o_pv), at<float4>(base, o_pv2)};
+        auto *part2 = reinterpret_cast<float2 *>(phi);   // double-float partials and potentials
+        auto *phic2 = reinterpret_cast<float2 *>(phic), *phin2 = reinterpret_cast<float2 *>(phin);
+        auto *sdf = reinterpret_cast<SegDF *>(ssum);
+        const float gfac_f = (float)gfac;
         int bps = 0;
         HALMA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, ub_pair_kernel, 256, 0));
         const int pgrid = device_sm_count() * std::max(bps, 1);
@@ -1080,7 +1433,7 @@ int unbind_device(int64_t n, int nh, const int64_t *d_off, const int64_t *h_off,
             HALMA_TRY(reduce(rs, 0));
             if (nchunks > 0)
                 HALMA_LAUNCH(ub_pack_kernel<float4>, nchunks, kSegThreads, 0, rs, off, dpoff, dcst, dchh, x, y, z, m,
-                             hs, pkb[0], pidxb[0]);
+                             vx, vy, vz, hs, pkb[0], pvb[0], pidxb[0]);
             float4 *rk = at<float4>(base, o_rk);
             for (int it = 0; it < p.max_iter; ++it) {
                 const int a = it & 1, b = a ^ 1;
@@ -1093,16 +1446,16 @@ int unbind_device(int64_t n, int nh, const int64_t *d_off, const int64_t *h_off,
                 // tiles of the small ones; incremental passes have only tiles
                 if (!inc)
                     HALMA_LAUNCH(ub_pair_sym_kernel, ygrid, 256, kSymSmem, rs, pkb[a], dpoff, dqoff, hs, nh, ystart,
-                                 idesc, cnt, cnt + 4, eps2, phi);
+                                 idesc, cnt, cnt + 4, eps2, part2);
                 HALMA_LAUNCH(ub_pair_kernel, pgrid, 256, 0, rs, pkb[a], rk, inc, dpoff, dqoff, hs, nh, istart, idesc,
-                             cnt, cnt + 1, eps2, slice_len / 32, phi);
+                             cnt, cnt + 1, eps2, slice_len / 32, part2);
                 if (profiling) HALMA_CUDA(cudaEventRecordWithFlags(prof.ev1[it], rs, cudaEventRecordExternal));
-                HALMA_LAUNCH(ub_energy_seg_kernel<float4>, sgrid, kSegThreads, 0, rs, sstart, sown, idesc, cnt + 2,
-                             dpoff, dqoff, inc, pidxb[a], phi, phin, phic, vx, vy, vz, m, gfac, hs, bound, phi_out,
-                             keepf, ssum);
-                HALMA_LAUNCH(ub_finalize_kernel, fgrid, 256, 0, rs, nh, dorder, sstart, ssum, gfac, hs, segpre);
-                HALMA_LAUNCH(ub_compact_seg_kernel<float4>, sgrid, kSegThreads, 0, rs, sstart, sown, idesc, cnt + 2,
-                             dpoff, hs, keepf, segpre, pkb[a], pidxb[a], phic, pkb[b], pidxb[b], phin, rk);
+                HALMA_LAUNCH(ub_energy_df_kernel, sgrid, kSegThreads, 0, rs, sstart, sown, idesc, cnt + 2, dpoff, dqoff,
+                             inc, pidxb[a], pvb[a], part2, phin2, phic2, x, y, z, vx, vy, vz, m, gfac_f, hs, bound,
+                             phi_out, keepf, sdf);
+                HALMA_LAUNCH(ub_finalize_df_kernel, fgrid, 256, 0, rs, nh, dorder, sstart, sdf, gfac, hs, segpre);
+                HALMA_LAUNCH(ub_compact_df_kernel, sgrid, kSegThreads, 0, rs, sstart, sown, idesc, cnt + 2, dpoff, hs,
+                             keepf, segpre, pkb[a], pvb[a], pidxb[a], phic2, pkb[b], pvb[b], pidxb[b], phin2, rk);
             }
             return HALMA_OK;
         };
@@ -1161,8 +1514,7 @@ int unbind_device(int64_t n, int nh, const int64_t *d_off, const int64_t *h_off,
         } else {
             HALMA_TRY(record(st));
         }
-        // final bound mass, centre and bulk velocity over the final bound sets
-        HALMA_TRY(reduce(st, 1));
+        // the halo state already holds the final bound set's mass, centre and bulk velocity
         if (profiling) {
             std::vector<unsigned long long> hp(2 * p.max_iter);
             HALMA_CUDA(cudaMemcpyAsync(hp.data(), dpairs, sizeof(unsigned long long) * 2 * p.max_iter,
@@ -1181,8 +1533,8 @@ int unbind_device(int64_t n, int nh, const int64_t *d_off, const int64_t *h_off,
         std::vector<HaloState> hh(nh);
         HALMA_TRY(reduce(st, 0));
         if (nchunks > 0)
-            HALMA_LAUNCH(ub_pack_kernel<double4>, nchunks, kSegThreads, 0, st, off, dpoff, dcst, dchh, x, y, z, m, hs,
-                         pkb[0], pidxb[0]);
+            HALMA_LAUNCH(ub_pack_kernel<double4>, nchunks, kSegThreads, 0, st, off, dpoff, dcst, dchh, x, y, z, m, vx,
+                         vy, vz, hs, pkb[0], nullptr, pidxb[0]);
         double4 *rk = at<double4>(base, o_rk);
         for (int it = 0; it < p.max_iter; ++it) {
             const int a = it & 1, b = a ^ 1;
