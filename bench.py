@@ -260,7 +260,7 @@ def run_gpu(args):
 
     # timed region: inputs resident in HBM, L2 flushed before every step
     ms, pairs, pair_ms, fof_ms, unbind_ms, passes = [], 0.0, 0.0, [], [], []
-    sym_pairs, per_pass = 0.0, []
+    sym_pairs, sym_ms, sym_launches, per_pass = 0.0, 0.0, 0, []
     sampler = ClockSampler(local)
     sampler.start()
     launches0 = _lib.launch_count()
@@ -277,13 +277,17 @@ def run_gpu(args):
         st = _lib.profile_stats()
         fof_ms.append(st["fof_ms"])
         unbind_ms.append(st["unbind_ms"])
-        for (p, t), sp in zip(st["passes"], st["sym_pairs"]):
+        for (p, t), sp, sm in zip(st["passes"], st["sym_pairs"], st["sym_ms"]):
             if p > 0:
                 pairs += p
                 pair_ms += t
                 sym_pairs += sp
+            if sp > 0:
+                sym_ms += sm
+                sym_launches += 1
         passes.append(sum(1 for p, _ in st["passes"] if p > 0))
-        per_pass = [[int(p), round(t, 4), int(sp)] for (p, t), sp in zip(st["passes"], st["sym_pairs"]) if p > 0]
+        per_pass = [[int(p), round(t, 4), int(sp), round(sm, 4)]
+                    for (p, t), sp, sm in zip(st["passes"], st["sym_pairs"], st["sym_ms"]) if p > 0]
     barrier()
     wall = time.perf_counter() - wall0
     launches = _lib.launch_count() - launches0
@@ -342,20 +346,35 @@ def run_gpu(args):
     lane_ops = OPS_PER_TERM * (pairs - sym_pairs) + OPS_PER_SYM_TERM * sym_pairs
     achieved = flops / (pair_ms * 1e-3) / 1e12 if pair_ms > 0 else 0.0
     pipe = lane_ops / (pair_ms * 1e-3) / (FP32_OPS_PER_CLK_SM * sms * sm_max * 1e6) if pair_ms > 0 else 0.0
-    traffic = None
+    traffic = {}
     tp = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(tp):
-        traffic = json.load(open(tp)).get("ub_pair_kernel_bytes_per_launch")
-    roofline = {"bound": "fp32", "kernel": "ub_pair_kernel", "achieved": achieved, "peak": pair_peak,
-                "unit": "TFLOP/s", "frac": achieved / pair_peak if pair_peak else None, "traffic": traffic,
-                "peak_source": f"FP32 peak: 128 lanes x 2 flops (FMA) x {sms} SMs x {sm_max:.0f} MHz (sm_max_mhz "
-                               f"{src}); flops from the instruction mix: 11 per pair term, 6.5 per term "
-                               f"on the symmetric block kernel (3 of every 7 or 8 lane-operations are "
-                               f"1-flop subtractions, so frac <= 0.79 at a full FP32 pipe)",
-                "fp32_pipe_frac": pipe,
-                "sym_pair_terms": sym_pairs,
-                "pairs_per_launch": pairs / max(n_pair_launches, 1), "ms_per_launch": pair_ms / max(n_pair_launches, 1),
-                "launches_timed": n_pair_launches, "last_step_passes_pairs_ms": per_pass}
+        traffic = json.load(open(tp))
+    # the dominant kernel: the symmetric block kernel of the first (full) pass, timed alone
+    sym_flops = FLOPS_PER_SYM_TERM * sym_pairs
+    sym_achieved = sym_flops / (sym_ms * 1e-3) / 1e12 if sym_ms > 0 else 0.0
+    sym_pipe = OPS_PER_SYM_TERM * sym_pairs / (sym_ms * 1e-3) / (FP32_OPS_PER_CLK_SM * sms * sm_max * 1e6) \
+        if sym_ms > 0 else 0.0
+    peak_note = (f"FP32 peak: 128 lanes x 2 flops (FMA) x {sms} SMs x {sm_max:.0f} MHz (sm_max_mhz {src}); "
+                 f"flops from the instruction mix: 6.5 per pair term on the symmetric block kernel (a pair "
+                 f"evaluated once for both particles: 3 sub + 3 fma + 2 fma = 13 flops), 11 per term on the "
+                 f"per-particle tile kernel (3 sub + 3 fma + 1 fma); 3 of every 8 (7) lane-operations are "
+                 f"1-flop subtractions, so frac <= 0.81 (0.79) at a full FP32 pipe")
+    roofline = {"bound": "fp32", "kernel": "ub_pair_sym_kernel", "achieved": sym_achieved, "peak": pair_peak,
+                "unit": "TFLOP/s", "frac": sym_achieved / pair_peak if pair_peak else None,
+                "traffic": traffic.get("ub_pair_sym_kernel_bytes_per_launch"),
+                "peak_source": peak_note, "fp32_pipe_frac": sym_pipe,
+                "pair_terms_per_launch": sym_pairs / max(sym_launches, 1),
+                "ms_per_launch": sym_ms / max(sym_launches, 1), "launches_timed": sym_launches,
+                "pair_terms_per_s": sym_pairs / (sym_ms * 1e-3) if sym_ms > 0 else 0.0}
+    roofline_pairs = {"bound": "fp32", "kernel": "ub_pair_sym_kernel + ub_pair_kernel (every pass)",
+                      "achieved": achieved, "peak": pair_peak, "unit": "TFLOP/s",
+                      "frac": achieved / pair_peak if pair_peak else None,
+                      "traffic_ub_pair_kernel": traffic.get("ub_pair_kernel_bytes_per_launch"),
+                      "fp32_pipe_frac": pipe, "sym_pair_terms": sym_pairs,
+                      "pairs_per_launch": pairs / max(n_pair_launches, 1),
+                      "ms_per_launch": pair_ms / max(n_pair_launches, 1), "launches_timed": n_pair_launches,
+                      "last_step_passes_pairs_ms_sympairs_symms": per_pass}
     fof_gbs = FOF_BYTES_PER_PARTICLE * n / (statistics.mean(fof_ms) * 1e-3) / 1e9
     roofline_fof = {"bound": "hbm", "achieved": fof_gbs, "peak": hbm, "unit": "GB/s", "frac": fof_gbs / hbm,
                     "traffic": None, "ms": statistics.mean(fof_ms),
@@ -370,7 +389,7 @@ def run_gpu(args):
                            unbind_ms=statistics.mean(unbind_ms), reductions="FP64",
                            parallelism=f"snapshot-per-rank x{world}"),
             "pair_interactions_per_s": pairs / (sum(ms) * 1e-3) * world,
-            "roofline": roofline, "roofline_fof": roofline_fof,
+            "roofline": roofline, "roofline_pair_kernels": roofline_pairs, "roofline_fof": roofline_fof,
             "e2e": {"value": n * world / (e2e_step * 1e-3), "unit": "particles/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "ms_per_step": e2e_step},
             "gpu_launches": launches, "clocks": clocks, "fp64_path": fp64, "wall_s_timed": wall}

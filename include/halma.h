@@ -31,6 +31,9 @@
  *                                    escape_velocity_unbinding_fortran (single pass),
  *                                    iterated until no particle is removed
  *   halma_potential_grad_f32      <- no reference counterpart (adjoint of the potential)
+ *   halma_fof_segmented           <- the per-halo fof.friends_of_friends_serial calls of the
+ *                                    substructure loop (pyHALMA.py:716-726), batched
+ *   halma_split_bridges           <- the substructure block pyHALMA.py:703-766
  */
 #ifndef HALMA_H
 #define HALMA_H
@@ -64,10 +67,11 @@ int64_t     halma_kernel_launch_count(void);
 /* Measurement hooks (no reference counterpart).  With profiling on, the unbinding records
  * CUDA events around every pair-kernel launch on the launching stream and the pair count of
  * every pass, and halma_find_haloes times its FoF and unbinding stages.  halma_profile_stats
- * fills out[] with [fof_ms, unbind_ms, n_passes, pairs_0, ms_0, sym_pairs_0, pairs_1, ...]
- * for the last call (per pass: pair terms, pair-kernel milliseconds, and the pair terms of
- * the haloes that ran on the symmetric block kernel, where each pair is evaluated once for
- * both particles) and returns the number of values available. */
+ * fills out[] with [fof_ms, unbind_ms, n_passes, pairs_0, ms_0, sym_pairs_0, sym_ms_0,
+ * pairs_1, ...] for the last call (per pass: pair terms, milliseconds of the pass's pair
+ * kernels, the pair terms of the haloes that ran on the symmetric block kernel, where each
+ * pair is evaluated once for both particles, and the milliseconds of that kernel alone) and
+ * returns the number of values available. */
 int         halma_set_profiling(int32_t on);
 int         halma_profile_stats(double *out, int32_t cap);
 
@@ -89,6 +93,44 @@ int halma_fof(int64_t n, const double *x, const double *y, const double *z,
 int halma_fof_groups(int64_t n, const int32_t *labels, int32_t min_members,
                      int64_t *offsets, int32_t *members, int64_t *n_groups,
                      halma_stream_t stream);
+
+/* FoF inside segments, all segments in one call: rows seg_offsets[s] .. seg_offsets[s+1]
+ * form segment s (offsets from 0 to n, non-decreasing) and two rows link only when they
+ * are in the same segment.  Replaces the per-halo calls
+ * fof.friends_of_friends_serial(st_x[part_list], st_y[part_list], st_z[part_list], sub_LL)
+ * of the substructure loop (pyHALMA.py:716-726): with the members of each halo gathered
+ * into consecutive rows, halma_fof_groups on these labels gives every halo's sub-groups in
+ * the reference order, halo after halo.  Same pair rule and labels as halma_fof (smallest
+ * row index of the component, -1 for rows without a friend in their segment). */
+int halma_fof_segmented(int64_t n, const double *x, const double *y, const double *z,
+                        int64_t n_segments, const int64_t *seg_offsets, double linking_length,
+                        int32_t *labels, int64_t *n_groups, halma_stream_t stream);
+
+/* Bridge splitting of the substructure block (pyHALMA.py:703-766), parameters as read from
+ * pyHALMA.dat (pyHALMA.py:96-98; lengths in the unit of the positions). */
+typedef struct {
+    double  linking_length;  /* LL of the FoF that made the groups                       */
+    double  dec_factor;      /* DEC_FACTOR (> 1): sub_LL = LL/DEC, LL/DEC^2, ...         */
+    double  min_ll;          /* MIN_LL: levels run while sub_LL > MIN_LL                 */
+    double  dist_factor;     /* DIST_FACTOR: a sub-group is cut off when its centre of
+                                mass is farther than DIST_FACTOR * r_half from the halo's */
+    int32_t minp_sub;        /* MINP_SUB: smallest sub-group considered                  */
+    int32_t minp;            /* MINP: smallest group kept at the end                      */
+} halma_substructure_params;
+
+/* Input: the FoF groups (after good_groups(MINP)) as CSR over snapshot indices, members
+ * ascending, in the reference order.  Output: the groups that pyHALMA.py:703-766 leaves,
+ * in its order: the input groups (reduced by the sub-groups cut off; emptied when less than
+ * 30 % of their particles remain) followed by the sub-groups cut off (halo by halo, level
+ * by level, each level by smallest member), every group with fewer than MINP members
+ * dropped.  *n_out receives the number of groups (HALMA_ERR_CAPACITY, with *n_out set,
+ * when it exceeds out_capacity); out_offsets holds n_out+1 entries, out_members at most
+ * the input's member count.  *n_cut (optional) receives the reference's counter_sub. */
+int halma_split_bridges(int64_t n, const double *x, const double *y, const double *z,
+                        const double *m, int64_t n_groups, const int64_t *group_offsets,
+                        const int32_t *group_members, const halma_substructure_params *params,
+                        int64_t *n_out, int64_t out_capacity, int64_t *out_offsets,
+                        int32_t *out_members, int64_t *n_cut, halma_stream_t stream);
 
 /* ------------------------------------------------------------------------------------ */
 /* Brute-force potential                                                                */

@@ -51,6 +51,12 @@ class UnbindParams(ctypes.Structure):
 UNBIND_FULL_RECOMPUTE = 1
 
 
+class SubstructureParams(ctypes.Structure):
+    _fields_ = [("linking_length", ctypes.c_double), ("dec_factor", ctypes.c_double),
+                ("min_ll", ctypes.c_double), ("dist_factor", ctypes.c_double),
+                ("minp_sub", ctypes.c_int32), ("minp", ctypes.c_int32)]
+
+
 _lock = threading.Lock()
 _lib = None
 
@@ -71,6 +77,9 @@ SIGNATURES = {
     "halma_profile_stats": ([_P, _I32], ctypes.c_int),
     "halma_fof": ([_I64, _P, _P, _P, _F64, _P, _P, _P], ctypes.c_int),
     "halma_fof_groups": ([_I64, _P, _I32, _P, _P, _P, _P], ctypes.c_int),
+    "halma_fof_segmented": ([_I64, _P, _P, _P, _I64, _P, _F64, _P, _P, _P], ctypes.c_int),
+    "halma_split_bridges": ([_I64, _P, _P, _P, _P, _I64, _P, _P, ctypes.POINTER(SubstructureParams), _P, _I64, _P,
+                             _P, _P, _P], ctypes.c_int),
     "halma_bf_potential_f32": ([_I64, _P, _P, _P, _P, _I64, _P, _P, _P, _P, _I32, _F64, _P], ctypes.c_int),
     "halma_potential_f64": ([_I64, _P, _P, _P, _P, _I64, _P, _P, _P, _F64, _I32, _I64, _P, _P], ctypes.c_int),
     "halma_potential_f32": ([_I64, _P, _P, _P, _P, _I64, _P, _P, _P, _F64, _I32, _I64, _P, _P], ctypes.c_int),
@@ -121,15 +130,18 @@ def set_profiling(on: bool):
 
 
 def profile_stats():
-    """Last call's measurements: dict(fof_ms, unbind_ms, passes=[(pairs, pair_kernel_ms), ...],
-    sym_pairs=[pairs of each pass evaluated by the symmetric block kernel])."""
+    """Last call's measurements: dict(fof_ms, unbind_ms, passes=[(pairs, pair_kernels_ms), ...],
+    sym_pairs=[pair terms of each pass evaluated by the symmetric block kernel],
+    sym_ms=[milliseconds of that kernel in each pass])."""
     n = lib().halma_profile_stats(None, 0)
     buf = np.zeros(max(n, 3))
     lib().halma_profile_stats(buf.ctypes.data_as(ctypes.c_void_p), len(buf))
     k = int(buf[2])
-    passes = [(float(buf[3 + 3 * i]), float(buf[4 + 3 * i])) for i in range(k)]
-    sym = [float(buf[5 + 3 * i]) for i in range(k)]
-    return {"fof_ms": float(buf[0]), "unbind_ms": float(buf[1]), "passes": passes, "sym_pairs": sym}
+    passes = [(float(buf[3 + 4 * i]), float(buf[4 + 4 * i])) for i in range(k)]
+    sym = [float(buf[5 + 4 * i]) for i in range(k)]
+    sym_ms = [float(buf[6 + 4 * i]) for i in range(k)]
+    return {"fof_ms": float(buf[0]), "unbind_ms": float(buf[1]), "passes": passes, "sym_pairs": sym,
+            "sym_ms": sym_ms}
 
 
 # ---------------------------------------------------------------------------------------

@@ -19,6 +19,7 @@
 // The result is the reference's partition exactly: same components, same canonical labels.
 #include <math.h>
 #include <limits.h>
+#include <string.h>
 
 #include "common.cuh"
 #include "sort.cuh"
@@ -37,6 +38,16 @@ struct FofGeom {
     float cs, lo, hi;
     long long ncx, ncy, ncz;
     int sb;   // low key bits holding the 4 x 4 x 4 sub-cell (Morton order) within the cell: 6 or 0
+};
+
+// Segmented FoF (links only inside a segment): every segment gets its own origin (the
+// minimum corner of its bounding box) and its own run of x columns of one virtual cell grid,
+// followed by an empty column, so that a cell's forward neighbours are either cells of the
+// same segment or empty.  All pointers are null for a plain FoF.
+struct SegGeom {
+    const int *seg_of = nullptr;       // segment of each particle
+    const double *smin = nullptr;      // [3 * nseg] origin of each segment
+    const long long *scol = nullptr;   // [4 * nseg] first virtual x column, columns in x, y, z
 };
 
 __device__ __forceinline__ uint64_t mix64(uint64_t k) {
@@ -155,17 +166,29 @@ __global__ void bbox_final_kernel(const double *__restrict__ part, int g, double
 // Morton order, so that each 32-particle chunk of a crowded cell is spatially compact.  The
 // order of particles inside a cell does not change the partition.
 __global__ void keys_kernel(const double *__restrict__ x, const double *__restrict__ y,
-                            const double *__restrict__ z, int n, FofGeom g,
+                            const double *__restrict__ z, int n, FofGeom g, SegGeom sg,
                             uint64_t *__restrict__ keys, int *__restrict__ vals) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const double tx = (x[i] - g.xmin) * g.inv_cell;
-        const double ty = (y[i] - g.ymin) * g.inv_cell;
-        const double tz = (z[i] - g.zmin) * g.inv_cell;
+        double ox = g.xmin, oy = g.ymin, oz = g.zmin;
+        long long x0 = 0, nx = g.ncx, ny = g.ncy, nz = g.ncz;
+        if (sg.seg_of) {
+            const int s = sg.seg_of[i];
+            ox = sg.smin[3 * s];
+            oy = sg.smin[3 * s + 1];
+            oz = sg.smin[3 * s + 2];
+            x0 = sg.scol[4 * s];
+            nx = sg.scol[4 * s + 1];
+            ny = sg.scol[4 * s + 2];
+            nz = sg.scol[4 * s + 3];
+        }
+        const double tx = (x[i] - ox) * g.inv_cell;
+        const double ty = (y[i] - oy) * g.inv_cell;
+        const double tz = (z[i] - oz) * g.inv_cell;
         long long cx = (long long)floor(tx), cy = (long long)floor(ty), cz = (long long)floor(tz);
-        cx = min(max(cx, 0ll), g.ncx - 1);
-        cy = min(max(cy, 0ll), g.ncy - 1);
-        cz = min(max(cz, 0ll), g.ncz - 1);
-        uint64_t key = ((uint64_t)cx * (uint64_t)g.ncy + (uint64_t)cy) * (uint64_t)g.ncz + (uint64_t)cz;
+        cx = min(max(cx, 0ll), nx - 1);
+        cy = min(max(cy, 0ll), ny - 1);
+        cz = min(max(cz, 0ll), nz - 1);
+        uint64_t key = ((uint64_t)(x0 + cx) * (uint64_t)g.ncy + (uint64_t)cy) * (uint64_t)g.ncz + (uint64_t)cz;
         if (g.sb) {
             const int sx = min(3, max(0, (int)((tx - (double)cx) * 4.0)));
             const int sy = min(3, max(0, (int)((ty - (double)cy) * 4.0)));
@@ -189,7 +212,7 @@ __device__ __forceinline__ void decode_key(uint64_t key, const FofGeom &g, long 
 
 // Sorted records, run heads, union-find / label initialisation.
 __global__ void prep_kernel(const double *__restrict__ x, const double *__restrict__ y,
-                            const double *__restrict__ z, int n, FofGeom g,
+                            const double *__restrict__ z, int n, FofGeom g, SegGeom sg,
                             const uint64_t *__restrict__ keys, const int *__restrict__ idx,
                             float4 *__restrict__ rec, int *__restrict__ head, int *__restrict__ parent,
                             unsigned char *__restrict__ has, int *__restrict__ minidx) {
@@ -198,9 +221,17 @@ __global__ void prep_kernel(const double *__restrict__ x, const double *__restri
         long long cx, cy, cz;
         decode_key(key, g, cx, cy, cz);
         const int i = idx[k];
-        const double ox = g.xmin + (double)cx * g.cell;
-        const double oy = g.ymin + (double)cy * g.cell;
-        const double oz = g.zmin + (double)cz * g.cell;
+        double x0 = g.xmin, y0 = g.ymin, z0 = g.zmin;
+        if (sg.seg_of) {   // the segment's own origin and first column
+            const int s = sg.seg_of[i];
+            x0 = sg.smin[3 * s];
+            y0 = sg.smin[3 * s + 1];
+            z0 = sg.smin[3 * s + 2];
+            cx -= sg.scol[4 * s];
+        }
+        const double ox = x0 + (double)cx * g.cell;
+        const double oy = y0 + (double)cy * g.cell;
+        const double oz = z0 + (double)cz * g.cell;
         rec[k] = make_float4((float)((x[i] - ox) * g.inv_scale), (float)((y[i] - oy) * g.inv_scale),
                              (float)((z[i] - oz) * g.inv_scale), __int_as_float(i));
         head[k] = (k == 0 || (keys[k - 1] >> g.sb) != key) ? 1 : 0;
@@ -447,6 +478,208 @@ int bits_for(uint64_t v) {
     return b < 1 ? 1 : b;
 }
 
+// --- segmented FoF: per-segment origin and columns -------------------------------------
+__global__ void seg_fill_kernel(int nseg, const int64_t *__restrict__ off, int *__restrict__ seg_of) {
+    for (int s = blockIdx.x; s < nseg; s += gridDim.x)
+        for (int64_t i = off[s] + threadIdx.x; i < off[s + 1]; i += blockDim.x) seg_of[i] = s;
+}
+
+// One block per segment: its bounding box (sbox[6s..6s+5] = min xyz, max xyz), the largest
+// extent over all segments (as the bits of a non-negative double) and a non-finite flag.
+__global__ void __launch_bounds__(256) seg_bbox_kernel(int nseg, const int64_t *__restrict__ off,
+                                                       const double *__restrict__ x, const double *__restrict__ y,
+                                                       const double *__restrict__ z, double *__restrict__ sbox,
+                                                       unsigned long long *__restrict__ ext_bits, int *__restrict__ bad) {
+    __shared__ double sh[6][8];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int s = blockIdx.x; s < nseg; s += gridDim.x) {
+        double mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
+        bool nf = false;
+        for (int64_t i = off[s] + threadIdx.x; i < off[s + 1]; i += blockDim.x) {
+            const double v[3] = {x[i], y[i], z[i]};
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                nf |= !isfinite(v[d]);
+                mn[d] = fmin(mn[d], v[d]);
+                mx[d] = fmax(mx[d], v[d]);
+            }
+        }
+        if (__any_sync(0xffffffffu, nf) && lane == 0) atomicOr(bad, 1);
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            for (int o = 16; o > 0; o >>= 1) {
+                mn[d] = fmin(mn[d], __shfl_xor_sync(0xffffffffu, mn[d], o));
+                mx[d] = fmax(mx[d], __shfl_xor_sync(0xffffffffu, mx[d], o));
+            }
+            if (lane == 0) {
+                sh[d][w] = mn[d];
+                sh[3 + d][w] = mx[d];
+            }
+        }
+        __syncthreads();
+        if (threadIdx.x < 6) {
+            const int q = threadIdx.x;
+            double v = sh[q][0];
+            for (int k = 1; k < (int)(blockDim.x >> 5); ++k) v = q < 3 ? fmin(v, sh[q][k]) : fmax(v, sh[q][k]);
+            sh[q][0] = v;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double e = 0.0;
+#pragma unroll
+            for (int q = 0; q < 6; ++q) sbox[6 * (int64_t)s + q] = sh[q][0];
+            if (off[s + 1] > off[s])
+                e = fmax(sh[3][0] - sh[0][0], fmax(sh[4][0] - sh[1][0], sh[5][0] - sh[2][0]));
+            if (isfinite(e) && e > 0.0) atomicMax(ext_bits, (unsigned long long)__double_as_longlong(e));
+        }
+        __syncthreads();
+    }
+}
+
+// One block: columns of every segment at cell side 1/inv_cell, the first virtual x column of
+// each (exclusive prefix of columns + 1 gap), and out = {total columns, max y columns, max z
+// columns}.  An empty segment takes one column.
+__global__ void __launch_bounds__(1024) seg_cols_kernel(int nseg, const double *__restrict__ sbox, double inv_cell,
+                                                        double *__restrict__ smin, long long *__restrict__ scol,
+                                                        long long *__restrict__ out) {
+    __shared__ long long part[1024];
+    __shared__ long long my[1024], mz[1024];
+    const int t = threadIdx.x, nt = blockDim.x;
+    const int per = (nseg + nt - 1) / nt;
+    const int s0 = min(nseg, t * per), s1 = min(nseg, s0 + per);
+    long long sum = 0, ay = 1, az = 1;
+    for (int s = s0; s < s1; ++s) {
+        const double *b = sbox + 6 * (int64_t)s;
+        long long cx = 1, cy = 1, cz = 1;
+        if (b[3] >= b[0]) {   // non-empty
+            cx = (long long)floor((b[3] - b[0]) * inv_cell) + 1;
+            cy = (long long)floor((b[4] - b[1]) * inv_cell) + 1;
+            cz = (long long)floor((b[5] - b[2]) * inv_cell) + 1;
+            smin[3 * (int64_t)s] = b[0];
+            smin[3 * (int64_t)s + 1] = b[1];
+            smin[3 * (int64_t)s + 2] = b[2];
+        } else {
+            smin[3 * (int64_t)s] = smin[3 * (int64_t)s + 1] = smin[3 * (int64_t)s + 2] = 0.0;
+        }
+        scol[4 * (int64_t)s + 1] = cx;
+        scol[4 * (int64_t)s + 2] = cy;
+        scol[4 * (int64_t)s + 3] = cz;
+        sum += cx + 1;
+        ay = max(ay, cy);
+        az = max(az, cz);
+    }
+    part[t] = sum;
+    my[t] = ay;
+    mz[t] = az;
+    __syncthreads();
+    if (t == 0) {   // 1024 partial sums: a serial pass is cheap next to the per-segment work
+        long long run = 0, by = 1, bz = 1;
+        for (int k = 0; k < nt; ++k) {
+            const long long v = part[k];
+            part[k] = run;
+            run += v;
+            by = max(by, my[k]);
+            bz = max(bz, mz[k]);
+        }
+        out[0] = run;
+        out[1] = by;
+        out[2] = bz;
+    }
+    __syncthreads();
+    long long run = part[t];
+    for (int s = s0; s < s1; ++s) {
+        scol[4 * (int64_t)s] = run;
+        run += scol[4 * (int64_t)s + 1] + 1;
+    }
+}
+
+// Cell side, band and scale for linking length ll; ext = the largest extent (ll == 0 only).
+void set_scale(FofGeom &g, double ll, double ext) {
+    if (ll > 0.0) {
+        g.cell = ll * (1.0 + 0x1p-20);
+        g.inv_scale = 1.0 / ll;
+        g.lo = 1.0f - 1e-5f;
+        g.hi = 1.0f + 1e-5f;
+    } else {
+        // ll == 0 links coincident points only: every float candidate is re-tested exactly
+        g.cell = ext > 0.0 ? ext * 0x1p-16 : 1.0;
+        g.inv_scale = 1.0 / g.cell;
+        g.lo = -1.0f;
+        g.hi = 1e-6f;
+    }
+    g.inv_cell = 1.0 / g.cell;
+    g.cs = (float)(g.cell * g.inv_scale);
+    g.r2 = ll * ll;
+}
+
+// Keys, sort, cells, links and labels for a geometry whose cell grid is known.
+int fof_core(int n, const double *x, const double *y, const double *z, FofGeom g, SegGeom sg, int *labels,
+             int64_t *n_groups, cudaStream_t st) {
+    const long double cells = (long double)g.ncx * g.ncy * g.ncz;
+    if (cells > 4.0e18L)
+        return fail(HALMA_ERR_CAPACITY, "cell grid too large (%lld x %lld x %lld cells)", g.ncx, g.ncy, g.ncz);
+    const int cell_bits = bits_for((uint64_t)(g.ncx * g.ncy * g.ncz - 1));
+    g.sb = cell_bits <= 58 ? 6 : 0;
+    const int end_bit = cell_bits + g.sb;
+    const int sms = device_sm_count();
+
+    uint64_t hcap = 1;
+    while (hcap < 2ull * (uint64_t)n) hcap <<= 1;
+    const size_t sort_b = sort_pairs_u64_i32_bytes(n, end_bit);
+    const size_t scan_b = exclusive_sum_i32_bytes(n);
+    Layout M;
+    const size_t o_kin = M.add(8ull * n), o_kout = M.add(8ull * n);
+    const size_t o_vin = M.add(4ull * n), o_vout = M.add(4ull * n);
+    const size_t o_rec = M.add(16ull * n);
+    const size_t o_head = M.add(4ull * n), o_cpos = M.add(4ull * n);
+    const size_t o_par = M.add(4ull * n), o_has = M.add(1ull * n), o_root = M.add(4ull * n);
+    const size_t o_min = M.add(4ull * n);
+    const size_t o_cst = M.add(4ull * (n + 1)), o_ckey = M.add(8ull * n);
+    const size_t o_hk = M.add(8ull * hcap), o_hv = M.add(4ull * hcap);
+    const size_t o_flag = M.add(4ull * n), o_ipos = M.add(4ull * n);
+    const size_t o_ik0 = M.add(4ull * n), o_icell = M.add(4ull * n);
+    const size_t o_cnt = M.add(64);
+    const size_t o_tmp = M.add(std::max(sort_b, scan_b));
+    void *base = nullptr;
+    HALMA_TRY(workspace(M.total, &base, st));
+    auto *kin = at<uint64_t>(base, o_kin), *kout = at<uint64_t>(base, o_kout);
+    auto *vin = at<int>(base, o_vin), *vout = at<int>(base, o_vout);
+    auto *rec = at<float4>(base, o_rec);
+    auto *head = at<int>(base, o_head), *cpos = at<int>(base, o_cpos);
+    auto *parent = at<int>(base, o_par), *root = at<int>(base, o_root), *minidx = at<int>(base, o_min);
+    auto *has = at<unsigned char>(base, o_has);
+    auto *cst = at<int>(base, o_cst);
+    auto *ckey = at<uint64_t>(base, o_ckey);
+    auto *hk = at<uint64_t>(base, o_hk);
+    auto *hv = at<int>(base, o_hv);
+    auto *flag = at<int>(base, o_flag), *ipos = at<int>(base, o_ipos);
+    auto *ik0 = at<int>(base, o_ik0), *icell = at<int>(base, o_icell);
+    int *cnt = at<int>(base, o_cnt);   // [0] ncell [1] nitems [2] ngroups [3] err
+    void *tmp = at<void>(base, o_tmp);
+    const int g1 = std::min(sms * 8, grid_for(n, 256));
+
+    HALMA_CUDA(cudaMemsetAsync(cnt, 0, 64, st));
+    HALMA_CUDA(cudaMemsetAsync(hk, 0xff, 8ull * hcap, st));
+    HALMA_LAUNCH(keys_kernel, g1, 256, 0, st, x, y, z, n, g, sg, kin, vin);
+    HALMA_TRY(sort_pairs_u64_i32(tmp, sort_b, kin, kout, vin, vout, n, end_bit, st));
+    HALMA_LAUNCH(prep_kernel, g1, 256, 0, st, x, y, z, n, g, sg, kout, vout, rec, head, parent, has, minidx);
+    HALMA_TRY(exclusive_sum_i32(tmp, scan_b, head, cpos, n, st));
+    HALMA_LAUNCH(cells_kernel, g1, 256, 0, st, n, g.sb, kout, head, cpos, cst, ckey, hk, hv, hcap - 1, cnt + 0);
+    HALMA_LAUNCH(itemflag_kernel, g1, 256, 0, st, n, head, cpos, cst, flag);
+    HALMA_TRY(exclusive_sum_i32(tmp, scan_b, flag, ipos, n, st));
+    HALMA_LAUNCH(items_kernel, g1, 256, 0, st, n, head, cpos, flag, ipos, ik0, icell, cnt + 1);
+    HALMA_LAUNCH(link_kernel, sms * 8, 32 * kFofWarps, 0, st, rec, cst, ckey, ik0, icell, cnt + 1, hk, hv,
+                 hcap - 1, g, x, y, z, parent, has, cnt + 3);
+    HALMA_LAUNCH(root_kernel, g1, 256, 0, st, n, rec, parent, has, root, minidx, cnt + 3);
+    HALMA_LAUNCH(label_kernel, g1, 256, 0, st, n, rec, has, root, minidx, labels, cnt + 2);
+    int hc[4];
+    HALMA_CUDA(cudaMemcpyAsync(hc, cnt, sizeof(hc), cudaMemcpyDeviceToHost, st));
+    HALMA_CUDA(cudaStreamSynchronize(st));
+    if (hc[3]) return fail(HALMA_ERR_NOT_CONVERGED, "union-find iteration cap reached");
+    if (n_groups) *n_groups = hc[2];
+    return HALMA_OK;
+}
+
 }  // namespace
 
 // Full FoF on device arrays (no staging, no locking); used by halma_fof and the pipeline.
@@ -458,8 +691,8 @@ int fof_device(int n, const double *x, const double *y, const double *z, double 
     }
     const int sms = device_sm_count();
     const int gb = std::min(sms * 4, grid_for(n, 256));
-    // pass 1: bounding box
-    {
+    FofGeom g{};
+    {   // bounding box
         Layout L;
         const size_t o_part = L.add(sizeof(double) * 7 * gb);
         const size_t o_out = L.add(sizeof(double) * 8);
@@ -471,92 +704,63 @@ int fof_device(int n, const double *x, const double *y, const double *z, double 
         HALMA_CUDA(cudaMemcpyAsync(bb, at<double>(base, o_out), sizeof(bb), cudaMemcpyDeviceToHost, st));
         HALMA_CUDA(cudaStreamSynchronize(st));
         if (bb[6] != 0.0) return fail(HALMA_ERR_INVALID, "non-finite particle position");
-        FofGeom g{};
         g.xmin = bb[0];
         g.ymin = bb[1];
         g.zmin = bb[2];
         const double ext = std::max(bb[3] - bb[0], std::max(bb[4] - bb[1], bb[5] - bb[2]));
-        if (ll > 0.0) {
-            g.cell = ll * (1.0 + 0x1p-20);
-            g.inv_scale = 1.0 / ll;
-            g.lo = 1.0f - 1e-5f;
-            g.hi = 1.0f + 1e-5f;
-        } else {
-            // ll == 0 links coincident points only: every float candidate is re-tested exactly
-            g.cell = ext > 0.0 ? ext * 0x1p-16 : 1.0;
-            g.inv_scale = 1.0 / g.cell;
-            g.lo = -1.0f;
-            g.hi = 1e-6f;
-        }
-        g.inv_cell = 1.0 / g.cell;
-        g.cs = (float)(g.cell * g.inv_scale);
-        g.r2 = ll * ll;
+        set_scale(g, ll, ext);
         g.ncx = (long long)floor((bb[3] - bb[0]) * g.inv_cell) + 1;
         g.ncy = (long long)floor((bb[4] - bb[1]) * g.inv_cell) + 1;
         g.ncz = (long long)floor((bb[5] - bb[2]) * g.inv_cell) + 1;
-        const long double cells = (long double)g.ncx * g.ncy * g.ncz;
-        if (cells > 4.0e18L)
-            return fail(HALMA_ERR_CAPACITY, "cell grid too large (%lld x %lld x %lld cells)", g.ncx, g.ncy, g.ncz);
-        const int cell_bits = bits_for((uint64_t)(g.ncx * g.ncy * g.ncz - 1));
-        g.sb = cell_bits <= 58 ? 6 : 0;
-        const int end_bit = cell_bits + g.sb;
-
-        // pass 2: everything else, one workspace layout sized by n
-        uint64_t hcap = 1;
-        while (hcap < 2ull * (uint64_t)n) hcap <<= 1;
-        const size_t sort_b = sort_pairs_u64_i32_bytes(n, end_bit);
-        const size_t scan_b = exclusive_sum_i32_bytes(n);
-        Layout M;
-        const size_t o_kin = M.add(8ull * n), o_kout = M.add(8ull * n);
-        const size_t o_vin = M.add(4ull * n), o_vout = M.add(4ull * n);
-        const size_t o_rec = M.add(16ull * n);
-        const size_t o_head = M.add(4ull * n), o_cpos = M.add(4ull * n);
-        const size_t o_par = M.add(4ull * n), o_has = M.add(1ull * n), o_root = M.add(4ull * n);
-        const size_t o_min = M.add(4ull * n);
-        const size_t o_cst = M.add(4ull * (n + 1)), o_ckey = M.add(8ull * n);
-        const size_t o_hk = M.add(8ull * hcap), o_hv = M.add(4ull * hcap);
-        const size_t o_flag = M.add(4ull * n), o_ipos = M.add(4ull * n);
-        const size_t o_ik0 = M.add(4ull * n), o_icell = M.add(4ull * n);
-        const size_t o_cnt = M.add(64);
-        const size_t o_tmp = M.add(std::max(sort_b, scan_b));
-        HALMA_TRY(workspace(M.total, &base, st));
-        auto *kin = at<uint64_t>(base, o_kin), *kout = at<uint64_t>(base, o_kout);
-        auto *vin = at<int>(base, o_vin), *vout = at<int>(base, o_vout);
-        auto *rec = at<float4>(base, o_rec);
-        auto *head = at<int>(base, o_head), *cpos = at<int>(base, o_cpos);
-        auto *parent = at<int>(base, o_par), *root = at<int>(base, o_root), *minidx = at<int>(base, o_min);
-        auto *has = at<unsigned char>(base, o_has);
-        auto *cst = at<int>(base, o_cst);
-        auto *ckey = at<uint64_t>(base, o_ckey);
-        auto *hk = at<uint64_t>(base, o_hk);
-        auto *hv = at<int>(base, o_hv);
-        auto *flag = at<int>(base, o_flag), *ipos = at<int>(base, o_ipos);
-        auto *ik0 = at<int>(base, o_ik0), *icell = at<int>(base, o_icell);
-        int *cnt = at<int>(base, o_cnt);   // [0] ncell [1] nitems [2] ngroups [3] err
-        void *tmp = at<void>(base, o_tmp);
-        const int g1 = std::min(sms * 8, grid_for(n, 256));
-
-        HALMA_CUDA(cudaMemsetAsync(cnt, 0, 64, st));
-        HALMA_CUDA(cudaMemsetAsync(hk, 0xff, 8ull * hcap, st));
-        HALMA_LAUNCH(keys_kernel, g1, 256, 0, st, x, y, z, n, g, kin, vin);
-        HALMA_TRY(sort_pairs_u64_i32(tmp, sort_b, kin, kout, vin, vout, n, end_bit, st));
-        HALMA_LAUNCH(prep_kernel, g1, 256, 0, st, x, y, z, n, g, kout, vout, rec, head, parent, has, minidx);
-        HALMA_TRY(exclusive_sum_i32(tmp, scan_b, head, cpos, n, st));
-        HALMA_LAUNCH(cells_kernel, g1, 256, 0, st, n, g.sb, kout, head, cpos, cst, ckey, hk, hv, hcap - 1, cnt + 0);
-        HALMA_LAUNCH(itemflag_kernel, g1, 256, 0, st, n, head, cpos, cst, flag);
-        HALMA_TRY(exclusive_sum_i32(tmp, scan_b, flag, ipos, n, st));
-        HALMA_LAUNCH(items_kernel, g1, 256, 0, st, n, head, cpos, flag, ipos, ik0, icell, cnt + 1);
-        HALMA_LAUNCH(link_kernel, sms * 8, 32 * kFofWarps, 0, st, rec, cst, ckey, ik0, icell, cnt + 1, hk, hv,
-                     hcap - 1, g, x, y, z, parent, has, cnt + 3);
-        HALMA_LAUNCH(root_kernel, g1, 256, 0, st, n, rec, parent, has, root, minidx, cnt + 3);
-        HALMA_LAUNCH(label_kernel, g1, 256, 0, st, n, rec, has, root, minidx, labels, cnt + 2);
-        int hc[4];
-        HALMA_CUDA(cudaMemcpyAsync(hc, cnt, sizeof(hc), cudaMemcpyDeviceToHost, st));
-        HALMA_CUDA(cudaStreamSynchronize(st));
-        if (hc[3]) return fail(HALMA_ERR_NOT_CONVERGED, "union-find iteration cap reached");
-        if (n_groups) *n_groups = hc[2];
     }
-    return HALMA_OK;
+    return fof_core(n, x, y, z, g, SegGeom{}, labels, n_groups, st);
+}
+
+// FoF inside segments (particles of segment s are rows off[s] .. off[s+1], off on the
+// device): one launch sequence for all segments.  Labels are the smallest row index of each
+// component, -1 for rows without a friend in their own segment.  The per-segment geometry
+// lives in workspace slot 2, the linking scratch in slot 0.
+int fof_segmented_device(int n, int nseg, const int64_t *off, const double *x, const double *y, const double *z,
+                         double ll, int *labels, int64_t *n_groups, cudaStream_t st) {
+    if (n == 0 || nseg == 0) {
+        if (n_groups) *n_groups = 0;
+        return HALMA_OK;
+    }
+    Layout L;
+    const size_t o_seg = L.add(4ull * n), o_box = L.add(48ull * nseg), o_min = L.add(24ull * nseg);
+    const size_t o_col = L.add(32ull * nseg), o_cnt = L.add(64);
+    void *base = nullptr;
+    HALMA_TRY(workspace(L.total, &base, st, 2));
+    int *seg_of = at<int>(base, o_seg);
+    double *sbox = at<double>(base, o_box), *smin = at<double>(base, o_min);
+    long long *scol = at<long long>(base, o_col);
+    unsigned long long *ext_bits = at<unsigned long long>(base, o_cnt);
+    int *bad = at<int>(base, o_cnt + 8);
+    long long *cols = at<long long>(base, o_cnt + 16);
+    const int gs = std::min(nseg, device_sm_count() * 16);
+    HALMA_CUDA(cudaMemsetAsync(at<void>(base, o_cnt), 0, 64, st));
+    HALMA_LAUNCH(seg_fill_kernel, gs, 256, 0, st, nseg, off, seg_of);
+    HALMA_LAUNCH(seg_bbox_kernel, gs, 256, 0, st, nseg, off, x, y, z, sbox, ext_bits, bad);
+    long long hc[2];
+    HALMA_CUDA(cudaMemcpyAsync(hc, at<void>(base, o_cnt), 16, cudaMemcpyDeviceToHost, st));
+    HALMA_CUDA(cudaStreamSynchronize(st));
+    if ((int)hc[1] != 0) return fail(HALMA_ERR_INVALID, "non-finite particle position");
+    double ext;
+    memcpy(&ext, &hc[0], 8);
+    FofGeom g{};
+    set_scale(g, ll, ext);
+    HALMA_LAUNCH(seg_cols_kernel, 1, 1024, 0, st, nseg, sbox, g.inv_cell, smin, scol, cols);
+    long long cc[3];
+    HALMA_CUDA(cudaMemcpyAsync(cc, cols, sizeof(cc), cudaMemcpyDeviceToHost, st));
+    HALMA_CUDA(cudaStreamSynchronize(st));
+    g.ncx = cc[0];
+    g.ncy = cc[1];
+    g.ncz = cc[2];
+    SegGeom sg;
+    sg.seg_of = seg_of;
+    sg.smin = smin;
+    sg.scol = scol;
+    return fof_core(n, x, y, z, g, sg, labels, n_groups, st);
 }
 
 }  // namespace halma

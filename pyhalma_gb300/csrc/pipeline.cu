@@ -161,6 +161,7 @@ extern "C" int halma_profile_stats(double *out, int32_t cap) {
         v.push_back(q.pairs);
         v.push_back(q.ms);
         v.push_back(q.sym_pairs);
+        v.push_back(q.sym_ms);
     }
     if (out)
         for (int i = 0; i < cap && i < (int)v.size(); ++i) out[i] = v[i];

@@ -1284,11 +1284,13 @@ TileTable tile_table() { return tile_table_ref(); }
 
 int Profile::ensure_events(int k) {
     while ((int)ev0.size() < k) {
-        cudaEvent_t a, b;
+        cudaEvent_t a, b, c;
         HALMA_CUDA(cudaEventCreate(&a));
         HALMA_CUDA(cudaEventCreate(&b));
+        HALMA_CUDA(cudaEventCreate(&c));
         ev0.push_back(a);
         ev1.push_back(b);
+        evm.push_back(c);
     }
     return HALMA_OK;
 }
@@ -1447,6 +1449,7 @@ int unbind_device(int64_t n, int nh, const int64_t *d_off, const int64_t *h_off,
                 if (!inc)
                     HALMA_LAUNCH(ub_pair_sym_kernel, ygrid, 256, kSymSmem, rs, pkb[a], dpoff, dqoff, hs, nh, ystart,
                                  idesc, cnt, cnt + 4, eps2, part2);
+                if (profiling) HALMA_CUDA(cudaEventRecordWithFlags(prof.evm[it], rs, cudaEventRecordExternal));
                 HALMA_LAUNCH(ub_pair_kernel, pgrid, 256, 0, rs, pkb[a], rk, inc, dpoff, dqoff, hs, nh, istart, idesc,
                              cnt, cnt + 1, eps2, slice_len / 32, part2);
                 if (profiling) HALMA_CUDA(cudaEventRecordWithFlags(prof.ev1[it], rs, cudaEventRecordExternal));
@@ -1522,9 +1525,10 @@ int unbind_device(int64_t n, int nh, const int64_t *d_off, const int64_t *h_off,
             HALMA_CUDA(cudaStreamSynchronize(st));
             prof.passes.clear();
             for (int it = 0; it < p.max_iter; ++it) {
-                float ms = 0.f;
+                float ms = 0.f, sms = 0.f;
                 HALMA_CUDA(cudaEventElapsedTime(&ms, prof.ev0[it], prof.ev1[it]));
-                prof.passes.push_back({(double)hp[2 * it], (double)ms, (double)hp[2 * it + 1]});
+                HALMA_CUDA(cudaEventElapsedTime(&sms, prof.ev0[it], prof.evm[it]));
+                prof.passes.push_back({(double)hp[2 * it], (double)ms, (double)hp[2 * it + 1], (double)sms});
             }
         }
     } else {

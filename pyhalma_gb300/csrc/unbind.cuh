@@ -9,9 +9,10 @@ namespace halma {
 // the pair count of each pass, read back at the end of the call.
 struct Profile {
     bool enabled = false;
-    std::vector<cudaEvent_t> ev0, ev1;
+    std::vector<cudaEvent_t> ev0, evm, ev1;   // per pass: before, between and after the pair kernels
     struct Pass {
         double pairs, ms, sym_pairs;   // sym_pairs: the part done by the symmetric block kernel
+        double sym_ms;                 // time of the symmetric block kernel alone (0 when absent)
     };
     std::vector<Pass> passes;
     double fof_ms = 0, unbind_ms = 0;
@@ -34,6 +35,11 @@ int fof_device(int n, const double *x, const double *y, const double *z, double 
                int64_t *n_groups, cudaStream_t st);
 int fof_groups_device(int n, const int *labels, int minp, int64_t *offsets, int *members,
                       int64_t *n_groups, int64_t *n_members, cudaStream_t st);
+int fof_segmented_device(int n, int nseg, const int64_t *off, const double *x, const double *y, const double *z,
+                         double ll, int *labels, int64_t *n_groups, cudaStream_t st);
+int reductions_device(int64_t n, int nh, const int64_t *off, const double *x, const double *y, const double *z,
+                      const double *vx, const double *vy, const double *vz, const double *m,
+                      const unsigned char *mask, const double *about, double *out, cudaStream_t st);
 int unbind_device(int64_t n, int nh, const int64_t *d_off, const int64_t *h_off, const double *x,
                   const double *y, const double *z, const double *vx, const double *vy,
                   const double *vz, const double *m, const halma_unbind_params &p,

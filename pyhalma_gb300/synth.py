@@ -145,6 +145,57 @@ def plummer_snapshot(n_particles, n_spheres, *, seed=0, box_mpc=10.0, bg_frac=0.
                          sphere_counts=counts, sphere_centre_kpc=centres))
 
 
+def bridged_snapshot(n_pairs, n_single, *, seed=0, box_mpc=2.0, n_lo=300, n_hi=6000, sep_lo=4.0, sep_hi=8.0,
+                     bridge_step_kpc=1.1, bg_frac=0.05, particle_mass=1e6, bulk_sigma=200.0,
+                     bg_sigma=300.0) -> Snapshot:
+    """Pairs of Plummer spheres joined by a thin stream, for the substructure block.
+
+    Each pair: two spheres of log-uniform particle counts in [n_lo, n_hi] whose centres are
+    sep_lo..sep_hi times the sum of their scale radii apart, and a line of particles between
+    the centres every bridge_step_kpc (jittered by 0.05 kpc): the line links at a linking
+    length of 1.5 kpc but not at 0.75 kpc, so FoF merges the pair and the sub-FoF of the
+    substructure block separates it.  Plus n_single lone spheres and a uniform background.
+    Positions in Mpc; ``sphere`` is the generating sphere id, -2 for stream particles and
+    -1 for background.
+    """
+    rng = np.random.default_rng(seed)
+    box_kpc = box_mpc * 1e3
+    n_sph = 2 * n_pairs + n_single
+    counts = np.exp(rng.uniform(np.log(n_lo), np.log(n_hi), n_sph)).astype(np.int64)
+    masses = counts * particle_mass
+    a = plummer_scale_radius_kpc(masses)
+    margin = 0.1 * box_kpc
+    centres = rng.uniform(-box_kpc / 2 + margin, box_kpc / 2 - margin, (n_sph, 3))
+    first, second = np.arange(n_pairs), np.arange(n_pairs, 2 * n_pairs)
+    sep = rng.uniform(sep_lo, sep_hi, n_pairs) * (a[first] + a[second])
+    centres[second] = centres[first] + _unit_vectors(rng, n_pairs) * sep[:, None]
+    bulk = rng.normal(0.0, bulk_sigma, (n_sph, 3))
+    pos, vel, sid, _ = _spheres(rng, counts, masses, centres, bulk, 0.0)
+    streams_p, streams_v = [], []
+    for k in range(n_pairs):
+        c0, c1 = centres[first[k]], centres[second[k]]
+        steps = max(int(np.linalg.norm(c1 - c0) / bridge_step_kpc), 1)
+        t = (np.arange(1, steps) / steps)[:, None]
+        streams_p.append(c0 + t * (c1 - c0) + rng.normal(0.0, 0.05, (steps - 1, 3)))
+        streams_v.append(0.5 * (bulk[first[k]] + bulk[second[k]]) + rng.normal(0.0, 30.0, (steps - 1, 3)))
+    sp = np.concatenate(streams_p) if streams_p else np.zeros((0, 3))
+    sv = np.concatenate(streams_v) if streams_v else np.zeros((0, 3))
+    n_in = pos.shape[0] + sp.shape[0]
+    n_bg = int(round(bg_frac * n_in / (1.0 - bg_frac)))
+    bg_pos = rng.uniform(-box_kpc / 2, box_kpc / 2, (n_bg, 3))
+    bg_vel = rng.normal(0.0, bg_sigma, (n_bg, 3))
+    pos = np.concatenate([pos, sp, bg_pos]) / 1e3
+    vel = np.concatenate([vel, sv, bg_vel])
+    n = pos.shape[0]
+    sid = np.concatenate([sid, np.full(sp.shape[0], -2), np.full(n_bg, -1)])
+    return Snapshot(np.ascontiguousarray(pos[:, 0]), np.ascontiguousarray(pos[:, 1]),
+                    np.ascontiguousarray(pos[:, 2]), np.ascontiguousarray(vel[:, 0]),
+                    np.ascontiguousarray(vel[:, 1]), np.ascontiguousarray(vel[:, 2]),
+                    np.full(n, particle_mass), sid.astype(np.int64), np.zeros(n, dtype=bool), box_mpc,
+                    dict(seed=seed, n_pairs=n_pairs, n_single=n_single, stream_particles=int(sp.shape[0]),
+                         background=n_bg))
+
+
 def powerlaw_counts(rng, n_haloes, alpha=1.0, n_min=50, n_max=200_000):
     """Halo sizes with dN/dlogN ∝ N^-alpha on [n_min, n_max] (inverse CDF in log N)."""
     u = rng.uniform(0.0, 1.0, n_haloes)

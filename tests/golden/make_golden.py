@@ -22,7 +22,9 @@ Fixtures written to tests/golden/ (all seeds fixed):
   reference's KDTree links them (pins the pair predicate);
 * halo_props.npz  — reference reductions (halo_properties.py) on a few haloes;
 * rps.npz         — reference ``halo_gas.RPS`` / ``most_bound_particle`` outputs with
-  ``np.random.seed`` fixed before each call (pins the sub-sampling and energy logic).
+  ``np.random.seed`` fixed before each call (pins the sub-sampling and energy logic);
+* substructure.npz — the driver's inline substructure block (pyHALMA.py:703-766) exec'd
+  from the reference's own source on bridged snapshots (input and output groups stored).
 """
 from __future__ import annotations
 
@@ -236,13 +238,61 @@ def rps_cases(hg):
     print(f"  rps/most-bound: {n} cases")
 
 
+def _reference_block(refdir, start_marker, end_marker, extra_lines=1):
+    """Source of an inline block of pyHALMA.py (from the line holding start_marker to the line
+    holding end_marker, plus extra_lines), dedented so that it can be exec'd on its own."""
+    import textwrap
+    src = open(os.path.join(refdir, "pyHALMA.py")).read().split("\n")
+    i0 = next(i for i, line in enumerate(src) if start_marker in line)
+    i1 = next(i for i in range(i0, len(src)) if end_marker in src[i])
+    return textwrap.dedent("\n".join(src[i0:i1 + 1 + extra_lines])), i0 + 1, i1 + 1 + extra_lines
+
+
+def substructure_cases(fof, hp, refdir):
+    """The driver's substructure block (pyHALMA.py:703-766) run as written: its source is
+    exec'd with the reference's fof / halo_properties modules, the driver's good_groups and
+    the FoF groups of a bridged snapshot (after good_groups(MINP), as at pyHALMA.py:592)."""
+    block, b0, b1 = _reference_block(refdir, "if SUBSTRUCTURE_FLAG:", "Substructures / Cut FoF bridges")
+    gg, _, _ = _reference_block(refdir, "def good_groups(groups, minp):", "def good_groups(groups, minp):")
+    out = {"block_lines": np.array([b0, b1], dtype=np.int64)}
+    cases = [("one_level", 1, 0.0015, 25, 2.0, 0.0005, 0.75, 50),
+             ("three_levels", 2, 0.0015, 25, 2.0, 0.0001, 0.75, 50),
+             ("dec1p5", 3, 0.0015, 10, 1.5, 0.0004, 0.5, 30)]
+    for name, seed, LL, MINP_SUB, DEC_FACTOR, MIN_LL, DIST_FACTOR, MINP in cases:
+        s = synth.bridged_snapshot(8, 4, seed=seed, box_mpc=1.0, n_hi=2500)
+        groups = fof.friends_of_friends_serial(s.x, s.y, s.z, LL)
+        ns = {"np": np, "fof": fof, "halo_properties": hp, "tqdm": lambda it: it, "print": lambda *a, **k: None}
+        exec(gg, ns)
+        groups = np.array(groups, dtype=object)
+        groups = groups[ns["good_groups"](groups, MINP)]
+        groups_in = [list(g) for g in groups]
+        ns.update(dict(SUBSTRUCTURE_FLAG=True, PYFOF_FLAG=False, groups=groups, st_x=s.x, st_y=s.y, st_z=s.z,
+                       st_mass=s.mass, LL=LL, MINP_SUB=MINP_SUB, DEC_FACTOR=DEC_FACTOR, MIN_LL=MIN_LL,
+                       DIST_FACTOR=DIST_FACTOR, MINP=MINP))
+        exec(block, ns)
+        res = [list(map(int, g)) for g in ns["groups"]]
+        lens_in = np.array([len(g) for g in groups_in], dtype=np.int64)
+        lens_out = np.array([len(g) for g in res], dtype=np.int64)
+        out[f"{name}__x"], out[f"{name}__y"], out[f"{name}__z"], out[f"{name}__m"] = s.x, s.y, s.z, s.mass
+        out[f"{name}__params"] = np.array([LL, MINP_SUB, DEC_FACTOR, MIN_LL, DIST_FACTOR, MINP], dtype=np.float64)
+        out[f"{name}__in_off"] = np.concatenate(([0], np.cumsum(lens_in)))
+        out[f"{name}__in_mem"] = np.concatenate([np.asarray(g, dtype=np.int64) for g in groups_in])
+        out[f"{name}__out_off"] = np.concatenate(([0], np.cumsum(lens_out)))
+        out[f"{name}__out_mem"] = np.concatenate([np.asarray(g, dtype=np.int64) for g in res]) if res \
+            else np.zeros(0, dtype=np.int64)
+        out[f"{name}__counter_sub"] = np.int64(ns["counter_sub"])
+        print(f"  substructure {name}: n={s.n} groups in={len(groups_in)} out={len(res)} "
+              f"cut={ns['counter_sub']}")
+    np.savez_compressed(os.path.join(HERE, "substructure.npz"), **out)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default="/root/reference")
     ap.add_argument("--only", default="")
     args = ap.parse_args()
     fof, hg, hp = import_reference(args.reference)
-    todo = args.only.split(",") if args.only else ["fof", "config1", "pred", "props", "rps"]
+    todo = args.only.split(",") if args.only else ["fof", "config1", "pred", "props", "rps", "sub"]
     if "fof" in todo:
         fof_cases(fof)
     if "config1" in todo:
@@ -253,6 +303,8 @@ def main():
         halo_props(hp)
     if "rps" in todo:
         rps_cases(hg)
+    if "sub" in todo:
+        substructure_cases(fof, hp, args.reference)
 
 
 if __name__ == "__main__":

@@ -100,3 +100,30 @@ def test_tile_table_validation_and_roundtrip():
 def test_unbind_params_layout():
     # the C struct: 3 doubles + 4 int32
     assert ctypes.sizeof(_lib.UnbindParams) == 40
+
+
+def test_substructure_entry_points_reject_bad_arguments():
+    L = _lib.lib()
+    x = np.zeros(4)
+    lab = np.zeros(4, dtype=np.int32)
+    off = np.array([0, 4], dtype=np.int64)
+    seg = lambda o, ll=1.0: L.halma_fof_segmented(4, *[_lib.ptr(x)] * 3, len(o) - 1, _lib.ptr(o), ll,
+                                                  _lib.ptr(lab), None, None)
+    assert seg(off, -1.0) == _lib.ERR_INVALID                                   # linking length
+    assert seg(np.array([0, 3], dtype=np.int64)) == _lib.ERR_INVALID            # offsets do not reach n
+    assert seg(np.array([0, 3, 2, 4], dtype=np.int64)) == _lib.ERR_INVALID      # decreasing offsets
+    mem = np.arange(4, dtype=np.int32)
+    out_off = np.zeros(8, dtype=np.int64)
+    out_mem = np.zeros(4, dtype=np.int32)
+    n_out = ctypes.c_int64(0)
+
+    def split(p, o=off):
+        return L.halma_split_bridges(4, *[_lib.ptr(x)] * 4, len(o) - 1, _lib.ptr(o), _lib.ptr(mem), ctypes.byref(p),
+                                     ctypes.byref(n_out), 7, _lib.ptr(out_off), _lib.ptr(out_mem), None, None)
+    assert split(_lib.SubstructureParams(0.0, 2.0, 0.0005, 0.75, 25, 50)) == _lib.ERR_INVALID      # LL > 0
+    assert split(_lib.SubstructureParams(0.0015, 1.0, 0.0005, 0.75, 25, 50)) == _lib.ERR_INVALID   # DEC > 1
+    assert split(_lib.SubstructureParams(0.0015, 2.0, -1.0, 0.75, 25, 50)) == _lib.ERR_INVALID     # MIN_LL >= 0
+    assert split(_lib.SubstructureParams(0.0015, 2.0, 0.0005, 0.75, 25, 50),
+                 np.array([0, 5], dtype=np.int64)) == _lib.ERR_INVALID   # more members than particles
+    # the C struct: 4 doubles + 2 int32
+    assert ctypes.sizeof(_lib.SubstructureParams) == 40
