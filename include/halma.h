@@ -34,6 +34,8 @@
  *   halma_fof_segmented           <- the per-halo fof.friends_of_friends_serial calls of the
  *                                    substructure loop (pyHALMA.py:716-726), batched
  *   halma_split_bridges           <- the substructure block pyHALMA.py:703-766
+ *   halma_ball_gather             <- halo_gas.py:223-277 st_gas_dm_particles_inside range
+ *                                    queries (KDTree.query_ball_point, parallel_inside)
  */
 #ifndef HALMA_H
 #define HALMA_H
@@ -131,6 +133,25 @@ int halma_split_bridges(int64_t n, const double *x, const double *y, const doubl
                         const int32_t *group_members, const halma_substructure_params *params,
                         int64_t *n_out, int64_t out_capacity, int64_t *out_offsets,
                         int32_t *out_members, int64_t *n_cut, halma_stream_t stream);
+
+/* ------------------------------------------------------------------------------------ */
+/* Ball gather                                                                          */
+/* ------------------------------------------------------------------------------------ */
+/* The particles inside each of n_balls spheres (centre cx/cy/cz[s], radius[s] >= 0), all
+ * spheres in one call.  Replaces the per-halo range queries of
+ * python_scripts/halo_gas.py:223-277 st_gas_dm_particles_inside:
+ *   strict = 0: st_kdtree / dm_kdtree.query_ball_point([cx, cy, cz], R) (halo_gas.py:254,
+ *               268), ((dx*dx + dy*dy) + dz*dz) <= R*R in IEEE double;
+ *   strict = 1: parallel_inside(x, y, z, R, cx, cy, cz) (halo_gas.py:218-220, 237),
+ *               sqrt((dx*dx + dy*dy) + dz*dz) < R.
+ * Output as CSR: offsets[n_balls+1] (optional) and indices[offsets[s] .. offsets[s+1]) the
+ * particle indices inside sphere s, ascending (KDTree.query_ball_point returns the same set
+ * in tree order).  *n_found receives the total.  With indices == NULL only the counts are
+ * computed; HALMA_ERR_CAPACITY (with *n_found set) when the total exceeds capacity. */
+int halma_ball_gather(int64_t n, const double *x, const double *y, const double *z,
+                      int64_t n_balls, const double *cx, const double *cy, const double *cz,
+                      const double *radius, int32_t strict, int64_t *offsets, int32_t *indices,
+                      int64_t capacity, int64_t *n_found, halma_stream_t stream);
 
 /* ------------------------------------------------------------------------------------ */
 /* Brute-force potential                                                                */

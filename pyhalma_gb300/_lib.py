@@ -80,6 +80,7 @@ SIGNATURES = {
     "halma_fof_segmented": ([_I64, _P, _P, _P, _I64, _P, _F64, _P, _P, _P], ctypes.c_int),
     "halma_split_bridges": ([_I64, _P, _P, _P, _P, _I64, _P, _P, ctypes.POINTER(SubstructureParams), _P, _I64, _P,
                              _P, _P, _P], ctypes.c_int),
+    "halma_ball_gather": ([_I64, _P, _P, _P, _I64, _P, _P, _P, _P, _I32, _P, _P, _I64, _P, _P], ctypes.c_int),
     "halma_bf_potential_f32": ([_I64, _P, _P, _P, _P, _I64, _P, _P, _P, _P, _I32, _F64, _P], ctypes.c_int),
     "halma_potential_f64": ([_I64, _P, _P, _P, _P, _I64, _P, _P, _P, _F64, _I32, _I64, _P, _P], ctypes.c_int),
     "halma_potential_f32": ([_I64, _P, _P, _P, _P, _I64, _P, _P, _P, _F64, _I32, _I64, _P, _P], ctypes.c_int),

@@ -682,6 +682,22 @@ int fof_core(int n, const double *x, const double *y, const double *z, FofGeom g
 
 }  // namespace
 
+// Bounding box of n > 0 device points, returned on the host: min x, y, z, max x, y, z, and a
+// non-zero seventh value if any coordinate is not finite.  Uses workspace slot 0.
+int bbox_device(int n, const double *x, const double *y, const double *z, double bb[7], cudaStream_t st) {
+    const int gb = std::min(device_sm_count() * 4, grid_for(n, 256));
+    Layout L;
+    const size_t o_part = L.add(sizeof(double) * 7 * gb);
+    const size_t o_out = L.add(sizeof(double) * 8);
+    void *base = nullptr;
+    HALMA_TRY(workspace(L.total, &base, st));
+    HALMA_LAUNCH(bbox_partial_kernel, gb, 256, 0, st, x, y, z, n, at<double>(base, o_part));
+    HALMA_LAUNCH(bbox_final_kernel, 1, 32, 0, st, at<double>(base, o_part), gb, at<double>(base, o_out));
+    HALMA_CUDA(cudaMemcpyAsync(bb, at<double>(base, o_out), 7 * sizeof(double), cudaMemcpyDeviceToHost, st));
+    HALMA_CUDA(cudaStreamSynchronize(st));
+    return HALMA_OK;
+}
+
 // Full FoF on device arrays (no staging, no locking); used by halma_fof and the pipeline.
 int fof_device(int n, const double *x, const double *y, const double *z, double ll, int *labels,
                int64_t *n_groups, cudaStream_t st) {
@@ -689,20 +705,10 @@ int fof_device(int n, const double *x, const double *y, const double *z, double 
         if (n_groups) *n_groups = 0;
         return HALMA_OK;
     }
-    const int sms = device_sm_count();
-    const int gb = std::min(sms * 4, grid_for(n, 256));
     FofGeom g{};
-    {   // bounding box
-        Layout L;
-        const size_t o_part = L.add(sizeof(double) * 7 * gb);
-        const size_t o_out = L.add(sizeof(double) * 8);
-        void *base = nullptr;
-        HALMA_TRY(workspace(L.total, &base, st));
-        HALMA_LAUNCH(bbox_partial_kernel, gb, 256, 0, st, x, y, z, n, at<double>(base, o_part));
-        HALMA_LAUNCH(bbox_final_kernel, 1, 32, 0, st, at<double>(base, o_part), gb, at<double>(base, o_out));
+    {
         double bb[7];
-        HALMA_CUDA(cudaMemcpyAsync(bb, at<double>(base, o_out), sizeof(bb), cudaMemcpyDeviceToHost, st));
-        HALMA_CUDA(cudaStreamSynchronize(st));
+        HALMA_TRY(bbox_device(n, x, y, z, bb, st));
         if (bb[6] != 0.0) return fail(HALMA_ERR_INVALID, "non-finite particle position");
         g.xmin = bb[0];
         g.ymin = bb[1];

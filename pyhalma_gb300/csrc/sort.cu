@@ -32,6 +32,29 @@ int sort_pairs_u32_i32(void *tmp, size_t tmp_bytes, const uint32_t *kin, uint32_
     return HALMA_OK;
 }
 
+size_t sort_keys_u64_bytes(int n, int end_bit) {
+    size_t b = 0;
+    cub::DeviceRadixSort::SortKeys(nullptr, b, (const uint64_t *)nullptr, (uint64_t *)nullptr, n, 0, end_bit);
+    return b;
+}
+
+int sort_keys_u64(void *tmp, size_t tmp_bytes, const uint64_t *kin, uint64_t *kout, int n, int end_bit,
+                  cudaStream_t s) {
+    HALMA_CUDA(cub::DeviceRadixSort::SortKeys(tmp, tmp_bytes, kin, kout, n, 0, end_bit, s));
+    return HALMA_OK;
+}
+
+size_t exclusive_sum_i64_bytes(int n) {
+    size_t b = 0;
+    cub::DeviceScan::ExclusiveSum(nullptr, b, (const int64_t *)nullptr, (int64_t *)nullptr, n);
+    return b;
+}
+
+int exclusive_sum_i64(void *tmp, size_t tmp_bytes, const int64_t *in, int64_t *out, int n, cudaStream_t s) {
+    HALMA_CUDA(cub::DeviceScan::ExclusiveSum(tmp, tmp_bytes, in, out, n, s));
+    return HALMA_OK;
+}
+
 size_t exclusive_sum_i32_bytes(int n) {
     size_t b = 0;
     cub::DeviceScan::ExclusiveSum(nullptr, b, (const int32_t *)nullptr, (int32_t *)nullptr, n);

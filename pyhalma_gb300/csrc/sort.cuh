@@ -11,6 +11,11 @@ int sort_pairs_u64_i32(void *tmp, size_t tmp_bytes, const uint64_t *kin, uint64_
 size_t sort_pairs_u32_i32_bytes(int n);
 int sort_pairs_u32_i32(void *tmp, size_t tmp_bytes, const uint32_t *kin, uint32_t *kout,
                        const int32_t *vin, int32_t *vout, int n, int end_bit, cudaStream_t s);
+size_t sort_keys_u64_bytes(int n, int end_bit);
+int sort_keys_u64(void *tmp, size_t tmp_bytes, const uint64_t *kin, uint64_t *kout, int n, int end_bit,
+                  cudaStream_t s);
+size_t exclusive_sum_i64_bytes(int n);
+int exclusive_sum_i64(void *tmp, size_t tmp_bytes, const int64_t *in, int64_t *out, int n, cudaStream_t s);
 size_t exclusive_sum_i32_bytes(int n);
 int exclusive_sum_i32(void *tmp, size_t tmp_bytes, const int32_t *in, int32_t *out, int n,
                       cudaStream_t s);

@@ -31,6 +31,7 @@ struct TileTable {
 };
 TileTable tile_table();
 
+int bbox_device(int n, const double *x, const double *y, const double *z, double bb[7], cudaStream_t st);
 int fof_device(int n, const double *x, const double *y, const double *z, double ll, int *labels,
                int64_t *n_groups, cudaStream_t st);
 int fof_groups_device(int n, const int *labels, int minp, int64_t *offsets, int *members,

@@ -5,6 +5,8 @@
 * ``serial_brute_force_binding_energy_fortran(...)``          halo_gas.py:191-215
 * ``RPS(...)``                                                halo_gas.py:285-492
 * ``most_bound_particle(...)``                                halo_gas.py:498-634
+* ``parallel_inside(...)``, ``st_gas_dm_particles_inside(...)`` halo_gas.py:218-277 (ball
+  gather on the GPU; ``balls_inside`` does many haloes' spheres in one call)
 
 The f2py kernel particle.particle.brute_force_binding_energy (particle_subroutines.f90:466-514)
 is replaced by ``halma_bf_potential_f32``.  Like the wrapper it casts every input to float32
@@ -155,3 +157,95 @@ def most_bound_particle(gas_x, gas_y, gas_z, gas_mass, dm_x, dm_y, dm_z, dm_mass
         phi += t
     k = np.argmin(-phi)
     return st_x[k], st_y[k], st_z[k], st_oripa[k]
+
+
+# ---------------------------------------------------------------------------------------
+# ball gather (halo_gas.py:218-277)
+# ---------------------------------------------------------------------------------------
+def balls_inside(x, y, z, cx, cy, cz, R, strict=False):
+    """Particles inside many spheres at once (C ABI ``halma_ball_gather``).
+
+    cx, cy, cz, R: one entry per sphere.  Returns CSR (offsets int64 [K+1], indices int32),
+    each sphere's indices ascending.  strict=False: ((dx*dx + dy*dy) + dz*dz) <= R*R, the
+    pair rule of ``KDTree.query_ball_point``; strict=True: sqrt(...) < R, ``parallel_inside``.
+    Host NumPy arrays or CUDA torch tensors (outputs on the same side).
+    """
+    import ctypes
+    if _lib._is_torch(x):
+        n = int(x.shape[0])
+        px, py, pz = x, y, z
+        b = tuple(a.to(dtype=x.dtype).reshape(-1).contiguous() for a in (cx, cy, cz, R))
+    else:
+        px, py, pz = (_lib.as_host(a, np.float64) for a in (x, y, z))
+        n = px.shape[0]
+        b = tuple(np.atleast_1d(_lib.as_host(a, np.float64)) for a in (cx, cy, cz, R))
+    k = int(b[0].shape[0])
+    if any(int(a.shape[0]) != k for a in b):
+        raise ValueError("cx, cy, cz and R must have the same length")
+    offsets = _lib.like(px, (k + 1,), np.int64)
+    found = ctypes.c_int64(0)
+    L = _lib.lib()
+    st = L.halma_ball_gather(n, _lib.ptr(px), _lib.ptr(py), _lib.ptr(pz), k, *[_lib.ptr(a) for a in b],
+                             1 if strict else 0, _lib.ptr(offsets), None, 0, ctypes.byref(found),
+                             _lib.stream_of(px))
+    _lib.check(st, "halma_ball_gather")
+    total = int(found.value)
+    indices = _lib.like(px, (max(total, 1),), np.int32)
+    if total > 0:
+        st = L.halma_ball_gather(n, _lib.ptr(px), _lib.ptr(py), _lib.ptr(pz), k, *[_lib.ptr(a) for a in b],
+                                 1 if strict else 0, _lib.ptr(offsets), _lib.ptr(indices), total,
+                                 ctypes.byref(found), _lib.stream_of(px))
+        _lib.check(st, "halma_ball_gather")
+    return offsets, indices[:total]
+
+
+def query_ball_point(x, y, z, centre, R):
+    """``KDTree(np.array((x, y, z)).T).query_ball_point(centre, R)`` for one centre: the
+    indices within R (inclusive), ascending (the KDTree returns the same set in tree order)."""
+    _, idx = balls_inside(x, y, z, [centre[0]], [centre[1]], [centre[2]], [R])
+    return idx
+
+
+def parallel_inside(array_x, array_y, array_z, R, cx, cy, cz):
+    """halo_gas.py:218-220: boolean mask sqrt((x-cx)**2 + (y-cy)**2 + (z-cz)**2) < R."""
+    n = len(array_x)
+    _, idx = balls_inside(array_x, array_y, array_z, [cx], [cy], [cz], [R], strict=True)
+    mask = np.zeros(n, dtype=bool)
+    mask[np.asarray(idx)] = True
+    return mask
+
+
+MASS_TO_SUN = 1.0   # masclet_framework units.mass_to_sun: set it when masses come in MASCLET units
+
+
+def st_gas_dm_particles_inside(rete, L, ncoarse, grid_data, gas_data, masclet_dm_data, masclet_st_data,
+                               st_kdtree, dm_kdtree, cx, cy, cz, R, rho_B):
+    """halo_gas.py:223-277 with the particle side on the GPU.
+
+    ``gas_data`` is the gas already turned into particles — the tuple (gas_x, gas_y, gas_z,
+    gas_vx, gas_vy, gas_vz, gas_mass, gas_temp) that ``AMRgrid_to_particles`` (halo_gas.py:
+    56-141) returns; that conversion reads MASCLET AMR grids and is not part of this package,
+    so ``L``, ``ncoarse``, ``grid_data`` and ``rho_B`` are accepted and unused.  The KD-trees
+    are replaced by the GPU ball gather (``st_kdtree`` / ``dm_kdtree`` are unused), so the DM
+    and star selections come back in ascending index order instead of tree order.  Returns the
+    reference's 17-tuple.
+    """
+    if grid_data is not None:
+        raise NotImplementedError("AMR grid to particle conversion needs MASCLET grids; pass the gas as "
+                                  "particles in gas_data and grid_data=None")
+    gas_x, gas_y, gas_z, gas_vx, gas_vy, gas_vz, gas_mass, gas_temp = (np.asarray(a) for a in gas_data)
+    inside = parallel_inside(gas_x, gas_y, gas_z, R, cx, cy, cz)
+    gas_x, gas_y, gas_z = gas_x[inside], gas_y[inside], gas_z[inside]
+    gas_vx, gas_vy, gas_vz = gas_vx[inside], gas_vy[inside], gas_vz[inside]
+    gas_mass, gas_temp = gas_mass[inside], gas_temp[inside]
+    gas_mass = gas_mass * rete ** 3      # comoving to physical volume (halo_gas.py:247)
+    dm_x, dm_y, dm_z = (np.asarray(masclet_dm_data[k]) for k in range(3))
+    dm_mass = np.asarray(masclet_dm_data[3]) * MASS_TO_SUN   # halo_gas.py:253
+    sel = np.asarray(query_ball_point(dm_x, dm_y, dm_z, (cx, cy, cz), R))
+    dm_x, dm_y, dm_z, dm_mass = dm_x[sel], dm_y[sel], dm_z[sel], dm_mass[sel]
+    st_x, st_y, st_z = (np.asarray(masclet_st_data[k]) for k in range(3))
+    st_mass, st_oripa = np.asarray(masclet_st_data[6]) * MASS_TO_SUN, np.asarray(masclet_st_data[9])
+    sel = np.asarray(query_ball_point(st_x, st_y, st_z, (cx, cy, cz), R))
+    st_x, st_y, st_z, st_mass, st_oripa = st_x[sel], st_y[sel], st_z[sel], st_mass[sel], st_oripa[sel]
+    return (gas_x, gas_y, gas_z, gas_vx, gas_vy, gas_vz, gas_mass, gas_temp,
+            dm_x, dm_y, dm_z, dm_mass, st_x, st_y, st_z, st_mass, st_oripa)

@@ -24,7 +24,11 @@ Fixtures written to tests/golden/ (all seeds fixed):
 * rps.npz         — reference ``halo_gas.RPS`` / ``most_bound_particle`` outputs with
   ``np.random.seed`` fixed before each call (pins the sub-sampling and energy logic);
 * substructure.npz — the driver's inline substructure block (pyHALMA.py:703-766) exec'd
-  from the reference's own source on bridged snapshots (input and output groups stored).
+  from the reference's own source on bridged snapshots (input and output groups stored);
+* ball.npz        — reference ``halo_gas.st_gas_dm_particles_inside`` with its MASCLET AMR
+  conversion replaced by a pass-through of gas particles (inputs and the 17 outputs stored);
+* psc.npz         — the driver's phase-space cleaning block (pyHALMA.py:774-877) exec'd from
+  the reference's own source on FoF groups of contaminated Plummer snapshots.
 """
 from __future__ import annotations
 
@@ -286,13 +290,97 @@ def substructure_cases(fof, hp, refdir):
     np.savez_compressed(os.path.join(HERE, "substructure.npz"), **out)
 
 
+def ball_cases(hg):
+    """The reference's st_gas_dm_particles_inside (halo_gas.py:223-277) run as written, with its
+    AMR-grid conversion (halo_gas.py:56-141, needs MASCLET grids) replaced by a pass-through of
+    gas particles; the KD-trees are built as the driver builds them (pyHALMA.py:543-545)."""
+    from scipy.spatial import KDTree
+    out = {}
+    orig = hg.AMRgrid_to_particles
+    try:
+        for k, (ngas, ndm, nst) in enumerate([(3000, 8000, 6000), (1500, 4000, 10000)]):
+            rng = np.random.default_rng(60 + k)
+            c = rng.uniform(-1, 1, 3)
+            gas = [c[q] + rng.normal(0, 0.01, ngas) for q in range(3)] + \
+                  [rng.normal(0, 100, ngas) for _ in range(3)] + [rng.lognormal(11, 1, ngas), rng.uniform(1e3, 1e6, ngas)]
+            dm = [c[q] + rng.normal(0, 0.02, ndm) for q in range(3)] + [rng.uniform(1e6, 1e7, ndm)]
+            st = [c[q] + rng.normal(0, 0.008, nst) for q in range(3)]
+            st_data = st + [np.zeros(nst) for _ in range(3)] + [rng.uniform(1e5, 1e6, nst),
+                                                                        np.zeros(nst), np.zeros(nst),
+                                                                        np.arange(nst) + 10_000 * k]
+            st_tree = KDTree(np.array((st[0], st[1], st[2])).T)
+            dm_tree = KDTree(np.array((dm[0], dm[1], dm[2])).T)
+            hg.AMRgrid_to_particles = lambda L, ncoarse, grid_data, gas_data, R, cx, cy, cz, rho_B: \
+                tuple(np.copy(a) for a in gas_data)
+            for j, R in enumerate((0.004, 0.015)):
+                res = hg.st_gas_dm_particles_inside(0.5, 40.0, 128, None, gas, dm, st_data, st_tree, dm_tree,
+                                                    c[0], c[1], c[2], R, 1.0)
+                for q, a in enumerate(res):
+                    out[f"c{k}r{j}_out{q}"] = np.asarray(a)
+                out[f"c{k}r{j}_R"] = np.float64(R)
+            for q, a in enumerate(gas):
+                out[f"c{k}_gas{q}"] = a
+            for q, a in enumerate(dm):
+                out[f"c{k}_dm{q}"] = a
+            for q, a in enumerate(st_data):
+                out[f"c{k}_st{q}"] = a
+            out[f"c{k}_centre"] = c
+            print(f"  ball gather case {k}: gas={ngas} dm={ndm} stars={nst}")
+    finally:
+        hg.AMRgrid_to_particles = orig
+    np.savez_compressed(os.path.join(HERE, "ball.npz"), ncase=np.int64(2), rete=np.float64(0.5), **out)
+
+
+def psc_cases(fof, hp, refdir):
+    """The driver's phase-space cleaning block (pyHALMA.py:774-877: calc_cell / clean_cell per
+    group, the reset for small groups, the MINP cut and the sort by size) run as written on the
+    FoF groups of contaminated Plummer snapshots."""
+    block, b0, b1 = _reference_block(refdir, "print('---> Phase-space cleaning begins <---')",
+                                     "which_cell_list_z = which_cell_list_z[sort_indices]", 0)
+    gg, _, _ = _reference_block(refdir, "def good_groups(groups, minp):", "def good_groups(groups, minp):")
+    out = {"block_lines": np.array([b0, b1], dtype=np.int64)}
+    cases = [("psc_on", 31, 0.0015, 1.0, 3.0, True, 50), ("psc_q2", 32, 0.0015, 2.0, 2.0, True, 40),
+             ("psc_aggr", 34, 0.0015, 3.0, 1.0, True, 30), ("psc_off", 33, 0.0015, 1.0, 3.0, False, 50)]
+    for name, seed, LL, Q_FIL, SIG_FIL, PSC_FLAG, MINP in cases:
+        s = synth.plummer_snapshot(12_000, 8, seed=seed, box_mpc=0.5, contaminant_frac=0.15, m_hi=3e10)
+        groups = fof.friends_of_friends_serial(s.x, s.y, s.z, LL)
+        ns = {"np": np, "halo_properties": hp, "tqdm": lambda it: it, "print": lambda *a, **k: None}
+        exec(gg, ns)
+        groups = np.array(groups, dtype=object)
+        groups = groups[ns["good_groups"](groups, MINP)]
+        groups_in = [list(g) for g in groups]
+        ns.update(dict(groups=groups, st_x=s.x, st_y=s.y, st_z=s.z, st_vx=s.vx, st_vy=s.vy, st_vz=s.vz,
+                       st_mass=s.mass, LL=LL, Q_FIL=Q_FIL, SIG_FIL=SIG_FIL, PSC_FLAG=PSC_FLAG, MINP=MINP))
+        exec(block, ns)
+        for k in ("x", "y", "z", "vx", "vy", "vz"):
+            out[f"{name}__{k}"] = getattr(s, k)
+        out[f"{name}__m"] = s.mass
+        out[f"{name}__params"] = np.array([LL, Q_FIL, SIG_FIL, float(PSC_FLAG), MINP], dtype=np.float64)
+        lens = [len(g) for g in groups_in]
+        out[f"{name}__in_off"] = np.concatenate(([0], np.cumsum(lens))).astype(np.int64)
+        out[f"{name}__in_mem"] = np.concatenate([np.asarray(g, dtype=np.int64) for g in groups_in])
+        ng = ns["new_groups"]
+        out[f"{name}__out_off"] = np.concatenate(([0], np.cumsum([len(g) for g in ng]))).astype(np.int64)
+        out[f"{name}__out_mem"] = np.concatenate([np.asarray(g, dtype=np.int64) for g in ng])
+        for k in ("center_x", "center_y", "center_z", "masses", "rmax", "num_particles", "num_cells"):
+            out[f"{name}__{k}"] = np.asarray(ns[k])
+        for a in "xyz":
+            wl = ns[f"which_cell_list_{a}"]
+            out[f"{name}__which_{a}_off"] = np.concatenate(([0], np.cumsum([len(w) for w in wl]))).astype(np.int64)
+            out[f"{name}__which_{a}"] = np.concatenate([np.asarray(w, dtype=np.int64) for w in wl])
+        print(f"  phase-space cleaning {name}: n={s.n} groups in={len(groups_in)} out={len(ng)} "
+              f"particles {sum(lens)} -> {int(np.sum(ns['num_particles']))}")
+    np.savez_compressed(os.path.join(HERE, "psc.npz"), **out)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default="/root/reference")
     ap.add_argument("--only", default="")
     args = ap.parse_args()
     fof, hg, hp = import_reference(args.reference)
-    todo = args.only.split(",") if args.only else ["fof", "config1", "pred", "props", "rps", "sub"]
+    todo = args.only.split(",") if args.only else ["fof", "config1", "pred", "props", "rps", "sub", "ball",
+                                                    "psc"]
     if "fof" in todo:
         fof_cases(fof)
     if "config1" in todo:
@@ -305,6 +393,10 @@ def main():
         rps_cases(hg)
     if "sub" in todo:
         substructure_cases(fof, hp, args.reference)
+    if "ball" in todo:
+        ball_cases(hg)
+    if "psc" in todo:
+        psc_cases(fof, hp, args.reference)
 
 
 if __name__ == "__main__":

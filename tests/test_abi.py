@@ -127,3 +127,17 @@ def test_substructure_entry_points_reject_bad_arguments():
                  np.array([0, 5], dtype=np.int64)) == _lib.ERR_INVALID   # more members than particles
     # the C struct: 4 doubles + 2 int32
     assert ctypes.sizeof(_lib.SubstructureParams) == 40
+
+
+def test_ball_gather_rejects_bad_arguments():
+    L = _lib.lib()
+    x = np.zeros(4)
+    c = np.zeros(2)
+    n_found = ctypes.c_int64(0)
+    g = lambda strict=0, nf=ctypes.byref(n_found), nb=2: L.halma_ball_gather(
+        4, *[_lib.ptr(x)] * 3, nb, *[_lib.ptr(c)] * 4, strict, None, None, 0, nf, None)
+    assert g(strict=2) == _lib.ERR_INVALID
+    assert g(nf=None) == _lib.ERR_INVALID
+    assert g(nb=-1) == _lib.ERR_INVALID
+    assert L.halma_ball_gather(4, None, None, None, 2, *[_lib.ptr(c)] * 4, 0, None, None, 0, ctypes.byref(n_found),
+                               None) == _lib.ERR_INVALID
