@@ -533,13 +533,200 @@ def run_full(args):
     return 0
 
 
+def _timed(fn, reps=3, warmup=1):
+    """Mean CUDA-event milliseconds of fn() on the current stream (after warm-up)."""
+    import torch
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    ms = []
+    for _ in range(reps):
+        e0, e1 = _events()
+        e0.record()
+        fn()
+        e1.record()
+        e1.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    return statistics.mean(ms)
+
+
+def _groups_csr(groups):
+    off = np.zeros(len(groups) + 1, dtype=np.int64)
+    np.cumsum([len(g) for g in groups], out=off[1:])
+    mem = np.concatenate([np.asarray(g, dtype=np.int32) for g in groups]) if off[-1] else np.zeros(0, np.int32)
+    return off, mem
+
+
+def _cpu_sample(groups, every, fn):
+    """Runs fn(group) on every `every`-th group; returns (seconds, particles of the sample)."""
+    t0 = time.perf_counter()
+    npart = 0
+    for g in groups[::every]:
+        fn(g)
+        npart += len(g)
+    return time.perf_counter() - t0, npart
+
+
+def run_substructure(args):
+    """Substructure identification (pyHALMA.py:703-766) of the FoF groups of a bridged
+    snapshot: 1000 sphere pairs joined by streams + 1000 lone spheres in a 20 Mpc box."""
+    import ctypes
+    import torch
+    import oracle
+    from oracle import fof_kdtree
+    from oracle.reductions import center_of_mass, half_mass_radius
+    from pyhalma_gb300 import _lib, fof, substructure, synth
+    dev = torch.device("cuda", 0)
+    s = synth.bridged_snapshot(1000, 1000, seed=5, box_mpc=20.0)
+    off, mem = fof.fof_groups(fof.fof_labels(s.x, s.y, s.z, 0.0015), 50)
+    groups = [mem[off[g]:off[g + 1]] for g in range(len(off) - 1)]
+    prm = (0.0015, 25, 2.0, 0.0005, 0.75, 50)
+    T = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+    dx, dy, dz, dm, doff, dmem = T(s.x), T(s.y), T(s.z), T(s.mass), T(off), T(mem)
+    cap = len(groups) + len(mem) // 25 + 1
+    oo, om = torch.zeros(cap + 1, dtype=torch.int64, device=dev), torch.zeros(max(len(mem), 1), dtype=torch.int32,
+                                                                                  device=dev)
+    P = _lib.SubstructureParams(*prm[:1], prm[2], prm[3], prm[4], prm[1], prm[5])
+    n_out, n_cut = ctypes.c_int64(0), ctypes.c_int64(0)
+
+    def gpu():
+        st = _lib.lib().halma_split_bridges(s.n, *[_lib.ptr(a) for a in (dx, dy, dz, dm)], len(groups),
+                                            _lib.ptr(doff), _lib.ptr(dmem), ctypes.byref(P), ctypes.byref(n_out),
+                                            cap, _lib.ptr(oo), _lib.ptr(om), ctypes.byref(n_cut),
+                                            _lib.stream_of(dx))
+        _lib.check(st, "halma_split_bridges")
+    ms = _timed(gpu, reps=max(args.steps, 3), warmup=args.warmup)
+    t0 = time.perf_counter()
+    out, cut = substructure.identify_substructure(groups, s.x, s.y, s.z, s.mass, *prm)
+    e2e = time.perf_counter() - t0
+    # CPU: the reference's per-group loop with its KD-tree FoF on a sample of the groups
+
+    def one(pl):
+        pl = np.asarray(pl)
+        cx, cy, cz, M = center_of_mass(pl, s.x, s.y, s.z, s.mass)
+        half_mass_radius(cx, cy, cz, M, pl, s.x, s.y, s.z, s.mass)
+        fof_kdtree.friends_of_friends_serial(s.x[pl], s.y[pl], s.z[pl], 0.00075)
+    every = max(1, len(groups) // 40)
+    t_cpu, n_cpu = _cpu_sample(groups, every, one)
+    nm = len(mem)
+    print(json.dumps({"workload": "substructure-bridged-1000pairs-1000single", "particles_in_groups": nm,
+                      "groups_in": len(groups), "groups_out": int(n_out.value), "cut": int(n_cut.value),
+                      "gpu_ms": ms, "gpu_particles_per_s": nm / (ms * 1e-3),
+                      "e2e_s_host_arrays": e2e, "e2e_particles_per_s": nm / e2e,
+                      "cpu_baseline": {"value": n_cpu / t_cpu, "unit": "particles/s", "cores": 1, "kind": "port",
+                                       "sample": f"every {every}th group ({n_cpu} particles): centre of mass, "
+                                                 f"half-mass radius and the KD-tree FoF at LL/2 per group"},
+                      "speedup_vs_cpu": (nm / (ms * 1e-3)) / (n_cpu / t_cpu)}), flush=True)
+    return 0
+
+
+def run_gather(args):
+    """Ball gather of the gas / potential set-up (halo_gas.py:223-277) on the 2e6-particle
+    snapshot: spheres of 2 r_half (FACTOR_R12_POT) around every FoF group's centre."""
+    import ctypes
+    import torch
+    from scipy.spatial import KDTree
+    from pyhalma_gb300 import _lib, fof, halo_gas, halo_properties
+    dev = torch.device("cuda", 0)
+    s = snapshot(1)
+    off, mem = fof.fof_groups(fof.fof_labels(s.x, s.y, s.z, 0.0015), 50)
+    red = halo_properties.halo_reductions(off, *(np.ascontiguousarray(a[mem]) for a in
+                                                 (s.x, s.y, s.z, s.vx, s.vy, s.vz, s.mass)))
+    F = {k: i for i, k in enumerate(_lib.RED_FIELDS)}
+    cx, cy, cz = (np.ascontiguousarray(red[:, F[k]]) for k in ("cx", "cy", "cz"))
+    R = np.ascontiguousarray(2.0 * red[:, F["r05"]])
+    T = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+    d = [T(a) for a in (s.x, s.y, s.z, cx, cy, cz, R)]
+    k = len(R)
+    doff = torch.zeros(k + 1, dtype=torch.int64, device=dev)
+    found = ctypes.c_int64(0)
+    _lib.lib().halma_ball_gather(s.n, *[_lib.ptr(a) for a in d], 0, _lib.ptr(doff), None, 0, ctypes.byref(found),
+                                 _lib.stream_of(d[0]))
+    total = int(found.value)
+    didx = torch.zeros(max(total, 1), dtype=torch.int32, device=dev)
+
+    def gpu():
+        st = _lib.lib().halma_ball_gather(s.n, *[_lib.ptr(a) for a in d], 0, _lib.ptr(doff), _lib.ptr(didx), total,
+                                          ctypes.byref(found), _lib.stream_of(d[0]))
+        _lib.check(st, "halma_ball_gather")
+    ms = _timed(gpu, reps=max(args.steps, 3), warmup=args.warmup)
+    t0 = time.perf_counter()
+    halo_gas.balls_inside(s.x, s.y, s.z, cx, cy, cz, R)
+    e2e = time.perf_counter() - t0
+    # CPU: the reference's calls, a KD-tree over the stars and one query_ball_point per halo
+    t0 = time.perf_counter()
+    tree = KDTree(np.array((s.x, s.y, s.z)).T)
+    t_build = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    nq = 0
+    for h in range(k):
+        nq += len(tree.query_ball_point([cx[h], cy[h], cz[h]], R[h], workers=1))
+    t_query = time.perf_counter() - t0
+    print(json.dumps({"workload": "ball-gather-2M-snapshot-2r05", "particles": s.n, "spheres": k,
+                      "particles_found": total, "gpu_ms": ms, "gpu_spheres_per_s": k / (ms * 1e-3),
+                      "gpu_found_per_s": total / (ms * 1e-3), "e2e_s_host_arrays": e2e,
+                      "cpu_baseline": {"value": nq / (t_build + t_query), "unit": "particles found/s", "cores": 1,
+                                       "kind": "reference",
+                                       "sample": f"scipy KDTree build ({t_build:.2f} s) + query_ball_point per halo "
+                                                 f"({t_query:.2f} s) over all {k} spheres, 1 worker"},
+                      "speedup_vs_cpu": (total / (ms * 1e-3)) / (nq / (t_build + t_query))}), flush=True)
+    return 0
+
+
+def run_psc(args):
+    """Phase-space cleaning (pyHALMA.py:774-877) of the 2e6-particle snapshot's FoF groups."""
+    import ctypes
+    import torch
+    import oracle.phase_space as ops
+    from pyhalma_gb300 import _lib, fof, phase_space
+    dev = torch.device("cuda", 0)
+    s = snapshot(1)
+    off, mem = fof.fof_groups(fof.fof_labels(s.x, s.y, s.z, 0.0015), 50)
+    groups = [mem[off[g]:off[g + 1]] for g in range(len(off) - 1)]
+    T = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+    d = [T(a) for a in (s.x, s.y, s.z, s.vx, s.vy, s.vz, s.mass)]
+    doff, dmem = T(off), T(mem)
+    G, nm = len(groups), len(mem)
+    ctl = torch.zeros(nm, dtype=torch.uint8, device=dev)
+    which = torch.zeros(3 * nm, dtype=torch.int32, device=dev)
+    nw = torch.zeros(G, dtype=torch.int64, device=dev)
+    table = torch.zeros(G * len(_lib.PSC_FIELDS), dtype=torch.float64, device=dev)
+    P = _lib.PscParams(0.0015, 1.0, 3.0, 1, 50, 50, 100_000)
+
+    def gpu():
+        st = _lib.lib().halma_phase_space_clean(s.n, *[_lib.ptr(a) for a in d], G, _lib.ptr(doff), _lib.ptr(dmem),
+                                                ctypes.byref(P), _lib.ptr(ctl), _lib.ptr(which), _lib.ptr(nw),
+                                                _lib.ptr(table), _lib.stream_of(d[0]))
+        _lib.check(st, "halma_phase_space_clean")
+    ms = _timed(gpu, reps=max(args.steps, 3), warmup=args.warmup)
+    t0 = time.perf_counter()
+    phase_space.phase_space_cleaning(groups, s.x, s.y, s.z, s.vx, s.vy, s.vz, s.mass, 0.0015, 1.0, 3.0, True, 50)
+    e2e = time.perf_counter() - t0
+    every = max(1, G // 30)
+    t0 = time.perf_counter()
+    sample = groups[::every]
+    ops.phase_space_cleaning(sample, s.x, s.y, s.z, s.vx, s.vy, s.vz, s.mass, 0.0015, 1.0, 3.0, True, 50)
+    t_cpu = time.perf_counter() - t0
+    n_cpu = sum(len(g) for g in sample)
+    passes = table.view(G, -1)[:, _lib.PSC_FIELDS.index("passes")].cpu().numpy()
+    print(json.dumps({"workload": "phase-space-cleaning-2M-snapshot", "particles_in_groups": nm, "groups": G,
+                      "max_sweeps": int(passes.max()), "gpu_ms": ms, "gpu_particles_per_s": nm / (ms * 1e-3),
+                      "e2e_s_host_arrays": e2e,
+                      "cpu_baseline": {"value": n_cpu / t_cpu, "unit": "particles/s", "cores": 1, "kind": "port",
+                                       "sample": f"every {every}th group ({n_cpu} particles), NumPy restatement of "
+                                                 f"calc_cell / clean_cell"},
+                      "speedup_vs_cpu": (nm / (ms * 1e-3)) / (n_cpu / t_cpu)}), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["snapshot", "batched", "gas", "full"], default="snapshot")
+    ap.add_argument("--workload", choices=["snapshot", "batched", "gas", "full", "substructure", "gather", "psc"],
+                    default="snapshot")
     ap.add_argument("--alpha", type=float, default=1.0)
     ap.add_argument("--full-n", type=int, default=200_000_000)
     ap.add_argument("--full-haloes", type=int, default=200_000)
@@ -557,6 +744,12 @@ def main():
         return run_gas(args)
     if args.workload == "full":
         return run_full(args)
+    if args.workload == "substructure":
+        return run_substructure(args)
+    if args.workload == "gather":
+        return run_gather(args)
+    if args.workload == "psc":
+        return run_psc(args)
     return run_gpu(args)
 
 

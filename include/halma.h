@@ -36,6 +36,8 @@
  *   halma_split_bridges           <- the substructure block pyHALMA.py:703-766
  *   halma_ball_gather             <- halo_gas.py:223-277 st_gas_dm_particles_inside range
  *                                    queries (KDTree.query_ball_point, parallel_inside)
+ *   halma_phase_space_clean       <- halo_properties.py:113-278 calc_cell / clean_cell and
+ *                                    the driver's loop pyHALMA.py:774-843
  */
 #ifndef HALMA_H
 #define HALMA_H
@@ -133,6 +135,47 @@ int halma_split_bridges(int64_t n, const double *x, const double *y, const doubl
                         const int32_t *group_members, const halma_substructure_params *params,
                         int64_t *n_out, int64_t out_capacity, int64_t *out_offsets,
                         int32_t *out_members, int64_t *n_cut, halma_stream_t stream);
+
+/* ------------------------------------------------------------------------------------ */
+/* Phase-space cleaning                                                                 */
+/* ------------------------------------------------------------------------------------ */
+/* pyHALMA's phase-space cleaning for all groups at once: calc_cell / clean_cell
+ * (python_scripts/halo_properties.py:113-278) inside the driver's loop over groups
+ * (pyHALMA.py:774-843), parameters as read from pyHALMA.dat (pyHALMA.py:71-73, 776). */
+typedef struct {
+    double  linking_length;  /* LL: grid cells are 2 LL wide                            */
+    double  q_fil;           /* Q_FIL: a particle in a cell of <= q_fil particles drops  */
+    double  sig_fil;         /* SIG_FIL: drop at |v - v_cell| >= fac_sig*SIG_FIL*sigma    */
+    int32_t enabled;         /* PSC_FLAG: 0 keeps every particle (the driver's reset)    */
+    int32_t min_part;        /* min_part_PSC (50): smaller groups keep every particle     */
+    int32_t minp;            /* MINP: groups with fewer kept particles are not kept       */
+    int32_t max_passes;      /* bound on the sweeps per group (a safety limit)            */
+} halma_psc_params;
+
+enum {
+    HALMA_PSC_CX = 0, HALMA_PSC_CY, HALMA_PSC_CZ,  /* centre of mass of the kept particles */
+    HALMA_PSC_MASS,      /* their mass                                                   */
+    HALMA_PSC_RMAX,      /* furthest kept particle from that centre                      */
+    HALMA_PSC_NPART,     /* kept particles                                               */
+    HALMA_PSC_NCELL,     /* grid points per axis of the first grid (the driver's n_cell) */
+    HALMA_PSC_KEPT,      /* 1 when NPART >= MINP                                         */
+    HALMA_PSC_PASSES,    /* sweeps made                                                  */
+    HALMA_PSC_NFIELDS
+};
+
+/* Groups as CSR over particle indices (group_offsets[n_groups+1], group_members).  Outputs:
+ * control[k] (1 = member k kept, the driver's part_list[control]); which_cell (optional,
+ * 3 x members: the x, y then z cell of every particle of clean_cell's final grid, group g's
+ * first n_which[g] entries from group_offsets[g] on, n_which optional); halo_out
+ * (n_groups x HALMA_PSC_NFIELDS).  Like the reference, a sweep after the first marks
+ * control[ip] with ip the particle's position in the list it sweeps.  HALMA_ERR_NOT_CONVERGED
+ * when a group needs more than max_passes sweeps. */
+int halma_phase_space_clean(int64_t n, const double *x, const double *y, const double *z,
+                            const double *vx, const double *vy, const double *vz, const double *m,
+                            int64_t n_groups, const int64_t *group_offsets,
+                            const int32_t *group_members, const halma_psc_params *params,
+                            uint8_t *control, int32_t *which_cell, int64_t *n_which,
+                            double *halo_out, halma_stream_t stream);
 
 /* ------------------------------------------------------------------------------------ */
 /* Ball gather                                                                          */

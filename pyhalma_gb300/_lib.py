@@ -57,6 +57,15 @@ class SubstructureParams(ctypes.Structure):
                 ("minp_sub", ctypes.c_int32), ("minp", ctypes.c_int32)]
 
 
+class PscParams(ctypes.Structure):
+    _fields_ = [("linking_length", ctypes.c_double), ("q_fil", ctypes.c_double), ("sig_fil", ctypes.c_double),
+                ("enabled", ctypes.c_int32), ("min_part", ctypes.c_int32), ("minp", ctypes.c_int32),
+                ("max_passes", ctypes.c_int32)]
+
+
+PSC_FIELDS = ["cx", "cy", "cz", "mass", "rmax", "npart", "n_cell", "kept", "passes"]
+
+
 _lock = threading.Lock()
 _lib = None
 
@@ -80,6 +89,8 @@ SIGNATURES = {
     "halma_fof_segmented": ([_I64, _P, _P, _P, _I64, _P, _F64, _P, _P, _P], ctypes.c_int),
     "halma_split_bridges": ([_I64, _P, _P, _P, _P, _I64, _P, _P, ctypes.POINTER(SubstructureParams), _P, _I64, _P,
                              _P, _P, _P], ctypes.c_int),
+    "halma_phase_space_clean": ([_I64, _P, _P, _P, _P, _P, _P, _P, _I64, _P, _P, ctypes.POINTER(PscParams), _P, _P,
+                                 _P, _P, _P], ctypes.c_int),
     "halma_ball_gather": ([_I64, _P, _P, _P, _I64, _P, _P, _P, _P, _I32, _P, _P, _I64, _P, _P], ctypes.c_int),
     "halma_bf_potential_f32": ([_I64, _P, _P, _P, _P, _I64, _P, _P, _P, _P, _I32, _F64, _P], ctypes.c_int),
     "halma_potential_f64": ([_I64, _P, _P, _P, _P, _I64, _P, _P, _P, _F64, _I32, _I64, _P, _P], ctypes.c_int),

@@ -48,3 +48,52 @@ def test_oracle_matches_reference_block(golden, name):
     d = golden("psc.npz")
     groups, arrays, params = _case(d, name)
     _check(d, name, ops.phase_space_cleaning(groups, *arrays, *params))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", CASES)
+def test_gpu_matches_reference_block(golden, cuda, name):
+    from pyhalma_gb300 import phase_space
+    d = golden("psc.npz")
+    groups, arrays, params = _case(d, name)
+    _check(d, name, phase_space.phase_space_cleaning(groups, *arrays, *params))
+
+
+@pytest.mark.gpu
+def test_gpu_matches_oracle_on_fof_groups(cuda):
+    """FoF groups of a 200k-particle contaminated snapshot, cleaning on and aggressive."""
+    from pyhalma_gb300 import fof, phase_space, synth
+    s = synth.plummer_snapshot(200_000, 60, seed=41, box_mpc=2.0, contaminant_frac=0.15)
+    groups = [g for g in fof.friends_of_friends_serial(s.x, s.y, s.z, 0.0015) if len(g) >= 50]
+    arrays = (s.x, s.y, s.z, s.vx, s.vy, s.vz, s.mass)
+    for params in ((0.0015, 1.0, 3.0, True, 50), (0.0015, 3.0, 1.0, True, 30)):
+        got = phase_space.phase_space_cleaning(groups, *arrays, *params)
+        ref = ops.phase_space_cleaning(groups, *arrays, *params)
+        assert [g.tolist() for g in got["new_groups"]] == [g.tolist() for g in ref["new_groups"]]
+        for k in ("num_particles", "num_cells"):
+            assert list(got[k]) == list(ref[k])
+        for k in ("which_x", "which_y", "which_z"):
+            assert all(np.array_equal(a, b) for a, b in zip(got[k], ref[k]))
+        for k in ("center_x", "masses", "rmax"):
+            np.testing.assert_allclose(got[k], ref[k], rtol=RTOL, atol=1e-15)
+
+
+@pytest.mark.gpu
+def test_edge_groups(cuda):
+    from pyhalma_gb300 import phase_space
+    rng = np.random.default_rng(8)
+    n = 500
+    x, y, z = rng.normal(0, 0.002, (3, n))
+    vx, vy, vz = rng.normal(0, 50, (3, n))
+    m = np.ones(n)
+    groups = [np.arange(0, 300), np.array([], dtype=np.int64), np.array([300]), np.arange(301, 340),
+              np.arange(340, 500)]
+    for flag in (True, False):
+        got = phase_space.phase_space_cleaning(groups, x, y, z, vx, vy, vz, m, 0.0015, 1.0, 3.0, flag, 1)
+        ref = ops.phase_space_cleaning(groups, x, y, z, vx, vy, vz, m, 0.0015, 1.0, 3.0, flag, 1)
+        assert [g.tolist() for g in got["new_groups"]] == [g.tolist() for g in ref["new_groups"]]
+        assert list(got["num_cells"]) == list(ref["num_cells"])
+        for k in ("which_x", "which_y", "which_z"):
+            assert all(np.array_equal(a, b) for a, b in zip(got[k], ref[k]))
+    with pytest.raises(ValueError):
+        phase_space.phase_space_cleaning([np.array([0, n])], x, y, z, vx, vy, vz, m, 0.0015, 1.0, 3.0, True, 1)
