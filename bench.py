@@ -640,13 +640,15 @@ def run_gather(args):
     k = len(R)
     doff = torch.zeros(k + 1, dtype=torch.int64, device=dev)
     found = ctypes.c_int64(0)
-    _lib.lib().halma_ball_gather(s.n, *[_lib.ptr(a) for a in d], 0, _lib.ptr(doff), None, 0, ctypes.byref(found),
-                                 _lib.stream_of(d[0]))
+    pts, balls = [_lib.ptr(a) for a in d[:3]], [_lib.ptr(a) for a in d[3:]]
+    st = _lib.lib().halma_ball_gather(s.n, *pts, k, *balls, 0, _lib.ptr(doff), None, 0, ctypes.byref(found),
+                                      _lib.stream_of(d[0]))
+    _lib.check(st, "halma_ball_gather")
     total = int(found.value)
     didx = torch.zeros(max(total, 1), dtype=torch.int32, device=dev)
 
     def gpu():
-        st = _lib.lib().halma_ball_gather(s.n, *[_lib.ptr(a) for a in d], 0, _lib.ptr(doff), _lib.ptr(didx), total,
+        st = _lib.lib().halma_ball_gather(s.n, *pts, k, *balls, 0, _lib.ptr(doff), _lib.ptr(didx), total,
                                           ctypes.byref(found), _lib.stream_of(d[0]))
         _lib.check(st, "halma_ball_gather")
     ms = _timed(gpu, reps=max(args.steps, 3), warmup=args.warmup)
@@ -719,14 +721,73 @@ def run_psc(args):
     return 0
 
 
+def run_props(args):
+    """The O(N) per-halo properties (pyHALMA.py:930-1016) of the 2e6-particle snapshot's groups
+    after phase-space cleaning."""
+    import ctypes
+    import torch
+    import oracle.properties as op
+    from oracle.reductions import CM_velocity, half_mass_radius, sigma_effective
+    from pyhalma_gb300 import _lib, fof, phase_space
+    dev = torch.device("cuda", 0)
+    s = snapshot(1)
+    arrays = (s.x, s.y, s.z, s.vx, s.vy, s.vz, s.mass)
+    off, mem = fof.fof_groups(fof.fof_labels(s.x, s.y, s.z, 0.0015), 50)
+    groups = [mem[off[g]:off[g + 1]] for g in range(len(off) - 1)]
+    cl = phase_space.phase_space_cleaning(groups, *arrays, 0.0015, 1.0, 3.0, True, 50)
+    ng = cl["new_groups"]
+    coff, cmem = _groups_csr(ng)
+    cen = np.stack([np.asarray(cl[k], dtype=np.float64) for k in ("center_x", "center_y", "center_z", "masses",
+                                                                    "rmax")], 1)
+    T = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+    d = [T(a) for a in arrays]
+    doff, dmem, dcen = T(coff), T(cmem), T(cen)
+    G, nm = len(ng), len(cmem)
+    out = torch.zeros(G * len(_lib.PROP_FIELDS), dtype=torch.float64, device=dev)
+
+    def gpu():
+        st = _lib.lib().halma_halo_properties(s.n, *[_lib.ptr(a) for a in d], G, _lib.ptr(doff), _lib.ptr(dmem),
+                                              _lib.ptr(dcen), 0.0015, _lib.ptr(out), _lib.stream_of(d[0]))
+        _lib.check(st, "halma_halo_properties")
+    ms = _timed(gpu, reps=max(args.steps, 3), warmup=args.warmup)
+    every = max(1, G // 30)
+
+    def one(h):
+        pl = ng[h]
+        cx, cy, cz, M, rmax = cen[h]
+        r05 = half_mass_radius(cx, cy, cz, M, pl, s.x, s.y, s.z, s.mass)
+        rp = op.half_mass_radius_proj(cx, cy, cz, M, pl, s.x, s.y, s.z, s.mass)
+        ux, uy, uz = CM_velocity(M, pl, s.vx, s.vy, s.vz, s.mass)
+        jx, jy, jz = op.angular_momentum(M, pl, *arrays[:6], s.mass, cx, cy, cz, ux, uy, uz)
+        op.tully_fisher_velocity(pl, cx, cy, cz, s.x, s.y, s.z, ux, uy, uz, jx, jy, jz, s.vx, s.vy, s.vz, s.mass, r05)
+        op.kinematic_morphology(pl, *arrays[:6], s.mass, cx, cy, cz, ux, uy, uz, jx, jy, jz)
+        op.halo_shape_fortran(pl, s.x, s.y, s.z, s.mass, cx, cy, cz, r05)
+        sigma_effective(pl, r05, s.x, s.y, s.z, s.vx, s.vy, s.vz, cx, cy, cz, ux, uy, uz)
+        grid = np.arange(-(rmax + 0.0015), rmax + 0.0015, 2 * 0.0015)
+        op.sigma_projections_fortran(grid, len(grid), pl, *arrays[:6], ux, uy, uz, s.mass, cx, cy, cz, *rp, 0.0015)
+    t0 = time.perf_counter()
+    n_cpu = 0
+    for h in range(0, G, every):
+        one(h)
+        n_cpu += len(ng[h])
+    t_cpu = time.perf_counter() - t0
+    print(json.dumps({"workload": "halo-properties-2M-snapshot", "particles_in_groups": nm, "groups": G,
+                      "gpu_ms": ms, "gpu_particles_per_s": nm / (ms * 1e-3),
+                      "cpu_baseline": {"value": n_cpu / t_cpu, "unit": "particles/s", "cores": 1, "kind": "port",
+                                       "sample": f"every {every}th group ({n_cpu} particles): NumPy restatements of "
+                                                 f"the numba functions, C restatement of the Fortran ones"},
+                      "speedup_vs_cpu": (nm / (ms * 1e-3)) / (n_cpu / t_cpu)}), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["snapshot", "batched", "gas", "full", "substructure", "gather", "psc"],
-                    default="snapshot")
+    ap.add_argument("--workload", choices=["snapshot", "batched", "gas", "full", "substructure", "gather", "psc",
+                                           "props"], default="snapshot")
     ap.add_argument("--alpha", type=float, default=1.0)
     ap.add_argument("--full-n", type=int, default=200_000_000)
     ap.add_argument("--full-haloes", type=int, default=200_000)
@@ -750,6 +811,8 @@ def main():
         return run_gather(args)
     if args.workload == "psc":
         return run_psc(args)
+    if args.workload == "props":
+        return run_props(args)
     return run_gpu(args)
 
 

@@ -38,6 +38,9 @@
  *                                    queries (KDTree.query_ball_point, parallel_inside)
  *   halma_phase_space_clean       <- halo_properties.py:113-278 calc_cell / clean_cell and
  *                                    the driver's loop pyHALMA.py:774-843
+ *   halma_halo_properties         <- halo_properties.py:45-96, 365-515, 607-625, 781-866 and
+ *                                    particle_subroutines.f90:12-461 as called at
+ *                                    pyHALMA.py:930-1016
  */
 #ifndef HALMA_H
 #define HALMA_H
@@ -176,6 +179,36 @@ int halma_phase_space_clean(int64_t n, const double *x, const double *y, const d
                             const int32_t *group_members, const halma_psc_params *params,
                             uint8_t *control, int32_t *which_cell, int64_t *n_which,
                             double *halo_out, halma_stream_t stream);
+
+/* ------------------------------------------------------------------------------------ */
+/* O(N) per-halo properties                                                             */
+/* ------------------------------------------------------------------------------------ */
+enum {
+    HALMA_PROP_R05 = 0,   /* half_mass_radius (halo_properties.py:365-392)                  */
+    HALMA_PROP_R05X, HALMA_PROP_R05Y, HALMA_PROP_R05Z,   /* half_mass_radius_proj :397-458  */
+    HALMA_PROP_VX, HALMA_PROP_VY, HALMA_PROP_VZ,         /* CM_velocity :45-60              */
+    HALMA_PROP_JX, HALMA_PROP_JY, HALMA_PROP_JZ,         /* angular_momentum :461-481       */
+    HALMA_PROP_J,         /* (jx^2 + jy^2 + jz^2)^0.5 (pyHALMA.py:961-963)                  */
+    HALMA_PROP_VTF,       /* tully_fisher_velocity :62-96 (NaN: no particle in 0.9-1.1 R05) */
+    HALMA_PROP_KCO,       /* kinematic_morphology :483-515                                  */
+    HALMA_PROP_SA, HALMA_PROP_SB, HALMA_PROP_SC,         /* halo_shape_fortran -> f90:160-214 */
+    HALMA_PROP_SIG3D,     /* sigma_effective :607-625                                       */
+    HALMA_PROP_SIG1DX, HALMA_PROP_SIG1DY, HALMA_PROP_SIG1DZ,  /* sigma_projections_fortran   */
+    HALMA_PROP_VSIGMA, HALMA_PROP_LAMBDA,                /* -> f90:217-461                  */
+    HALMA_PROP_NFIELDS
+};
+
+/* The O(N) properties of pyHALMA's property loop (pyHALMA.py:930-1016) for all groups at
+ * once.  Groups as CSR over particle indices; centre: n_groups x 5 rows (cx, cy, cz, mass,
+ * rmax), the center_x / masses / rmax arrays the phase-space cleaning leaves; out: n_groups x
+ * HALMA_PROP_NFIELDS.  As in the reference, JZ is sum m (rx*vvy - ry*vvz) / M.  The FP32
+ * Fortran quantities (shape, projections) are summed in the Fortran's order, every operation
+ * rounded on its own. */
+int halma_halo_properties(int64_t n, const double *x, const double *y, const double *z,
+                          const double *vx, const double *vy, const double *vz, const double *m,
+                          int64_t n_groups, const int64_t *group_offsets,
+                          const int32_t *group_members, const double *centre,
+                          double linking_length, double *out, halma_stream_t stream);
 
 /* ------------------------------------------------------------------------------------ */
 /* Ball gather                                                                          */

@@ -66,6 +66,10 @@ class PscParams(ctypes.Structure):
 PSC_FIELDS = ["cx", "cy", "cz", "mass", "rmax", "npart", "n_cell", "kept", "passes"]
 
 
+PROP_FIELDS = ["r05", "r05x", "r05y", "r05z", "vx", "vy", "vz", "jx", "jy", "jz", "j", "v_tf", "k_co", "a", "b", "c",
+               "sig_3d", "sig_1d_x", "sig_1d_y", "sig_1d_z", "v_sigma", "lambda"]
+
+
 _lock = threading.Lock()
 _lib = None
 
@@ -91,6 +95,7 @@ SIGNATURES = {
                              _P, _P, _P], ctypes.c_int),
     "halma_phase_space_clean": ([_I64, _P, _P, _P, _P, _P, _P, _P, _I64, _P, _P, ctypes.POINTER(PscParams), _P, _P,
                                  _P, _P, _P], ctypes.c_int),
+    "halma_halo_properties": ([_I64, _P, _P, _P, _P, _P, _P, _P, _I64, _P, _P, _P, _F64, _P, _P], ctypes.c_int),
     "halma_ball_gather": ([_I64, _P, _P, _P, _I64, _P, _P, _P, _P, _I32, _P, _P, _I64, _P, _P], ctypes.c_int),
     "halma_bf_potential_f32": ([_I64, _P, _P, _P, _P, _I64, _P, _P, _P, _P, _I32, _F64, _P], ctypes.c_int),
     "halma_potential_f64": ([_I64, _P, _P, _P, _P, _I64, _P, _P, _P, _F64, _I32, _I64, _P, _P], ctypes.c_int),

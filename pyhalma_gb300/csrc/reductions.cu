@@ -138,40 +138,33 @@ __global__ void __launch_bounds__(256) red_r05_kernel(const int64_t *__restrict_
     const int64_t b = off[h], e = off[h + 1];
     const Red r = red[h];
     const int64_t nmem = (int64_t)r.n;
-    __shared__ double wtot[8];
-    __shared__ double running;
     __shared__ long long first;
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    if (threadIdx.x == 0) {
-        running = 0.0;
-        first = LLONG_MAX;   // atomicMin target: no crossing yet
-    }
-    __syncthreads();
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const double half = 0.5 * r.mref;
     const bool given = !isnan(r.r05);   // caller supplied R05: skip the search
-    for (int64_t k0 = 0; !given && k0 < nmem; k0 += blockDim.x) {
-        const int64_t k = k0 + threadIdx.x;
-        const double mk = k < nmem ? m[order[b + k]] : 0.0;
-        double inc = mk;
-        for (int o = 1; o < 32; o <<= 1) {
-            const double u = __shfl_up_sync(0xffffffffu, inc, o);
-            if (lane >= o) inc += u;
+    if (threadIdx.x == 0) first = LLONG_MAX;
+    __syncthreads();
+    if (!given && w == 0) {
+        // one running FP64 sum in increasing distance, added in order like the reference's loop
+        // (halo_properties.py:385-390): 32 masses are loaded at a time and every lane adds them
+        // one by one, so all lanes hold the same sum and leave the loop together
+        double cum = 0.0;
+        long long f = LLONG_MAX;
+        for (int64_t k0 = 0; k0 < nmem && f == LLONG_MAX; k0 += 32) {
+            const int64_t k = k0 + lane;
+            const double mk = k < nmem ? m[order[b + k]] : 0.0;
+            const int cnt = nmem - k0 < 32 ? (int)(nmem - k0) : 32;
+            for (int t = 0; t < cnt; ++t) {
+                cum = __dadd_rn(cum, __shfl_sync(0xffffffffu, mk, t));
+                if (cum > half) {
+                    f = k0 + t;
+                    break;
+                }
+            }
         }
-        if (lane == 31) wtot[w] = inc;
-        __syncthreads();
-        double pre = running;
-        for (int q = 0; q < w; ++q) pre += wtot[q];
-        const double cum = pre + inc;
-        if (k < nmem && cum > half) atomicMin(&first, (long long)k);
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            double t = 0.0;
-            for (int q = 0; q < nw; ++q) t += wtot[q];
-            running += t;
-        }
-        __syncthreads();
-        if (first != LLONG_MAX) break;
+        if (lane == 0) first = f;
     }
+    __syncthreads();
     __shared__ double r05s;
     if (threadIdx.x == 0) {
         double r05 = 0.0;

@@ -142,3 +142,53 @@ def escape_velocity_unbinding_particles(cx, cy, cz, vx, vy, vz, Rmax, part_list,
     e *= factor_v ** 2
     ek = 0.5 * ((st_vx[pl] - vx) ** 2 + (st_vy[pl] - vy) ** 2 + (st_vz[pl] - vz) ** 2)
     return (ek + e) <= 0.
+
+
+# ---------------------------------------------------------------------------------------
+# the O(N) part of the driver's property loop (pyHALMA.py:930-1016)
+# ---------------------------------------------------------------------------------------
+PROP = {k: i for i, k in enumerate(_lib.PROP_FIELDS)}
+# driver array name -> field (pyHALMA.py:945-1013)
+DRIVER_NAMES = {"rad05": "r05", "rad05_x": "r05x", "rad05_y": "r05y", "rad05_z": "r05z", "velocities_x": "vx",
+                "velocities_y": "vy", "velocities_z": "vz", "specific_angular_momentum_x": "jx",
+                "specific_angular_momentum_y": "jy", "specific_angular_momentum_z": "jz",
+                "specific_angular_momentum": "j", "tully_fisher_velocities": "v_tf",
+                "kinematic_morphologies": "k_co", "s_axis_major": "a", "s_axis_intermediate": "b",
+                "s_axis_minor": "c", "sig_3D": "sig_3d", "sig_1D_x": "sig_1d_x", "sig_1D_y": "sig_1d_y",
+                "sig_1D_z": "sig_1d_z", "vsigma": "v_sigma", "lambda_ensellem": "lambda"}
+
+
+def halo_property_table(offsets, members, st_x, st_y, st_z, st_vx, st_vy, st_vz, st_mass, centre, LL):
+    """C ABI ``halma_halo_properties``: groups as CSR over particle indices, centre rows
+    (cx, cy, cz, mass, rmax); returns an (n_groups, len(PROP_FIELDS)) float64 table."""
+    offsets = _lib.as_host(offsets, np.int64)
+    members = _lib.as_host(members, np.int32)
+    arrs = tuple(_lib.as_host(a, np.float64) for a in (st_x, st_y, st_z, st_vx, st_vy, st_vz, st_mass))
+    centre = _lib.as_host(centre, np.float64).reshape(-1, 5)
+    G = offsets.shape[0] - 1
+    if centre.shape[0] != G:
+        raise ValueError("one centre row (cx, cy, cz, mass, rmax) per group")
+    out = np.zeros((max(G, 1), len(_lib.PROP_FIELDS)), dtype=np.float64)
+    if G > 0:
+        st = _lib.lib().halma_halo_properties(arrs[0].shape[0], *[_lib.ptr(a) for a in arrs], G, _lib.ptr(offsets),
+                                              _lib.ptr(members), _lib.ptr(centre), float(LL), _lib.ptr(out), None)
+        _lib.check(st, "halma_halo_properties")
+    return out[:G]
+
+
+def property_loop(new_groups, st_x, st_y, st_z, st_vx, st_vy, st_vz, st_mass, center_x, center_y, center_z, masses,
+                  rmax, LL):
+    """The O(N) properties the driver's loop computes per halo (pyHALMA.py:930-1016), for all
+    haloes at once.  Inputs as the phase-space cleaning leaves them; returns a dict keyed by the
+    driver's array names (rad05, rad05_x, ..., sig_3D, sig_1D_x, vsigma, lambda_ensellem)."""
+    lens = np.fromiter((len(g) for g in new_groups), dtype=np.int64, count=len(new_groups))
+    offsets = np.zeros(len(new_groups) + 1, dtype=np.int64)
+    np.cumsum(lens, out=offsets[1:])
+    members = np.concatenate([np.asarray(g, dtype=np.int64) for g in new_groups]) if offsets[-1] > 0 \
+        else np.zeros(0, dtype=np.int64)
+    if members.size and (members.min() < 0 or members.max() >= len(st_x)):
+        raise ValueError("group members must be indices into the particle arrays")
+    centre = np.stack([np.asarray(a, dtype=np.float64) for a in (center_x, center_y, center_z, masses, rmax)], 1) \
+        if len(new_groups) else np.zeros((0, 5))
+    t = halo_property_table(offsets, members, st_x, st_y, st_z, st_vx, st_vy, st_vz, st_mass, centre, LL)
+    return {name: t[:, PROP[f]].copy() for name, f in DRIVER_NAMES.items()}

@@ -28,7 +28,11 @@ Fixtures written to tests/golden/ (all seeds fixed):
 * ball.npz        — reference ``halo_gas.st_gas_dm_particles_inside`` with its MASCLET AMR
   conversion replaced by a pass-through of gas particles (inputs and the 17 outputs stored);
 * psc.npz         — the driver's phase-space cleaning block (pyHALMA.py:774-877) exec'd from
-  the reference's own source on FoF groups of contaminated Plummer snapshots.
+  the reference's own source on FoF groups of contaminated Plummer snapshots;
+* properties.npz  — the reference's O(N) per-halo property functions (half-mass radii, bulk
+  velocity, angular momentum, Tully-Fisher velocity, kappa_co, shape, sigma_effective,
+  sigma projections) called as the driver's property loop calls them; the f2py routines
+  halo_shape / sigma_projections map onto the C restatement of the Fortran.
 """
 from __future__ import annotations
 
@@ -89,6 +93,27 @@ def install_stubs():
             return oracle.bf_potential_f32(m, x, y, z, tx, ty, tz, ncores=max(int(ncores), 1))
 
         serial_brute_force_binding_energy = None
+
+        @staticmethod
+        def halo_shape(ncore, npart, x, y, z, mass):
+            from oracle import properties as op
+            assert x.dtype == np.float32 and int(npart) == len(x)
+            out = np.zeros(3, dtype=np.float32)
+            op.lib().oracle_halo_shape(int(npart), op._p(x), op._p(y), op._p(z), op._p(mass), op._p(out))
+            return out
+
+        @staticmethod
+        def sigma_projections(ncore, npart, grid, n_cell, part_list, st_x, st_y, st_z, st_vx, st_vy, st_vz,
+                              st_mass, cx, cy, cz, R05x, R05y, R05z, ll):
+            from oracle import properties as op
+            assert grid.dtype == np.float32 and st_vx.dtype == np.float32
+            pl = np.ascontiguousarray(part_list.astype(np.int64) - 1)          # Fortran indices start at 1
+            out = np.zeros(5, dtype=np.float32)
+            arrs = [np.ascontiguousarray(a) for a in (st_x, st_y, st_z, st_vx, st_vy, st_vz, st_mass)]
+            op.lib().oracle_sigma_projections(int(npart), op._p(grid), int(n_cell), op._p(pl),
+                                              *[op._p(a) for a in arrs],
+                                              *[float(v) for v in (cx, cy, cz, R05x, R05y, R05z, ll)], op._p(out))
+            return tuple(out)
 
     part.particle = _P
     fm.particle = part
@@ -373,6 +398,45 @@ def psc_cases(fof, hp, refdir):
     np.savez_compressed(os.path.join(HERE, "psc.npz"), **out)
 
 
+def property_cases(hp):
+    """The O(N) per-halo properties of the driver's property loop (pyHALMA.py:930-1016), called
+    as the driver calls them, on the groups and centres that phase-space cleaning leaves for a
+    contaminated Plummer snapshot.  The Fortran routines (halo_shape, sigma_projections) run
+    through the reference's Python wrappers on the C restatement of the Fortran."""
+    from oracle import phase_space as ops
+    s = synth.plummer_snapshot(16_000, 10, seed=51, box_mpc=0.6, contaminant_frac=0.1, m_hi=3e10)
+    groups = [g for g in oracle.labels_to_groups(oracle.fof_labels(s.x, s.y, s.z, 0.0015)) if len(g) >= 50]
+    LL = 0.0015
+    cl = ops.phase_space_cleaning(groups, s.x, s.y, s.z, s.vx, s.vy, s.vz, s.mass, LL, 1.0, 3.0, True, 50)
+    rows = []
+    for h, pl in enumerate(cl["new_groups"]):
+        pl = np.asarray(pl, dtype=np.int64)
+        cx, cy, cz, mass, rmax = (cl[k][h] for k in ("center_x", "center_y", "center_z", "masses", "rmax"))
+        rad05 = hp.half_mass_radius(cx, cy, cz, mass, pl, s.x, s.y, s.z, s.mass)
+        r05x, r05y, r05z = hp.half_mass_radius_proj(cx, cy, cz, mass, pl, s.x, s.y, s.z, s.mass)
+        vx, vy, vz = hp.CM_velocity(mass, pl, s.vx, s.vy, s.vz, s.mass)
+        jx, jy, jz = hp.angular_momentum(mass, pl, s.x, s.y, s.z, s.vx, s.vy, s.vz, s.mass, cx, cy, cz, vx, vy, vz)
+        j = (jx ** 2 + jy ** 2 + jz ** 2) ** 0.5
+        vtf = hp.tully_fisher_velocity(pl, cx, cy, cz, s.x, s.y, s.z, vx, vy, vz, jx, jy, jz, s.vx, s.vy, s.vz,
+                                       s.mass, rad05)
+        kco = hp.kinematic_morphology(pl, s.x, s.y, s.z, s.vx, s.vy, s.vz, s.mass, cx, cy, cz, vx, vy, vz, jx, jy, jz)
+        sa, sb, sc = hp.halo_shape_fortran(pl, s.x, s.y, s.z, s.mass, cx, cy, cz, rad05)
+        sig3 = hp.sigma_effective(pl, rad05, s.x, s.y, s.z, s.vx, s.vy, s.vz, cx, cy, cz, vx, vy, vz)
+        grid = np.arange(-(rmax + LL), rmax + LL, 2 * LL)
+        s1x, s1y, s1z, vsig, lam = hp.sigma_projections_fortran(grid, len(grid), pl, s.x, s.y, s.z, s.vx, s.vy,
+                                                                s.vz, vx, vy, vz, s.mass, cx, cy, cz,
+                                                                r05x, r05y, r05z, LL)
+        rows.append([cx, cy, cz, mass, rmax, rad05, r05x, r05y, r05z, vx, vy, vz, jx, jy, jz, j, vtf, kco,
+                     sa, sb, sc, sig3, s1x, s1y, s1z, vsig, lam])
+    lens = [len(g) for g in cl["new_groups"]]
+    out = {"x": s.x, "y": s.y, "z": s.z, "vx": s.vx, "vy": s.vy, "vz": s.vz, "m": s.mass,
+           "off": np.concatenate(([0], np.cumsum(lens))).astype(np.int64),
+           "mem": np.concatenate([np.asarray(g, dtype=np.int64) for g in cl["new_groups"]]),
+           "rows": np.array(rows, dtype=np.float64), "ll": np.float64(LL)}
+    np.savez_compressed(os.path.join(HERE, "properties.npz"), **out)
+    print(f"  halo properties (O(N) set): {len(rows)} groups")
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default="/root/reference")
@@ -380,7 +444,7 @@ def main():
     args = ap.parse_args()
     fof, hg, hp = import_reference(args.reference)
     todo = args.only.split(",") if args.only else ["fof", "config1", "pred", "props", "rps", "sub", "ball",
-                                                    "psc"]
+                                                    "psc", "prop"]
     if "fof" in todo:
         fof_cases(fof)
     if "config1" in todo:
@@ -397,6 +461,8 @@ def main():
         ball_cases(hg)
     if "psc" in todo:
         psc_cases(fof, hp, args.reference)
+    if "prop" in todo:
+        property_cases(hp)
 
 
 if __name__ == "__main__":

@@ -1,0 +1,105 @@
+"""The O(N) per-halo properties of the driver's property loop (pyHALMA.py:930-1016) against the
+reference's own functions (golden fixture; the Fortran routines through the reference's
+wrappers on the C restatement of the Fortran) and the oracle.
+
+Tolerances: FP64 quantities whose reference sums run in an unspecified order (numba
+fastmath) at 1e-10 relative; the FP32 Fortran quantities (shape, projections) and the
+half-mass radii, which the GPU computes in the reference's own order, exactly.
+"""
+import numpy as np
+import pytest
+
+import oracle.properties as op
+from oracle.reductions import CM_velocity, half_mass_radius, sigma_effective
+
+COLS = ["cx", "cy", "cz", "mass", "rmax", "r05", "r05x", "r05y", "r05z", "vx", "vy", "vz", "jx", "jy", "jz", "j",
+        "v_tf", "k_co", "a", "b", "c", "sig_3d", "sig_1d_x", "sig_1d_y", "sig_1d_z", "v_sigma", "lambda"]
+EXACT = {"r05", "r05x", "r05y", "r05z", "a", "b", "c", "sig_1d_x", "sig_1d_y", "sig_1d_z", "v_sigma", "lambda"}
+RTOL = 1e-10
+
+
+def _load(d):
+    arrays = tuple(d[k] for k in ("x", "y", "z", "vx", "vy", "vz", "m"))
+    return arrays, d["off"], d["mem"], d["rows"], float(d["ll"])
+
+
+def test_oracle_matches_reference_functions(golden):
+    (x, y, z, vx, vy, vz, m), off, mem, rows, LL = _load(golden("properties.npz"))
+    assert len(rows) >= 5
+    for h, row in enumerate(rows):
+        pl = mem[off[h]:off[h + 1]]
+        cx, cy, cz, M, rmax = row[:5]
+        r05 = half_mass_radius(cx, cy, cz, M, pl, x, y, z, m)
+        r05x, r05y, r05z = op.half_mass_radius_proj(cx, cy, cz, M, pl, x, y, z, m)
+        ux, uy, uz = CM_velocity(M, pl, vx, vy, vz, m)
+        jx, jy, jz = op.angular_momentum(M, pl, x, y, z, vx, vy, vz, m, cx, cy, cz, ux, uy, uz)
+        j = (jx ** 2 + jy ** 2 + jz ** 2) ** 0.5
+        vtf = op.tully_fisher_velocity(pl, cx, cy, cz, x, y, z, ux, uy, uz, jx, jy, jz, vx, vy, vz, m, r05)
+        kco = op.kinematic_morphology(pl, x, y, z, vx, vy, vz, m, cx, cy, cz, ux, uy, uz, jx, jy, jz)
+        sa, sb, sc = op.halo_shape_fortran(pl, x, y, z, m, cx, cy, cz, r05)
+        s3 = sigma_effective(pl, r05, x, y, z, vx, vy, vz, cx, cy, cz, ux, uy, uz)
+        grid = np.arange(-(rmax + LL), rmax + LL, 2 * LL)
+        sp = op.sigma_projections_fortran(grid, len(grid), pl, x, y, z, vx, vy, vz, ux, uy, uz, m, cx, cy, cz,
+                                          r05x, r05y, r05z, LL)
+        got = [cx, cy, cz, M, rmax, r05, r05x, r05y, r05z, ux, uy, uz, jx, jy, jz, j, vtf, kco, sa, sb, sc, s3, *sp]
+        for k, (g, r) in enumerate(zip(got, row)):
+            if COLS[k] in EXACT:
+                assert g == r, (h, COLS[k])
+            else:
+                assert abs(g - r) <= RTOL * abs(r) + 1e-300, (h, COLS[k], g, r)
+
+
+def test_shape_known_answer():
+    # an ellipsoidal shell with semi-axes 3, 2, 1: <x^2> = a^2 / 3, so sqrt(eigenvalues) = a/sqrt(3)
+    rng = np.random.default_rng(1)
+    u = rng.normal(size=(100_000, 3))
+    u /= np.linalg.norm(u, axis=1)[:, None]
+    p = u * np.array([3.0, 2.0, 1.0])
+    a, b, c = op.halo_shape_fortran(np.arange(len(p)), p[:, 0], p[:, 1], p[:, 2], np.ones(len(p)), 0, 0, 0, 1.0)
+    assert np.allclose([a, b, c], np.array([3.0, 2.0, 1.0]) / np.sqrt(3.0), rtol=5e-3)
+
+
+@pytest.mark.gpu
+def test_gpu_matches_reference_functions(golden, cuda):
+    from pyhalma_gb300 import _lib, halo_properties
+    (x, y, z, vx, vy, vz, m), off, mem, rows, LL = _load(golden("properties.npz"))
+    t = halo_properties.halo_property_table(off, mem, x, y, z, vx, vy, vz, m, rows[:, :5], LL)
+    for f in _lib.PROP_FIELDS:
+        got, ref = t[:, _lib.PROP_FIELDS.index(f)], rows[:, COLS.index(f)]
+        if f in EXACT:
+            assert np.array_equal(got, ref.astype(np.float32).astype(np.float64) if f not in
+                                  ("r05", "r05x", "r05y", "r05z") else ref), f
+        else:
+            np.testing.assert_allclose(got, ref, rtol=RTOL, atol=0, err_msg=f)
+
+
+@pytest.mark.gpu
+def test_gpu_property_loop_on_cleaned_groups(cuda):
+    """FoF -> phase-space cleaning -> property loop on a 200k-particle snapshot, against the
+    oracle group by group."""
+    import oracle.phase_space as ops
+    from pyhalma_gb300 import fof, halo_properties, phase_space, synth
+    s = synth.plummer_snapshot(200_000, 60, seed=43, box_mpc=2.0, contaminant_frac=0.1)
+    arrays = (s.x, s.y, s.z, s.vx, s.vy, s.vz, s.mass)
+    groups = [g for g in fof.friends_of_friends_serial(s.x, s.y, s.z, 0.0015) if len(g) >= 50]
+    cl = phase_space.phase_space_cleaning(groups, *arrays, 0.0015, 1.0, 3.0, True, 50)
+    res = halo_properties.property_loop(cl["new_groups"], *arrays, cl["center_x"], cl["center_y"], cl["center_z"],
+                                        cl["masses"], cl["rmax"], 0.0015)
+    for h, pl in enumerate(cl["new_groups"]):
+        cx, cy, cz, M, rmax = (cl[k][h] for k in ("center_x", "center_y", "center_z", "masses", "rmax"))
+        r05 = half_mass_radius(cx, cy, cz, M, pl, s.x, s.y, s.z, s.mass)
+        assert res["rad05"][h] == r05
+        rp = op.half_mass_radius_proj(cx, cy, cz, M, pl, s.x, s.y, s.z, s.mass)
+        assert (res["rad05_x"][h], res["rad05_y"][h], res["rad05_z"][h]) == rp
+        ux, uy, uz = CM_velocity(M, pl, s.vx, s.vy, s.vz, s.mass)
+        jx, jy, jz = op.angular_momentum(M, pl, *arrays[:6], s.mass, cx, cy, cz, ux, uy, uz)
+        np.testing.assert_allclose([res["specific_angular_momentum_x"][h], res["specific_angular_momentum_y"][h],
+                                    res["specific_angular_momentum_z"][h]], [jx, jy, jz], rtol=1e-9)
+        kco = op.kinematic_morphology(pl, *arrays[:6], s.mass, cx, cy, cz, ux, uy, uz, jx, jy, jz)
+        np.testing.assert_allclose(res["kinematic_morphologies"][h], kco, rtol=1e-9)
+        sa, sb, sc = op.halo_shape_fortran(pl, s.x, s.y, s.z, s.mass, cx, cy, cz, r05)
+        assert (res["s_axis_major"][h], res["s_axis_intermediate"][h], res["s_axis_minor"][h]) == (sa, sb, sc)
+        grid = np.arange(-(rmax + 0.0015), rmax + 0.0015, 2 * 0.0015)
+        sp = op.sigma_projections_fortran(grid, len(grid), pl, *arrays[:6], ux, uy, uz, s.mass, cx, cy, cz, *rp,
+                                          0.0015)
+        assert tuple(res[k][h] for k in ("sig_1D_x", "sig_1D_y", "sig_1D_z", "vsigma", "lambda_ensellem")) == sp
