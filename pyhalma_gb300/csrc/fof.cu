@@ -241,11 +241,38 @@ __global__ void prep_kernel(const double *__restrict__ x, const double *__restri
     }
 }
 
+// Particles with the same full key (cell and 4 x 4 x 4 sub-cell) lie at most sqrt(3)/4 of a
+// cell (0.44 LL) apart, so they are friends whatever the rounding: each such run is joined
+// up front, every member under the run's first sorted position (which keeps "a root is the
+// smallest position of its tree").  runstart[k] = k at a run's first position, else 0; an
+// inclusive max-scan turns it into the run head of every position.
+__global__ void subrun_kernel(int n, const uint64_t *__restrict__ keys, int *__restrict__ runstart) {
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x)
+        runstart[k] = (k == 0 || keys[k] != keys[k - 1]) ? k : 0;
+}
+
+__global__ void preunion_kernel(int n, const uint64_t *__restrict__ keys, const int *__restrict__ runhead,
+                                int *__restrict__ parent, unsigned char *__restrict__ has) {
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        parent[k] = runhead[k];
+        const bool friend_before = k > 0 && keys[k - 1] == keys[k];
+        const bool friend_after = k + 1 < n && keys[k + 1] == keys[k];
+        has[k] = (friend_before || friend_after) ? 1 : 0;
+    }
+}
+
 // Cell table + hash insert, from the exclusive scan of the run heads.
+// Hash slot: cell key, first sorted position and particle count of the cell, so that a
+// neighbour lookup is one 16-byte load per probe.
+struct __align__(16) CellSlot {
+    unsigned long long key;
+    int start, count;
+};
+
 __global__ void cells_kernel(int n, int sb, const uint64_t *__restrict__ keys, const int *__restrict__ head,
                              const int *__restrict__ cellpos, int *__restrict__ cell_start,
-                             uint64_t *__restrict__ cell_key, uint64_t *__restrict__ hkeys,
-                             int *__restrict__ hvals, uint64_t hmask, int *__restrict__ ncell) {
+                             uint64_t *__restrict__ cell_key, CellSlot *__restrict__ slots,
+                             int *__restrict__ cell_slot, uint64_t hmask, int *__restrict__ ncell) {
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
         if (head[k]) {
             const int c = cellpos[k];
@@ -255,10 +282,9 @@ __global__ void cells_kernel(int n, int sb, const uint64_t *__restrict__ keys, c
             uint64_t h = mix64(key) & hmask;
             for (uint64_t probe = 0; probe <= hmask; ++probe) {
                 const unsigned long long prev =
-                    atomicCAS((unsigned long long *)(hkeys + h), (unsigned long long)kEmptyKey,
-                              (unsigned long long)key);
+                    atomicCAS(&slots[h].key, (unsigned long long)kEmptyKey, (unsigned long long)key);
                 if (prev == kEmptyKey || prev == key) {
-                    hvals[h] = c;
+                    cell_slot[c] = (int)h;
                     break;
                 }
                 h = (h + 1) & hmask;
@@ -269,6 +295,16 @@ __global__ void cells_kernel(int n, int sb, const uint64_t *__restrict__ keys, c
             *ncell = m;
             cell_start[m] = n;
         }
+    }
+}
+
+__global__ void slot_fill_kernel(const int *__restrict__ ncell_p, const int *__restrict__ cell_start,
+                                 const int *__restrict__ cell_slot, CellSlot *__restrict__ slots) {
+    const int nc = *ncell_p;
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x) {
+        CellSlot &sl = slots[cell_slot[c]];
+        sl.start = cell_start[c];
+        sl.count = cell_start[c + 1] - cell_start[c];
     }
 }
 
@@ -293,16 +329,16 @@ __global__ void items_kernel(int n, const int *__restrict__ head, const int *__r
     }
 }
 
-__device__ __forceinline__ int hash_lookup(const uint64_t *__restrict__ hkeys, const int *__restrict__ hvals,
-                                           uint64_t hmask, uint64_t key) {
+// (start, count) of the cell with this key, count 0 when it holds no particle.
+__device__ __forceinline__ int2 hash_lookup(const CellSlot *__restrict__ slots, uint64_t hmask, uint64_t key) {
     uint64_t h = mix64(key) & hmask;
     for (uint64_t probe = 0; probe <= hmask; ++probe) {
-        const uint64_t k = hkeys[h];
-        if (k == key) return hvals[h];
-        if (k == kEmptyKey) return -1;
+        const ulonglong2 v = __ldg(reinterpret_cast<const ulonglong2 *>(slots + h));
+        if (v.x == key) return make_int2((int)(v.y & 0xffffffffull), (int)(v.y >> 32));
+        if (v.x == kEmptyKey) return make_int2(0, 0);
         h = (h + 1) & hmask;
     }
-    return -1;
+    return make_int2(0, 0);
 }
 
 __device__ __forceinline__ bool exact_link(const double *__restrict__ x, const double *__restrict__ y,
@@ -332,7 +368,7 @@ constexpr int kHomeSeg = 13;
 __global__ void __launch_bounds__(256) link_kernel(
     const float4 *__restrict__ rec, const int *__restrict__ cell_start, const uint64_t *__restrict__ cell_key,
     const int *__restrict__ item_k0, const int *__restrict__ item_cell, const int *__restrict__ nitems_p,
-    const uint64_t *__restrict__ hkeys, const int *__restrict__ hvals, uint64_t hmask, FofGeom g,
+    int *item_counter, const CellSlot *__restrict__ slots, uint64_t hmask, FofGeom g,
     const double *__restrict__ x, const double *__restrict__ y, const double *__restrict__ z,
     int *parent, unsigned char *has, int *err) {
     __shared__ float4 buf[kFofWarps][32];
@@ -340,7 +376,12 @@ __global__ void __launch_bounds__(256) link_kernel(
     __shared__ int jbuf[kFofWarps][32];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int nitems = *nitems_p;
-    for (int item = blockIdx.x * kFofWarps + w; item < nitems; item += gridDim.x * kFofWarps) {
+    // items come from a counter: their cost varies by orders of magnitude (dense cores)
+    for (;;) {
+        int item = 0;
+        if (lane == 0) item = atomicAdd(item_counter, 1);
+        item = __shfl_sync(0xffffffffu, item, 0);
+        if (item >= nitems) break;
         const int c = item_cell[item];
         const int k0 = item_k0[item];
         const int ce = cell_start[c + 1];
@@ -357,11 +398,9 @@ __global__ void __launch_bounds__(256) link_kernel(
             const long long nx = cx + c_stencil[lane][0], ny = cy + c_stencil[lane][1], nz = cz + c_stencil[lane][2];
             if (nx < g.ncx && ny >= 0 && ny < g.ncy && nz >= 0 && nz < g.ncz) {
                 const uint64_t nkey = ((uint64_t)nx * (uint64_t)g.ncy + (uint64_t)ny) * (uint64_t)g.ncz + (uint64_t)nz;
-                const int cc = hash_lookup(hkeys, hvals, hmask, nkey);
-                if (cc >= 0) {
-                    sjs = cell_start[cc];
-                    sn = cell_start[cc + 1] - sjs;
-                }
+                const int2 sc = hash_lookup(slots, hmask, nkey);
+                sjs = sc.x;
+                sn = sc.y;
             }
         } else if (lane == kHomeSeg) {
             sjs = k0 + 1;
@@ -626,7 +665,7 @@ int fof_core(int n, const double *x, const double *y, const double *z, FofGeom g
     uint64_t hcap = 1;
     while (hcap < 2ull * (uint64_t)n) hcap <<= 1;
     const size_t sort_b = sort_pairs_u64_i32_bytes(n, end_bit);
-    const size_t scan_b = exclusive_sum_i32_bytes(n);
+    const size_t scan_b = std::max(exclusive_sum_i32_bytes(n), inclusive_max_i32_bytes(n));
     Layout M;
     const size_t o_kin = M.add(8ull * n), o_kout = M.add(8ull * n);
     const size_t o_vin = M.add(4ull * n), o_vout = M.add(4ull * n);
@@ -635,7 +674,7 @@ int fof_core(int n, const double *x, const double *y, const double *z, FofGeom g
     const size_t o_par = M.add(4ull * n), o_has = M.add(1ull * n), o_root = M.add(4ull * n);
     const size_t o_min = M.add(4ull * n);
     const size_t o_cst = M.add(4ull * (n + 1)), o_ckey = M.add(8ull * n);
-    const size_t o_hk = M.add(8ull * hcap), o_hv = M.add(4ull * hcap);
+    const size_t o_hk = M.add(16ull * hcap), o_hv = M.add(4ull * n);   // hash slots, slot of each cell
     const size_t o_flag = M.add(4ull * n), o_ipos = M.add(4ull * n);
     const size_t o_ik0 = M.add(4ull * n), o_icell = M.add(4ull * n);
     const size_t o_cnt = M.add(64);
@@ -650,25 +689,31 @@ int fof_core(int n, const double *x, const double *y, const double *z, FofGeom g
     auto *has = at<unsigned char>(base, o_has);
     auto *cst = at<int>(base, o_cst);
     auto *ckey = at<uint64_t>(base, o_ckey);
-    auto *hk = at<uint64_t>(base, o_hk);
+    auto *hk = at<CellSlot>(base, o_hk);
     auto *hv = at<int>(base, o_hv);
     auto *flag = at<int>(base, o_flag), *ipos = at<int>(base, o_ipos);
     auto *ik0 = at<int>(base, o_ik0), *icell = at<int>(base, o_icell);
-    int *cnt = at<int>(base, o_cnt);   // [0] ncell [1] nitems [2] ngroups [3] err
+    int *cnt = at<int>(base, o_cnt);   // [0] ncell [1] nitems [2] ngroups [3] err [5] link item counter
     void *tmp = at<void>(base, o_tmp);
     const int g1 = std::min(sms * 8, grid_for(n, 256));
 
     HALMA_CUDA(cudaMemsetAsync(cnt, 0, 64, st));
-    HALMA_CUDA(cudaMemsetAsync(hk, 0xff, 8ull * hcap, st));
+    HALMA_CUDA(cudaMemsetAsync(hk, 0xff, 16ull * hcap, st));
     HALMA_LAUNCH(keys_kernel, g1, 256, 0, st, x, y, z, n, g, sg, kin, vin);
     HALMA_TRY(sort_pairs_u64_i32(tmp, sort_b, kin, kout, vin, vout, n, end_bit, st));
     HALMA_LAUNCH(prep_kernel, g1, 256, 0, st, x, y, z, n, g, sg, kout, vout, rec, head, parent, has, minidx);
+    if (g.sb != 0 && g.lo > 0.f) {   // sub-cells in the key and a positive linking length
+        HALMA_LAUNCH(subrun_kernel, g1, 256, 0, st, n, kout, flag);
+        HALMA_TRY(inclusive_max_i32(tmp, scan_b, flag, root, n, st));
+        HALMA_LAUNCH(preunion_kernel, g1, 256, 0, st, n, kout, root, parent, has);
+    }
     HALMA_TRY(exclusive_sum_i32(tmp, scan_b, head, cpos, n, st));
     HALMA_LAUNCH(cells_kernel, g1, 256, 0, st, n, g.sb, kout, head, cpos, cst, ckey, hk, hv, hcap - 1, cnt + 0);
+    HALMA_LAUNCH(slot_fill_kernel, g1, 256, 0, st, cnt + 0, cst, hv, hk);
     HALMA_LAUNCH(itemflag_kernel, g1, 256, 0, st, n, head, cpos, cst, flag);
     HALMA_TRY(exclusive_sum_i32(tmp, scan_b, flag, ipos, n, st));
     HALMA_LAUNCH(items_kernel, g1, 256, 0, st, n, head, cpos, flag, ipos, ik0, icell, cnt + 1);
-    HALMA_LAUNCH(link_kernel, sms * 8, 32 * kFofWarps, 0, st, rec, cst, ckey, ik0, icell, cnt + 1, hk, hv,
+    HALMA_LAUNCH(link_kernel, sms * 8, 32 * kFofWarps, 0, st, rec, cst, ckey, ik0, icell, cnt + 1, cnt + 5, hk,
                  hcap - 1, g, x, y, z, parent, has, cnt + 3);
     HALMA_LAUNCH(root_kernel, g1, 256, 0, st, n, rec, parent, has, root, minidx, cnt + 3);
     HALMA_LAUNCH(label_kernel, g1, 256, 0, st, n, rec, has, root, minidx, labels, cnt + 2);

@@ -180,45 +180,66 @@ __device__ void jacobi3(const float in[3][3], float out[3]) {
     for (int i = 0; i < 3; ++i) out[i] = (float)eig[i];
 }
 
-// One thread per group: the FP32 inertia tensor in particle order (f90:183-200), its
-// normalisation, Jacobi, the decreasing sort (f90:129-157) and the square roots.
-__global__ void pr_shape_kernel(int G, const int64_t *__restrict__ off, const double *__restrict__ g, int64_t nm,
-                                const double *__restrict__ cen, double *__restrict__ out) {
-    for (int h = blockIdx.x * blockDim.x + threadIdx.x; h < G; h += gridDim.x * blockDim.x) {
+constexpr int kTile = 1024;
+
+// Block per group: the FP32 inertia tensor in particle order (f90:183-200), its
+// normalisation, Jacobi, the decreasing sort (f90:129-157) and the square roots.  Members
+// are staged in shared memory a tile at a time; the nine tensor sums and the mass sum are
+// independent chains, so threads 0..9 each add one of them in member order.
+__global__ void __launch_bounds__(256) pr_shape_kernel(int G, const int64_t *__restrict__ off,
+                                                       const double *__restrict__ g, int64_t nm,
+                                                       const double *__restrict__ cen, double *__restrict__ out) {
+    __shared__ float sr[4][kTile];   // x, y, z relative to the centre (FP32), mass
+    __shared__ float acc[10];
+    for (int h = blockIdx.x; h < G; h += gridDim.x) {
         const double *c = cen + (int64_t)h * kCenFields;
-        float it[3][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
-        float mt = 0.f;
-        for (int64_t k = off[h]; k < off[h + 1]; ++k) {
-            const float r[3] = {(float)__dsub_rn(g[k], c[0]), (float)__dsub_rn(g[nm + k], c[1]),
-                                (float)__dsub_rn(g[2 * nm + k], c[2])};
-            const float mk = (float)g[6 * nm + k];
-#pragma unroll
-            for (int j = 0; j < 3; ++j)
-#pragma unroll
-                for (int i = 0; i < 3; ++i) it[i][j] = __fadd_rn(it[i][j], __fmul_rn(__fmul_rn(mk, r[i]), r[j]));
-            mt = __fadd_rn(mt, mk);
-        }
-        for (int j = 0; j < 3; ++j)
-            for (int i = 0; i < 3; ++i) it[i][j] = __fdiv_rn(it[i][j], mt);
-        float e[3];
-        jacobi3(it, e);
-        for (int ii = 0; ii < 2; ++ii) {   // SORT_EIGEN
-            int kk = ii;
-            float v = e[ii];
-            for (int jj = ii + 1; jj < 3; ++jj)
-                if (e[jj] >= v) {
-                    kk = jj;
-                    v = e[jj];
-                }
-            if (kk != ii) {
-                e[kk] = e[ii];
-                e[ii] = v;
+        const int t = threadIdx.x;
+        float a = 0.f;   // thread t < 9: it[t % 3][t / 3]; thread 9: mass
+        for (int64_t b = off[h]; b < off[h + 1]; b += kTile) {
+            const int cnt = (off[h + 1] - b < kTile ? (int)(off[h + 1] - b) : kTile);
+            for (int q = t; q < cnt; q += blockDim.x) {
+                const int64_t k = b + q;
+                sr[0][q] = (float)__dsub_rn(g[k], c[0]);
+                sr[1][q] = (float)__dsub_rn(g[nm + k], c[1]);
+                sr[2][q] = (float)__dsub_rn(g[2 * nm + k], c[2]);
+                sr[3][q] = (float)g[6 * nm + k];
             }
+            __syncthreads();
+            if (t < 9) {
+                const int i = t % 3, j = t / 3;
+                for (int q = 0; q < cnt; ++q) a = __fadd_rn(a, __fmul_rn(__fmul_rn(sr[3][q], sr[i][q]), sr[j][q]));
+            } else if (t == 9) {
+                for (int q = 0; q < cnt; ++q) a = __fadd_rn(a, sr[3][q]);
+            }
+            __syncthreads();
         }
-        double *o = out + (int64_t)h * HALMA_PROP_NFIELDS;
-        o[HALMA_PROP_SA] = (double)__fsqrt_rn(e[0]);
-        o[HALMA_PROP_SB] = (double)__fsqrt_rn(e[1]);
-        o[HALMA_PROP_SC] = (double)__fsqrt_rn(e[2]);
+        if (t < 10) acc[t] = a;
+        __syncthreads();
+        if (t == 0) {
+            float it[3][3];
+            for (int j = 0; j < 3; ++j)
+                for (int i = 0; i < 3; ++i) it[i][j] = __fdiv_rn(acc[i + 3 * j], acc[9]);
+            float e[3];
+            jacobi3(it, e);
+            for (int ii = 0; ii < 2; ++ii) {   // SORT_EIGEN
+                int kk = ii;
+                float v = e[ii];
+                for (int jj = ii + 1; jj < 3; ++jj)
+                    if (e[jj] >= v) {
+                        kk = jj;
+                        v = e[jj];
+                    }
+                if (kk != ii) {
+                    e[kk] = e[ii];
+                    e[ii] = v;
+                }
+            }
+            double *o = out + (int64_t)h * HALMA_PROP_NFIELDS;
+            o[HALMA_PROP_SA] = (double)__fsqrt_rn(e[0]);
+            o[HALMA_PROP_SB] = (double)__fsqrt_rn(e[1]);
+            o[HALMA_PROP_SC] = (double)__fsqrt_rn(e[2]);
+        }
+        __syncthreads();
     }
 }
 
@@ -405,54 +426,108 @@ __device__ __forceinline__ int lower_bound_key(const uint64_t *__restrict__ keys
     return lo;
 }
 
-// One thread per (group, projection): the mean cell sigma over the members inside the
-// projected half-mass radius (members in order), and the V/sigma and lambda sums over the
-// group's cells with R_cell < R05 + 2 ll in the Fortran's loop order.
-__global__ void pr_proj_kernel(int G, int64_t nm, const int64_t *__restrict__ off, const double *__restrict__ g,
-                               const double *__restrict__ cen, double ll, int cbits, const int *__restrict__ rid,
-                               const float4 *__restrict__ cellv, const uint64_t *__restrict__ cellkey, int ncell,
-                               float *__restrict__ res /* G x 3 x 3: sig05, vsigma, lambda */) {
-    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < 3 * G; t += gridDim.x * blockDim.x) {
-        const int h = t / 3, a = t % 3;
+// Block per group: per projection the mean cell sigma over the members inside the projected
+// half-mass radius (members in order), and the V/sigma and lambda sums over the group's cells
+// with R_cell < R05 + 2 ll in the Fortran's loop order.  Tiles of members (then of cells) are
+// staged in shared memory by the whole block; each sum is then added in order by one thread
+// (three for the sigma sums, four per projection for the V/sigma and lambda sums).
+__global__ void __launch_bounds__(256) pr_proj_kernel(int G, int64_t nm, const int64_t *__restrict__ off,
+                                                      const double *__restrict__ g, const double *__restrict__ cen,
+                                                      double ll, int cbits, const int *__restrict__ rid,
+                                                      const float4 *__restrict__ cellv,
+                                                      const uint64_t *__restrict__ cellkey, int ncell,
+                                                      float *__restrict__ res /* G x 3 x 3 */) {
+    __shared__ float term[4][kTile];
+    __shared__ float red[12];
+    const int t = threadIdx.x;
+    for (int h = blockIdx.x; h < G; h += gridDim.x) {
         const double *c = cen + (int64_t)h * kCenFields;
         const ProjGrid p = proj_grid(c[4], ll);
         const float cx = (float)c[0], cy = (float)c[1], cz = (float)c[2];
+        float r05[3];
+        for (int a = 0; a < 3; ++a) r05[a] = res[((int64_t)h * 3 + a) * 3];
+        // mean cell sigma inside R05: term[a] = the member's cell sigma (or -1 outside)
         float s05 = 0.f;
         int cnt = 0;
-        const float r05 = (float)res[(int64_t)t * 3 + 0];   // the caller stores R05 of projection a here
-        for (int64_t k = off[h]; k < off[h + 1]; ++k) {
-            const float dx = __fsub_rn((float)g[k], cx), dy = __fsub_rn((float)g[nm + k], cy),
-                        dz = __fsub_rn((float)g[2 * nm + k], cz);
-            float d2;
-            if (a == 0) d2 = __fadd_rn(__fmul_rn(dy, dy), __fmul_rn(dz, dz));
-            else if (a == 1) d2 = __fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dz, dz));
-            else d2 = __fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy));
-            if (__fsqrt_rn(d2) < r05) {
-                s05 = __fadd_rn(s05, cellv[rid[a * nm + k]].z);
-                cnt += 1;
+        for (int64_t b = off[h]; b < off[h + 1]; b += kTile) {
+            const int nt = (off[h + 1] - b < kTile ? (int)(off[h + 1] - b) : kTile);
+            for (int q = t; q < nt; q += blockDim.x) {
+                const int64_t k = b + q;
+                const float dx = __fsub_rn((float)g[k], cx), dy = __fsub_rn((float)g[nm + k], cy),
+                            dz = __fsub_rn((float)g[2 * nm + k], cz);
+                const float d2[3] = {__fadd_rn(__fmul_rn(dy, dy), __fmul_rn(dz, dz)),
+                                     __fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dz, dz)),
+                                     __fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy))};
+                for (int a = 0; a < 3; ++a)
+                    term[a][q] = __fsqrt_rn(d2[a]) < r05[a] ? cellv[rid[a * nm + k]].z : -1.f;
             }
+            __syncthreads();
+            if (t < 3)
+                for (int q = 0; q < nt; ++q)
+                    if (term[t][q] >= 0.f) {
+                        s05 = __fadd_rn(s05, term[t][q]);
+                        cnt += 1;
+                    }
+            __syncthreads();
         }
-        if (cnt > 0) s05 = __fdiv_rn(s05, (float)cnt);
-        float sumV = 0.f, sumS = 0.f, up = 0.f, down = 0.f;
-        const float lim = __fadd_rn(r05, __fmul_rn(2.f, (float)ll));
-        const uint64_t k0 = (uint64_t)(3 * (int64_t)h + a) << cbits, k1 = (uint64_t)(3 * (int64_t)h + a + 1) << cbits;
-        for (int r = lower_bound_key(cellkey, ncell, k0); r < ncell && cellkey[r] < k1; ++r) {
-            const uint64_t cell = cellkey[r] - k0;
-            const long long inner = (long long)(cell % (uint64_t)p.n), outer = (long long)(cell / (uint64_t)p.n);
-            const float gi = grid32(p, inner), go = grid32(p, outer);
-            const float rbin = __fsqrt_rn(__fadd_rn(__fmul_rn(gi, gi), __fmul_rn(go, go)));
-            if (rbin < lim) {
-                const float4 cv = cellv[r];   // (SD, VCM, SIG)
-                sumV = __fadd_rn(sumV, __fmul_rn(__fmul_rn(cv.y, cv.y), cv.x));
-                sumS = __fadd_rn(sumS, __fmul_rn(__fmul_rn(cv.z, cv.z), cv.x));
-                up = __fadd_rn(up, __fmul_rn(__fmul_rn(cv.x, rbin), fabsf(cv.y)));
-                down = __fadd_rn(down, __fmul_rn(__fmul_rn(cv.x, rbin),
-                                                 __fsqrt_rn(__fadd_rn(__fmul_rn(cv.y, cv.y), __fmul_rn(cv.z, cv.z)))));
+        if (t < 3) red[t] = cnt > 0 ? __fdiv_rn(s05, (float)cnt) : s05;
+        __syncthreads();
+        // V/sigma and lambda per projection: term[q] of every cell of the tile (0 outside)
+        for (int a = 0; a < 3; ++a) {
+            const float lim = __fadd_rn(r05[a], __fmul_rn(2.f, (float)ll));
+            const uint64_t k0 = (uint64_t)(3 * (int64_t)h + a) << cbits, k1 = (uint64_t)(3 * (int64_t)h + a + 1) << cbits;
+            __shared__ int range[2];
+            if (t == 0) {
+                int lo = 0, hi = ncell;
+                while (lo < hi) {
+                    const int mid = (lo + hi) >> 1;
+                    if (cellkey[mid] < k0) lo = mid + 1;
+                    else hi = mid;
+                }
+                int e = lo, hi2 = ncell;
+                while (e < hi2) {
+                    const int mid = (e + hi2) >> 1;
+                    if (cellkey[mid] < k1) e = mid + 1;
+                    else hi2 = mid;
+                }
+                range[0] = lo;
+                range[1] = e;
             }
+            __syncthreads();
+            const int r0 = range[0], r1 = range[1];
+            float sum = 0.f;   // thread q < 4: sumV, sumSigma, sumUp, sumDown
+            for (int b = r0; b < r1; b += kTile) {
+                const int nt = min(kTile, r1 - b);
+                for (int q = t; q < nt; q += blockDim.x) {
+                    const int r = b + q;
+                    const uint64_t cell = cellkey[r] - k0;
+                    const float gi = grid32(p, (long long)(cell % (uint64_t)p.n)),
+                                go = grid32(p, (long long)(cell / (uint64_t)p.n));
+                    const float rbin = __fsqrt_rn(__fadd_rn(__fmul_rn(gi, gi), __fmul_rn(go, go)));
+                    const float4 cv = cellv[r];   // (SD, VCM, SIG)
+                    const bool in = rbin < lim;
+                    term[0][q] = in ? __fmul_rn(__fmul_rn(cv.y, cv.y), cv.x) : -1.f;
+                    term[1][q] = __fmul_rn(__fmul_rn(cv.z, cv.z), cv.x);
+                    term[2][q] = __fmul_rn(__fmul_rn(cv.x, rbin), fabsf(cv.y));
+                    term[3][q] = __fmul_rn(__fmul_rn(cv.x, rbin),
+                                           __fsqrt_rn(__fadd_rn(__fmul_rn(cv.y, cv.y), __fmul_rn(cv.z, cv.z))));
+                }
+                __syncthreads();
+                if (t < 4)
+                    for (int q = 0; q < nt; ++q)
+                        if (term[0][q] >= 0.f) sum = __fadd_rn(sum, term[t][q]);
+                __syncthreads();
+            }
+            if (t < 4) red[3 + t] = sum;
+            __syncthreads();
+            if (t == 0) {
+                float *o = res + ((int64_t)h * 3 + a) * 3;
+                o[0] = red[a];
+                o[1] = red[4] > 0.f ? __fsqrt_rn(__fdiv_rn(red[3], red[4])) : 0.f;
+                o[2] = red[6] > 0.f ? __fdiv_rn(red[5], red[6]) : 0.f;
+            }
+            __syncthreads();
         }
-        res[(int64_t)t * 3 + 0] = s05;
-        res[(int64_t)t * 3 + 1] = sumS > 0.f ? __fsqrt_rn(__fdiv_rn(sumV, sumS)) : 0.f;
-        res[(int64_t)t * 3 + 2] = down > 0.f ? __fdiv_rn(up, down) : 0.f;
     }
 }
 
@@ -607,7 +682,7 @@ extern "C" int halma_halo_properties(int64_t n, const double *x, const double *y
                                     red + (int64_t)r * G * HALMA_RED_NFIELDS, st));
     HALMA_LAUNCH(pr_r05_kernel, gH, 128, 0, st, G, red, dout, res);
     HALMA_LAUNCH(pr_kin_kernel, gG, 256, 0, st, G, doff, gbuf, NM, dcen, dout);
-    HALMA_LAUNCH(pr_shape_kernel, gH, 128, 0, st, G, doff, gbuf, NM, dcen, dout);
+    HALMA_LAUNCH(pr_shape_kernel, gG, 256, 0, st, G, doff, gbuf, NM, dcen, dout);
     if (N0 > 0) {
         HALMA_LAUNCH(pr_pkeys_kernel, gN, 256, 0, st, N0, G, doff, own, gbuf, dcen, linking_length, cbits, kin, vin);
         const int n3 = (int)(3 * N0);
@@ -622,8 +697,8 @@ extern "C" int halma_halo_properties(int64_t n, const double *x, const double *y
         const int ncell = last[0] + last[1];
         HALMA_LAUNCH(pr_cells_kernel, g3, 256, 0, st, n3, N0, kout, head, rpos, vout, own, gbuf, dout, cellv, cellkey,
                      rid);
-        HALMA_LAUNCH(pr_proj_kernel, grid_for(3 * G, 64), 64, 0, st, G, N0, doff, gbuf, dcen, linking_length, cbits,
-                     rid, cellv, cellkey, ncell, res);
+        HALMA_LAUNCH(pr_proj_kernel, gG, 256, 0, st, G, N0, doff, gbuf, dcen, linking_length, cbits, rid, cellv,
+                     cellkey, ncell, res);
         HALMA_LAUNCH(pr_proj_out_kernel, gH, 128, 0, st, G, res, dout);
     }
     (void)cnt;

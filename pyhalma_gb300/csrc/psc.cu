@@ -195,39 +195,72 @@ __global__ void psc_head_kernel(int64_t nl, const uint64_t *__restrict__ keys, i
         head[k] = (keys[k] != ~0ull && (k == 0 || keys[k] != keys[k - 1])) ? 1 : 0;
 }
 
-// One thread per cell (run of equal keys, members in list order): count, mass, mass-weighted
-// mean velocity, then the dispersion; every member's entry gets the cell's index.
-__global__ void psc_run_kernel(int64_t nl, const uint64_t *__restrict__ keys, const int *__restrict__ head,
-                               const int *__restrict__ runpos, const int *__restrict__ vals,
-                               const int *__restrict__ list, const int *__restrict__ mem,
+// Run starts: runstart[r] = first sorted position of cell r; runstart[nrun] = the end of the
+// last cell (entries of groups that do not sweep sort last, with key ~0); *nrun_out = nrun.
+__global__ void psc_runstart_kernel(int64_t nl, const uint64_t *__restrict__ keys, const int *__restrict__ head,
+                                    const int *__restrict__ rpos, int *__restrict__ runstart, int *__restrict__ nrun_out) {
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < nl; k += (int64_t)gridDim.x * blockDim.x) {
+        if (head[k]) runstart[rpos[k]] = (int)k;
+        if (keys[k] != ~0ull && (k + 1 == nl || keys[k + 1] == ~0ull)) {
+            runstart[rpos[k] + head[k]] = (int)(k + 1);
+            *nrun_out = rpos[k] + head[k];
+        }
+    }
+}
+
+// One warp per cell (members in list order): count, mass, mass-weighted mean velocity, then
+// the dispersion; every member's entry gets the cell's index.  The lanes load 32 members at
+// a time and all of them add the 32 values in order (shuffles), so the sums are the
+// sequential ones.
+__global__ void psc_run_kernel(const int *__restrict__ nrun_p, const int *__restrict__ runstart,
+                               const int *__restrict__ vals, const int *__restrict__ list, const int *__restrict__ mem,
                                const double *__restrict__ vx, const double *__restrict__ vy,
                                const double *__restrict__ vz, const double *__restrict__ m,
                                double4 *__restrict__ cell_v, double *__restrict__ cell_sig, int *__restrict__ rid) {
-    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < nl; k += (int64_t)gridDim.x * blockDim.x) {
-        if (!head[k]) continue;
-        const uint64_t key = keys[k];
-        int64_t e = k;
+    const int lane = threadIdx.x & 31;
+    const int nrun = *nrun_p;
+    const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    for (int64_t r = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; r < nrun; r += warps) {
+        const int b = runstart[r], e = runstart[r + 1];
         double q = 0.0, mass = 0.0, sx = 0.0, sy = 0.0, sz = 0.0;
-        for (; e < nl && keys[e] == key; ++e) {
-            const int i = mem[list[vals[e]]];
-            const double mi = m[i];
-            sx = __dadd_rn(sx, __dmul_rn(vx[i], mi));
-            sy = __dadd_rn(sy, __dmul_rn(vy[i], mi));
-            sz = __dadd_rn(sz, __dmul_rn(vz[i], mi));
-            mass = __dadd_rn(mass, mi);
-            q += 1.0;
+        for (int k0 = b; k0 < e; k0 += 32) {
+            const int k = k0 + lane;
+            double a = 0.0, c = 0.0, d = 0.0, mi = 0.0;
+            if (k < e) {
+                const int i = mem[list[vals[k]]];
+                a = vx[i];
+                c = vy[i];
+                d = vz[i];
+                mi = m[i];
+                rid[vals[k]] = (int)r;
+            }
+            const int cnt = e - k0 < 32 ? e - k0 : 32;
+            for (int t = 0; t < cnt; ++t) {
+                const double mt = __shfl_sync(0xffffffffu, mi, t);
+                sx = __dadd_rn(sx, __dmul_rn(__shfl_sync(0xffffffffu, a, t), mt));
+                sy = __dadd_rn(sy, __dmul_rn(__shfl_sync(0xffffffffu, c, t), mt));
+                sz = __dadd_rn(sz, __dmul_rn(__shfl_sync(0xffffffffu, d, t), mt));
+                mass = __dadd_rn(mass, mt);
+                q += 1.0;
+            }
         }
         const double ux = __ddiv_rn(sx, mass), uy = __ddiv_rn(sy, mass), uz = __ddiv_rn(sz, mass);
         double s2 = 0.0;
-        const int r = runpos[k];
-        for (int64_t f = k; f < e; ++f) {
-            const int i = mem[list[vals[f]]];
-            const double dx = __dsub_rn(ux, vx[i]), dy = __dsub_rn(uy, vy[i]), dz = __dsub_rn(uz, vz[i]);
-            s2 = __dadd_rn(s2, __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz)));
-            rid[vals[f]] = r;
+        for (int k0 = b; k0 < e; k0 += 32) {
+            const int k = k0 + lane;
+            double t2 = 0.0;
+            if (k < e) {
+                const int i = mem[list[vals[k]]];
+                const double dx = __dsub_rn(ux, vx[i]), dy = __dsub_rn(uy, vy[i]), dz = __dsub_rn(uz, vz[i]);
+                t2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+            }
+            const int cnt = e - k0 < 32 ? e - k0 : 32;
+            for (int t = 0; t < cnt; ++t) s2 = __dadd_rn(s2, __shfl_sync(0xffffffffu, t2, t));
         }
-        cell_v[r] = make_double4(ux, uy, uz, q);
-        cell_sig[r] = __dsqrt_rn(__ddiv_rn(__ddiv_rn(s2, 3.0), q));
+        if (lane == 0) {
+            cell_v[r] = make_double4(ux, uy, uz, q);
+            cell_sig[r] = __dsqrt_rn(__ddiv_rn(__ddiv_rn(s2, 3.0), q));
+        }
     }
 }
 
@@ -428,7 +461,7 @@ extern "C" int halma_phase_space_clean(int64_t n, const double *x, const double 
     const size_t o_own = L.add(4ull * NL), o_kin = L.add(8ull * NL), o_kout = L.add(8ull * NL);
     const size_t o_vin = L.add(4ull * NL), o_vout = L.add(4ull * NL), o_head = L.add(4ull * NL);
     const size_t o_rpos = L.add(4ull * NL), o_rid = L.add(4ull * NL), o_cv = L.add(32ull * NL);
-    const size_t o_sig = L.add(8ull * NL), o_flag = L.add(4ull * NL), o_pos = L.add(4ull * NL);
+    const size_t o_sig = L.add(8ull * NL), o_flag = L.add(4ull * (NL + 1)), o_pos = L.add(4ull * NL);
     const size_t o_w = L.add(12ull * NL), o_nw = L.add(8ull * G), o_cnt = L.add(64);
     const size_t sort_b = sort_pairs_u64_i32_bytes((int)NL, 64), scan_b = exclusive_sum_i32_bytes((int)NL);
     const size_t o_tmp = L.add(std::max(sort_b, scan_b));
@@ -499,7 +532,9 @@ extern "C" int halma_phase_space_clean(int64_t n, const double *x, const double 
                 HALMA_TRY(sort_pairs_u64_i32(tmp, sort_b, kin, kout, vin, vout, (int)nl, 64, st));
                 HALMA_LAUNCH(psc_head_kernel, gl, 256, 0, st, nl, kout, head);
                 HALMA_TRY(exclusive_sum_i32(tmp, scan_b, head, rpos, (int)nl, st));
-                HALMA_LAUNCH(psc_run_kernel, gl, 256, 0, st, nl, kout, head, rpos, vout, list, dmem, dvx, dvy, dvz, dm,
+                HALMA_CUDA(cudaMemsetAsync(cnt + 2, 0, 4, st));
+                HALMA_LAUNCH(psc_runstart_kernel, gl, 256, 0, st, nl, kout, head, rpos, flag, cnt + 2);
+                HALMA_LAUNCH(psc_run_kernel, sms * 16, 256, 0, st, cnt + 2, flag, vout, list, dmem, dvx, dvy, dvz, dm,
                              cv, csig, rid);
                 HALMA_LAUNCH(psc_sweep_kernel, gl, 256, 0, st, nl, list, own, off, dgoff, dmem, dvx, dvy, dvz, cv, csig,
                              rid, p.q_fil, p.sig_fil, state, dctl);

@@ -139,30 +139,35 @@ __global__ void __launch_bounds__(256) red_r05_kernel(const int64_t *__restrict_
     const Red r = red[h];
     const int64_t nmem = (int64_t)r.n;
     __shared__ long long first;
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const double half = 0.5 * r.mref;
     const bool given = !isnan(r.r05);   // caller supplied R05: skip the search
     if (threadIdx.x == 0) first = LLONG_MAX;
     __syncthreads();
-    if (!given && w == 0) {
+    if (!given) {
         // one running FP64 sum in increasing distance, added in order like the reference's loop
-        // (halo_properties.py:385-390): 32 masses are loaded at a time and every lane adds them
-        // one by one, so all lanes hold the same sum and leave the loop together
-        double cum = 0.0;
-        long long f = LLONG_MAX;
-        for (int64_t k0 = 0; k0 < nmem && f == LLONG_MAX; k0 += 32) {
-            const int64_t k = k0 + lane;
-            const double mk = k < nmem ? m[order[b + k]] : 0.0;
-            const int cnt = nmem - k0 < 32 ? (int)(nmem - k0) : 32;
-            for (int t = 0; t < cnt; ++t) {
-                cum = __dadd_rn(cum, __shfl_sync(0xffffffffu, mk, t));
-                if (cum > half) {
-                    f = k0 + t;
-                    break;
+        // (halo_properties.py:385-390): the block stages 1024 masses in shared memory, thread 0
+        // adds them one by one and stops at the first sum above M/2
+        __shared__ double tile[1024];
+        __shared__ double cum;
+        if (threadIdx.x == 0) cum = 0.0;
+        for (int64_t k0 = 0; k0 < nmem; k0 += 1024) {
+            const int cnt = nmem - k0 < 1024 ? (int)(nmem - k0) : 1024;
+            for (int q = threadIdx.x; q < cnt; q += blockDim.x) tile[q] = m[order[b + k0 + q]];
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                double c = cum;
+                for (int q = 0; q < cnt; ++q) {
+                    c = __dadd_rn(c, tile[q]);
+                    if (c > half) {
+                        first = k0 + q;
+                        break;
+                    }
                 }
+                cum = c;
             }
+            __syncthreads();
+            if (first != LLONG_MAX) break;
         }
-        if (lane == 0) first = f;
     }
     __syncthreads();
     __shared__ double r05s;

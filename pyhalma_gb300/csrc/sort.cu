@@ -1,6 +1,7 @@
 // Radix sorts and scans (CUB device primitives) used by FoF, groups and reductions.
 #include <cub/device/device_radix_sort.cuh>
 #include <cub/device/device_scan.cuh>
+#include <cuda/functional>
 
 #include "sort.cuh"
 
@@ -52,6 +53,17 @@ size_t exclusive_sum_i64_bytes(int n) {
 
 int exclusive_sum_i64(void *tmp, size_t tmp_bytes, const int64_t *in, int64_t *out, int n, cudaStream_t s) {
     HALMA_CUDA(cub::DeviceScan::ExclusiveSum(tmp, tmp_bytes, in, out, n, s));
+    return HALMA_OK;
+}
+
+size_t inclusive_max_i32_bytes(int n) {
+    size_t b = 0;
+    cub::DeviceScan::InclusiveScan(nullptr, b, (const int32_t *)nullptr, (int32_t *)nullptr, cuda::maximum<>{}, n);
+    return b;
+}
+
+int inclusive_max_i32(void *tmp, size_t tmp_bytes, const int32_t *in, int32_t *out, int n, cudaStream_t s) {
+    HALMA_CUDA(cub::DeviceScan::InclusiveScan(tmp, tmp_bytes, in, out, cuda::maximum<>{}, n, s));
     return HALMA_OK;
 }
 

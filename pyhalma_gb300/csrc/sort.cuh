@@ -16,6 +16,8 @@ int sort_keys_u64(void *tmp, size_t tmp_bytes, const uint64_t *kin, uint64_t *ko
                   cudaStream_t s);
 size_t exclusive_sum_i64_bytes(int n);
 int exclusive_sum_i64(void *tmp, size_t tmp_bytes, const int64_t *in, int64_t *out, int n, cudaStream_t s);
+size_t inclusive_max_i32_bytes(int n);
+int inclusive_max_i32(void *tmp, size_t tmp_bytes, const int32_t *in, int32_t *out, int n, cudaStream_t s);
 size_t exclusive_sum_i32_bytes(int n);
 int exclusive_sum_i32(void *tmp, size_t tmp_bytes, const int32_t *in, int32_t *out, int n,
                       cudaStream_t s);
