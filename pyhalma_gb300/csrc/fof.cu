@@ -153,12 +153,31 @@ __global__ void bbox_partial_kernel(const double *__restrict__ x, const double *
     }
 }
 
-__global__ void bbox_final_kernel(const double *__restrict__ part, int g, double *__restrict__ out) {
+// One block of 256 threads: the g partial boxes strided over the threads, then a tree.
+__global__ void __launch_bounds__(256) bbox_final_kernel(const double *__restrict__ part, int g,
+                                                         double *__restrict__ out) {
+    __shared__ double sh[7][8];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    double v[7];
+#pragma unroll
+    for (int q = 0; q < 7; ++q) v[q] = q < 3 ? INFINITY : -INFINITY;
+    for (int k = threadIdx.x; k < g; k += blockDim.x)
+#pragma unroll
+        for (int q = 0; q < 7; ++q) v[q] = q < 3 ? fmin(v[q], part[k * 7 + q]) : fmax(v[q], part[k * 7 + q]);
+#pragma unroll
+    for (int q = 0; q < 7; ++q) {
+        for (int o = 16; o > 0; o >>= 1) {
+            const double u = __shfl_down_sync(0xffffffffu, v[q], o);
+            v[q] = q < 3 ? fmin(v[q], u) : fmax(v[q], u);
+        }
+        if (lane == 0) sh[q][w] = v[q];
+    }
+    __syncthreads();
     if (threadIdx.x < 7) {
         const int q = threadIdx.x;
-        double v = part[q];
-        for (int k = 1; k < g; ++k) v = (q < 3) ? fmin(v, part[k * 7 + q]) : fmax(v, part[k * 7 + q]);
-        out[q] = v;
+        double r = sh[q][0];
+        for (int k = 1; k < (int)(blockDim.x >> 5); ++k) r = q < 3 ? fmin(r, sh[q][k]) : fmax(r, sh[q][k]);
+        out[q] = r;
     }
 }
 
@@ -261,6 +280,112 @@ __global__ void preunion_kernel(int n, const uint64_t *__restrict__ keys, const 
     }
 }
 
+// Dense cells (>= kDenseMin particles): the occupied 4 x 4 x 4 sub-cells of a cell (side
+// cell/4) are joined without pair tests when every pair of their points is closer than the
+// linking length: for a sub-cell offset d, the largest distance is sqrt(sum_i (|d_i|+1)^2)/4
+// cells, and offsets with sum_i (|d_i|+1)^2 <= 15 stay below 0.97 LL (the rounding of the
+// sub-cell assignment moves a point by ~1e-9 cells at most).  One warp per dense cell labels
+// its occupied sub-cells with the smallest run head of their component (min-label
+// propagation over those offsets), hooks every run head under its label (a smaller sorted
+// position, so a root stays the smallest position of its tree), marks the particles of
+// multi-particle components as having friends, and records whether the whole cell is one
+// component (conn[c]).  Smaller cells are connected when all their particles share one run.
+constexpr int kDenseMin = 32;
+
+__device__ __forceinline__ int lower_bound_key(const uint64_t *__restrict__ keys, int lo, int hi, uint64_t k) {
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (keys[mid] < k) lo = mid + 1;
+        else hi = mid;
+    }
+    return lo;
+}
+
+__global__ void __launch_bounds__(256) dense_cell_kernel(const int *__restrict__ ncell_p, const int *__restrict__ cell_start,
+                                                         const uint64_t *__restrict__ keys, int *__restrict__ parent,
+                                                         unsigned char *__restrict__ has, unsigned char *__restrict__ conn) {
+    __shared__ unsigned long long nbmask[64];   // guaranteed-link neighbours of each sub-cell (Morton codes)
+    __shared__ int lab[8][64];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (threadIdx.x < 64) {
+        const int m = threadIdx.x;
+        const int sx = (((m >> 5) & 1) << 1) | ((m >> 2) & 1), sy = (((m >> 4) & 1) << 1) | ((m >> 1) & 1),
+                  sz = (((m >> 3) & 1) << 1) | (m & 1);
+        unsigned long long mask = 0;
+        for (int dx = -2; dx <= 2; ++dx)
+            for (int dy = -2; dy <= 2; ++dy)
+                for (int dz = -2; dz <= 2; ++dz) {
+                    const int ax = abs(dx) + 1, ay = abs(dy) + 1, az = abs(dz) + 1;
+                    if ((dx | dy | dz) == 0 || ax * ax + ay * ay + az * az > 15) continue;
+                    const int tx = sx + dx, ty = sy + dy, tz = sz + dz;
+                    if (tx < 0 || tx > 3 || ty < 0 || ty > 3 || tz < 0 || tz > 3) continue;
+                    const int t = ((tx >> 1) << 5) | ((ty >> 1) << 4) | ((tz >> 1) << 3) | ((tx & 1) << 2) |
+                                  ((ty & 1) << 1) | (tz & 1);
+                    mask |= 1ull << t;
+                }
+        nbmask[m] = mask;
+    }
+    __syncthreads();
+    const int nc = *ncell_p;
+    const int warps = gridDim.x * (blockDim.x >> 5);
+    for (int c = blockIdx.x * (blockDim.x >> 5) + w; c < nc; c += warps) {
+        const int cs = cell_start[c], ce = cell_start[c + 1], cnt = ce - cs;
+        if (cnt < kDenseMin) {
+            if (lane == 0) conn[c] = keys[cs] == keys[ce - 1] ? 1 : 0;
+            continue;
+        }
+        const uint64_t ck = keys[cs] & ~63ull;   // the cell's key with the sub-cell bits cleared
+        int lo[2], hi[2];
+        bool occ[2];
+        for (int r = 0; r < 2; ++r) {
+            const int m = lane + 32 * r;
+            lo[r] = lower_bound_key(keys, cs, ce, ck | (uint64_t)m);
+            hi[r] = lower_bound_key(keys, lo[r], ce, (ck | (uint64_t)m) + 1);
+            occ[r] = hi[r] > lo[r];
+            lab[w][m] = occ[r] ? lo[r] : INT_MAX;
+        }
+        const unsigned long long occm = (unsigned long long)__ballot_sync(0xffffffffu, occ[0]) |
+                                        ((unsigned long long)__ballot_sync(0xffffffffu, occ[1]) << 32);
+        __syncwarp();
+        for (int round = 0; round < 64; ++round) {   // converges in a few rounds
+            bool changed = false;
+            for (int r = 0; r < 2; ++r) {
+                const int m = lane + 32 * r;
+                if (!occ[r]) continue;
+                int v = lab[w][m];
+                unsigned long long nb = nbmask[m] & occm;
+                while (nb) {
+                    const int t = __ffsll((long long)nb) - 1;
+                    nb &= nb - 1;
+                    v = min(v, lab[w][t]);
+                }
+                if (v < lab[w][m]) {
+                    lab[w][m] = v;
+                    changed = true;
+                }
+            }
+            __syncwarp();
+            if (!__any_sync(0xffffffffu, changed)) break;
+        }
+        int mn = INT_MAX;
+        for (int r = 0; r < 2; ++r)
+            if (occ[r]) mn = min(mn, lab[w][lane + 32 * r]);
+        for (int o = 16; o > 0; o >>= 1) mn = min(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+        const bool one = __all_sync(0xffffffffu, (!occ[0] || lab[w][lane] == mn) && (!occ[1] || lab[w][lane + 32] == mn));
+        for (int r = 0; r < 2; ++r) {
+            if (!occ[r]) continue;
+            const int m = lane + 32 * r, L = lab[w][m];
+            if (L != lo[r]) parent[lo[r]] = L;   // run head under the component's smallest run head
+            int members = 0;                     // occupied sub-cells in this component
+            for (int t = 0; t < 64; ++t) members += lab[w][t] == L ? 1 : 0;
+            if (members > 1 || hi[r] - lo[r] > 1)
+                for (int q = lo[r]; q < hi[r]; ++q) has[q] = 1;
+        }
+        if (lane == 0) conn[c] = one ? 1 : 0;
+        __syncwarp();
+    }
+}
+
 // Cell table + hash insert, from the exclusive scan of the run heads.
 // Hash slot: cell key, first sorted position and particle count of the cell, so that a
 // neighbour lookup is one 16-byte load per probe.
@@ -298,13 +423,15 @@ __global__ void cells_kernel(int n, int sb, const uint64_t *__restrict__ keys, c
     }
 }
 
+// count carries the cell's "one component" flag (conn) in bit 31.
 __global__ void slot_fill_kernel(const int *__restrict__ ncell_p, const int *__restrict__ cell_start,
-                                 const int *__restrict__ cell_slot, CellSlot *__restrict__ slots) {
+                                 const int *__restrict__ cell_slot, const unsigned char *__restrict__ conn,
+                                 CellSlot *__restrict__ slots) {
     const int nc = *ncell_p;
     for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x) {
         CellSlot &sl = slots[cell_slot[c]];
         sl.start = cell_start[c];
-        sl.count = cell_start[c + 1] - cell_start[c];
+        sl.count = (cell_start[c + 1] - cell_start[c]) | (conn[c] ? (int)0x80000000u : 0);
     }
 }
 
@@ -365,10 +492,11 @@ __constant__ int c_stencil[13][3] = {{0, 0, 1},  {0, 1, -1}, {0, 1, 0},  {0, 1, 
 // into the home cell's frame when it is loaded.
 constexpr int kHomeSeg = 13;
 
-__global__ void __launch_bounds__(256) link_kernel(
+__global__ void __launch_bounds__(256, 6) link_kernel(
     const float4 *__restrict__ rec, const int *__restrict__ cell_start, const uint64_t *__restrict__ cell_key,
     const int *__restrict__ item_k0, const int *__restrict__ item_cell, const int *__restrict__ nitems_p,
-    int *item_counter, const CellSlot *__restrict__ slots, uint64_t hmask, FofGeom g,
+    int *item_counter, const CellSlot *__restrict__ slots, const unsigned char *__restrict__ conn,
+    uint64_t hmask, FofGeom g,
     const double *__restrict__ x, const double *__restrict__ y, const double *__restrict__ z,
     int *parent, unsigned char *has, int *err) {
     __shared__ float4 buf[kFofWarps][32];
@@ -393,6 +521,7 @@ __global__ void __launch_bounds__(256) link_kernel(
         decode_key(cell_key[c], g, cx, cy, cz);
         // lane s < 13 owns stencil cell s, lane 13 the rest of the home cell
         int sjs = 0, sn = 0, soff = 0x15;   // soff: stencil offset + 1 per axis, 2 bits each
+        bool sconn = false;                 // the segment's cell is one component
         if (lane < 13) {
             soff = (c_stencil[lane][0] + 1) | (c_stencil[lane][1] + 1) << 2 | (c_stencil[lane][2] + 1) << 4;
             const long long nx = cx + c_stencil[lane][0], ny = cy + c_stencil[lane][1], nz = cz + c_stencil[lane][2];
@@ -400,9 +529,10 @@ __global__ void __launch_bounds__(256) link_kernel(
                 const uint64_t nkey = ((uint64_t)nx * (uint64_t)g.ncy + (uint64_t)ny) * (uint64_t)g.ncz + (uint64_t)nz;
                 const int2 sc = hash_lookup(slots, hmask, nkey);
                 sjs = sc.x;
-                sn = sc.y;
+                sn = sc.y & 0x7fffffff;
+                sconn = sc.y < 0;
             }
-        } else if (lane == kHomeSeg) {
+        } else if (lane == kHomeSeg && !conn[c]) {   // a cell that is one component has no new pair inside
             sjs = k0 + 1;
             sn = ce - sjs;
         }
@@ -427,7 +557,33 @@ __global__ void __launch_bounds__(256) link_kernel(
             }
         }
         int myroot = hv ? uf_find_cached(parent, k, err) : -1;
-        for (int v0 = 0; v0 < total; v0 += 32) {
+        int next = 0;
+        for (int v0 = 0; v0 < total; v0 = next) {
+            next = v0 + 32;
+            // a round starting in a neighbour cell that is one component, already in the set of a
+            // home chunk that is itself in one set, skips the rest of that cell
+            {
+                int seg0 = 0;   // the segment holding candidate v0 (over all 14 segments)
+#pragma unroll
+                for (int s = 0; s <= kHomeSeg; ++s)
+                    if (__shfl_sync(0xffffffffu, spre, s) <= v0) seg0 = s;
+                const int n0 = __shfl_sync(0xffffffffu, sn, seg0);
+                const int js = __shfl_sync(0xffffffffu, sjs, seg0);
+                const int end0 = __shfl_sync(0xffffffffu, spre, seg0) + n0;
+                if (seg0 < kHomeSeg && n0 >= 16 && end0 > v0 && __shfl_sync(0xffffffffu, (int)sconn, seg0)) {
+                    if (v0 > 0 && hv) myroot = uf_find_cached(parent, k, err);
+                    const int r0 = __shfl_sync(0xffffffffu, myroot, 0);
+                    if (__all_sync(0xffffffffu, !hv || myroot == r0)) {
+                        int rr = -1;
+                        if (lane == 0) rr = uf_find_cached(parent, js, err);
+                        rr = __shfl_sync(0xffffffffu, rr, 0);
+                        if (rr == r0) {
+                            next = end0;   // > v0: the loop always moves forward
+                            continue;
+                        }
+                    }
+                }
+            }
             const int v = v0 + lane;
             bool cv = v < total;
             // segment of candidate v: the last segment starting at or before v (empty
@@ -677,7 +833,7 @@ int fof_core(int n, const double *x, const double *y, const double *z, FofGeom g
     const size_t o_hk = M.add(16ull * hcap), o_hv = M.add(4ull * n);   // hash slots, slot of each cell
     const size_t o_flag = M.add(4ull * n), o_ipos = M.add(4ull * n);
     const size_t o_ik0 = M.add(4ull * n), o_icell = M.add(4ull * n);
-    const size_t o_cnt = M.add(64);
+    const size_t o_cnt = M.add(64), o_conn = M.add(1ull * n);
     const size_t o_tmp = M.add(std::max(sort_b, scan_b));
     void *base = nullptr;
     HALMA_TRY(workspace(M.total, &base, st));
@@ -709,12 +865,19 @@ int fof_core(int n, const double *x, const double *y, const double *z, FofGeom g
     }
     HALMA_TRY(exclusive_sum_i32(tmp, scan_b, head, cpos, n, st));
     HALMA_LAUNCH(cells_kernel, g1, 256, 0, st, n, g.sb, kout, head, cpos, cst, ckey, hk, hv, hcap - 1, cnt + 0);
-    HALMA_LAUNCH(slot_fill_kernel, g1, 256, 0, st, cnt + 0, cst, hv, hk);
+    // one-component cells (sub-cells in the key and a positive linking length only)
+    unsigned char *conn = at<unsigned char>(base, o_conn);
+    if (g.sb != 0 && g.lo > 0.f) {
+        HALMA_LAUNCH(dense_cell_kernel, sms * 8, 256, 0, st, cnt + 0, cst, kout, parent, has, conn);
+    } else {
+        HALMA_CUDA(cudaMemsetAsync(conn, 0, n, st));
+    }
+    HALMA_LAUNCH(slot_fill_kernel, g1, 256, 0, st, cnt + 0, cst, hv, conn, hk);
     HALMA_LAUNCH(itemflag_kernel, g1, 256, 0, st, n, head, cpos, cst, flag);
     HALMA_TRY(exclusive_sum_i32(tmp, scan_b, flag, ipos, n, st));
     HALMA_LAUNCH(items_kernel, g1, 256, 0, st, n, head, cpos, flag, ipos, ik0, icell, cnt + 1);
     HALMA_LAUNCH(link_kernel, sms * 8, 32 * kFofWarps, 0, st, rec, cst, ckey, ik0, icell, cnt + 1, cnt + 5, hk,
-                 hcap - 1, g, x, y, z, parent, has, cnt + 3);
+                 conn, hcap - 1, g, x, y, z, parent, has, cnt + 3);
     HALMA_LAUNCH(root_kernel, g1, 256, 0, st, n, rec, parent, has, root, minidx, cnt + 3);
     HALMA_LAUNCH(label_kernel, g1, 256, 0, st, n, rec, has, root, minidx, labels, cnt + 2);
     int hc[4];
@@ -737,7 +900,7 @@ int bbox_device(int n, const double *x, const double *y, const double *z, double
     void *base = nullptr;
     HALMA_TRY(workspace(L.total, &base, st));
     HALMA_LAUNCH(bbox_partial_kernel, gb, 256, 0, st, x, y, z, n, at<double>(base, o_part));
-    HALMA_LAUNCH(bbox_final_kernel, 1, 32, 0, st, at<double>(base, o_part), gb, at<double>(base, o_out));
+    HALMA_LAUNCH(bbox_final_kernel, 1, 256, 0, st, at<double>(base, o_part), gb, at<double>(base, o_out));
     HALMA_CUDA(cudaMemcpyAsync(bb, at<double>(base, o_out), 7 * sizeof(double), cudaMemcpyDeviceToHost, st));
     HALMA_CUDA(cudaStreamSynchronize(st));
     return HALMA_OK;
