@@ -376,43 +376,65 @@ __global__ void pr_head_kernel(int64_t n, const uint64_t *__restrict__ keys, int
         head[k] = (k == 0 || keys[k] != keys[k - 1]) ? 1 : 0;
 }
 
-// One thread per cell: FP32 mass SD, mass-weighted velocity VCM (then / SD), count, and
-// sigma = sqrt(sum (v - VCM)^2 / count), members in order; rid[member entry] = cell.
-__global__ void pr_cells_kernel(int64_t n3, int64_t nm, const uint64_t *__restrict__ keys,
-                                const int *__restrict__ head, const int *__restrict__ rpos,
-                                const int *__restrict__ vals, const int *__restrict__ owner,
-                                const double *__restrict__ g, const double *__restrict__ out,
-                                float4 *__restrict__ cellv, uint64_t *__restrict__ cellkey, int *__restrict__ rid) {
+// Cell starts: runstart[r] = first sorted entry of cell r, runstart[ncell] = n3.
+__global__ void pr_runstart_kernel(int64_t n3, const int *__restrict__ head, const int *__restrict__ rpos,
+                                   int *__restrict__ runstart) {
     for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n3; k += (int64_t)gridDim.x * blockDim.x) {
-        if (!head[k]) continue;
-        const uint64_t key = keys[k];
-        const int a = vals[k] / (int)nm;   // projection of the run
-        int64_t e = k;
+        if (head[k]) runstart[rpos[k]] = (int)k;
+        if (k == n3 - 1) runstart[rpos[k] + head[k]] = (int)n3;
+    }
+}
+
+// One warp per cell: FP32 mass SD, mass-weighted velocity VCM (then / SD), count, and
+// sigma = sqrt(sum (v - VCM)^2 / count), members in order: the lanes load 32 members at a
+// time and every lane adds them one by one (shuffles), so the sums are the sequential ones;
+// rid[member entry] = cell.
+__global__ void pr_cells_kernel(int ncell, int64_t nm, const int *__restrict__ runstart,
+                                const uint64_t *__restrict__ keys, const int *__restrict__ vals,
+                                const int *__restrict__ owner, const double *__restrict__ g,
+                                const double *__restrict__ out, float4 *__restrict__ cellv,
+                                uint64_t *__restrict__ cellkey, int *__restrict__ rid) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    for (int64_t r = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; r < ncell; r += warps) {
+        const int b = runstart[r], e = runstart[r + 1];
+        const int a = vals[b] / (int)nm;   // projection of the cell
         float sd = 0.f, vc = 0.f;
-        int q = 0;
-        for (; e < n3 && keys[e] == key; ++e) {
-            const int mk = vals[e] - a * (int)nm;
-            const double *o = out + (int64_t)owner[mk] * HALMA_PROP_NFIELDS;
-            const float v = (float)__dsub_rn(g[(3 + a) * nm + mk], o[HALMA_PROP_VX + a]);
-            const float m = (float)g[6 * nm + mk];
-            vc = __fadd_rn(vc, __fmul_rn(v, m));
-            sd = __fadd_rn(sd, m);
-            q += 1;
+        for (int k0 = b; k0 < e; k0 += 32) {
+            const int k = k0 + lane;
+            float v = 0.f, m = 0.f;
+            if (k < e) {
+                const int mk = vals[k] - a * (int)nm;
+                const double *o = out + (int64_t)owner[mk] * HALMA_PROP_NFIELDS;
+                v = (float)__dsub_rn(g[(3 + a) * nm + mk], o[HALMA_PROP_VX + a]);
+                m = (float)g[6 * nm + mk];
+                rid[vals[k]] = (int)r;
+            }
+            const int cnt = e - k0 < 32 ? e - k0 : 32;
+            for (int t = 0; t < cnt; ++t) {
+                const float vt = __shfl_sync(0xffffffffu, v, t), mt = __shfl_sync(0xffffffffu, m, t);
+                vc = __fadd_rn(vc, __fmul_rn(vt, mt));
+                sd = __fadd_rn(sd, mt);
+            }
         }
         if (sd != 0.f) vc = __fdiv_rn(vc, sd);
         float s2 = 0.f;
-        const int r = rpos[k];
-        for (int64_t f = k; f < e; ++f) {
-            const int mk = vals[f] - a * (int)nm;
-            const double *o = out + (int64_t)owner[mk] * HALMA_PROP_NFIELDS;
-            const float v = (float)__dsub_rn(g[(3 + a) * nm + mk], o[HALMA_PROP_VX + a]);
-            const float d = __fsub_rn(v, vc);
-            s2 = __fadd_rn(s2, __fmul_rn(d, d));
-            rid[vals[f]] = r;
+        for (int k0 = b; k0 < e; k0 += 32) {
+            const int k = k0 + lane;
+            float d2 = 0.f;
+            if (k < e) {
+                const int mk = vals[k] - a * (int)nm;
+                const double *o = out + (int64_t)owner[mk] * HALMA_PROP_NFIELDS;
+                const float d = __fsub_rn((float)__dsub_rn(g[(3 + a) * nm + mk], o[HALMA_PROP_VX + a]), vc);
+                d2 = __fmul_rn(d, d);
+            }
+            const int cnt = e - k0 < 32 ? e - k0 : 32;
+            for (int t = 0; t < cnt; ++t) s2 = __fadd_rn(s2, __shfl_sync(0xffffffffu, d2, t));
         }
-        const float sig = __fsqrt_rn(__fdiv_rn(s2, (float)q));
-        cellv[r] = make_float4(sd, vc, sig, 0.f);
-        cellkey[r] = key;
+        if (lane == 0) {
+            cellv[r] = make_float4(sd, vc, __fsqrt_rn(__fdiv_rn(s2, (float)(e - b))), 0.f);
+            cellkey[r] = keys[b];
+        }
     }
 }
 
@@ -635,7 +657,7 @@ extern "C" int halma_halo_properties(int64_t n, const double *x, const double *y
     sg.plan(L);
     const size_t o_g = L.add(64ull * NM), o_ab = L.add(8ull * 4 * G * HALMA_ABOUT_NFIELDS);
     const size_t o_red = L.add(8ull * 4 * G * HALMA_RED_NFIELDS), o_own = L.add(4ull * NM);
-    const size_t o_kin = L.add(8ull * N3), o_kout = L.add(8ull * N3), o_vin = L.add(4ull * N3),
+    const size_t o_kin = L.add(8ull * N3), o_kout = L.add(8ull * N3), o_vin = L.add(4ull * (N3 + 1)),
                  o_vout = L.add(4ull * N3);
     const size_t o_head = L.add(4ull * N3), o_rpos = L.add(4ull * N3), o_rid = L.add(4ull * N3);
     const size_t o_cv = L.add(16ull * N3), o_ck = L.add(8ull * N3), o_res = L.add(4ull * 9 * G), o_cnt = L.add(64);
@@ -695,8 +717,10 @@ extern "C" int halma_halo_properties(int64_t n, const double *x, const double *y
         HALMA_CUDA(cudaMemcpyAsync(&last[1], head + n3 - 1, 4, cudaMemcpyDeviceToHost, st));
         HALMA_CUDA(cudaStreamSynchronize(st));
         const int ncell = last[0] + last[1];
-        HALMA_LAUNCH(pr_cells_kernel, g3, 256, 0, st, n3, N0, kout, head, rpos, vout, own, gbuf, dout, cellv, cellkey,
-                     rid);
+        int *runstart = vin;   // the sort's input values are no longer needed
+        HALMA_LAUNCH(pr_runstart_kernel, g3, 256, 0, st, n3, head, rpos, runstart);
+        HALMA_LAUNCH(pr_cells_kernel, sms * 16, 256, 0, st, ncell, N0, runstart, kout, vout, own, gbuf, dout, cellv,
+                     cellkey, rid);
         HALMA_LAUNCH(pr_proj_kernel, gG, 256, 0, st, G, N0, doff, gbuf, dcen, linking_length, cbits, rid, cellv,
                      cellkey, ncell, res);
         HALMA_LAUNCH(pr_proj_out_kernel, gH, 128, 0, st, G, res, dout);

@@ -155,14 +155,28 @@ __global__ void __launch_bounds__(256) red_r05_kernel(const int64_t *__restrict_
             for (int q = threadIdx.x; q < cnt; q += blockDim.x) tile[q] = m[order[b + k0 + q]];
             __syncthreads();
             if (threadIdx.x == 0) {
+                // eight masses at a time: the loads and the chain of adds do not wait on each
+                // other's branches; the first sum above M/2 is found after each batch
                 double c = cum;
-                for (int q = 0; q < cnt; ++q) {
-                    c = __dadd_rn(c, tile[q]);
-                    if (c > half) {
-                        first = k0 + q;
-                        break;
-                    }
+                long long f = LLONG_MAX;
+                int q = 0;
+                for (; q + 8 <= cnt && f == LLONG_MAX; q += 8) {
+                    double t[8], cs[8];
+#pragma unroll
+                    for (int u = 0; u < 8; ++u) t[u] = tile[q + u];
+                    cs[0] = __dadd_rn(c, t[0]);
+#pragma unroll
+                    for (int u = 1; u < 8; ++u) cs[u] = __dadd_rn(cs[u - 1], t[u]);
+#pragma unroll
+                    for (int u = 7; u >= 0; --u)
+                        if (cs[u] > half) f = k0 + q + u;
+                    c = cs[7];
                 }
+                for (; q < cnt && f == LLONG_MAX; ++q) {
+                    c = __dadd_rn(c, tile[q]);
+                    if (c > half) f = k0 + q;
+                }
+                if (f != LLONG_MAX) first = f;
                 cum = c;
             }
             __syncthreads();

@@ -1254,16 +1254,30 @@ __global__ void ub_output_kernel(int nh, const HaloState *__restrict__ hs, doubl
     }
 }
 
+// The passes are captured in chunks of kPassChunk (the first chunk also holds the reduction
+// and packing); one graph per chunk start, all cached for the same problem shape.
+constexpr int kPassChunk = 8;
 struct GraphCache {
-    cudaGraphExec_t exec = nullptr;
+    struct Entry {
+        cudaGraphExec_t exec = nullptr;
+        int64_t nodes = 0;
+    };
+    std::vector<Entry> chunks;   // by chunk start / kPassChunk
     std::vector<uintptr_t> key;
     cudaStream_t capture_stream = nullptr;
     int capture_device = -1;
-    int64_t nodes = 0;
 };
 GraphCache &graph_cache() {
     static GraphCache g;
     return g;
+}
+
+// Number of haloes still active after a chunk of passes (the host stops replaying at 0).
+__global__ void ub_active_kernel(int nh, const HaloState *__restrict__ hs, int *__restrict__ count) {
+    int a = 0;
+    for (int h = blockIdx.x * blockDim.x + threadIdx.x; h < nh; h += gridDim.x * blockDim.x) a += hs[h].active;
+    for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
+    if ((threadIdx.x & 31) == 0 && a) atomicAdd(count, a);
 }
 
 }  // namespace
@@ -1429,15 +1443,17 @@ int unbind_device(int64_t n, int nh, const int64_t *d_off, const int64_t *h_off,
         HALMA_CUDA(cudaFuncSetAttribute(ub_pair_sym_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSymSmem));
         HALMA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, ub_pair_sym_kernel, 256, kSymSmem));
         const int ygrid = device_sm_count() * std::max(bps, 1);
-        auto record = [&](cudaStream_t rs) -> int {
+        auto record = [&](cudaStream_t rs, int it0, int it1) -> int {
             // first pass: centre of mass and packing into buffer 0; every pass then compacts
             // its survivors into the other buffer and sets the next pass's halo state
-            HALMA_TRY(reduce(rs, 0));
-            if (nchunks > 0)
-                HALMA_LAUNCH(ub_pack_kernel<float4>, nchunks, kSegThreads, 0, rs, off, dpoff, dcst, dchh, x, y, z, m,
-                             vx, vy, vz, hs, pkb[0], pvb[0], pidxb[0]);
+            if (it0 == 0) {
+                HALMA_TRY(reduce(rs, 0));
+                if (nchunks > 0)
+                    HALMA_LAUNCH(ub_pack_kernel<float4>, nchunks, kSegThreads, 0, rs, off, dpoff, dcst, dchh, x, y, z,
+                                 m, vx, vy, vz, hs, pkb[0], pvb[0], pidxb[0]);
+            }
             float4 *rk = at<float4>(base, o_rk);
-            for (int it = 0; it < p.max_iter; ++it) {
+            for (int it = it0; it < it1; ++it) {
                 const int a = it & 1, b = a ^ 1;
                 const int inc = (it > 0 && incremental) ? 1 : 0;
                 HALMA_LAUNCH(ub_items_kernel, 1, 1024, 0, rs, nh, dorder, hs, tab, slice_len, inc, 1, istart, ystart,
@@ -1460,14 +1476,17 @@ int unbind_device(int64_t n, int nh, const int64_t *d_off, const int64_t *h_off,
                 HALMA_LAUNCH(ub_compact_df_kernel, sgrid, kSegThreads, 0, rs, sstart, sown, idesc, cnt + 2, dpoff, hs,
                              keepf, segpre, pkb[a], pvb[a], pidxb[a], phic2, pkb[b], pvb[b], pidxb[b], phin2, rk);
             }
+            HALMA_CUDA(cudaMemsetAsync(cnt + 6, 0, sizeof(int), rs));
+            HALMA_LAUNCH(ub_active_kernel, std::min(grid_for(nh, 256), 64), 256, 0, rs, nh, hs, cnt + 6);
             return HALMA_OK;
         };
+        int passes_run = p.max_iter;
         if (p.use_graph) {
             std::vector<uintptr_t> key = {(uintptr_t)base, (uintptr_t)off, (uintptr_t)x, (uintptr_t)y, (uintptr_t)z,
                                           (uintptr_t)vx, (uintptr_t)vy, (uintptr_t)vz, (uintptr_t)m,
                                           (uintptr_t)bound, (uintptr_t)phi_out, (uintptr_t)n, (uintptr_t)nh,
                                           (uintptr_t)p.max_iter, (uintptr_t)st};
-            uint64_t eb, gb;
+            uint64_t eb = 0, gb = 0;
             memcpy(&eb, &eps2, sizeof(float));
             memcpy(&gb, &gfac, sizeof(double));
             key.push_back((uintptr_t)eb);
@@ -1485,37 +1504,51 @@ int unbind_device(int64_t n, int nh, const int64_t *d_off, const int64_t *h_off,
                 key.push_back((uintptr_t)tab.t[c]);
             }
             GraphCache &gc = graph_cache();
-            if (!gc.exec || gc.key != key) {
-                if (gc.exec) {
-                    cudaGraphExecDestroy(gc.exec);
-                    gc.exec = nullptr;
-                }
-                // capture on a private stream (the legacy default stream cannot be captured)
-                if (!gc.capture_stream || gc.capture_device != current_device()) {
-                    HALMA_CUDA(cudaStreamCreateWithFlags(&gc.capture_stream, cudaStreamNonBlocking));
-                    gc.capture_device = current_device();
-                }
-                cudaGraph_t graph = nullptr;
-                HALMA_CUDA(cudaStreamBeginCapture(gc.capture_stream, cudaStreamCaptureModeThreadLocal));
-                const int64_t before = halma_kernel_launch_count();
-                int s = record(gc.capture_stream);
-                cudaError_t ce = cudaStreamEndCapture(gc.capture_stream, &graph);
-                if (s != HALMA_OK) {
-                    if (graph) cudaGraphDestroy(graph);
-                    return s;
-                }
-                HALMA_CUDA(ce);
-                cudaError_t ie = cudaGraphInstantiate(&gc.exec, graph, 0);
-                cudaGraphDestroy(graph);
-                HALMA_CUDA(ie);
+            if (gc.key != key) {
+                for (auto &e : gc.chunks)
+                    if (e.exec) cudaGraphExecDestroy(e.exec);
+                gc.chunks.clear();
                 gc.key = key;
-                gc.nodes = halma_kernel_launch_count() - before;
-                add_launches(-gc.nodes);   // counted again at every replay below
             }
-            HALMA_CUDA(cudaGraphLaunch(gc.exec, st));
-            add_launches(gc.nodes);
+            // capture on a private stream (the legacy default stream cannot be captured)
+            if (!gc.capture_stream || gc.capture_device != current_device()) {
+                HALMA_CUDA(cudaStreamCreateWithFlags(&gc.capture_stream, cudaStreamNonBlocking));
+                gc.capture_device = current_device();
+            }
+            const int nchunk = (p.max_iter + kPassChunk - 1) / kPassChunk;
+            gc.chunks.resize(nchunk);
+            passes_run = 0;
+            for (int ci = 0; ci < nchunk; ++ci) {
+                const int it0 = ci * kPassChunk, it1 = std::min(p.max_iter, it0 + kPassChunk);
+                GraphCache::Entry &ge = gc.chunks[ci];
+                if (!ge.exec) {
+                    cudaGraph_t graph = nullptr;
+                    HALMA_CUDA(cudaStreamBeginCapture(gc.capture_stream, cudaStreamCaptureModeThreadLocal));
+                    const int64_t before = halma_kernel_launch_count();
+                    int s = record(gc.capture_stream, it0, it1);
+                    cudaError_t ce = cudaStreamEndCapture(gc.capture_stream, &graph);
+                    if (s != HALMA_OK) {
+                        if (graph) cudaGraphDestroy(graph);
+                        return s;
+                    }
+                    HALMA_CUDA(ce);
+                    cudaError_t ie = cudaGraphInstantiate(&ge.exec, graph, 0);
+                    cudaGraphDestroy(graph);
+                    HALMA_CUDA(ie);
+                    ge.nodes = halma_kernel_launch_count() - before;
+                    add_launches(-ge.nodes);   // counted again at every replay below
+                }
+                HALMA_CUDA(cudaGraphLaunch(ge.exec, st));
+                add_launches(ge.nodes);
+                passes_run = it1;
+                if (it1 >= p.max_iter) break;
+                int active = 0;
+                HALMA_CUDA(cudaMemcpyAsync(&active, cnt + 6, sizeof(int), cudaMemcpyDeviceToHost, st));
+                HALMA_CUDA(cudaStreamSynchronize(st));
+                if (active == 0) break;
+            }
         } else {
-            HALMA_TRY(record(st));
+            HALMA_TRY(record(st, 0, p.max_iter));
         }
         // the halo state already holds the final bound set's mass, centre and bulk velocity
         if (profiling) {
@@ -1524,7 +1557,7 @@ int unbind_device(int64_t n, int nh, const int64_t *d_off, const int64_t *h_off,
                                        cudaMemcpyDeviceToHost, st));
             HALMA_CUDA(cudaStreamSynchronize(st));
             prof.passes.clear();
-            for (int it = 0; it < p.max_iter; ++it) {
+            for (int it = 0; it < passes_run; ++it) {
                 float ms = 0.f, sms = 0.f;
                 HALMA_CUDA(cudaEventElapsedTime(&ms, prof.ev0[it], prof.ev1[it]));
                 HALMA_CUDA(cudaEventElapsedTime(&sms, prof.ev0[it], prof.evm[it]));
