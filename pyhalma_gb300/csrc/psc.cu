@@ -225,24 +225,25 @@ __global__ void psc_run_kernel(const int *__restrict__ nrun_p, const int *__rest
         double q = 0.0, mass = 0.0, sx = 0.0, sy = 0.0, sz = 0.0;
         for (int k0 = b; k0 < e; k0 += 32) {
             const int k = k0 + lane;
+            // the products v*m do not depend on the sums: each lane forms its own, then the
+            // warp adds them in order (the FP64 pipe is the limit here)
             double a = 0.0, c = 0.0, d = 0.0, mi = 0.0;
             if (k < e) {
                 const int i = mem[list[vals[k]]];
-                a = vx[i];
-                c = vy[i];
-                d = vz[i];
                 mi = m[i];
+                a = __dmul_rn(vx[i], mi);
+                c = __dmul_rn(vy[i], mi);
+                d = __dmul_rn(vz[i], mi);
                 rid[vals[k]] = (int)r;
             }
             const int cnt = e - k0 < 32 ? e - k0 : 32;
             for (int t = 0; t < cnt; ++t) {
-                const double mt = __shfl_sync(0xffffffffu, mi, t);
-                sx = __dadd_rn(sx, __dmul_rn(__shfl_sync(0xffffffffu, a, t), mt));
-                sy = __dadd_rn(sy, __dmul_rn(__shfl_sync(0xffffffffu, c, t), mt));
-                sz = __dadd_rn(sz, __dmul_rn(__shfl_sync(0xffffffffu, d, t), mt));
-                mass = __dadd_rn(mass, mt);
-                q += 1.0;
+                sx = __dadd_rn(sx, __shfl_sync(0xffffffffu, a, t));
+                sy = __dadd_rn(sy, __shfl_sync(0xffffffffu, c, t));
+                sz = __dadd_rn(sz, __shfl_sync(0xffffffffu, d, t));
+                mass = __dadd_rn(mass, __shfl_sync(0xffffffffu, mi, t));
             }
+            q += (double)cnt;
         }
         const double ux = __ddiv_rn(sx, mass), uy = __ddiv_rn(sy, mass), uz = __ddiv_rn(sz, mass);
         double s2 = 0.0;
