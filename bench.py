@@ -337,6 +337,25 @@ def run_gpu(args):
         t64 = e0.elapsed_time(e1)
         fp64 = {"value": n / (t64 * 1e-3), "unit": "particles/s", "ms_per_step": t64,
                 "speedup_fp32c_vs_fp64": t64 / statistics.mean(ms)}
+        # potential error of the batched FP32C path against the plain FP64 path, per halo:
+        # one pass over every group (all members), phi of the members both paths keep bound
+        from pyhalma_gb300.unbinding import unbind_batched
+        midx = cat.members.long()
+        garr = [a[midx].contiguous() for a in dev_in]
+        _, _, p32 = unbind_batched(cat.offsets, *garr, UnbindOptions(eps=opt.eps, max_iter=1, precision="fp32c"),
+                                   want_phi=True)
+        _, _, p64 = unbind_batched(cat.offsets, *garr, UnbindOptions(eps=opt.eps, max_iter=1, precision="fp64"),
+                                   want_phi=True)
+        p32, p64, off_h = p32.cpu().numpy(), p64.cpu().numpy(), cat.offsets.cpu().numpy()
+        per_halo = []
+        for h in range(len(off_h) - 1):
+            a, b = p32[off_h[h]:off_h[h + 1]], p64[off_h[h]:off_h[h + 1]]
+            both = (a != 0) & (b != 0)
+            if both.any():
+                per_halo.append(float(np.max(np.abs(a[both] / b[both] - 1.0))))
+        fp64["potential_rel_err_vs_fp64"] = {"per_halo_max": float(np.max(per_halo)),
+                                             "per_halo_median": float(np.median(per_halo)),
+                                             "haloes": len(per_halo), "bound": 1e-6}
 
     hbm, sm_max, src = peaks()
     sms = torch.cuda.get_device_properties(dev).multi_processor_count

@@ -119,74 +119,104 @@ __device__ __forceinline__ void uf_union(int *parent, int a, int b, int *err) {
     }
 }
 
+// Doubles as order-preserving signed 64-bit integers (sign-magnitude turned into two's
+// complement), so that a bounding box is integer min / max: GB300 issues FP64 instructions at
+// a small fraction of its integer rate.  -0.0 orders just below +0.0; NaN and infinities are
+// flagged separately.
+__device__ __forceinline__ long long ord_of(double v) {
+    const long long u = __double_as_longlong(v);
+    return u ^ ((u >> 63) & 0x7fffffffffffffffll);
+}
+
+__device__ __forceinline__ double val_of(long long k) {
+    return __longlong_as_double(k ^ ((k >> 63) & 0x7fffffffffffffffll));
+}
+
+__device__ __forceinline__ bool nonfinite(double v) {
+    return (__double_as_longlong(v) & 0x7ff0000000000000ll) == 0x7ff0000000000000ll;
+}
+
+// part[7 * block + q]: the block's min x, y, z and max x, y, z as order keys, and a non-finite flag.
 __global__ void bbox_partial_kernel(const double *__restrict__ x, const double *__restrict__ y,
-                                    const double *__restrict__ z, int n, double *__restrict__ part) {
-    double mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
-    double bad = 0.0;
+                                    const double *__restrict__ z, int n, long long *__restrict__ part) {
+    long long mn[3] = {LLONG_MAX, LLONG_MAX, LLONG_MAX}, mx[3] = {LLONG_MIN, LLONG_MIN, LLONG_MIN};
+    bool bad = false;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const double v[3] = {x[i], y[i], z[i]};
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
-            if (!isfinite(v[d])) bad = 1.0;
-            mn[d] = fmin(mn[d], v[d]);
-            mx[d] = fmax(mx[d], v[d]);
+            bad |= nonfinite(v[d]);
+            const long long k = ord_of(v[d]);
+            mn[d] = min(mn[d], k);
+            mx[d] = max(mx[d], k);
         }
     }
-    __shared__ double sh[7][32];
+    __shared__ long long sh[7][32];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    double vals[7] = {mn[0], mn[1], mn[2], mx[0], mx[1], mx[2], bad};
+    long long vals[7] = {mn[0], mn[1], mn[2], mx[0], mx[1], mx[2], __any_sync(0xffffffffu, bad) ? 1ll : 0ll};
 #pragma unroll
     for (int q = 0; q < 7; ++q) {
-        double v = vals[q];
+        long long v = vals[q];
         for (int o = 16; o > 0; o >>= 1) {
-            const double u = __shfl_down_sync(0xffffffffu, v, o);
-            v = (q < 3) ? fmin(v, u) : fmax(v, u);
+            const long long u = __shfl_down_sync(0xffffffffu, v, o);
+            v = (q < 3) ? min(v, u) : max(v, u);
         }
         if (lane == 0) sh[q][w] = v;
     }
     __syncthreads();
     if (threadIdx.x < 7) {
         const int q = threadIdx.x;
-        double v = sh[q][0];
-        for (int k = 1; k < (int)(blockDim.x >> 5); ++k) v = (q < 3) ? fmin(v, sh[q][k]) : fmax(v, sh[q][k]);
+        long long v = sh[q][0];
+        for (int k = 1; k < (int)(blockDim.x >> 5); ++k) v = (q < 3) ? min(v, sh[q][k]) : max(v, sh[q][k]);
         part[blockIdx.x * 7 + q] = v;
     }
 }
 
-// One block of 256 threads: the g partial boxes strided over the threads, then a tree.
-__global__ void __launch_bounds__(256) bbox_final_kernel(const double *__restrict__ part, int g,
+// One block of 256 threads: the g partial boxes strided over the threads, then a tree; out =
+// min x, y, z, max x, y, z as doubles and 1.0 if any coordinate is not finite.
+__global__ void __launch_bounds__(256) bbox_final_kernel(const long long *__restrict__ part, int g,
                                                          double *__restrict__ out) {
-    __shared__ double sh[7][8];
+    __shared__ long long sh[7][8];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    double v[7];
+    long long v[7];
 #pragma unroll
-    for (int q = 0; q < 7; ++q) v[q] = q < 3 ? INFINITY : -INFINITY;
+    for (int q = 0; q < 7; ++q) v[q] = q < 3 ? LLONG_MAX : LLONG_MIN;
     for (int k = threadIdx.x; k < g; k += blockDim.x)
 #pragma unroll
-        for (int q = 0; q < 7; ++q) v[q] = q < 3 ? fmin(v[q], part[k * 7 + q]) : fmax(v[q], part[k * 7 + q]);
+        for (int q = 0; q < 7; ++q) v[q] = q < 3 ? min(v[q], part[k * 7 + q]) : max(v[q], part[k * 7 + q]);
 #pragma unroll
     for (int q = 0; q < 7; ++q) {
         for (int o = 16; o > 0; o >>= 1) {
-            const double u = __shfl_down_sync(0xffffffffu, v[q], o);
-            v[q] = q < 3 ? fmin(v[q], u) : fmax(v[q], u);
+            const long long u = __shfl_down_sync(0xffffffffu, v[q], o);
+            v[q] = q < 3 ? min(v[q], u) : max(v[q], u);
         }
         if (lane == 0) sh[q][w] = v[q];
     }
     __syncthreads();
     if (threadIdx.x < 7) {
         const int q = threadIdx.x;
-        double r = sh[q][0];
-        for (int k = 1; k < (int)(blockDim.x >> 5); ++k) r = q < 3 ? fmin(r, sh[q][k]) : fmax(r, sh[q][k]);
-        out[q] = r;
+        long long r = sh[q][0];
+        for (int k = 1; k < (int)(blockDim.x >> 5); ++k) r = q < 3 ? min(r, sh[q][k]) : max(r, sh[q][k]);
+        out[q] = q < 6 ? val_of(r) : (r ? 1.0 : 0.0);
     }
 }
 
 // Sort key: row-major cell index, then (when there is room) the particle's 4 x 4 x 4 sub-cell in
 // Morton order, so that each 32-particle chunk of a crowded cell is spatially compact.  The
-// order of particles inside a cell does not change the partition.
+// order of particles inside a cell does not change the partition.  The kernel also writes the
+// particle's position inside its cell in units of the linking length (pre[i], in input order,
+// with the index in .w), so that the sorted records are one 16-byte gather.
+//
+// Cell coordinates: t = 4 * (x - origin) / cell is evaluated as one FMA, x * (4 / cell) -
+// origin * (4 / cell); the cell is floor(t) >> 2 and the sub-cell floor(t) & 3.  Any rounding
+// here is harmless as long as it is the same for every particle: the cell side is
+// ll * (1 + 2^-20), so two points within ll of each other stay in the same or adjacent cells
+// whenever the cell coordinate's error is below 2^-21 cells (it is ~1e-12 cells).
 __global__ void keys_kernel(const double *__restrict__ x, const double *__restrict__ y,
                             const double *__restrict__ z, int n, FofGeom g, SegGeom sg,
-                            uint64_t *__restrict__ keys, int *__restrict__ vals) {
+                            uint64_t *__restrict__ keys, int *__restrict__ vals, float4 *__restrict__ pre) {
+    const double s4 = 4.0 * g.inv_cell;   // exact: a power-of-two scaling
+    const float cs4 = 0.25f * g.cs;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         double ox = g.xmin, oy = g.ymin, oz = g.zmin;
         long long x0 = 0, nx = g.ncx, ny = g.ncy, nz = g.ncz;
@@ -200,24 +230,27 @@ __global__ void keys_kernel(const double *__restrict__ x, const double *__restri
             ny = sg.scol[4 * s + 2];
             nz = sg.scol[4 * s + 3];
         }
-        const double tx = (x[i] - ox) * g.inv_cell;
-        const double ty = (y[i] - oy) * g.inv_cell;
-        const double tz = (z[i] - oz) * g.inv_cell;
-        long long cx = (long long)floor(tx), cy = (long long)floor(ty), cz = (long long)floor(tz);
-        cx = min(max(cx, 0ll), nx - 1);
-        cy = min(max(cy, 0ll), ny - 1);
-        cz = min(max(cz, 0ll), nz - 1);
+        const double tx = fma(x[i], s4, -ox * s4);
+        const double ty = fma(y[i], s4, -oy * s4);
+        const double tz = fma(z[i], s4, -oz * s4);
+        // quarter-cell coordinates, clamped to the grid (rounding can put a point on the
+        // grid's edge a hair outside it)
+        const long long qx = min(max(__double2ll_rd(tx), 0ll), 4 * nx - 1);
+        const long long qy = min(max(__double2ll_rd(ty), 0ll), 4 * ny - 1);
+        const long long qz = min(max(__double2ll_rd(tz), 0ll), 4 * nz - 1);
+        const long long cx = qx >> 2, cy = qy >> 2, cz = qz >> 2;
         uint64_t key = ((uint64_t)(x0 + cx) * (uint64_t)g.ncy + (uint64_t)cy) * (uint64_t)g.ncz + (uint64_t)cz;
         if (g.sb) {
-            const int sx = min(3, max(0, (int)((tx - (double)cx) * 4.0)));
-            const int sy = min(3, max(0, (int)((ty - (double)cy) * 4.0)));
-            const int sz = min(3, max(0, (int)((tz - (double)cz) * 4.0)));
+            const int sx = (int)(qx & 3), sy = (int)(qy & 3), sz = (int)(qz & 3);
             const int mort = ((sx >> 1) << 5) | ((sy >> 1) << 4) | ((sz >> 1) << 3) | ((sx & 1) << 2) |
                              ((sy & 1) << 1) | (sz & 1);
             key = (key << 6) | (uint64_t)mort;
         }
         keys[i] = key;
         vals[i] = i;
+        // t - 4 * cell is exact (Sterbenz: both within a factor of two, or the cell is 0)
+        pre[i] = make_float4((float)(tx - (double)(cx << 2)) * cs4, (float)(ty - (double)(cy << 2)) * cs4,
+                             (float)(tz - (double)(cz << 2)) * cs4, __int_as_float(i));
     }
 }
 
@@ -230,30 +263,13 @@ __device__ __forceinline__ void decode_key(uint64_t key, const FofGeom &g, long 
 }
 
 // Sorted records, run heads, union-find / label initialisation.
-__global__ void prep_kernel(const double *__restrict__ x, const double *__restrict__ y,
-                            const double *__restrict__ z, int n, FofGeom g, SegGeom sg,
-                            const uint64_t *__restrict__ keys, const int *__restrict__ idx,
-                            float4 *__restrict__ rec, int *__restrict__ head, int *__restrict__ parent,
-                            unsigned char *__restrict__ has, int *__restrict__ minidx) {
+__global__ void prep_kernel(int n, int sb, const uint64_t *__restrict__ keys, const int *__restrict__ idx,
+                            const float4 *__restrict__ pre, float4 *__restrict__ rec, int *__restrict__ head,
+                            int *__restrict__ parent, unsigned char *__restrict__ has, int *__restrict__ minidx) {
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
-        const uint64_t key = keys[k] >> g.sb;
-        long long cx, cy, cz;
-        decode_key(key, g, cx, cy, cz);
-        const int i = idx[k];
-        double x0 = g.xmin, y0 = g.ymin, z0 = g.zmin;
-        if (sg.seg_of) {   // the segment's own origin and first column
-            const int s = sg.seg_of[i];
-            x0 = sg.smin[3 * s];
-            y0 = sg.smin[3 * s + 1];
-            z0 = sg.smin[3 * s + 2];
-            cx -= sg.scol[4 * s];
-        }
-        const double ox = x0 + (double)cx * g.cell;
-        const double oy = y0 + (double)cy * g.cell;
-        const double oz = z0 + (double)cz * g.cell;
-        rec[k] = make_float4((float)((x[i] - ox) * g.inv_scale), (float)((y[i] - oy) * g.inv_scale),
-                             (float)((z[i] - oz) * g.inv_scale), __int_as_float(i));
-        head[k] = (k == 0 || (keys[k - 1] >> g.sb) != key) ? 1 : 0;
+        const uint64_t key = keys[k] >> sb;
+        rec[k] = pre[idx[k]];
+        head[k] = (k == 0 || (keys[k - 1] >> sb) != key) ? 1 : 0;
         parent[k] = k;
         has[k] = 0;
         minidx[k] = INT_MAX;
@@ -394,17 +410,43 @@ struct __align__(16) CellSlot {
     int start, count;
 };
 
+// First probe slot of a cell key: runs of 8 consecutive keys (8 neighbouring cells along z)
+// share one scattered block of 8 slots (128 bytes), so that the z-neighbours a warp looks up
+// together mostly fall in one cache line.
+__device__ __forceinline__ uint64_t slot_of(uint64_t key, uint64_t hmask) {
+    return ((mix64(key >> 3) << 3) | (key & 7)) & hmask;
+}
+
+// Hash capacity from the number of occupied cells: the smallest power of two >= 2 x cells, at
+// least 1024 slots and at most the cap_max allocated; kept on the device as a mask.
+__global__ void hash_size_kernel(int n, const int *__restrict__ head, const int *__restrict__ cellpos,
+                                 unsigned long long cap_max, unsigned long long *__restrict__ hmask) {
+    const unsigned long long nc = (unsigned long long)(cellpos[n - 1] + head[n - 1]);
+    unsigned long long cap = 1024;
+    while (cap < 2 * nc && cap < cap_max) cap <<= 1;
+    *hmask = (cap < cap_max ? cap : cap_max) - 1;
+}
+
+__global__ void hash_clear_kernel(const unsigned long long *__restrict__ hmask_p, CellSlot *__restrict__ slots) {
+    const unsigned long long cap = *hmask_p + 1;
+    for (unsigned long long s = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; s < cap;
+         s += (unsigned long long)gridDim.x * blockDim.x)
+        reinterpret_cast<ulonglong2 *>(slots)[s] = make_ulonglong2(kEmptyKey, 0ull);
+}
+
 __global__ void cells_kernel(int n, int sb, const uint64_t *__restrict__ keys, const int *__restrict__ head,
                              const int *__restrict__ cellpos, int *__restrict__ cell_start,
                              uint64_t *__restrict__ cell_key, CellSlot *__restrict__ slots,
-                             int *__restrict__ cell_slot, uint64_t hmask, int *__restrict__ ncell) {
+                             int *__restrict__ cell_slot, const unsigned long long *__restrict__ hmask_p,
+                             int *__restrict__ ncell) {
+    const uint64_t hmask = *hmask_p;
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
         if (head[k]) {
             const int c = cellpos[k];
             const uint64_t key = keys[k] >> sb;
             cell_start[c] = k;
             cell_key[c] = key;
-            uint64_t h = mix64(key) & hmask;
+            uint64_t h = slot_of(key, hmask);
             for (uint64_t probe = 0; probe <= hmask; ++probe) {
                 const unsigned long long prev =
                     atomicCAS(&slots[h].key, (unsigned long long)kEmptyKey, (unsigned long long)key);
@@ -458,7 +500,7 @@ __global__ void items_kernel(int n, const int *__restrict__ head, const int *__r
 
 // (start, count) of the cell with this key, count 0 when it holds no particle.
 __device__ __forceinline__ int2 hash_lookup(const CellSlot *__restrict__ slots, uint64_t hmask, uint64_t key) {
-    uint64_t h = mix64(key) & hmask;
+    uint64_t h = slot_of(key, hmask);
     for (uint64_t probe = 0; probe <= hmask; ++probe) {
         const ulonglong2 v = __ldg(reinterpret_cast<const ulonglong2 *>(slots + h));
         if (v.x == key) return make_int2((int)(v.y & 0xffffffffull), (int)(v.y >> 32));
@@ -496,7 +538,7 @@ __global__ void __launch_bounds__(256, 6) link_kernel(
     const float4 *__restrict__ rec, const int *__restrict__ cell_start, const uint64_t *__restrict__ cell_key,
     const int *__restrict__ item_k0, const int *__restrict__ item_cell, const int *__restrict__ nitems_p,
     int *item_counter, const CellSlot *__restrict__ slots, const unsigned char *__restrict__ conn,
-    uint64_t hmask, FofGeom g,
+    const unsigned long long *__restrict__ hmask_p, FofGeom g,
     const double *__restrict__ x, const double *__restrict__ y, const double *__restrict__ z,
     int *parent, unsigned char *has, int *err) {
     __shared__ float4 buf[kFofWarps][32];
@@ -504,6 +546,7 @@ __global__ void __launch_bounds__(256, 6) link_kernel(
     __shared__ int jbuf[kFofWarps][32];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int nitems = *nitems_p;
+    const uint64_t hmask = *hmask_p;
     // items come from a counter: their cost varies by orders of magnitude (dense cores)
     for (;;) {
         int item = 0;
@@ -646,13 +689,31 @@ __global__ void __launch_bounds__(256, 6) link_kernel(
     }
 }
 
+// Root of every sorted position, and per root the smallest original index of its members.
+// Consecutive sorted positions mostly share a root (a cell, a group), so the lanes of a warp
+// first take the minimum per distinct root and issue one atomicMin each.  The loop runs the
+// same number of rounds on every lane of a warp (blockDim.x is a multiple of 32).
 __global__ void root_kernel(int n, const float4 *__restrict__ rec, int *parent,
                             const unsigned char *__restrict__ has, int *__restrict__ root,
                             int *__restrict__ minidx, int *err) {
-    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
-        const int r = uf_find(parent, k, err);
-        root[k] = r;
-        if (has[k]) atomicMin(minidx + r, __float_as_int(rec[k].w));
+    const int lane = threadIdx.x & 31;
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k - lane < n;
+         k += (int64_t)gridDim.x * blockDim.x) {
+        int r = -1, v = INT_MAX;
+        if (k < n) {
+            r = uf_find(parent, (int)k, err);
+            root[k] = r;
+            if (has[k]) v = __float_as_int(rec[k].w);
+        }
+        unsigned todo = __ballot_sync(0xffffffffu, v != INT_MAX);
+        while (todo) {
+            const int rl = __shfl_sync(0xffffffffu, r, __ffs(todo) - 1);
+            const bool mine = r == rl && v != INT_MAX;
+            const int m = __reduce_min_sync(0xffffffffu, mine ? v : INT_MAX);
+            const unsigned grp = __ballot_sync(0xffffffffu, mine);
+            if (lane == __ffs(grp) - 1) atomicMin(minidx + rl, m);
+            todo &= ~grp;
+        }
     }
 }
 
@@ -685,26 +746,27 @@ __global__ void __launch_bounds__(256) seg_bbox_kernel(int nseg, const int64_t *
                                                        const double *__restrict__ x, const double *__restrict__ y,
                                                        const double *__restrict__ z, double *__restrict__ sbox,
                                                        unsigned long long *__restrict__ ext_bits, int *__restrict__ bad) {
-    __shared__ double sh[6][8];
+    __shared__ long long sh[6][8];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     for (int s = blockIdx.x; s < nseg; s += gridDim.x) {
-        double mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
+        long long mn[3] = {LLONG_MAX, LLONG_MAX, LLONG_MAX}, mx[3] = {LLONG_MIN, LLONG_MIN, LLONG_MIN};
         bool nf = false;
         for (int64_t i = off[s] + threadIdx.x; i < off[s + 1]; i += blockDim.x) {
             const double v[3] = {x[i], y[i], z[i]};
 #pragma unroll
             for (int d = 0; d < 3; ++d) {
-                nf |= !isfinite(v[d]);
-                mn[d] = fmin(mn[d], v[d]);
-                mx[d] = fmax(mx[d], v[d]);
+                nf |= nonfinite(v[d]);
+                const long long k = ord_of(v[d]);
+                mn[d] = min(mn[d], k);
+                mx[d] = max(mx[d], k);
             }
         }
         if (__any_sync(0xffffffffu, nf) && lane == 0) atomicOr(bad, 1);
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
             for (int o = 16; o > 0; o >>= 1) {
-                mn[d] = fmin(mn[d], __shfl_xor_sync(0xffffffffu, mn[d], o));
-                mx[d] = fmax(mx[d], __shfl_xor_sync(0xffffffffu, mx[d], o));
+                mn[d] = min(mn[d], __shfl_xor_sync(0xffffffffu, mn[d], o));
+                mx[d] = max(mx[d], __shfl_xor_sync(0xffffffffu, mx[d], o));
             }
             if (lane == 0) {
                 sh[d][w] = mn[d];
@@ -714,17 +776,20 @@ __global__ void __launch_bounds__(256) seg_bbox_kernel(int nseg, const int64_t *
         __syncthreads();
         if (threadIdx.x < 6) {
             const int q = threadIdx.x;
-            double v = sh[q][0];
-            for (int k = 1; k < (int)(blockDim.x >> 5); ++k) v = q < 3 ? fmin(v, sh[q][k]) : fmax(v, sh[q][k]);
+            long long v = sh[q][0];
+            for (int k = 1; k < (int)(blockDim.x >> 5); ++k) v = q < 3 ? min(v, sh[q][k]) : max(v, sh[q][k]);
             sh[q][0] = v;
         }
         __syncthreads();
         if (threadIdx.x == 0) {
-            double e = 0.0;
+            const bool empty = off[s + 1] <= off[s];
+            double b[6];
 #pragma unroll
-            for (int q = 0; q < 6; ++q) sbox[6 * (int64_t)s + q] = sh[q][0];
-            if (off[s + 1] > off[s])
-                e = fmax(sh[3][0] - sh[0][0], fmax(sh[4][0] - sh[1][0], sh[5][0] - sh[2][0]));
+            for (int q = 0; q < 6; ++q) {
+                b[q] = empty ? (q < 3 ? INFINITY : -INFINITY) : val_of(sh[q][0]);
+                sbox[6 * (int64_t)s + q] = b[q];
+            }
+            const double e = empty ? 0.0 : fmax(b[3] - b[0], fmax(b[4] - b[1], b[5] - b[2]));
             if (isfinite(e) && e > 0.0) atomicMax(ext_bits, (unsigned long long)__double_as_longlong(e));
         }
         __syncthreads();
@@ -818,14 +883,14 @@ int fof_core(int n, const double *x, const double *y, const double *z, FofGeom g
     const int end_bit = cell_bits + g.sb;
     const int sms = device_sm_count();
 
-    uint64_t hcap = 1;
+    uint64_t hcap = 1024;   // slots allocated; the kernels use a power of two >= 2 x cells of it
     while (hcap < 2ull * (uint64_t)n) hcap <<= 1;
     const size_t sort_b = sort_pairs_u64_i32_bytes(n, end_bit);
     const size_t scan_b = std::max(exclusive_sum_i32_bytes(n), inclusive_max_i32_bytes(n));
     Layout M;
     const size_t o_kin = M.add(8ull * n), o_kout = M.add(8ull * n);
     const size_t o_vin = M.add(4ull * n), o_vout = M.add(4ull * n);
-    const size_t o_rec = M.add(16ull * n);
+    const size_t o_rec = M.add(16ull * n), o_pre = M.add(16ull * n);
     const size_t o_head = M.add(4ull * n), o_cpos = M.add(4ull * n);
     const size_t o_par = M.add(4ull * n), o_has = M.add(1ull * n), o_root = M.add(4ull * n);
     const size_t o_min = M.add(4ull * n);
@@ -839,7 +904,7 @@ int fof_core(int n, const double *x, const double *y, const double *z, FofGeom g
     HALMA_TRY(workspace(M.total, &base, st));
     auto *kin = at<uint64_t>(base, o_kin), *kout = at<uint64_t>(base, o_kout);
     auto *vin = at<int>(base, o_vin), *vout = at<int>(base, o_vout);
-    auto *rec = at<float4>(base, o_rec);
+    auto *rec = at<float4>(base, o_rec), *pre = at<float4>(base, o_pre);
     auto *head = at<int>(base, o_head), *cpos = at<int>(base, o_cpos);
     auto *parent = at<int>(base, o_par), *root = at<int>(base, o_root), *minidx = at<int>(base, o_min);
     auto *has = at<unsigned char>(base, o_has);
@@ -850,21 +915,23 @@ int fof_core(int n, const double *x, const double *y, const double *z, FofGeom g
     auto *flag = at<int>(base, o_flag), *ipos = at<int>(base, o_ipos);
     auto *ik0 = at<int>(base, o_ik0), *icell = at<int>(base, o_icell);
     int *cnt = at<int>(base, o_cnt);   // [0] ncell [1] nitems [2] ngroups [3] err [5] link item counter
+    auto *hmask = reinterpret_cast<unsigned long long *>(cnt + 6);   // [6..7] hash slot mask
     void *tmp = at<void>(base, o_tmp);
     const int g1 = std::min(sms * 8, grid_for(n, 256));
 
     HALMA_CUDA(cudaMemsetAsync(cnt, 0, 64, st));
-    HALMA_CUDA(cudaMemsetAsync(hk, 0xff, 16ull * hcap, st));
-    HALMA_LAUNCH(keys_kernel, g1, 256, 0, st, x, y, z, n, g, sg, kin, vin);
+    HALMA_LAUNCH(keys_kernel, g1, 256, 0, st, x, y, z, n, g, sg, kin, vin, pre);
     HALMA_TRY(sort_pairs_u64_i32(tmp, sort_b, kin, kout, vin, vout, n, end_bit, st));
-    HALMA_LAUNCH(prep_kernel, g1, 256, 0, st, x, y, z, n, g, sg, kout, vout, rec, head, parent, has, minidx);
+    HALMA_LAUNCH(prep_kernel, g1, 256, 0, st, n, g.sb, kout, vout, pre, rec, head, parent, has, minidx);
     if (g.sb != 0 && g.lo > 0.f) {   // sub-cells in the key and a positive linking length
         HALMA_LAUNCH(subrun_kernel, g1, 256, 0, st, n, kout, flag);
         HALMA_TRY(inclusive_max_i32(tmp, scan_b, flag, root, n, st));
         HALMA_LAUNCH(preunion_kernel, g1, 256, 0, st, n, kout, root, parent, has);
     }
     HALMA_TRY(exclusive_sum_i32(tmp, scan_b, head, cpos, n, st));
-    HALMA_LAUNCH(cells_kernel, g1, 256, 0, st, n, g.sb, kout, head, cpos, cst, ckey, hk, hv, hcap - 1, cnt + 0);
+    HALMA_LAUNCH(hash_size_kernel, 1, 1, 0, st, n, head, cpos, (unsigned long long)hcap, hmask);
+    HALMA_LAUNCH(hash_clear_kernel, g1, 256, 0, st, hmask, hk);
+    HALMA_LAUNCH(cells_kernel, g1, 256, 0, st, n, g.sb, kout, head, cpos, cst, ckey, hk, hv, hmask, cnt + 0);
     // one-component cells (sub-cells in the key and a positive linking length only)
     unsigned char *conn = at<unsigned char>(base, o_conn);
     if (g.sb != 0 && g.lo > 0.f) {
@@ -877,7 +944,7 @@ int fof_core(int n, const double *x, const double *y, const double *z, FofGeom g
     HALMA_TRY(exclusive_sum_i32(tmp, scan_b, flag, ipos, n, st));
     HALMA_LAUNCH(items_kernel, g1, 256, 0, st, n, head, cpos, flag, ipos, ik0, icell, cnt + 1);
     HALMA_LAUNCH(link_kernel, sms * 8, 32 * kFofWarps, 0, st, rec, cst, ckey, ik0, icell, cnt + 1, cnt + 5, hk,
-                 conn, hcap - 1, g, x, y, z, parent, has, cnt + 3);
+                 conn, hmask, g, x, y, z, parent, has, cnt + 3);
     HALMA_LAUNCH(root_kernel, g1, 256, 0, st, n, rec, parent, has, root, minidx, cnt + 3);
     HALMA_LAUNCH(label_kernel, g1, 256, 0, st, n, rec, has, root, minidx, labels, cnt + 2);
     int hc[4];
@@ -899,8 +966,8 @@ int bbox_device(int n, const double *x, const double *y, const double *z, double
     const size_t o_out = L.add(sizeof(double) * 8);
     void *base = nullptr;
     HALMA_TRY(workspace(L.total, &base, st));
-    HALMA_LAUNCH(bbox_partial_kernel, gb, 256, 0, st, x, y, z, n, at<double>(base, o_part));
-    HALMA_LAUNCH(bbox_final_kernel, 1, 256, 0, st, at<double>(base, o_part), gb, at<double>(base, o_out));
+    HALMA_LAUNCH(bbox_partial_kernel, gb, 256, 0, st, x, y, z, n, at<long long>(base, o_part));
+    HALMA_LAUNCH(bbox_final_kernel, 1, 256, 0, st, at<long long>(base, o_part), gb, at<double>(base, o_out));
     HALMA_CUDA(cudaMemcpyAsync(bb, at<double>(base, o_out), 7 * sizeof(double), cudaMemcpyDeviceToHost, st));
     HALMA_CUDA(cudaStreamSynchronize(st));
     return HALMA_OK;

@@ -122,3 +122,21 @@ def test_empty_inputs(cuda):
         halo_gas.balls_inside(np.ones(3), np.ones(3), np.ones(3), [0.0], [0.0], [0.0], [-1.0])
     with pytest.raises(ValueError):
         halo_gas.balls_inside(np.ones(3), np.ones(3), np.ones(3), [np.nan], [0.0], [0.0], [1.0])
+
+
+@pytest.mark.gpu
+def test_duplicates_and_zero_radius(cuda):
+    """Repeated points and a zero radius centred on a particle: every copy of that particle is
+    inside (d^2 = 0 <= 0), nothing else; strict mode keeps nothing at R = 0."""
+    from pyhalma_gb300 import halo_gas
+    rng = np.random.default_rng(5)
+    base = rng.uniform(0, 0.01, (2000, 3))
+    pts = np.concatenate([base, base[:300], base[:10]])
+    x, y, z = (np.ascontiguousarray(pts[:, q]) for q in range(3))
+    c = pts[3]
+    got = halo_gas.query_ball_point(x, y, z, c, 0.0)
+    assert np.array_equal(got, og.query_ball_point(x, y, z, c, 0.0)) and len(got) == 3
+    off, idx = halo_gas.balls_inside(x, y, z, [c[0]], [c[1]], [c[2]], [0.0], strict=True)
+    assert len(idx) == 0
+    for R in (1e-4, 1e-3, 5e-3):
+        assert np.array_equal(halo_gas.query_ball_point(x, y, z, c, R), og.query_ball_point(x, y, z, c, R))

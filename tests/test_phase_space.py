@@ -97,3 +97,24 @@ def test_edge_groups(cuda):
             assert all(np.array_equal(a, b) for a, b in zip(got[k], ref[k]))
     with pytest.raises(ValueError):
         phase_space.phase_space_cleaning([np.array([0, n])], x, y, z, vx, vy, vz, m, 0.0015, 1.0, 3.0, True, 1)
+
+
+@pytest.mark.gpu
+def test_groups_that_clean_away(cuda):
+    """Q_FIL above every cell count drops every particle in the first sweep (remaining 0:
+    empty final grid), and SIG_FIL 0 drops particles in later sweeps too; both paths against
+    the oracle."""
+    from pyhalma_gb300 import phase_space
+    rng = np.random.default_rng(12)
+    n = 3000
+    x, y, z = rng.normal(0, 0.003, (3, n))
+    vx, vy, vz = rng.normal(0, 80, (3, n))
+    m = rng.uniform(0.5, 2.0, n)
+    groups = [np.arange(0, 1200), np.arange(1200, 3000)]
+    for q_fil, sig_fil in ((1e9, 3.0), (1.0, 0.0), (2.0, 0.3)):
+        got = phase_space.phase_space_cleaning(groups, x, y, z, vx, vy, vz, m, 0.0015, q_fil, sig_fil, True, 1)
+        ref = ops.phase_space_cleaning(groups, x, y, z, vx, vy, vz, m, 0.0015, q_fil, sig_fil, True, 1)
+        assert [g.tolist() for g in got["new_groups"]] == [g.tolist() for g in ref["new_groups"]]
+        assert list(got["num_particles"]) == list(ref["num_particles"])
+        for k in ("which_x", "which_y", "which_z"):
+            assert all(np.array_equal(a, b) for a, b in zip(got[k], ref[k]))

@@ -103,3 +103,44 @@ def test_gpu_property_loop_on_cleaned_groups(cuda):
         sp = op.sigma_projections_fortran(grid, len(grid), pl, *arrays[:6], ux, uy, uz, s.mass, cx, cy, cz, *rp,
                                           0.0015)
         assert tuple(res[k][h] for k in ("sig_1D_x", "sig_1D_y", "sig_1D_z", "vsigma", "lambda_ensellem")) == sp
+
+
+def _same(a, b):
+    """Equal value for value (float32 widened exactly), NaN equal to NaN."""
+    return np.array_equal(np.asarray(a, dtype=np.float64), np.asarray(b, dtype=np.float64), equal_nan=True)
+
+
+@pytest.mark.gpu
+def test_tiny_groups(cuda):
+    """One- and two-member groups: the projections of a single cell, an empty Tully-Fisher
+    shell (NaN here, ZeroDivisionError in the reference), shape of a degenerate tensor."""
+    from pyhalma_gb300 import halo_properties
+    x = np.array([0.10, 0.1004, 0.3, 0.3002, 0.3001])
+    y = np.array([0.20, 0.2003, 0.1, 0.1001, 0.1003])
+    z = np.array([0.00, 0.0001, 0.5, 0.5004, 0.4999])
+    vx, vy, vz = np.array([[10.0, -20.0, 5.0, 7.0, -3.0], [1.0, 2.0, 3.0, 4.0, 5.0], [0.0, 1.0, -1.0, 2.0, -2.0]])
+    m = np.array([1.0, 2.0, 1.0, 1.0, 3.0])
+    groups = [np.array([0]), np.array([0, 1]), np.array([2, 3, 4])]
+    cen = []
+    for g in groups:
+        M = m[g].sum()
+        c = [(m[g] * a[g]).sum() / M for a in (x, y, z)]
+        r = np.sqrt((c[0] - x[g]) ** 2 + (c[1] - y[g]) ** 2 + (c[2] - z[g]) ** 2).max()
+        cen.append(c + [M, r])
+    off = np.array([0, 1, 3, 6])
+    t = halo_properties.halo_property_table(off, np.concatenate(groups), x, y, z, vx, vy, vz, m, np.array(cen), 0.0015)
+    from pyhalma_gb300 import _lib
+    F = {k: i for i, k in enumerate(_lib.PROP_FIELDS)}
+    for h, g in enumerate(groups):
+        cx, cy, cz, M, rmax = cen[h]
+        r05 = half_mass_radius(cx, cy, cz, M, g, x, y, z, m)
+        assert t[h, F["r05"]] == r05
+        sa, sb, sc = op.halo_shape_fortran(g, x, y, z, m, cx, cy, cz, r05)
+        assert _same((t[h, F["a"]], t[h, F["b"]], t[h, F["c"]]), (sa, sb, sc))
+        ux, uy, uz = CM_velocity(M, g, vx, vy, vz, m)
+        rp = op.half_mass_radius_proj(cx, cy, cz, M, g, x, y, z, m)
+        grid = np.arange(-(rmax + 0.0015), rmax + 0.0015, 2 * 0.0015)
+        sp = op.sigma_projections_fortran(grid, len(grid), g, x, y, z, vx, vy, vz, ux, uy, uz, m, cx, cy, cz, *rp,
+                                          0.0015)
+        assert _same(tuple(t[h, F[k]] for k in ("sig_1d_x", "sig_1d_y", "sig_1d_z", "v_sigma", "lambda")), sp)
+    assert np.isnan(t[0, F["v_tf"]])
