@@ -410,12 +410,9 @@ struct __align__(16) CellSlot {
     int start, count;
 };
 
-// First probe slot of a cell key: runs of 8 consecutive keys (8 neighbouring cells along z)
-// share one scattered block of 8 slots (128 bytes), so that the z-neighbours a warp looks up
-// together mostly fall in one cache line.
-__device__ __forceinline__ uint64_t slot_of(uint64_t key, uint64_t hmask) {
-    return ((mix64(key >> 3) << 3) | (key & 7)) & hmask;
-}
+// First probe slot of a cell key (fully scattered: runs of neighbouring keys placed side by
+// side made the CAS inserts of crowded regions collide more than they saved on lookups).
+__device__ __forceinline__ uint64_t slot_of(uint64_t key, uint64_t hmask) { return mix64(key) & hmask; }
 
 // Hash capacity from the number of occupied cells: the smallest power of two >= 2 x cells, at
 // least 1024 slots and at most the cap_max allocated; kept on the device as a mask.
@@ -486,13 +483,27 @@ __global__ void itemflag_kernel(int n, const int *__restrict__ head, const int *
     }
 }
 
+// A work item as the linking kernel reads it, in two 16-byte loads: the chunk's first sorted
+// position, the cell's end with the cell's one-component flag in bit 31, and the cell's
+// coordinates (decoded here once instead of in the latency-bound linking kernel).
+struct __align__(16) ItemRec {
+    int k0, ce_conn;
+    long long cx, cy, cz;
+};
+
 __global__ void items_kernel(int n, const int *__restrict__ head, const int *__restrict__ cellpos,
                              const int *__restrict__ flag, const int *__restrict__ itempos,
-                             int *__restrict__ item_k0, int *__restrict__ item_cell, int *__restrict__ nitems) {
+                             const int *__restrict__ cell_start, const uint64_t *__restrict__ cell_key,
+                             const unsigned char *__restrict__ conn, FofGeom g, ItemRec *__restrict__ items,
+                             int *__restrict__ nitems) {
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
         if (flag[k]) {
-            item_k0[itempos[k]] = k;
-            item_cell[itempos[k]] = cellpos[k] + head[k] - 1;
+            const int c = cellpos[k] + head[k] - 1;
+            ItemRec r;
+            r.k0 = k;
+            r.ce_conn = cell_start[c + 1] | (conn[c] ? (int)0x80000000u : 0);
+            decode_key(cell_key[c], g, r.cx, r.cy, r.cz);
+            items[itempos[k]] = r;
         }
         if (k == n - 1) *nitems = itempos[k] + flag[k];
     }
@@ -535,10 +546,8 @@ __constant__ int c_stencil[13][3] = {{0, 0, 1},  {0, 1, -1}, {0, 1, 0},  {0, 1, 
 constexpr int kHomeSeg = 13;
 
 __global__ void __launch_bounds__(256, 6) link_kernel(
-    const float4 *__restrict__ rec, const int *__restrict__ cell_start, const uint64_t *__restrict__ cell_key,
-    const int *__restrict__ item_k0, const int *__restrict__ item_cell, const int *__restrict__ nitems_p,
-    int *item_counter, const CellSlot *__restrict__ slots, const unsigned char *__restrict__ conn,
-    const unsigned long long *__restrict__ hmask_p, FofGeom g,
+    const float4 *__restrict__ rec, const ItemRec *__restrict__ items, const int *__restrict__ nitems_p,
+    int *item_counter, const CellSlot *__restrict__ slots, const unsigned long long *__restrict__ hmask_p, FofGeom g,
     const double *__restrict__ x, const double *__restrict__ y, const double *__restrict__ z,
     int *parent, unsigned char *has, int *err) {
     __shared__ float4 buf[kFofWarps][32];
@@ -547,21 +556,25 @@ __global__ void __launch_bounds__(256, 6) link_kernel(
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int nitems = *nitems_p;
     const uint64_t hmask = *hmask_p;
-    // items come from a counter: their cost varies by orders of magnitude (dense cores)
+    // items come from a counter: their cost varies by orders of magnitude (dense cores).  The
+    // next item's number is fetched while the current one is processed.
+    int nxt = 0;
+    if (lane == 0) nxt = atomicAdd(item_counter, 1);
     for (;;) {
-        int item = 0;
-        if (lane == 0) item = atomicAdd(item_counter, 1);
-        item = __shfl_sync(0xffffffffu, item, 0);
+        const int item = __shfl_sync(0xffffffffu, nxt, 0);
         if (item >= nitems) break;
-        const int c = item_cell[item];
-        const int k0 = item_k0[item];
-        const int ce = cell_start[c + 1];
+        if (lane == 0) nxt = atomicAdd(item_counter, 1);
+        const int4 ia = __ldg(reinterpret_cast<const int4 *>(items + item));
+        const longlong2 ib = __ldg(reinterpret_cast<const longlong2 *>(items + item) + 1);
+        const int k0 = ia.x;
+        const int ce = ia.y & 0x7fffffff;
+        const bool home_conn = ia.y < 0;
+        const long long cx = (long long)(((unsigned long long)(unsigned)ia.w << 32) | (unsigned)ia.z);
+        const long long cy = ib.x, cz = ib.y;
         const int k = k0 + lane;
         const bool hv = k < ce;
         const float4 hp = hv ? rec[k] : make_float4(0.f, 0.f, 0.f, 0.f);
         const int hidx = __float_as_int(hp.w);
-        long long cx, cy, cz;
-        decode_key(cell_key[c], g, cx, cy, cz);
         // lane s < 13 owns stencil cell s, lane 13 the rest of the home cell
         int sjs = 0, sn = 0, soff = 0x15;   // soff: stencil offset + 1 per axis, 2 bits each
         bool sconn = false;                 // the segment's cell is one component
@@ -575,7 +588,7 @@ __global__ void __launch_bounds__(256, 6) link_kernel(
                 sn = sc.y & 0x7fffffff;
                 sconn = sc.y < 0;
             }
-        } else if (lane == kHomeSeg && !conn[c]) {   // a cell that is one component has no new pair inside
+        } else if (lane == kHomeSeg && !home_conn) {   // a cell that is one component has no new pair inside
             sjs = k0 + 1;
             sn = ce - sjs;
         }
@@ -897,7 +910,7 @@ int fof_core(int n, const double *x, const double *y, const double *z, FofGeom g
     const size_t o_cst = M.add(4ull * (n + 1)), o_ckey = M.add(8ull * n);
     const size_t o_hk = M.add(16ull * hcap), o_hv = M.add(4ull * n);   // hash slots, slot of each cell
     const size_t o_flag = M.add(4ull * n), o_ipos = M.add(4ull * n);
-    const size_t o_ik0 = M.add(4ull * n), o_icell = M.add(4ull * n);
+    const size_t o_items = M.add(sizeof(ItemRec) * (size_t)n);
     const size_t o_cnt = M.add(64), o_conn = M.add(1ull * n);
     const size_t o_tmp = M.add(std::max(sort_b, scan_b));
     void *base = nullptr;
@@ -913,7 +926,7 @@ int fof_core(int n, const double *x, const double *y, const double *z, FofGeom g
     auto *hk = at<CellSlot>(base, o_hk);
     auto *hv = at<int>(base, o_hv);
     auto *flag = at<int>(base, o_flag), *ipos = at<int>(base, o_ipos);
-    auto *ik0 = at<int>(base, o_ik0), *icell = at<int>(base, o_icell);
+    auto *items = at<ItemRec>(base, o_items);
     int *cnt = at<int>(base, o_cnt);   // [0] ncell [1] nitems [2] ngroups [3] err [5] link item counter
     auto *hmask = reinterpret_cast<unsigned long long *>(cnt + 6);   // [6..7] hash slot mask
     void *tmp = at<void>(base, o_tmp);
@@ -942,9 +955,9 @@ int fof_core(int n, const double *x, const double *y, const double *z, FofGeom g
     HALMA_LAUNCH(slot_fill_kernel, g1, 256, 0, st, cnt + 0, cst, hv, conn, hk);
     HALMA_LAUNCH(itemflag_kernel, g1, 256, 0, st, n, head, cpos, cst, flag);
     HALMA_TRY(exclusive_sum_i32(tmp, scan_b, flag, ipos, n, st));
-    HALMA_LAUNCH(items_kernel, g1, 256, 0, st, n, head, cpos, flag, ipos, ik0, icell, cnt + 1);
-    HALMA_LAUNCH(link_kernel, sms * 8, 32 * kFofWarps, 0, st, rec, cst, ckey, ik0, icell, cnt + 1, cnt + 5, hk,
-                 conn, hmask, g, x, y, z, parent, has, cnt + 3);
+    HALMA_LAUNCH(items_kernel, g1, 256, 0, st, n, head, cpos, flag, ipos, cst, ckey, conn, g, items, cnt + 1);
+    HALMA_LAUNCH(link_kernel, sms * 8, 32 * kFofWarps, 0, st, rec, items, cnt + 1, cnt + 5, hk, hmask, g, x, y, z,
+                 parent, has, cnt + 3);
     HALMA_LAUNCH(root_kernel, g1, 256, 0, st, n, rec, parent, has, root, minidx, cnt + 3);
     HALMA_LAUNCH(label_kernel, g1, 256, 0, st, n, rec, has, root, minidx, labels, cnt + 2);
     int hc[4];

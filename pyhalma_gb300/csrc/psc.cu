@@ -41,7 +41,7 @@ enum { kModeNone = 0, kModeSweep = 1, kModeFinal = 2 };
 
 struct PscState {
     double cx, cy, cz, M, rr;
-    double start, next, delta, step;
+    double start, next, delta, step, inv_step;
     double fac_sig;
     long long n, n0;              // grid points per axis: current, and of the first grid
     long long cleaned, remaining;
@@ -53,8 +53,10 @@ __device__ __forceinline__ double grid_at(const PscState &s, long long i) {
     return i == 0 ? s.start : (i == 1 ? s.next : __dadd_rn(s.start, __dmul_rn((double)i, s.delta)));
 }
 
+// The first guess uses the reciprocal of the step (GB300's FP64 divide is a long sequence):
+// it is within one point of the nearest grid point, and the two neighbours are checked.
 __device__ __forceinline__ long long nearest(const PscState &s, double v) {
-    long long k = (long long)floor((v - s.start) / s.step + 0.5);
+    long long k = (long long)floor((v - s.start) * s.inv_step + 0.5);
     k = k < 0 ? 0 : (k > s.n - 1 ? s.n - 1 : k);
     long long best = k;
     double bd = fabs(__dsub_rn(grid_at(s, k), v));
@@ -78,85 +80,148 @@ __global__ void psc_fill_kernel(int G, const int64_t *__restrict__ off, int *__r
 // One block per group whose mode matches: FP64 centre of mass of the list (zeros when the
 // mass is not positive), furthest particle from it, and the grid around it.  With `driver`
 // the results go to the output row instead of the state.
-__global__ void __launch_bounds__(256) psc_com_kernel(int G, const int64_t *__restrict__ off,
+// Centre of mass and furthest particle of every group that sweeps or takes its final step
+// (with all, of every group: the driver's final values).  A group's list is split over up to
+// S blocks of at least kPscMin entries; each block writes its partial sums, and the last block
+// of the group to finish (a counter per group, no waiting) adds them in block order.  The
+// furthest particle is the square root of the largest squared distance (the square root is
+// correctly rounded and monotone, so this is the largest of the square roots).
+constexpr int kPscMin = 2048;
+
+__device__ __forceinline__ bool psc_part_of(int bid, int S, int G, const int64_t *__restrict__ off, int &h, int &sh,
+                                            int64_t &b, int64_t &e) {
+    h = bid / S;
+    const int s = bid % S;
+    if (h >= G) return false;
+    const int64_t b0 = off[h], len = off[h + 1] - b0;
+    sh = (int)std::min<int64_t>(S, std::max<int64_t>(1, (len + kPscMin - 1) / kPscMin));
+    if (s >= sh) return false;
+    b = b0 + len * s / sh;
+    e = b0 + len * (s + 1) / sh;
+    return true;
+}
+
+__global__ void __launch_bounds__(256) psc_sum_kernel(int G, const int64_t *__restrict__ off,
                                                       const int *__restrict__ list, const int *__restrict__ mem,
                                                       const double *__restrict__ x, const double *__restrict__ y,
                                                       const double *__restrict__ z, const double *__restrict__ m,
-                                                      double ll, int want, PscState *st, double *out,
-                                                      int64_t *__restrict__ nwhich) {
-    __shared__ double sh[4][8];
-    __shared__ double cen[3];
+                                                      int S, int all, const PscState *__restrict__ st,
+                                                      double *__restrict__ part, int *__restrict__ ctr,
+                                                      double *__restrict__ cen,
+                                                      unsigned long long *__restrict__ rr2) {
+    int h, sh;
+    int64_t b, e;
+    if (!psc_part_of(blockIdx.x, S, G, off, h, sh, b, e)) return;
+    if (!all && st[h].mode == kModeNone) return;
+    __shared__ double sm[4][8];
+    __shared__ int last;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    for (int h = blockIdx.x; h < G; h += gridDim.x) {
-        if (!out && st[h].mode != want) continue;
-        double v[4] = {0, 0, 0, 0};
-        for (int64_t e = off[h] + threadIdx.x; e < off[h + 1]; e += blockDim.x) {
-            const int i = mem[list[e]];
-            const double mi = m[i];
-            v[0] += mi * x[i];
-            v[1] += mi * y[i];
-            v[2] += mi * z[i];
-            v[3] += mi;
-        }
+    double v[4] = {0, 0, 0, 0};
+    for (int64_t k = b + threadIdx.x; k < e; k += blockDim.x) {
+        const int i = mem[list[k]];
+        const double mi = m[i];
+        v[0] += mi * x[i];
+        v[1] += mi * y[i];
+        v[2] += mi * z[i];
+        v[3] += mi;
+    }
 #pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        for (int o = 16; o > 0; o >>= 1) v[q] += __shfl_down_sync(0xffffffffu, v[q], o);
+        if (lane == 0) sm[q][w] = v[q];
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const int s = blockIdx.x % S;
         for (int q = 0; q < 4; ++q) {
-            for (int o = 16; o > 0; o >>= 1) v[q] += __shfl_down_sync(0xffffffffu, v[q], o);
-            if (lane == 0) sh[q][w] = v[q];
+            double t = 0.0;
+            for (int k = 0; k < nw; ++k) t += sm[q][k];
+            part[((int64_t)h * S + s) * 4 + q] = t;
         }
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            double t[4] = {0, 0, 0, 0};
-            for (int q = 0; q < 4; ++q)
-                for (int k = 0; k < nw; ++k) t[q] += sh[q][k];
-            const double M = t[3];
-            cen[0] = M > 0 ? t[0] / M : 0.0;
-            cen[1] = M > 0 ? t[1] / M : 0.0;
-            cen[2] = M > 0 ? t[2] / M : 0.0;
-            sh[3][0] = M > 0 ? M : 0.0;
+        __threadfence();
+        last = atomicAdd(ctr + h, 1) == sh - 1;
+    }
+    __syncthreads();
+    if (last && threadIdx.x == 0) {
+        __threadfence();
+        double t[4] = {0, 0, 0, 0};
+        for (int s = 0; s < sh; ++s)
+            for (int q = 0; q < 4; ++q) t[q] += __ldcg(part + ((int64_t)h * S + s) * 4 + q);
+        const double M = t[3];
+        cen[4 * h + 0] = M > 0 ? t[0] / M : 0.0;
+        cen[4 * h + 1] = M > 0 ? t[1] / M : 0.0;
+        cen[4 * h + 2] = M > 0 ? t[2] / M : 0.0;
+        cen[4 * h + 3] = M > 0 ? M : 0.0;
+        rr2[h] = 0ull;
+        ctr[h] = 0;
+    }
+}
+
+__global__ void __launch_bounds__(256) psc_rmax_kernel(int G, const int64_t *__restrict__ off,
+                                                       const int *__restrict__ list, const int *__restrict__ mem,
+                                                       const double *__restrict__ x, const double *__restrict__ y,
+                                                       const double *__restrict__ z, double ll, int S, int all,
+                                                       PscState *st, double *out, int64_t *__restrict__ nwhich,
+                                                       int *__restrict__ ctr, const double *__restrict__ cen,
+                                                       unsigned long long *__restrict__ rr2) {
+    int h, sh;
+    int64_t b, e;
+    if (!psc_part_of(blockIdx.x, S, G, off, h, sh, b, e)) return;
+    if (!all && st[h].mode == kModeNone) return;
+    __shared__ double sm[8];
+    __shared__ int last;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const double cx = cen[4 * h], cy = cen[4 * h + 1], cz = cen[4 * h + 2];
+    double r2 = 0.0;
+    for (int64_t k = b + threadIdx.x; k < e; k += blockDim.x) {
+        const int i = mem[list[k]];
+        const double dx = __dsub_rn(cx, x[i]), dy = __dsub_rn(cy, y[i]), dz = __dsub_rn(cz, z[i]);
+        r2 = fmax(r2, __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz)));
+    }
+    for (int o = 16; o > 0; o >>= 1) r2 = fmax(r2, __shfl_down_sync(0xffffffffu, r2, o));
+    if (lane == 0) sm[w] = r2;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int k = 0; k < nw; ++k) t = fmax(t, sm[k]);
+        // non-negative doubles order like their bit patterns
+        atomicMax(rr2 + h, (unsigned long long)__double_as_longlong(t));
+        __threadfence();
+        last = atomicAdd(ctr + h, 1) == sh - 1;
+    }
+    __syncthreads();
+    if (last && threadIdx.x == 0) {
+        __threadfence();
+        const double r = __dsqrt_rn(__longlong_as_double((long long)atomicAdd(rr2 + h, 0ull)));
+        const double M = cen[4 * h + 3];
+        ctr[h] = 0;
+        if (out) {
+            double *o = out + (int64_t)h * HALMA_PSC_NFIELDS;
+            o[HALMA_PSC_CX] = cx;
+            o[HALMA_PSC_CY] = cy;
+            o[HALMA_PSC_CZ] = cz;
+            o[HALMA_PSC_MASS] = M;
+            o[HALMA_PSC_RMAX] = r;
+            o[HALMA_PSC_NPART] = (double)(off[h + 1] - off[h]);
+        } else {
+            PscState &s = st[h];
+            nwhich[h] = off[h + 1] - off[h];   // the which_cell arrays of this grid
+            s.cx = cx;
+            s.cy = cy;
+            s.cz = cz;
+            s.M = M;
+            s.rr = r;
+            // np.arange(-(r + ll), r + ll, 2 ll): length ceil((stop - start) / step)
+            const double stop = __dadd_rn(r, ll), start = -stop, step = __dmul_rn(2.0, ll);
+            s.start = start;
+            s.step = step;
+            s.inv_step = 1.0 / step;
+            s.next = __dadd_rn(start, step);
+            s.delta = __dsub_rn(s.next, start);
+            s.n = (long long)ceil(__ddiv_rn(__dsub_rn(stop, start), step));
+            if (s.n < 1) s.n = 1;
+            if (s.first) s.n0 = s.n;
         }
-        __syncthreads();
-        const double cx = cen[0], cy = cen[1], cz = cen[2], M = sh[3][0];
-        double rr = 0.0;
-        for (int64_t e = off[h] + threadIdx.x; e < off[h + 1]; e += blockDim.x) {
-            const int i = mem[list[e]];
-            const double dx = __dsub_rn(cx, x[i]), dy = __dsub_rn(cy, y[i]), dz = __dsub_rn(cz, z[i]);
-            rr = fmax(rr, __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz))));
-        }
-        for (int o = 16; o > 0; o >>= 1) rr = fmax(rr, __shfl_down_sync(0xffffffffu, rr, o));
-        __syncthreads();
-        if (lane == 0) sh[0][w] = rr;
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            double r = 0.0;
-            for (int k = 0; k < nw; ++k) r = fmax(r, sh[0][k]);
-            if (out) {
-                double *o = out + (int64_t)h * HALMA_PSC_NFIELDS;
-                o[HALMA_PSC_CX] = cx;
-                o[HALMA_PSC_CY] = cy;
-                o[HALMA_PSC_CZ] = cz;
-                o[HALMA_PSC_MASS] = M;
-                o[HALMA_PSC_RMAX] = r;
-                o[HALMA_PSC_NPART] = (double)(off[h + 1] - off[h]);
-            } else {
-                PscState &s = st[h];
-                nwhich[h] = off[h + 1] - off[h];   // the which_cell arrays of this grid
-                s.cx = cx;
-                s.cy = cy;
-                s.cz = cz;
-                s.M = M;
-                s.rr = r;
-                // np.arange(-(r + ll), r + ll, 2 ll): length ceil((stop - start) / step)
-                const double stop = __dadd_rn(r, ll), start = -stop, step = __dmul_rn(2.0, ll);
-                s.start = start;
-                s.step = step;
-                s.next = __dadd_rn(start, step);
-                s.delta = __dsub_rn(s.next, start);
-                s.n = (long long)ceil(__ddiv_rn(__dsub_rn(stop, start), step));
-                if (s.n < 1) s.n = 1;
-                if (s.first) s.n0 = s.n;
-            }
-        }
-        __syncthreads();
     }
 }
 
@@ -464,6 +529,9 @@ extern "C" int halma_phase_space_clean(int64_t n, const double *x, const double 
     const size_t o_rpos = L.add(4ull * NL), o_rid = L.add(4ull * NL), o_cv = L.add(32ull * NL);
     const size_t o_sig = L.add(8ull * NL), o_flag = L.add(4ull * (NL + 1)), o_pos = L.add(4ull * NL);
     const size_t o_w = L.add(12ull * NL), o_nw = L.add(8ull * G), o_cnt = L.add(64);
+    const int S = G >= 8192 ? 1 : 16;   // blocks per group for the centre and furthest particle
+    const size_t o_part = L.add(32ull * S * G), o_ctr = L.add(4ull * G), o_cen = L.add(32ull * G),
+                 o_rr2 = L.add(8ull * G);
     const size_t sort_b = sort_pairs_u64_i32_bytes((int)NL, 64), scan_b = exclusive_sum_i32_bytes((int)NL);
     const size_t o_tmp = L.add(std::max(sort_b, scan_b));
     void *base = nullptr;
@@ -481,8 +549,20 @@ extern "C" int halma_phase_space_clean(int64_t n, const double *x, const double 
     int *wbuf = dwhich ? dwhich : at<int>(base, o_w);
     int64_t *nw = dnw ? dnw : at<int64_t>(base, o_nw);
     int *cnt = at<int>(base, o_cnt);
+    double *part = at<double>(base, o_part), *cen = at<double>(base, o_cen);
+    int *ctr = at<int>(base, o_ctr);
+    auto *rr2 = at<unsigned long long>(base, o_rr2);
     void *tmp = at<void>(base, o_tmp);
     int *wx = wbuf, *wy = wbuf + N0, *wz = wbuf + 2 * N0;
+    const int gS = G * S;
+    // centre of mass and furthest particle of the groups that sweep or end (all: every group)
+    auto centres = [&](int all, double *o) -> int {
+        HALMA_LAUNCH(psc_sum_kernel, gS, 256, 0, st, G, off, list, dmem, dx, dy, dz, dm, S, all, state, part, ctr,
+                     cen, rr2);
+        HALMA_LAUNCH(psc_rmax_kernel, gS, 256, 0, st, G, off, list, dmem, dx, dy, dz, p.linking_length, S, all, state,
+                     o, nw, ctr, cen, rr2);
+        return HALMA_OK;
+    };
     const int sms = device_sm_count();
     const int gN = std::min(sms * 8, grid_for(NL, 256)), gG = std::min(G, sms * 16), gH = grid_for(G, 256);
 
@@ -499,6 +579,7 @@ extern "C" int halma_phase_space_clean(int64_t n, const double *x, const double 
     const int gbits = bits_needed((uint64_t)G);
     HALMA_LAUNCH(psc_init_kernel, std::max(gN, gH), 256, 0, st, G, dgoff, N0, state, dctl);
     HALMA_CUDA(cudaMemsetAsync(nw, 0, 8ull * G, st));
+    HALMA_CUDA(cudaMemsetAsync(ctr, 0, 4ull * G, st));
     // the first lists are the groups themselves
     HALMA_LAUNCH(psc_flag_kernel, gN, 256, 0, st, N0, dctl, flag);
     HALMA_TRY(exclusive_sum_i32(tmp, scan_b, flag, pos, (int)NL, st));
@@ -507,10 +588,7 @@ extern "C" int halma_phase_space_clean(int64_t n, const double *x, const double 
     for (int pass = 0; (sweeping > 0 || finals > 0) && N0 > 0; ++pass) {
         if (pass >= p.max_passes + 1) return fail(HALMA_ERR_NOT_CONVERGED, "phase-space cleaning did not stop in %d passes", p.max_passes);
         HALMA_LAUNCH(psc_fill_kernel, gG, 256, 0, st, G, off, own);
-        HALMA_LAUNCH(psc_com_kernel, gG, 256, 0, st, G, off, list, dmem, dx, dy, dz, dm, p.linking_length,
-                     (int)kModeSweep, state, nullptr, nw);
-        HALMA_LAUNCH(psc_com_kernel, gG, 256, 0, st, G, off, list, dmem, dx, dy, dz, dm, p.linking_length,
-                     (int)kModeFinal, state, nullptr, nw);
+        HALMA_TRY(centres(0, nullptr));
         // the largest grid decides the cell bits
         std::vector<PscState> hs(G);
         HALMA_CUDA(cudaMemcpyAsync(hs.data(), state, sizeof(PscState) * G, cudaMemcpyDeviceToHost, st));
@@ -557,8 +635,7 @@ extern "C" int halma_phase_space_clean(int64_t n, const double *x, const double 
     HALMA_LAUNCH(psc_flag_kernel, gN, 256, 0, st, N0, dctl, flag);
     HALMA_TRY(exclusive_sum_i32(tmp, scan_b, flag, pos, (int)NL, st));
     HALMA_LAUNCH(psc_compact_kernel, gN, 256, 0, st, N0, G, flag, pos, dgoff, list, off);
-    HALMA_LAUNCH(psc_com_kernel, gG, 256, 0, st, G, off, list, dmem, dx, dy, dz, dm, p.linking_length, 0, state,
-                 dout, nw);
+    HALMA_TRY(centres(1, dout));
     HALMA_LAUNCH(psc_out_kernel, gH, 256, 0, st, G, state, p.minp, dout);
     HALMA_TRY(sg.download(st));
     HALMA_CUDA(cudaStreamSynchronize(st));
