@@ -97,6 +97,7 @@ SIGNATURES = {
                                  _P, _P, _P], ctypes.c_int),
     "halma_halo_properties": ([_I64, _P, _P, _P, _P, _P, _P, _P, _I64, _P, _P, _P, _F64, _P, _P], ctypes.c_int),
     "halma_ball_gather": ([_I64, _P, _P, _P, _I64, _P, _P, _P, _P, _I32, _P, _P, _I64, _P, _P], ctypes.c_int),
+    "halma_sequential_sum_f64": ([_I64, _P, _I64, _P, _P, _P], ctypes.c_int),
     "halma_bf_potential_f32": ([_I64, _P, _P, _P, _P, _I64, _P, _P, _P, _P, _I32, _F64, _P], ctypes.c_int),
     "halma_potential_f64": ([_I64, _P, _P, _P, _P, _I64, _P, _P, _P, _F64, _I32, _I64, _P, _P], ctypes.c_int),
     "halma_potential_f32": ([_I64, _P, _P, _P, _P, _I64, _P, _P, _P, _F64, _I32, _I64, _P, _P], ctypes.c_int),

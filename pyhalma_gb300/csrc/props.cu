@@ -243,68 +243,145 @@ __global__ void __launch_bounds__(256) pr_shape_kernel(int G, const int64_t *__r
     }
 }
 
-// Block per group: specific angular momentum (with the reference's z component), then kappa_co
-// and the Tully-Fisher velocity about it.
-__global__ void __launch_bounds__(256) pr_kin_kernel(int G, const int64_t *__restrict__ off,
-                                                     const double *__restrict__ g, int64_t nm,
-                                                     const double *__restrict__ cen, double *__restrict__ out) {
-    __shared__ double sh[4][8];
-    for (int h = blockIdx.x; h < G; h += gridDim.x) {
-        const double *c = cen + (int64_t)h * kCenFields;
-        double *o = out + (int64_t)h * HALMA_PROP_NFIELDS;
-        const double M = c[3], ux = o[HALMA_PROP_VX], uy = o[HALMA_PROP_VY], uz = o[HALMA_PROP_VZ];
-        const double r05 = o[HALMA_PROP_R05];
-        double l[3] = {0, 0, 0};
-        for (int64_t k = off[h] + threadIdx.x; k < off[h + 1]; k += blockDim.x) {
-            const double rx = g[k] - c[0], ry = g[nm + k] - c[1], rz = g[2 * nm + k] - c[2];
-            const double vvx = g[3 * nm + k] - ux, vvy = g[4 * nm + k] - uy, vvz = g[5 * nm + k] - uz;
-            const double mk = g[6 * nm + k];
-            l[0] += mk * (ry * vvz - rz * vvy);
-            l[1] += mk * (rz * vvx - rx * vvz);
-            l[2] += mk * (rx * vvy - ry * vvz);   // as angular_momentum (halo_properties.py:478)
-        }
-        block_sums<3>(l, sh);
-        const double jx = l[0] / M, jy = l[1] / M, jz = l[2] / M;
+// Specific angular momentum (with the reference's z component), then kappa_co and the
+// Tully-Fisher velocity about it.
+// A group's members are split over up to S blocks of at least kKinMin (the FP64 work per member
+// is heavy and GB300's FP64 pipe is narrow, so one block per group would leave the biggest
+// group's SM as the critical path); each block writes partial sums and the last block of the
+// group to finish (a per-group counter, no waiting) adds them in block order.
+constexpr int kKinMin = 2048;
+
+__device__ __forceinline__ bool kin_part_of(int bid, int S, int G, const int64_t *__restrict__ off, int &h, int &sh,
+                                            int64_t &b, int64_t &e) {
+    h = bid / S;
+    const int s = bid % S;
+    if (h >= G) return false;
+    const int64_t b0 = off[h], len = off[h + 1] - b0;
+    sh = (int)std::min<int64_t>(S, std::max<int64_t>(1, (len + kKinMin - 1) / kKinMin));
+    if (s >= sh) return false;
+    b = b0 + len * s / sh;
+    e = b0 + len * (s + 1) / sh;
+    return true;
+}
+
+// Phase 1: angular momentum (halo_properties.py:463-482); the last block stores j, |j| and the
+// unit vector for phase 2.
+__global__ void __launch_bounds__(256) pr_kin1_kernel(int G, int S, const int64_t *__restrict__ off,
+                                                      const double *__restrict__ g, int64_t nm,
+                                                      const double *__restrict__ cen, const double *__restrict__ out,
+                                                      double *__restrict__ part, int *__restrict__ ctr,
+                                                      double *__restrict__ jvec) {
+    int h, sh;
+    int64_t b, e;
+    if (!kin_part_of(blockIdx.x, S, G, off, h, sh, b, e)) return;
+    __shared__ double sm[4][8];
+    __shared__ int last;
+    const double *c = cen + (int64_t)h * kCenFields;
+    const double *o = out + (int64_t)h * HALMA_PROP_NFIELDS;
+    const double ux = o[HALMA_PROP_VX], uy = o[HALMA_PROP_VY], uz = o[HALMA_PROP_VZ];
+    double l[3] = {0, 0, 0};
+    for (int64_t k = b + threadIdx.x; k < e; k += blockDim.x) {
+        const double rx = g[k] - c[0], ry = g[nm + k] - c[1], rz = g[2 * nm + k] - c[2];
+        const double vvx = g[3 * nm + k] - ux, vvy = g[4 * nm + k] - uy, vvz = g[5 * nm + k] - uz;
+        const double mk = g[6 * nm + k];
+        l[0] += mk * (ry * vvz - rz * vvy);
+        l[1] += mk * (rz * vvx - rx * vvz);
+        l[2] += mk * (rx * vvy - ry * vvz);   // as angular_momentum (halo_properties.py:478)
+    }
+    block_sums<3>(l, sm);
+    if (threadIdx.x == 0) {
+        const int s = blockIdx.x % S;
+        for (int q = 0; q < 3; ++q) part[((int64_t)h * S + s) * 4 + q] = l[q];
+        __threadfence();
+        last = atomicAdd(ctr + h, 1) == sh - 1;
+    }
+    __syncthreads();
+    if (last && threadIdx.x == 0) {
+        __threadfence();
+        double t[3] = {0, 0, 0};
+        for (int s = 0; s < sh; ++s)
+            for (int q = 0; q < 3; ++q) t[q] += __ldcg(part + ((int64_t)h * S + s) * 4 + q);
+        const double M = c[3];
+        const double jx = t[0] / M, jy = t[1] / M, jz = t[2] / M;
         const double jn = sqrt(jx * jx + jy * jy + jz * jz);
-        const double ex = jx / jn, ey = jy / jn, ez = jz / jn;
-        double s[4] = {0, 0, 0, 0};   // kin_corot, kin_total, v_TF, mass in the shell
-        for (int64_t k = off[h] + threadIdx.x; k < off[h + 1]; k += blockDim.x) {
-            const double rx = g[k] - c[0], ry = g[nm + k] - c[1], rz = g[2 * nm + k] - c[2];
-            const double vvx = g[3 * nm + k] - ux, vvy = g[4 * nm + k] - uy, vvz = g[5 * nm + k] - uz;
-            const double mk = g[6 * nm + k];
-            const double llx = mk * (ry * vvz - rz * vvy), lly = mk * (rz * vvx - rx * vvz),
-                         llz = mk * (rx * vvy - ry * vvx);
-            const double lz = llx * ex + lly * ey + llz * ez;
-            const double zi = rx * ex + ry * ey + rz * ez;
-            const double r2 = rx * rx + ry * ry + rz * rz;
-            const double R = sqrt(r2 - zi * zi);
-            s[1] += 0.5 * mk * (vvx * vvx + vvy * vvy + vvz * vvz);
-            if (lz > 0.0) {
-                const double q = lz / (mk * R);
-                s[0] += 0.5 * mk * q * q;
-            }
-            const double dist = sqrt(r2);
-            if (0.9 * r05 < dist && dist < 1.1 * r05) {
-                // R_ip = r - (r.u)u, u_R = R_ip/|R_ip|, v_rot = v - (v.u)u - (v.u_R)u_R
-                const double Rx = rx - zi * ex, Ry = ry - zi * ey, Rz = rz - zi * ez;
-                const double Rn = sqrt(Rx * Rx + Ry * Ry + Rz * Rz);
-                const double qx = Rx / Rn, qy = Ry / Rn, qz = Rz / Rn;
-                const double vu = vvx * ex + vvy * ey + vvz * ez, vq = vvx * qx + vvy * qy + vvz * qz;
-                const double wx = vvx - vu * ex - vq * qx, wy = vvy - vu * ey - vq * qy, wz = vvz - vu * ez - vq * qz;
-                s[2] += sqrt(wx * wx + wy * wy + wz * wz) * mk;
-                s[3] += mk;
-            }
+        double *jv = jvec + (int64_t)h * 8;
+        jv[0] = jx;
+        jv[1] = jy;
+        jv[2] = jz;
+        jv[3] = jn;
+        jv[4] = jx / jn;
+        jv[5] = jy / jn;
+        jv[6] = jz / jn;
+        ctr[h] = 0;
+    }
+}
+
+// Phase 2: kappa_co (halo_properties.py:781-866) and the Tully-Fisher shell velocity
+// (:484-515); the last block writes the group's outputs.
+__global__ void __launch_bounds__(256) pr_kin2_kernel(int G, int S, const int64_t *__restrict__ off,
+                                                      const double *__restrict__ g, int64_t nm,
+                                                      const double *__restrict__ cen, double *__restrict__ out,
+                                                      double *__restrict__ part, int *__restrict__ ctr,
+                                                      const double *__restrict__ jvec) {
+    int h, sh;
+    int64_t b, e;
+    if (!kin_part_of(blockIdx.x, S, G, off, h, sh, b, e)) return;
+    __shared__ double sm[4][8];
+    __shared__ int last;
+    const double *c = cen + (int64_t)h * kCenFields;
+    double *o = out + (int64_t)h * HALMA_PROP_NFIELDS;
+    const double ux = o[HALMA_PROP_VX], uy = o[HALMA_PROP_VY], uz = o[HALMA_PROP_VZ];
+    const double r05 = o[HALMA_PROP_R05];
+    const double *jv = jvec + (int64_t)h * 8;
+    const double ex = jv[4], ey = jv[5], ez = jv[6];
+    double s[4] = {0, 0, 0, 0};   // kin_corot, kin_total, v_TF, mass in the shell
+    for (int64_t k = b + threadIdx.x; k < e; k += blockDim.x) {
+        const double rx = g[k] - c[0], ry = g[nm + k] - c[1], rz = g[2 * nm + k] - c[2];
+        const double vvx = g[3 * nm + k] - ux, vvy = g[4 * nm + k] - uy, vvz = g[5 * nm + k] - uz;
+        const double mk = g[6 * nm + k];
+        const double llx = mk * (ry * vvz - rz * vvy), lly = mk * (rz * vvx - rx * vvz),
+                     llz = mk * (rx * vvy - ry * vvx);
+        const double lz = llx * ex + lly * ey + llz * ez;
+        const double zi = rx * ex + ry * ey + rz * ez;
+        const double r2 = rx * rx + ry * ry + rz * rz;
+        const double R = sqrt(r2 - zi * zi);
+        s[1] += 0.5 * mk * (vvx * vvx + vvy * vvy + vvz * vvz);
+        if (lz > 0.0) {
+            const double q = lz / (mk * R);
+            s[0] += 0.5 * mk * q * q;
         }
-        block_sums<4>(s, sh);
-        if (threadIdx.x == 0) {
-            o[HALMA_PROP_JX] = jx;
-            o[HALMA_PROP_JY] = jy;
-            o[HALMA_PROP_JZ] = jz;
-            o[HALMA_PROP_J] = jn;
-            o[HALMA_PROP_KCO] = s[0] / s[1];
-            o[HALMA_PROP_VTF] = s[2] / s[3];   // NaN when no particle lies in 0.9..1.1 R05
+        const double dist = sqrt(r2);
+        if (0.9 * r05 < dist && dist < 1.1 * r05) {
+            // R_ip = r - (r.u)u, u_R = R_ip/|R_ip|, v_rot = v - (v.u)u - (v.u_R)u_R
+            const double Rx = rx - zi * ex, Ry = ry - zi * ey, Rz = rz - zi * ez;
+            const double Rn = sqrt(Rx * Rx + Ry * Ry + Rz * Rz);
+            const double qx = Rx / Rn, qy = Ry / Rn, qz = Rz / Rn;
+            const double vu = vvx * ex + vvy * ey + vvz * ez, vq = vvx * qx + vvy * qy + vvz * qz;
+            const double wx = vvx - vu * ex - vq * qx, wy = vvy - vu * ey - vq * qy, wz = vvz - vu * ez - vq * qz;
+            s[2] += sqrt(wx * wx + wy * wy + wz * wz) * mk;
+            s[3] += mk;
         }
-        __syncthreads();
+    }
+    block_sums<4>(s, sm);
+    if (threadIdx.x == 0) {
+        const int sb = blockIdx.x % S;
+        for (int q = 0; q < 4; ++q) part[((int64_t)h * S + sb) * 4 + q] = s[q];
+        __threadfence();
+        last = atomicAdd(ctr + h, 1) == sh - 1;
+    }
+    __syncthreads();
+    if (last && threadIdx.x == 0) {
+        __threadfence();
+        double t[4] = {0, 0, 0, 0};
+        for (int q0 = 0; q0 < sh; ++q0)
+            for (int q = 0; q < 4; ++q) t[q] += __ldcg(part + ((int64_t)h * S + q0) * 4 + q);
+        o[HALMA_PROP_JX] = jv[0];
+        o[HALMA_PROP_JY] = jv[1];
+        o[HALMA_PROP_JZ] = jv[2];
+        o[HALMA_PROP_J] = jv[3];
+        o[HALMA_PROP_KCO] = t[0] / t[1];
+        o[HALMA_PROP_VTF] = t[2] / t[3];   // NaN when no particle lies in 0.9..1.1 R05
+        ctr[h] = 0;
     }
 }
 
@@ -661,6 +738,8 @@ extern "C" int halma_halo_properties(int64_t n, const double *x, const double *y
                  o_vout = L.add(4ull * N3);
     const size_t o_head = L.add(4ull * N3), o_rpos = L.add(4ull * N3), o_rid = L.add(4ull * N3);
     const size_t o_cv = L.add(16ull * N3), o_ck = L.add(8ull * N3), o_res = L.add(4ull * 9 * G), o_cnt = L.add(64);
+    const int S = G >= 8192 ? 1 : 16;   // blocks per group for the angular-momentum kernels
+    const size_t o_kp = L.add(32ull * S * G), o_kctr = L.add(4ull * G), o_jv = L.add(64ull * G);
     const size_t sort_b = sort_pairs_u64_i32_bytes((int)N3, 64), scan_b = exclusive_sum_i32_bytes((int)N3);
     const size_t o_tmp = L.add(std::max(sort_b, scan_b));
     void *base = nullptr;
@@ -675,6 +754,8 @@ extern "C" int halma_halo_properties(int64_t n, const double *x, const double *y
     auto *cellkey = at<uint64_t>(base, o_ck);
     float *res = at<float>(base, o_res);
     int *cnt = at<int>(base, o_cnt);
+    double *kpart = at<double>(base, o_kp), *jvec = at<double>(base, o_jv);
+    int *kctr = at<int>(base, o_kctr);
     void *tmp = at<void>(base, o_tmp);
     const int sms = device_sm_count();
     const int gN = std::min(sms * 8, grid_for(NM, 256)), gG = std::min(G, sms * 16), gH = grid_for(G, 128);
@@ -703,7 +784,9 @@ extern "C" int halma_halo_properties(int64_t n, const double *x, const double *y
                                     about + (int64_t)r * G * HALMA_ABOUT_NFIELDS,
                                     red + (int64_t)r * G * HALMA_RED_NFIELDS, st));
     HALMA_LAUNCH(pr_r05_kernel, gH, 128, 0, st, G, red, dout, res);
-    HALMA_LAUNCH(pr_kin_kernel, gG, 256, 0, st, G, doff, gbuf, NM, dcen, dout);
+    HALMA_CUDA(cudaMemsetAsync(kctr, 0, 4ull * G, st));
+    HALMA_LAUNCH(pr_kin1_kernel, G * S, 256, 0, st, G, S, doff, gbuf, NM, dcen, dout, kpart, kctr, jvec);
+    HALMA_LAUNCH(pr_kin2_kernel, G * S, 256, 0, st, G, S, doff, gbuf, NM, dcen, dout, kpart, kctr, jvec);
     HALMA_LAUNCH(pr_shape_kernel, gG, 256, 0, st, G, doff, gbuf, NM, dcen, dout);
     if (N0 > 0) {
         HALMA_LAUNCH(pr_pkeys_kernel, gN, 256, 0, st, N0, G, doff, own, gbuf, dcen, linking_length, cbits, kin, vin);

@@ -31,6 +31,7 @@
 #include <vector>
 
 #include "common.cuh"
+#include "seqsum.cuh"
 #include "sort.cuh"
 #include "unbind.cuh"
 
@@ -273,59 +274,123 @@ __global__ void psc_runstart_kernel(int64_t nl, const uint64_t *__restrict__ key
     }
 }
 
-// One warp per cell (members in list order): count, mass, mass-weighted mean velocity, then
-// the dispersion; every member's entry gets the cell's index.  The lanes load 32 members at
-// a time and all of them add the 32 values in order (shuffles), so the sums are the
-// sequential ones.
+// Velocity and mass of every sorted list entry, gathered into cell order so that the per-cell
+// sums read contiguous memory (and can fetch the next 32 members while adding the current).
+struct __align__(16) VelMass {
+    double vx, vy, vz, m;
+};
+
+__global__ void psc_gather_kernel(int64_t nl, const int *__restrict__ vals, const int *__restrict__ list,
+                                  const int *__restrict__ mem, const double *__restrict__ vx,
+                                  const double *__restrict__ vy, const double *__restrict__ vz,
+                                  const double *__restrict__ m, VelMass *__restrict__ gv) {
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < nl; k += (int64_t)gridDim.x * blockDim.x) {
+        const int i = mem[list[vals[k]]];
+        VelMass p;
+        p.vx = vx[i];
+        p.vy = vy[i];
+        p.vz = vz[i];
+        p.m = m[i];
+        gv[k] = p;
+    }
+}
+
+__device__ __forceinline__ VelMass vm_load(const VelMass *__restrict__ gv, int k, int e) {
+    if (k < e) return gv[k];
+    VelMass z;
+    z.vx = z.vy = z.vz = z.m = 0.0;
+    return z;
+}
+
+// Per cell (members in list order): count, mass, mass-weighted mean velocity, then the
+// dispersion; every member's entry gets the cell's index.  Most cells hold a few members, so
+// cells of up to kPscSmall members take one thread each (plain sequential FP64 adds, and the
+// divisions of 32 cells share one warp instruction); larger cells take one warp each.
+constexpr int kPscSmall = 32;
+
+__global__ void psc_small_kernel(const int *__restrict__ nrun_p, const int *__restrict__ runstart,
+                                 const int *__restrict__ vals, const VelMass *__restrict__ gv,
+                                 double4 *__restrict__ cell_v, double *__restrict__ cell_sig, int *__restrict__ rid) {
+    const int nrun = *nrun_p;
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < nrun; r += (int64_t)gridDim.x * blockDim.x) {
+        const int b = runstart[r], e = runstart[r + 1];
+        if (e - b > kPscSmall) continue;
+        double mass = 0.0, sx = 0.0, sy = 0.0, sz = 0.0;
+        for (int k = b; k < e; ++k) {
+            const VelMass p = gv[k];
+            sx = __dadd_rn(sx, __dmul_rn(p.vx, p.m));
+            sy = __dadd_rn(sy, __dmul_rn(p.vy, p.m));
+            sz = __dadd_rn(sz, __dmul_rn(p.vz, p.m));
+            mass = __dadd_rn(mass, p.m);
+            rid[vals[k]] = (int)r;
+        }
+        const double q = (double)(e - b);
+        const double ux = __ddiv_rn(sx, mass), uy = __ddiv_rn(sy, mass), uz = __ddiv_rn(sz, mass);
+        double s2 = 0.0;
+        for (int k = b; k < e; ++k) {
+            const VelMass p = gv[k];
+            const double dx = __dsub_rn(ux, p.vx), dy = __dsub_rn(uy, p.vy), dz = __dsub_rn(uz, p.vz);
+            s2 = __dadd_rn(s2, __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz)));
+        }
+        cell_v[r] = make_double4(ux, uy, uz, q);
+        cell_sig[r] = __dsqrt_rn(__ddiv_rn(__ddiv_rn(s2, 3.0), q));
+    }
+}
+
+// Cells of more than kPscSmall members, one warp each: the lanes take 32 members at a time and
+// form their products; the sums are the sequential FP64 ones, added 32 values at a time in
+// integer ulps (seqsum.cuh), so the warp does not wait on a chain of FP64 adds.
 __global__ void psc_run_kernel(const int *__restrict__ nrun_p, const int *__restrict__ runstart,
-                               const int *__restrict__ vals, const int *__restrict__ list, const int *__restrict__ mem,
-                               const double *__restrict__ vx, const double *__restrict__ vy,
-                               const double *__restrict__ vz, const double *__restrict__ m,
+                               const int *__restrict__ vals, const VelMass *__restrict__ gv,
                                double4 *__restrict__ cell_v, double *__restrict__ cell_sig, int *__restrict__ rid) {
     const int lane = threadIdx.x & 31;
     const int nrun = *nrun_p;
     const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
     for (int64_t r = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; r < nrun; r += warps) {
         const int b = runstart[r], e = runstart[r + 1];
-        double q = 0.0, mass = 0.0, sx = 0.0, sy = 0.0, sz = 0.0;
+        if (e - b <= kPscSmall) continue;
+        SeqSum mass, sx, sy, sz;
+        seq_init(mass);
+        seq_init(sx);
+        seq_init(sy);
+        seq_init(sz);
+        VelMass nxt = vm_load(gv, b + lane, e);
         for (int k0 = b; k0 < e; k0 += 32) {
             const int k = k0 + lane;
-            // the products v*m do not depend on the sums: each lane forms its own, then the
-            // warp adds them in order (the FP64 pipe is the limit here)
-            double a = 0.0, c = 0.0, d = 0.0, mi = 0.0;
+            const VelMass p = nxt;
+            nxt = vm_load(gv, k + 32, e);
+            double a = 0.0, c = 0.0, d = 0.0;
             if (k < e) {
-                const int i = mem[list[vals[k]]];
-                mi = m[i];
-                a = __dmul_rn(vx[i], mi);
-                c = __dmul_rn(vy[i], mi);
-                d = __dmul_rn(vz[i], mi);
+                a = __dmul_rn(p.vx, p.m);
+                c = __dmul_rn(p.vy, p.m);
+                d = __dmul_rn(p.vz, p.m);
                 rid[vals[k]] = (int)r;
             }
             const int cnt = e - k0 < 32 ? e - k0 : 32;
-            for (int t = 0; t < cnt; ++t) {
-                sx = __dadd_rn(sx, __shfl_sync(0xffffffffu, a, t));
-                sy = __dadd_rn(sy, __shfl_sync(0xffffffffu, c, t));
-                sz = __dadd_rn(sz, __shfl_sync(0xffffffffu, d, t));
-                mass = __dadd_rn(mass, __shfl_sync(0xffffffffu, mi, t));
-            }
-            q += (double)cnt;
+            seq_add_warp(sx, a, cnt, lane);
+            seq_add_warp(sy, c, cnt, lane);
+            seq_add_warp(sz, d, cnt, lane);
+            seq_add_warp(mass, p.m, cnt, lane);
         }
-        const double ux = __ddiv_rn(sx, mass), uy = __ddiv_rn(sy, mass), uz = __ddiv_rn(sz, mass);
-        double s2 = 0.0;
+        const double q = (double)(e - b), M = seq_value(mass);
+        const double ux = __ddiv_rn(seq_value(sx), M), uy = __ddiv_rn(seq_value(sy), M), uz = __ddiv_rn(seq_value(sz), M);
+        SeqSum s2;
+        seq_init(s2);
+        nxt = vm_load(gv, b + lane, e);
         for (int k0 = b; k0 < e; k0 += 32) {
             const int k = k0 + lane;
+            const VelMass p = nxt;
+            nxt = vm_load(gv, k + 32, e);
             double t2 = 0.0;
             if (k < e) {
-                const int i = mem[list[vals[k]]];
-                const double dx = __dsub_rn(ux, vx[i]), dy = __dsub_rn(uy, vy[i]), dz = __dsub_rn(uz, vz[i]);
+                const double dx = __dsub_rn(ux, p.vx), dy = __dsub_rn(uy, p.vy), dz = __dsub_rn(uz, p.vz);
                 t2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
             }
-            const int cnt = e - k0 < 32 ? e - k0 : 32;
-            for (int t = 0; t < cnt; ++t) s2 = __dadd_rn(s2, __shfl_sync(0xffffffffu, t2, t));
+            seq_add_warp(s2, t2, e - k0 < 32 ? e - k0 : 32, lane);
         }
         if (lane == 0) {
             cell_v[r] = make_double4(ux, uy, uz, q);
-            cell_sig[r] = __dsqrt_rn(__ddiv_rn(__ddiv_rn(s2, 3.0), q));
+            cell_sig[r] = __dsqrt_rn(__ddiv_rn(__ddiv_rn(seq_value(s2), 3.0), q));
         }
     }
 }
@@ -527,6 +592,7 @@ extern "C" int halma_phase_space_clean(int64_t n, const double *x, const double 
     const size_t o_own = L.add(4ull * NL), o_kin = L.add(8ull * NL), o_kout = L.add(8ull * NL);
     const size_t o_vin = L.add(4ull * NL), o_vout = L.add(4ull * NL), o_head = L.add(4ull * NL);
     const size_t o_rpos = L.add(4ull * NL), o_rid = L.add(4ull * NL), o_cv = L.add(32ull * NL);
+    const size_t o_gv = L.add(sizeof(VelMass) * NL);
     const size_t o_sig = L.add(8ull * NL), o_flag = L.add(4ull * (NL + 1)), o_pos = L.add(4ull * NL);
     const size_t o_w = L.add(12ull * NL), o_nw = L.add(8ull * G), o_cnt = L.add(64);
     const int S = G >= 8192 ? 1 : 16;   // blocks per group for the centre and furthest particle
@@ -544,6 +610,7 @@ extern "C" int halma_phase_space_clean(int64_t n, const double *x, const double 
     int *vin = at<int>(base, o_vin), *vout = at<int>(base, o_vout), *head = at<int>(base, o_head);
     int *rpos = at<int>(base, o_rpos), *rid = at<int>(base, o_rid);
     auto *cv = at<double4>(base, o_cv);
+    auto *gv = at<VelMass>(base, o_gv);
     double *csig = at<double>(base, o_sig);
     int *flag = at<int>(base, o_flag), *pos = at<int>(base, o_pos);
     int *wbuf = dwhich ? dwhich : at<int>(base, o_w);
@@ -613,8 +680,9 @@ extern "C" int halma_phase_space_clean(int64_t n, const double *x, const double 
                 HALMA_TRY(exclusive_sum_i32(tmp, scan_b, head, rpos, (int)nl, st));
                 HALMA_CUDA(cudaMemsetAsync(cnt + 2, 0, 4, st));
                 HALMA_LAUNCH(psc_runstart_kernel, gl, 256, 0, st, nl, kout, head, rpos, flag, cnt + 2);
-                HALMA_LAUNCH(psc_run_kernel, sms * 16, 256, 0, st, cnt + 2, flag, vout, list, dmem, dvx, dvy, dvz, dm,
-                             cv, csig, rid);
+                HALMA_LAUNCH(psc_gather_kernel, gl, 256, 0, st, nl, vout, list, dmem, dvx, dvy, dvz, dm, gv);
+                HALMA_LAUNCH(psc_small_kernel, sms * 8, 256, 0, st, cnt + 2, flag, vout, gv, cv, csig, rid);
+                HALMA_LAUNCH(psc_run_kernel, sms * 16, 256, 0, st, cnt + 2, flag, vout, gv, cv, csig, rid);
                 HALMA_LAUNCH(psc_sweep_kernel, gl, 256, 0, st, nl, list, own, off, dgoff, dmem, dvx, dvy, dvz, cv, csig,
                              rid, p.q_fil, p.sig_fil, state, dctl);
             }

@@ -23,6 +23,31 @@ import numpy as np
 from . import _lib
 
 
+def sequential_sums(values, offsets):
+    """Left-to-right FP64 sum of every segment values[offsets[s]:offsets[s+1]], rounded after
+    each addition like the reference's numba loops (the building block of the per-cell sums);
+    C ABI ``halma_sequential_sum_f64``.  Host or device arrays; returns float64 [segments]."""
+    dev = _lib._is_torch(values)
+    if dev:
+        nseg = int(offsets.shape[0]) - 1
+        out = _lib.like(values, (max(nseg, 0),), np.float64)
+        n = int(values.shape[0])
+        arrs = (values, offsets)
+    else:
+        values = _lib.as_host(values, np.float64)
+        offsets = _lib.as_host(offsets, np.int64)
+        nseg = offsets.shape[0] - 1
+        n = values.shape[0]
+        out = np.zeros(max(nseg, 0), dtype=np.float64)
+        arrs = (values, offsets)
+    if nseg <= 0:
+        return out
+    st = _lib.lib().halma_sequential_sum_f64(n, _lib.ptr(arrs[0]), nseg, _lib.ptr(arrs[1]), _lib.ptr(out),
+                                             _lib.stream_of(*arrs))
+    _lib.check(st, "halma_sequential_sum_f64")
+    return out
+
+
 def clean_groups(offsets, members, st_x, st_y, st_z, st_vx, st_vy, st_vz, st_mass, LL, Q_FIL, SIG_FIL,
                  PSC_FLAG=True, MINP=50, min_part_PSC=50, max_passes=100_000):
     """CSR form: returns (control uint8 [members], which_cell int32 [3, members] with group

@@ -141,3 +141,16 @@ def test_ball_gather_rejects_bad_arguments():
     assert g(nb=-1) == _lib.ERR_INVALID
     assert L.halma_ball_gather(4, None, None, None, 2, *[_lib.ptr(c)] * 4, 0, None, None, 0, ctypes.byref(n_found),
                                None) == _lib.ERR_INVALID
+
+
+def test_sequential_sum_rejects_bad_arguments():
+    L = _lib.lib()
+    v = np.ones(4)
+    out = np.zeros(3)
+    s = lambda o, n=4: L.halma_sequential_sum_f64(n, _lib.ptr(v), len(o) - 1, _lib.ptr(o), _lib.ptr(out), None)
+    assert s(np.array([0, 2, 4], dtype=np.int64), n=-1) == _lib.ERR_INVALID
+    assert s(np.array([0, 3], dtype=np.int64)) == _lib.ERR_INVALID                # offsets do not reach n
+    assert s(np.array([0, 3, 2, 4], dtype=np.int64)) == _lib.ERR_INVALID          # decreasing offsets
+    assert s(np.array([1, 2, 4], dtype=np.int64)) == _lib.ERR_INVALID             # offsets do not start at 0
+    assert L.halma_sequential_sum_f64(4, None, 2, _lib.ptr(np.array([0, 2, 4], dtype=np.int64)), _lib.ptr(out),
+                                      None) == _lib.ERR_INVALID

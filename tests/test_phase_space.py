@@ -118,3 +118,47 @@ def test_groups_that_clean_away(cuda):
         assert list(got["num_particles"]) == list(ref["num_particles"])
         for k in ("which_x", "which_y", "which_z"):
             assert all(np.array_equal(a, b) for a, b in zip(got[k], ref[k]))
+
+
+def _sequential(v):
+    """The reference's loop: s = 0.0, then s += v[i] in order, each addition rounded."""
+    return float(np.add.accumulate(np.concatenate([[0.0], np.asarray(v, dtype=np.float64)]))[-1])
+
+
+@pytest.mark.gpu
+def test_sequential_sums_are_the_scalar_loop(cuda):
+    """The building block of the per-cell sums against the scalar FP64 loop, bit for bit:
+    sums that change sign, cancel to zero, cross binades, meet ties of half an ulp, hold
+    subnormals, infinities and NaN; segments of 0 to 3000 values."""
+    from pyhalma_gb300 import phase_space
+    rng = np.random.default_rng(31)
+    u = 2.0 ** -53
+    segs = [np.zeros(0), np.array([-0.0]), np.array([1.0, -1.0]), np.array([5e-324, -5e-324, 5e-324]),
+            np.array([1e308, 1e308, -1e308]), np.array([1.0, np.inf, -np.inf]), np.array([np.nan, 1.0]),
+            np.concatenate([[1.0], rng.integers(-8, 9, 3000) * u]),
+            np.concatenate([[1e300, -1e300], rng.normal(0, 1, 500)])]
+    for kind in range(40):
+        n = int(rng.integers(1, 3000))
+        if kind % 5 == 0:
+            v = rng.normal(0, 1, n)
+        elif kind % 5 == 1:
+            v = rng.normal(250, 60, n) * rng.uniform(1e5, 1e7, n)            # mass x velocity
+        elif kind % 5 == 2:
+            v = rng.normal(0, 1, n) * np.exp(rng.uniform(-30, 30, n))
+        elif kind % 5 == 3:
+            v = np.full(n, 0.1) * np.where(rng.random(n) < 0.4, -1.0, 1.0)
+        else:
+            h = rng.normal(0, 1, n // 2)
+            v = np.concatenate([h, -h[::-1], [0.0]])
+        segs.append(v)
+    off = np.zeros(len(segs) + 1, dtype=np.int64)
+    np.cumsum([len(s) for s in segs], out=off[1:])
+    vals = np.concatenate(segs)
+    got = phase_space.sequential_sums(vals, off)
+    want = np.array([_sequential(s) for s in segs])
+    assert np.array_equal(got, want, equal_nan=True)
+    num = ~np.isnan(want)                     # signed zeros agree too (a NaN's sign bit is not defined)
+    assert np.array_equal(np.signbit(got[num]), np.signbit(want[num]))
+    import torch
+    T = lambda a: torch.from_numpy(a).to(cuda)
+    assert np.array_equal(phase_space.sequential_sums(T(vals), T(off)).cpu().numpy(), want, equal_nan=True)
