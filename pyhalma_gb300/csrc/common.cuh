@@ -80,15 +80,16 @@ struct Stager {
         bool in, out, host;
         size_t off;
         void **slot;
+        bool late;   // uploaded on the late stream of bind_and_upload, when one is given
     };
     std::vector<Item> items;
     bool any_host = false;
 
     // `slot` receives the device pointer the kernels must use.
     template <class T, class U>
-    void add(const T *user, size_t count, bool in, bool out, U **slot) {
+    void add(const T *user, size_t count, bool in, bool out, U **slot, bool late = false) {
         Item it{user, count * sizeof(T), in, out, false, 0,
-                reinterpret_cast<void **>(const_cast<typename std::remove_const<U>::type **>(slot))};
+                reinterpret_cast<void **>(const_cast<typename std::remove_const<U>::type **>(slot)), late};
         if (user && count > 0) it.host = !is_device_pointer(user);
         any_host |= it.host;
         items.push_back(it);
@@ -97,7 +98,9 @@ struct Stager {
         for (auto &it : items)
             if (it.host) it.off = L.add(it.bytes);
     }
-    int bind_and_upload(void *base, cudaStream_t s) {
+    // Host inputs are copied on s, or (items added as late) on late_s, which the caller makes
+    // s wait for before their first use.
+    int bind_and_upload(void *base, cudaStream_t s, cudaStream_t late_s = nullptr) {
         for (auto &it : items) {
             if (!it.user || it.bytes == 0) {
                 *it.slot = const_cast<void *>(it.user);
@@ -105,7 +108,9 @@ struct Stager {
             }
             if (it.host) {
                 *it.slot = at<void>(base, it.off);
-                if (it.in) HALMA_CUDA(cudaMemcpyAsync(*it.slot, it.user, it.bytes, cudaMemcpyHostToDevice, s));
+                if (it.in)
+                    HALMA_CUDA(cudaMemcpyAsync(*it.slot, it.user, it.bytes, cudaMemcpyHostToDevice,
+                                               it.late && late_s ? late_s : s));
             } else {
                 *it.slot = const_cast<void *>(it.user);
             }

@@ -4,6 +4,8 @@
 #include <math.h>
 #include <string.h>
 
+#include <map>
+
 #include "common.cuh"
 #include "unbind.cuh"
 
@@ -31,6 +33,24 @@ __global__ void scatter_bound_kernel(int64_t nm, const int *__restrict__ members
                                      unsigned char *__restrict__ bound) {
     for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < nm; k += (int64_t)gridDim.x * blockDim.x)
         bound[members[k]] = bs[k];
+}
+
+// A second stream (and its completion event) per device, for the host-to-device copies of the
+// velocities and masses, which overlap the FoF stage (it reads positions only).
+struct SideStream {
+    cudaStream_t s = nullptr;
+    cudaEvent_t done = nullptr;
+};
+
+int side_stream(SideStream **out) {
+    static std::map<int, SideStream> m;
+    SideStream &ss = m[current_device()];
+    if (!ss.s) {
+        HALMA_CUDA(cudaStreamCreateWithFlags(&ss.s, cudaStreamNonBlocking));
+        HALMA_CUDA(cudaEventCreateWithFlags(&ss.done, cudaEventDisableTiming));
+    }
+    *out = &ss;
+    return HALMA_OK;
 }
 
 }  // namespace
@@ -71,10 +91,10 @@ extern "C" int halma_find_haloes(int64_t n, const double *x, const double *y, co
     sg.add(x, n, true, false, &dx);
     sg.add(y, n, true, false, &dy);
     sg.add(z, n, true, false, &dz);
-    sg.add(vx, n, true, false, &dvx);
-    sg.add(vy, n, true, false, &dvy);
-    sg.add(vz, n, true, false, &dvz);
-    sg.add(m, n, true, false, &dm);
+    sg.add(vx, n, true, false, &dvx, true);
+    sg.add(vy, n, true, false, &dvy, true);
+    sg.add(vz, n, true, false, &dvz, true);
+    sg.add(m, n, true, false, &dm, true);
     // private scratch for everything that must outlive the individual stages
     Layout L;
     sg.plan(L);
@@ -87,7 +107,11 @@ extern "C" int halma_find_haloes(int64_t n, const double *x, const double *y, co
         void *p = nullptr;
     } buf;
     HALMA_TRY(workspace(L.total, &buf.p, st, 1));
-    HALMA_TRY(sg.bind_and_upload(buf.p, st));
+    // velocities and masses from host memory are copied on a side stream while FoF runs
+    SideStream *side = nullptr;
+    HALMA_TRY(side_stream(&side));
+    HALMA_TRY(sg.bind_and_upload(buf.p, st, side->s));
+    HALMA_CUDA(cudaEventRecord(side->done, side->s));
     int *dlab = at<int>(buf.p, o_lab);
     int64_t *doff = at<int64_t>(buf.p, o_off);
     int *dmem = at<int>(buf.p, o_mem);
@@ -107,6 +131,7 @@ extern "C" int halma_find_haloes(int64_t n, const double *x, const double *y, co
     if (prof.enabled) HALMA_CUDA(cudaEventRecord(ev[1], st));
     *n_haloes = ng;
     HALMA_CUDA(cudaMemsetAsync(dbnd, 0, n, st));
+    HALMA_CUDA(cudaStreamWaitEvent(st, side->done, 0));
     if (ng > 0) {
         const int g = std::min(device_sm_count() * 8, grid_for(nm, 256));
         HALMA_LAUNCH(gather7_kernel, g, 256, 0, st, nm, dmem, dx, dy, dz, dvx, dvy, dvz, dm, g7);

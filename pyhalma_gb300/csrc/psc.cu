@@ -306,7 +306,7 @@ __device__ __forceinline__ VelMass vm_load(const VelMass *__restrict__ gv, int k
 // dispersion; every member's entry gets the cell's index.  Most cells hold a few members, so
 // cells of up to kPscSmall members take one thread each (plain sequential FP64 adds, and the
 // divisions of 32 cells share one warp instruction); larger cells take one warp each.
-constexpr int kPscSmall = 32;
+constexpr int kPscSmall = 128;
 
 __global__ void psc_small_kernel(const int *__restrict__ nrun_p, const int *__restrict__ runstart,
                                  const int *__restrict__ vals, const VelMass *__restrict__ gv,
