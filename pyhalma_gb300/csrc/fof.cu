@@ -1106,14 +1106,14 @@ __global__ void group_keys_kernel(int n, const int *__restrict__ labels, uint32_
                                   int *__restrict__ vals) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const int l = labels[i];
-        keys[i] = l < 0 ? 0xffffffffu : (uint32_t)l;
+        keys[i] = l < 0 ? (uint32_t)n : (uint32_t)l;   // particles without a friend sort last
         vals[i] = i;
     }
 }
 
 __global__ void group_heads_kernel(int n, const uint32_t *__restrict__ keys, int *__restrict__ head) {
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x)
-        head[k] = (keys[k] != 0xffffffffu && (k == 0 || keys[k] != keys[k - 1])) ? 1 : 0;
+        head[k] = (keys[k] != (uint32_t)n && (k == 0 || keys[k] != keys[k - 1])) ? 1 : 0;
 }
 
 // gstart[gid] = first sorted position of group gid; cnt[0] = groups, cnt[1] = members
@@ -1121,8 +1121,8 @@ __global__ void group_starts_kernel(int n, const uint32_t *__restrict__ keys, co
                                     const int *__restrict__ gid, int *__restrict__ gstart, int *__restrict__ cnt) {
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
         if (head[k]) gstart[gid[k]] = k;
-        const bool valid = keys[k] != 0xffffffffu;
-        const bool last_valid = valid && (k == n - 1 || keys[k + 1] == 0xffffffffu);
+        const bool valid = keys[k] != (uint32_t)n;
+        const bool last_valid = valid && (k == n - 1 || keys[k + 1] == (uint32_t)n);
         if (last_valid) {
             cnt[0] = gid[k] + head[k];
             cnt[1] = k + 1;
@@ -1138,7 +1138,7 @@ __global__ void group_keep_kernel(int n, const uint32_t *__restrict__ keys, cons
     const int ng = cnt[0];
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
         int kp = 0;
-        if (keys[k] != 0xffffffffu) {
+        if (keys[k] != (uint32_t)n) {
             const int g = gid[k] + head[k] - 1;
             kp = (gstart[g + 1] - gstart[g]) >= minp;
         }
@@ -1193,7 +1193,8 @@ int fof_groups_device(int n, const int *labels, int minp, int64_t *offsets, int 
     HALMA_CUDA(cudaMemsetAsync(cnt, 0, 64, st));
     HALMA_CUDA(cudaMemsetAsync(offsets, 0, sizeof(int64_t), st));
     HALMA_LAUNCH(group_keys_kernel, g1, 256, 0, st, n, labels, kin, vin);
-    HALMA_TRY(sort_pairs_u32_i32(tmp, sort_b, kin, kout, vin, vout, n, 32, st));
+    // labels are < n, and n marks a particle without a friend: only the bits of n are sorted
+    HALMA_TRY(sort_pairs_u32_i32(tmp, sort_b, kin, kout, vin, vout, n, bits_for((uint64_t)n), st));
     HALMA_LAUNCH(group_heads_kernel, g1, 256, 0, st, n, kout, head);
     HALMA_TRY(exclusive_sum_i32(tmp, scan_b, head, gid, n, st));
     HALMA_LAUNCH(group_starts_kernel, g1, 256, 0, st, n, kout, head, gid, gst, cnt);

@@ -284,7 +284,7 @@ __global__ void __launch_bounds__(256) red_walk_kernel(const int64_t *__restrict
     const int64_t nmem = (int64_t)r.n;
     const double half = 0.5 * r.mref;
     const int lane = threadIdx.x & 31;
-    __shared__ double tile[1024];
+    __shared__ double tile[2][1024];   // warp 0 walks one while the other warps fill the next
     __shared__ long long first;
     if (threadIdx.x == 0) first = LLONG_MAX;
     SeqSum q;   // lane 0's state (warp 0)
@@ -294,11 +294,16 @@ __global__ void __launch_bounds__(256) red_walk_kernel(const int64_t *__restrict
     q.hl = 0;
     q.e = 0;
     const bool plain = r.plain != 0.0;
+    for (int i = threadIdx.x; i < (nmem < 1024 ? (int)nmem : 1024); i += blockDim.x) tile[0][i] = m[order[b + i]];
     __syncthreads();
-    for (int64_t k0 = 0; k0 < nmem; k0 += 1024) {
+    int cur = 0;
+    for (int64_t k0 = 0; k0 < nmem; k0 += 1024, cur ^= 1) {
         const int cnt = nmem - k0 < 1024 ? (int)(nmem - k0) : 1024;
-        for (int i = threadIdx.x; i < cnt; i += blockDim.x) tile[i] = m[order[b + k0 + i]];
-        __syncthreads();
+        if (threadIdx.x >= 32 && k0 + 1024 < nmem) {
+            const int64_t k1 = k0 + 1024;
+            const int cn = nmem - k1 < 1024 ? (int)(nmem - k1) : 1024;
+            for (int i = threadIdx.x - 32; i < cn; i += blockDim.x - 32) tile[cur ^ 1][i] = m[order[b + k1 + i]];
+        }
         if (threadIdx.x < 32) {
             long long f = LLONG_MAX;
             for (int q0 = 0; q0 < cnt && f == LLONG_MAX; q0 += 32) {
@@ -312,7 +317,7 @@ __global__ void __launch_bounds__(256) red_walk_kernel(const int64_t *__restrict
                         long long fl = 0;
                         int code = 0;
                         bool big = false;
-                        if (lane < nb) mass_ulps(tile[q0 + lane], e, fl, code, big);
+                        if (lane < nb) mass_ulps(tile[cur][q0 + lane], e, fl, code, big);
                         // increments without ties; a tie or a big mass forces the replay
                         const bool odd = big || code == 2;
                         long long inc = fl + (code == 1 ? 1 : 0);
@@ -329,8 +334,8 @@ __global__ void __launch_bounds__(256) red_walk_kernel(const int64_t *__restrict
                 }
                 if (replay && lane == 0) {
                     for (int u = 0; u < nb; ++u) {
-                        const bool over = plain ? ((q.c = __dadd_rn(q.c, tile[q0 + u])) > half)
-                                                : seq_add(q, tile[q0 + u], half);
+                        const bool over = plain ? ((q.c = __dadd_rn(q.c, tile[cur][q0 + u])) > half)
+                                                : seq_add(q, tile[cur][q0 + u], half);
                         if (over) {
                             f = k0 + q0 + u;
                             break;
