@@ -259,7 +259,7 @@ __device__ __forceinline__ int warp_incl_scan(int v, int lane) {
 // kernel instead: blocks of kSymBlock slots, one item per block pair (tb <= sb), B(B+1)/2
 // items for B blocks, listed from ystart[q]; the partial sums are then kept per block
 // (B slices of kSymBlock).  idesc[q].w is the number of partial slices the energy kernel adds.
-constexpr int kSymWarps = 8, kSymT = 4;
+constexpr int kSymWarps = 4, kSymT = 8;
 constexpr int kSymBlock = kSymWarps * 32 * kSymT;   // 1024 slots
 
 __global__ void __launch_bounds__(1024) ub_items_kernel(int nh, const int *__restrict__ order, const HaloState *hs,
@@ -565,14 +565,15 @@ __device__ __forceinline__ void chunk_pairs_sym(const float4 *sa, const float4 *
 
 // Full passes over the haloes of more than kSymBlock bound particles.  The halo's slots are
 // cut into blocks of kSymBlock; an item is a block pair (tb, sb), tb <= sb, taken by one CTA
-// from an atomic counter.  The CTA stages the source block in shared memory; warp w holds
-// targets tb*kSymBlock + w*128 + t*32 + lane.  Diagonal items (tb == sb) are plain (self pair
+// from an atomic counter.  The CTA (4 warps of 8 targets per lane, so that the source-side
+// reduce-scatter serves 8 targets) stages the source block in shared memory; warp w holds
+// targets tb*kSymBlock + w*256 + t*32 + lane.  Diagonal items (tb == sb) are plain (self pair
 // skipped) and write the targets' partial for slice sb.  Off-diagonal items compute each pair
 // once: the targets' partial goes to slice sb (part[qoff + sb*npad + r]) and the sources'
-// partial -- per source, the 8 warps' sums added in warp order, compensated -- to slice tb.  So
+// partial -- per source, the 4 warps' sums added in warp order, compensated -- to slice tb.  So
 // slot r of block b receives slice k from item (b, k) for k >= b and from item (k, b) for
 // k < b: every slice exactly once, and the energy kernel adds slices 0..B-1 in order.
-__global__ void __launch_bounds__(256) ub_pair_sym_kernel(const float4 *__restrict__ pk,
+__global__ void __launch_bounds__(128) ub_pair_sym_kernel(const float4 *__restrict__ pk,
                                                           const int64_t *__restrict__ poff,
                                                           const int64_t *__restrict__ qoff,
                                                           const HaloState *__restrict__ hs, int nh,
@@ -684,7 +685,7 @@ __global__ void __launch_bounds__(256) ub_pair_sym_kernel(const float4 *__restri
             for (int k = threadIdx.x; k < nch * 32; k += blockDim.x) {
                 const int s = s0 + k;
                 if (s < nb) {
-                    float sum = 0.f, comp = 0.f;   // the 8 warps' sums in warp order, compensated
+                    float sum = 0.f, comp = 0.f;   // the warps' sums in warp order, compensated
 #pragma unroll
                     for (int ww = 0; ww < kSymWarps; ++ww) two_sum_acc(sum, comp, spart[ww * kSymBlock + k]);
                     out[s] = df_from_acc(sum, comp);
@@ -1441,7 +1442,7 @@ int unbind_device(int64_t n, int nh, const int64_t *d_off, const int64_t *h_off,
         const int pgrid = device_sm_count() * std::max(bps, 1);
         constexpr int kSymSmem = kSymBlock * (int)sizeof(float4) + kSymWarps * kSymBlock * (int)sizeof(float);
         HALMA_CUDA(cudaFuncSetAttribute(ub_pair_sym_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSymSmem));
-        HALMA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, ub_pair_sym_kernel, 256, kSymSmem));
+        HALMA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, ub_pair_sym_kernel, 128, kSymSmem));
         const int ygrid = device_sm_count() * std::max(bps, 1);
         auto record = [&](cudaStream_t rs, int it0, int it1) -> int {
             // first pass: centre of mass and packing into buffer 0; every pass then compacts
@@ -1463,7 +1464,7 @@ int unbind_device(int64_t n, int nh, const int64_t *d_off, const int64_t *h_off,
                 // full passes: the big haloes' block pairs first (the longest items), then the
                 // tiles of the small ones; incremental passes have only tiles
                 if (!inc)
-                    HALMA_LAUNCH(ub_pair_sym_kernel, ygrid, 256, kSymSmem, rs, pkb[a], dpoff, dqoff, hs, nh, ystart,
+                    HALMA_LAUNCH(ub_pair_sym_kernel, ygrid, 128, kSymSmem, rs, pkb[a], dpoff, dqoff, hs, nh, ystart,
                                  idesc, cnt, cnt + 4, eps2, part2);
                 if (profiling) HALMA_CUDA(cudaEventRecordWithFlags(prof.evm[it], rs, cudaEventRecordExternal));
                 HALMA_LAUNCH(ub_pair_kernel, pgrid, 256, 0, rs, pkb[a], rk, inc, dpoff, dqoff, hs, nh, istart, idesc,
