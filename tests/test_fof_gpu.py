@@ -93,3 +93,20 @@ def test_dense_lattices_and_random_clusters_property(cuda):
     pts = synth.lattice_points(24, 0.0015, origin=(37.1, -12.3, 4.4), jitter_ulps=1, seed=4)
     lab = fof.fof_labels(pts[:, 0].copy(), pts[:, 1].copy(), pts[:, 2].copy(), 0.0015)
     assert np.array_equal(lab, oracle.fof_labels(pts[:, 0], pts[:, 1], pts[:, 2], 0.0015))
+
+
+def test_far_offsets_and_elongated_boxes(cuda):
+    """Cell keys from one FMA per axis stay exact far from the origin (a cloud 3e4 Mpc away) and
+    on grids millions of cells long on one axis (a chain of particles 0.5-1.2 LL apart)."""
+    rng = np.random.default_rng(23)
+    pts = rng.normal(0, 0.003, (20_000, 3)) + np.array([1.0e4, -2.5e4, 7.5e3])
+    lab = fof.fof_labels(pts[:, 0].copy(), pts[:, 1].copy(), pts[:, 2].copy(), 0.0007)
+    assert np.array_equal(lab, oracle.fof_labels(pts[:, 0], pts[:, 1], pts[:, 2], 0.0007))
+    n = 6000
+    chain = np.zeros((n, 3))
+    chain[:, 0] = 3.0e3 + np.cumsum(rng.uniform(0.5, 1.2, n)) * 0.001
+    chain[:, 1] = rng.normal(0, 2e-5, n)
+    chain[:, 2] = -4.0e2 + rng.normal(0, 2e-5, n)
+    chain = np.concatenate([chain, chain[::7] + np.array([0.0, 1.0, 0.0])])   # a second, sparser line
+    lab = fof.fof_labels(chain[:, 0].copy(), chain[:, 1].copy(), chain[:, 2].copy(), 0.001)
+    assert np.array_equal(lab, oracle.fof_labels(chain[:, 0], chain[:, 1], chain[:, 2], 0.001))
