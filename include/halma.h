@@ -42,7 +42,7 @@
  *                                    particle_subroutines.f90:12-461 as called at
  *                                    pyHALMA.py:930-1016
  *   halma_sequential_sum_f64      <- the scalar FP64 accumulation loops of the numba kernels
- *                                    (e.g. halo_properties.py:173-197), exposed on its own
+ *                                    (e.g. halo_properties.py:120-157), exposed on its own
  */
 #ifndef HALMA_H
 #define HALMA_H
@@ -233,7 +233,7 @@ int halma_ball_gather(int64_t n, const double *x, const double *y, const double 
 
 /* Sequential FP64 sums: out[s] = values[offsets[s]] + values[offsets[s]+1] + ... added left to
  * right and rounded after every addition, as the reference's numba loops add (e.g. the
- * per-cell sums of clean_cell, halo_properties.py:173-197).  The GPU adds 32 values at a time
+ * per-cell sums of calc_cell, halo_properties.py:120-157).  The GPU adds 32 values at a time
  * in integer ulps of the running sum's binade and falls back to one IEEE add where the sum
  * leaves its binade, changes sign or meets a tie, so the result equals the scalar loop bit
  * for bit for any finite or non-finite input.  offsets[n_segments+1] runs from 0 to n. */

@@ -264,7 +264,7 @@ __device__ __forceinline__ bool kin_part_of(int bid, int S, int G, const int64_t
     return true;
 }
 
-// Phase 1: angular momentum (halo_properties.py:463-482); the last block stores j, |j| and the
+// Phase 1: angular momentum (halo_properties.py:461-482); the last block stores j, |j| and the
 // unit vector for phase 2.
 __global__ void __launch_bounds__(256) pr_kin1_kernel(int G, int S, const int64_t *__restrict__ off,
                                                       const double *__restrict__ g, int64_t nm,
@@ -316,8 +316,8 @@ __global__ void __launch_bounds__(256) pr_kin1_kernel(int G, int S, const int64_
     }
 }
 
-// Phase 2: kappa_co (halo_properties.py:781-866) and the Tully-Fisher shell velocity
-// (:484-515); the last block writes the group's outputs.
+// Phase 2: kappa_co (kinematic_morphology, halo_properties.py:483-517) and the Tully-Fisher
+// shell velocity (tully_fisher_velocity, :63-96); the last block writes the group's outputs.
 __global__ void __launch_bounds__(256) pr_kin2_kernel(int G, int S, const int64_t *__restrict__ off,
                                                       const double *__restrict__ g, int64_t nm,
                                                       const double *__restrict__ cen, double *__restrict__ out,

@@ -1,7 +1,7 @@
 // halma_sequential_sum_f64: the left-to-right FP64 sum of every segment, rounded after each
 // addition exactly as a scalar loop would, with the warp-wide integer-ulp adds of seqsum.cuh.
 // It is the building block of the cleaning's per-cell sums (a numba loop in the reference,
-// python_scripts/halo_properties.py:173-197) and lets the tests pin that building block against
+// python_scripts/halo_properties.py:120-157) and lets the tests pin that building block against
 // numpy's sequential accumulation on any values.
 #include <string.h>
 
