@@ -792,7 +792,8 @@ extern "C" int halma_halo_properties(int64_t n, const double *x, const double *y
         HALMA_LAUNCH(pr_pkeys_kernel, gN, 256, 0, st, N0, G, doff, own, gbuf, dcen, linking_length, cbits, kin, vin);
         const int n3 = (int)(3 * N0);
         const int g3 = std::min(sms * 8, grid_for(n3, 256));
-        HALMA_TRY(sort_pairs_u64_i32(tmp, sort_b, kin, kout, vin, vout, n3, 64, st));
+        // keys hold (3 group + projection) above cbits of cell index: sort only those bits
+        HALMA_TRY(sort_pairs_u64_i32(tmp, sort_b, kin, kout, vin, vout, n3, cbits + nbits((uint64_t)3 * G), st));
         HALMA_LAUNCH(pr_head_kernel, g3, 256, 0, st, n3, kout, head);
         HALMA_TRY(exclusive_sum_i32(tmp, scan_b, head, rpos, n3, st));
         int last[2];

@@ -450,7 +450,9 @@ int reductions_device(int64_t n, int nh, const int64_t *off, const double *x, co
         HALMA_LAUNCH(iota_kernel, g, 256, 0, st, n, v0);
         HALMA_TRY(sort_pairs_u64_i32(tmp, s64, dk, dk2, v0, v1, (int)n, 64, st));
         HALMA_LAUNCH(gather_hid_kernel, g, 256, 0, st, n, v1, hid, hid2);
-        HALMA_TRY(sort_pairs_u32_i32(tmp, s32, hid2, hid3, v1, v2, (int)n, 32, st));
+        int hbits = 1;   // halo ids are < nh: sort only their bits
+        while (hbits < 32 && ((uint64_t)(nh - 1) >> hbits) != 0) ++hbits;
+        HALMA_TRY(sort_pairs_u32_i32(tmp, s32, hid2, hid3, v1, v2, (int)n, hbits, st));
     }
     HALMA_LAUNCH(red_walk_kernel, nh, 256, 0, st, off, v2, dist, m, red);
     HALMA_LAUNCH(red_sigma_kernel, cmax, 256, 0, st, nh, off, cst, chunk_h, dist, vx, vy, vz, mask, red, part2);
