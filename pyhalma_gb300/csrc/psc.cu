@@ -42,7 +42,7 @@ enum { kModeNone = 0, kModeSweep = 1, kModeFinal = 2 };
 
 struct PscState {
     double cx, cy, cz, M, rr;
-    double start, next, delta, step, inv_step;
+    double start, next, delta, step, inv_step, inv_delta, margin;
     double fac_sig;
     long long n, n0;              // grid points per axis: current, and of the first grid
     long long cleaned, remaining;
@@ -54,9 +54,20 @@ __device__ __forceinline__ double grid_at(const PscState &s, long long i) {
     return i == 0 ? s.start : (i == 1 ? s.next : __dadd_rn(s.start, __dmul_rn((double)i, s.delta)));
 }
 
-// The first guess uses the reciprocal of the step (GB300's FP64 divide is a long sequence):
-// it is within one point of the nearest grid point, and the two neighbours are checked.
+// The grid points are a[i] = start + i * delta rounded, so t = (v - start) / delta locates v
+// among them to within ~3n x 1.1e-16 points.  Unless t lies within `margin` (1e-12 (n + 8),
+// thousands of times that error) of a midpoint, the nearest point is t rounded (clamped to the
+// grid); otherwise it is decided on the grid's own values: the guess from the reciprocal of the
+// step (GB300's FP64 divide is a long sequence) is within one point, and both neighbours are
+// checked, ties going to the first index as numpy's argmin.
 __device__ __forceinline__ long long nearest(const PscState &s, double v) {
+    {
+        const double t = (v - s.start) * s.inv_delta, fl = floor(t), f = t - fl;
+        if (fabs(f - 0.5) > s.margin) {
+            const long long k = (long long)fl + (f > 0.5 ? 1 : 0);
+            return k < 0 ? 0 : (k > s.n - 1 ? s.n - 1 : k);
+        }
+    }
     long long k = (long long)floor((v - s.start) * s.inv_step + 0.5);
     k = k < 0 ? 0 : (k > s.n - 1 ? s.n - 1 : k);
     long long best = k;
@@ -219,8 +230,10 @@ __global__ void __launch_bounds__(256) psc_rmax_kernel(int G, const int64_t *__r
             s.inv_step = 1.0 / step;
             s.next = __dadd_rn(start, step);
             s.delta = __dsub_rn(s.next, start);
+            s.inv_delta = 1.0 / s.delta;
             s.n = (long long)ceil(__ddiv_rn(__dsub_rn(stop, start), step));
             if (s.n < 1) s.n = 1;
+            s.margin = 1e-12 * (double)(s.n + 8);
             if (s.first) s.n0 = s.n;
         }
     }
@@ -411,11 +424,28 @@ __global__ void psc_sweep_kernel(int64_t nl, const int *__restrict__ list, const
         const double q = c.w;
         bool drop = true;
         if (q > q_fil) {
-            const double dx = __dsub_rn(c.x, vx[i]), dy = __dsub_rn(c.y, vy[i]), dz = __dsub_rn(c.z, vz[i]);
-            double bas = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz)));
+            const double thr = __dmul_rn(st[h].fac_sig, sig_fil);
             const bool norm = st[h].first ? q > 2.0 : q >= 2.0;
-            bas = norm ? __ddiv_rn(bas, cell_sig[rid[e]]) : 0.0;
-            drop = bas >= __dmul_rn(st[h].fac_sig, sig_fil);
+            if (!norm) {
+                drop = 0.0 >= thr;   // the reference's bas = 0 when the cell is not normalised
+            } else {
+                const double dx = __dsub_rn(c.x, vx[i]), dy = __dsub_rn(c.y, vy[i]), dz = __dsub_rn(c.z, vz[i]);
+                const double d2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+                const double sig = cell_sig[rid[e]];
+                // sqrt(d2) / sig >= thr, rounded as the reference rounds it: far from the threshold
+                // (relative 4e-12, against rounding errors of ~5e-16) the squares decide it without
+                // the FP64 square root and divide; near it, or for a zero or non-finite sigma, the
+                // reference's operations do
+                const double ts = thr * sig, t2 = ts * ts;
+                const bool ok = sig > 0.0 && thr > 0.0 && t2 >= 2.2250738585072014e-308 && t2 < 1e300;
+                if (ok && d2 > t2 * (1.0 + 4e-12)) {
+                    drop = true;
+                } else if (ok && d2 < t2 * (1.0 - 4e-12)) {
+                    drop = false;
+                } else {
+                    drop = __ddiv_rn(__dsqrt_rn(d2), sig) >= thr;
+                }
+            }
         }
         if (drop) {
             control[goff[h] + (e - off[h])] = 0;   // position in the list being swept
