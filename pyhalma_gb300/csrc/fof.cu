@@ -317,7 +317,22 @@ __device__ __forceinline__ int lower_bound_key(const uint64_t *__restrict__ keys
     return lo;
 }
 
-__global__ void __launch_bounds__(256) dense_cell_kernel(const int *__restrict__ ncell_p, const int *__restrict__ cell_start,
+// Cells of fewer than kDenseMin particles, one thread each: one component when the first and
+// last particles share a sub-cell run; the dense cells are listed for dense_cell_kernel (the
+// list order does not matter: each dense cell only joins runs of its own).
+__global__ void small_cell_kernel(const int *__restrict__ ncell_p, const int *__restrict__ cell_start,
+                                  const uint64_t *__restrict__ keys, unsigned char *__restrict__ conn,
+                                  int *__restrict__ dense, int *__restrict__ ndense) {
+    const int nc = *ncell_p;
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x) {
+        const int cs = cell_start[c], ce = cell_start[c + 1];
+        if (ce - cs < kDenseMin) conn[c] = keys[cs] == keys[ce - 1] ? 1 : 0;
+        else dense[atomicAdd(ndense, 1)] = c;
+    }
+}
+
+__global__ void __launch_bounds__(256) dense_cell_kernel(const int *__restrict__ ndense_p, const int *__restrict__ dense,
+                                                         const int *__restrict__ cell_start,
                                                          const uint64_t *__restrict__ keys, int *__restrict__ parent,
                                                          unsigned char *__restrict__ has, unsigned char *__restrict__ conn) {
     __shared__ unsigned long long nbmask[64];   // guaranteed-link neighbours of each sub-cell (Morton codes)
@@ -342,63 +357,62 @@ __global__ void __launch_bounds__(256) dense_cell_kernel(const int *__restrict__
         nbmask[m] = mask;
     }
     __syncthreads();
-    const int nc = *ncell_p;
+    const int nd = *ndense_p;
     const int warps = gridDim.x * (blockDim.x >> 5);
-    for (int c = blockIdx.x * (blockDim.x >> 5) + w; c < nc; c += warps) {
-        const int cs = cell_start[c], ce = cell_start[c + 1], cnt = ce - cs;
-        if (cnt < kDenseMin) {
-            if (lane == 0) conn[c] = keys[cs] == keys[ce - 1] ? 1 : 0;
-            continue;
-        }
-        const uint64_t ck = keys[cs] & ~63ull;   // the cell's key with the sub-cell bits cleared
-        int lo[2], hi[2];
-        bool occ[2];
-        for (int r = 0; r < 2; ++r) {
-            const int m = lane + 32 * r;
-            lo[r] = lower_bound_key(keys, cs, ce, ck | (uint64_t)m);
-            hi[r] = lower_bound_key(keys, lo[r], ce, (ck | (uint64_t)m) + 1);
-            occ[r] = hi[r] > lo[r];
-            lab[w][m] = occ[r] ? lo[r] : INT_MAX;
-        }
-        const unsigned long long occm = (unsigned long long)__ballot_sync(0xffffffffu, occ[0]) |
-                                        ((unsigned long long)__ballot_sync(0xffffffffu, occ[1]) << 32);
-        __syncwarp();
-        for (int round = 0; round < 64; ++round) {   // converges in a few rounds
-            bool changed = false;
+    for (int di = blockIdx.x * (blockDim.x >> 5) + w; di < nd; di += warps) {
+        {
+            const int c = dense[di];
+            const int cs = cell_start[c], ce = cell_start[c + 1];
+            const uint64_t ck = keys[cs] & ~63ull;   // the cell's key with the sub-cell bits cleared
+            int lo[2], hi[2];
+            bool occ[2];
             for (int r = 0; r < 2; ++r) {
                 const int m = lane + 32 * r;
-                if (!occ[r]) continue;
-                int v = lab[w][m];
-                unsigned long long nb = nbmask[m] & occm;
-                while (nb) {
-                    const int t = __ffsll((long long)nb) - 1;
-                    nb &= nb - 1;
-                    v = min(v, lab[w][t]);
-                }
-                if (v < lab[w][m]) {
-                    lab[w][m] = v;
-                    changed = true;
-                }
+                lo[r] = lower_bound_key(keys, cs, ce, ck | (uint64_t)m);
+                hi[r] = lower_bound_key(keys, lo[r], ce, (ck | (uint64_t)m) + 1);
+                occ[r] = hi[r] > lo[r];
+                lab[w][m] = occ[r] ? lo[r] : INT_MAX;
             }
+            const unsigned long long occm = (unsigned long long)__ballot_sync(0xffffffffu, occ[0]) |
+                                            ((unsigned long long)__ballot_sync(0xffffffffu, occ[1]) << 32);
             __syncwarp();
-            if (!__any_sync(0xffffffffu, changed)) break;
+            for (int round = 0; round < 64; ++round) {   // converges in a few rounds
+                bool changed = false;
+                for (int r = 0; r < 2; ++r) {
+                    const int m = lane + 32 * r;
+                    if (!occ[r]) continue;
+                    int v = lab[w][m];
+                    unsigned long long nb = nbmask[m] & occm;
+                    while (nb) {
+                        const int t = __ffsll((long long)nb) - 1;
+                        nb &= nb - 1;
+                        v = min(v, lab[w][t]);
+                    }
+                    if (v < lab[w][m]) {
+                        lab[w][m] = v;
+                        changed = true;
+                    }
+                }
+                __syncwarp();
+                if (!__any_sync(0xffffffffu, changed)) break;
+            }
+            int mn = INT_MAX;
+            for (int r = 0; r < 2; ++r)
+                if (occ[r]) mn = min(mn, lab[w][lane + 32 * r]);
+            for (int o = 16; o > 0; o >>= 1) mn = min(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+            const bool one = __all_sync(0xffffffffu, (!occ[0] || lab[w][lane] == mn) && (!occ[1] || lab[w][lane + 32] == mn));
+            for (int r = 0; r < 2; ++r) {
+                if (!occ[r]) continue;
+                const int m = lane + 32 * r, L = lab[w][m];
+                if (L != lo[r]) parent[lo[r]] = L;   // run head under the component's smallest run head
+                int members = 0;                     // occupied sub-cells in this component
+                for (int t = 0; t < 64; ++t) members += lab[w][t] == L ? 1 : 0;
+                if (members > 1 || hi[r] - lo[r] > 1)
+                    for (int q = lo[r]; q < hi[r]; ++q) has[q] = 1;
+            }
+            if (lane == 0) conn[c] = one ? 1 : 0;
+            __syncwarp();
         }
-        int mn = INT_MAX;
-        for (int r = 0; r < 2; ++r)
-            if (occ[r]) mn = min(mn, lab[w][lane + 32 * r]);
-        for (int o = 16; o > 0; o >>= 1) mn = min(mn, __shfl_xor_sync(0xffffffffu, mn, o));
-        const bool one = __all_sync(0xffffffffu, (!occ[0] || lab[w][lane] == mn) && (!occ[1] || lab[w][lane + 32] == mn));
-        for (int r = 0; r < 2; ++r) {
-            if (!occ[r]) continue;
-            const int m = lane + 32 * r, L = lab[w][m];
-            if (L != lo[r]) parent[lo[r]] = L;   // run head under the component's smallest run head
-            int members = 0;                     // occupied sub-cells in this component
-            for (int t = 0; t < 64; ++t) members += lab[w][t] == L ? 1 : 0;
-            if (members > 1 || hi[r] - lo[r] > 1)
-                for (int q = lo[r]; q < hi[r]; ++q) has[q] = 1;
-        }
-        if (lane == 0) conn[c] = one ? 1 : 0;
-        __syncwarp();
     }
 }
 
@@ -912,6 +926,7 @@ int fof_core(int n, const double *x, const double *y, const double *z, FofGeom g
     const size_t o_flag = M.add(4ull * n), o_ipos = M.add(4ull * n);
     const size_t o_items = M.add(sizeof(ItemRec) * (size_t)n);
     const size_t o_cnt = M.add(64), o_conn = M.add(1ull * n);
+    const size_t o_dlist = M.add(4ull * ((uint64_t)n / kDenseMin + 1));   // cells of >= kDenseMin particles
     const size_t o_tmp = M.add(std::max(sort_b, scan_b));
     void *base = nullptr;
     HALMA_TRY(workspace(M.total, &base, st));
@@ -947,8 +962,10 @@ int fof_core(int n, const double *x, const double *y, const double *z, FofGeom g
     HALMA_LAUNCH(cells_kernel, g1, 256, 0, st, n, g.sb, kout, head, cpos, cst, ckey, hk, hv, hmask, cnt + 0);
     // one-component cells (sub-cells in the key and a positive linking length only)
     unsigned char *conn = at<unsigned char>(base, o_conn);
+    int *dlist = at<int>(base, o_dlist);
     if (g.sb != 0 && g.lo > 0.f) {
-        HALMA_LAUNCH(dense_cell_kernel, sms * 8, 256, 0, st, cnt + 0, cst, kout, parent, has, conn);
+        HALMA_LAUNCH(small_cell_kernel, g1, 256, 0, st, cnt + 0, cst, kout, conn, dlist, cnt + 8);
+        HALMA_LAUNCH(dense_cell_kernel, sms * 8, 256, 0, st, cnt + 8, dlist, cst, kout, parent, has, conn);
     } else {
         HALMA_CUDA(cudaMemsetAsync(conn, 0, n, st));
     }
