@@ -1,19 +1,24 @@
 #!/usr/bin/env python
 """FoF + batched unbinding throughput of one synthetic snapshot (single-GPU workload).
 
-Workload (one "step"): 2,000,000 star particles in a 10 Mpc box, 500 Plummer spheres with
-log-uniform masses 1e8-1e11 Msun, 15 % contaminants per sphere at 3 v_esc, 10 % uniform
-background; FoF at LL = 1.5 kpc (exact reference partition), groups >= 50 members, then
-iterative unbinding of every group (FP32 pair terms, compensated sums, FP64 reductions,
-softening 0.1 kpc) until no particle is removed.  Inputs are seeded synthetic data.
+Default workload (one "step"): a 100 Mpc box with 20,000 Plummer haloes whose particle
+counts follow dN/dlogN ∝ N^-alpha on [50, 2e5], alpha fitted so that the haloes hold
+4.5e7 particles on average, 15 % contaminants per halo (uniform inside 3a at 3 v_esc) and a
+uniform background filling the snapshot to 5e7 particles; FoF at LL = 1.5 kpc (exact
+reference partition), groups >= 50 members, then iterative unbinding of every group (FP32
+pair terms with compensated sums, FP64 reductions, softening 0.1 kpc) until no particle is
+removed.  Inputs are seeded synthetic data (no public dataset is involved).  The same line
+carries the 2e8-particle, 200,000-halo snapshot (one timed call, FoF stage broken out) under
+``full_snapshot``.
 
 Arms:
   default           the GB300 path; `value` = particles/s with inputs resident in HBM,
                     `e2e` = the same through the C ABI from pinned host buffers.
   --impl reference  the reference's CPU algorithm on this host (the oracle port: the KDTree
-                    flood fill of fof.py and the float32 potential loop of
-                    particle_subroutines.f90 with OpenMP), timed on bounded samples and
-                    extrapolated to the full snapshot.
+                    flood fill of fof.py step for step and the float32 potential loop of
+                    particle_subroutines.f90 with OpenMP) on a size-stratified sample of the
+                    same snapshot, measured per step; the full-snapshot time extrapolated from
+                    it is reported under a separate key.
 """
 from __future__ import annotations
 
@@ -32,9 +37,22 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "particles/sec FoF+unbinding and pair-interactions/sec, batched FP32 vs FP64 at ≤1e-6"
-WORKLOAD = dict(workload="plummer-2M-500sph-15pc-contaminants", particles=2_000_000, spheres=500, box_mpc=10.0,
-                contaminant_frac=0.15, background_frac=0.10, linking_length_kpc=1.5, min_members=50,
-                softening_kpc=0.1, max_passes=30)
+WORKLOADS = {
+    # the default: 20k power-law haloes, 5e7 particles
+    "northstar": dict(workload="powerlaw-20k-haloes-50M-particles", particles=50_000_000, haloes=20_000,
+                      box_mpc=100.0, halo_sizes="dN/dlogN ~ N^-alpha on [50, 2e5], alpha fitted to a mean of 2250",
+                      contaminant_frac=0.15, background_frac=0.10, linking_length_kpc=1.5, min_members=50,
+                      softening_kpc=0.1, max_passes=30),
+    # 2e6 particles in 500 Plummer spheres (the medium configuration)
+    "plummer2m": dict(workload="plummer-2M-500sph-15pc-contaminants", particles=2_000_000, spheres=500,
+                      box_mpc=10.0, contaminant_frac=0.15, background_frac=0.10, linking_length_kpc=1.5,
+                      min_members=50, softening_kpc=0.1, max_passes=30),
+    # 2e8 particles, 200k haloes, 5 % of them in bridged pairs, 20 % background
+    "full": dict(workload="full-2e8-particles-200k-haloes", particles=200_000_000, haloes=200_000, box_mpc=100.0,
+                 halo_sizes="dN/dlogN ~ N^-alpha on [50, 2e5], alpha fitted to a mean of 800", bridged_frac=0.05,
+                 background_frac=0.20, contaminant_frac=0.0, linking_length_kpc=1.5, min_members=50,
+                 softening_kpc=0.1, max_passes=30),
+}
 # FP32-pipe work of the pair kernels, counted from the instruction mix (an FMA is 2 flops):
 #   a pair term evaluated for one particle (tiles, incremental passes): 3 sub + 3 fma for
 #   r^2 + 1 fma to accumulate = 7 lane-operations, 11 flops, and one rsqrt;
@@ -42,12 +60,12 @@ WORKLOAD = dict(workload="plummer-2M-500sph-15pc-contaminants", particles=2_000_
 #   haloes above 1024 particles): 3 sub + 3 fma + 2 fma = 8 lane-operations, 13 flops, one
 #   rsqrt -- per pair term of the pass (each pair is two terms) 4 lane-operations, 6.5 flops
 #   (the diagonal blocks, evaluated per particle, are counted the same way).
-# The FP32 pipe does 128 lane-operations per clock per SM; ncu shows the special-function
-# pipe at 42 % when the FP32 pipe is at 76 %, so the FP32 pipe binds.
 FLOPS_PER_TERM, OPS_PER_TERM = 11.0, 7.0
 FLOPS_PER_SYM_TERM, OPS_PER_SYM_TERM = 6.5, 4.0
-FP32_OPS_PER_CLK_SM = 128.0
 FOF_BYTES_PER_PARTICLE = 28  # FP64 xyz read once + int32 label written once
+# CPU samples: every k-th halo by size rank + 1/k of the background; the reference arm runs
+# one such sample per step (K + W steps), the GPU arm's cpu_baseline one larger sample
+CPU_STRIDE_ARM, CPU_STRIDE_BASELINE = 600, 250
 
 
 def peaks():
@@ -58,11 +76,19 @@ def peaks():
     return 6800.0, 2070.0, "fallback"
 
 
-def snapshot(seed):
+def make_snapshot(w, seed):
     from pyhalma_gb300 import synth
-    w = WORKLOAD
-    return synth.plummer_snapshot(w["particles"], w["spheres"], seed=seed, box_mpc=w["box_mpc"],
-                                  bg_frac=w["background_frac"], contaminant_frac=w["contaminant_frac"])
+    if "spheres" in w:
+        return synth.plummer_snapshot(w["particles"], w["spheres"], seed=seed, box_mpc=w["box_mpc"],
+                                      bg_frac=w["background_frac"], contaminant_frac=w["contaminant_frac"])
+    return synth.full_snapshot(w["particles"], w["haloes"], seed=seed, box_mpc=w["box_mpc"],
+                               bg_frac=w["background_frac"], bridge_frac=w.get("bridged_frac", 0.0),
+                               contaminant_frac=w["contaminant_frac"])
+
+
+def snapshot(seed):
+    """The 2e6-particle Plummer snapshot of the side workloads."""
+    return make_snapshot(WORKLOADS["plummer2m"], seed)
 
 
 # ---------------------------------------------------------------------------------------
@@ -83,7 +109,7 @@ class ClockSampler:
             fd, self.path = tempfile.mkstemp(suffix=".csv")
             os.close(fd)
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
-                                          "--format=csv,noheader,nounits", "-lms", "20"],
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
                                          stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
@@ -114,36 +140,43 @@ class ClockSampler:
 
 
 # ---------------------------------------------------------------------------------------
-# CPU leg: the reference algorithm on bounded samples of the same snapshot
+# CPU leg: the reference algorithm on a size-stratified sample of the same snapshot
 # ---------------------------------------------------------------------------------------
-def cpu_measure(s, every=20, ncores=None):
-    """Returns (particles/s estimate for the full snapshot, details).
+def cpu_sample(s, stride, seed=7):
+    """Indices of the CPU sample: every `stride`-th generating halo in order of size (so the
+    sample's halo sizes follow the snapshot's distribution) and 1/stride of the background."""
+    hid = np.asarray(s.sphere)
+    nh = int(hid.max()) + 1 if hid.size and hid.max() >= 0 else 0
+    sizes = np.bincount(hid[hid >= 0], minlength=nh)
+    order = np.argsort(sizes, kind="stable")
+    picked = np.zeros(nh, dtype=bool)
+    picked[order[stride // 2::stride]] = True
+    rng = np.random.default_rng(seed)
+    take = np.zeros(s.n, dtype=bool)
+    take[hid >= 0] = picked[hid[hid >= 0]]
+    bg = hid < 0
+    take[bg] = rng.random(int(bg.sum())) < 1.0 / stride
+    return np.nonzero(take)[0], int(picked.sum())
 
-    FoF: the KDTree flood fill (fof.py:18-79 restated) on every `every`-th sphere plus the same
-    share of background, single-threaded like the reference's serial FoF.  Unbinding: the
-    iterative cut with the float32 potential loop (particle_subroutines.f90:466-514 restated,
-    OpenMP over all cores) on the sample's groups; the full snapshot's pair count is scaled by
-    the sum of squared group sizes (full FoF from the exact C oracle)."""
+
+def cpu_step(s, idx, w, ncores):
+    """One step of the reference's CPU path on the particles idx: the KDTree flood fill
+    (fof.py:18-79 step for step, one thread, as the reference's serial FoF), groups of >=
+    min_members, then per group the iterative escape cut (halo_properties.py:282-361 repeated)
+    with the float32 potential loop of particle_subroutines.f90:466-514 (OpenMP over ncores):
+    full potential in the first pass, then the potential of the particles removed by the
+    previous pass subtracted, as the GPU path does."""
     import oracle
     from oracle import fof_kdtree
-    ncores = ncores or oracle.ncores_default()
-    w = WORKLOAD
     ll = w["linking_length_kpc"] * 1e-3
-    rng = np.random.default_rng(7)
-    take = (s.sphere >= 0) & (s.sphere % every == 0)
-    take |= (s.sphere < 0) & (rng.random(s.n) < 1.0 / every)
-    idx = np.nonzero(take)[0]
     t0 = time.perf_counter()
     groups = fof_kdtree.friends_of_friends_serial(s.x[idx], s.y[idx], s.z[idx], ll)
     t_fof = time.perf_counter() - t0
     groups = [np.asarray(g) for g in groups if len(g) >= w["min_members"]]
     pairs = 0.0
     G = 4.3e-9
-    eps = w["softening_kpc"] * 1e-3  # the float32 reference loop has no softening; eps only shapes the cut
     t0 = time.perf_counter()
     for g in groups:
-        # the same iteration as the GPU path: full potential in the first pass, then the
-        # potential of the particles removed by the previous pass is subtracted
         gi = idx[g]
         m_all = s.mass[gi]
         c = [(m_all * a[gi]).sum() / m_all.sum() for a in (s.x, s.y, s.z)]
@@ -169,25 +202,28 @@ def cpu_measure(s, every=20, ncores=None):
                                                      pz[keep], ncores=ncores)
                 pairs += float(gone.size) * keep.size
     t_unb = time.perf_counter() - t0
-    # full snapshot: pair count scaled by sum N^2 of all groups vs the sample's groups
-    lab = oracle.fof_labels(s.x, s.y, s.z, ll)
-    _, cnt = np.unique(lab[lab >= 0], return_counts=True)
-    full_n2 = float((cnt[cnt >= w["min_members"]].astype(np.float64) ** 2).sum())
-    samp_n2 = float(sum(float(len(g)) ** 2 for g in groups)) or 1.0
-    pairs_full = pairs * full_n2 / samp_n2
-    fof_rate = len(idx) / t_fof
-    pair_rate = pairs / max(t_unb, 1e-9)
-    t_full = s.n / fof_rate + pairs_full / pair_rate
-    return s.n / t_full, dict(t_fof=t_fof, n_fof=len(idx), t_unbind=t_unb, pairs=pairs, pairs_full=pairs_full,
-                              fof_rate=fof_rate, pair_rate=pair_rate, cores=ncores, groups=len(groups))
+    sum_n2 = float(sum(float(len(g)) ** 2 for g in groups))
+    return dict(t_fof=t_fof, t_unbind=t_unb, n=len(idx), pairs=pairs, groups=len(groups), sum_n2=sum_n2,
+                cores=ncores)
 
 
-def cpu_sample_text(d, every):
-    return (f"FoF: KDTree flood fill, 1 thread, on every {every}th sphere + 1/{every} of the background "
-            f"({d['n_fof']} particles, {d['t_fof']:.2f} s); unbinding: float32 reference loop with OpenMP on "
-            f"{d['cores']} threads over the sample's {d['groups']} groups, full first pass then incremental "
-            f"passes like the GPU ({d['pairs']:.3g} pairs, {d['t_unbind']:.2f} s); extrapolated to the full "
-            f"snapshot ({d['pairs_full']:.3g} pairs)")
+def cpu_extrapolation(d, n_full, sum_n2_full, source):
+    """Full-snapshot CPU time from a sample step: FoF time scaled by particles, unbinding time
+    by the sum of squared group sizes."""
+    t_fof = d["t_fof"] * n_full / max(d["n"], 1)
+    t_unb = d["t_unbind"] * sum_n2_full / max(d["sum_n2"], 1.0)
+    return {"value": n_full / (t_fof + t_unb), "unit": "particles/s", "seconds": t_fof + t_unb,
+            "fof_s": t_fof, "unbind_s": t_unb, "kind": "extrapolated",
+            "rule": "FoF seconds x N / N_sample + unbinding seconds x sum N_h^2 / sum N_h^2 of the sample",
+            "group_sizes": source}
+
+
+def cpu_sample_text(d, n_haloes, stride):
+    return (f"measured: every {stride}th halo by size rank ({n_haloes} haloes) + 1/{stride} of the background, "
+            f"{d['n']} particles; FoF: KDTree flood fill of fof.py step for step, 1 thread ({d['t_fof']:.2f} s); "
+            f"unbinding: float32 potential loop of the Fortran with OpenMP on {d['cores']} threads over the "
+            f"sample's {d['groups']} groups, full first pass then incremental passes like the GPU "
+            f"({d['pairs']:.3g} pair terms, {d['t_unbind']:.2f} s)")
 
 
 # ---------------------------------------------------------------------------------------
@@ -204,26 +240,178 @@ def run_reference(args):
         return 0
     import oracle
     oracle.build()
-    s = snapshot(seed=1)
-    every = 20
-    vals = []
+    w = WORKLOADS[args.workload]
+    s = make_snapshot(w, seed=1)
+    idx, nsh = cpu_sample(s, CPU_STRIDE_ARM)
+    ncores = oracle.ncores_default()
     for _ in range(args.warmup):
-        cpu_measure(s, every)
-    last = None
+        cpu_step(s, idx, w, ncores)
+    secs, last = [], None
+    t_all = time.perf_counter()
     for _ in range(args.steps):
-        v, last = cpu_measure(s, every)
-        vals.append(v)
-    value = statistics.median(vals)
+        t0 = time.perf_counter()
+        last = cpu_step(s, idx, w, ncores)
+        secs.append(time.perf_counter() - t0)
+    timed = time.perf_counter() - t_all
+    step_s = statistics.median(secs)
+    value = last["n"] / step_s
+    counts = s.meta.get("halo_counts")
+    if counts is None:
+        counts = s.meta.get("sphere_counts")
+    counts = np.asarray(counts, dtype=np.float64)
+    counts = counts[counts >= w["min_members"]]
+    ext = cpu_extrapolation(last, s.n, float((counts ** 2).sum()), "generating halo sizes >= min_members")
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "particles/s", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": s.n / value * 1e3,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic", "config": dict(WORKLOAD),
-            "cpu_baseline": {"value": value, "unit": "particles/s", "cores": last["cores"], "kind": "port",
-                             "sample": cpu_sample_text(last, every)},
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_s * 1e3,
+            "timed_region_s": timed, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic", "config": dict(w, particles=s.n),
+            "cpu_baseline": {"value": value, "unit": "particles/s", "cores": ncores, "kind": "port",
+                             "sample": cpu_sample_text(last, nsh, CPU_STRIDE_ARM)},
             "e2e": {"value": value, "unit": "particles/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-            "pair_interactions_per_s": last["pair_rate"]}
+            "pair_interactions_per_s": last["pairs"] / max(last["t_unbind"], 1e-9),
+            "extrapolated_full_snapshot": ext}
     print(json.dumps(line), flush=True)
     return 0
+
+
+# ---------------------------------------------------------------------------------------
+# the plain FP64 per-halo path, on a size-stratified sample of the haloes
+# ---------------------------------------------------------------------------------------
+def fp64_sampled(off, members, dev_in, opt, per_class=3, n_classes=8):
+    """Times the plain FP64 per-halo path (one pair launch per halo per pass, host-checked
+    convergence) on `per_class` haloes of each logarithmic size class, spread evenly over the
+    class in size order, and scales each class's time by the class's sum of N_h^2 over the
+    sample's; the fixed cost of one call (measured on the smallest sampled halo alone) is taken
+    off every class before scaling and counted once.  Also returns the per-halo relative
+    potential error of one FP32C pass against one FP64 pass over the same sampled haloes."""
+    import torch
+    from pyhalma_gb300.unbinding import UnbindOptions, unbind_batched
+    dev = dev_in[0].device
+    sizes = np.diff(off)
+    edges = np.geomspace(max(sizes.min(), 1), sizes.max() + 1, n_classes + 1)
+    cls = np.clip(np.searchsorted(edges, sizes, side="right") - 1, 0, n_classes - 1)
+    midx = members.long()
+
+    def gather(hs):
+        sel = np.concatenate([np.arange(off[h], off[h + 1]) for h in hs])
+        soff = np.concatenate([[0], np.cumsum(sizes[hs])]).astype(np.int64)
+        arr = [a[midx[torch.from_numpy(sel).to(dev)]].contiguous() for a in dev_in]
+        return torch.from_numpy(soff).to(dev), arr
+
+    def timed(doff, arr, o):
+        unbind_batched(doff, *arr, o)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        _, halo, _ = unbind_batched(doff, *arr, o)
+        e1.record()
+        e1.synchronize()
+        return e0.elapsed_time(e1) * 1e-3, halo
+
+    o64 = UnbindOptions(eps=opt.eps, max_iter=opt.max_iter, precision="fp64")
+    picks, rows = [], []
+    for c in range(n_classes):
+        hs = np.nonzero(cls == c)[0]
+        if hs.size == 0:
+            continue
+        hs = hs[np.argsort(sizes[hs], kind="stable")]
+        k = min(per_class, hs.size)
+        pick = hs[np.linspace(0, hs.size - 1, k).round().astype(int)]
+        picks.append(pick)
+        rows.append((c, hs, pick))
+    smallest = min((p for p in np.concatenate(picks)), key=lambda h: sizes[h])
+    t_fixed, _ = timed(*gather(np.array([smallest])), o64)
+    total, classes = t_fixed, []
+    for c, hs, pick in rows:
+        t, halo = timed(*gather(pick), o64)
+        n2c = float((sizes[hs].astype(np.float64) ** 2).sum())
+        n2p = float((sizes[pick].astype(np.float64) ** 2).sum())
+        est = max(t - t_fixed, 0.0) * n2c / n2p
+        total += est
+        classes.append({"sizes": [int(edges[c]), int(edges[c + 1])], "haloes": int(hs.size),
+                        "sampled": [int(sizes[h]) for h in pick], "sample_s": t, "class_s": est,
+                        "passes": [int(v) for v in halo[:, 8].cpu().numpy()]})
+    # potential error of one FP32C pass against one FP64 pass on every sampled halo
+    allp = np.sort(np.concatenate(picks))
+    doff, arr = gather(allp)
+    _, _, p32 = unbind_batched(doff, *arr, UnbindOptions(eps=opt.eps, max_iter=1, precision="fp32c"), want_phi=True)
+    _, _, p64 = unbind_batched(doff, *arr, UnbindOptions(eps=opt.eps, max_iter=1, precision="fp64"), want_phi=True)
+    p32, p64, so = p32.cpu().numpy(), p64.cpu().numpy(), doff.cpu().numpy()
+    per_halo = []
+    for h in range(len(so) - 1):
+        a, b = p32[so[h]:so[h + 1]], p64[so[h]:so[h + 1]]
+        both = (a != 0) & (b != 0)
+        if both.any():
+            per_halo.append(float(np.max(np.abs(a[both] / b[both] - 1.0))))
+    err = {"per_halo_max": float(np.max(per_halo)), "per_halo_median": float(np.median(per_halo)),
+           "haloes": len(per_halo), "bound": 1e-6, "sample": "the haloes sampled for the FP64 timing"}
+    return total, classes, t_fixed, err
+
+
+# ---------------------------------------------------------------------------------------
+def _free_device_memory():
+    import gc
+    import torch
+    from pyhalma_gb300 import _lib
+    gc.collect()
+    torch.cuda.synchronize()
+    _lib.lib().halma_release_workspace()
+    torch.cuda.empty_cache()
+
+
+def full_snapshot_run(args, check_crop=True):
+    """The 2e8-particle snapshot: FoF + groups + batched unbinding in one call (one warm-up,
+    then args.full_steps timed calls), FoF stages broken out, FoF of a 1e7-particle crop
+    checked bit-exact against the C oracle."""
+    import torch
+    import oracle
+    from pyhalma_gb300 import _lib, fof
+    from pyhalma_gb300.unbinding import UnbindOptions, find_haloes
+    w = WORKLOADS["full"]
+    dev = torch.device("cuda", 0)
+    t0 = time.perf_counter()
+    s = make_snapshot(w, seed=2)
+    gen_s = time.perf_counter() - t0
+    d = [torch.from_numpy(a).to(dev) for a in (s.x, s.y, s.z, s.vx, s.vy, s.vz, s.mass)]
+    ll = w["linking_length_kpc"] * 1e-3
+    opt = UnbindOptions(eps=w["softening_kpc"] * 1e-3, max_iter=w["max_passes"])
+    _lib.set_profiling(True)
+    find_haloes(*d, ll, w["min_members"], options=opt)
+    torch.cuda.synchronize()
+    ms, fof_ms, unb_ms, stages = [], [], [], []
+    for _ in range(max(args.full_steps, 1)):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        cat = find_haloes(*d, ll, w["min_members"], options=opt)
+        e1.record()
+        e1.synchronize()
+        ms.append(e0.elapsed_time(e1))
+        st = _lib.profile_stats()
+        fof_ms.append(st["fof_ms"])
+        unb_ms.append(st["unbind_ms"])
+        stages.append(_lib.profile_fof_stages())
+    hbm, _, src = peaks()
+    t_fof = statistics.mean(fof_ms)
+    fof_gbs = FOF_BYTES_PER_PARTICLE * s.n / (t_fof * 1e-3) / 1e9
+    out = {"workload": w["workload"], "particles": s.n, "haloes_generated": w["haloes"],
+           "haloes_found": cat.n_haloes, "ms": statistics.mean(ms), "particles_per_s": s.n / (statistics.mean(ms) * 1e-3),
+           "fof_ms": t_fof, "unbind_ms": statistics.mean(unb_ms),
+           "fof_stages_ms": {k: statistics.mean(st[k] for st in stages) for k in stages[0]},
+           "roofline_fof": {"bound": "hbm", "achieved": fof_gbs, "peak": hbm, "unit": "GB/s", "frac": fof_gbs / hbm,
+                            "note": f"{FOF_BYTES_PER_PARTICLE} algorithmic B/particle over the FoF stage; hbm_gbs {src}"},
+           "generate_s": gen_s, "alpha": s.meta["alpha"], "timed_calls": len(ms)}
+    _lib.set_profiling(False)
+    del d, cat
+    _free_device_memory()
+    if check_crop:
+        k = min(args.crop, s.n)
+        crop = np.sort(np.argpartition(s.x, k - 1)[:k])
+        cx, cy, cz = (np.ascontiguousarray(a[crop]) for a in (s.x, s.y, s.z))
+        lab_gpu = fof.fof_labels(cx, cy, cz, ll)
+        lab_ref = oracle.fof_labels(cx, cy, cz, ll)
+        out["crop_particles"] = int(k)
+        out["crop_fof_bit_exact_vs_c_oracle"] = bool(np.array_equal(lab_gpu, lab_ref))
+    return out
 
 
 def run_gpu(args):
@@ -236,8 +424,10 @@ def run_gpu(args):
     dev = torch.device("cuda", local)
     from pyhalma_gb300 import _lib
     from pyhalma_gb300.unbinding import UnbindOptions, find_haloes
-    w = WORKLOAD
-    s = snapshot(seed=1 + rank)
+    w = WORKLOADS[args.workload]
+    t0 = time.perf_counter()
+    s = make_snapshot(w, seed=1 + rank)
+    gen_s = time.perf_counter() - t0
     n = s.n
     ll = w["linking_length_kpc"] * 1e-3
     opt = UnbindOptions(eps=w["softening_kpc"] * 1e-3, max_iter=w["max_passes"], precision="fp32c")
@@ -247,6 +437,8 @@ def run_gpu(args):
     pinned_np = [t.numpy() for t in pinned]
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)   # > 129 MB L2
     stream = torch.cuda.current_stream()
+    # the FP32 pipe's peak on this GPU: packed and scalar FMA chains, the faster one
+    fp32_peak = max(_lib.measure_fp32_fma_rate(packed=True)[0], _lib.measure_fp32_fma_rate(packed=False)[0])
 
     def barrier():
         torch.cuda.synchronize()
@@ -259,22 +451,25 @@ def run_gpu(args):
     torch.cuda.synchronize()
 
     # timed region: inputs resident in HBM, L2 flushed before every step
-    ms, pairs, pair_ms, fof_ms, unbind_ms, passes = [], 0.0, 0.0, [], [], []
-    sym_pairs, sym_ms, sym_launches, per_pass = 0.0, 0.0, 0, []
+    ms, wall_ms, pairs, pair_ms, fof_ms, unbind_ms, passes = [], [], 0.0, 0.0, [], [], []
+    sym_pairs, sym_ms, sym_launches, per_pass, stages = 0.0, 0.0, 0, [], []
     sampler = ClockSampler(local)
     sampler.start()
     launches0 = _lib.launch_count()
     barrier()
     wall0 = time.perf_counter()
     for _ in range(args.steps):
+        w0 = time.perf_counter()
         flush.zero_()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
         cat = find_haloes(*dev_in, ll, w["min_members"], options=opt)
         e1.record(stream)
         e1.synchronize()
+        wall_ms.append((time.perf_counter() - w0) * 1e3)
         ms.append(e0.elapsed_time(e1))
         st = _lib.profile_stats()
+        stages.append(_lib.profile_fof_stages())
         fof_ms.append(st["fof_ms"])
         unbind_ms.append(st["unbind_ms"])
         for (p, t), sp, sm in zip(st["passes"], st["sym_pairs"], st["sym_ms"]):
@@ -301,6 +496,7 @@ def run_gpu(args):
     value = n * world / (step_ms * 1e-3)
 
     # end to end through the C ABI from pinned host buffers (copies inside the timed region)
+    _lib.set_profiling(False)
     e2e_ms = []
     for k in range(args.warmup + args.steps):
         flush.zero_()
@@ -322,73 +518,52 @@ def run_gpu(args):
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         e2e_step = float(t.item())
 
-    # plain FP64 per-halo path on the same snapshot (the comparator of the batched path)
+    # the plain FP64 per-halo path on a size-stratified sample, extrapolated to every halo
     fp64 = None
     if not args.skip_fp64:
-        _lib.set_profiling(False)
-        o64 = UnbindOptions(eps=opt.eps, max_iter=opt.max_iter, precision="fp64")
-        find_haloes(*dev_in, ll, w["min_members"], options=o64)
-        torch.cuda.synchronize()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        find_haloes(*dev_in, ll, w["min_members"], options=o64)
-        e1.record(stream)
-        e1.synchronize()
-        t64 = e0.elapsed_time(e1)
-        fp64 = {"value": n / (t64 * 1e-3), "unit": "particles/s", "ms_per_step": t64,
-                "speedup_fp32c_vs_fp64": t64 / statistics.mean(ms)}
-        # potential error of the batched FP32C path against the plain FP64 path, per halo:
-        # one pass over every group (all members), phi of the members both paths keep bound
-        from pyhalma_gb300.unbinding import unbind_batched
-        midx = cat.members.long()
-        garr = [a[midx].contiguous() for a in dev_in]
-        _, _, p32 = unbind_batched(cat.offsets, *garr, UnbindOptions(eps=opt.eps, max_iter=1, precision="fp32c"),
-                                   want_phi=True)
-        _, _, p64 = unbind_batched(cat.offsets, *garr, UnbindOptions(eps=opt.eps, max_iter=1, precision="fp64"),
-                                   want_phi=True)
-        p32, p64, off_h = p32.cpu().numpy(), p64.cpu().numpy(), cat.offsets.cpu().numpy()
-        per_halo = []
-        for h in range(len(off_h) - 1):
-            a, b = p32[off_h[h]:off_h[h + 1]], p64[off_h[h]:off_h[h + 1]]
-            both = (a != 0) & (b != 0)
-            if both.any():
-                per_halo.append(float(np.max(np.abs(a[both] / b[both] - 1.0))))
-        fp64["potential_rel_err_vs_fp64"] = {"per_halo_max": float(np.max(per_halo)),
-                                             "per_halo_median": float(np.median(per_halo)),
-                                             "haloes": len(per_halo), "bound": 1e-6}
+        off = cat.offsets.cpu().numpy()
+        t_unb64, classes, t_fixed, err = fp64_sampled(off, cat.members, dev_in, opt)
+        t_fof = statistics.mean(fof_ms) * 1e-3
+        t64 = t_fof + t_unb64
+        fp64 = {"value": n / t64, "unit": "particles/s", "ms_per_step": t64 * 1e3, "kind": "extrapolated",
+                "speedup_fp32c_vs_fp64": t64 / (step_ms * 1e-3),
+                "speedup_unbinding_only": t_unb64 / (statistics.mean(unbind_ms) * 1e-3),
+                "rule": "FoF as measured + per size class: (FP64 time of the sampled haloes - one call's fixed "
+                        "cost) x sum N_h^2 of the class / sum N_h^2 of the sample, + the fixed cost once",
+                "fixed_call_s": t_fixed, "classes": classes, "potential_rel_err_vs_fp64": err}
 
     hbm, sm_max, src = peaks()
     sms = torch.cuda.get_device_properties(dev).multi_processor_count
-    pair_peak = 2.0 * FP32_OPS_PER_CLK_SM * sms * sm_max * 1e6 / 1e12   # FP32 TFLOP/s, FMA = 2
     n_pair_launches = sum(passes)
     flops = FLOPS_PER_TERM * (pairs - sym_pairs) + FLOPS_PER_SYM_TERM * sym_pairs
     lane_ops = OPS_PER_TERM * (pairs - sym_pairs) + OPS_PER_SYM_TERM * sym_pairs
+    pipe_ops = fp32_peak * 1e12 / 2.0   # FP32 lane-operations per second at the measured peak
     achieved = flops / (pair_ms * 1e-3) / 1e12 if pair_ms > 0 else 0.0
-    pipe = lane_ops / (pair_ms * 1e-3) / (FP32_OPS_PER_CLK_SM * sms * sm_max * 1e6) if pair_ms > 0 else 0.0
+    pipe = lane_ops / (pair_ms * 1e-3) / pipe_ops if pair_ms > 0 else 0.0
     traffic = {}
     tp = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(tp):
         traffic = json.load(open(tp))
     # the dominant kernel: the symmetric block kernel of the first (full) pass, timed alone
-    sym_flops = FLOPS_PER_SYM_TERM * sym_pairs
-    sym_achieved = sym_flops / (sym_ms * 1e-3) / 1e12 if sym_ms > 0 else 0.0
-    sym_pipe = OPS_PER_SYM_TERM * sym_pairs / (sym_ms * 1e-3) / (FP32_OPS_PER_CLK_SM * sms * sm_max * 1e6) \
-        if sym_ms > 0 else 0.0
-    peak_note = (f"FP32 peak: 128 lanes x 2 flops (FMA) x {sms} SMs x {sm_max:.0f} MHz (sm_max_mhz {src}); "
-                 f"flops from the instruction mix: 6.5 per pair term on the symmetric block kernel (a pair "
-                 f"evaluated once for both particles: 3 sub + 3 fma + 2 fma = 13 flops), 11 per term on the "
-                 f"per-particle tile kernel (3 sub + 3 fma + 1 fma); 3 of every 8 (7) lane-operations are "
-                 f"1-flop subtractions, so frac <= 0.81 (0.79) at a full FP32 pipe")
-    roofline = {"bound": "fp32", "kernel": "ub_pair_sym_kernel", "achieved": sym_achieved, "peak": pair_peak,
-                "unit": "TFLOP/s", "frac": sym_achieved / pair_peak if pair_peak else None,
+    sym_achieved = FLOPS_PER_SYM_TERM * sym_pairs / (sym_ms * 1e-3) / 1e12 if sym_ms > 0 else 0.0
+    sym_pipe = OPS_PER_SYM_TERM * sym_pairs / (sym_ms * 1e-3) / pipe_ops if sym_ms > 0 else 0.0
+    peak_note = (f"FP32 peak measured on this GPU by the library's FMA-chain kernel "
+                 f"(halma_measure_fp32_fma_rate, packed and scalar, the faster); {sms} SMs, SM clock during the "
+                 f"timed region in `clocks`; flops from the instruction mix: 6.5 per pair term on the symmetric "
+                 f"block kernel (a pair evaluated once for both particles: 3 sub + 3 fma + 2 fma = 13 flops), "
+                 f"11 per term on the per-particle tile kernel (3 sub + 3 fma + 1 fma); 3 of every 8 (7) "
+                 f"lane-operations are 1-flop subtractions, so frac <= 0.81 (0.79) at a full FP32 pipe; "
+                 f"fp32_pipe_frac = lane-operations / (peak / 2)")
+    roofline = {"bound": "fp32", "kernel": "ub_pair_sym_kernel", "achieved": sym_achieved, "peak": fp32_peak,
+                "unit": "TFLOP/s", "frac": sym_achieved / fp32_peak if fp32_peak else None,
                 "traffic": traffic.get("ub_pair_sym_kernel_bytes_per_launch"),
                 "peak_source": peak_note, "fp32_pipe_frac": sym_pipe,
                 "pair_terms_per_launch": sym_pairs / max(sym_launches, 1),
                 "ms_per_launch": sym_ms / max(sym_launches, 1), "launches_timed": sym_launches,
                 "pair_terms_per_s": sym_pairs / (sym_ms * 1e-3) if sym_ms > 0 else 0.0}
     roofline_pairs = {"bound": "fp32", "kernel": "ub_pair_sym_kernel + ub_pair_kernel (every pass)",
-                      "achieved": achieved, "peak": pair_peak, "unit": "TFLOP/s",
-                      "frac": achieved / pair_peak if pair_peak else None,
+                      "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
+                      "frac": achieved / fp32_peak if fp32_peak else None,
                       "traffic_ub_pair_kernel": traffic.get("ub_pair_kernel_bytes_per_launch"),
                       "fp32_pipe_frac": pipe, "sym_pair_terms": sym_pairs,
                       "pairs_per_launch": pairs / max(n_pair_launches, 1),
@@ -397,15 +572,18 @@ def run_gpu(args):
     fof_gbs = FOF_BYTES_PER_PARTICLE * n / (statistics.mean(fof_ms) * 1e-3) / 1e9
     roofline_fof = {"bound": "hbm", "achieved": fof_gbs, "peak": hbm, "unit": "GB/s", "frac": fof_gbs / hbm,
                     "traffic": None, "ms": statistics.mean(fof_ms),
+                    "stages_ms": {k: statistics.mean(st[k] for st in stages) for k in stages[0]},
                     "note": f"{FOF_BYTES_PER_PARTICLE} algorithmic B/particle over the whole FoF stage "
                             f"(bbox, keys, sort, cells, links, labels, groups); hbm_gbs {src}"}
 
     line = {"metric": METRIC, "value": value, "unit": "particles/s", "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": dict(WORKLOAD, l2="flushed before every step (256 MB device write)", haloes=n_haloes,
-                           passes_mean=statistics.mean(passes), fof_ms=statistics.mean(fof_ms),
-                           unbind_ms=statistics.mean(unbind_ms), reductions="FP64",
+            "warmup": args.warmup, "ms_per_step": step_ms, "wall_ms_per_step": statistics.mean(wall_ms),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded generator of the configuration; no public dataset)",
+            "config": dict(w, particles=n, haloes_found=n_haloes, generate_s=gen_s,
+                           l2=f"inputs ({7 * 8 * n / 1e9:.1f} GB) larger than L2, and L2 flushed before every step "
+                              f"(256 MB device write)", passes_mean=statistics.mean(passes),
+                           fof_ms=statistics.mean(fof_ms), unbind_ms=statistics.mean(unbind_ms), reductions="FP64",
                            parallelism=f"snapshot-per-rank x{world}"),
             "pair_interactions_per_s": pairs / (sum(ms) * 1e-3) * world,
             "roofline": roofline, "roofline_pair_kernels": roofline_pairs, "roofline_fof": roofline_fof,
@@ -413,10 +591,19 @@ def run_gpu(args):
                     "d2h_bytes_per_step": d2h, "ms_per_step": e2e_step},
             "gpu_launches": launches, "clocks": clocks, "fp64_path": fp64, "wall_s_timed": wall}
     if rank == 0 and world == 1 and not args.skip_cpu:
-        every = 20
-        v, d = cpu_measure(s, every)
+        import oracle
+        idx, nsh = cpu_sample(s, CPU_STRIDE_BASELINE)
+        d = cpu_step(s, idx, w, oracle.ncores_default())
+        v = d["n"] / (d["t_fof"] + d["t_unbind"])
+        sizes = np.diff(cat.offsets.cpu().numpy()).astype(np.float64)
         line["cpu_baseline"] = {"value": v, "unit": "particles/s", "cores": d["cores"], "kind": "port",
-                                "sample": cpu_sample_text(d, every)}
+                                "sample": cpu_sample_text(d, nsh, CPU_STRIDE_BASELINE),
+                                "extrapolated_full_snapshot": cpu_extrapolation(d, n, float((sizes ** 2).sum()),
+                                                                                "the GPU's FoF groups")}
+    del dev_in, pinned, pinned_np, flush, cat, hc
+    if rank == 0 and world == 1 and args.workload == "northstar" and not args.skip_full:
+        _free_device_memory()
+        line["full_snapshot"] = full_snapshot_run(args)
     if world > 1:
         torch.distributed.destroy_process_group()
     if rank == 0:
@@ -517,38 +704,8 @@ def run_gas(args):
 
 
 def run_full(args):
-    """2e8 stars in a 100 Mpc box, 200 000 power-law haloes (5 % in bridged pairs), 20 %
-    background: FoF + groups + batched unbinding in one call; FoF checked bit-exact against
-    the C oracle on a 1e7-particle crop."""
-    import torch
-    import oracle
-    from pyhalma_gb300 import fof, synth
-    from pyhalma_gb300.unbinding import UnbindOptions, find_haloes
-    dev = torch.device("cuda", 0)
-    t0 = time.perf_counter()
-    s = synth.full_snapshot(args.full_n, args.full_haloes, seed=2)
-    gen_s = time.perf_counter() - t0
-    d = [torch.from_numpy(a).to(dev) for a in (s.x, s.y, s.z, s.vx, s.vy, s.vz, s.mass)]
-    opt = UnbindOptions(eps=1e-4, max_iter=30)
-    find_haloes(*d, 0.0015, 50, options=opt)
-    torch.cuda.synchronize()
-    e0, e1 = _events()
-    e0.record()
-    cat = find_haloes(*d, 0.0015, 50, options=opt)
-    e1.record()
-    e1.synchronize()
-    ms = e0.elapsed_time(e1)
-    # bit-exact FoF on a slab crop (the args.crop particles of smallest x), GPU vs C oracle
-    k = min(args.crop, s.n)
-    crop = np.sort(np.argpartition(s.x, k - 1)[:k])
-    lab_gpu = fof.fof_labels(np.ascontiguousarray(s.x[crop]), np.ascontiguousarray(s.y[crop]),
-                             np.ascontiguousarray(s.z[crop]), 0.0015)
-    lab_ref = oracle.fof_labels(s.x[crop], s.y[crop], s.z[crop], 0.0015)
-    print(json.dumps({"workload": f"full-{s.n:.2e}-particles-{args.full_haloes}-haloes", "particles": s.n,
-                      "haloes_found": cat.n_haloes, "ms": ms, "particles_per_s": s.n / (ms * 1e-3),
-                      "generate_s": gen_s, "crop_particles": int(len(crop)),
-                      "crop_fof_bit_exact": bool(np.array_equal(lab_gpu, lab_ref)), "alpha": s.meta["alpha"]}),
-          flush=True)
+    """The 2e8-particle snapshot alone (see full_snapshot_run)."""
+    print(json.dumps(full_snapshot_run(args)), flush=True)
     return 0
 
 
@@ -805,16 +962,18 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["snapshot", "batched", "gas", "full", "substructure", "gather", "psc",
-                                           "props"], default="snapshot")
+    ap.add_argument("--workload", choices=["northstar", "plummer2m", "batched", "gas", "full", "substructure",
+                                           "gather", "psc", "props"], default="northstar")
     ap.add_argument("--alpha", type=float, default=1.0)
-    ap.add_argument("--full-n", type=int, default=200_000_000)
-    ap.add_argument("--full-haloes", type=int, default=200_000)
+    ap.add_argument("--full-steps", type=int, default=2)
     ap.add_argument("--crop", type=int, default=10_000_000)
     ap.add_argument("--skip-fp64", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--skip-full", action="store_true")
     args = ap.parse_args()
     if args.impl == "reference":
+        if args.workload not in ("northstar", "plummer2m"):
+            args.workload = "northstar"
         return run_reference(args)
     from pyhalma_gb300 import build
     build.build()

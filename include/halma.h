@@ -34,6 +34,8 @@
  *   halma_fof_segmented           <- the per-halo fof.friends_of_friends_serial calls of the
  *                                    substructure loop (pyHALMA.py:716-726), batched
  *   halma_split_bridges           <- the substructure block pyHALMA.py:703-766
+ *   halma_amr_to_particles        <- halo_gas.py:9-52 patch_to_particles and :56-141
+ *                                    AMRgrid_to_particles (the loop over the box's patches)
  *   halma_ball_gather             <- halo_gas.py:223-277 st_gas_dm_particles_inside range
  *                                    queries (KDTree.query_ball_point, parallel_inside)
  *   halma_phase_space_clean       <- halo_properties.py:113-278 calc_cell / clean_cell and
@@ -83,6 +85,23 @@ int64_t     halma_kernel_launch_count(void);
  * returns the number of values available. */
 int         halma_set_profiling(int32_t on);
 int         halma_profile_stats(double *out, int32_t cap);
+/* With profiling on: milliseconds of the FoF stages of the last halma_find_haloes call
+ * (bounding box + keys, key sort, sorted records + sub-cell runs, cell table + hash +
+ * one-component cells, work items, linking, roots + labels, groups); returns the count (8). */
+int         halma_profile_fof_stages(double *out, int32_t cap);
+/* Measurement hook (no reference counterpart): the FP32 FMA rate of the current device, from
+ * a kernel of independent FMA chains (packed != 0: fma.rn.f32x2, else fma.rn.f32), iters
+ * chain steps per thread, fastest of three timed launches after one warm-up; an FMA counts
+ * as two flops.  The roofline denominator of the CUDA-core pair kernels. */
+int         halma_measure_fp32_fma_rate(int32_t packed, int32_t iters, double *tflops, double *ms,
+                                        halma_stream_t stream);
+/* Debug knob (no reference counterpart): the iteration bound of every union-find loop of the
+ * FoF kernels (find walks, CAS retries).  A loop that reaches it stops, and the FoF call
+ * returns HALMA_ERR_NOT_CONVERGED with the device still usable.  cap < 0 restores the default
+ * (2^26, never reached on real inputs); cap = 0 stops at the first step of any walk.  Applies
+ * to all later FoF calls in the process (halma_fof, halma_fof_segmented, halma_find_haloes,
+ * halma_split_bridges). */
+int         halma_set_union_find_cap(int32_t cap);
 
 /* ------------------------------------------------------------------------------------ */
 /* Friends-of-friends                                                                   */
@@ -213,6 +232,30 @@ int halma_halo_properties(int64_t n, const double *x, const double *y, const dou
                           double linking_length, double *out, halma_stream_t stream);
 
 /* ------------------------------------------------------------------------------------ */
+/* AMR gas cells to particles                                                           */
+/* ------------------------------------------------------------------------------------ */
+/* Replaces python_scripts/halo_gas.py:56-141 AMRgrid_to_particles (with the numba kernel
+ * patch_to_particles, :9-52) for one box: every cell of the n_patches patches given (levels
+ * >= 1, in the order to emit) whose centre x0 + i*res (x0 = r - res/2, res = (L/ncoarse)/2^level)
+ * lies strictly inside box = [xmin, xmax, ymin, ymax, zmin, zmax] and whose cr0amr and
+ * solapst flags are both non-zero becomes one gas particle: the centre, the velocity times
+ * 3e5, mass ((1 + delta) * rho_B) * res^3 (comoving) and the temperature.  Patch tables are
+ * host arrays: patch_level[p], patch_n[3p..3p+2] = nx, ny, nz, patch_r[3p..3p+2] = the
+ * reference's patchrx/ry/rz, cell_offset[p] = first cell of patch p (cell_offset[n] = total).
+ * Cell arrays (host or device) hold each patch's cells x-major: cell (ix, iy, iz) of patch p
+ * at cell_offset[p] + (ix*ny + iy)*nz + iz.  Particles come out in patch order, x-major, as
+ * the reference emits them; *n_out receives the count (HALMA_ERR_CAPACITY when it exceeds
+ * capacity). */
+int halma_amr_to_particles(int32_t n_patches, const int32_t *patch_level, const int32_t *patch_n,
+                           const double *patch_r, const int64_t *cell_offset, const double *delta,
+                           const double *vx, const double *vy, const double *vz, const double *temp,
+                           const uint8_t *cr0amr, const uint8_t *solapst, double L, int32_t ncoarse,
+                           const double *box, double rho_B, int64_t capacity, double *out_x,
+                           double *out_y, double *out_z, double *out_vx, double *out_vy,
+                           double *out_vz, double *out_mass, double *out_temp, int64_t *n_out,
+                           halma_stream_t stream);
+
+/* ------------------------------------------------------------------------------------ */
 /* Ball gather                                                                          */
 /* ------------------------------------------------------------------------------------ */
 /* The particles inside each of n_balls spheres (centre cx/cy/cz[s], radius[s] >= 0), all
@@ -262,15 +305,17 @@ int halma_bf_potential_f32(int64_t ntotal, const float *total_mass, const float 
 #define HALMA_MASK_NONE  2
 
 /* Allocation-free twin of halma_bf_potential_f32 in HALMA_POT_FAST mode (no counterpart in
- * the reference).  For callers that cannot allocate device memory when they need the
- * potential — code running while its stream is captured into a CUDA graph (cudaMalloc is not
- * allowed during capture) and host applications whose own pool owns all device memory.  It
- * takes device arrays only, calls no cudaMalloc/cudaFree, and keeps its scratch (the partial
- * sums of the source slices) in a 16 MiB static device array held by every GPU that loads the
- * library.  Same source split and same results as halma_bf_potential_f32(HALMA_POT_FAST);
- * returns HALMA_ERR_CAPACITY when the split needs more than 2,097,152 partial sums (source
- * slices x targets).  The first call on a device looks up the array's address: make it before
- * any stream capture.  Calls share the array: calls that overlap on the GPU race. */
+ * the reference).  For callers that cannot let a library allocate device memory: host codes
+ * (an AMR simulation calling the halo finder between steps) that reserve nearly all device
+ * memory in their own pool, and callers that keep several streams busy, for whom the
+ * device-wide synchronisation of a cudaFree is a stall.  It takes arrays in the current
+ * device's memory only, calls no cudaMalloc/cudaFree, and keeps its scratch (the partial sums
+ * of the source slices) in a 16 MiB static device array held by every GPU that loads the
+ * library.  Same source split, same kernels and identical results as
+ * halma_bf_potential_f32(HALMA_POT_FAST); returns HALMA_ERR_CAPACITY when the split needs more
+ * than 2,097,152 partial sums (source slices x targets).  The first call on a device looks up
+ * the array's address: make it before any stream capture.  Calls share the array: calls that
+ * overlap on the GPU race. */
 int halma_bf_potential_f32_noalloc(int64_t ntotal, const float *total_mass, const float *total_x,
                                    const float *total_y, const float *total_z, int64_t ntest,
                                    const float *test_x, const float *test_y, const float *test_z,

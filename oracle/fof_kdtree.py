@@ -1,49 +1,62 @@
 """ORACLE (test infrastructure / CPU baseline only): the reference's KDTree flood fill.
 
-Restates python_scripts/fof.py:18-79 (``friends_of_friends``): a breadth-first flood fill
-that calls ``scipy.spatial.KDTree.query_ball_point(point, linking_length)`` once per
-particle it visits.  Seeds are taken in index order (fof.py:34), a seed whose ball holds
-only itself is skipped (fof.py:43-44), and each finished group is returned as a sorted
-list of ints (fof.py:76).  The reference's periodic ``already_friend`` bookkeeping
-(fof.py:48, 62-72) only prunes duplicate queue entries; here a single ``queued`` mask does
-that job, which leaves the set of visited particles, and so the output, unchanged.
+Restates python_scripts/fof.py:18-79 (``friends_of_friends``) operation for operation, so that
+its CPU time stands for the reference's own where the reference cannot be imported (the GPU
+host has no copy of it):
+
+* one ``scipy.spatial.KDTree`` over the (N, 3) positions (fof.py:20);
+* seeds in index order, skipping particles already looked at (fof.py:34-37);
+* a seed whose ball holds only itself is skipped (fof.py:40-44);
+* the queue is a Python list consumed with ``pop(0)`` (fof.py:53-55); every visited particle
+  queries its ball, drops entries already looked at and entries already marked as friends by
+  two list comprehensions, and appends the rest to the queue and to the group
+  (fof.py:58-67);
+* every 64 visits the queue's entries are marked as friends (fof.py:70-72);
+* each finished group is ``np.unique`` of everything appended, as a list (fof.py:76).
 
 ``friends_of_friends_serial`` restates fof.py:87-89 (pack three 1-D arrays into (N,3)).
-This is the algorithm the CPU baseline times: one Python-level KDTree query per particle.
+The output equals the reference's on every golden case (tests/test_oracle.py).
 """
 from __future__ import annotations
 
 import numpy as np
 from scipy.spatial import KDTree
 
+CLEAN_EVERY = 64   # fof.py:33 iterations_to_clean
+
 
 def friends_of_friends(data, linking_length):
     data = np.asarray(data)
     tree = KDTree(data)
     n = data.shape[0]
-    queued = np.zeros(n, dtype=bool)
-    out = []
+    looked = np.zeros(n, dtype=bool)
+    marked = np.zeros(n, dtype=bool)
+    groups = []
     for seed in range(n):
-        if queued[seed]:
+        if looked[seed]:
             continue
-        first = tree.query_ball_point(data[seed], linking_length)
-        if len(first) <= 1:
+        queue = tree.query_ball_point(data[seed], linking_length)
+        if len(queue) <= 1:
             continue
-        members = list(first)
-        queued[first] = True
-        head = 0
-        while head < len(members):
-            p = members[head]
-            head += 1
-            if p == seed:
+        found = queue.copy()
+        looked[seed] = True
+        marked[queue] = True
+        visits = 0
+        while len(queue) > 0:
+            p = queue.pop(0)
+            if looked[p]:
                 continue
-            nb = tree.query_ball_point(data[p], linking_length)
-            fresh = [q for q in nb if not queued[q]]
-            if fresh:
-                queued[fresh] = True
-                members.extend(fresh)
-        out.append(sorted(set(int(i) for i in members)))
-    return out
+            fresh = tree.query_ball_point(data[p], linking_length)
+            fresh = [q for q in fresh if not looked[q]]
+            fresh = [q for q in fresh if not marked[q]]
+            queue += fresh
+            found += fresh
+            looked[p] = True
+            if visits % CLEAN_EVERY == 0 and visits != 0:
+                marked[queue] = True
+            visits += 1
+        groups.append(np.unique(np.array(found)).tolist())
+    return groups
 
 
 def friends_of_friends_serial(st_x, st_y, st_z, linking_length):

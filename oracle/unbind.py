@@ -23,6 +23,19 @@ from . import MASK_SELF, potential_f64
 G_MPC = 4.3e-9
 
 
+def unbind_pass(x, y, z, vx, vy, vz, m, eps=1e-4, factor_v=1.0, G=G_MPC, ncores=None):
+    """One pass of the cut over the particles given (all treated as bound): returns
+    (phi, kinetic energy, total energy) per particle in FP64; the particle stays iff
+    energy <= 0 (halo_properties.py:359)."""
+    M = m.sum()
+    vbx, vby, vbz = ((m * v).sum() / M for v in (vx, vy, vz))
+    cx, cy, cz = ((m * a).sum() / M for a in (x, y, z))
+    px, py, pz = x - cx, y - cy, z - cz
+    phi = potential_f64(m, px, py, pz, px, py, pz, eps2=float(eps) ** 2, mask=MASK_SELF, ncores=ncores)
+    ek = 0.5 * ((vx - vbx) ** 2 + (vy - vby) ** 2 + (vz - vbz) ** 2)
+    return phi, ek, ek - G * phi * factor_v * factor_v
+
+
 def unbind_halo(x, y, z, vx, vy, vz, m, eps=1e-4, factor_v=1.0, max_iter=20, G=G_MPC,
                 ncores=None, return_energy=False):
     """Returns (bound mask, passes run[, energies, potentials]).

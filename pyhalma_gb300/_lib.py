@@ -88,6 +88,9 @@ SIGNATURES = {
     "halma_set_tile_table": ([_I32, _P, _P, _I32], ctypes.c_int),
     "halma_get_tile_table": ([_P, _P, _P, _P], ctypes.c_int),
     "halma_profile_stats": ([_P, _I32], ctypes.c_int),
+    "halma_set_union_find_cap": ([_I32], ctypes.c_int),
+    "halma_profile_fof_stages": ([_P, _I32], ctypes.c_int),
+    "halma_measure_fp32_fma_rate": ([_I32, _I32, _P, _P, _P], ctypes.c_int),
     "halma_fof": ([_I64, _P, _P, _P, _F64, _P, _P, _P], ctypes.c_int),
     "halma_fof_groups": ([_I64, _P, _I32, _P, _P, _P, _P], ctypes.c_int),
     "halma_fof_segmented": ([_I64, _P, _P, _P, _I64, _P, _F64, _P, _P, _P], ctypes.c_int),
@@ -98,6 +101,8 @@ SIGNATURES = {
     "halma_halo_properties": ([_I64, _P, _P, _P, _P, _P, _P, _P, _I64, _P, _P, _P, _F64, _P, _P], ctypes.c_int),
     "halma_ball_gather": ([_I64, _P, _P, _P, _I64, _P, _P, _P, _P, _I32, _P, _P, _I64, _P, _P], ctypes.c_int),
     "halma_sequential_sum_f64": ([_I64, _P, _I64, _P, _P, _P], ctypes.c_int),
+    "halma_amr_to_particles": ([_I32, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _F64, _I32, _P, _F64, _I64,
+                                _P, _P, _P, _P, _P, _P, _P, _P, _P, _P], ctypes.c_int),
     "halma_bf_potential_f32": ([_I64, _P, _P, _P, _P, _I64, _P, _P, _P, _P, _I32, _F64, _P], ctypes.c_int),
     "halma_potential_f64": ([_I64, _P, _P, _P, _P, _I64, _P, _P, _P, _F64, _I32, _I64, _P, _P], ctypes.c_int),
     "halma_potential_f32": ([_I64, _P, _P, _P, _P, _I64, _P, _P, _P, _F64, _I32, _I64, _P, _P], ctypes.c_int),
@@ -160,6 +165,24 @@ def profile_stats():
     sym_ms = [float(buf[6 + 4 * i]) for i in range(k)]
     return {"fof_ms": float(buf[0]), "unbind_ms": float(buf[1]), "passes": passes, "sym_pairs": sym,
             "sym_ms": sym_ms}
+
+
+FOF_STAGES = ["bbox_keys", "sort", "records", "cells", "items", "link", "labels", "groups"]
+
+
+def measure_fp32_fma_rate(packed=True, iters=1 << 15):
+    """(TFLOP/s, ms) of the FP32 FMA peak kernel on the current device."""
+    t, ms = ctypes.c_double(0), ctypes.c_double(0)
+    check(lib().halma_measure_fp32_fma_rate(1 if packed else 0, int(iters), ctypes.byref(t), ctypes.byref(ms), None),
+          "halma_measure_fp32_fma_rate")
+    return t.value, ms.value
+
+
+def profile_fof_stages():
+    """Milliseconds of each FoF stage of the last find_haloes call (profiling on)."""
+    buf = np.zeros(len(FOF_STAGES))
+    lib().halma_profile_fof_stages(buf.ctypes.data_as(ctypes.c_void_p), len(buf))
+    return dict(zip(FOF_STAGES, buf.tolist()))
 
 
 # ---------------------------------------------------------------------------------------

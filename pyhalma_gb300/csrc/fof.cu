@@ -23,6 +23,7 @@
 
 #include "common.cuh"
 #include "sort.cuh"
+#include "unbind.cuh"
 
 namespace halma {
 
@@ -30,7 +31,10 @@ namespace {
 
 constexpr int kFofWarps = 8;
 constexpr uint64_t kEmptyKey = ~0ull;
-constexpr int kUfCap = 1 << 26;      // bound on any union-find loop (never reached in practice)
+constexpr int kUfCapDefault = 1 << 26;   // bound on any union-find loop (never reached in practice)
+// The bound the kernels use: halma_set_union_find_cap changes it (a debug knob, so that tests
+// can make the loops run out); pushed to each device before its next FoF.
+__constant__ int c_uf_cap = kUfCapDefault;
 
 struct FofGeom {
     double xmin, ymin, zmin;
@@ -63,12 +67,13 @@ __device__ __forceinline__ uint64_t mix64(uint64_t k) {
 __device__ __forceinline__ int uf_find(int *parent, int v, int *err) {
     int p = __ldcg(parent + v);
     int guard = 0;
+    const int cap = c_uf_cap;
     while (p != v) {
         const int gp = __ldcg(parent + p);
         if (gp != p) __stcg(parent + v, gp);   // path halving: gp is an ancestor of v
         v = p;
         p = gp;
-        if (++guard > kUfCap) {
+        if (++guard > cap) {
             atomicOr(err, 1);
             break;
         }
@@ -85,12 +90,13 @@ __device__ __forceinline__ int uf_find(int *parent, int v, int *err) {
 __device__ __forceinline__ int uf_find_cached(int *parent, int v, int *err) {
     int p = parent[v];
     int guard = 0;
+    const int cap = c_uf_cap;
     while (p != v) {
         const int gp = parent[p];
         if (gp != p) __stcg(parent + v, gp);
         v = p;
         p = gp;
-        if (++guard > kUfCap) {
+        if (++guard > cap) {
             atomicOr(err, 1);
             break;
         }
@@ -102,6 +108,7 @@ __device__ __forceinline__ int uf_find_cached(int *parent, int v, int *err) {
 // CAS loses a race.  Every root of a tree is its smallest sorted position.
 __device__ __forceinline__ void uf_union(int *parent, int a, int b, int *err) {
     int guard = 0;
+    const int cap = c_uf_cap;
     while (a != b) {
         if (a < b) {
             const int t = a;
@@ -112,7 +119,7 @@ __device__ __forceinline__ void uf_union(int *parent, int a, int b, int *err) {
         if (old == a) return;
         a = uf_find(parent, old, err);
         b = uf_find(parent, b, err);
-        if (++guard > kUfCap) {
+        if (++guard > cap) {
             atomicOr(err, 1);
             return;
         }
@@ -899,6 +906,26 @@ void set_scale(FofGeom &g, double ll, double ext) {
     g.r2 = ll * ll;
 }
 
+int g_uf_cap_host = kUfCapDefault;   // guarded by api_mutex()
+int g_uf_cap_pushed[64];             // value last copied to each device (0 = never)
+bool g_uf_cap_init = false;
+
+// Copies the host's union-find cap to the current device when it differs from the last copy.
+int push_uf_cap(cudaStream_t st) {
+    if (!g_uf_cap_init) {
+        for (int &v : g_uf_cap_pushed) v = kUfCapDefault;   // the __constant__ initialiser
+        g_uf_cap_init = true;
+    }
+    const int dev = current_device();
+    if (dev < 0 || dev >= 64) return fail(HALMA_ERR_CAPACITY, "device ordinal %d out of range", dev);
+    if (g_uf_cap_pushed[dev] != g_uf_cap_host) {
+        HALMA_CUDA(cudaMemcpyToSymbolAsync(c_uf_cap, &g_uf_cap_host, sizeof(int), 0, cudaMemcpyHostToDevice, st));
+        HALMA_CUDA(cudaStreamSynchronize(st));
+        g_uf_cap_pushed[dev] = g_uf_cap_host;
+    }
+    return HALMA_OK;
+}
+
 // Keys, sort, cells, links and labels for a geometry whose cell grid is known.
 int fof_core(int n, const double *x, const double *y, const double *z, FofGeom g, SegGeom sg, int *labels,
              int64_t *n_groups, cudaStream_t st) {
@@ -929,6 +956,7 @@ int fof_core(int n, const double *x, const double *y, const double *z, FofGeom g
     const size_t o_dlist = M.add(4ull * ((uint64_t)n / kDenseMin + 1));   // cells of >= kDenseMin particles
     const size_t o_tmp = M.add(std::max(sort_b, scan_b));
     void *base = nullptr;
+    HALMA_TRY(push_uf_cap(st));
     HALMA_TRY(workspace(M.total, &base, st));
     auto *kin = at<uint64_t>(base, o_kin), *kout = at<uint64_t>(base, o_kout);
     auto *vin = at<int>(base, o_vin), *vout = at<int>(base, o_vout);
@@ -947,15 +975,21 @@ int fof_core(int n, const double *x, const double *y, const double *z, FofGeom g
     void *tmp = at<void>(base, o_tmp);
     const int g1 = std::min(sms * 8, grid_for(n, 256));
 
+    Profile &prof = profile();
+    const bool stages = !sg.seg_of;   // stage times of the plain FoF only
+    auto mark = [&](int k) { return stages ? prof.fof_mark(k, st) : HALMA_OK; };
     HALMA_CUDA(cudaMemsetAsync(cnt, 0, 64, st));
     HALMA_LAUNCH(keys_kernel, g1, 256, 0, st, x, y, z, n, g, sg, kin, vin, pre);
+    HALMA_TRY(mark(1));
     HALMA_TRY(sort_pairs_u64_i32(tmp, sort_b, kin, kout, vin, vout, n, end_bit, st));
+    HALMA_TRY(mark(2));
     HALMA_LAUNCH(prep_kernel, g1, 256, 0, st, n, g.sb, kout, vout, pre, rec, head, parent, has, minidx);
     if (g.sb != 0 && g.lo > 0.f) {   // sub-cells in the key and a positive linking length
         HALMA_LAUNCH(subrun_kernel, g1, 256, 0, st, n, kout, flag);
         HALMA_TRY(inclusive_max_i32(tmp, scan_b, flag, root, n, st));
         HALMA_LAUNCH(preunion_kernel, g1, 256, 0, st, n, kout, root, parent, has);
     }
+    HALMA_TRY(mark(3));
     HALMA_TRY(exclusive_sum_i32(tmp, scan_b, head, cpos, n, st));
     HALMA_LAUNCH(hash_size_kernel, 1, 1, 0, st, n, head, cpos, (unsigned long long)hcap, hmask);
     HALMA_LAUNCH(hash_clear_kernel, g1, 256, 0, st, hmask, hk);
@@ -970,13 +1004,17 @@ int fof_core(int n, const double *x, const double *y, const double *z, FofGeom g
         HALMA_CUDA(cudaMemsetAsync(conn, 0, n, st));
     }
     HALMA_LAUNCH(slot_fill_kernel, g1, 256, 0, st, cnt + 0, cst, hv, conn, hk);
+    HALMA_TRY(mark(4));
     HALMA_LAUNCH(itemflag_kernel, g1, 256, 0, st, n, head, cpos, cst, flag);
     HALMA_TRY(exclusive_sum_i32(tmp, scan_b, flag, ipos, n, st));
     HALMA_LAUNCH(items_kernel, g1, 256, 0, st, n, head, cpos, flag, ipos, cst, ckey, conn, g, items, cnt + 1);
+    HALMA_TRY(mark(5));
     HALMA_LAUNCH(link_kernel, sms * 8, 32 * kFofWarps, 0, st, rec, items, cnt + 1, cnt + 5, hk, hmask, g, x, y, z,
                  parent, has, cnt + 3);
+    HALMA_TRY(mark(6));
     HALMA_LAUNCH(root_kernel, g1, 256, 0, st, n, rec, parent, has, root, minidx, cnt + 3);
     HALMA_LAUNCH(label_kernel, g1, 256, 0, st, n, rec, has, root, minidx, labels, cnt + 2);
+    HALMA_TRY(mark(7));
     int hc[4];
     HALMA_CUDA(cudaMemcpyAsync(hc, cnt, sizeof(hc), cudaMemcpyDeviceToHost, st));
     HALMA_CUDA(cudaStreamSynchronize(st));
@@ -1011,6 +1049,7 @@ int fof_device(int n, const double *x, const double *y, const double *z, double 
         return HALMA_OK;
     }
     FofGeom g{};
+    HALMA_TRY(profile().fof_mark(0, st));
     {
         double bb[7];
         HALMA_TRY(bbox_device(n, x, y, z, bb, st));
@@ -1077,6 +1116,12 @@ int fof_segmented_device(int n, int nseg, const int64_t *off, const double *x, c
 }  // namespace halma
 
 using namespace halma;
+
+extern "C" int halma_set_union_find_cap(int32_t cap) {
+    std::lock_guard<std::mutex> guard(api_mutex());
+    g_uf_cap_host = cap < 0 ? kUfCapDefault : cap;
+    return HALMA_OK;
+}
 
 extern "C" int halma_fof(int64_t n, const double *x, const double *y, const double *z, double linking_length,
                          int32_t *labels, int64_t *n_groups, halma_stream_t stream) {

@@ -128,6 +128,7 @@ extern "C" int halma_find_haloes(int64_t n, const double *x, const double *y, co
     HALMA_TRY(fof_device((int)n, dx, dy, dz, linking_length, dlab, nullptr, st));
     int64_t ng = 0, nm = 0;
     HALMA_TRY(fof_groups_device((int)n, dlab, std::max(min_members, 1), doff, dmem, &ng, &nm, st));
+    HALMA_TRY(prof.fof_mark(Profile::kFofStages, st));
     if (prof.enabled) HALMA_CUDA(cudaEventRecord(ev[1], st));
     *n_haloes = ng;
     HALMA_CUDA(cudaMemsetAsync(dbnd, 0, n, st));
@@ -151,6 +152,11 @@ extern "C" int halma_find_haloes(int64_t n, const double *x, const double *y, co
         if (ng > 0) HALMA_CUDA(cudaEventElapsedTime(&b, ev[2], ev[3]));
         prof.fof_ms = a;
         prof.unbind_ms = b;
+        for (int k = 0; k < Profile::kFofStages; ++k) {
+            float t = 0.f;
+            HALMA_CUDA(cudaEventElapsedTime(&t, prof.fev[k], prof.fev[k + 1]));
+            prof.fof_stage_ms[k] = t;
+        }
         for (auto &e : ev) cudaEventDestroy(e);
     }
     // outputs (host or device)
@@ -176,6 +182,13 @@ extern "C" int halma_set_profiling(int32_t on) {
     std::lock_guard<std::mutex> guard(api_mutex());
     profile().enabled = on != 0;
     return HALMA_OK;
+}
+
+extern "C" int halma_profile_fof_stages(double *out, int32_t cap) {
+    std::lock_guard<std::mutex> guard(api_mutex());
+    const Profile &p = profile();
+    for (int i = 0; out && i < cap && i < Profile::kFofStages; ++i) out[i] = p.fof_stage_ms[i];
+    return Profile::kFofStages;
 }
 
 extern "C" int halma_profile_stats(double *out, int32_t cap) {

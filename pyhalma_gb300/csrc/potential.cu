@@ -348,18 +348,21 @@ extern "C" int halma_potential_f64(int64_t ns, const double *mm, const double *s
 // ---------------------------------------------------------------------------------------
 // Allocation-free variant of the fast (compensated FP32) potential.
 //
-// Some callers cannot allocate device memory at the moment they need the potential: code
-// that runs while its stream is being captured into a CUDA graph (cudaMalloc is not allowed
-// during capture), and host applications that own every byte of device memory through their
-// own pool and forbid libraries from calling cudaMalloc/cudaFree behind their back.  This
-// entry point serves them: it takes device arrays only and keeps its scratch — the per-slice
-// partial sums of the source-split kernel — in the fixed array below instead of the library's
-// cached workspace.
+// Some callers cannot let a library allocate device memory.  Simulation codes that embed the
+// halo finder (an AMR code calling it between time steps, say) usually reserve almost all of
+// the GPU's memory up front for their own pool and hand out pieces themselves, so a
+// cudaMalloc from the library either fails or breaks the host's accounting; and a cudaFree
+// synchronises the whole device, which stalls every other stream of a caller that keeps
+// several streams busy.  This entry point serves such callers: it takes device arrays only
+// and keeps its scratch -- the per-slice partial sums of the source-split kernel -- in the
+// fixed array below instead of the library's cached workspace.  It calls no cudaMalloc,
+// cudaFree or allocating library routine.
 //
 // Limit: the scratch holds kNoAllocScratchDoubles = 2,097,152 partial sums (16 MiB).  The call
-// splits the sources exactly as halma_bf_potential_f32 does in HALMA_POT_FAST mode (so the two
-// return the same values); when that split needs more than 2,097,152 partial sums
-// (source slices x targets) the call is rejected with HALMA_ERR_CAPACITY.
+// splits the sources exactly as halma_bf_potential_f32 does in HALMA_POT_FAST mode and runs
+// the same kernels, so the two return identical values; when that split needs more than
+// 2,097,152 partial sums (source slices x targets) the call is rejected with
+// HALMA_ERR_CAPACITY.
 //
 // Every GPU that loads this library holds the 16 MiB array until the process exits.  All calls
 // share it and it keeps the previous call's contents; each partial sum a call reads is written
@@ -374,6 +377,19 @@ namespace {
 constexpr int kMaxDevices = 64;
 std::mutex g_noalloc_mutex;
 double *g_noalloc_ptr[kMaxDevices] = {};
+
+// Memory the current device's kernels can use in place: device memory of this device, or
+// managed memory.  Another GPU's device memory is refused rather than read over the peer link.
+bool is_local_device_pointer(const void *p) {
+    if (!p) return false;
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    if (a.type == cudaMemoryTypeManaged) return true;
+    return a.type == cudaMemoryTypeDevice && a.device == current_device();
+}
 
 // Device address of g_noalloc_scratch on the current device (looked up once per device).
 int noalloc_scratch(double **out) {
@@ -401,8 +417,9 @@ extern "C" int halma_bf_potential_f32_noalloc(int64_t ntotal, const float *total
     if (!(eps2 >= 0.0) || !isfinite(eps2)) return fail(HALMA_ERR_INVALID, "eps2 must be finite and >= 0");
     const void *arrays[8] = {test_x, test_y, test_z, binding_energy, total_mass, total_x, total_y, total_z};
     for (int k = 0; k < (ntotal > 0 ? 8 : 4); ++k)
-        if (!is_device_pointer(arrays[k]))
-            return fail(HALMA_ERR_INVALID, "the allocation-free entry point takes device arrays only");
+        if (!is_local_device_pointer(arrays[k]))
+            return fail(HALMA_ERR_INVALID,
+                        "the allocation-free entry point takes arrays in the current device's memory only");
     cudaStream_t st = (cudaStream_t)stream;
     if (ntotal == 0) {
         HALMA_CUDA(cudaMemsetAsync(binding_energy, 0, sizeof(float) * ntest, st));

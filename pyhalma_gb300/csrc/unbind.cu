@@ -1297,6 +1297,13 @@ static TileTable &tile_table_ref() {
 
 TileTable tile_table() { return tile_table_ref(); }
 
+int Profile::fof_mark(int stage, cudaStream_t st) {
+    if (!enabled) return HALMA_OK;
+    if (!fev[stage]) HALMA_CUDA(cudaEventCreate(&fev[stage]));
+    HALMA_CUDA(cudaEventRecord(fev[stage], st));
+    return HALMA_OK;
+}
+
 int Profile::ensure_events(int k) {
     while ((int)ev0.size() < k) {
         cudaEvent_t a, b, c;

@@ -16,7 +16,13 @@ struct Profile {
     };
     std::vector<Pass> passes;
     double fof_ms = 0, unbind_ms = 0;
+    // FoF stages of the last plain FoF (keys, sort, records, cells, items, links, labels,
+    // groups), milliseconds between events recorded on the launching stream
+    static constexpr int kFofStages = 8;
+    cudaEvent_t fev[kFofStages + 1] = {};
+    double fof_stage_ms[kFofStages] = {};
     int ensure_events(int k);
+    int fof_mark(int stage, cudaStream_t st);   // records fev[stage] when profiling (0..kFofStages)
 };
 Profile &profile();
 

@@ -7,6 +7,8 @@
 * ``most_bound_particle(...)``                                halo_gas.py:498-634
 * ``parallel_inside(...)``, ``st_gas_dm_particles_inside(...)`` halo_gas.py:218-277 (ball
   gather on the GPU; ``balls_inside`` does many haloes' spheres in one call)
+* ``AMRgrid_to_particles(...)``                               halo_gas.py:56-141 (with the
+  numba kernel patch_to_particles, :9-52): the box's AMR cells to gas particles on the GPU
 
 The f2py kernel particle.particle.brute_force_binding_energy (particle_subroutines.f90:466-514)
 is replaced by ``halma_bf_potential_f32``.  Like the wrapper it casts every input to float32
@@ -25,12 +27,20 @@ mass tallies — with every potential evaluated on the GPU.
 """
 from __future__ import annotations
 
+import ctypes
+
 import numpy as np
 
 from . import _lib
 
 POTENTIAL_MODE = "reference"
 _MODES = {"reference": _lib.POT_REFERENCE, "fast": _lib.POT_FAST}
+
+try:   # MASCLET's code mass unit in Msun, when masclet_framework is installed
+    from masclet_framework import units as _units
+    MASS_TO_SUN = float(_units.mass_to_sun)
+except Exception:   # masses are taken as already in Msun
+    MASS_TO_SUN = 1.0
 
 
 def bf_potential(total_mass, total_x, total_y, total_z, test_x, test_y, test_z, mode=None, eps2=0.0):
@@ -170,7 +180,6 @@ def balls_inside(x, y, z, cx, cy, cz, R, strict=False):
     pair rule of ``KDTree.query_ball_point``; strict=True: sqrt(...) < R, ``parallel_inside``.
     Host NumPy arrays or CUDA torch tensors (outputs on the same side).
     """
-    import ctypes
     if _lib._is_torch(x):
         n = int(x.shape[0])
         px, py, pz = x, y, z
@@ -215,24 +224,92 @@ def parallel_inside(array_x, array_y, array_z, R, cx, cy, cz):
     return mask
 
 
-MASS_TO_SUN = 1.0   # masclet_framework units.mass_to_sun: set it when masses come in MASCLET units
+def create_vector_levels(npatch):
+    """Refinement level of every patch: patch 0 is the base grid (level 0), followed by
+    npatch[1] patches of level 1, npatch[2] of level 2, ... (the patch numbering of MASCLET
+    grids; masclet_framework.tools.create_vector_levels, a third-party helper the reference
+    calls at halo_gas.py:91, restated)."""
+    npatch = np.asarray(npatch, dtype=np.int64)
+    return np.concatenate([np.zeros(1, dtype=np.int64)] +
+                          [np.full(int(c), lev, dtype=np.int64) for lev, c in enumerate(npatch[1:], start=1)])
+
+
+def _patches_in_box(box, levels, patchnx, patchny, patchnz, patchrx, patchry, patchrz, L, ncoarse):
+    """Refined patches (level >= 1) whose extent, widened by one cell on each side, meets the
+    box, in patch order.  A superset of the patches holding a cell centre strictly inside the
+    box; the cell test itself runs in the kernel, so the particles do not depend on how tight
+    this preselection is (the reference preselects with masclet_framework.tools.
+    which_patches_inside_box, halo_gas.py:90)."""
+    lev = np.asarray(levels, dtype=np.int64)
+    res = (L / ncoarse) / 2.0 ** lev
+    keep = lev >= 1
+    for n, r, lo, hi in ((patchnx, patchrx, box[0], box[1]), (patchny, patchry, box[2], box[3]),
+                         (patchnz, patchrz, box[4], box[5])):
+        n = np.asarray(n, dtype=np.float64)
+        r = np.asarray(r, dtype=np.float64)
+        keep &= (r - 2.0 * res <= hi) & (r + (n + 1.0) * res >= lo)
+    return np.nonzero(keep)[0]
+
+
+def AMRgrid_to_particles(L, ncoarse, grid_data, gas_data, Rrps, cx, cy, cz, rho_B):
+    """halo_gas.py:56-141: one gas particle per leaf cell (cr0amr and solapst true) of the
+    refined patches whose centre lies strictly inside the cube of half-side Rrps about
+    (cx, cy, cz); returns (x, y, z, vx, vy, vz, mass, temp) float64 arrays in the reference's
+    order (patches in order, cells x-major), velocities in km/s (cell values times 3e5) and
+    comoving masses (1 + delta) * rho_B * res^3.  ``grid_data`` / ``gas_data`` are the
+    reference's MASCLET tuples (grid_data[5] npatch, [6:9] patchnx/ny/nz, [12:15]
+    patchrx/ry/rz; gas_data[:7] delta, vx, vy, vz, temp, cr0amr, solapst as per-patch 3-D
+    arrays indexed [ix, iy, iz]).  The cell loop runs on the GPU (halma_amr_to_particles);
+    cell values are taken in float64 (numba's arithmetic on float32 fields)."""
+    npatch = grid_data[5]
+    patchnx, patchny, patchnz = grid_data[6], grid_data[7], grid_data[8]
+    patchrx, patchry, patchrz = grid_data[12], grid_data[13], grid_data[14]
+    gas_delta, gas_vx, gas_vy, gas_vz, gas_temp, gas_cr0amr, gas_solapst = gas_data[:7]
+    box = np.array([cx - Rrps, cx + Rrps, cy - Rrps, cy + Rrps, cz - Rrps, cz + Rrps], dtype=np.float64)
+    levels = create_vector_levels(npatch)
+    sel = _patches_in_box(box, levels, patchnx, patchny, patchnz, patchrx, patchry, patchrz, float(L), int(ncoarse))
+    k = len(sel)
+    plev = np.ascontiguousarray(levels[sel], dtype=np.int32)
+    pn = np.ascontiguousarray(np.stack([np.asarray(patchnx)[sel], np.asarray(patchny)[sel],
+                                        np.asarray(patchnz)[sel]], 1), dtype=np.int32).reshape(-1)
+    pr = np.ascontiguousarray(np.stack([np.asarray(patchrx)[sel], np.asarray(patchry)[sel],
+                                        np.asarray(patchrz)[sel]], 1), dtype=np.float64).reshape(-1)
+    cells = pn.reshape(-1, 3).astype(np.int64).prod(axis=1) if k else np.zeros(0, dtype=np.int64)
+    coff = np.zeros(k + 1, dtype=np.int64)
+    np.cumsum(cells, out=coff[1:])
+    flat = lambda fields, dt: (np.ascontiguousarray(np.concatenate([np.ravel(np.asarray(fields[p], dtype=dt))
+                                                                    for p in sel]), dtype=dt)
+                               if k else np.zeros(0, dtype=dt))
+    delta, vx, vy, vz, temp = (flat(f, np.float64) for f in (gas_delta, gas_vx, gas_vy, gas_vz, gas_temp))
+    leaf = lambda fields: np.ascontiguousarray(np.concatenate([np.ravel(np.asarray(fields[p]) != 0) for p in sel])
+                                               .astype(np.uint8) if k else np.zeros(0, dtype=np.uint8))
+    cr0, sol = leaf(gas_cr0amr), leaf(gas_solapst)
+    cap = int(coff[-1])
+    out = [np.empty(max(cap, 1), dtype=np.float64) for _ in range(8)]
+    n_out = ctypes.c_int64(0)
+    st = _lib.lib().halma_amr_to_particles(k, _lib.ptr(plev), _lib.ptr(pn), _lib.ptr(pr), _lib.ptr(coff),
+                                           *[_lib.ptr(a) for a in (delta, vx, vy, vz, temp, cr0, sol)], float(L),
+                                           int(ncoarse), _lib.ptr(box), float(rho_B), cap,
+                                           *[_lib.ptr(a) for a in out], ctypes.byref(n_out), None)
+    _lib.check(st, "halma_amr_to_particles")
+    m = int(n_out.value)
+    return tuple(a[:m].copy() for a in out)
 
 
 def st_gas_dm_particles_inside(rete, L, ncoarse, grid_data, gas_data, masclet_dm_data, masclet_st_data,
                                st_kdtree, dm_kdtree, cx, cy, cz, R, rho_B):
     """halo_gas.py:223-277 with the particle side on the GPU.
 
-    ``gas_data`` is the gas already turned into particles — the tuple (gas_x, gas_y, gas_z,
-    gas_vx, gas_vy, gas_vz, gas_mass, gas_temp) that ``AMRgrid_to_particles`` (halo_gas.py:
-    56-141) returns; that conversion reads MASCLET AMR grids and is not part of this package,
-    so ``L``, ``ncoarse``, ``grid_data`` and ``rho_B`` are accepted and unused.  The KD-trees
-    are replaced by the GPU ball gather (``st_kdtree`` / ``dm_kdtree`` are unused), so the DM
-    and star selections come back in ascending index order instead of tree order.  Returns the
-    reference's 17-tuple.
+    With ``grid_data`` given, the gas comes from ``AMRgrid_to_particles(L, ncoarse,
+    grid_data, gas_data, R, cx, cy, cz, rho_B)`` as in the reference (halo_gas.py:231-233).
+    With ``grid_data=None``, ``gas_data`` is taken as gas already turned into particles — the
+    tuple (gas_x, gas_y, gas_z, gas_vx, gas_vy, gas_vz, gas_mass, gas_temp) that conversion
+    returns.  The KD-trees are replaced by the GPU ball gather (``st_kdtree`` / ``dm_kdtree``
+    are unused), so the DM and star selections come back in ascending index order instead of
+    tree order.  Returns the reference's 17-tuple.
     """
     if grid_data is not None:
-        raise NotImplementedError("AMR grid to particle conversion needs MASCLET grids; pass the gas as "
-                                  "particles in gas_data and grid_data=None")
+        gas_data = AMRgrid_to_particles(L, ncoarse, grid_data, gas_data, R, cx, cy, cz, rho_B)
     gas_x, gas_y, gas_z, gas_vx, gas_vy, gas_vz, gas_mass, gas_temp = (np.asarray(a) for a in gas_data)
     inside = parallel_inside(gas_x, gas_y, gas_z, R, cx, cy, cz)
     gas_x, gas_y, gas_z = gas_x[inside], gas_y[inside], gas_z[inside]

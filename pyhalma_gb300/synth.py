@@ -276,11 +276,13 @@ def alpha_for_mean(mean, n_min=50, n_max=200_000):
 
 def full_snapshot(n_total=200_000_000, n_haloes=200_000, *, seed=0, box_mpc=100.0, bg_frac=0.20,
                   bridge_frac=0.05, alpha=None, n_min=50, n_max=200_000, particle_mass=1e6,
-                  bulk_sigma=200.0, bg_sigma=300.0, chunk=20_000):
+                  bulk_sigma=200.0, bg_sigma=300.0, contaminant_frac=0.0, chunk=20_000):
     """Large snapshot: power-law Plummer haloes (a fraction placed in pairs within 2a of a
     partner to form FoF bridges) plus a uniform background.  With alpha=None the slope is
-    chosen so that haloes hold (1 - bg_frac) of n_total on average.  Returns float64 arrays
-    in Mpc, km/s, Msun and the per-particle generating halo id (-1 background)."""
+    chosen so that haloes hold (1 - bg_frac) of n_total on average; the background fills the
+    rest up to n_total.  ``contaminant_frac`` of each halo's members are contaminants (uniform
+    inside 3a at 3 v_esc).  Returns float64 arrays in Mpc, km/s, Msun and the per-particle
+    generating halo id (-1 background)."""
     rng = np.random.default_rng(seed)
     n_bg_target = int(round(bg_frac * n_total))
     if alpha is None:
@@ -301,16 +303,18 @@ def full_snapshot(n_total=200_000_000, n_haloes=200_000, *, seed=0, box_mpc=100.
     n = n_halo + n_bg
     out = {k: np.empty(n) for k in ("x", "y", "z", "vx", "vy", "vz")}
     hid = np.empty(n, dtype=np.int32)
+    cont = np.zeros(n, dtype=bool)
     pos = 0
     for h0 in range(0, n_haloes, chunk):
         sl = slice(h0, min(h0 + chunk, n_haloes))
-        p, v, sid, _ = _spheres(rng, counts[sl], masses[sl], centres[sl], bulk[sl], 0.0)
+        p, v, sid, c = _spheres(rng, counts[sl], masses[sl], centres[sl], bulk[sl], contaminant_frac)
         k = p.shape[0]
         for d, key in enumerate(("x", "y", "z")):
             out[key][pos:pos + k] = p[:, d] / 1e3
         for d, key in enumerate(("vx", "vy", "vz")):
             out[key][pos:pos + k] = v[:, d]
         hid[pos:pos + k] = sid + h0
+        cont[pos:pos + k] = c
         pos += k
     for q0 in range(0, n_bg, 10_000_000):
         k = min(10_000_000, n_bg - q0)
@@ -321,10 +325,10 @@ def full_snapshot(n_total=200_000_000, n_haloes=200_000, *, seed=0, box_mpc=100.
         hid[pos:pos + k] = -1
         pos += k
     mass = np.full(n, particle_mass)
-    return Snapshot(out["x"], out["y"], out["z"], out["vx"], out["vy"], out["vz"], mass, hid,
-                    np.zeros(n, dtype=bool), box_mpc,
+    return Snapshot(out["x"], out["y"], out["z"], out["vx"], out["vy"], out["vz"], mass, hid, cont, box_mpc,
                     dict(seed=seed, alpha=alpha, n_haloes=n_haloes, halo_particles=n_halo, background=n_bg,
-                         bridged_pairs=n_pair // 2))
+                         bridged_pairs=n_pair // 2, contaminant_frac=contaminant_frac,
+                         halo_counts=counts))
 
 
 def _nfw_radius(rng, n, c, r_vir):

@@ -1,12 +1,18 @@
 """One-call snapshot pipeline (FoF -> groups >= minp -> batched unbinding) against the
-oracle composition on the 1e5-particle Plummer snapshot."""
+oracle composition on the 1e5-particle Plummer snapshot.
+
+FoF labels and groups are compared exactly; the unbinding stage must give exactly what
+unbind_batched gives on the gathered groups (whose every pass is checked against the FP64
+oracle in test_unbind_gpu.py); against the oracle's own FP64 iteration a handful of
+particles may differ.
+"""
 import numpy as np
 import pytest
 
 import oracle
 from oracle.unbind import unbind_halo
 from pyhalma_gb300 import synth
-from pyhalma_gb300.unbinding import G_MPC, UnbindOptions, find_haloes
+from pyhalma_gb300.unbinding import UnbindOptions, find_haloes, unbind_batched
 
 pytestmark = pytest.mark.gpu
 
@@ -23,12 +29,16 @@ def test_find_haloes_matches_oracle_composition(cuda):
     for h, g in enumerate(groups):
         g = np.array(g)
         assert np.array_equal(cat.members[cat.offsets[h]:cat.offsets[h + 1]], g)
-        b, it, e, phi = unbind_halo(s.x[g], s.y[g], s.z[g], s.vx[g], s.vy[g], s.vz[g], s.mass[g], eps=1e-4,
-                                    max_iter=50, return_energy=True)
-        diff = cat.bound[g].astype(bool) != b
-        if diff.any():
-            scale = np.abs(e) / (np.abs(e) + G_MPC * np.abs(phi))
-            assert np.all(scale[diff] <= 1e-5)
+        b, _ = unbind_halo(s.x[g], s.y[g], s.z[g], s.vx[g], s.vy[g], s.vz[g], s.mass[g], eps=1e-4, max_iter=50)
         expect[g] = b
+    mem = cat.members
+    bound, halo, _ = unbind_batched(cat.offsets, *(np.ascontiguousarray(a[mem]) for a in
+                                                   (s.x, s.y, s.z, s.vx, s.vy, s.vz, s.mass)),
+                                    UnbindOptions(eps=1e-4, max_iter=50))
+    assert np.array_equal(cat.bound[mem], bound)
+    assert np.array_equal(cat.haloes, halo)
+    outside = np.ones(s.n, dtype=bool)
+    outside[mem] = False
+    assert not cat.bound[outside].any()
     assert (cat.bound != expect).sum() <= 5
     assert cat.haloes.shape == (cat.n_haloes, 11)
