@@ -23,17 +23,30 @@ from . import MASK_SELF, potential_f64
 G_MPC = 4.3e-9
 
 
+def escape_pass(src_m, src_x, src_y, src_z, x, y, z, vx, vy, vz, v_bulk, eps=0.0, factor_v=1.0, G=G_MPC,
+                mask=None, ncores=None):
+    """The single-pass escape cut of halo_properties.py:320-361 in FP64: phi_i over the given
+    sources (no softening and the coordinate-inequality mask of particle_subroutines.f90:499-501
+    by default), E_i = 1/2 |v_i - v_bulk|^2 - G phi_i factor_v^2; returns (phi, E_kin, E)."""
+    from . import MASK_COORD
+    phi = potential_f64(src_m, src_x, src_y, src_z, x, y, z, eps2=float(eps) ** 2,
+                        mask=MASK_COORD if mask is None else mask, ncores=ncores)
+    ek = 0.5 * ((vx - v_bulk[0]) ** 2 + (vy - v_bulk[1]) ** 2 + (vz - v_bulk[2]) ** 2)
+    return phi, ek, ek - G * phi * factor_v * factor_v
+
+
 def unbind_pass(x, y, z, vx, vy, vz, m, eps=1e-4, factor_v=1.0, G=G_MPC, ncores=None):
     """One pass of the cut over the particles given (all treated as bound): returns
     (phi, kinetic energy, total energy) per particle in FP64; the particle stays iff
     energy <= 0 (halo_properties.py:359)."""
+    # the escape pass with the set as both sources and targets, the set's own bulk velocity
+    # and centre, softening and the self pair skipped
     M = m.sum()
-    vbx, vby, vbz = ((m * v).sum() / M for v in (vx, vy, vz))
+    vb = [(m * v).sum() / M for v in (vx, vy, vz)]
     cx, cy, cz = ((m * a).sum() / M for a in (x, y, z))
     px, py, pz = x - cx, y - cy, z - cz
-    phi = potential_f64(m, px, py, pz, px, py, pz, eps2=float(eps) ** 2, mask=MASK_SELF, ncores=ncores)
-    ek = 0.5 * ((vx - vbx) ** 2 + (vy - vby) ** 2 + (vz - vbz) ** 2)
-    return phi, ek, ek - G * phi * factor_v * factor_v
+    return escape_pass(m, px, py, pz, px, py, pz, vx, vy, vz, vb, eps=eps, factor_v=factor_v, G=G,
+                       mask=MASK_SELF, ncores=ncores)
 
 
 def unbind_halo(x, y, z, vx, vy, vz, m, eps=1e-4, factor_v=1.0, max_iter=20, G=G_MPC,

@@ -16,9 +16,11 @@ kernel over the halo's members:
 * ``half_mass_radius(cx, cy, cz, M, part_list, st_x, st_y, st_z, st_mass)`` :365-392
 * ``sigma_effective(part_list, R05, st_x, ..., vx, vy, vz)``           :607-625
 
-``escape_velocity_unbinding_particles`` is the single-pass stellar escape cut of
-halo_properties.py:282-361 with the gas and dark-matter particles supplied by the caller
-(the reference builds them from MASCLET AMR grids, which this package does not read).
+* ``escape_velocity_unbinding_fortran(rete, L, ncoarse, grid_data, gas_data, masclet_dm_data,
+  cx, cy, cz, vx, vy, vz, Rmax, part_list, st_x, ..., st_mass, factor_v, rho_B)`` :282-361,
+  the single-pass stellar escape cut with the AMR gas conversion and the potential on the GPU;
+  ``escape_velocity_unbinding_particles`` is the same cut with the gas and dark-matter
+  particles supplied by the caller.
 """
 from __future__ import annotations
 
@@ -112,13 +114,63 @@ def sigma_effective(part_list, R05, st_x, st_y, st_z, st_vx, st_vy, st_vz, cx, c
     return float(r[RED["sigma"]])
 
 
+def escape_velocity_unbinding_fortran(rete, L, ncoarse, grid_data, gas_data, masclet_dm_data, cx, cy, cz, vx, vy, vz,
+                                      Rmax, part_list, st_x, st_y, st_z, st_vx, st_vy, st_vz, st_mass, factor_v,
+                                      rho_B):
+    """halo_properties.py:282-361, same signature and result (bool per halo star, True =
+    bound), with the AMR conversion and the potential on the GPU.
+
+    Sources: the gas cells of the refined patches inside Rmax (``halo_gas.AMRgrid_to_particles``,
+    masses times rete**3), the halo's stars, and the DM particles inside Rmax (masses times
+    ``halo_gas.MASS_TO_SUN``, the reference's units.mass_to_sun), concatenated in that order
+    (:333-336); the float32 potential of the f2py kernel (halma_bf_potential_f32, bit-identical
+    to the Fortran loop in the default reference mode); E = 1/2 |v - v_bulk|^2 - G phi
+    factor_v^2 with G = 4.3e-9; bound = E <= 0.  The host arithmetic around the kernel is the
+    reference's, in its order and dtypes, so the result is the reference's bit for bit.  With
+    ``grid_data=None``, ``gas_data`` is taken as gas particles (x, y, z, vx, vy, vz, mass, temp)
+    already converted (comoving masses)."""
+    from .halo_gas import AMRgrid_to_particles, MASS_TO_SUN, brute_force_binding_energy_fortran
+    dm_x, dm_y, dm_z = (np.asarray(masclet_dm_data[k]) for k in range(3))
+    dm_mass = np.asarray(masclet_dm_data[3]) * MASS_TO_SUN
+    inside = np.sqrt((dm_x - cx) ** 2 + (dm_y - cy) ** 2 + (dm_z - cz) ** 2) < Rmax
+    dm_x, dm_y, dm_z, dm_mass = dm_x[inside], dm_y[inside], dm_z[inside], dm_mass[inside]
+    st_x_halo, st_y_halo, st_z_halo = st_x[part_list], st_y[part_list], st_z[part_list]
+    st_vx_halo, st_vy_halo, st_vz_halo = st_vx[part_list], st_vy[part_list], st_vz[part_list]
+    st_mass_halo = st_mass[part_list]
+    if grid_data is not None:
+        gas = AMRgrid_to_particles(L, ncoarse, grid_data, gas_data, Rmax, cx, cy, cz, rho_B)
+    else:
+        gas = tuple(np.asarray(a) for a in gas_data)
+    gas_x, gas_y, gas_z, gas_mass = gas[0], gas[1], gas[2], gas[6]
+    inside = np.sqrt((gas_x - cx) ** 2 + (gas_y - cy) ** 2 + (gas_z - cz) ** 2) < Rmax
+    gas_x, gas_y, gas_z, gas_mass = gas_x[inside], gas_y[inside], gas_z[inside], gas_mass[inside]
+    gas_mass *= rete ** 3
+    total_x = np.concatenate((gas_x, st_x_halo, dm_x))
+    total_y = np.concatenate((gas_y, st_y_halo, dm_y))
+    total_z = np.concatenate((gas_z, st_z_halo, dm_z))
+    total_mass = np.concatenate((gas_mass, st_mass_halo, dm_mass))
+    binding_energy = brute_force_binding_energy_fortran(total_mass, total_x, total_y, total_z,
+                                                        st_x_halo, st_y_halo, st_z_halo)
+    binding_energy = -binding_energy
+    G_const = 4.3 * 1e-3
+    G_const *= 1e-6
+    binding_energy *= G_const
+    binding_energy *= factor_v ** 2
+    st_v2 = 0.5 * ((st_vx_halo - vx) ** 2 + (st_vy_halo - vy) ** 2 + (st_vz_halo - vz) ** 2)
+    total_energy = st_v2 + binding_energy
+    return total_energy <= 0.
+
+
 def escape_velocity_unbinding_particles(cx, cy, cz, vx, vy, vz, Rmax, part_list, st_x, st_y, st_z, st_vx, st_vy,
                                         st_vz, st_mass, factor_v, gas_x=(), gas_y=(), gas_z=(), gas_mass=(),
                                         dm_x=(), dm_y=(), dm_z=(), dm_mass=()):
-    """Single-pass escape cut (halo_properties.py:320-361): sources are the gas cells, the
-    halo's stars and the DM particles inside Rmax (concatenated in that order, :333-336);
-    E = 1/2 |v - v_bulk|^2 - G phi factor_v^2; returns ``E <= 0`` per halo star.  The
-    selection of gas and DM inside Rmax is host bookkeeping; the potential runs on the GPU."""
+    """Single-pass escape cut (halo_properties.py:320-361) on gas and DM given as particles:
+    sources are the gas cells, the halo's stars and the DM particles inside Rmax
+    (concatenated in that order, :333-336); E = 1/2 |v - v_bulk|^2 - G phi factor_v^2;
+    returns ``E <= 0`` per halo star.  Unlike escape_velocity_unbinding_fortran, the masses
+    are used as given: the caller applies the reference's two unit conversions, DM masses
+    times units.mass_to_sun (:292) and gas masses times rete**3 (comoving to physical, :326).
+    The selection of gas and DM inside Rmax is host bookkeeping; the potential runs on the GPU."""
     gx, gy, gz, gm = (np.asarray(a, dtype=np.float64) for a in (gas_x, gas_y, gas_z, gas_mass))
     dmx, dmy, dmz, dmm = (np.asarray(a, dtype=np.float64) for a in (dm_x, dm_y, dm_z, dm_mass))
     if dmx.size:

@@ -1,11 +1,19 @@
-"""Multi-rank sharding of the unbinding work (one process per GPU).
+"""Multi-rank sharding of the halo-finding path (one process per GPU).
 
-Haloes are independent, so the data path needs no collective: haloes are dealt to ranks by
-longest-processing-time on their cost N_h^2 (largest first, each to the least-loaded rank),
-every rank unbinds its own haloes on its own GPU, and the per-halo results are gathered on
-the host (``torch.distributed.all_gather_object``) only to assemble the catalogue.  FoF is
-not split: a snapshot is processed by one rank, and ranks take different snapshots (the
-driver's loop over snapshots, pyHALMA.py:455).
+Unbinding: haloes are independent, so the data path needs no collective: haloes are dealt to
+ranks by longest-processing-time on their cost N_h^2 (largest first, each to the least-loaded
+rank), every rank unbinds its own haloes on its own GPU, and the per-halo results are gathered
+on the host (``torch.distributed.all_gather_object``) only to assemble the catalogue.
+
+FoF (``fof_slabs``): the box is cut into x-slabs at least one linking length wide, one per
+rank.  Each rank receives from its two neighbours their particles within one linking length
+of the shared face (ghosts), runs the FoF of its own particles plus the ghosts on its own GPU,
+and reports, for every particle that lives on two ranks, the smallest global id of the local
+component it fell in.  One all-gather of those (id, component minimum) pairs, a union of them
+and a relabel to the smallest global id give every rank the exact global partition for its
+own particles.  The reference's decomposed FoF (fof.py:95-176) instead cuts the box into
+sub-cubes with a fixed 0.1 Mpc buffer and deduplicates groups by centre of mass, which can
+split groups longer than the buffer; this one is exact for any group size.
 """
 from __future__ import annotations
 
@@ -73,3 +81,110 @@ def unbind_sharded(offsets, x, y, z, vx, vy, vz, m, options=None, compute=None, 
     if full_table is None:
         full_table = np.zeros((nh, 11))
     return full_bound, full_table
+
+
+# ---------------------------------------------------------------------------------------
+# FoF over x-slabs
+# ---------------------------------------------------------------------------------------
+def slab_edges(xmin, xmax, world, linking_length):
+    """x edges of the slabs (len = slabs + 1): `world` slabs of equal width, fewer when the
+    box is narrower than world linking lengths (every slab is at least one linking length
+    wide, so a ghost layer only ever comes from the two neighbouring slabs).  The last edge is
+    nudged above xmax so that every particle falls in [edges[r], edges[r + 1])."""
+    width = float(xmax) - float(xmin)
+    k = int(max(1, min(world, width // max(float(linking_length), 1e-300)))) if width > 0 else 1
+    edges = float(xmin) + width * np.arange(k + 1) / k
+    edges[-1] = np.nextafter(float(xmax), np.inf)
+    return edges
+
+
+def slab_of(x, edges):
+    """Slab index of every particle."""
+    return np.clip(np.searchsorted(edges, np.asarray(x), side="right") - 1, 0, len(edges) - 2)
+
+
+def _merge_pairs(pairs):
+    """Union of (id, id) pairs; returns (ids, root) with root[k] the smallest id connected to
+    ids[k]."""
+    if len(pairs) == 0:
+        return np.zeros(0, dtype=np.int64), np.zeros(0, dtype=np.int64)
+    from scipy.sparse import coo_matrix
+    from scipy.sparse.csgraph import connected_components
+    pairs = np.asarray(pairs, dtype=np.int64).reshape(-1, 2)
+    ids, inv = np.unique(pairs, return_inverse=True)
+    inv = inv.reshape(-1, 2)
+    k = len(ids)
+    g = coo_matrix((np.ones(len(inv)), (inv[:, 0], inv[:, 1])), shape=(k, k))
+    _, comp = connected_components(g, directed=False)
+    cmin = np.full(comp.max() + 1, np.iinfo(np.int64).max, dtype=np.int64)
+    np.minimum.at(cmin, comp, ids)
+    return ids, cmin[comp]
+
+
+def fof_slabs(x, y, z, gid, linking_length, edges, local_fof=None, group=None):
+    """FoF of the rank's slab particles (x in [edges[rank], edges[rank + 1])), exact across
+    slab faces.  ``gid`` are the particles' global ids (their index in the whole snapshot).
+    Returns int64 labels for the rank's particles: the smallest global id of the FoF
+    component (all ranks' particles), -1 for particles without a friend — the labels of
+    ``fof.fof_labels`` on the whole snapshot, restricted to this rank.
+
+    ``local_fof(x, y, z, ll)`` is the per-rank FoF (default: the GPU's ``fof.fof_labels``);
+    with one rank or one slab no exchange happens."""
+    import torch.distributed as dist
+    if local_fof is None:
+        from .fof import fof_labels as local_fof
+    world = dist.get_world_size(group) if dist.is_initialized() else 1
+    rank = dist.get_rank(group) if dist.is_initialized() else 0
+    x, y, z = (np.ascontiguousarray(a, dtype=np.float64) for a in (x, y, z))
+    gid = np.asarray(gid, dtype=np.int64)
+    n = len(x)
+    ll = float(linking_length)
+    nslab = len(edges) - 1
+    if world == 1 or nslab == 1:
+        lab = np.asarray(local_fof(x, y, z, ll)).astype(np.int64)
+        return np.where(lab >= 0, gid[np.maximum(lab, 0)], -1)
+    if rank >= nslab:
+        lo_face, hi_face = np.inf, -np.inf   # a rank without a slab holds no particles
+    else:
+        lo_face, hi_face = edges[rank], edges[rank + 1]
+    # ghosts: own particles within ll of a face (plus a hair against the rounding of the
+    # face +- ll), for the neighbour across it; sending a few too many changes nothing
+    pad = 1e-9 * (ll + max(abs(lo_face), abs(hi_face))) if rank < nslab else 0.0
+    down = np.nonzero(x <= lo_face + ll + pad)[0] if rank > 0 else np.zeros(0, dtype=np.int64)
+    up = np.nonzero(x >= hi_face - ll - pad)[0] if rank + 1 < nslab else np.zeros(0, dtype=np.int64)
+    pack = lambda idx: (x[idx], y[idx], z[idx], gid[idx])
+    everyone = [None] * world
+    dist.all_gather_object(everyone, (pack(down), pack(up)), group=group)
+    recv = []
+    if rank > 0:
+        recv.append(everyone[rank - 1][1])          # the lower neighbour's upper ghosts
+    if rank + 1 < world:
+        recv.append(everyone[rank + 1][0])          # the upper neighbour's lower ghosts
+    gx = np.concatenate([x] + [r[0] for r in recv])
+    gy = np.concatenate([y] + [r[1] for r in recv])
+    gz = np.concatenate([z] + [r[2] for r in recv])
+    gg = np.concatenate([gid] + [r[3] for r in recv])
+    lab = np.asarray(local_fof(gx, gy, gz, ll)).astype(np.int64)
+    # smallest global id of every local component
+    member = lab >= 0
+    cmin = np.full(len(gx), np.iinfo(np.int64).max, dtype=np.int64)
+    np.minimum.at(cmin, lab[member], gg[member])
+    comp_min = np.where(member, cmin[np.maximum(lab, 0)], -1)
+    # particles held by two ranks (ghosts received and own particles sent): (id, component min)
+    shared = np.zeros(len(gx), dtype=bool)
+    shared[n:] = True
+    shared[down] = True
+    shared[up] = True
+    shared &= member
+    pairs = np.stack([gg[shared], comp_min[shared]], 1)
+    allpairs = [None] * world
+    dist.all_gather_object(allpairs, pairs, group=group)
+    ids, root = _merge_pairs(np.concatenate([p for p in allpairs if len(p)]) if any(len(p) for p in allpairs)
+                             else np.zeros((0, 2), dtype=np.int64))
+    out = comp_min[:n].copy()
+    if len(ids):
+        pos = np.searchsorted(ids, out)
+        hit = (out >= 0) & (pos < len(ids))
+        hit[hit] = ids[pos[hit]] == out[hit]
+        out[hit] = root[pos[hit]]
+    return out

@@ -399,3 +399,67 @@ def lattice_points(n_side, spacing, *, origin=(0.0, 0.0, 0.0), jitter_ulps=0, se
         d = rng.integers(-1, 2, pts.shape)
         pts = np.where(d > 0, np.nextafter(pts, np.inf), np.where(d < 0, np.nextafter(pts, -np.inf), pts))
     return pts
+
+
+@dataclass
+class AMRGrid:
+    """A MASCLET-like AMR gas grid in the reference's tuple layout: ``grid_data[2]`` nl,
+    ``[5]`` npatch (patches per level, npatch[0] = 0), ``[6:9]`` patchnx/ny/nz, ``[12:15]``
+    patchrx/ry/rz (the centre of each patch's first cell of the parent level, Mpc);
+    ``gas_data`` = [delta, vx, vy, vz, temp, cr0amr, solapst], each a list of per-patch 3-D
+    arrays indexed [ix, iy, iz] (velocities in units of c).  Patch 0 is the base grid; the
+    conversion never reads its cells, so it is stored as a single cell."""
+    grid_data: list
+    gas_data: list
+    L: float
+    ncoarse: int
+    rho_B: float
+    centre: np.ndarray
+
+
+def amr_grid(*, seed=0, L=40.0, ncoarse=128, levels=(1, 2, 3, 4, 5, 6, 7), per_level=2, n_lo=6, n_hi=14,
+             centre_mpc=(1.3, -0.7, 2.2), rho_B=5e10, sigma_v_kms=120.0):
+    """Synthetic refined patches around a halo centre: per level `per_level` patches of
+    n_lo..n_hi cells a side placed over the centre with random offsets, lognormal overdensity
+    rising towards the centre, Gaussian velocities, about 25 % refined / 15 % overlapped
+    cells (cr0amr / solapst false).  Cell values are float32 numbers (MASCLET writes float32
+    fields) held in float64 arrays."""
+    rng = np.random.default_rng(seed)
+    c = np.asarray(centre_mpc, dtype=np.float64)
+    cell0 = L / ncoarse
+    nx, ny, nz, rx, ry, rz, lev = [1], [1], [1], [0.0], [0.0], [0.0], [0]
+    fields = [[np.zeros((1, 1, 1))] for _ in range(5)] + [[np.zeros((1, 1, 1), dtype=bool)] for _ in range(2)]
+    npatch = [0] * (max(levels) + 1)
+    for lvl in levels:
+        res = cell0 / 2 ** lvl
+        for _ in range(per_level):
+            n = rng.integers(n_lo, n_hi + 1, 3)
+            off = (n / 2.0 + rng.uniform(-0.3, 0.3, 3) * n) * res
+            r0 = c - off + res / 2.0          # centre of the first cell of the parent level
+            nx.append(int(n[0]))
+            ny.append(int(n[1]))
+            nz.append(int(n[2]))
+            rx.append(float(r0[0]))
+            ry.append(float(r0[1]))
+            rz.append(float(r0[2]))
+            lev.append(lvl)
+            npatch[lvl] += 1
+            ix, iy, iz = np.meshgrid(np.arange(n[0]), np.arange(n[1]), np.arange(n[2]), indexing="ij")
+            px = r0[0] - res / 2 + ix * res - c[0]
+            py = r0[1] - res / 2 + iy * res - c[1]
+            pz = r0[2] - res / 2 + iz * res - c[2]
+            rr = np.sqrt(px * px + py * py + pz * pz) * 1e3   # kpc
+            shape = tuple(int(v) for v in n)
+            f32 = lambda a: a.astype(np.float32).astype(np.float64)
+            fields[0].append(f32(np.exp(rng.normal(np.log(2e3 / (1.0 + rr / 5.0) ** 2), 0.8, shape))))
+            for k in (1, 2, 3):
+                fields[k].append(f32(rng.normal(0.0, sigma_v_kms / 3e5, shape)))
+            fields[4].append(f32(np.exp(rng.normal(np.log(3e4), 1.0, shape))))
+            fields[5].append(rng.random(shape) > 0.25)
+            fields[6].append(rng.random(shape) > 0.15)
+    grid = [None] * 15
+    grid[2] = max(levels)
+    grid[5] = np.array(npatch, dtype=np.int64)
+    grid[6], grid[7], grid[8] = (np.array(a, dtype=np.int64) for a in (nx, ny, nz))
+    grid[12], grid[13], grid[14] = (np.array(a, dtype=np.float64) for a in (rx, ry, rz))
+    return AMRGrid(grid, fields, float(L), int(ncoarse), float(rho_B), c)

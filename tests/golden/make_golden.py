@@ -1,14 +1,19 @@
 """Generate golden fixtures by running pyHALMA's own Python code in this container.
 
-Run from the repository root:  python tests/golden/make_golden.py [--reference DIR]
+Run from the repository root:
+    python tests/golden/make_golden.py --reference DIR      (or PYHALMA_REFERENCE=DIR)
 
-The reference tree is read in place (default /root/reference) and never modified.  Modules
+DIR is a checkout of pyHALMA; it is read in place and never modified.  Modules
 that are absent here are replaced by stubs in ``sys.modules`` before the import:
 
 * ``numba``: ``njit`` returns the function unchanged, ``prange`` is ``range`` and
   ``get_num_threads`` returns 1, so the numba kernels run as plain Python;
-* ``masclet_framework``, ``matplotlib``: empty namespaces (only ``units.mass_to_sun`` is
-  read on the paths used here);
+* ``masclet_framework``, ``matplotlib``: empty namespaces except ``units.mass_to_sun`` (1.0:
+  masses are generated in Msun) and two third-party helpers of ``tools`` that the AMR
+  conversion calls (halo_gas.py:90-91), restated: ``create_vector_levels`` (patch 0 is the
+  base grid, then npatch[1] patches of level 1, ...) and ``which_patches_inside_box`` (the
+  base grid plus every patch whose extent [r - res, r - res + n*res] per axis overlaps the
+  box; the conversion re-tests every cell, so any superset gives the same particles);
 * ``fortran_modules.particle``: ``particle.brute_force_binding_energy`` maps onto the
   oracle's float32 restatement of particle_subroutines.f90:466-514 (gfortran is absent).
 
@@ -29,6 +34,10 @@ Fixtures written to tests/golden/ (all seeds fixed):
   conversion replaced by a pass-through of gas particles (inputs and the 17 outputs stored);
 * psc.npz         — the driver's phase-space cleaning block (pyHALMA.py:774-877) exec'd from
   the reference's own source on FoF groups of contaminated Plummer snapshots;
+* amr.npz         — reference ``halo_gas.AMRgrid_to_particles`` (with its numba kernel
+  patch_to_particles) on synthetic refined patches, several boxes;
+* escape.npz      — reference ``halo_properties.escape_velocity_unbinding_fortran`` with the
+  same AMR grids, DM particles and a stellar halo (two factor_v, two Rmax);
 * properties.npz  — the reference's O(N) per-halo property functions (half-mass radii, bulk
   velocity, angular momentum, Tully-Fisher velocity, kappa_co, shape, sigma_effective,
   sigma projections) called as the driver's property loop calls them; the f2py routines
@@ -74,6 +83,26 @@ def install_stubs():
         setattr(mf, sub, m)
         sys.modules["masclet_framework." + sub] = m
     mf.units.mass_to_sun = 1.0
+
+    def create_vector_levels(npatch):
+        out = [0]
+        for lev, cnt in enumerate(list(npatch)[1:], start=1):
+            out += [lev] * int(cnt)
+        return np.array(out)
+
+    def which_patches_inside_box(box, patchnx, patchny, patchnz, patchrx, patchry, patchrz, npatch, size, nmax):
+        levels = create_vector_levels(npatch)
+        keep = [0]
+        for p in range(1, len(patchnx)):
+            res = size / nmax / 2 ** levels[p]
+            lo = [patchrx[p] - res, patchry[p] - res, patchrz[p] - res]
+            hi = [lo[0] + patchnx[p] * res, lo[1] + patchny[p] * res, lo[2] + patchnz[p] * res]
+            if all(box[2 * q] < hi[q] and box[2 * q + 1] > lo[q] for q in range(3)):
+                keep.append(p)
+        return keep
+
+    mf.tools.create_vector_levels = create_vector_levels
+    mf.tools.which_patches_inside_box = which_patches_inside_box
     sys.modules["masclet_framework"] = mf
 
     mpl = types.ModuleType("matplotlib")
@@ -356,6 +385,81 @@ def ball_cases(hg):
     np.savez_compressed(os.path.join(HERE, "ball.npz"), ncase=np.int64(2), rete=np.float64(0.5), **out)
 
 
+def _store_grid(out, key, g):
+    """A synthetic AMR grid as flat arrays: patch table and every field's cells concatenated
+    patch by patch, each patch x-major (tests/test_amr_escape.py rebuilds the lists)."""
+    gd = g.grid_data
+    out[key + "_npatch"] = np.asarray(gd[5])
+    out[key + "_patchn"] = np.stack([gd[6], gd[7], gd[8]], 1)
+    out[key + "_patchr"] = np.stack([gd[12], gd[13], gd[14]], 1)
+    for j, f in enumerate(g.gas_data):   # float32 values (exact) and flags
+        flat = np.concatenate([np.ravel(a) for a in f])
+        out[key + f"_f{j}"] = flat.astype(np.float32) if j < 5 else flat.astype(bool)
+    out[key + "_scalars"] = np.array([g.L, g.ncoarse, g.rho_B], dtype=np.float64)
+    out[key + "_centre"] = g.centre
+
+
+def amr_cases(hg):
+    """The reference's AMRgrid_to_particles on two synthetic grids, three boxes each."""
+    out = {}
+    for k in range(2):
+        g = synth.amr_grid(seed=70 + k, centre_mpc=(1.3 + k, -0.7, 2.2 - k))
+        _store_grid(out, f"g{k}", g)
+        for j, (R, shift) in enumerate(((0.01, 0.0), (0.03, 0.004), (0.2, -0.01))):
+            c = g.centre + shift
+            res = hg.AMRgrid_to_particles(g.L, g.ncoarse, g.grid_data, g.gas_data, R, c[0], c[1], c[2], g.rho_B)
+            for q, a in enumerate(res):
+                out[f"g{k}b{j}_out{q}"] = np.asarray(a, dtype=np.float64)
+            out[f"g{k}b{j}_box"] = np.array([R, *c], dtype=np.float64)
+            print(f"  AMR grid {k} box {j}: {len(res[0])} gas particles")
+    np.savez_compressed(os.path.join(HERE, "amr.npz"), ngrid=np.int64(2), nbox=np.int64(3), **out)
+
+
+def escape_cases(hp):
+    """The reference's escape_velocity_unbinding_fortran (halo_properties.py:282-361): gas from
+    the AMR grids of amr.npz, DM particles, and a Plummer stellar halo with a hot tail, two
+    factor_v and two Rmax per grid."""
+    out = {}
+    for k in range(2):
+        g = synth.amr_grid(seed=70 + k, centre_mpc=(1.3 + k, -0.7, 2.2 - k))
+        rng = np.random.default_rng(90 + k)
+        c = g.centre
+        nst, ndm, nfield = 3000 + 1000 * k, 8000, 1500
+        a = 0.004
+        u = rng.uniform(1e-6, 0.999, nst)
+        r = a / np.sqrt(u ** (-2.0 / 3.0) - 1.0)
+        d = rng.normal(size=(nst, 3))
+        d /= np.linalg.norm(d, axis=1)[:, None]
+        st = c + r[:, None] * d
+        bulk = rng.normal(0, 150, 3)
+        sig = np.where(rng.random(nst) < 0.2, 400.0, 60.0)
+        stv = bulk + rng.normal(size=(nst, 3)) * sig[:, None]
+        field = c + rng.uniform(-0.2, 0.2, (nfield, 3))
+        fv = rng.normal(0, 200, (nfield, 3))
+        allp = np.concatenate([field, st])
+        allv = np.concatenate([fv, stv])
+        st_x, st_y, st_z = (np.ascontiguousarray(allp[:, q]) for q in range(3))
+        st_vx, st_vy, st_vz = (np.ascontiguousarray(allv[:, q]) for q in range(3))
+        st_mass = rng.uniform(5e5, 2e6, nfield + nst)
+        part_list = np.arange(nfield, nfield + nst)
+        dm = c + rng.normal(0, 0.015, (ndm, 3))
+        dm_data = [np.ascontiguousarray(dm[:, q]) for q in range(3)] + [rng.uniform(5e6, 2e7, ndm)]
+        for q, arr in enumerate(dm_data):
+            out[f"g{k}_dm{q}"] = arr
+        for name, arr in (("st_x", st_x), ("st_y", st_y), ("st_z", st_z), ("st_vx", st_vx), ("st_vy", st_vy),
+                          ("st_vz", st_vz), ("st_mass", st_mass), ("part_list", part_list)):
+            out[f"g{k}_{name}"] = arr
+        for j, (Rmax, fv_) in enumerate(((0.02, 1.0), (0.05, 1.3))):
+            bound = hp.escape_velocity_unbinding_fortran(0.5, g.L, g.ncoarse, g.grid_data, g.gas_data, dm_data,
+                                                         c[0], c[1], c[2], bulk[0], bulk[1], bulk[2], Rmax,
+                                                         part_list, st_x, st_y, st_z, st_vx, st_vy, st_vz,
+                                                         st_mass, fv_, g.rho_B)
+            out[f"g{k}e{j}_bound"] = np.asarray(bound)
+            out[f"g{k}e{j}_params"] = np.array([0.5, Rmax, fv_, *bulk], dtype=np.float64)
+            print(f"  escape grid {k} case {j}: {int(np.sum(bound))} of {len(bound)} bound")
+    np.savez_compressed(os.path.join(HERE, "escape.npz"), ngrid=np.int64(2), ncase=np.int64(2), **out)
+
+
 def psc_cases(fof, hp, refdir):
     """The driver's phase-space cleaning block (pyHALMA.py:774-877: calc_cell / clean_cell per
     group, the reset for small groups, the MINP cut and the sort by size) run as written on the
@@ -439,12 +543,15 @@ def property_cases(hp):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--reference", default=os.environ.get("PYHALMA_REFERENCE"),
+                    help="pyHALMA checkout (default: $PYHALMA_REFERENCE)")
     ap.add_argument("--only", default="")
     args = ap.parse_args()
+    if not args.reference:
+        ap.error("give the pyHALMA checkout with --reference DIR or PYHALMA_REFERENCE")
     fof, hg, hp = import_reference(args.reference)
     todo = args.only.split(",") if args.only else ["fof", "config1", "pred", "props", "rps", "sub", "ball",
-                                                    "psc", "prop"]
+                                                    "psc", "prop", "amr", "escape"]
     if "fof" in todo:
         fof_cases(fof)
     if "config1" in todo:
@@ -463,6 +570,10 @@ def main():
         psc_cases(fof, hp, args.reference)
     if "prop" in todo:
         property_cases(hp)
+    if "amr" in todo:
+        amr_cases(hg)
+    if "escape" in todo:
+        escape_cases(hp)
 
 
 if __name__ == "__main__":

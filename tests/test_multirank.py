@@ -72,3 +72,77 @@ def test_two_rank_gloo_gather_equals_single_process():
     for rank, b, t in res:
         assert np.array_equal(b, b1), rank
         assert np.array_equal(t, t1), rank
+
+
+# ---------------------------------------------------------------------------------------
+# FoF over x-slabs: two gloo ranks, the C oracle as each rank's local FoF
+# ---------------------------------------------------------------------------------------
+def _slab_snapshot():
+    """Plummer clumps on both sides of the slab face, one clump sitting on it, and a chain of
+    particles 0.9 LL apart crossing the face (a bridge that only the exchange can join)."""
+    s = synth.plummer_snapshot(30_000, 12, seed=9, box_mpc=0.4, bg_frac=0.2)
+    x0 = 0.5 * (s.x.min() + s.x.max())
+    t = np.arange(-60, 61, dtype=np.float64)
+    cx = x0 + 0.0009 * t
+    cy = np.full(t.shape, 0.07) + 1e-6 * np.sin(t)
+    cz = np.full(t.shape, -0.03)
+    rng = np.random.default_rng(2)
+    blob = rng.normal(0, 0.0007, (400, 3)) + np.array([x0, -0.05, 0.02])
+    x = np.concatenate([s.x, cx, blob[:, 0]])
+    y = np.concatenate([s.y, cy, blob[:, 1]])
+    z = np.concatenate([s.z, cz, blob[:, 2]])
+    return x, y, z
+
+
+def _slab_worker(rank, world, port, q):
+    import torch.distributed as dist
+    import oracle
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    x, y, z = _slab_snapshot()
+    ll = 0.0015
+    edges = shard.slab_edges(x.min(), x.max(), world, ll)
+    mine = np.nonzero(shard.slab_of(x, edges) == rank)[0]
+    lab = shard.fof_slabs(x[mine], y[mine], z[mine], mine, ll, edges, local_fof=oracle.fof_labels)
+    q.put((rank, mine, lab))
+    dist.destroy_process_group()
+
+
+def test_slab_fof_two_ranks_equals_single_process():
+    import multiprocessing as mp
+    import oracle
+    oracle.build()
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_slab_worker, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    res = [q.get(timeout=240) for _ in procs]
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    x, y, z = _slab_snapshot()
+    ref = oracle.fof_labels(x, y, z, 0.0015)
+    got = np.full(len(x), -2, dtype=np.int64)
+    for rank, mine, lab in res:
+        got[mine] = lab
+    assert (got != -2).all()
+    assert np.array_equal(got, ref)
+    # the chain crosses the face: one group with members on both ranks
+    edges = shard.slab_edges(x.min(), x.max(), 2, 0.0015)
+    side = shard.slab_of(x, edges)
+    chain = np.arange(len(x) - 400 - 121, len(x) - 400)
+    assert len(set(got[chain])) == 1 and len(set(side[chain])) == 2
+
+
+def test_slab_edges_and_single_rank():
+    import oracle
+    e = shard.slab_edges(0.0, 1.0, 4, 0.3)
+    assert len(e) == 4 and e[0] == 0.0 and e[-1] > 1.0          # only 3 slabs fit 0.3 wide
+    assert np.all(np.diff(e) >= 0.3)
+    x, y, z = _slab_snapshot()
+    lab = shard.fof_slabs(x, y, z, np.arange(len(x)), 0.0015, shard.slab_edges(x.min(), x.max(), 1, 0.0015),
+                          local_fof=oracle.fof_labels)
+    assert np.array_equal(lab, oracle.fof_labels(x, y, z, 0.0015))

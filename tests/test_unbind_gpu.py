@@ -3,8 +3,8 @@
 The iterative cut repeats the reference's single pass (halo_properties.py:282-361), so it
 is checked pass by pass: the GPU's bound set after k-1 passes is the input of an FP64 oracle
 pass, and the GPU's pass k must agree with it.  Tolerances written here:
-* potential: |phi_gpu / phi_fp64 - 1| <= RTOL_PHI = 1e-6 for every particle the pass
-  evaluates (FP32-compensated path; the north-star bound);
+* potential: |phi_gpu / phi_fp64 - 1| <= RTOL_PHI = 1e-6 for every particle a pass
+  evaluates and keeps (the potential is returned for those; FP32-compensated path);
 * membership: the GPU's pass may keep or remove a particle against the FP64 pass only if
   that particle's FP64 energy lies within BAND = 2e-6 * (E_kin + G*phi) of zero (the 1e-6
   potential bound with a factor-2 margin);
@@ -70,10 +70,12 @@ def _check_pass_contract(cat, rtol_phi, band, **opt):
             sel = lambda a: a[sl][s]
             p_ref, ek, e = unbind_pass(sel(cat.x), sel(cat.y), sel(cat.z), sel(cat.vx), sel(cat.vy), sel(cat.vz),
                                        sel(cat.mass), eps=EPS)
-            if halo[h, 8] >= k:   # the halo was still active in pass k: its potential is this pass's
-                p = phi[sl][s]
-                assert np.max(np.abs(p / p_ref - 1.0)) <= rtol_phi, (k, h)
             keep_gpu, keep_ref = bound[sl][s], e <= 0.0
+            if halo[h, 8] >= k and keep_gpu.any():
+                # the halo ran pass k: the potential returned for the particles it kept is the
+                # one that pass evaluated (the removed ones get none)
+                p = phi[sl][s][keep_gpu]
+                assert np.max(np.abs(p / p_ref[keep_gpu] - 1.0)) <= rtol_phi, (k, h)
             diff = keep_gpu != keep_ref
             if diff.any():
                 scale = np.abs(e) / (ek + G_MPC * np.abs(p_ref))
