@@ -436,44 +436,47 @@ struct __align__(16) CellSlot {
 __device__ __forceinline__ uint64_t slot_of(uint64_t key, uint64_t hmask) { return mix64(key) & hmask; }
 
 // Hash capacity from the number of occupied cells: the smallest power of two >= 2 x cells, at
-// least 1024 slots and at most the cap_max allocated; kept on the device as a mask.
+// least 1024 slots and at most the cap_max allocated; kept on the device as a mask.  The Bloom
+// filter of occupied cells gets the smallest power of two >= 8 bits per cell (at most bcap_max
+// bits): one bit per cell, so a lookup of an empty neighbour cell is a false positive with
+// probability 1 - e^(-1/8) = 12 %, and at 8 bits per cell the filter of a 5e7-cell snapshot
+// (64 MB) stays in L2.
 __global__ void hash_size_kernel(int n, const int *__restrict__ head, const int *__restrict__ cellpos,
-                                 unsigned long long cap_max, unsigned long long *__restrict__ hmask) {
+                                 unsigned long long cap_max, unsigned long long bcap_max,
+                                 unsigned long long *__restrict__ hmask, unsigned long long *__restrict__ bmask) {
     const unsigned long long nc = (unsigned long long)(cellpos[n - 1] + head[n - 1]);
     unsigned long long cap = 1024;
     while (cap < 2 * nc && cap < cap_max) cap <<= 1;
     *hmask = (cap < cap_max ? cap : cap_max) - 1;
+    unsigned long long bc = 1024;
+    while (bc < 8 * nc && bc < bcap_max) bc <<= 1;
+    *bmask = (bc < bcap_max ? bc : bcap_max) - 1;
 }
 
-__global__ void hash_clear_kernel(const unsigned long long *__restrict__ hmask_p, CellSlot *__restrict__ slots) {
-    const unsigned long long cap = *hmask_p + 1;
-    for (unsigned long long s = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; s < cap;
-         s += (unsigned long long)gridDim.x * blockDim.x)
-        reinterpret_cast<ulonglong2 *>(slots)[s] = make_ulonglong2(kEmptyKey, 0ull);
+__global__ void hash_clear_kernel(const unsigned long long *__restrict__ hmask_p, CellSlot *__restrict__ slots,
+                                  const unsigned long long *__restrict__ bmask_p, unsigned *__restrict__ bloom) {
+    const unsigned long long cap = *hmask_p + 1, words = (*bmask_p + 1) >> 5;
+    for (unsigned long long s = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; s < cap || s < words;
+         s += (unsigned long long)gridDim.x * blockDim.x) {
+        if (s < cap) reinterpret_cast<ulonglong2 *>(slots)[s] = make_ulonglong2(kEmptyKey, 0ull);
+        if (s < words) bloom[s] = 0u;
+    }
 }
 
-__global__ void cells_kernel(int n, int sb, const uint64_t *__restrict__ keys, const int *__restrict__ head,
-                             const int *__restrict__ cellpos, int *__restrict__ cell_start,
-                             uint64_t *__restrict__ cell_key, CellSlot *__restrict__ slots,
-                             int *__restrict__ cell_slot, const unsigned long long *__restrict__ hmask_p,
-                             int *__restrict__ ncell) {
-    const uint64_t hmask = *hmask_p;
+__device__ __forceinline__ uint64_t bloom_bit(uint64_t key, uint64_t bmask) {
+    return mix64(key ^ 0x9e3779b97f4a7c15ull) & bmask;
+}
+
+// Start and key of every occupied cell (cells in sorted order), from the exclusive scan of
+// the run heads.
+__global__ void cell_table_kernel(int n, int sb, const uint64_t *__restrict__ keys, const int *__restrict__ head,
+                                  const int *__restrict__ cellpos, int *__restrict__ cell_start,
+                                  uint64_t *__restrict__ cell_key, int *__restrict__ ncell) {
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
         if (head[k]) {
             const int c = cellpos[k];
-            const uint64_t key = keys[k] >> sb;
             cell_start[c] = k;
-            cell_key[c] = key;
-            uint64_t h = slot_of(key, hmask);
-            for (uint64_t probe = 0; probe <= hmask; ++probe) {
-                const unsigned long long prev =
-                    atomicCAS(&slots[h].key, (unsigned long long)kEmptyKey, (unsigned long long)key);
-                if (prev == kEmptyKey || prev == key) {
-                    cell_slot[c] = (int)h;
-                    break;
-                }
-                h = (h + 1) & hmask;
-            }
+            cell_key[c] = keys[k] >> sb;
         }
         if (k == n - 1) {
             const int m = cellpos[k] + head[k];
@@ -483,24 +486,42 @@ __global__ void cells_kernel(int n, int sb, const uint64_t *__restrict__ keys, c
     }
 }
 
-// count carries the cell's "one component" flag (conn) in bit 31.
-__global__ void slot_fill_kernel(const int *__restrict__ ncell_p, const int *__restrict__ cell_start,
-                                 const int *__restrict__ cell_slot, const unsigned char *__restrict__ conn,
-                                 CellSlot *__restrict__ slots) {
+// Hash insert of every cell with its first position, its count and its one-component flag
+// (bit 31 of the count) in one slot, and the cell's bit in the Bloom filter.
+__global__ void cell_insert_kernel(const int *__restrict__ ncell_p, const int *__restrict__ cell_start,
+                                   const uint64_t *__restrict__ cell_key, const unsigned char *__restrict__ conn,
+                                   CellSlot *__restrict__ slots, const unsigned long long *__restrict__ hmask_p,
+                                   unsigned *__restrict__ bloom, const unsigned long long *__restrict__ bmask_p) {
     const int nc = *ncell_p;
+    const uint64_t hmask = *hmask_p, bmask = *bmask_p;
     for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x) {
-        CellSlot &sl = slots[cell_slot[c]];
-        sl.start = cell_start[c];
-        sl.count = (cell_start[c + 1] - cell_start[c]) | (conn[c] ? (int)0x80000000u : 0);
+        const uint64_t key = cell_key[c];
+        const int cs = cell_start[c];
+        const int count = (cell_start[c + 1] - cs) | (conn[c] ? (int)0x80000000u : 0);
+        uint64_t h = slot_of(key, hmask);
+        for (uint64_t probe = 0; probe <= hmask; ++probe) {
+            const unsigned long long prev =
+                atomicCAS(&slots[h].key, (unsigned long long)kEmptyKey, (unsigned long long)key);
+            if (prev == kEmptyKey) {
+                slots[h].start = cs;
+                slots[h].count = count;
+                break;
+            }
+            h = (h + 1) & hmask;
+        }
+        const uint64_t b = bloom_bit(key, bmask);
+        atomicOr(bloom + (b >> 5), 1u << (b & 31));
     }
 }
 
-// Marks the first particle of every 32-particle chunk of every cell.
+// Marks the first particle of every 32-particle chunk of every cell that has linking work
+// (bit 13 of its neighbour mask, see nbmask_kernel).
 __global__ void itemflag_kernel(int n, const int *__restrict__ head, const int *__restrict__ cellpos,
-                                const int *__restrict__ cell_start, int *__restrict__ flag) {
+                                const int *__restrict__ cell_start, const int *__restrict__ cmask,
+                                int *__restrict__ flag) {
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
         const int c = cellpos[k] + head[k] - 1;
-        flag[k] = ((k - cell_start[c]) & 31) == 0 ? 1 : 0;
+        flag[k] = ((cmask[c] >> 13) & 1) && ((k - cell_start[c]) & 31) == 0 ? 1 : 0;
     }
 }
 
@@ -515,7 +536,8 @@ struct __align__(16) ItemRec {
 __global__ void items_kernel(int n, const int *__restrict__ head, const int *__restrict__ cellpos,
                              const int *__restrict__ flag, const int *__restrict__ itempos,
                              const int *__restrict__ cell_start, const uint64_t *__restrict__ cell_key,
-                             const unsigned char *__restrict__ conn, FofGeom g, ItemRec *__restrict__ items,
+                             const unsigned char *__restrict__ conn, const int *__restrict__ cmask, FofGeom g,
+                             ItemRec *__restrict__ items, unsigned short *__restrict__ imask,
                              int *__restrict__ nitems) {
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
         if (flag[k]) {
@@ -525,6 +547,7 @@ __global__ void items_kernel(int n, const int *__restrict__ head, const int *__r
             r.ce_conn = cell_start[c + 1] | (conn[c] ? (int)0x80000000u : 0);
             decode_key(cell_key[c], g, r.cx, r.cy, r.cz);
             items[itempos[k]] = r;
+            imask[itempos[k]] = (unsigned short)(cmask[c] & 0x1fff);
         }
         if (k == n - 1) *nitems = itempos[k] + flag[k];
     }
@@ -558,6 +581,39 @@ __constant__ int c_stencil[13][3] = {{0, 0, 1},  {0, 1, -1}, {0, 1, 0},  {0, 1, 
                                      {1, -1, 0}, {1, -1, 1}, {1, 0, -1}, {1, 0, 0},  {1, 0, 1},
                                      {1, 1, -1}, {1, 1, 0},  {1, 1, 1}};
 
+// The occupied forward neighbours of every cell as a 13-bit mask (bit j: stencil cell j),
+// one thread per cell: a Bloom-filter test per neighbour (L2-resident) and a hash lookup only
+// for the ones it lets through.  Bit 13 marks the cells with linking work: an occupied
+// neighbour, or more than one particle in a cell that is not one component already.  Cells
+// without work (isolated particles, isolated one-component cells) get no work item.  (Linking
+// the cells of at most 4 particles one thread each instead of one warp per chunk measured
+// slower: 76 against 66 ms for the links of the 2e8-particle snapshot.)
+__global__ void nbmask_kernel(const int *__restrict__ ncell_p, const int *__restrict__ cell_start,
+                              const uint64_t *__restrict__ cell_key, const unsigned char *__restrict__ conn,
+                              const CellSlot *__restrict__ slots, const unsigned long long *__restrict__ hmask_p,
+                              const unsigned *__restrict__ bloom, const unsigned long long *__restrict__ bmask_p,
+                              FofGeom g, int *__restrict__ cmask) {
+    const int nc = *ncell_p;
+    const uint64_t hmask = *hmask_p, bmask = *bmask_p;
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x) {
+        long long cx, cy, cz;
+        decode_key(cell_key[c], g, cx, cy, cz);
+        int m = 0;
+#pragma unroll 1
+        for (int j = 0; j < 13; ++j) {
+            const long long nx = cx + c_stencil[j][0], ny = cy + c_stencil[j][1], nz = cz + c_stencil[j][2];
+            if (nx >= g.ncx || ny < 0 || ny >= g.ncy || nz < 0 || nz >= g.ncz) continue;
+            const uint64_t nkey = ((uint64_t)nx * (uint64_t)g.ncy + (uint64_t)ny) * (uint64_t)g.ncz + (uint64_t)nz;
+            const uint64_t b = bloom_bit(nkey, bmask);
+            if (!((__ldg(bloom + (b >> 5)) >> (b & 31)) & 1u)) continue;
+            if (hash_lookup(slots, hmask, nkey).y != 0) m |= 1 << j;
+        }
+        const int count = cell_start[c + 1] - cell_start[c];
+        const bool work = m != 0 || (count > 1 && !conn[c]);
+        cmask[c] = m | (work ? 1 << 13 : 0);
+    }
+}
+
 // One warp per item (a chunk of up to 32 particles of one cell).  The candidates of the item
 // are the later particles of its own cell (j > k) and every particle of the 13 forward
 // neighbour cells; they are concatenated into one list ("segments" 0..12 = stencil cells, 13 =
@@ -567,8 +623,9 @@ __constant__ int c_stencil[13][3] = {{0, 0, 1},  {0, 1, -1}, {0, 1, 0},  {0, 1, 
 constexpr int kHomeSeg = 13;
 
 __global__ void __launch_bounds__(256, 6) link_kernel(
-    const float4 *__restrict__ rec, const ItemRec *__restrict__ items, const int *__restrict__ nitems_p,
-    int *item_counter, const CellSlot *__restrict__ slots, const unsigned long long *__restrict__ hmask_p, FofGeom g,
+    const float4 *__restrict__ rec, const ItemRec *__restrict__ items, const unsigned short *__restrict__ imask,
+    const int *__restrict__ nitems_p, int *item_counter, const CellSlot *__restrict__ slots,
+    const unsigned long long *__restrict__ hmask_p, FofGeom g,
     const double *__restrict__ x, const double *__restrict__ y, const double *__restrict__ z,
     int *parent, unsigned char *has, int *err) {
     __shared__ float4 buf[kFofWarps][32];
@@ -602,7 +659,7 @@ __global__ void __launch_bounds__(256, 6) link_kernel(
         if (lane < 13) {
             soff = (c_stencil[lane][0] + 1) | (c_stencil[lane][1] + 1) << 2 | (c_stencil[lane][2] + 1) << 4;
             const long long nx = cx + c_stencil[lane][0], ny = cy + c_stencil[lane][1], nz = cz + c_stencil[lane][2];
-            if (nx < g.ncx && ny >= 0 && ny < g.ncy && nz >= 0 && nz < g.ncz) {
+            if ((__ldg(imask + item) >> lane) & 1u) {   // in the grid and occupied (nbmask_kernel)
                 const uint64_t nkey = ((uint64_t)nx * (uint64_t)g.ncy + (uint64_t)ny) * (uint64_t)g.ncz + (uint64_t)nz;
                 const int2 sc = hash_lookup(slots, hmask, nkey);
                 sjs = sc.x;
@@ -709,15 +766,23 @@ __global__ void __launch_bounds__(256, 6) link_kernel(
                 const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
                 bool hit = hv && d2 <= g.hi && (jb < 0 || jb > k);
                 if (hit && d2 >= g.lo) hit = exact_link(x, y, z, hidx, __float_as_int(qq.w), g.r2);
-                if (hit) {
-                    const int rq = rbuf[w][t];
-                    if (rq != myroot) {
-                        uf_union(parent, myroot, rq, err);
-                        has[k] = 1;
-                        has[jb < 0 ? ~jb : jb] = 1;
-                        myroot = uf_find_cached(parent, k, err);
-                    }
-                }
+                if (!__any_sync(0xffffffffu, hit)) continue;
+                // the candidate's current root (the one read at the start of the round is
+                // outdated once an earlier candidate of its set has been joined)
+                int rq = rbuf[w][t];
+                if (lane == 0) rq = uf_find_cached(parent, rq, err);
+                rq = __shfl_sync(0xffffffffu, rq, 0);
+                const bool need = hit && myroot != rq;
+                const unsigned nm = __ballot_sync(0xffffffffu, need);
+                if (!nm) continue;
+                // one union per distinct root among the home particles that hit: in a crowded
+                // cell most of the 32 share one, and their unions would all contend for it
+                const unsigned peers = __match_any_sync(0xffffffffu, need ? myroot : ~lane);
+                if (need && lane == __ffs(peers) - 1) uf_union(parent, myroot, rq, err);
+                if (need) has[k] = 1;
+                if (lane == __ffs(nm) - 1) has[jb < 0 ? ~jb : jb] = 1;
+                __syncwarp();
+                if (need) myroot = uf_find_cached(parent, k, err);
             }
         }
     }
@@ -939,6 +1004,8 @@ int fof_core(int n, const double *x, const double *y, const double *z, FofGeom g
 
     uint64_t hcap = 1024;   // slots allocated; the kernels use a power of two >= 2 x cells of it
     while (hcap < 2ull * (uint64_t)n) hcap <<= 1;
+    uint64_t bcap = 1024;   // Bloom-filter bits allocated; the kernels use >= 8 bits per cell of it
+    while (bcap < 8ull * (uint64_t)n) bcap <<= 1;
     const size_t sort_b = sort_pairs_u64_i32_bytes(n, end_bit);
     const size_t scan_b = std::max(exclusive_sum_i32_bytes(n), inclusive_max_i32_bytes(n));
     Layout M;
@@ -949,7 +1016,8 @@ int fof_core(int n, const double *x, const double *y, const double *z, FofGeom g
     const size_t o_par = M.add(4ull * n), o_has = M.add(1ull * n), o_root = M.add(4ull * n);
     const size_t o_min = M.add(4ull * n);
     const size_t o_cst = M.add(4ull * (n + 1)), o_ckey = M.add(8ull * n);
-    const size_t o_hk = M.add(16ull * hcap), o_hv = M.add(4ull * n);   // hash slots, slot of each cell
+    const size_t o_hk = M.add(16ull * hcap), o_cm = M.add(4ull * n);   // hash slots, neighbour mask per cell
+    const size_t o_bloom = M.add(bcap / 8), o_imask = M.add(2ull * n);
     const size_t o_flag = M.add(4ull * n), o_ipos = M.add(4ull * n);
     const size_t o_items = M.add(sizeof(ItemRec) * (size_t)n);
     const size_t o_cnt = M.add(64), o_conn = M.add(1ull * n);
@@ -967,11 +1035,14 @@ int fof_core(int n, const double *x, const double *y, const double *z, FofGeom g
     auto *cst = at<int>(base, o_cst);
     auto *ckey = at<uint64_t>(base, o_ckey);
     auto *hk = at<CellSlot>(base, o_hk);
-    auto *hv = at<int>(base, o_hv);
+    auto *cmask = at<int>(base, o_cm);
+    auto *bloom = at<unsigned>(base, o_bloom);
+    auto *imask = at<unsigned short>(base, o_imask);
     auto *flag = at<int>(base, o_flag), *ipos = at<int>(base, o_ipos);
     auto *items = at<ItemRec>(base, o_items);
     int *cnt = at<int>(base, o_cnt);   // [0] ncell [1] nitems [2] ngroups [3] err [5] link item counter
     auto *hmask = reinterpret_cast<unsigned long long *>(cnt + 6);   // [6..7] hash slot mask
+    auto *bmask = reinterpret_cast<unsigned long long *>(cnt + 10);  // [10..11] Bloom bit mask ([8] dense cells)
     void *tmp = at<void>(base, o_tmp);
     const int g1 = std::min(sms * 8, grid_for(n, 256));
 
@@ -991,9 +1062,7 @@ int fof_core(int n, const double *x, const double *y, const double *z, FofGeom g
     }
     HALMA_TRY(mark(3));
     HALMA_TRY(exclusive_sum_i32(tmp, scan_b, head, cpos, n, st));
-    HALMA_LAUNCH(hash_size_kernel, 1, 1, 0, st, n, head, cpos, (unsigned long long)hcap, hmask);
-    HALMA_LAUNCH(hash_clear_kernel, g1, 256, 0, st, hmask, hk);
-    HALMA_LAUNCH(cells_kernel, g1, 256, 0, st, n, g.sb, kout, head, cpos, cst, ckey, hk, hv, hmask, cnt + 0);
+    HALMA_LAUNCH(cell_table_kernel, g1, 256, 0, st, n, g.sb, kout, head, cpos, cst, ckey, cnt + 0);
     // one-component cells (sub-cells in the key and a positive linking length only)
     unsigned char *conn = at<unsigned char>(base, o_conn);
     int *dlist = at<int>(base, o_dlist);
@@ -1003,14 +1072,19 @@ int fof_core(int n, const double *x, const double *y, const double *z, FofGeom g
     } else {
         HALMA_CUDA(cudaMemsetAsync(conn, 0, n, st));
     }
-    HALMA_LAUNCH(slot_fill_kernel, g1, 256, 0, st, cnt + 0, cst, hv, conn, hk);
+    HALMA_LAUNCH(hash_size_kernel, 1, 1, 0, st, n, head, cpos, (unsigned long long)hcap, (unsigned long long)bcap,
+                 hmask, bmask);
+    HALMA_LAUNCH(hash_clear_kernel, g1, 256, 0, st, hmask, hk, bmask, bloom);
+    HALMA_LAUNCH(cell_insert_kernel, g1, 256, 0, st, cnt + 0, cst, ckey, conn, hk, hmask, bloom, bmask);
+    HALMA_LAUNCH(nbmask_kernel, g1, 256, 0, st, cnt + 0, cst, ckey, conn, hk, hmask, bloom, bmask, g, cmask);
     HALMA_TRY(mark(4));
-    HALMA_LAUNCH(itemflag_kernel, g1, 256, 0, st, n, head, cpos, cst, flag);
+    HALMA_LAUNCH(itemflag_kernel, g1, 256, 0, st, n, head, cpos, cst, cmask, flag);
     HALMA_TRY(exclusive_sum_i32(tmp, scan_b, flag, ipos, n, st));
-    HALMA_LAUNCH(items_kernel, g1, 256, 0, st, n, head, cpos, flag, ipos, cst, ckey, conn, g, items, cnt + 1);
+    HALMA_LAUNCH(items_kernel, g1, 256, 0, st, n, head, cpos, flag, ipos, cst, ckey, conn, cmask, g, items, imask,
+                 cnt + 1);
     HALMA_TRY(mark(5));
-    HALMA_LAUNCH(link_kernel, sms * 8, 32 * kFofWarps, 0, st, rec, items, cnt + 1, cnt + 5, hk, hmask, g, x, y, z,
-                 parent, has, cnt + 3);
+    HALMA_LAUNCH(link_kernel, sms * 8, 32 * kFofWarps, 0, st, rec, items, imask, cnt + 1, cnt + 5, hk, hmask, g, x,
+                 y, z, parent, has, cnt + 3);
     HALMA_TRY(mark(6));
     HALMA_LAUNCH(root_kernel, g1, 256, 0, st, n, rec, parent, has, root, minidx, cnt + 3);
     HALMA_LAUNCH(label_kernel, g1, 256, 0, st, n, rec, has, root, minidx, labels, cnt + 2);
