@@ -8,6 +8,7 @@
 
 #include "common.cuh"
 #include "pair_math.cuh"
+#include "unbind.cuh"
 
 namespace halma {
 
@@ -252,6 +253,71 @@ static int potential_fast_api(int64_t ns, const float *mm, const float *sx_, con
     return sg.download(st);
 }
 
+// ---------------------------------------------------------------------------------------
+// Targets that are the first nt sources (self-potential of a set, plus other sources): the
+// pairs inside the set go through the symmetric block kernel of the unbinding, each pair
+// evaluated once for both particles; the remaining sources through the tile kernel.
+constexpr int64_t kSymMinTargets = 8192;
+
+__global__ void pack_sources_kernel(int64_t n, const float *__restrict__ m, const float *__restrict__ x,
+                                    const float *__restrict__ y, const float *__restrict__ z, float4 *__restrict__ pk) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        pk[i] = make_float4(x[i], y[i], z[i], m[i]);
+}
+
+// phi_i = the set's slices in block order + the other sources (float32 or per-slice FP64
+// partials) + the self term m_i eps^-1 when the self pair is counted (mask NONE); FP64 sum.
+__global__ void sym_finish_kernel(int64_t nt, int nblk, int64_t npad, const float2 *__restrict__ part,
+                                  const float *__restrict__ tail, const double *__restrict__ tail_part, int n_tail,
+                                  const float *__restrict__ m, double self_scale, float *__restrict__ out) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nt; i += (int64_t)gridDim.x * blockDim.x) {
+        double acc = 0.0;
+        for (int b = 0; b < nblk; ++b) {
+            const float2 v = part[(int64_t)b * npad + i];
+            acc += (double)v.x + (double)v.y;
+        }
+        if (tail) acc += (double)tail[i];
+        for (int s = 0; s < n_tail; ++s) acc += tail_part[(int64_t)s * nt + i];
+        acc += self_scale * (double)m[i];
+        out[i] = (float)acc;
+    }
+}
+
+static int potential_sym_api(int64_t ns, const float *m, const float *x, const float *y, const float *z, int64_t nt,
+                             double eps2, int mask, float *out, cudaStream_t st) {
+    constexpr int T = 4;
+    const int nblk = sym_block_count((int)nt);
+    const int64_t npad = (nt + 31) / 32 * 32;
+    const int64_t nrest = ns - nt;
+    int n_split = 1;
+    int64_t split_len = nrest;
+    if (nrest > 0) choose_split(nrest, nt, T, &n_split, &split_len);
+    Layout L;
+    const size_t o_pk = L.add(sizeof(float4) * npad), o_part = L.add(sizeof(float2) * (size_t)nblk * npad);
+    const size_t o_desc = L.add(512);
+    const size_t o_tail = L.add(sizeof(float) * (nrest > 0 && n_split == 1 ? nt : 1));
+    const size_t o_tp = L.add(sizeof(double) * (nrest > 0 && n_split > 1 ? (size_t)n_split * nt : 1));
+    void *base = nullptr;
+    HALMA_TRY(workspace(L.total, &base, st, 9));
+    float4 *pk = at<float4>(base, o_pk);
+    float2 *part = at<float2>(base, o_part);
+    const int g = std::min(device_sm_count() * 8, grid_for(nt, 256));
+    HALMA_LAUNCH(pack_sources_kernel, g, 256, 0, st, nt, m, x, y, z, pk);
+    HALMA_TRY(sym_self_potential_device(pk, (int)nt, (float)eps2, part, at<void>(base, o_desc), st));
+    float *tail = nullptr;
+    double *tail_part = nullptr;
+    if (nrest > 0) {
+        if (n_split > 1) tail_part = at<double>(base, o_tp);
+        else tail = at<float>(base, o_tail);
+        HALMA_TRY(launch_fast<T>(m + nt, x + nt, y + nt, z + nt, nrest, x, y, z, nt, (float)eps2, n_split, split_len,
+                                 HALMA_MASK_NONE, 0, tail, tail_part, st));
+    }
+    const double self_scale = (mask == HALMA_MASK_NONE && eps2 > 0.0) ? 1.0 / sqrt(eps2) : 0.0;
+    HALMA_LAUNCH(sym_finish_kernel, g, 256, 0, st, nt, nblk, npad, part, tail, tail_part, tail_part ? n_split : 0, m,
+                 self_scale, out);
+    return HALMA_OK;
+}
+
 }  // namespace halma
 
 using namespace halma;
@@ -309,6 +375,15 @@ extern "C" int halma_potential_f32(int64_t ns, const float *m, const float *sx, 
     if (mask < HALMA_MASK_COORD || mask > HALMA_MASK_NONE) return fail(HALMA_ERR_INVALID, "unknown mask %d", mask);
     if (!(eps2 >= 0.0) || !isfinite(eps2)) return fail(HALMA_ERR_INVALID, "eps2 must be finite and >= 0");
     std::lock_guard<std::mutex> guard(api_mutex());
+    // targets that are the first sources (device arrays): the set's pairs once for both
+    // particles; eps2 > 0 with mask NONE (the self pair is then a finite term), or mask SELF
+    // skipping exactly the self pair
+    const bool self_set = tx == sx && ty == sy && tz == sz && nt >= kSymMinTargets && nt <= ns &&
+                          nt <= 65535ll * 1024 && ((mask == HALMA_MASK_NONE && eps2 > 0.0) ||
+                                                   (mask == HALMA_MASK_SELF && self_offset == 0));
+    if (self_set && is_device_pointer(m) && is_device_pointer(sx) && is_device_pointer(sy) && is_device_pointer(sz) &&
+        is_device_pointer(phi))
+        return potential_sym_api(ns, m, sx, sy, sz, nt, eps2, mask, phi, (cudaStream_t)stream);
     return potential_fast_api(ns, m, sx, sy, sz, nt, tx, ty, tz, eps2, mask, self_offset, phi, (cudaStream_t)stream);
 }
 

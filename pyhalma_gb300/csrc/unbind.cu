@@ -1317,6 +1317,43 @@ int Profile::ensure_events(int k) {
     return HALMA_OK;
 }
 
+int sym_block_count(int nb) { return (nb + kSymBlock - 1) / kSymBlock; }
+
+// Self-potential of nb particles packed as float4 (x, y, z, m), every pair evaluated once for
+// both particles by the symmetric block kernel: part[b * npad + r] (npad = nb rounded up to
+// 32) receives the double-float sum over the sources of block b of m_j (r^2 + eps2)^-1/2,
+// j != r, for b < sym_block_count(nb).  scratch: 512 bytes of device memory for the
+// description of the single work list.
+int sym_self_potential_device(const float4 *pk, int nb, float eps2, float2 *part, void *scratch, cudaStream_t st) {
+    if (nb <= 0) return HALMA_OK;
+    if (nb > 65535 * kSymBlock) return fail(HALMA_ERR_CAPACITY, "at most %d particles", 65535 * kSymBlock);
+    const int64_t B = sym_block_count(nb);
+    struct Desc {
+        HaloState hs;
+        int64_t poff[2], qoff[2];
+        int4 idesc;
+        int ystart[2];
+        int cnt[8];
+    } d{};
+    static_assert(sizeof(Desc) <= 512, "work description exceeds its scratch");
+    d.hs.nb = nb;
+    d.hs.active = 1;
+    d.poff[1] = ((int64_t)nb + 31) / 32 * 32;
+    d.idesc = make_int4(0, kSymT, 1, (int)B);
+    d.ystart[1] = (int)(B * (B + 1) / 2);
+    d.cnt[3] = d.ystart[1];
+    HALMA_CUDA(cudaMemcpyAsync(scratch, &d, sizeof(Desc), cudaMemcpyHostToDevice, st));
+    Desc *dd = static_cast<Desc *>(scratch);
+    constexpr int kSymSmem = kSymBlock * (int)sizeof(float4) + kSymWarps * kSymBlock * (int)sizeof(float);
+    HALMA_CUDA(cudaFuncSetAttribute(ub_pair_sym_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSymSmem));
+    int bps = 0;
+    HALMA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, ub_pair_sym_kernel, 128, kSymSmem));
+    const int grid = (int)std::min<int64_t>((int64_t)device_sm_count() * std::max(bps, 1), d.cnt[3]);
+    HALMA_LAUNCH(ub_pair_sym_kernel, grid, 128, kSymSmem, st, pk, dd->poff, dd->qoff, &dd->hs, 1, dd->ystart,
+                 &dd->idesc, dd->cnt, dd->cnt + 4, eps2, part);
+    return HALMA_OK;
+}
+
 // Device-array implementation shared by halma_unbind_batched and the pipeline.
 int unbind_device(int64_t n, int nh, const int64_t *d_off, const int64_t *h_off, const double *x, const double *y,
                   const double *z, const double *vx, const double *vy, const double *vz, const double *m,

@@ -47,6 +47,8 @@ int fof_segmented_device(int n, int nseg, const int64_t *off, const double *x, c
 int reductions_device(int64_t n, int nh, const int64_t *off, const double *x, const double *y, const double *z,
                       const double *vx, const double *vy, const double *vz, const double *m,
                       const unsigned char *mask, const double *about, double *out, cudaStream_t st);
+int sym_block_count(int nb);
+int sym_self_potential_device(const float4 *pk, int nb, float eps2, float2 *part, void *scratch, cudaStream_t st);
 int unbind_device(int64_t n, int nh, const int64_t *d_off, const int64_t *h_off, const double *x,
                   const double *y, const double *z, const double *vx, const double *vy,
                   const double *vz, const double *m, const halma_unbind_params &p,

@@ -116,3 +116,28 @@ def test_device_tensor_path(cuda):
     assert phi.is_cuda
     ref = oracle.bf_potential_f32(m, p[:, 0], p[:, 1], p[:, 2], p[:, 0], p[:, 1], p[:, 2])
     assert np.array_equal(phi.cpu().numpy(), ref)
+
+
+@pytest.mark.parametrize("nt,ns,self_mask", [(20_001, 20_001, False), (20_001, 26_000, False),
+                                             (9_000, 300_000, False), (12_345, 15_000, True)])
+def test_self_set_potential_symmetric_route(cuda, nt, ns, self_mask):
+    """Targets that are the first sources (the same device arrays): the set's pairs go through
+    the symmetric block kernel, once for both particles; the other sources through the tile
+    kernel.  Against the FP64 oracle at RTOL_FAST and against the tile kernel alone (the same
+    targets as separate arrays) at RTOL_FAST."""
+    import torch
+    from pyhalma_gb300.autograd import potential_f32
+    rng = np.random.default_rng(nt + ns)
+    p, m = _cloud(rng, ns, scale=0.005, centre=(0.3, -0.2, 0.1))
+    f = lambda a: torch.tensor(np.ascontiguousarray(a, dtype=np.float32), device=cuda)
+    sx, sy, sz, sm = f(p[:, 0]), f(p[:, 1]), f(p[:, 2]), f(m)
+    eps = 1e-4
+    so = 0 if self_mask else None
+    phi = potential_f32(sx, sy, sz, sm, sx[:nt], sy[:nt], sz[:nt], eps, self_offset=so).cpu().numpy()
+    tile = potential_f32(sx, sy, sz, sm, sx[:nt].clone(), sy[:nt].clone(), sz[:nt].clone(), eps,
+                         self_offset=so).cpu().numpy()
+    q = p.astype(np.float32).astype(np.float64)
+    ref = oracle.potential_f64(m.astype(np.float32).astype(np.float64), *q.T, *q[:nt].T, eps2=eps * eps,
+                               mask=oracle.MASK_SELF if self_mask else oracle.MASK_NONE)
+    assert np.max(np.abs(phi / ref - 1.0)) <= RTOL_FAST
+    assert np.max(np.abs(phi.astype(np.float64) / tile - 1.0)) <= RTOL_FAST
