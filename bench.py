@@ -977,7 +977,17 @@ def main():
     ap.add_argument("--skip-fp64", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-full", action="store_true")
+    ap.add_argument("--scale", type=float, default=1.0,
+                    help="multiply the particle and halo counts of the workload (small cases for profiling)")
     args = ap.parse_args()
+    if args.scale != 1.0:
+        for w in WORKLOADS.values():
+            w["particles"] = int(round(w["particles"] * args.scale))
+            if "haloes" in w:
+                w["haloes"] = int(round(w["haloes"] * args.scale))
+            if "spheres" in w:
+                w["spheres"] = max(1, int(round(w["spheres"] * args.scale)))
+            w["workload"] += f"-scaled-{args.scale:g}"
     if args.impl == "reference":
         if args.workload not in ("northstar", "plummer2m"):
             args.workload = "northstar"
