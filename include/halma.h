@@ -323,6 +323,11 @@ int halma_bf_potential_f32_noalloc(int64_t ntotal, const float *total_mass, cons
 
 /* float32 pair terms (rsqrt) with compensated sums and a selectable mask: the smooth
  * (differentiable) forward of halma_potential_grad_f32 when mask is SELF or NONE.
+ * When the targets are the first nt sources (tx == sx, ty == sy, tz == sz, device arrays,
+ * nt >= 8192) and the mask is NONE with eps2 > 0 or SELF with self_offset 0, the pairs among
+ * those nt particles are evaluated once for both particles (symmetric block kernel) and the
+ * other sources per target; the result agrees with the per-target route within the same
+ * 1e-6 relative bound, not bit for bit.
  * No reference counterpart beyond the potential above. */
 int halma_potential_f32(int64_t ns, const float *m, const float *sx, const float *sy,
                         const float *sz, int64_t nt, const float *tx, const float *ty,

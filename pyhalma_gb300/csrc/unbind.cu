@@ -283,6 +283,7 @@ __global__ void __launch_bounds__(1024) ub_items_kernel(int nh, const int *__res
     for (int h0 = 0; h0 < nh; h0 += blockDim.x) {
         const int q = h0 + threadIdx.x;
         int h = -1, n = 0, T = 4, nsl = 1, nseg = 0, ny = 0, nsl_e = 0;
+        unsigned long long my_pairs = 0, my_spairs = 0;
         if (q < nh) {
             h = order[q];
             if (hs[h].active) {
@@ -294,13 +295,23 @@ __global__ void __launch_bounds__(1024) ub_items_kernel(int nh, const int *__res
                     const int B = (nb + kSymBlock - 1) / kSymBlock;   // B <= 65535: B(B+1)/2 < 2^31
                     ny = (int)((int64_t)B * (B + 1) / 2);
                     nsl_e = B;
-                    atomicAdd(&spairs, (unsigned long long)nb * (unsigned long long)nb);
+                    my_spairs = (unsigned long long)nb * (unsigned long long)nb;
                 } else {
                     n = ns > 0 ? ((nb + 32 * T - 1) / (32 * T)) * nsl : 0;
                     nsl_e = nsl;
                 }
                 nseg = max(1, (nb + kSeg - 1) / kSeg);
-                if (nb > 0) atomicAdd(&pairs, (unsigned long long)nb * (unsigned long long)ns);
+                my_pairs = (unsigned long long)nb * (unsigned long long)ns;
+            }
+        }
+        if (pairs_out) {   // pair counts for the profile: one shared atomic per warp
+            for (int o = 16; o > 0; o >>= 1) {
+                my_pairs += __shfl_xor_sync(0xffffffffu, my_pairs, o);
+                my_spairs += __shfl_xor_sync(0xffffffffu, my_spairs, o);
+            }
+            if (lane == 0) {
+                atomicAdd(&pairs, my_pairs);
+                atomicAdd(&spairs, my_spairs);
             }
         }
         const int incl = warp_incl_scan(n, lane);
