@@ -113,6 +113,16 @@ class ClockSampler:
                                          stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
+            return
+        # nvidia-smi's start-up (NVML initialisation) stalls CUDA calls of this process for a
+        # few hundred milliseconds: wait for its first sample so that it falls before the
+        # timed region (on a 7 ms step it had made the wall clock 4x the event clock)
+        t0 = time.perf_counter()
+        while time.perf_counter() - t0 < 5.0 and self.proc.poll() is None:
+            if os.path.getsize(self.path) > 0:
+                break
+            time.sleep(0.02)
+        time.sleep(0.2)
 
     def stop(self):
         if not self.proc:
@@ -446,7 +456,8 @@ def run_gpu(args):
             torch.distributed.barrier()
 
     _lib.set_profiling(True)
-    for _ in range(args.warmup):
+    for _ in range(args.warmup):   # warm-up steps as the timed ones (the first L2 flush loads its kernel)
+        flush.zero_()
         find_haloes(*dev_in, ll, w["min_members"], options=opt)
     torch.cuda.synchronize()
 
