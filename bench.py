@@ -531,7 +531,7 @@ def run_gpu(args):
 
     # the plain FP64 per-halo path on a size-stratified sample, extrapolated to every halo
     fp64 = None
-    if not args.skip_fp64:
+    if not args.skip_fp64 and rank == 0:
         off = cat.offsets.cpu().numpy()
         t_unb64, classes, t_fixed, err = fp64_sampled(off, cat.members, dev_in, opt)
         t_fof = statistics.mean(fof_ms) * 1e-3
