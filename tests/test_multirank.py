@@ -146,3 +146,58 @@ def test_slab_edges_and_single_rank():
     lab = shard.fof_slabs(x, y, z, np.arange(len(x)), 0.0015, shard.slab_edges(x.min(), x.max(), 1, 0.0015),
                           local_fof=oracle.fof_labels)
     assert np.array_equal(lab, oracle.fof_labels(x, y, z, 0.0015))
+
+
+def _slab_worker3(rank, world, port, q):
+    """Three ranks over a box whose x-extent holds only two slabs: the third rank has no slab
+    and no particles but takes part in the exchange."""
+    import torch.distributed as dist
+    import oracle
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    x, y, z = _narrow_snapshot()
+    ll = 0.0015
+    edges = shard.slab_edges(x.min(), x.max(), world, ll)
+    mine = np.nonzero(shard.slab_of(x, edges) == rank)[0] if rank < len(edges) - 1 else np.zeros(0, dtype=np.int64)
+    lab = shard.fof_slabs(x[mine], y[mine], z[mine], mine, ll, edges, local_fof=oracle.fof_labels)
+    q.put((rank, mine, lab, len(edges) - 1))
+    dist.destroy_process_group()
+
+
+def _narrow_snapshot():
+    """A 2.2 LL wide strip of particles (so only two slabs of >= LL fit) with chains along x
+    that cross the face."""
+    rng = np.random.default_rng(6)
+    n = 3000
+    x = rng.uniform(0.0, 0.0033, n)
+    y = rng.uniform(-0.05, 0.05, n)
+    z = rng.uniform(-0.05, 0.05, n)
+    t = np.arange(0, 5, dtype=np.float64)
+    cx, cy, cz = 0.0002 + 0.0007 * t, np.full(5, 0.01), np.full(5, 0.02)
+    return np.concatenate([x, cx]), np.concatenate([y, cy]), np.concatenate([z, cz])
+
+
+def test_slab_fof_three_ranks_two_slabs():
+    import multiprocessing as mp
+    import oracle
+    oracle.build()
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_slab_worker3, args=(r, 3, port, q)) for r in range(3)]
+    for p in procs:
+        p.start()
+    res = [q.get(timeout=240) for _ in procs]
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    x, y, z = _narrow_snapshot()
+    ref = oracle.fof_labels(x, y, z, 0.0015)
+    got = np.full(len(x), -2, dtype=np.int64)
+    for rank, mine, lab, nslab in res:
+        assert nslab == 2
+        got[mine] = lab
+    assert (got != -2).all()
+    assert np.array_equal(got, ref)
+    assert len(set(got[-5:])) == 1
