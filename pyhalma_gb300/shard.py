@@ -188,3 +188,86 @@ def fof_slabs(x, y, z, gid, linking_length, edges, local_fof=None, group=None):
         hit[hit] = ids[pos[hit]] == out[hit]
         out[hit] = root[pos[hit]]
     return out
+
+
+# ---------------------------------------------------------------------------------------
+# one snapshot over several ranks: slab FoF, groups, halo-sharded unbinding
+# ---------------------------------------------------------------------------------------
+def find_haloes_sharded(x, y, z, vx, vy, vz, m, gid, linking_length, minp, edges, options=None,
+                        local_fof=None, compute=None, group=None):
+    """FoF + groups of >= minp members + iterative unbinding of one snapshot spread over the
+    ranks by x-slab.  Each rank passes its slab's particles and their global ids; returns
+    (labels, bound) for those particles — the labels of the single-process FoF (smallest global
+    id of the group, -1 alone) and 1 for members of kept groups that survive the unbinding —
+    and (halo_ids, table): the groups this rank unbound (identified by their label) and their
+    unbinding table rows.
+
+    Groups are dealt to ranks by longest-processing-time on N_h^2; a group's members are sent
+    to its rank (one all-gather of the members of groups that span or leave a slab), sorted by
+    global id (the reference's member order), unbound there, and the bound flags go back to
+    the ranks that hold the particles (one more all-gather).  ``local_fof`` and ``compute``
+    default to the GPU's FoF and ``unbinding.unbind_batched``."""
+    import torch.distributed as dist
+    world = dist.get_world_size(group) if dist.is_initialized() else 1
+    rank = dist.get_rank(group) if dist.is_initialized() else 0
+    if compute is None:
+        from .unbinding import unbind_batched as compute
+    cols = [np.ascontiguousarray(a, dtype=np.float64) for a in (x, y, z, vx, vy, vz, m)]
+    gid = np.asarray(gid, dtype=np.int64)
+    lab = fof_slabs(cols[0], cols[1], cols[2], gid, linking_length, edges, local_fof=local_fof, group=group)
+
+    def allgather(obj):
+        if world == 1:
+            return [obj]
+        out = [None] * world
+        dist.all_gather_object(out, obj, group=group)
+        return out
+    # group sizes over all ranks
+    inn = lab >= 0
+    ul, cnt = np.unique(lab[inn], return_counts=True)
+    parts = allgather((ul, cnt))
+    allul = np.concatenate([p[0] for p in parts]) if parts else np.zeros(0, dtype=np.int64)
+    allcnt = np.concatenate([p[1] for p in parts]) if parts else np.zeros(0, dtype=np.int64)
+    labels_g, inv = np.unique(allul, return_inverse=True)
+    sizes = np.zeros(len(labels_g), dtype=np.int64)
+    np.add.at(sizes, inv, allcnt)
+    keep = sizes >= max(int(minp), 1)
+    kept, ksize = labels_g[keep], sizes[keep]          # ascending label = the reference's group order
+    owner_of = np.full(len(kept), -1, dtype=np.int64)
+    for r, hs in enumerate(partition_haloes(ksize, world)):
+        owner_of[hs] = r
+    # members to their group's rank
+    pos = np.searchsorted(kept, lab)
+    mine_in = inn & (pos < len(kept))
+    mine_in[mine_in] = kept[pos[mine_in]] == lab[mine_in]
+    rows = np.nonzero(mine_in)[0]
+    send = (lab[rows], gid[rows], np.stack([c[rows] for c in cols], 1))
+    got = allgather(send)
+    mylab = np.concatenate([g[0] for g in got])
+    mygid = np.concatenate([g[1] for g in got])
+    mydat = np.concatenate([g[2] for g in got]) if mylab.size else np.zeros((0, 7))
+    sel = owner_of[np.searchsorted(kept, mylab)] == rank if mylab.size else np.zeros(0, dtype=bool)
+    mylab, mygid, mydat = mylab[sel], mygid[sel], mydat[sel]
+    order = np.lexsort((mygid, mylab))                 # groups by label, members by global id
+    mylab, mygid, mydat = mylab[order], mygid[order], mydat[order]
+    halo_ids, starts = np.unique(mylab, return_index=True)
+    off = np.append(starts, len(mylab)).astype(np.int64)
+    if len(halo_ids):
+        res = compute(off, *[np.ascontiguousarray(mydat[:, q]) for q in range(7)], options) \
+            if options is not None else compute(off, *[np.ascontiguousarray(mydat[:, q]) for q in range(7)])
+        b, table = np.asarray(res[0]).astype(np.uint8), np.asarray(res[1])
+    else:
+        b, table = np.zeros(0, dtype=np.uint8), np.zeros((0, 11))
+    # bound flags back to the ranks holding the particles
+    back = allgather((mygid, b))
+    bgid = np.concatenate([g[0] for g in back])
+    bval = np.concatenate([g[1] for g in back])
+    bound = np.zeros(len(gid), dtype=np.uint8)
+    if bgid.size:
+        o = np.argsort(bgid, kind="stable")
+        bgid, bval = bgid[o], bval[o]
+        p2 = np.searchsorted(bgid, gid)
+        hit = p2 < len(bgid)
+        hit[hit] = bgid[p2[hit]] == gid[hit]
+        bound[hit] = bval[p2[hit]]
+    return lab, bound, halo_ids, table

@@ -201,3 +201,73 @@ def test_slab_fof_three_ranks_two_slabs():
     assert (got != -2).all()
     assert np.array_equal(got, ref)
     assert len(set(got[-5:])) == 1
+
+
+def _pipeline_snapshot():
+    """Contaminated Plummer spheres; the largest one is moved onto the middle of the x-range,
+    where the two-slab face lies, so that its group spans both slabs."""
+    s = synth.plummer_snapshot(20_000, 10, seed=12, box_mpc=0.3, bg_frac=0.1, contaminant_frac=0.15)
+    big = int(np.argmax(np.bincount(s.sphere[s.sphere >= 0])))
+    sel = s.sphere == big
+    s.x[sel] += 0.5 * (s.x.min() + s.x.max()) - np.median(s.x[sel])
+    return s
+
+
+def _pipeline_worker(rank, world, port, q):
+    import torch.distributed as dist
+    import oracle
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    s = _pipeline_snapshot()
+    edges = shard.slab_edges(s.x.min(), s.x.max(), world, 0.0015)
+    mine = np.nonzero(shard.slab_of(s.x, edges) == rank)[0]
+    cols = [a[mine] for a in (s.x, s.y, s.z, s.vx, s.vy, s.vz, s.mass)]
+    lab, bound, ids, table = shard.find_haloes_sharded(*cols, mine, 0.0015, 50, edges, local_fof=oracle.fof_labels,
+                                                       compute=_oracle_compute)
+    q.put((rank, mine, lab, bound, ids, table))
+    dist.destroy_process_group()
+
+
+def test_sharded_pipeline_two_ranks_equals_single_process():
+    """Slab FoF, groups of >= 50, LPT halo sharding and the bound flags sent back: the same
+    labels, bound flags and per-halo pass counts as one process doing it all."""
+    import multiprocessing as mp
+    import oracle
+    oracle.build()
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_pipeline_worker, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    res = [q.get(timeout=300) for _ in procs]
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    s = _pipeline_snapshot()
+    lab_ref = oracle.fof_labels(s.x, s.y, s.z, 0.0015)
+    groups = [np.asarray(g) for g in oracle.labels_to_groups(lab_ref) if len(g) >= 50]
+    off = np.concatenate([[0], np.cumsum([len(g) for g in groups])]).astype(np.int64)
+    mem = np.concatenate(groups)
+    b_ref, t_ref, _ = _oracle_compute(off, *[a[mem] for a in (s.x, s.y, s.z, s.vx, s.vy, s.vz, s.mass)])
+    bound_ref = np.zeros(s.n, dtype=np.uint8)
+    bound_ref[mem] = b_ref
+    lab = np.full(s.n, -2, dtype=np.int64)
+    bound = np.zeros(s.n, dtype=np.uint8)
+    tables = {}
+    for rank, mine, l, b, ids, table in res:
+        lab[mine] = l
+        bound[mine] = b
+        for h, row in zip(ids, table):
+            tables[int(h)] = row
+    assert np.array_equal(lab, lab_ref)
+    assert np.array_equal(bound, bound_ref)
+    assert sorted(tables) == [int(g[0]) for g in groups]
+    for k, g in enumerate(groups):
+        assert tables[int(g[0])][7] == t_ref[k, 7] and tables[int(g[0])][8] == t_ref[k, 8]
+    # some group spans both slabs, and both ranks unbind haloes
+    edges = shard.slab_edges(s.x.min(), s.x.max(), 2, 0.0015)
+    side = shard.slab_of(s.x, edges)
+    assert any(len(set(side[g])) == 2 for g in groups)
+    assert all(len(r[4]) > 0 for r in res)
