@@ -208,6 +208,48 @@ __global__ void __launch_bounds__(256) bbox_final_kernel(const long long *__rest
     }
 }
 
+// floor(t) and the value t - 4 * floor(t / 4) of a double t, clamped to [0, qmax], from the
+// double's bits with integer operations only: a particle's cell and sub-cell come from one FMA
+// per axis, and the rest of the conversion (double to integer, the remainder, the float in-cell
+// coordinate) would otherwise be half a dozen more FP64-pipe instructions per axis -- the
+// kernel's bound on GB300, whose FP64 rate is a small fraction of its integer rate.  The
+// remainder w (quarter cells, in [0, 4) away from the grid's edges) is truncated to 24
+// significant bits, an error below 1e-7 of a cell: far inside the +-1e-5 band whose pairs are
+// re-tested in FP64.
+__device__ __forceinline__ void quarter_split(double t, long long qmax, long long &q, float &w) {
+    const long long bits = __double_as_longlong(t);
+    if (bits <= 0) {   // +0.0 or negative (the sign bit makes the pattern negative)
+        q = 0;
+        w = 0.f;
+        return;
+    }
+    const int e = (int)((bits >> 52) & 0x7ff) - 1023;
+    const unsigned long long m = (unsigned long long)(bits & 0xfffffffffffffll) | (1ull << 52);
+    if (e < 0) {   // t < 1: the float with the double's exponent and top mantissa bits
+        q = 0;
+        w = e + 127 > 0 ? __int_as_float(((e + 127) << 23) | (int)((m >> 29) & 0x7fffff)) : 0.f;
+        return;
+    }
+    if (e > 52) {   // no fraction bits (cell grids beyond 2^51 quarter cells on an axis)
+        const long long qq = e - 52 < 10 ? (long long)(m << (e - 52)) : LLONG_MAX;
+        q = min(qq, qmax);
+        w = (float)(qq - ((q >> 2) << 2));
+        return;
+    }
+    const int sh = 52 - e;
+    const long long qq = (long long)(m >> sh);
+    q = min(qq, qmax);
+    // remainder as a fixed-point number with sh fraction bits, then its top 24 bits as a float
+    const unsigned long long v = ((unsigned long long)(qq - ((q >> 2) << 2)) << sh) | (m & ((1ull << sh) - 1));
+    if (v == 0) {
+        w = 0.f;
+        return;
+    }
+    const int lz = __clzll((long long)v);
+    const int fe = (63 - lz) - sh + 127;   // biased exponent of v * 2^-sh
+    w = fe > 0 ? __int_as_float((fe << 23) | (int)(((v << lz) >> 40) & 0x7fffff)) : 0.f;
+}
+
 // Sort key: row-major cell index, then (when there is room) the particle's 4 x 4 x 4 sub-cell in
 // Morton order, so that each 32-particle chunk of a crowded cell is spatially compact.  The
 // order of particles inside a cell does not change the partition.  The kernel also writes the
@@ -224,27 +266,27 @@ __global__ void keys_kernel(const double *__restrict__ x, const double *__restri
                             uint64_t *__restrict__ keys, int *__restrict__ vals, float4 *__restrict__ pre) {
     const double s4 = 4.0 * g.inv_cell;   // exact: a power-of-two scaling
     const float cs4 = 0.25f * g.cs;
+    const double bx0 = -g.xmin * s4, by0 = -g.ymin * s4, bz0 = -g.zmin * s4;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        double ox = g.xmin, oy = g.ymin, oz = g.zmin;
+        double bx = bx0, by = by0, bz = bz0;   // -origin * (4 / cell)
         long long x0 = 0, nx = g.ncx, ny = g.ncy, nz = g.ncz;
         if (sg.seg_of) {
             const int s = sg.seg_of[i];
-            ox = sg.smin[3 * s];
-            oy = sg.smin[3 * s + 1];
-            oz = sg.smin[3 * s + 2];
+            bx = -sg.smin[3 * s] * s4;
+            by = -sg.smin[3 * s + 1] * s4;
+            bz = -sg.smin[3 * s + 2] * s4;
             x0 = sg.scol[4 * s];
             nx = sg.scol[4 * s + 1];
             ny = sg.scol[4 * s + 2];
             nz = sg.scol[4 * s + 3];
         }
-        const double tx = fma(x[i], s4, -ox * s4);
-        const double ty = fma(y[i], s4, -oy * s4);
-        const double tz = fma(z[i], s4, -oz * s4);
         // quarter-cell coordinates, clamped to the grid (rounding can put a point on the
-        // grid's edge a hair outside it)
-        const long long qx = min(max(__double2ll_rd(tx), 0ll), 4 * nx - 1);
-        const long long qy = min(max(__double2ll_rd(ty), 0ll), 4 * ny - 1);
-        const long long qz = min(max(__double2ll_rd(tz), 0ll), 4 * nz - 1);
+        // grid's edge a hair outside it), and the position inside the cell in quarter cells
+        long long qx, qy, qz;
+        float wx, wy, wz;
+        quarter_split(fma(x[i], s4, bx), 4 * nx - 1, qx, wx);
+        quarter_split(fma(y[i], s4, by), 4 * ny - 1, qy, wy);
+        quarter_split(fma(z[i], s4, bz), 4 * nz - 1, qz, wz);
         const long long cx = qx >> 2, cy = qy >> 2, cz = qz >> 2;
         uint64_t key = ((uint64_t)(x0 + cx) * (uint64_t)g.ncy + (uint64_t)cy) * (uint64_t)g.ncz + (uint64_t)cz;
         if (g.sb) {
@@ -255,9 +297,7 @@ __global__ void keys_kernel(const double *__restrict__ x, const double *__restri
         }
         keys[i] = key;
         vals[i] = i;
-        // t - 4 * cell is exact (Sterbenz: both within a factor of two, or the cell is 0)
-        pre[i] = make_float4((float)(tx - (double)(cx << 2)) * cs4, (float)(ty - (double)(cy << 2)) * cs4,
-                             (float)(tz - (double)(cz << 2)) * cs4, __int_as_float(i));
+        pre[i] = make_float4(wx * cs4, wy * cs4, wz * cs4, __int_as_float(i));
     }
 }
 
@@ -620,6 +660,16 @@ __global__ void nbmask_kernel(const int *__restrict__ ncell_p, const int *__rest
 // the home cell from the chunk start) and walked 32 at a time, so a sparse region costs one
 // or two rounds of loads per item instead of one per neighbour cell.  Each candidate is moved
 // into the home cell's frame when it is loaded.
+//
+// Segment of a candidate: the non-empty segments are ranked in lane order (a per-warp table
+// maps rank -> segment); in a round, the segments that start inside it set one bit each of a
+// start mask (one OR-reduction), and a candidate's rank is the rank of the round's first
+// segment plus the starts at or before it.
+//
+// Pair tests: the candidates that need a test (within reach of the home chunk's bounding box,
+// not already in the home chunk's set) are tested one at a time against all home particles,
+// or -- when the chunk holds fewer particles than that (sparse cells) -- the home particles
+// one at a time against all those candidates.
 constexpr int kHomeSeg = 13;
 
 __global__ void __launch_bounds__(256, 6) link_kernel(
@@ -628,10 +678,13 @@ __global__ void __launch_bounds__(256, 6) link_kernel(
     const unsigned long long *__restrict__ hmask_p, FofGeom g,
     const double *__restrict__ x, const double *__restrict__ y, const double *__restrict__ z,
     int *parent, unsigned char *has, int *err) {
-    __shared__ float4 buf[kFofWarps][32];
+    __shared__ float4 buf[kFofWarps][32];    // candidates of the round (candidate-major tests)
+    __shared__ float4 hbuf[kFofWarps][32];   // home particles of the item (home-major tests)
     __shared__ int rbuf[kFofWarps][32];
     __shared__ int jbuf[kFofWarps][32];
+    __shared__ int segtab[kFofWarps][16];    // rank of a non-empty segment -> segment (lane)
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const unsigned lt_mask = (1u << lane) - 1u;
     const int nitems = *nitems_p;
     const uint64_t hmask = *hmask_p;
     // items come from a counter: their cost varies by orders of magnitude (dense cores).  The
@@ -653,6 +706,8 @@ __global__ void __launch_bounds__(256, 6) link_kernel(
         const bool hv = k < ce;
         const float4 hp = hv ? rec[k] : make_float4(0.f, 0.f, 0.f, 0.f);
         const int hidx = __float_as_int(hp.w);
+        const unsigned homes = __ballot_sync(0xffffffffu, hv);
+        const int nhome = __popc(homes);
         // lane s < 13 owns stencil cell s, lane 13 the rest of the home cell
         int sjs = 0, sn = 0, soff = 0x15;   // soff: stencil offset + 1 per axis, 2 bits each
         bool sconn = false;                 // the segment's cell is one component
@@ -678,6 +733,12 @@ __global__ void __launch_bounds__(256, 6) link_kernel(
         }
         const int spre = incl - sn;
         const int total = __shfl_sync(0xffffffffu, incl, kHomeSeg);
+        const bool nonempty = lane <= kHomeSeg && sn > 0;
+        const unsigned ne_mask = __ballot_sync(0xffffffffu, nonempty);
+        __syncwarp();
+        if (nonempty) segtab[w][__popc(ne_mask & lt_mask)] = lane;
+        hbuf[w][lane] = hp;
+        __syncwarp();
         // bounding box of the home chunk: a candidate farther than the linking length from it
         // cannot link to any home particle
         float bl[3] = {hv ? hp.x : INFINITY, hv ? hp.y : INFINITY, hv ? hp.z : INFINITY};
@@ -694,17 +755,19 @@ __global__ void __launch_bounds__(256, 6) link_kernel(
         int next = 0;
         for (int v0 = 0; v0 < total; v0 = next) {
             next = v0 + 32;
+            // rank of the segment holding candidate v0, and the segments starting in this round
+            const int rfirst = __popc(__ballot_sync(0xffffffffu, nonempty && spre <= v0)) - 1;
+            const int so = spre - v0;
+            const unsigned starts =
+                __reduce_or_sync(0xffffffffu, (nonempty && so > 0 && so < 32) ? (1u << so) : 0u);
             // a round starting in a neighbour cell that is one component, already in the set of a
             // home chunk that is itself in one set, skips the rest of that cell
             {
-                int seg0 = 0;   // the segment holding candidate v0 (over all 14 segments)
-#pragma unroll
-                for (int s = 0; s <= kHomeSeg; ++s)
-                    if (__shfl_sync(0xffffffffu, spre, s) <= v0) seg0 = s;
+                const int seg0 = segtab[w][rfirst];
                 const int n0 = __shfl_sync(0xffffffffu, sn, seg0);
                 const int js = __shfl_sync(0xffffffffu, sjs, seg0);
                 const int end0 = __shfl_sync(0xffffffffu, spre, seg0) + n0;
-                if (seg0 < kHomeSeg && n0 >= 16 && end0 > v0 && __shfl_sync(0xffffffffu, (int)sconn, seg0)) {
+                if (seg0 < kHomeSeg && n0 >= 16 && __shfl_sync(0xffffffffu, (int)sconn, seg0)) {
                     if (v0 > 0 && hv) myroot = uf_find_cached(parent, k, err);
                     const int r0 = __shfl_sync(0xffffffffu, myroot, 0);
                     if (__all_sync(0xffffffffu, !hv || myroot == r0)) {
@@ -720,12 +783,9 @@ __global__ void __launch_bounds__(256, 6) link_kernel(
             }
             const int v = v0 + lane;
             bool cv = v < total;
-            // segment of candidate v: the last segment starting at or before v (empty
-            // segments share their successor's start and are passed over)
-            int seg = 0;
-#pragma unroll
-            for (int s = 0; s <= kHomeSeg; ++s)
-                if (__shfl_sync(0xffffffffu, spre, s) <= v) seg = s;
+            // candidate v's segment: the round's first segment plus the starts at or before v
+            const unsigned upto = lane == 31 ? 0xffffffffu : ((2u << lane) - 1u);
+            const int seg = segtab[w][rfirst + __popc(starts & upto)];
             const int jl = __shfl_sync(0xffffffffu, sjs, seg) + v - __shfl_sync(0xffffffffu, spre, seg);
             const int off = __shfl_sync(0xffffffffu, soff, seg);
             float4 q = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -750,21 +810,58 @@ __global__ void __launch_bounds__(256, 6) link_kernel(
             // when every home particle is in one set, candidates already in it need no test
             const int r0 = __shfl_sync(0xffffffffu, myroot, 0);   // lane 0 is always a home particle
             const bool uniform = __all_sync(0xffffffffu, !hv || myroot == r0);
-            unsigned todo = __ballot_sync(0xffffffffu, cv && !(uniform && rql == r0));
+            const bool mine = cv && !(uniform && rql == r0);
+            unsigned todo = __ballot_sync(0xffffffffu, mine);
             if (!todo) continue;
+            const int jb = seg == kHomeSeg ? jl : ~jl;   // home-cell candidates keep the j > k test
+            if (__popc(todo) > nhome) {
+                // home-major: each home particle against all candidates of the round
+                unsigned hm = homes;
+                while (hm) {
+                    const int p = __ffs(hm) - 1;
+                    hm &= hm - 1;
+                    const float4 pp = hbuf[w][p];
+                    const int kp = k0 + p;
+                    bool hit = false;
+                    if (mine) {
+                        const float dx = q.x - pp.x, dy = q.y - pp.y, dz = q.z - pp.z;
+                        const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                        hit = d2 <= g.hi && (jb < 0 || jb > kp);
+                        if (hit && d2 >= g.lo) hit = exact_link(x, y, z, __float_as_int(pp.w), __float_as_int(q.w), g.r2);
+                    }
+                    if (!__any_sync(0xffffffffu, hit)) continue;
+                    // the candidates' current roots (a union of an earlier home particle may
+                    // have hooked them) against home particle p's
+                    if (hit) rql = uf_find_cached(parent, rql, err);
+                    const int rp = __shfl_sync(0xffffffffu, myroot, p);
+                    const bool need = hit && rql != rp;
+                    const unsigned nm = __ballot_sync(0xffffffffu, need);
+                    if (!nm) continue;
+                    // one union per distinct candidate root among the lanes that hit
+                    const unsigned peers = __match_any_sync(0xffffffffu, need ? rql : ~lane);
+                    if (need && lane == __ffs(peers) - 1) uf_union(parent, rp, rql, err);
+                    if (need) has[jb < 0 ? ~jb : jb] = 1;
+                    __syncwarp();
+                    if (lane == p) {
+                        has[k] = 1;
+                        myroot = uf_find_cached(parent, k, err);
+                    }
+                }
+                continue;
+            }
             __syncwarp();
             buf[w][lane] = q;
             rbuf[w][lane] = rql;
-            jbuf[w][lane] = seg == kHomeSeg ? jl : ~jl;   // home-cell candidates keep the j > k test
+            jbuf[w][lane] = jb;
             __syncwarp();
             while (todo) {
                 const int t = __ffs(todo) - 1;
                 todo &= todo - 1;
                 const float4 qq = buf[w][t];
-                const int jb = jbuf[w][t];
+                const int jt = jbuf[w][t];
                 const float dx = qq.x - hp.x, dy = qq.y - hp.y, dz = qq.z - hp.z;
                 const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-                bool hit = hv && d2 <= g.hi && (jb < 0 || jb > k);
+                bool hit = hv && d2 <= g.hi && (jt < 0 || jt > k);
                 if (hit && d2 >= g.lo) hit = exact_link(x, y, z, hidx, __float_as_int(qq.w), g.r2);
                 if (!__any_sync(0xffffffffu, hit)) continue;
                 // the candidate's current root (the one read at the start of the round is
@@ -780,7 +877,7 @@ __global__ void __launch_bounds__(256, 6) link_kernel(
                 const unsigned peers = __match_any_sync(0xffffffffu, need ? myroot : ~lane);
                 if (need && lane == __ffs(peers) - 1) uf_union(parent, myroot, rq, err);
                 if (need) has[k] = 1;
-                if (lane == __ffs(nm) - 1) has[jb < 0 ? ~jb : jb] = 1;
+                if (lane == __ffs(nm) - 1) has[jt < 0 ? ~jt : jt] = 1;
                 __syncwarp();
                 if (need) myroot = uf_find_cached(parent, k, err);
             }
@@ -1238,112 +1335,103 @@ extern "C" int halma_fof(int64_t n, const double *x, const double *y, const doub
 namespace halma {
 namespace {
 
-__global__ void group_keys_kernel(int n, const int *__restrict__ labels, uint32_t *__restrict__ keys,
-                                  int *__restrict__ vals) {
+// Members per label (a label is the smallest index of its group), one atomic per distinct
+// label among the lanes of a warp: group members are often neighbours in index order.
+__global__ void group_count_kernel(int n, const int *__restrict__ labels, int *__restrict__ gsize) {
+    const int lane = threadIdx.x & 31;
+    for (int i0 = blockIdx.x * blockDim.x; i0 < n; i0 += gridDim.x * blockDim.x) {
+        const int i = i0 + threadIdx.x;
+        const int l = i < n ? labels[i] : -1;
+        const unsigned peers = __match_any_sync(0xffffffffu, l);
+        if (l >= 0 && lane == __ffs(peers) - 1) atomicAdd(gsize + l, __popc(peers));
+    }
+}
+
+// Per particle: kept (its group has >= minp members) in the low 32 bits and group head (kept,
+// and the smallest index of its group) in the high 32 bits, for one exclusive scan giving every
+// kept particle its position among the kept particles and every group its index: the heads
+// appear in index order, which is the order of the groups' smallest members.
+__global__ void group_flag_kernel(int n, const int *__restrict__ labels, const int *__restrict__ gsize, int minp,
+                                  long long *__restrict__ flags) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const int l = labels[i];
-        keys[i] = l < 0 ? (uint32_t)n : (uint32_t)l;   // particles without a friend sort last
-        vals[i] = i;
+        const bool keep = l >= 0 && gsize[l] >= minp;
+        flags[i] = keep ? (1ll | (l == i ? 1ll << 32 : 0ll)) : 0ll;
     }
 }
 
-__global__ void group_heads_kernel(int n, const uint32_t *__restrict__ keys, int *__restrict__ head) {
-    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x)
-        head[k] = (keys[k] != (uint32_t)n && (k == 0 || keys[k] != keys[k - 1])) ? 1 : 0;
-}
-
-// gstart[gid] = first sorted position of group gid; cnt[0] = groups, cnt[1] = members
-__global__ void group_starts_kernel(int n, const uint32_t *__restrict__ keys, const int *__restrict__ head,
-                                    const int *__restrict__ gid, int *__restrict__ gstart, int *__restrict__ cnt) {
-    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
-        if (head[k]) gstart[gid[k]] = k;
-        const bool valid = keys[k] != (uint32_t)n;
-        const bool last_valid = valid && (k == n - 1 || keys[k + 1] == (uint32_t)n);
-        if (last_valid) {
-            cnt[0] = gid[k] + head[k];
-            cnt[1] = k + 1;
-            gstart[gid[k] + head[k]] = k + 1;
+// Kept particles in index order, keyed by their group's index; the counts go to cnt[2..3]
+// and the member count to offsets[groups].
+__global__ void group_scatter_kernel(int n, const int *__restrict__ labels, const long long *__restrict__ flags,
+                                     const long long *__restrict__ pre, uint32_t *__restrict__ keys,
+                                     int *__restrict__ vals, int *__restrict__ cnt, int64_t *__restrict__ offsets) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const long long f = flags[i];
+        if (f) {
+            const int pos = (int)(pre[i] & 0xffffffffll);
+            keys[pos] = (uint32_t)(pre[labels[i]] >> 32);   // heads before the group's head
+            vals[pos] = i;
+        }
+        if (i == n - 1) {
+            const long long t = pre[i] + f;
+            cnt[2] = (int)(t >> 32);
+            cnt[3] = (int)(t & 0xffffffffll);
+            offsets[t >> 32] = t & 0xffffffffll;
         }
     }
 }
 
-__global__ void group_keep_kernel(int n, const uint32_t *__restrict__ keys, const int *__restrict__ head,
-                                  const int *__restrict__ gid, const int *__restrict__ gstart,
-                                  const int *__restrict__ cnt, int minp, int *__restrict__ keep,
-                                  int *__restrict__ keepg) {
-    const int ng = cnt[0];
-    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
-        int kp = 0;
-        if (keys[k] != (uint32_t)n) {
-            const int g = gid[k] + head[k] - 1;
-            kp = (gstart[g + 1] - gstart[g]) >= minp;
-        }
-        keep[k] = kp;
-        keepg[k] = (k < ng) ? ((gstart[k + 1] - gstart[k]) >= minp) : 0;
-    }
-}
-
-__global__ void group_emit_kernel(int n, const uint32_t *__restrict__ keys, const int *__restrict__ head,
-                                  const int *__restrict__ gid, const int *__restrict__ vals,
-                                  const int *__restrict__ keep, const int *__restrict__ pos,
-                                  const int *__restrict__ keepg, const int *__restrict__ gpos,
-                                  int *__restrict__ members, int64_t *__restrict__ offsets,
-                                  int *__restrict__ cnt) {
-    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
-        if (keep[k]) {
-            members[pos[k]] = vals[k];
-            if (head[k]) offsets[gpos[gid[k]]] = pos[k];
-        }
-        if (k == n - 1) {
-            const int kept_members = pos[k] + keep[k];
-            const int kept_groups = gpos[k] + keepg[k];
-            offsets[kept_groups] = kept_members;
-            cnt[2] = kept_groups;
-            cnt[3] = kept_members;
-        }
-    }
+// Group offsets from the sorted keys: a group starts where its index first appears.
+__global__ void group_offsets_kernel(int nm, const uint32_t *__restrict__ keys, int64_t *__restrict__ offsets) {
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nm; k += gridDim.x * blockDim.x)
+        if (k == 0 || keys[k] != keys[k - 1]) offsets[keys[k]] = k;
 }
 
 }  // namespace
 
-// Groups of >= minp members in the reference order, on device arrays; the counts are
-// returned on the host (one synchronisation).
+// Groups of >= minp members in the reference order, on device arrays: members per label,
+// flags and one scan over the particles (position among the kept, group index), the kept
+// particles keyed by group index in index order, one stable radix sort over the bits of the
+// group count, offsets from the sorted keys.  The counts are returned on the host (one
+// synchronisation, before the sort).
 int fof_groups_device(int n, const int *labels, int minp, int64_t *offsets, int *members,
                       int64_t *n_groups, int64_t *n_members, cudaStream_t st) {
     const size_t sort_b = sort_pairs_u32_i32_bytes(n);
-    const size_t scan_b = exclusive_sum_i32_bytes(n);
+    const size_t scan_b = exclusive_sum_i64_bytes(n);
     Layout L;
-    const size_t o_kin = L.add(4ull * n), o_kout = L.add(4ull * n), o_vin = L.add(4ull * n), o_vout = L.add(4ull * n);
-    const size_t o_head = L.add(4ull * n), o_gid = L.add(4ull * n), o_gst = L.add(4ull * (n + 2));
-    const size_t o_keep = L.add(4ull * n), o_pos = L.add(4ull * n), o_keepg = L.add(4ull * n), o_gpos = L.add(4ull * n);
+    const size_t o_gsize = L.add(4ull * n), o_flag = L.add(8ull * n), o_pre = L.add(8ull * n);
+    const size_t o_kin = L.add(4ull * n), o_kout = L.add(4ull * n), o_vin = L.add(4ull * n);
     const size_t o_cnt = L.add(64), o_tmp = L.add(std::max(sort_b, scan_b));
     void *base = nullptr;
     HALMA_TRY(workspace(L.total, &base, st));
+    auto *gsize = at<int>(base, o_gsize);
+    auto *flags = at<long long>(base, o_flag), *pre = at<long long>(base, o_pre);
     auto *kin = at<uint32_t>(base, o_kin), *kout = at<uint32_t>(base, o_kout);
-    auto *vin = at<int>(base, o_vin), *vout = at<int>(base, o_vout);
-    auto *head = at<int>(base, o_head), *gid = at<int>(base, o_gid), *gst = at<int>(base, o_gst);
-    auto *keep = at<int>(base, o_keep), *pos = at<int>(base, o_pos), *keepg = at<int>(base, o_keepg), *gpos = at<int>(base, o_gpos);
+    auto *vin = at<int>(base, o_vin);
     int *cnt = at<int>(base, o_cnt);
     void *tmp = at<void>(base, o_tmp);
     const int g1 = std::min(device_sm_count() * 8, grid_for(n, 256));
     HALMA_CUDA(cudaMemsetAsync(cnt, 0, 64, st));
-    HALMA_CUDA(cudaMemsetAsync(offsets, 0, sizeof(int64_t), st));
-    HALMA_LAUNCH(group_keys_kernel, g1, 256, 0, st, n, labels, kin, vin);
-    // labels are < n, and n marks a particle without a friend: only the bits of n are sorted
-    HALMA_TRY(sort_pairs_u32_i32(tmp, sort_b, kin, kout, vin, vout, n, bits_for((uint64_t)n), st));
-    HALMA_LAUNCH(group_heads_kernel, g1, 256, 0, st, n, kout, head);
-    HALMA_TRY(exclusive_sum_i32(tmp, scan_b, head, gid, n, st));
-    HALMA_LAUNCH(group_starts_kernel, g1, 256, 0, st, n, kout, head, gid, gst, cnt);
-    HALMA_LAUNCH(group_keep_kernel, g1, 256, 0, st, n, kout, head, gid, gst, cnt, minp, keep, keepg);
-    HALMA_TRY(exclusive_sum_i32(tmp, scan_b, keep, pos, n, st));
-    HALMA_TRY(exclusive_sum_i32(tmp, scan_b, keepg, gpos, n, st));
-    HALMA_LAUNCH(group_emit_kernel, g1, 256, 0, st, n, kout, head, gid, vout, keep, pos, keepg, gpos, members,
-                 offsets, cnt);
+    HALMA_CUDA(cudaMemsetAsync(gsize, 0, 4ull * n, st));
+    HALMA_LAUNCH(group_count_kernel, g1, 256, 0, st, n, labels, gsize);
+    HALMA_LAUNCH(group_flag_kernel, g1, 256, 0, st, n, labels, gsize, std::max(minp, 1), flags);
+    HALMA_TRY(exclusive_sum_i64(tmp, scan_b, reinterpret_cast<const int64_t *>(flags),
+                                reinterpret_cast<int64_t *>(pre), n, st));
+    HALMA_LAUNCH(group_scatter_kernel, g1, 256, 0, st, n, labels, flags, pre, kin, vin, cnt, offsets);
     int hc[4];
     HALMA_CUDA(cudaMemcpyAsync(hc, cnt, sizeof(hc), cudaMemcpyDeviceToHost, st));
     HALMA_CUDA(cudaStreamSynchronize(st));
-    *n_groups = hc[2];
-    if (n_members) *n_members = hc[3];
+    const int ng = hc[2], nm = hc[3];
+    if (nm > 0) {
+        if (ng > 1)
+            HALMA_TRY(sort_pairs_u32_i32(tmp, sort_b, kin, kout, vin, members, nm, bits_for((uint64_t)(ng - 1)), st));
+        else   // one group: already in order
+            HALMA_CUDA(cudaMemcpyAsync(members, vin, 4ull * nm, cudaMemcpyDeviceToDevice, st));
+        HALMA_LAUNCH(group_offsets_kernel, std::min(device_sm_count() * 8, grid_for(nm, 256)), 256, 0, st, nm,
+                     ng > 1 ? kout : kin, offsets);
+    }
+    *n_groups = ng;
+    if (n_members) *n_members = nm;
     return HALMA_OK;
 }
 
