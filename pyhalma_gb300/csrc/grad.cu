@@ -7,9 +7,9 @@
 //   over sources a = s_j, partners b = t_i, weights w_b = g_i:
 //       S_a = sum_b w_b r^-1,  V_a = sum_b w_b (p_b - p_a) r^-3
 //                                                   -> dL/dm_j = S_a, dL/ds_j = m_j * V_a
-// with r^2 = |p_b - p_a|^2 + eps2.  FP32 pair terms (rsqrt), per-chunk FP32 partials folded
-// into TwoSum-compensated accumulators.  The self pair (b == a + self_offset) is skipped when
-// the mask asks for it.
+// with r^2 = |p_b - p_a|^2 + eps2.  FP32 pair terms (rsqrt) as f32x2 instructions (two partners
+// per instruction), per-chunk FP32 partials folded into TwoSum-compensated accumulators.  The
+// self pair (b == a + self_offset) is skipped when the mask asks for it.
 #include <math.h>
 #include <string.h>
 
@@ -29,60 +29,104 @@ __device__ __forceinline__ float4 load_b(const float *__restrict__ x, const floa
     return make_float4(kFarG, kFarG, kFarG, 0.f);
 }
 
+// 32 partners of the staged chunk against the lane's T particles, two partners per f32x2
+// instruction: sa[kp] = {x_2kp, x_2kp+1, y_2kp, y_2kp+1}, sb[kp] = {z.., z.., w.., w..}.  Per
+// pair: r^-1 and w r^-3 (p_b - p_a); the chunk's partials are {even, odd} pairs.  SELF: the
+// pair whose partner index (j0 + slot) equals self[t] is skipped.
+template <int T, bool WANT_S, bool SELF>
+__device__ __forceinline__ void adjoint_chunk(const float4 *sa, const float4 *sb, const f2x (&px)[T],
+                                              const f2x (&py)[T], const f2x (&pz)[T], f2x e2, int64_t j0,
+                                              const int64_t (&self)[T], f2x (&ps)[T], f2x (&pvx)[T],
+                                              f2x (&pvy)[T], f2x (&pvz)[T]) {
+#pragma unroll 4
+    for (int kp = 0; kp < 16; ++kp) {
+        const float4 qa = sa[kp], qb = sb[kp];
+        const f2x X = pack2(qa.x, qa.y), Y = pack2(qa.z, qa.w), Z = pack2(qb.x, qb.y), W = pack2(qb.z, qb.w);
+#pragma unroll
+        for (int t = 0; t < T; ++t) {
+            const f2x dx = sub2(X, px[t]), dy = sub2(Y, py[t]), dz = sub2(Z, pz[t]);
+            f2x r2 = fma2(dz, dz, e2);
+            r2 = fma2(dy, dy, r2);
+            r2 = fma2(dx, dx, r2);
+            float r0, r1;
+            unpack2(r2, r0, r1);
+            float i0 = rsqrt_ftz(r0), i1 = rsqrt_ftz(r1);
+            if (SELF) {
+                if (j0 + 2 * kp == self[t]) i0 = 0.f;
+                if (j0 + 2 * kp + 1 == self[t]) i1 = 0.f;
+            }
+            const f2x ri = pack2(i0, i1);
+            const f2x wr = mul2(W, ri);
+            const f2x wr3 = mul2(mul2(wr, ri), ri);
+            if (WANT_S) ps[t] = add2(ps[t], wr);
+            pvx[t] = fma2(wr3, dx, pvx[t]);
+            pvy[t] = fma2(wr3, dy, pvy[t]);
+            pvz[t] = fma2(wr3, dz, pvz[t]);
+        }
+    }
+}
+
+__device__ __forceinline__ void fold2(float &s, float &c, f2x v) {
+    float lo, hi;
+    unpack2(v, lo, hi);
+    two_sum_acc(s, c, lo + hi);
+}
+
+// One warp per tile of 32*T particles a against all partners b, streamed in chunks of 32
+// through a per-warp shared buffer; chunk partials folded into TwoSum-compensated sums.
 template <int T, bool WANT_S>
-__global__ void __launch_bounds__(256) adjoint_kernel(
+__global__ void __launch_bounds__(256, 3) adjoint_kernel(
     const float *__restrict__ bx, const float *__restrict__ by, const float *__restrict__ bz,
     const float *__restrict__ bw, int64_t nb, const float *__restrict__ ax, const float *__restrict__ ay,
     const float *__restrict__ az, int64_t na, float eps2, int self_mask, int64_t self_off,
     const float *__restrict__ vscale, float *__restrict__ out_s, float *__restrict__ out_v) {
     __shared__ float4 buf[kGWarps][32];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    float *sa = reinterpret_cast<float *>(buf[w]);        // 16 float4: x/y pairs
+    float *sb = reinterpret_cast<float *>(buf[w] + 16);   // 16 float4: z/w pairs
+    const int kp = lane >> 1, hf = lane & 1;
+    const f2x e2 = pack2(eps2, eps2);
     const int64_t ntiles = (na + 32 * T - 1) / (32 * T);
     for (int64_t tile = (int64_t)blockIdx.x * kGWarps + w; tile < ntiles; tile += (int64_t)gridDim.x * kGWarps) {
-        float px[T], py[T], pz[T];
+        f2x px[T], py[T], pz[T];
         float ss[T], sc[T], vxs[T], vxc[T], vys[T], vyc[T], vzs[T], vzc[T];
         int64_t self[T];
 #pragma unroll
         for (int t = 0; t < T; ++t) {
             const int64_t a = tile * 32 * T + t * 32 + lane;
             const bool v = a < na;
-            px[t] = v ? ax[a] : kFarG;
-            py[t] = v ? ay[a] : kFarG;
-            pz[t] = v ? az[a] : kFarG;
+            const float x = v ? ax[a] : kFarG, y = v ? ay[a] : kFarG, z = v ? az[a] : kFarG;
+            px[t] = pack2(x, x);
+            py[t] = pack2(y, y);
+            pz[t] = pack2(z, z);
             self[t] = (v && self_mask) ? a + self_off : -1;
             ss[t] = sc[t] = vxs[t] = vxc[t] = vys[t] = vyc[t] = vzs[t] = vzc[t] = 0.f;
         }
+        // partner indices self[t] lie in [lo_self, lo_self + 32 * T) for this tile
+        const int64_t lo_self = tile * 32 * T + self_off;
         float4 nxt = load_b(bx, by, bz, bw, lane, nb);
         for (int64_t j0 = 0; j0 < nb; j0 += 32) {
             __syncwarp();
-            buf[w][lane] = nxt;
+            sa[kp * 4 + hf] = nxt.x;
+            sa[kp * 4 + 2 + hf] = nxt.y;
+            sb[kp * 4 + hf] = nxt.z;
+            sb[kp * 4 + 2 + hf] = nxt.w;
             __syncwarp();
             nxt = load_b(bx, by, bz, bw, j0 + 32 + lane, nb);
-            float ps[T], pvx[T], pvy[T], pvz[T];
+            f2x ps[T], pvx[T], pvy[T], pvz[T];
 #pragma unroll
-            for (int t = 0; t < T; ++t) ps[t] = pvx[t] = pvy[t] = pvz[t] = 0.f;
-            for (int k = 0; k < 32; ++k) {
-                const float4 q = buf[w][k];
-#pragma unroll
-                for (int t = 0; t < T; ++t) {
-                    const float dx = q.x - px[t], dy = q.y - py[t], dz = q.z - pz[t];
-                    const float r2 = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, eps2)));
-                    float ri = rsqrtf(r2);
-                    if (j0 + k == self[t]) ri = 0.f;
-                    const float wr = q.w * ri;
-                    const float wr3 = wr * ri * ri;
-                    if (WANT_S) ps[t] += wr;
-                    pvx[t] = fmaf(wr3, dx, pvx[t]);
-                    pvy[t] = fmaf(wr3, dy, pvy[t]);
-                    pvz[t] = fmaf(wr3, dz, pvz[t]);
-                }
-            }
+            for (int t = 0; t < T; ++t) ps[t] = pvx[t] = pvy[t] = pvz[t] = pack2(0.f, 0.f);
+            const bool self_chunk = self_mask && j0 + 32 > lo_self && j0 < lo_self + 32 * T;
+            if (self_chunk)
+                adjoint_chunk<T, WANT_S, true>(buf[w], buf[w] + 16, px, py, pz, e2, j0, self, ps, pvx, pvy, pvz);
+            else
+                adjoint_chunk<T, WANT_S, false>(buf[w], buf[w] + 16, px, py, pz, e2, j0, self, ps, pvx, pvy, pvz);
 #pragma unroll
             for (int t = 0; t < T; ++t) {
-                if (WANT_S) two_sum_acc(ss[t], sc[t], ps[t]);
-                two_sum_acc(vxs[t], vxc[t], pvx[t]);
-                two_sum_acc(vys[t], vyc[t], pvy[t]);
-                two_sum_acc(vzs[t], vzc[t], pvz[t]);
+                if (WANT_S) fold2(ss[t], sc[t], ps[t]);
+                fold2(vxs[t], vxc[t], pvx[t]);
+                fold2(vys[t], vyc[t], pvy[t]);
+                fold2(vzs[t], vzc[t], pvz[t]);
             }
         }
 #pragma unroll

@@ -67,6 +67,26 @@ int inclusive_max_i32(void *tmp, size_t tmp_bytes, const int32_t *in, int32_t *o
     return HALMA_OK;
 }
 
+namespace {
+struct Int3Sum {
+    __device__ __forceinline__ int4 operator()(const int4 &a, const int4 &b) const {
+        return make_int4(a.x + b.x, a.y + b.y, a.z + b.z, 0);
+    }
+};
+}  // namespace
+
+size_t exclusive_sum_int3_bytes(int n) {
+    size_t b = 0;
+    cub::DeviceScan::ExclusiveScan(nullptr, b, (const int4 *)nullptr, (int4 *)nullptr, Int3Sum{},
+                                   make_int4(0, 0, 0, 0), n);
+    return b;
+}
+
+int exclusive_sum_int3(void *tmp, size_t tmp_bytes, const int4 *in, int4 *out, int n, cudaStream_t s) {
+    HALMA_CUDA(cub::DeviceScan::ExclusiveScan(tmp, tmp_bytes, in, out, Int3Sum{}, make_int4(0, 0, 0, 0), n, s));
+    return HALMA_OK;
+}
+
 size_t exclusive_sum_i32_bytes(int n) {
     size_t b = 0;
     cub::DeviceScan::ExclusiveSum(nullptr, b, (const int32_t *)nullptr, (int32_t *)nullptr, n);

@@ -18,6 +18,9 @@ size_t exclusive_sum_i64_bytes(int n);
 int exclusive_sum_i64(void *tmp, size_t tmp_bytes, const int64_t *in, int64_t *out, int n, cudaStream_t s);
 size_t inclusive_max_i32_bytes(int n);
 int inclusive_max_i32(void *tmp, size_t tmp_bytes, const int32_t *in, int32_t *out, int n, cudaStream_t s);
+// Exclusive prefix sums of the x, y and z fields of int4 values at once (w is ignored, set to 0).
+size_t exclusive_sum_int3_bytes(int n);
+int exclusive_sum_int3(void *tmp, size_t tmp_bytes, const int4 *in, int4 *out, int n, cudaStream_t s);
 size_t exclusive_sum_i32_bytes(int n);
 int exclusive_sum_i32(void *tmp, size_t tmp_bytes, const int32_t *in, int32_t *out, int n,
                       cudaStream_t s);

@@ -26,6 +26,7 @@
 
 #include "common.cuh"
 #include "pair_math.cuh"
+#include "sort.cuh"
 #include "unbind.cuh"
 
 namespace halma {
@@ -262,26 +263,23 @@ __device__ __forceinline__ int warp_incl_scan(int v, int lane) {
 constexpr int kSymWarps = 4, kSymT = 8;
 constexpr int kSymBlock = kSymWarps * 32 * kSymT;   // 1024 slots
 
-__global__ void __launch_bounds__(1024) ub_items_kernel(int nh, const int *__restrict__ order, const HaloState *hs,
-                                                        TileTable tab, int slice_len, int inc, int sym_ok,
-                                                        int *__restrict__ istart, int *__restrict__ ystart,
-                                                        int4 *__restrict__ idesc, int *__restrict__ sstart,
-                                                        int *__restrict__ sown, int *__restrict__ cnt,
-                                                        unsigned long long *__restrict__ pairs_out) {
-    __shared__ int wsum[32], wseg[32], wsym[32];
-    __shared__ int base, sbase, ybase;
-    __shared__ unsigned long long pairs, spairs;
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    if (threadIdx.x == 0) {
-        base = 0;
-        sbase = 0;
-        ybase = 0;
-        pairs = 0;
-        spairs = 0;
-    }
-    __syncthreads();
-    for (int h0 = 0; h0 < nh; h0 += blockDim.x) {
-        const int q = h0 + threadIdx.x;
+// The pass's work list, built in three steps over the haloes in size order (q):
+//   count - per halo q: its halo h, tile shape, source slices, and three counts: warp items
+//           (tiles x slices), energy segments, symmetric block-pair items (0 unless active);
+//   scan  - exclusive prefix sums of the three counts (CUB);
+//   fill  - the prefix sums become istart / sstart / ystart, every segment records its owner
+//           (sown), and the totals go to cnt[] (warp items, energy segments, block-pair items,
+//           their counters reset) and to the last entries of the start arrays.
+// With pairs_out (profiling), the pass's pair terms (nb x sources, all haloes) and those of the
+// haloes on the symmetric block kernel are summed into pairs_out[0..1] (zeroed beforehand).
+__global__ void __launch_bounds__(256) ub_items_count_kernel(int nh, const int *__restrict__ order,
+                                                             const HaloState *hs, TileTable tab, int slice_len,
+                                                             int inc, int sym_ok, int4 *__restrict__ counts,
+                                                             int4 *__restrict__ idesc,
+                                                             unsigned long long *__restrict__ pairs_out) {
+    const int lane = threadIdx.x & 31;
+    for (int q0 = blockIdx.x * blockDim.x; q0 < nh; q0 += gridDim.x * blockDim.x) {
+        const int q = q0 + threadIdx.x;
         int h = -1, n = 0, T = 4, nsl = 1, nseg = 0, ny = 0, nsl_e = 0;
         unsigned long long my_pairs = 0, my_spairs = 0;
         if (q < nh) {
@@ -303,66 +301,41 @@ __global__ void __launch_bounds__(1024) ub_items_kernel(int nh, const int *__res
                 nseg = max(1, (nb + kSeg - 1) / kSeg);
                 my_pairs = (unsigned long long)nb * (unsigned long long)ns;
             }
+            counts[q] = make_int4(n, nseg, ny, 0);
+            idesc[q] = make_int4(h, T, max(nsl, 1), nsl_e);
         }
-        if (pairs_out) {   // pair counts for the profile: one shared atomic per warp
+        if (pairs_out) {   // one atomic per warp
             for (int o = 16; o > 0; o >>= 1) {
                 my_pairs += __shfl_xor_sync(0xffffffffu, my_pairs, o);
                 my_spairs += __shfl_xor_sync(0xffffffffu, my_spairs, o);
             }
-            if (lane == 0) {
-                atomicAdd(&pairs, my_pairs);
-                atomicAdd(&spairs, my_spairs);
+            if (lane == 0 && (my_pairs | my_spairs)) {
+                atomicAdd(pairs_out, my_pairs);
+                atomicAdd(pairs_out + 1, my_spairs);
             }
         }
-        const int incl = warp_incl_scan(n, lane);
-        const int sincl = warp_incl_scan(nseg, lane);
-        const int yincl = warp_incl_scan(ny, lane);
-        if (lane == 31) {
-            wsum[w] = incl;
-            wseg[w] = sincl;
-            wsym[w] = yincl;
-        }
-        __syncthreads();
-        int pre = base, spre = sbase, ypre = ybase;
-        for (int k = 0; k < w; ++k) {
-            pre += wsum[k];
-            spre += wseg[k];
-            ypre += wsym[k];
-        }
-        if (q < nh) {
-            istart[q] = pre + incl - n;
-            ystart[q] = ypre + yincl - ny;
-            idesc[q] = make_int4(h, T, max(nsl, 1), nsl_e);
-            const int s0 = spre + sincl - nseg;
-            sstart[q] = s0;
-            for (int sg = 0; sg < nseg; ++sg) sown[s0 + sg] = q;
-        }
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            int tot = 0, stot = 0, ytot = 0;
-            for (int k = 0; k < (int)(blockDim.x >> 5); ++k) {
-                tot += wsum[k];
-                stot += wseg[k];
-                ytot += wsym[k];
-            }
-            base += tot;
-            sbase += stot;
-            ybase += ytot;
-        }
-        __syncthreads();
     }
-    if (threadIdx.x == 0) {
-        istart[nh] = base;
-        sstart[nh] = sbase;
-        ystart[nh] = ybase;
-        cnt[0] = base;    // warp items
-        cnt[1] = 0;       // their counter
-        cnt[2] = sbase;   // energy segments
-        cnt[3] = ybase;   // symmetric block items
-        cnt[4] = 0;       // their counter
-        if (pairs_out) {
-            pairs_out[0] = pairs;    // pair terms of the pass (nb x sources, every halo)
-            pairs_out[1] = spairs;   // of which in haloes on the symmetric block kernel
+}
+
+__global__ void __launch_bounds__(256) ub_items_fill_kernel(int nh, const int4 *__restrict__ counts,
+                                                            const int4 *__restrict__ pre, int *__restrict__ istart,
+                                                            int *__restrict__ ystart, int *__restrict__ sstart,
+                                                            int *__restrict__ sown, int *__restrict__ cnt) {
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < nh; q += gridDim.x * blockDim.x) {
+        const int4 c = counts[q], p = pre[q];
+        istart[q] = p.x;
+        sstart[q] = p.y;
+        ystart[q] = p.z;
+        for (int sg = 0; sg < c.y; ++sg) sown[p.y + sg] = q;
+        if (q == nh - 1) {
+            istart[nh] = p.x + c.x;
+            sstart[nh] = p.y + c.y;
+            ystart[nh] = p.z + c.z;
+            cnt[0] = p.x + c.x;   // warp items
+            cnt[1] = 0;           // their counter
+            cnt[2] = p.y + c.y;   // energy segments
+            cnt[3] = p.z + c.z;   // symmetric block items
+            cnt[4] = 0;           // their counter
         }
     }
 }
@@ -1427,6 +1400,9 @@ int unbind_device(int64_t n, int nh, const int64_t *d_off, const int64_t *h_off,
     const size_t o_pairs = L.add(sizeof(unsigned long long) * 2 * p.max_iter);
     const size_t o_ystart = L.add(sizeof(int) * (nh + 1));
     const size_t o_off = d_off ? 0 : L.add(sizeof(int64_t) * (nh + 1));
+    const size_t o_icnt = L.add(sizeof(int4) * std::max(nh, 1)), o_ipre = L.add(sizeof(int4) * std::max(nh, 1));
+    const size_t iscan_bytes = exclusive_sum_int3_bytes(std::max(nh, 1));
+    const size_t o_iscan = L.add(iscan_bytes);
     void *base = nullptr;
     HALMA_TRY(workspace(L.total, &base, st));
     auto *hs = at<HaloState>(base, o_hs);
@@ -1471,6 +1447,18 @@ int unbind_device(int64_t n, int nh, const int64_t *d_off, const int64_t *h_off,
     if (nchunks > 0)
         HALMA_CUDA(cudaMemcpyAsync(dchh, chunk_h.data(), sizeof(int) * nchunks, cudaMemcpyHostToDevice, st));
     const int fgrid = grid_for((int64_t)nh * 32, 256);   // one warp per halo
+    // the pass's work list (count, scan, fill; see ub_items_count_kernel)
+    auto *icount = at<int4>(base, o_icnt), *ipre = at<int4>(base, o_ipre);
+    void *iscan_tmp = at<void>(base, o_iscan);
+    const int igrid = std::min(grid_for(nh, 256), device_sm_count() * 4);
+    auto items = [&](cudaStream_t rs, int inc, int sym_ok, unsigned long long *pairs) -> int {
+        if (pairs) HALMA_CUDA(cudaMemsetAsync(pairs, 0, 2 * sizeof(unsigned long long), rs));
+        HALMA_LAUNCH(ub_items_count_kernel, igrid, 256, 0, rs, nh, dorder, hs, tab, slice_len, inc, sym_ok, icount,
+                     idesc, pairs);
+        HALMA_TRY(exclusive_sum_int3(iscan_tmp, iscan_bytes, icount, ipre, nh, rs));
+        HALMA_LAUNCH(ub_items_fill_kernel, igrid, 256, 0, rs, nh, icount, ipre, istart, ystart, sstart, sown, cnt);
+        return HALMA_OK;
+    };
     // FP64 bound mass, centre and bulk velocity per halo (active ones, or all with force)
     auto reduce = [&](cudaStream_t rs, int force) -> int {
         if (nchunks > 0)
@@ -1512,8 +1500,7 @@ int unbind_device(int64_t n, int nh, const int64_t *d_off, const int64_t *h_off,
             for (int it = it0; it < it1; ++it) {
                 const int a = it & 1, b = a ^ 1;
                 const int inc = (it > 0 && incremental) ? 1 : 0;
-                HALMA_LAUNCH(ub_items_kernel, 1, 1024, 0, rs, nh, dorder, hs, tab, slice_len, inc, 1, istart, ystart,
-                             idesc, sstart, sown, cnt, profiling ? dpairs + 2 * it : nullptr);
+                HALMA_TRY(items(rs, inc, 1, profiling ? dpairs + 2 * it : nullptr));
                 // External: captured as an event-record node, so the replay records it
                 if (profiling) HALMA_CUDA(cudaEventRecordWithFlags(prof.ev0[it], rs, cudaEventRecordExternal));
                 // full passes: the big haloes' block pairs first (the longest items), then the
@@ -1631,8 +1618,7 @@ int unbind_device(int64_t n, int nh, const int64_t *d_off, const int64_t *h_off,
         double4 *rk = at<double4>(base, o_rk);
         for (int it = 0; it < p.max_iter; ++it) {
             const int a = it & 1, b = a ^ 1;
-            HALMA_LAUNCH(ub_items_kernel, 1, 1024, 0, st, nh, dorder, hs, tab, slice_len, 0, 0, istart, ystart, idesc,
-                         sstart, sown, cnt, nullptr);
+            HALMA_TRY(items(st, 0, 0, nullptr));
             HALMA_CUDA(cudaMemcpyAsync(hh.data(), hs, sizeof(HaloState) * nh, cudaMemcpyDeviceToHost, st));
             HALMA_CUDA(cudaStreamSynchronize(st));
             int any = 0;
