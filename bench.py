@@ -449,6 +449,8 @@ def run_gpu(args):
     stream = torch.cuda.current_stream()
     # the FP32 pipe's peak on this GPU: packed and scalar FMA chains, the faster one
     fp32_peak = max(_lib.measure_fp32_fma_rate(packed=True)[0], _lib.measure_fp32_fma_rate(packed=False)[0])
+    # the ceiling of the pair arithmetic itself (FP32 pipe and special-function unit together)
+    pair_ceiling = _lib.measure_pair_rate()[0]
 
     def barrier():
         torch.cuda.synchronize()
@@ -508,17 +510,22 @@ def run_gpu(args):
 
     # end to end through the C ABI from pinned host buffers (copies inside the timed region)
     _lib.set_profiling(False)
-    e2e_ms = []
+    e2e_ms, e2e_wall = [], []
+    sampler_e2e = ClockSampler(local)
+    sampler_e2e.start()
     for k in range(args.warmup + args.steps):
         flush.zero_()
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        w0 = time.perf_counter()
         e0.record(stream)
         hc = find_haloes(*pinned_np, ll, w["min_members"], options=opt)
         e1.record(stream)
         e1.synchronize()
         if k >= args.warmup:
             e2e_ms.append(e0.elapsed_time(e1))
+            e2e_wall.append((time.perf_counter() - w0) * 1e3)
+    clocks_e2e = sampler_e2e.stop()
     ng = hc.n_haloes
     nm = int(hc.offsets[-1]) if ng else 0
     h2d = 7 * 8 * n
@@ -571,7 +578,16 @@ def run_gpu(args):
                 "peak_source": peak_note, "fp32_pipe_frac": sym_pipe,
                 "pair_terms_per_launch": sym_pairs / max(sym_launches, 1),
                 "ms_per_launch": sym_ms / max(sym_launches, 1), "launches_timed": sym_launches,
-                "pair_terms_per_s": sym_pairs / (sym_ms * 1e-3) if sym_ms > 0 else 0.0}
+                "pair_terms_per_s": sym_pairs / (sym_ms * 1e-3) if sym_ms > 0 else 0.0,
+                "pair_arithmetic_ceiling": {
+                    "pairs_per_s": pair_ceiling,
+                    "kernel_pairs_per_s": sym_pairs / 2 / (sym_ms * 1e-3) if sym_ms > 0 else 0.0,
+                    "frac": (sym_pairs / 2 / (sym_ms * 1e-3)) / pair_ceiling if sym_ms > 0 and pair_ceiling else None,
+                    "note": "measured in the same run by the library's pair-arithmetic kernel "
+                            "(halma_measure_pair_rate: the block kernel's per-pair f32x2 sub/fma and rsqrt from "
+                            "shared memory, no reductions or bookkeeping, full occupancy); the mix needs the FP32 "
+                            "pipe (8 lane-ops per pair) and the special-function unit (1 rsqrt per pair) each at "
+                            "its throughput, so this, not the FP32 peak, is the kernel's practical ceiling"}}
     roofline_pairs = {"bound": "fp32", "kernel": "ub_pair_sym_kernel + ub_pair_kernel (every pass)",
                       "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
                       "frac": achieved / fp32_peak if fp32_peak else None,
@@ -599,7 +615,9 @@ def run_gpu(args):
             "pair_interactions_per_s": pairs / (sum(ms) * 1e-3) * world,
             "roofline": roofline, "roofline_pair_kernels": roofline_pairs, "roofline_fof": roofline_fof,
             "e2e": {"value": n * world / (e2e_step * 1e-3), "unit": "particles/s", "h2d_bytes_per_step": h2d,
-                    "d2h_bytes_per_step": d2h, "ms_per_step": e2e_step},
+                    "d2h_bytes_per_step": d2h, "ms_per_step": e2e_step,
+                    "steps_ms": [round(v, 2) for v in e2e_ms], "wall_ms_per_step": statistics.mean(e2e_wall),
+                    "clocks": clocks_e2e},
             "gpu_launches": launches, "clocks": clocks, "fp64_path": fp64, "wall_s_timed": wall}
     if rank == 0 and world == 1 and not args.skip_cpu:
         import oracle

@@ -95,6 +95,14 @@ int         halma_profile_fof_stages(double *out, int32_t cap);
  * as two flops.  The roofline denominator of the CUDA-core pair kernels. */
 int         halma_measure_fp32_fma_rate(int32_t packed, int32_t iters, double *tflops, double *ms,
                                         halma_stream_t stream);
+/* Measurement hook (no reference counterpart): the rate of the pair kernels' arithmetic alone
+ * on the current device -- per pair of particles 3 sub + 3 fma + 2 fma as f32x2 instructions
+ * and one rsqrt, sources from shared memory, 8 targets per lane, at the occupancy its registers
+ * allow -- in pairs per second (each pair gives one term to each particle), fastest of three
+ * timed launches after one warm-up.  This mix loads the FP32 pipe and the special-function
+ * unit both to their throughput, so its rate, not either peak alone, is the ceiling of the
+ * symmetric block kernel. */
+int         halma_measure_pair_rate(int32_t iters, double *pairs_per_s, double *ms, halma_stream_t stream);
 /* Debug knob (no reference counterpart): the iteration bound of every union-find loop of the
  * FoF kernels (find walks, CAS retries).  A loop that reaches it stops, and the FoF call
  * returns HALMA_ERR_NOT_CONVERGED with the device still usable.  cap < 0 restores the default

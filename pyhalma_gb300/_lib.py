@@ -91,6 +91,7 @@ SIGNATURES = {
     "halma_set_union_find_cap": ([_I32], ctypes.c_int),
     "halma_profile_fof_stages": ([_P, _I32], ctypes.c_int),
     "halma_measure_fp32_fma_rate": ([_I32, _I32, _P, _P, _P], ctypes.c_int),
+    "halma_measure_pair_rate": ([_I32, _P, _P, _P], ctypes.c_int),
     "halma_fof": ([_I64, _P, _P, _P, _F64, _P, _P, _P], ctypes.c_int),
     "halma_fof_groups": ([_I64, _P, _I32, _P, _P, _P, _P], ctypes.c_int),
     "halma_fof_segmented": ([_I64, _P, _P, _P, _I64, _P, _F64, _P, _P, _P], ctypes.c_int),
@@ -178,6 +179,14 @@ def measure_fp32_fma_rate(packed=True, iters=1 << 15):
     return t.value, ms.value
 
 
+def measure_pair_rate(iters=1 << 12):
+    """(pairs/s, ms) of the pair-arithmetic ceiling kernel on the current device."""
+    r, ms = ctypes.c_double(0), ctypes.c_double(0)
+    check(lib().halma_measure_pair_rate(int(iters), ctypes.byref(r), ctypes.byref(ms), None),
+          "halma_measure_pair_rate")
+    return r.value, ms.value
+
+
 def profile_fof_stages():
     """Milliseconds of each FoF stage of the last find_haloes call (profiling on)."""
     buf = np.zeros(len(FOF_STAGES))
@@ -217,6 +226,24 @@ def stream_of(*arrays):
 def as_host(a, dtype):
     """Contiguous NumPy array of the given dtype (copy only when needed)."""
     return np.ascontiguousarray(a, dtype=dtype)
+
+
+def pinned_empty(shape, dtype):
+    """An uninitialised NumPy array in page-locked host memory from torch's caching pinned
+    allocator (plain np.empty without torch or a CUDA device).  Device-to-host copies into it
+    are DMA transfers with no CPU memcpy; a pageable destination makes the driver copy through
+    staging buffers on the host and fault fresh pages in, whose cost depends on the host's
+    other load.  The block goes back to torch's cache when the array is released, so repeated
+    calls of the same size allocate nothing."""
+    try:
+        import torch
+        if not torch.cuda.is_available():
+            raise ImportError
+    except ImportError:
+        return np.empty(shape, dtype=dtype)
+    tmap = {np.float32: torch.float32, np.float64: torch.float64, np.int32: torch.int32,
+            np.int64: torch.int64, np.uint8: torch.uint8}
+    return torch.empty(shape, dtype=tmap[np.dtype(dtype).type], pin_memory=True).numpy()
 
 
 def like(a, shape, dtype):

@@ -5,6 +5,8 @@
 #include <string.h>
 
 #include <map>
+#include <string>
+#include <thread>
 
 #include "common.cuh"
 #include "unbind.cuh"
@@ -35,11 +37,14 @@ __global__ void scatter_bound_kernel(int64_t nm, const int *__restrict__ members
         bound[members[k]] = bs[k];
 }
 
-// A second stream (and its completion event) per device, for the host-to-device copies of the
-// velocities and masses, which overlap the FoF stage (it reads positions only).
+// A second stream per device, for the host-to-device copies of the velocities and masses,
+// which overlap the FoF stage (it reads positions only), and for the copies of the labels and
+// the groups to the caller, which overlap the unbinding.  `done` marks the end of the uploads,
+// `groups` the point where the labels and the groups are final.
 struct SideStream {
     cudaStream_t s = nullptr;
     cudaEvent_t done = nullptr;
+    cudaEvent_t groups = nullptr;
 };
 
 int side_stream(SideStream **out) {
@@ -48,10 +53,41 @@ int side_stream(SideStream **out) {
     if (!ss.s) {
         HALMA_CUDA(cudaStreamCreateWithFlags(&ss.s, cudaStreamNonBlocking));
         HALMA_CUDA(cudaEventCreateWithFlags(&ss.done, cudaEventDisableTiming));
+        HALMA_CUDA(cudaEventCreateWithFlags(&ss.groups, cudaEventDisableTiming));
     }
     *out = &ss;
     return HALMA_OK;
 }
+
+// One output of the early copies: caller's destination, device source, bytes.
+struct OutCopy {
+    void *user;
+    const void *dev;
+    size_t bytes;
+};
+
+// The labels and the groups to the caller's buffers (host or device) on the side stream once
+// `groups` has fired, waiting for the copies to end.  Runs on a helper thread while the
+// calling thread drives the unbinding: a copy to pageable host memory returns only when it is
+// complete.  (Staging them through pinned memory and a CPU memcpy measured far slower: the
+// driver's own pageable path writes fresh pages much faster than a memcpy that faults them in.)
+int copy_groups_out(int dev, SideStream *side, const OutCopy *outs, int nout) {
+    HALMA_CUDA(cudaSetDevice(dev));
+    HALMA_CUDA(cudaStreamWaitEvent(side->s, side->groups, 0));
+    for (int k = 0; k < nout; ++k)
+        if (outs[k].user && outs[k].bytes)
+            HALMA_CUDA(cudaMemcpyAsync(outs[k].user, outs[k].dev, outs[k].bytes, cudaMemcpyDefault, side->s));
+    HALMA_CUDA(cudaStreamSynchronize(side->s));
+    return HALMA_OK;
+}
+
+// Joins a helper thread on every way out of the scope that started it.
+struct JoinOnExit {
+    std::thread &t;
+    ~JoinOnExit() {
+        if (t.joinable()) t.join();
+    }
+};
 
 }  // namespace
 }  // namespace halma
@@ -131,6 +167,21 @@ extern "C" int halma_find_haloes(int64_t n, const double *x, const double *y, co
     HALMA_TRY(prof.fof_mark(Profile::kFofStages, st));
     if (prof.enabled) HALMA_CUDA(cudaEventRecord(ev[1], st));
     *n_haloes = ng;
+    // the labels and the groups are final: their copies to the caller run during the unbinding
+    const bool fits = !(ng > halo_capacity && (halo_offsets || halo_out));
+    int early_status = HALMA_OK;
+    std::string early_msg;
+    std::thread early;
+    JoinOnExit join_early{early};
+    const OutCopy outs[3] = {{labels, dlab, 4ull * n}, {halo_offsets, doff, 8ull * (ng + 1)}, {members, dmem, 4ull * nm}};
+    if (fits) {
+        HALMA_CUDA(cudaEventRecord(side->groups, st));
+        const int dev = current_device();
+        early = std::thread([&, dev]() {
+            early_status = copy_groups_out(dev, side, outs, 3);
+            if (early_status != HALMA_OK) early_msg = halma_last_error();
+        });
+    }
     HALMA_CUDA(cudaMemsetAsync(dbnd, 0, n, st));
     HALMA_CUDA(cudaStreamWaitEvent(st, side->done, 0));
     if (ng > 0) {
@@ -165,16 +216,16 @@ extern "C" int halma_find_haloes(int64_t n, const double *x, const double *y, co
         HALMA_CUDA(cudaMemcpyAsync(user, dev, bytes, cudaMemcpyDefault, st));
         return HALMA_OK;
     };
-    HALMA_TRY(put(labels, dlab, 4ull * n));
     HALMA_TRY(put(bound, dbnd, 1ull * n));
-    if (ng > halo_capacity && (halo_offsets || halo_out)) {
+    if (!fits) {
+        HALMA_TRY(put(labels, dlab, 4ull * n));
         HALMA_CUDA(cudaStreamSynchronize(st));
         return fail(HALMA_ERR_CAPACITY, "%lld haloes found, capacity %lld", (long long)ng, (long long)halo_capacity);
     }
-    HALMA_TRY(put(halo_offsets, doff, 8ull * (ng + 1)));
-    HALMA_TRY(put(members, dmem, 4ull * nm));
     HALMA_TRY(put(halo_out, dhalo, 8ull * HALMA_UB_NFIELDS * ng));
     HALMA_CUDA(cudaStreamSynchronize(st));
+    early.join();
+    if (early_status != HALMA_OK) return fail(early_status, "%s", early_msg.c_str());
     return HALMA_OK;
 }
 

@@ -109,11 +109,13 @@ def find_haloes(st_x, st_y, st_z, st_vx, st_vy, st_vz, st_mass, linking_length, 
         arrs = tuple(_lib.as_host(a, np.float64) for a in (st_x, st_y, st_z, st_vx, st_vy, st_vz, st_mass))
         n = arrs[0].shape[0]
     cap = max(n // max(int(minp), 2) + 1, 1)
-    labels = _lib.like(arrs[0], (n,), np.int32)
-    bound = _lib.like(arrs[0], (n,), np.uint8)
-    offsets = _lib.like(arrs[0], (cap + 1,), np.int64)
-    members = _lib.like(arrs[0], (max(n, 1),), np.int32)
-    haloes = _lib.like(arrs[0], (cap, len(_lib.UB_FIELDS)), np.float64)
+    # host outputs in pinned memory: their copies are DMA transfers that overlap the unbinding
+    out = _lib.like if dev else (lambda a, shape, dtype: _lib.pinned_empty(shape, dtype))
+    labels = out(arrs[0], (n,), np.int32)
+    bound = out(arrs[0], (n,), np.uint8)
+    offsets = out(arrs[0], (cap + 1,), np.int64)
+    members = out(arrs[0], (max(n, 1),), np.int32)
+    haloes = out(arrs[0], (cap, len(_lib.UB_FIELDS)), np.float64)
     nh = ctypes.c_int64(0)
     p = opt.params()
     st = _lib.lib().halma_find_haloes(n, *[_lib.ptr(a) for a in arrs], float(linking_length), int(minp),
