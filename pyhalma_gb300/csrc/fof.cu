@@ -81,6 +81,24 @@ __device__ __forceinline__ int uf_find(int *parent, int v, int *err) {
     return v;
 }
 
+// The cached walk below, continued from p = parent[v] loaded earlier (so that the caller can
+// issue that load next to other independent ones).
+__device__ __forceinline__ int uf_find_from(int *parent, int v, int p, int *err) {
+    int guard = 0;
+    const int cap = c_uf_cap;
+    while (p != v) {
+        const int gp = parent[p];
+        if (gp != p) __stcg(parent + v, gp);
+        v = p;
+        p = gp;
+        if (++guard > cap) {
+            atomicOr(err, 1);
+            break;
+        }
+    }
+    return v;
+}
+
 // Same walk with L1-cached loads, for the linking kernel.  A value read from L1 may be older
 // than the one in L2 (another SM hooked or compressed since), which is harmless there: an
 // older parent is still an ancestor (parents only move toward the root, and every value in a
@@ -104,9 +122,12 @@ __device__ __forceinline__ int uf_find_cached(int *parent, int v, int *err) {
     return v;
 }
 
-// Hooks the larger of two roots under the smaller; retries from the new parent when the
-// CAS loses a race.  Every root of a tree is its smallest sorted position.
-__device__ __forceinline__ void uf_union(int *parent, int a, int b, int *err) {
+// Joins the sets of two ancestors a and b (roots or not): hooks the larger root under the
+// smaller, retrying from the current roots when the CAS finds that a is no longer a root.
+// Every root of a tree is its smallest sorted position.  Returns the node hooked under (or
+// the common root when the two are one set already): an ancestor of every member of both
+// sets, which the caller may use in place of a fresh find.
+__device__ __forceinline__ int uf_union(int *parent, int a, int b, int *err) {
     int guard = 0;
     const int cap = c_uf_cap;
     while (a != b) {
@@ -116,14 +137,15 @@ __device__ __forceinline__ void uf_union(int *parent, int a, int b, int *err) {
             b = t;
         }
         const int old = atomicCAS(parent + a, a, b);
-        if (old == a) return;
+        if (old == a) return b;
         a = uf_find(parent, old, err);
         b = uf_find(parent, b, err);
         if (++guard > cap) {
             atomicOr(err, 1);
-            return;
+            return b;
         }
     }
+    return a;
 }
 
 // Doubles as order-preserving signed 64-bit integers (sign-magnitude turned into two's
@@ -705,6 +727,7 @@ __global__ void __launch_bounds__(256, 6) link_kernel(
         const int k = k0 + lane;
         const bool hv = k < ce;
         const float4 hp = hv ? rec[k] : make_float4(0.f, 0.f, 0.f, 0.f);
+        const int pk0 = hv ? parent[k] : -1;   // issued with the record; walked further below
         const int hidx = __float_as_int(hp.w);
         const unsigned homes = __ballot_sync(0xffffffffu, hv);
         const int nhome = __popc(homes);
@@ -751,7 +774,7 @@ __global__ void __launch_bounds__(256, 6) link_kernel(
                 bh[d] = fmaxf(bh[d], __shfl_xor_sync(0xffffffffu, bh[d], o));
             }
         }
-        int myroot = hv ? uf_find_cached(parent, k, err) : -1;
+        int myroot = hv ? uf_find_from(parent, k, pk0, err) : -1;
         int next = 0;
         for (int v0 = 0; v0 < total; v0 = next) {
             next = v0 + 32;
@@ -790,6 +813,10 @@ __global__ void __launch_bounds__(256, 6) link_kernel(
             const int off = __shfl_sync(0xffffffffu, soff, seg);
             float4 q = make_float4(0.f, 0.f, 0.f, 0.f);
             int rql = -1;
+            // the candidates' parents and the home particles' own are loaded next to the
+            // candidate records, so that the root walks below start without another round trip
+            const int pj = cv ? parent[jl] : -1;
+            const int pk = (v0 > 0 && hv) ? parent[k] : -1;
             if (cv) {
                 q = rec[jl];
                 q.x += (float)((off & 3) - 1) * g.cs;
@@ -804,9 +831,9 @@ __global__ void __launch_bounds__(256, 6) link_kernel(
             // roots of the candidates, found once per round instead of once per hit; a root
             // read here may be outdated by later unions, which is safe: equal roots prove the
             // same set, unequal ones are re-checked by uf_union
-            if (cv) rql = uf_find_cached(parent, jl, err);
+            if (cv) rql = uf_find_from(parent, jl, pj, err);
             // pick up unions made by other warps since the last look
-            if (v0 > 0 && hv) myroot = uf_find_cached(parent, k, err);
+            if (v0 > 0 && hv) myroot = uf_find_from(parent, k, pk, err);
             // when every home particle is in one set, candidates already in it need no test
             const int r0 = __shfl_sync(0xffffffffu, myroot, 0);   // lane 0 is always a home particle
             const bool uniform = __all_sync(0xffffffffu, !hv || myroot == r0);
@@ -830,21 +857,27 @@ __global__ void __launch_bounds__(256, 6) link_kernel(
                         if (hit && d2 >= g.lo) hit = exact_link(x, y, z, __float_as_int(pp.w), __float_as_int(q.w), g.r2);
                     }
                     if (!__any_sync(0xffffffffu, hit)) continue;
-                    // the candidates' current roots (a union of an earlier home particle may
-                    // have hooked them) against home particle p's
-                    if (hit) rql = uf_find_cached(parent, rql, err);
+                    // the candidates' roots as this round knows them against home particle p's
                     const int rp = __shfl_sync(0xffffffffu, myroot, p);
                     const bool need = hit && rql != rp;
                     const unsigned nm = __ballot_sync(0xffffffffu, need);
                     if (!nm) continue;
                     // one union per distinct candidate root among the lanes that hit
                     const unsigned peers = __match_any_sync(0xffffffffu, need ? rql : ~lane);
-                    if (need && lane == __ffs(peers) - 1) uf_union(parent, rp, rql, err);
+                    const bool leader = need && lane == __ffs(peers) - 1;
+                    int nr = 0;
+                    if (leader) nr = uf_union(parent, rp, rql, err);
                     if (need) has[jb < 0 ? ~jb : jb] = 1;
-                    __syncwarp();
-                    if (lane == p) {
-                        has[k] = 1;
-                        myroot = uf_find_cached(parent, k, err);
+                    if (lane == p) has[k] = 1;
+                    // the joined sets' members now carry the node each union returned
+                    unsigned lm = __ballot_sync(0xffffffffu, leader);
+                    while (lm) {
+                        const int l = __ffs(lm) - 1;
+                        lm &= lm - 1;
+                        const int old = __shfl_sync(0xffffffffu, rql, l);
+                        const int nw = __shfl_sync(0xffffffffu, nr, l);
+                        if (myroot == old || myroot == rp) myroot = nw;
+                        if (rql == old || rql == rp) rql = nw;
                     }
                 }
                 continue;
@@ -864,22 +897,34 @@ __global__ void __launch_bounds__(256, 6) link_kernel(
                 bool hit = hv && d2 <= g.hi && (jt < 0 || jt > k);
                 if (hit && d2 >= g.lo) hit = exact_link(x, y, z, hidx, __float_as_int(qq.w), g.r2);
                 if (!__any_sync(0xffffffffu, hit)) continue;
-                // the candidate's current root (the one read at the start of the round is
-                // outdated once an earlier candidate of its set has been joined)
-                int rq = rbuf[w][t];
-                if (lane == 0) rq = uf_find_cached(parent, rq, err);
-                rq = __shfl_sync(0xffffffffu, rq, 0);
+                // the candidate's root as this round knows it: refreshed after every union of
+                // the round below, without a memory round trip; a root another warp has hooked
+                // since is still an ancestor, which uf_union handles
+                const int rq = rbuf[w][t];
                 const bool need = hit && myroot != rq;
                 const unsigned nm = __ballot_sync(0xffffffffu, need);
                 if (!nm) continue;
                 // one union per distinct root among the home particles that hit: in a crowded
                 // cell most of the 32 share one, and their unions would all contend for it
                 const unsigned peers = __match_any_sync(0xffffffffu, need ? myroot : ~lane);
-                if (need && lane == __ffs(peers) - 1) uf_union(parent, myroot, rq, err);
+                const bool leader = need && lane == __ffs(peers) - 1;
+                int nr = 0;
+                if (leader) nr = uf_union(parent, myroot, rq, err);
                 if (need) has[k] = 1;
                 if (lane == __ffs(nm) - 1) has[jt < 0 ? ~jt : jt] = 1;
+                // the joined sets' members (home particles, the round's candidates) now carry
+                // the node each union returned
+                unsigned lm = __ballot_sync(0xffffffffu, leader);
+                while (lm) {
+                    const int l = __ffs(lm) - 1;
+                    lm &= lm - 1;
+                    const int old = __shfl_sync(0xffffffffu, myroot, l);
+                    const int nw = __shfl_sync(0xffffffffu, nr, l);
+                    if (myroot == old || myroot == rq) myroot = nw;
+                    if (rql == old || rql == rq) rql = nw;
+                }
+                rbuf[w][lane] = rql;
                 __syncwarp();
-                if (need) myroot = uf_find_cached(parent, k, err);
             }
         }
     }
