@@ -4,8 +4,9 @@
 //   1. bounding box (FP64) -> host picks the cell geometry (cell side = ll * (1 + 2^-20));
 //   2. each particle gets a row-major cell key; keys are radix-sorted with their indices;
 //   3. per sorted particle: a float4 record (position inside its cell in units of ll, and
-//      the original index), run heads of equal keys -> cell table + open-addressing hash
-//      from cell key to cell id;
+//      the original index), run heads of equal keys -> cell table -> per cell the first
+//      positions and counts of its 13 forward neighbour cells, found by lower bounds in the
+//      sorted cell keys (the key grid is padded so that a neighbour key is a constant offset);
 //   4. work items = 32-particle chunks of a cell; one warp per item tests its particles
 //      against the same cell and the 13 neighbour cells that sort after it, staging each
 //      neighbour chunk in shared memory (coalesced float4 loads, broadcast reads);
@@ -30,7 +31,6 @@ namespace halma {
 namespace {
 
 constexpr int kFofWarps = 8;
-constexpr uint64_t kEmptyKey = ~0ull;
 constexpr int kUfCapDefault = 1 << 26;   // bound on any union-find loop (never reached in practice)
 // The bound the kernels use: halma_set_union_find_cap changes it (a debug knob, so that tests
 // can make the loops run out); pushed to each device before its next FoF.
@@ -41,6 +41,10 @@ struct FofGeom {
     double cell, inv_cell, inv_scale, r2;
     float cs, lo, hi;
     long long ncx, ncy, ncz;
+    // key dimensions: ncy + 1 and ncz + 1.  Every y-row and z-column of the key grid ends in an
+    // empty pad cell, so that a neighbour's key is the cell's key plus a constant that never
+    // wraps onto an occupied cell (a wrap lands on a pad cell or past the last slab)
+    long long ky, kz;
     int sb;   // low key bits holding the 4 x 4 x 4 sub-cell (Morton order) within the cell: 6 or 0
 };
 
@@ -53,16 +57,6 @@ struct SegGeom {
     const double *smin = nullptr;      // [3 * nseg] origin of each segment
     const long long *scol = nullptr;   // [4 * nseg] first virtual x column, columns in x, y, z
 };
-
-__device__ __forceinline__ uint64_t mix64(uint64_t k) {
-    // MurmurHash3 64-bit finaliser
-    k ^= k >> 33;
-    k *= 0xff51afd7ed558ccdull;
-    k ^= k >> 33;
-    k *= 0xc4ceb9fe1a85ec53ull;
-    k ^= k >> 33;
-    return k;
-}
 
 __device__ __forceinline__ int uf_find(int *parent, int v, int *err) {
     int p = __ldcg(parent + v);
@@ -310,7 +304,7 @@ __global__ void keys_kernel(const double *__restrict__ x, const double *__restri
         quarter_split(fma(y[i], s4, by), 4 * ny - 1, qy, wy);
         quarter_split(fma(z[i], s4, bz), 4 * nz - 1, qz, wz);
         const long long cx = qx >> 2, cy = qy >> 2, cz = qz >> 2;
-        uint64_t key = ((uint64_t)(x0 + cx) * (uint64_t)g.ncy + (uint64_t)cy) * (uint64_t)g.ncz + (uint64_t)cz;
+        uint64_t key = ((uint64_t)(x0 + cx) * (uint64_t)g.ky + (uint64_t)cy) * (uint64_t)g.kz + (uint64_t)cz;
         if (g.sb) {
             const int sx = (int)(qx & 3), sy = (int)(qy & 3), sz = (int)(qz & 3);
             const int mort = ((sx >> 1) << 5) | ((sy >> 1) << 4) | ((sz >> 1) << 3) | ((sx & 1) << 2) |
@@ -321,14 +315,6 @@ __global__ void keys_kernel(const double *__restrict__ x, const double *__restri
         vals[i] = i;
         pre[i] = make_float4(wx * cs4, wy * cs4, wz * cs4, __int_as_float(i));
     }
-}
-
-__device__ __forceinline__ void decode_key(uint64_t key, const FofGeom &g, long long &cx, long long &cy,
-                                           long long &cz) {
-    cz = (long long)(key % (uint64_t)g.ncz);
-    const uint64_t t = key / (uint64_t)g.ncz;
-    cy = (long long)(t % (uint64_t)g.ncy);
-    cx = (long long)(t / (uint64_t)g.ncy);
 }
 
 // Sorted records, run heads, union-find / label initialisation.
@@ -485,50 +471,6 @@ __global__ void __launch_bounds__(256) dense_cell_kernel(const int *__restrict__
     }
 }
 
-// Cell table + hash insert, from the exclusive scan of the run heads.
-// Hash slot: cell key, first sorted position and particle count of the cell, so that a
-// neighbour lookup is one 16-byte load per probe.
-struct __align__(16) CellSlot {
-    unsigned long long key;
-    int start, count;
-};
-
-// First probe slot of a cell key (fully scattered: runs of neighbouring keys placed side by
-// side made the CAS inserts of crowded regions collide more than they saved on lookups).
-__device__ __forceinline__ uint64_t slot_of(uint64_t key, uint64_t hmask) { return mix64(key) & hmask; }
-
-// Hash capacity from the number of occupied cells: the smallest power of two >= 2 x cells, at
-// least 1024 slots and at most the cap_max allocated; kept on the device as a mask.  The Bloom
-// filter of occupied cells gets the smallest power of two >= 8 bits per cell (at most bcap_max
-// bits): one bit per cell, so a lookup of an empty neighbour cell is a false positive with
-// probability 1 - e^(-1/8) = 12 %, and at 8 bits per cell the filter of a 5e7-cell snapshot
-// (64 MB) stays in L2.
-__global__ void hash_size_kernel(int n, const int *__restrict__ head, const int *__restrict__ cellpos,
-                                 unsigned long long cap_max, unsigned long long bcap_max,
-                                 unsigned long long *__restrict__ hmask, unsigned long long *__restrict__ bmask) {
-    const unsigned long long nc = (unsigned long long)(cellpos[n - 1] + head[n - 1]);
-    unsigned long long cap = 1024;
-    while (cap < 2 * nc && cap < cap_max) cap <<= 1;
-    *hmask = (cap < cap_max ? cap : cap_max) - 1;
-    unsigned long long bc = 1024;
-    while (bc < 8 * nc && bc < bcap_max) bc <<= 1;
-    *bmask = (bc < bcap_max ? bc : bcap_max) - 1;
-}
-
-__global__ void hash_clear_kernel(const unsigned long long *__restrict__ hmask_p, CellSlot *__restrict__ slots,
-                                  const unsigned long long *__restrict__ bmask_p, unsigned *__restrict__ bloom) {
-    const unsigned long long cap = *hmask_p + 1, words = (*bmask_p + 1) >> 5;
-    for (unsigned long long s = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; s < cap || s < words;
-         s += (unsigned long long)gridDim.x * blockDim.x) {
-        if (s < cap) reinterpret_cast<ulonglong2 *>(slots)[s] = make_ulonglong2(kEmptyKey, 0ull);
-        if (s < words) bloom[s] = 0u;
-    }
-}
-
-__device__ __forceinline__ uint64_t bloom_bit(uint64_t key, uint64_t bmask) {
-    return mix64(key ^ 0x9e3779b97f4a7c15ull) & bmask;
-}
-
 // Start and key of every occupied cell (cells in sorted order), from the exclusive scan of
 // the run heads.
 __global__ void cell_table_kernel(int n, int sb, const uint64_t *__restrict__ keys, const int *__restrict__ head,
@@ -548,34 +490,6 @@ __global__ void cell_table_kernel(int n, int sb, const uint64_t *__restrict__ ke
     }
 }
 
-// Hash insert of every cell with its first position, its count and its one-component flag
-// (bit 31 of the count) in one slot, and the cell's bit in the Bloom filter.
-__global__ void cell_insert_kernel(const int *__restrict__ ncell_p, const int *__restrict__ cell_start,
-                                   const uint64_t *__restrict__ cell_key, const unsigned char *__restrict__ conn,
-                                   CellSlot *__restrict__ slots, const unsigned long long *__restrict__ hmask_p,
-                                   unsigned *__restrict__ bloom, const unsigned long long *__restrict__ bmask_p) {
-    const int nc = *ncell_p;
-    const uint64_t hmask = *hmask_p, bmask = *bmask_p;
-    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x) {
-        const uint64_t key = cell_key[c];
-        const int cs = cell_start[c];
-        const int count = (cell_start[c + 1] - cs) | (conn[c] ? (int)0x80000000u : 0);
-        uint64_t h = slot_of(key, hmask);
-        for (uint64_t probe = 0; probe <= hmask; ++probe) {
-            const unsigned long long prev =
-                atomicCAS(&slots[h].key, (unsigned long long)kEmptyKey, (unsigned long long)key);
-            if (prev == kEmptyKey) {
-                slots[h].start = cs;
-                slots[h].count = count;
-                break;
-            }
-            h = (h + 1) & hmask;
-        }
-        const uint64_t b = bloom_bit(key, bmask);
-        atomicOr(bloom + (b >> 5), 1u << (b & 31));
-    }
-}
-
 // Marks the first particle of every 32-particle chunk of every cell that has linking work
 // (bit 13 of its neighbour mask, see nbmask_kernel).
 __global__ void itemflag_kernel(int n, const int *__restrict__ head, const int *__restrict__ cellpos,
@@ -587,44 +501,31 @@ __global__ void itemflag_kernel(int n, const int *__restrict__ head, const int *
     }
 }
 
-// A work item as the linking kernel reads it, in two 16-byte loads: the chunk's first sorted
-// position, the cell's end with the cell's one-component flag in bit 31, and the cell's
-// coordinates (decoded here once instead of in the latency-bound linking kernel).
+// A work item as the linking kernel reads it, in one 16-byte load: the chunk's first sorted
+// position, the cell's end with the cell's one-component flag in bit 31, and the cell's index
+// (its row of the neighbour table).
 struct __align__(16) ItemRec {
-    int k0, ce_conn;
-    long long cx, cy, cz;
+    int k0, ce_conn, cell, pad;
 };
 
 __global__ void items_kernel(int n, const int *__restrict__ head, const int *__restrict__ cellpos,
                              const int *__restrict__ flag, const int *__restrict__ itempos,
-                             const int *__restrict__ cell_start, const uint64_t *__restrict__ cell_key,
-                             const unsigned char *__restrict__ conn, const int *__restrict__ cmask, FofGeom g,
-                             ItemRec *__restrict__ items, unsigned short *__restrict__ imask,
-                             int *__restrict__ nitems) {
+                             const int *__restrict__ cell_start, const unsigned char *__restrict__ conn,
+                             const int *__restrict__ cmask, ItemRec *__restrict__ items,
+                             unsigned short *__restrict__ imask, int *__restrict__ nitems) {
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
         if (flag[k]) {
             const int c = cellpos[k] + head[k] - 1;
             ItemRec r;
             r.k0 = k;
             r.ce_conn = cell_start[c + 1] | (conn[c] ? (int)0x80000000u : 0);
-            decode_key(cell_key[c], g, r.cx, r.cy, r.cz);
+            r.cell = c;
+            r.pad = 0;
             items[itempos[k]] = r;
             imask[itempos[k]] = (unsigned short)(cmask[c] & 0x1fff);
         }
         if (k == n - 1) *nitems = itempos[k] + flag[k];
     }
-}
-
-// (start, count) of the cell with this key, count 0 when it holds no particle.
-__device__ __forceinline__ int2 hash_lookup(const CellSlot *__restrict__ slots, uint64_t hmask, uint64_t key) {
-    uint64_t h = slot_of(key, hmask);
-    for (uint64_t probe = 0; probe <= hmask; ++probe) {
-        const ulonglong2 v = __ldg(reinterpret_cast<const ulonglong2 *>(slots + h));
-        if (v.x == key) return make_int2((int)(v.y & 0xffffffffull), (int)(v.y >> 32));
-        if (v.x == kEmptyKey) return make_int2(0, 0);
-        h = (h + 1) & hmask;
-    }
-    return make_int2(0, 0);
 }
 
 __device__ __forceinline__ bool exact_link(const double *__restrict__ x, const double *__restrict__ y,
@@ -643,32 +544,67 @@ __constant__ int c_stencil[13][3] = {{0, 0, 1},  {0, 1, -1}, {0, 1, 0},  {0, 1, 
                                      {1, -1, 0}, {1, -1, 1}, {1, 0, -1}, {1, 0, 0},  {1, 0, 1},
                                      {1, 1, -1}, {1, 1, 0},  {1, 1, 1}};
 
-// The occupied forward neighbours of every cell as a 13-bit mask (bit j: stencil cell j),
-// one thread per cell: a Bloom-filter test per neighbour (L2-resident) and a hash lookup only
-// for the ones it lets through.  Bit 13 marks the cells with linking work: an occupied
-// neighbour, or more than one particle in a cell that is not one component already.  Cells
-// without work (isolated particles, isolated one-component cells) get no work item.  (Linking
-// the cells of at most 4 particles one thread each instead of one warp per chunk measured
-// slower: 76 against 66 ms for the links of the 2e8-particle snapshot.)
-__global__ void nbmask_kernel(const int *__restrict__ ncell_p, const int *__restrict__ cell_start,
-                              const uint64_t *__restrict__ cell_key, const unsigned char *__restrict__ conn,
-                              const CellSlot *__restrict__ slots, const unsigned long long *__restrict__ hmask_p,
-                              const unsigned *__restrict__ bloom, const unsigned long long *__restrict__ bmask_p,
-                              FofGeom g, int *__restrict__ cmask) {
+// Lower bound of q in the sorted keys[lo, n), searched forward from lo: doubling steps, then
+// bisection of the last step.
+__device__ __forceinline__ int gallop_lower_bound(const uint64_t *__restrict__ keys, int lo, int n, uint64_t q) {
+    if (lo >= n || keys[lo] >= q) return lo;
+    int prev = lo;   // keys[prev] < q
+    long long cur = (long long)lo + 1, step = 1;
+    while (cur < n && keys[cur] < q) {
+        prev = (int)cur;
+        step <<= 1;
+        cur = prev + step;
+    }
+    int a = prev + 1, b = (int)(cur < n ? cur : n);
+    while (a < b) {
+        const int mid = (a + b) >> 1;
+        if (keys[mid] < q) a = mid + 1;
+        else b = mid;
+    }
+    return a;
+}
+
+// The 13 forward neighbours of every cell, found in the sorted cell keys, one thread per cell.
+// On the padded key grid a neighbour's key is the cell's key plus a constant, so (0, 0, +1) is
+// the next cell or none, and for each of the stencil's four columns (0, 1), (1, -1), (1, 0),
+// (1, 1), whose bases increase, one lower bound of the column's z - 1 key -- galloping forward
+// from the cell itself, then from the previous column's bound -- gives its three z neighbours
+// in order.  nbinfo[13 c + j] = (first sorted position, count | one-component flag << 31) of
+// stencil cell j, (0, 0) when it holds no particle; cmask[c] = the 13-bit mask of occupied
+// neighbours, and bit 13 when the cell has linking work: an occupied neighbour, or more than
+// one particle in a cell that is not one component already.  Cells without work (isolated
+// particles, isolated one-component cells) get no work item.
+__global__ void nbtab_kernel(const int *__restrict__ ncell_p, const int *__restrict__ cell_start,
+                             const uint64_t *__restrict__ cell_key, const unsigned char *__restrict__ conn,
+                             long long ky, long long kz, int2 *__restrict__ nbinfo, int *__restrict__ cmask) {
     const int nc = *ncell_p;
-    const uint64_t hmask = *hmask_p, bmask = *bmask_p;
+    const uint64_t zrow = (uint64_t)kz, slab = (uint64_t)ky * (uint64_t)kz;
     for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x) {
-        long long cx, cy, cz;
-        decode_key(cell_key[c], g, cx, cy, cz);
+        const uint64_t key = cell_key[c];
+        int2 *row = nbinfo + (int64_t)c * 13;
         int m = 0;
-#pragma unroll 1
-        for (int j = 0; j < 13; ++j) {
-            const long long nx = cx + c_stencil[j][0], ny = cy + c_stencil[j][1], nz = cz + c_stencil[j][2];
-            if (nx >= g.ncx || ny < 0 || ny >= g.ncy || nz < 0 || nz >= g.ncz) continue;
-            const uint64_t nkey = ((uint64_t)nx * (uint64_t)g.ncy + (uint64_t)ny) * (uint64_t)g.ncz + (uint64_t)nz;
-            const uint64_t b = bloom_bit(nkey, bmask);
-            if (!((__ldg(bloom + (b >> 5)) >> (b & 31)) & 1u)) continue;
-            if (hash_lookup(slots, hmask, nkey).y != 0) m |= 1 << j;
+        auto put = [&](int j, int d) {
+            int2 v = make_int2(0, 0);
+            if (d >= 0) {
+                const int s0 = cell_start[d];
+                v = make_int2(s0, (cell_start[d + 1] - s0) | (conn[d] ? (int)0x80000000u : 0));
+                m |= 1 << j;
+            }
+            row[j] = v;
+        };
+        put(0, (c + 1 < nc && cell_key[c + 1] == key + 1) ? c + 1 : -1);
+        const uint64_t base[4] = {key + zrow, key + slab - zrow, key + slab, key + slab + zrow};
+        int lb = c + 1;
+#pragma unroll
+        for (int col = 0; col < 4; ++col) {
+            lb = gallop_lower_bound(cell_key, lb, nc, base[col] - 1);
+            int at_ = lb;
+#pragma unroll
+            for (int dz = -1; dz <= 1; ++dz) {
+                int d = -1;
+                if (at_ < nc && cell_key[at_] == base[col] + (uint64_t)(long long)dz) d = at_++;
+                put(1 + 3 * col + (dz + 1), d);
+            }
         }
         const int count = cell_start[c + 1] - cell_start[c];
         const bool work = m != 0 || (count > 1 && !conn[c]);
@@ -696,8 +632,7 @@ constexpr int kHomeSeg = 13;
 
 __global__ void __launch_bounds__(256, 6) link_kernel(
     const float4 *__restrict__ rec, const ItemRec *__restrict__ items, const unsigned short *__restrict__ imask,
-    const int *__restrict__ nitems_p, int *item_counter, const CellSlot *__restrict__ slots,
-    const unsigned long long *__restrict__ hmask_p, FofGeom g,
+    const int *__restrict__ nitems_p, int *item_counter, const int2 *__restrict__ nbinfo, FofGeom g,
     const double *__restrict__ x, const double *__restrict__ y, const double *__restrict__ z,
     int *parent, unsigned char *has, int *err) {
     __shared__ float4 buf[kFofWarps][32];    // candidates of the round (candidate-major tests)
@@ -708,7 +643,6 @@ __global__ void __launch_bounds__(256, 6) link_kernel(
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const unsigned lt_mask = (1u << lane) - 1u;
     const int nitems = *nitems_p;
-    const uint64_t hmask = *hmask_p;
     // items come from a counter: their cost varies by orders of magnitude (dense cores).  The
     // next item's number is fetched while the current one is processed.
     int nxt = 0;
@@ -718,12 +652,10 @@ __global__ void __launch_bounds__(256, 6) link_kernel(
         if (item >= nitems) break;
         if (lane == 0) nxt = atomicAdd(item_counter, 1);
         const int4 ia = __ldg(reinterpret_cast<const int4 *>(items + item));
-        const longlong2 ib = __ldg(reinterpret_cast<const longlong2 *>(items + item) + 1);
         const int k0 = ia.x;
         const int ce = ia.y & 0x7fffffff;
         const bool home_conn = ia.y < 0;
-        const long long cx = (long long)(((unsigned long long)(unsigned)ia.w << 32) | (unsigned)ia.z);
-        const long long cy = ib.x, cz = ib.y;
+        const int cell = ia.z;
         const int k = k0 + lane;
         const bool hv = k < ce;
         const float4 hp = hv ? rec[k] : make_float4(0.f, 0.f, 0.f, 0.f);
@@ -736,10 +668,8 @@ __global__ void __launch_bounds__(256, 6) link_kernel(
         bool sconn = false;                 // the segment's cell is one component
         if (lane < 13) {
             soff = (c_stencil[lane][0] + 1) | (c_stencil[lane][1] + 1) << 2 | (c_stencil[lane][2] + 1) << 4;
-            const long long nx = cx + c_stencil[lane][0], ny = cy + c_stencil[lane][1], nz = cz + c_stencil[lane][2];
-            if ((__ldg(imask + item) >> lane) & 1u) {   // in the grid and occupied (nbmask_kernel)
-                const uint64_t nkey = ((uint64_t)nx * (uint64_t)g.ncy + (uint64_t)ny) * (uint64_t)g.ncz + (uint64_t)nz;
-                const int2 sc = hash_lookup(slots, hmask, nkey);
+            if ((__ldg(imask + item) >> lane) & 1u) {   // occupied (nbtab_kernel)
+                const int2 sc = __ldg(nbinfo + (int64_t)cell * 13 + lane);
                 sjs = sc.x;
                 sn = sc.y & 0x7fffffff;
                 sconn = sc.y < 0;
@@ -1136,18 +1066,16 @@ int push_uf_cap(cudaStream_t st) {
 // Keys, sort, cells, links and labels for a geometry whose cell grid is known.
 int fof_core(int n, const double *x, const double *y, const double *z, FofGeom g, SegGeom sg, int *labels,
              int64_t *n_groups, cudaStream_t st) {
-    const long double cells = (long double)g.ncx * g.ncy * g.ncz;
+    g.ky = g.ncy + 1;
+    g.kz = g.ncz + 1;
+    const long double cells = (long double)g.ncx * g.ky * g.kz;
     if (cells > 4.0e18L)
         return fail(HALMA_ERR_CAPACITY, "cell grid too large (%lld x %lld x %lld cells)", g.ncx, g.ncy, g.ncz);
-    const int cell_bits = bits_for((uint64_t)(g.ncx * g.ncy * g.ncz - 1));
+    const int cell_bits = bits_for((uint64_t)(g.ncx * g.ky * g.kz - 1));
     g.sb = cell_bits <= 58 ? 6 : 0;
     const int end_bit = cell_bits + g.sb;
     const int sms = device_sm_count();
 
-    uint64_t hcap = 1024;   // slots allocated; the kernels use a power of two >= 2 x cells of it
-    while (hcap < 2ull * (uint64_t)n) hcap <<= 1;
-    uint64_t bcap = 1024;   // Bloom-filter bits allocated; the kernels use >= 8 bits per cell of it
-    while (bcap < 8ull * (uint64_t)n) bcap <<= 1;
     const size_t sort_b = sort_pairs_u64_i32_bytes(n, end_bit);
     const size_t scan_b = std::max(exclusive_sum_i32_bytes(n), inclusive_max_i32_bytes(n));
     Layout M;
@@ -1158,8 +1086,7 @@ int fof_core(int n, const double *x, const double *y, const double *z, FofGeom g
     const size_t o_par = M.add(4ull * n), o_has = M.add(1ull * n), o_root = M.add(4ull * n);
     const size_t o_min = M.add(4ull * n);
     const size_t o_cst = M.add(4ull * (n + 1)), o_ckey = M.add(8ull * n);
-    const size_t o_hk = M.add(16ull * hcap), o_cm = M.add(4ull * n);   // hash slots, neighbour mask per cell
-    const size_t o_bloom = M.add(bcap / 8), o_imask = M.add(2ull * n);
+    const size_t o_cm = M.add(4ull * n), o_imask = M.add(2ull * n);   // neighbour masks: per cell, per item
     const size_t o_flag = M.add(4ull * n), o_ipos = M.add(4ull * n);
     const size_t o_items = M.add(sizeof(ItemRec) * (size_t)n);
     const size_t o_cnt = M.add(64), o_conn = M.add(1ull * n);
@@ -1176,15 +1103,11 @@ int fof_core(int n, const double *x, const double *y, const double *z, FofGeom g
     auto *has = at<unsigned char>(base, o_has);
     auto *cst = at<int>(base, o_cst);
     auto *ckey = at<uint64_t>(base, o_ckey);
-    auto *hk = at<CellSlot>(base, o_hk);
     auto *cmask = at<int>(base, o_cm);
-    auto *bloom = at<unsigned>(base, o_bloom);
     auto *imask = at<unsigned short>(base, o_imask);
     auto *flag = at<int>(base, o_flag), *ipos = at<int>(base, o_ipos);
     auto *items = at<ItemRec>(base, o_items);
-    int *cnt = at<int>(base, o_cnt);   // [0] ncell [1] nitems [2] ngroups [3] err [5] link item counter
-    auto *hmask = reinterpret_cast<unsigned long long *>(cnt + 6);   // [6..7] hash slot mask
-    auto *bmask = reinterpret_cast<unsigned long long *>(cnt + 10);  // [10..11] Bloom bit mask ([8] dense cells)
+    int *cnt = at<int>(base, o_cnt);   // [0] ncell [1] nitems [2] ngroups [3] err [5] link item counter [8] dense cells
     void *tmp = at<void>(base, o_tmp);
     const int g1 = std::min(sms * 8, grid_for(n, 256));
 
@@ -1214,19 +1137,23 @@ int fof_core(int n, const double *x, const double *y, const double *z, FofGeom g
     } else {
         HALMA_CUDA(cudaMemsetAsync(conn, 0, n, st));
     }
-    HALMA_LAUNCH(hash_size_kernel, 1, 1, 0, st, n, head, cpos, (unsigned long long)hcap, (unsigned long long)bcap,
-                 hmask, bmask);
-    HALMA_LAUNCH(hash_clear_kernel, g1, 256, 0, st, hmask, hk, bmask, bloom);
-    HALMA_LAUNCH(cell_insert_kernel, g1, 256, 0, st, cnt + 0, cst, ckey, conn, hk, hmask, bloom, bmask);
-    HALMA_LAUNCH(nbmask_kernel, g1, 256, 0, st, cnt + 0, cst, ckey, conn, hk, hmask, bloom, bmask, g, cmask);
+    // the neighbour table (13 x 8 bytes per occupied cell) in its own cached buffer, sized from
+    // the cell count
+    int ncell = 0;
+    HALMA_CUDA(cudaMemcpyAsync(&ncell, cnt + 0, sizeof(int), cudaMemcpyDeviceToHost, st));
+    HALMA_CUDA(cudaStreamSynchronize(st));
+    void *nbbase = nullptr;
+    HALMA_TRY(workspace(sizeof(int2) * 13 * (size_t)std::max(ncell, 1), &nbbase, st, 10));
+    int2 *nbinfo = static_cast<int2 *>(nbbase);
+    HALMA_LAUNCH(nbtab_kernel, std::min(sms * 8, grid_for(ncell, 256)), 256, 0, st, cnt + 0, cst, ckey, conn, g.ky,
+                 g.kz, nbinfo, cmask);
     HALMA_TRY(mark(4));
     HALMA_LAUNCH(itemflag_kernel, g1, 256, 0, st, n, head, cpos, cst, cmask, flag);
     HALMA_TRY(exclusive_sum_i32(tmp, scan_b, flag, ipos, n, st));
-    HALMA_LAUNCH(items_kernel, g1, 256, 0, st, n, head, cpos, flag, ipos, cst, ckey, conn, cmask, g, items, imask,
-                 cnt + 1);
+    HALMA_LAUNCH(items_kernel, g1, 256, 0, st, n, head, cpos, flag, ipos, cst, conn, cmask, items, imask, cnt + 1);
     HALMA_TRY(mark(5));
-    HALMA_LAUNCH(link_kernel, sms * 8, 32 * kFofWarps, 0, st, rec, items, imask, cnt + 1, cnt + 5, hk, hmask, g, x,
-                 y, z, parent, has, cnt + 3);
+    HALMA_LAUNCH(link_kernel, sms * 8, 32 * kFofWarps, 0, st, rec, items, imask, cnt + 1, cnt + 5, nbinfo, g, x, y,
+                 z, parent, has, cnt + 3);
     HALMA_TRY(mark(6));
     HALMA_LAUNCH(root_kernel, g1, 256, 0, st, n, rec, parent, has, root, minidx, cnt + 3);
     HALMA_LAUNCH(label_kernel, g1, 256, 0, st, n, rec, has, root, minidx, labels, cnt + 2);
