@@ -511,8 +511,7 @@ struct __align__(16) ItemRec {
 __global__ void items_kernel(int n, const int *__restrict__ head, const int *__restrict__ cellpos,
                              const int *__restrict__ flag, const int *__restrict__ itempos,
                              const int *__restrict__ cell_start, const unsigned char *__restrict__ conn,
-                             const int *__restrict__ cmask, ItemRec *__restrict__ items,
-                             unsigned short *__restrict__ imask, int *__restrict__ nitems) {
+                             ItemRec *__restrict__ items, int *__restrict__ nitems) {
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
         if (flag[k]) {
             const int c = cellpos[k] + head[k] - 1;
@@ -522,7 +521,6 @@ __global__ void items_kernel(int n, const int *__restrict__ head, const int *__r
             r.cell = c;
             r.pad = 0;
             items[itempos[k]] = r;
-            imask[itempos[k]] = (unsigned short)(cmask[c] & 0x1fff);
         }
         if (k == n - 1) *nitems = itempos[k] + flag[k];
     }
@@ -631,8 +629,7 @@ __global__ void nbtab_kernel(const int *__restrict__ ncell_p, const int *__restr
 constexpr int kHomeSeg = 13;
 
 __global__ void __launch_bounds__(256, 6) link_kernel(
-    const float4 *__restrict__ rec, const ItemRec *__restrict__ items, const unsigned short *__restrict__ imask,
-    const int *__restrict__ nitems_p, int *item_counter, const int2 *__restrict__ nbinfo, FofGeom g,
+    const float4 *__restrict__ rec, const ItemRec *__restrict__ items, const int *__restrict__ nitems_p, int *item_counter, const int2 *__restrict__ nbinfo, FofGeom g,
     const double *__restrict__ x, const double *__restrict__ y, const double *__restrict__ z,
     int *parent, unsigned char *has, int *err) {
     __shared__ float4 buf[kFofWarps][32];    // candidates of the round (candidate-major tests)
@@ -644,18 +641,30 @@ __global__ void __launch_bounds__(256, 6) link_kernel(
     const unsigned lt_mask = (1u << lane) - 1u;
     const int nitems = *nitems_p;
     // items come from a counter: their cost varies by orders of magnitude (dense cores).  The
-    // next item's number is fetched while the current one is processed.
+    // next item's number, its record and its row of the neighbour table (lanes 0..12) are
+    // fetched while the current item is processed.
     int nxt = 0;
     if (lane == 0) nxt = atomicAdd(item_counter, 1);
+    int item = __shfl_sync(0xffffffffu, nxt, 0);
+    int4 ia_next = make_int4(0, 0, 0, 0);
+    int2 nb_next = make_int2(0, 0);
+    if (item < nitems) {
+        ia_next = __ldg(reinterpret_cast<const int4 *>(items + item));
+        if (lane < 13) nb_next = __ldg(nbinfo + (int64_t)ia_next.z * 13 + lane);
+    }
+    if (lane == 0) nxt = atomicAdd(item_counter, 1);
     for (;;) {
-        const int item = __shfl_sync(0xffffffffu, nxt, 0);
         if (item >= nitems) break;
-        if (lane == 0) nxt = atomicAdd(item_counter, 1);
-        const int4 ia = __ldg(reinterpret_cast<const int4 *>(items + item));
+        const int4 ia = ia_next;
+        const int2 nbr = nb_next;   // this lane's neighbour cell (lanes 0..12): first position, count | flag
+        item = __shfl_sync(0xffffffffu, nxt, 0);
+        if (item < nitems) {
+            ia_next = __ldg(reinterpret_cast<const int4 *>(items + item));
+            if (lane == 0) nxt = atomicAdd(item_counter, 1);
+        }
         const int k0 = ia.x;
         const int ce = ia.y & 0x7fffffff;
         const bool home_conn = ia.y < 0;
-        const int cell = ia.z;
         const int k = k0 + lane;
         const bool hv = k < ce;
         const float4 hp = hv ? rec[k] : make_float4(0.f, 0.f, 0.f, 0.f);
@@ -666,14 +675,11 @@ __global__ void __launch_bounds__(256, 6) link_kernel(
         // lane s < 13 owns stencil cell s, lane 13 the rest of the home cell
         int sjs = 0, sn = 0, soff = 0x15;   // soff: stencil offset + 1 per axis, 2 bits each
         bool sconn = false;                 // the segment's cell is one component
-        if (lane < 13) {
+        if (lane < 13) {   // an empty neighbour has count 0
             soff = (c_stencil[lane][0] + 1) | (c_stencil[lane][1] + 1) << 2 | (c_stencil[lane][2] + 1) << 4;
-            if ((__ldg(imask + item) >> lane) & 1u) {   // occupied (nbtab_kernel)
-                const int2 sc = __ldg(nbinfo + (int64_t)cell * 13 + lane);
-                sjs = sc.x;
-                sn = sc.y & 0x7fffffff;
-                sconn = sc.y < 0;
-            }
+            sjs = nbr.x;
+            sn = nbr.y & 0x7fffffff;
+            sconn = nbr.y < 0;
         } else if (lane == kHomeSeg && !home_conn) {   // a cell that is one component has no new pair inside
             sjs = k0 + 1;
             sn = ce - sjs;
@@ -704,6 +710,8 @@ __global__ void __launch_bounds__(256, 6) link_kernel(
                 bh[d] = fmaxf(bh[d], __shfl_xor_sync(0xffffffffu, bh[d], o));
             }
         }
+        // the next item's neighbour row, now that its record has arrived
+        if (item < nitems && lane < 13) nb_next = __ldg(nbinfo + (int64_t)ia_next.z * 13 + lane);
         int myroot = hv ? uf_find_from(parent, k, pk0, err) : -1;
         int next = 0;
         for (int v0 = 0; v0 < total; v0 = next) {
@@ -1086,7 +1094,7 @@ int fof_core(int n, const double *x, const double *y, const double *z, FofGeom g
     const size_t o_par = M.add(4ull * n), o_has = M.add(1ull * n), o_root = M.add(4ull * n);
     const size_t o_min = M.add(4ull * n);
     const size_t o_cst = M.add(4ull * (n + 1)), o_ckey = M.add(8ull * n);
-    const size_t o_cm = M.add(4ull * n), o_imask = M.add(2ull * n);   // neighbour masks: per cell, per item
+    const size_t o_cm = M.add(4ull * n);   // occupied-neighbour mask and work flag per cell
     const size_t o_flag = M.add(4ull * n), o_ipos = M.add(4ull * n);
     const size_t o_items = M.add(sizeof(ItemRec) * (size_t)n);
     const size_t o_cnt = M.add(64), o_conn = M.add(1ull * n);
@@ -1104,7 +1112,6 @@ int fof_core(int n, const double *x, const double *y, const double *z, FofGeom g
     auto *cst = at<int>(base, o_cst);
     auto *ckey = at<uint64_t>(base, o_ckey);
     auto *cmask = at<int>(base, o_cm);
-    auto *imask = at<unsigned short>(base, o_imask);
     auto *flag = at<int>(base, o_flag), *ipos = at<int>(base, o_ipos);
     auto *items = at<ItemRec>(base, o_items);
     int *cnt = at<int>(base, o_cnt);   // [0] ncell [1] nitems [2] ngroups [3] err [5] link item counter [8] dense cells
@@ -1150,10 +1157,10 @@ int fof_core(int n, const double *x, const double *y, const double *z, FofGeom g
     HALMA_TRY(mark(4));
     HALMA_LAUNCH(itemflag_kernel, g1, 256, 0, st, n, head, cpos, cst, cmask, flag);
     HALMA_TRY(exclusive_sum_i32(tmp, scan_b, flag, ipos, n, st));
-    HALMA_LAUNCH(items_kernel, g1, 256, 0, st, n, head, cpos, flag, ipos, cst, conn, cmask, items, imask, cnt + 1);
+    HALMA_LAUNCH(items_kernel, g1, 256, 0, st, n, head, cpos, flag, ipos, cst, conn, items, cnt + 1);
     HALMA_TRY(mark(5));
-    HALMA_LAUNCH(link_kernel, sms * 8, 32 * kFofWarps, 0, st, rec, items, imask, cnt + 1, cnt + 5, nbinfo, g, x, y,
-                 z, parent, has, cnt + 3);
+    HALMA_LAUNCH(link_kernel, sms * 8, 32 * kFofWarps, 0, st, rec, items, cnt + 1, cnt + 5, nbinfo, g, x, y, z,
+                 parent, has, cnt + 3);
     HALMA_TRY(mark(6));
     HALMA_LAUNCH(root_kernel, g1, 256, 0, st, n, rec, parent, has, root, minidx, cnt + 3);
     HALMA_LAUNCH(label_kernel, g1, 256, 0, st, n, rec, has, root, minidx, labels, cnt + 2);
