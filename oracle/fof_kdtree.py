@@ -25,9 +25,10 @@ from scipy.spatial import KDTree
 CLEAN_EVERY = 64   # fof.py:33 iterations_to_clean
 
 
-def friends_of_friends(data, linking_length):
+def friends_of_friends(data, linking_length, boxsize=None):
+    """fof.py:18-79; ``boxsize`` (None in the reference) gives the tree a periodic box."""
     data = np.asarray(data)
-    tree = KDTree(data)
+    tree = KDTree(data) if boxsize is None else KDTree(data, boxsize=boxsize)
     n = data.shape[0]
     looked = np.zeros(n, dtype=bool)
     marked = np.zeros(n, dtype=bool)
@@ -59,6 +60,6 @@ def friends_of_friends(data, linking_length):
     return groups
 
 
-def friends_of_friends_serial(st_x, st_y, st_z, linking_length):
+def friends_of_friends_serial(st_x, st_y, st_z, linking_length, boxsize=None):
     data = np.array((st_x, st_y, st_z)).T
-    return friends_of_friends(data, linking_length)
+    return friends_of_friends(data, linking_length, boxsize)

@@ -93,6 +93,7 @@ SIGNATURES = {
     "halma_measure_fp32_fma_rate": ([_I32, _I32, _P, _P, _P], ctypes.c_int),
     "halma_measure_pair_rate": ([_I32, _P, _P, _P], ctypes.c_int),
     "halma_fof": ([_I64, _P, _P, _P, _F64, _P, _P, _P], ctypes.c_int),
+    "halma_fof_periodic": ([_I64, _P, _P, _P, _F64, _F64, _P, _P, _P], ctypes.c_int),
     "halma_fof_groups": ([_I64, _P, _I32, _P, _P, _P, _P], ctypes.c_int),
     "halma_fof_segmented": ([_I64, _P, _P, _P, _I64, _P, _F64, _P, _P, _P], ctypes.c_int),
     "halma_split_bridges": ([_I64, _P, _P, _P, _P, _I64, _P, _P, ctypes.POINTER(SubstructureParams), _P, _I64, _P,

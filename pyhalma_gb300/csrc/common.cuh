@@ -62,7 +62,7 @@ struct Layout {
 // demand.  Slot 0 is the scratch of one stage (FoF, unbinding, potentials); slot 1 holds what
 // the one-call pipeline keeps across its stages.  The others: 2 segmented-FoF geometry, 3
 // bridge splitting, 4 / 5 / 8 ball gather, 6 phase-space cleaning, 7 properties, 9 symmetric
-// potentials, 10 the FoF neighbour table.  Slot 0 is reused by consecutive stages; what must
+// potentials, 10 the FoF neighbour table, 11 / 12 the periodic FoF's images.  Slot 0 is reused by consecutive stages; what must
 // survive a call into another stage lives in a slot that no stage it calls uses.
 int workspace(size_t bytes, void **ptr, cudaStream_t stream, int slot = 0);
 

@@ -27,10 +27,12 @@ import numpy as np
 from . import _lib
 
 
-def fof_labels(x, y, z, linking_length):
+def fof_labels(x, y, z, linking_length, boxsize=None):
     """Canonical FoF labels: smallest member index of each particle's group, -1 if alone.
 
     x, y, z: float64 NumPy arrays (host) or CUDA torch tensors (device, used in place).
+    boxsize: None (non-periodic, as fof.py) or the side of a periodic box [0, boxsize)^3 whose
+    faces the groups may cross (nearest-image distances; boxsize >= 3 linking lengths).
     Returns int32 labels on the same side as the inputs.
     """
     if _lib._is_torch(x):
@@ -46,9 +48,15 @@ def fof_labels(x, y, z, linking_length):
             raise ValueError("x, y and z must have the same length")
         labels = np.empty(n, dtype=np.int32)
     ng = ctypes.c_int64(0)
-    st = _lib.lib().halma_fof(n, _lib.ptr(px), _lib.ptr(py), _lib.ptr(pz), float(linking_length),
-                              _lib.ptr(labels), ctypes.byref(ng), _lib.stream_of(px, labels))
-    _lib.check(st, "halma_fof")
+    if boxsize is None:
+        st = _lib.lib().halma_fof(n, _lib.ptr(px), _lib.ptr(py), _lib.ptr(pz), float(linking_length),
+                                  _lib.ptr(labels), ctypes.byref(ng), _lib.stream_of(px, labels))
+        _lib.check(st, "halma_fof")
+    else:
+        st = _lib.lib().halma_fof_periodic(n, _lib.ptr(px), _lib.ptr(py), _lib.ptr(pz), float(linking_length),
+                                           float(boxsize), _lib.ptr(labels), ctypes.byref(ng),
+                                           _lib.stream_of(px, labels))
+        _lib.check(st, "halma_fof_periodic")
     return labels
 
 
@@ -78,18 +86,20 @@ def _split(offsets, members):
     return [members[offsets[g]:offsets[g + 1]] for g in range(len(offsets) - 1)]
 
 
-def friends_of_friends(data, linking_length):
+def friends_of_friends(data, linking_length, boxsize=None):
+    """fof.py:18-79; ``boxsize`` (an addition, None by default as in the reference) makes the
+    box periodic, as ``KDTree(data, boxsize=...)`` would."""
     data = np.asarray(data, dtype=np.float64)
     if data.ndim != 2 or data.shape[1] != 3:
         raise ValueError("data must have shape (N, 3)")
     lab = fof_labels(np.ascontiguousarray(data[:, 0]), np.ascontiguousarray(data[:, 1]),
-                     np.ascontiguousarray(data[:, 2]), linking_length)
+                     np.ascontiguousarray(data[:, 2]), linking_length, boxsize)
     off, mem = fof_groups(lab, 2)
     return [g.tolist() for g in _split(off, mem)]
 
 
-def friends_of_friends_serial(st_x, st_y, st_z, linking_length):
-    lab = fof_labels(st_x, st_y, st_z, linking_length)
+def friends_of_friends_serial(st_x, st_y, st_z, linking_length, boxsize=None):
+    lab = fof_labels(st_x, st_y, st_z, linking_length, boxsize)
     off, mem = fof_groups(lab, 2)
     return [g.tolist() for g in _split(off, mem)]
 
