@@ -110,3 +110,28 @@ def test_far_offsets_and_elongated_boxes(cuda):
     chain = np.concatenate([chain, chain[::7] + np.array([0.0, 1.0, 0.0])])   # a second, sparser line
     lab = fof.fof_labels(chain[:, 0].copy(), chain[:, 1].copy(), chain[:, 2].copy(), 0.001)
     assert np.array_equal(lab, oracle.fof_labels(chain[:, 0], chain[:, 1], chain[:, 2], 0.001))
+
+
+def test_flat_and_thin_grids(cuda):
+    """Grids one cell thick on one or two axes (planes and lines of particles): the neighbour
+    keys of the padded key grid wrap across a row or column end there on every cell, and must
+    land on the pad, never on a cell of the next row."""
+    rng = np.random.default_rng(29)
+    ll = 0.001
+    cases = []
+    # planes z = const (one cell in z), y = const (one cell in y)
+    pl = rng.uniform(0, 0.2, (20_000, 3))
+    cases.append((pl[:, 0], pl[:, 1], np.full(len(pl), 0.5)))
+    cases.append((pl[:, 0], np.full(len(pl), -0.25), pl[:, 1]))
+    # lines along x, y and z with steps of 0.5-1.2 LL and a parallel line 1.5 LL away
+    for axis in range(3):
+        t = np.cumsum(rng.uniform(0.5, 1.2, 5000)) * ll
+        a = [np.full(len(t), 0.3), np.full(len(t), 0.3), np.full(len(t), 0.3)]
+        a[axis] = t
+        b = [v.copy() for v in a]
+        b[(axis + 1) % 3] = b[(axis + 1) % 3] + 1.5 * ll
+        cases.append(tuple(np.concatenate([u, v]) for u, v in zip(a, b)))
+    for k, (x, y, z) in enumerate(cases):
+        x, y, z = (np.ascontiguousarray(v, dtype=np.float64) for v in (x, y, z))
+        lab = fof.fof_labels(x, y, z, ll)
+        assert np.array_equal(lab, oracle.fof_labels(x, y, z, ll)), k
