@@ -102,20 +102,29 @@ struct Stager {
             if (it.host) it.off = L.add(it.bytes);
     }
     // Host inputs are copied on s, or (items added as late) on late_s, which the caller makes
-    // s wait for before their first use.
-    int bind_and_upload(void *base, cudaStream_t s, cudaStream_t late_s = nullptr) {
-        for (auto &it : items) {
-            if (!it.user || it.bytes == 0) {
-                *it.slot = const_cast<void *>(it.user);
-                continue;
+    // s wait for before their first use.  With after_ev, the late copies start once the copies
+    // on s have been done (after_ev is recorded on s and late_s waits for it).
+    int bind_and_upload(void *base, cudaStream_t s, cudaStream_t late_s = nullptr, cudaEvent_t after_ev = nullptr) {
+        for (int pass = 0; pass < 2; ++pass) {   // the items on s first, then the late ones
+            if (pass == 1 && late_s && after_ev) {
+                HALMA_CUDA(cudaEventRecord(after_ev, s));
+                HALMA_CUDA(cudaStreamWaitEvent(late_s, after_ev, 0));
             }
-            if (it.host) {
-                *it.slot = at<void>(base, it.off);
-                if (it.in)
-                    HALMA_CUDA(cudaMemcpyAsync(*it.slot, it.user, it.bytes, cudaMemcpyHostToDevice,
-                                               it.late && late_s ? late_s : s));
-            } else {
-                *it.slot = const_cast<void *>(it.user);
+            for (auto &it : items) {
+                const bool late = it.late && late_s;
+                if (late != (pass == 1)) continue;
+                if (!it.user || it.bytes == 0) {
+                    *it.slot = const_cast<void *>(it.user);
+                    continue;
+                }
+                if (it.host) {
+                    *it.slot = at<void>(base, it.off);
+                    if (it.in)
+                        HALMA_CUDA(cudaMemcpyAsync(*it.slot, it.user, it.bytes, cudaMemcpyHostToDevice,
+                                                   late ? late_s : s));
+                } else {
+                    *it.slot = const_cast<void *>(it.user);
+                }
             }
         }
         return HALMA_OK;

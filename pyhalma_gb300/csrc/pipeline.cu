@@ -40,11 +40,12 @@ __global__ void scatter_bound_kernel(int64_t nm, const int *__restrict__ members
 // A second stream per device, for the host-to-device copies of the velocities and masses,
 // which overlap the FoF stage (it reads positions only), and for the copies of the labels and
 // the groups to the caller, which overlap the unbinding.  `done` marks the end of the uploads,
-// `groups` the point where the labels and the groups are final.
+// `groups` the point where the labels and the groups are final and the halo offsets read.
 struct SideStream {
     cudaStream_t s = nullptr;
     cudaEvent_t done = nullptr;
     cudaEvent_t groups = nullptr;
+    cudaEvent_t pos = nullptr;   // the positions' uploads have been issued on the main stream
 };
 
 int side_stream(SideStream **out) {
@@ -54,6 +55,7 @@ int side_stream(SideStream **out) {
         HALMA_CUDA(cudaStreamCreateWithFlags(&ss.s, cudaStreamNonBlocking));
         HALMA_CUDA(cudaEventCreateWithFlags(&ss.done, cudaEventDisableTiming));
         HALMA_CUDA(cudaEventCreateWithFlags(&ss.groups, cudaEventDisableTiming));
+        HALMA_CUDA(cudaEventCreateWithFlags(&ss.pos, cudaEventDisableTiming));
     }
     *out = &ss;
     return HALMA_OK;
@@ -143,10 +145,11 @@ extern "C" int halma_find_haloes(int64_t n, const double *x, const double *y, co
         void *p = nullptr;
     } buf;
     HALMA_TRY(workspace(L.total, &buf.p, st, 1));
-    // velocities and masses from host memory are copied on a side stream while FoF runs
+    // velocities and masses from host memory are copied on a side stream while FoF runs, after
+    // the positions (so that the positions, which FoF waits for, have the link to themselves)
     SideStream *side = nullptr;
     HALMA_TRY(side_stream(&side));
-    HALMA_TRY(sg.bind_and_upload(buf.p, st, side->s));
+    HALMA_TRY(sg.bind_and_upload(buf.p, st, side->s, side->pos));
     HALMA_CUDA(cudaEventRecord(side->done, side->s));
     int *dlab = at<int>(buf.p, o_lab);
     int64_t *doff = at<int64_t>(buf.p, o_off);
@@ -174,6 +177,17 @@ extern "C" int halma_find_haloes(int64_t n, const double *x, const double *y, co
     std::thread early;
     JoinOnExit join_early{early};
     const OutCopy outs[3] = {{labels, dlab, 4ull * n}, {halo_offsets, doff, 8ull * (ng + 1)}, {members, dmem, 4ull * nm}};
+    HALMA_CUDA(cudaMemsetAsync(dbnd, 0, n, st));
+    HALMA_CUDA(cudaStreamWaitEvent(st, side->done, 0));
+    const int g = std::min(device_sm_count() * 8, grid_for(std::max<int64_t>(nm, 1), 256));
+    std::vector<int64_t> h_off(ng + 1);
+    if (ng > 0) {
+        HALMA_LAUNCH(gather7_kernel, g, 256, 0, st, nm, dmem, dx, dy, dz, dvx, dvy, dvz, dm, g7);
+        HALMA_CUDA(cudaMemcpyAsync(h_off.data(), doff, 8ull * (ng + 1), cudaMemcpyDeviceToHost, st));
+        HALMA_CUDA(cudaStreamSynchronize(st));
+    }
+    // started only now, so that the halo offsets above did not queue behind them on the
+    // device-to-host copy engine
     if (fits) {
         HALMA_CUDA(cudaEventRecord(side->groups, st));
         const int dev = current_device();
@@ -182,14 +196,7 @@ extern "C" int halma_find_haloes(int64_t n, const double *x, const double *y, co
             if (early_status != HALMA_OK) early_msg = halma_last_error();
         });
     }
-    HALMA_CUDA(cudaMemsetAsync(dbnd, 0, n, st));
-    HALMA_CUDA(cudaStreamWaitEvent(st, side->done, 0));
     if (ng > 0) {
-        const int g = std::min(device_sm_count() * 8, grid_for(nm, 256));
-        HALMA_LAUNCH(gather7_kernel, g, 256, 0, st, nm, dmem, dx, dy, dz, dvx, dvy, dvz, dm, g7);
-        std::vector<int64_t> h_off(ng + 1);
-        HALMA_CUDA(cudaMemcpyAsync(h_off.data(), doff, 8ull * (ng + 1), cudaMemcpyDeviceToHost, st));
-        HALMA_CUDA(cudaStreamSynchronize(st));
         if (prof.enabled) HALMA_CUDA(cudaEventRecord(ev[2], st));
         HALMA_TRY(unbind_device(nm, (int)ng, doff, h_off.data(), g7, g7 + nm, g7 + 2 * nm, g7 + 3 * nm, g7 + 4 * nm,
                                 g7 + 5 * nm, g7 + 6 * nm, p, bs, nullptr, dhalo, st));
