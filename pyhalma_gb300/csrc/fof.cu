@@ -872,7 +872,7 @@ __global__ void __launch_bounds__(256, 6) link_kernel(
 // Consecutive sorted positions mostly share a root (a cell, a group), so the lanes of a warp
 // first take the minimum per distinct root and issue one atomicMin each.  The loop runs the
 // same number of rounds on every lane of a warp (blockDim.x is a multiple of 32).
-__global__ void root_kernel(int n, const float4 *__restrict__ rec, int *parent,
+__global__ void root_kernel(int n, const int *__restrict__ idx, int *parent,
                             const unsigned char *__restrict__ has, int *__restrict__ root,
                             int *__restrict__ minidx, int *err) {
     const int lane = threadIdx.x & 31;
@@ -882,7 +882,7 @@ __global__ void root_kernel(int n, const float4 *__restrict__ rec, int *parent,
         if (k < n) {
             r = uf_find(parent, (int)k, err);
             root[k] = r;
-            if (has[k]) v = __float_as_int(rec[k].w);
+            if (has[k]) v = idx[k];
         }
         unsigned todo = __ballot_sync(0xffffffffu, v != INT_MAX);
         while (todo) {
@@ -896,11 +896,11 @@ __global__ void root_kernel(int n, const float4 *__restrict__ rec, int *parent,
     }
 }
 
-__global__ void label_kernel(int n, const float4 *__restrict__ rec, const unsigned char *__restrict__ has,
+__global__ void label_kernel(int n, const int *__restrict__ idx, const unsigned char *__restrict__ has,
                              const int *__restrict__ root, const int *__restrict__ minidx,
                              int *__restrict__ labels, int *__restrict__ ngroups) {
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
-        const int i = __float_as_int(rec[k].w);
+        const int i = idx[k];
         const int r = root[k];
         labels[i] = has[k] ? minidx[r] : -1;
         if (has[k] && r == k) atomicAdd(ngroups, 1);
@@ -1162,8 +1162,9 @@ int fof_core(int n, const double *x, const double *y, const double *z, FofGeom g
     HALMA_LAUNCH(link_kernel, sms * 8, 32 * kFofWarps, 0, st, rec, items, cnt + 1, cnt + 5, nbinfo, g, x, y, z,
                  parent, has, cnt + 3);
     HALMA_TRY(mark(6));
-    HALMA_LAUNCH(root_kernel, g1, 256, 0, st, n, rec, parent, has, root, minidx, cnt + 3);
-    HALMA_LAUNCH(label_kernel, g1, 256, 0, st, n, rec, has, root, minidx, labels, cnt + 2);
+    // the sorted original indices (4 bytes a position) rather than the records' 16
+    HALMA_LAUNCH(root_kernel, g1, 256, 0, st, n, vout, parent, has, root, minidx, cnt + 3);
+    HALMA_LAUNCH(label_kernel, g1, 256, 0, st, n, vout, has, root, minidx, labels, cnt + 2);
     HALMA_TRY(mark(7));
     int hc[4];
     HALMA_CUDA(cudaMemcpyAsync(hc, cnt, sizeof(hc), cudaMemcpyDeviceToHost, st));
