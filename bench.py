@@ -510,6 +510,21 @@ def run_gpu(args):
 
     # end to end through the C ABI from pinned host buffers (copies inside the timed region)
     _lib.set_profiling(False)
+
+    def h2d_gbs():
+        """The host-to-device copy rate of the positions (pinned -> HBM), for context: the
+        positions' upload is the one copy on the end-to-end path that nothing overlaps."""
+        dst = [torch.empty_like(t, device=dev) for t in pinned[:3]]
+        torch.cuda.synchronize()
+        c0, c1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        c0.record(stream)
+        for d_, h_ in zip(dst, pinned[:3]):
+            d_.copy_(h_, non_blocking=True)
+        c1.record(stream)
+        c1.synchronize()
+        return 3 * 8 * n / (c0.elapsed_time(c1) * 1e-3) / 1e9
+
+    h2d_before = h2d_gbs()
     e2e_ms, e2e_wall = [], []
     sampler_e2e = ClockSampler(local)
     sampler_e2e.start()
@@ -526,6 +541,7 @@ def run_gpu(args):
             e2e_ms.append(e0.elapsed_time(e1))
             e2e_wall.append((time.perf_counter() - w0) * 1e3)
     clocks_e2e = sampler_e2e.stop()
+    h2d_after = h2d_gbs()
     ng = hc.n_haloes
     nm = int(hc.offsets[-1]) if ng else 0
     h2d = 7 * 8 * n
@@ -617,7 +633,8 @@ def run_gpu(args):
             "e2e": {"value": n * world / (e2e_step * 1e-3), "unit": "particles/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "ms_per_step": e2e_step,
                     "steps_ms": [round(v, 2) for v in e2e_ms], "wall_ms_per_step": statistics.mean(e2e_wall),
-                    "clocks": clocks_e2e},
+                    "clocks": clocks_e2e,
+                    "h2d_positions_gbs_before_after": [round(h2d_before, 1), round(h2d_after, 1)]},
             "gpu_launches": launches, "clocks": clocks, "fp64_path": fp64, "wall_s_timed": wall}
     if rank == 0 and world == 1 and not args.skip_cpu:
         import oracle
