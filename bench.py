@@ -451,6 +451,7 @@ def run_gpu(args):
     fp32_peak = max(_lib.measure_fp32_fma_rate(packed=True)[0], _lib.measure_fp32_fma_rate(packed=False)[0])
     # the ceiling of the pair arithmetic itself (FP32 pipe and special-function unit together)
     pair_ceiling = _lib.measure_pair_rate()[0]
+    term_ceiling = _lib.measure_term_rate()[0]   # the same for the tile kernel's per-particle terms
 
     def barrier():
         torch.cuda.synchronize()
@@ -609,6 +610,15 @@ def run_gpu(args):
                       "frac": achieved / fp32_peak if fp32_peak else None,
                       "traffic_ub_pair_kernel": traffic.get("ub_pair_kernel_bytes_per_launch"),
                       "fp32_pipe_frac": pipe, "sym_pair_terms": sym_pairs,
+                      "tile_kernel_ceiling": {
+                          "terms_per_s": term_ceiling,
+                          "kernel_terms_per_s": (pairs - sym_pairs) / ((pair_ms - sym_ms) * 1e-3)
+                          if pair_ms > sym_ms else 0.0,
+                          "frac": ((pairs - sym_pairs) / ((pair_ms - sym_ms) * 1e-3)) / term_ceiling
+                          if pair_ms > sym_ms and term_ceiling else None,
+                          "note": "ub_pair_kernel (incremental passes and the small haloes' tiles) against the "
+                                  "library's term-arithmetic kernel (halma_measure_term_rate: 3 sub + 3 fma + 1 fma "
+                                  "as f32x2 and one rsqrt per term, 4 targets per lane, full occupancy)"},
                       "pairs_per_launch": pairs / max(n_pair_launches, 1),
                       "ms_per_launch": pair_ms / max(n_pair_launches, 1), "launches_timed": n_pair_launches,
                       "last_step_passes_pairs_ms_sympairs_symms": per_pass}

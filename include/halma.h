@@ -103,6 +103,10 @@ int         halma_measure_fp32_fma_rate(int32_t packed, int32_t iters, double *t
  * unit both to their throughput, so its rate, not either peak alone, is the ceiling of the
  * symmetric block kernel. */
 int         halma_measure_pair_rate(int32_t iters, double *pairs_per_s, double *ms, halma_stream_t stream);
+/* Measurement hook (no reference counterpart): the same for the tile kernel of the incremental
+ * passes, whose pair terms are evaluated for one particle each: per term 3 sub + 3 fma + 1 fma
+ * as f32x2 instructions and one rsqrt, 4 targets per lane, in pair terms per second. */
+int         halma_measure_term_rate(int32_t iters, double *terms_per_s, double *ms, halma_stream_t stream);
 /* Debug knob (no reference counterpart): the iteration bound of every union-find loop of the
  * FoF kernels (find walks, CAS retries).  A loop that reaches it stops, and the FoF call
  * returns HALMA_ERR_NOT_CONVERGED with the device still usable.  cap < 0 restores the default

@@ -92,6 +92,7 @@ SIGNATURES = {
     "halma_profile_fof_stages": ([_P, _I32], ctypes.c_int),
     "halma_measure_fp32_fma_rate": ([_I32, _I32, _P, _P, _P], ctypes.c_int),
     "halma_measure_pair_rate": ([_I32, _P, _P, _P], ctypes.c_int),
+    "halma_measure_term_rate": ([_I32, _P, _P, _P], ctypes.c_int),
     "halma_fof": ([_I64, _P, _P, _P, _F64, _P, _P, _P], ctypes.c_int),
     "halma_fof_periodic": ([_I64, _P, _P, _P, _F64, _F64, _P, _P, _P], ctypes.c_int),
     "halma_fof_groups": ([_I64, _P, _I32, _P, _P, _P, _P], ctypes.c_int),
@@ -185,6 +186,14 @@ def measure_pair_rate(iters=1 << 12):
     r, ms = ctypes.c_double(0), ctypes.c_double(0)
     check(lib().halma_measure_pair_rate(int(iters), ctypes.byref(r), ctypes.byref(ms), None),
           "halma_measure_pair_rate")
+    return r.value, ms.value
+
+
+def measure_term_rate(iters=1 << 12):
+    """(pair terms/s, ms) of the tile kernel's arithmetic ceiling on the current device."""
+    r, ms = ctypes.c_double(0), ctypes.c_double(0)
+    check(lib().halma_measure_term_rate(int(iters), ctypes.byref(r), ctypes.byref(ms), None),
+          "halma_measure_term_rate")
     return r.value, ms.value
 
 

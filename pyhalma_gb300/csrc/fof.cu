@@ -266,6 +266,59 @@ __device__ __forceinline__ void quarter_split(double t, long long qmax, long lon
     w = fe > 0 ? __int_as_float((fe << 23) | (int)(((v << lz) >> 40) & 0x7fffff)) : 0.f;
 }
 
+// floor(x * s4 * 2^24) + B exactly, with integer operations only (s4 = S * 2^(es - 52) a
+// positive double with 53-bit mantissa S): the product of the two 53-bit mantissas as a 128-bit
+// integer, shifted to 24 fraction bits and floored (towards -inf for negative x).  A map that
+// is exact to 2^-24 quarter cells and monotone in x, for callers that keep |x * s4| and |B|
+// below 2^37 quarter cells.
+__device__ __forceinline__ long long fixed_quarter(double x, unsigned long long S, int es, long long B) {
+    const long long bits = __double_as_longlong(x);
+    int ex = (int)((bits >> 52) & 0x7ff);
+    unsigned long long X = (unsigned long long)(bits & 0xfffffffffffffll);
+    if (ex == 0)
+        ex = 1;   // zero or subnormal: no implicit bit
+    else
+        X |= 1ull << 52;
+    const unsigned long long lo = X * S, hi = __umul64hi(X, S);
+    const int sh = 80 - (ex - 1023) - es;   // (X * S) * 2^-sh = x * s4 * 2^24
+    unsigned long long mag;
+    bool rem;
+    if (sh <= 0) {   // outside the callers' range: saturate
+        mag = 1ull << 62;
+        rem = false;
+    } else if (sh < 64) {
+        mag = (hi << (64 - sh)) | (lo >> sh);
+        rem = (lo & ((1ull << sh) - 1)) != 0;
+    } else if (sh < 128) {
+        mag = hi >> (sh - 64);
+        rem = lo != 0 || (hi & ((1ull << (sh - 64)) - 1)) != 0;
+    } else {
+        mag = 0;
+        rem = (hi | lo) != 0;
+    }
+    const long long p = bits < 0 ? -(long long)mag - (rem ? 1 : 0) : (long long)mag;
+    return p + B;
+}
+
+// quarter_split for a fixed-point t (24 fraction bits): floor(t) clamped to [0, qmax] and the
+// remainder t - 4 * floor(t / 4) as a float truncated to 24 significant bits.
+__device__ __forceinline__ void quarter_split_fixed(long long t, long long qmax, long long &q, float &w) {
+    if (t < 0) {
+        q = 0;
+        w = 0.f;
+        return;
+    }
+    q = min(t >> 24, qmax);
+    const unsigned long long v = (unsigned long long)(t - ((q >> 2) << 26));
+    if (v == 0) {
+        w = 0.f;
+        return;
+    }
+    const int lz = __clzll((long long)v);
+    const int fe = (63 - lz) - 24 + 127;   // biased exponent of v * 2^-24
+    w = __int_as_float((fe << 23) | (int)(((v << lz) >> 40) & 0x7fffff));
+}
+
 // Sort key: row-major cell index, then (when there is room) the particle's 4 x 4 x 4 sub-cell in
 // Morton order, so that each 32-particle chunk of a crowded cell is spatially compact.  The
 // order of particles inside a cell does not change the partition.  The kernel also writes the
@@ -277,12 +330,23 @@ __device__ __forceinline__ void quarter_split(double t, long long qmax, long lon
 // here is harmless as long as it is the same for every particle: the cell side is
 // ll * (1 + 2^-20), so two points within ll of each other stay in the same or adjacent cells
 // whenever the cell coordinate's error is below 2^-21 cells (it is ~1e-12 cells).
+//
+// FIXED (plain FoF on coordinates and grids within 2^37 quarter cells): the quarter-cell
+// coordinate is the exact integer map fixed_quarter instead of the FP64 FMA, so that the
+// kernel issues no FP64 instruction at all (with three FMAs a particle it was FP64-bound:
+// ncu showed the FP64 pipe 78 % busy).  Both maps are consistent over all particles, which is
+// all the cell assignment needs; B = floor(-origin * (4 / cell) * 2^24) per axis.
+template <bool FIXED>
 __global__ void keys_kernel(const double *__restrict__ x, const double *__restrict__ y,
-                            const double *__restrict__ z, int n, FofGeom g, SegGeom sg,
-                            uint64_t *__restrict__ keys, int *__restrict__ vals, float4 *__restrict__ pre) {
+                            const double *__restrict__ z, int n, FofGeom g, SegGeom sg, long long Bx, long long By,
+                            long long Bz, uint64_t *__restrict__ keys, int *__restrict__ vals,
+                            float4 *__restrict__ pre) {
     const double s4 = 4.0 * g.inv_cell;   // exact: a power-of-two scaling
     const float cs4 = 0.25f * g.cs;
     const double bx0 = -g.xmin * s4, by0 = -g.ymin * s4, bz0 = -g.zmin * s4;
+    const long long s4bits = __double_as_longlong(s4);
+    const unsigned long long S4 = (unsigned long long)(s4bits & 0xfffffffffffffll) | (1ull << 52);
+    const int es4 = (int)((s4bits >> 52) & 0x7ff) - 1023;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         double bx = bx0, by = by0, bz = bz0;   // -origin * (4 / cell)
         long long x0 = 0, nx = g.ncx, ny = g.ncy, nz = g.ncz;
@@ -300,9 +364,15 @@ __global__ void keys_kernel(const double *__restrict__ x, const double *__restri
         // grid's edge a hair outside it), and the position inside the cell in quarter cells
         long long qx, qy, qz;
         float wx, wy, wz;
-        quarter_split(fma(x[i], s4, bx), 4 * nx - 1, qx, wx);
-        quarter_split(fma(y[i], s4, by), 4 * ny - 1, qy, wy);
-        quarter_split(fma(z[i], s4, bz), 4 * nz - 1, qz, wz);
+        if (FIXED) {
+            quarter_split_fixed(fixed_quarter(x[i], S4, es4, Bx), 4 * nx - 1, qx, wx);
+            quarter_split_fixed(fixed_quarter(y[i], S4, es4, By), 4 * ny - 1, qy, wy);
+            quarter_split_fixed(fixed_quarter(z[i], S4, es4, Bz), 4 * nz - 1, qz, wz);
+        } else {
+            quarter_split(fma(x[i], s4, bx), 4 * nx - 1, qx, wx);
+            quarter_split(fma(y[i], s4, by), 4 * ny - 1, qy, wy);
+            quarter_split(fma(z[i], s4, bz), 4 * nz - 1, qz, wz);
+        }
         const long long cx = qx >> 2, cy = qy >> 2, cz = qz >> 2;
         uint64_t key = ((uint64_t)(x0 + cx) * (uint64_t)g.ky + (uint64_t)cy) * (uint64_t)g.kz + (uint64_t)cz;
         if (g.sb) {
@@ -1122,7 +1192,20 @@ int fof_core(int n, const double *x, const double *y, const double *z, FofGeom g
     const bool stages = !sg.seg_of;   // stage times of the plain FoF only
     auto mark = [&](int k) { return stages ? prof.fof_mark(k, st) : HALMA_OK; };
     HALMA_CUDA(cudaMemsetAsync(cnt, 0, 64, st));
-    HALMA_LAUNCH(keys_kernel, g1, 256, 0, st, x, y, z, n, g, sg, kin, vin, pre);
+    // the integer map when the coordinates and the grid stay within 2^37 quarter cells (plain
+    // FoF; the segmented one has per-segment origins and keeps the FP64 map)
+    const double s4 = 4.0 * g.inv_cell, lim = 0x1p37;
+    const double bxd = -g.xmin * s4, byd = -g.ymin * s4, bzd = -g.zmin * s4;
+    double reach = fmax(fabs(g.xmin), fabs(g.xmin + g.cell * (double)g.ncx));
+    reach = fmax(reach, fmax(fabs(g.ymin), fabs(g.ymin + g.cell * (double)g.ncy)));
+    reach = fmax(reach, fmax(fabs(g.zmin), fabs(g.zmin + g.cell * (double)g.ncz))) * s4;
+    const bool fixed = !sg.seg_of && s4 >= 0x1p-1000 && reach < lim && fabs(bxd) < lim && fabs(byd) < lim &&
+                       fabs(bzd) < lim;
+    if (fixed)
+        HALMA_LAUNCH(keys_kernel<true>, g1, 256, 0, st, x, y, z, n, g, sg, (long long)floor(bxd * 0x1p24),
+                     (long long)floor(byd * 0x1p24), (long long)floor(bzd * 0x1p24), kin, vin, pre);
+    else
+        HALMA_LAUNCH(keys_kernel<false>, g1, 256, 0, st, x, y, z, n, g, sg, 0ll, 0ll, 0ll, kin, vin, pre);
     HALMA_TRY(mark(1));
     HALMA_TRY(sort_pairs_u64_i32(tmp, sort_b, kin, kout, vin, vout, n, end_bit, st));
     HALMA_TRY(mark(2));
