@@ -126,8 +126,8 @@ int halma_fof(int64_t n, const double *x, const double *y, const double *z,
               double linking_length, int32_t *labels, int64_t *n_groups,
               halma_stream_t stream);
 
-/* The same in a periodic box (the periodic option of the FoF call the survey of the path asks
- * for; fof.py:20 itself builds its KDTree without a box size).  Positions must lie in
+/* The same in a periodic box (an opt-in option: fof.py:20 itself builds its KDTree without a
+ * box size; this is what the same flood fill gives with KDTree(data, boxsize=box)).  Positions must lie in
  * [0, box)^3 (HALMA_ERR_INVALID otherwise) and box must be at least 3 linking lengths.  Two
  * particles are friends when the distance between one and the nearest periodic image of the
  * other passes the same predicate, the image coordinate being x +- box rounded in IEEE

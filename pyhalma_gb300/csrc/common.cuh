@@ -84,6 +84,7 @@ struct Stager {
         size_t off;
         void **slot;
         bool late;   // uploaded on the late stream of bind_and_upload, when one is given
+        cudaEvent_t mark = nullptr;   // a marker, not an array: the event recorded at this point
     };
     std::vector<Item> items;
     bool any_host = false;
@@ -95,6 +96,13 @@ struct Stager {
                 reinterpret_cast<void **>(const_cast<typename std::remove_const<U>::type **>(slot)), late};
         if (user && count > 0) it.host = !is_device_pointer(user);
         any_host |= it.host;
+        items.push_back(it);
+    }
+    // Records ev on the stream of the copies before it (s, or late_s for late), once those
+    // copies have been issued.
+    void add_mark(cudaEvent_t ev, bool late = false) {
+        Item it{nullptr, 0, false, false, false, 0, nullptr, late};
+        it.mark = ev;
         items.push_back(it);
     }
     void plan(Layout &L) {
@@ -113,6 +121,10 @@ struct Stager {
             for (auto &it : items) {
                 const bool late = it.late && late_s;
                 if (late != (pass == 1)) continue;
+                if (it.mark) {
+                    HALMA_CUDA(cudaEventRecord(it.mark, late ? late_s : s));
+                    continue;
+                }
                 if (!it.user || it.bytes == 0) {
                     *it.slot = const_cast<void *>(it.user);
                     continue;

@@ -530,9 +530,9 @@ __global__ void __launch_bounds__(256) dense_cell_kernel(const int *__restrict__
                 if (!occ[r]) continue;
                 const int m = lane + 32 * r, L = lab[w][m];
                 if (L != lo[r]) parent[lo[r]] = L;   // run head under the component's smallest run head
-                int members = 0;                     // occupied sub-cells in this component
-                for (int t = 0; t < 64; ++t) members += lab[w][t] == L ? 1 : 0;
-                if (members > 1 || hi[r] - lo[r] > 1)
+                // the component holds another sub-cell exactly when an occupied sub-cell is
+                // among this one's guaranteed-link neighbours
+                if ((nbmask[m] & occm) != 0 || hi[r] - lo[r] > 1)
                     for (int q = lo[r]; q < hi[r]; ++q) has[q] = 1;
             }
             if (lane == 0) conn[c] = one ? 1 : 0;

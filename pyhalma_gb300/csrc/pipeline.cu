@@ -14,20 +14,24 @@
 namespace halma {
 namespace {
 
-__global__ void gather7_kernel(int64_t nm, const int *__restrict__ members, const double *__restrict__ x,
-                               const double *__restrict__ y, const double *__restrict__ z,
-                               const double *__restrict__ vx, const double *__restrict__ vy,
-                               const double *__restrict__ vz, const double *__restrict__ m,
-                               double *__restrict__ out /* 7 x nm */) {
+// Members gathered into halo-contiguous arrays: field f of member k goes to
+// out[col[f] * nm + k] (the 7 x nm array x, y, z, vx, vy, vz, m).
+template <int NF>
+struct GatherSrc {
+    const double *src[NF];
+    int col[NF];
+};
+
+template <int NF>
+__global__ void gather_kernel(int64_t nm, const int *__restrict__ members, GatherSrc<NF> g,
+                              double *__restrict__ out) {
     for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < nm; k += (int64_t)gridDim.x * blockDim.x) {
         const int i = members[k];
-        out[k] = x[i];
-        out[nm + k] = y[i];
-        out[2 * nm + k] = z[i];
-        out[3 * nm + k] = vx[i];
-        out[4 * nm + k] = vy[i];
-        out[5 * nm + k] = vz[i];
-        out[6 * nm + k] = m[i];
+        double v[NF];
+#pragma unroll
+        for (int f = 0; f < NF; ++f) v[f] = g.src[f][i];
+#pragma unroll
+        for (int f = 0; f < NF; ++f) out[g.col[f] * nm + k] = v[f];
     }
 }
 
@@ -37,15 +41,18 @@ __global__ void scatter_bound_kernel(int64_t nm, const int *__restrict__ members
         bound[members[k]] = bs[k];
 }
 
-// A second stream per device, for the host-to-device copies of the velocities and masses,
-// which overlap the FoF stage (it reads positions only), and for the copies of the labels and
-// the groups to the caller, which overlap the unbinding.  `done` marks the end of the uploads,
-// `groups` the point where the labels and the groups are final and the halo offsets read.
+// A second stream per device, for the host-to-device copies of the masses and velocities,
+// which overlap the FoF stage (it reads positions only), for the gather of the velocities,
+// which overlaps the first unbinding pass's pair kernels, and for the copies of the labels and
+// the groups to the caller, which overlap the unbinding.
 struct SideStream {
     cudaStream_t s = nullptr;
-    cudaEvent_t done = nullptr;
-    cudaEvent_t groups = nullptr;
-    cudaEvent_t pos = nullptr;   // the positions' uploads have been issued on the main stream
+    cudaEvent_t pos = nullptr;       // the positions' uploads have been issued on the main stream
+    cudaEvent_t mass = nullptr;      // the masses are on the device
+    cudaEvent_t done = nullptr;      // all uploads are done
+    cudaEvent_t members = nullptr;   // the groups' member lists are final (main stream)
+    cudaEvent_t vel = nullptr;       // the members' velocities are gathered
+    cudaEvent_t groups = nullptr;    // labels and groups final, the halo offsets read
 };
 
 int side_stream(SideStream **out) {
@@ -53,9 +60,8 @@ int side_stream(SideStream **out) {
     SideStream &ss = m[current_device()];
     if (!ss.s) {
         HALMA_CUDA(cudaStreamCreateWithFlags(&ss.s, cudaStreamNonBlocking));
-        HALMA_CUDA(cudaEventCreateWithFlags(&ss.done, cudaEventDisableTiming));
-        HALMA_CUDA(cudaEventCreateWithFlags(&ss.groups, cudaEventDisableTiming));
-        HALMA_CUDA(cudaEventCreateWithFlags(&ss.pos, cudaEventDisableTiming));
+        for (cudaEvent_t *e : {&ss.pos, &ss.mass, &ss.done, &ss.members, &ss.vel, &ss.groups})
+            HALMA_CUDA(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
     }
     *out = &ss;
     return HALMA_OK;
@@ -89,6 +95,13 @@ struct JoinOnExit {
     ~JoinOnExit() {
         if (t.joinable()) t.join();
     }
+};
+
+// Waits for a stream on every way out of a scope (no copy from the caller's host buffers
+// outlives the call that was given them, whatever error ended it).
+struct SyncOnExit {
+    cudaStream_t s;
+    ~SyncOnExit() { cudaStreamSynchronize(s); }
 };
 
 }  // namespace
@@ -126,13 +139,17 @@ extern "C" int halma_find_haloes(int64_t n, const double *x, const double *y, co
     Stager sg;
     const double *dx = nullptr, *dy = nullptr, *dz = nullptr, *dvx = nullptr, *dvy = nullptr, *dvz = nullptr,
                  *dm = nullptr;
+    SideStream *side = nullptr;
+    HALMA_TRY(side_stream(&side));
+    SyncOnExit side_idle{side->s};
     sg.add(x, n, true, false, &dx);
     sg.add(y, n, true, false, &dy);
     sg.add(z, n, true, false, &dz);
+    sg.add(m, n, true, false, &dm, true);
+    sg.add_mark(side->mass, true);
     sg.add(vx, n, true, false, &dvx, true);
     sg.add(vy, n, true, false, &dvy, true);
     sg.add(vz, n, true, false, &dvz, true);
-    sg.add(m, n, true, false, &dm, true);
     // private scratch for everything that must outlive the individual stages
     Layout L;
     sg.plan(L);
@@ -145,10 +162,9 @@ extern "C" int halma_find_haloes(int64_t n, const double *x, const double *y, co
         void *p = nullptr;
     } buf;
     HALMA_TRY(workspace(L.total, &buf.p, st, 1));
-    // velocities and masses from host memory are copied on a side stream while FoF runs, after
-    // the positions (so that the positions, which FoF waits for, have the link to themselves)
-    SideStream *side = nullptr;
-    HALMA_TRY(side_stream(&side));
+    // masses and velocities from host memory are copied on a side stream while FoF runs, after
+    // the positions (so that the positions, which FoF waits for, have the link to themselves);
+    // the masses first, which the first unbinding pass needs from its start
     HALMA_TRY(sg.bind_and_upload(buf.p, st, side->s, side->pos));
     HALMA_CUDA(cudaEventRecord(side->done, side->s));
     int *dlab = at<int>(buf.p, o_lab);
@@ -178,11 +194,26 @@ extern "C" int halma_find_haloes(int64_t n, const double *x, const double *y, co
     JoinOnExit join_early{early};
     const OutCopy outs[3] = {{labels, dlab, 4ull * n}, {halo_offsets, doff, 8ull * (ng + 1)}, {members, dmem, 4ull * nm}};
     HALMA_CUDA(cudaMemsetAsync(dbnd, 0, n, st));
-    HALMA_CUDA(cudaStreamWaitEvent(st, side->done, 0));
+    // Velocities copied from host memory are waited for only by the first pass's energy
+    // kernel (FP32C path): on a slow host link their upload then overlaps the first pass's
+    // pair kernels instead of delaying the unbinding's start.
+    const bool defer_vel = p.precision == HALMA_UNBIND_FP32C &&
+                           (!is_device_pointer(vx) || !is_device_pointer(vy) || !is_device_pointer(vz));
+    HALMA_CUDA(cudaStreamWaitEvent(st, defer_vel ? side->mass : side->done, 0));
     const int g = std::min(device_sm_count() * 8, grid_for(std::max<int64_t>(nm, 1), 256));
     std::vector<int64_t> h_off(ng + 1);
     if (ng > 0) {
-        HALMA_LAUNCH(gather7_kernel, g, 256, 0, st, nm, dmem, dx, dy, dz, dvx, dvy, dvz, dm, g7);
+        if (defer_vel) {
+            HALMA_LAUNCH(gather_kernel<4>, g, 256, 0, st, nm, dmem, (GatherSrc<4>{{dx, dy, dz, dm}, {0, 1, 2, 6}}), g7);
+            HALMA_CUDA(cudaEventRecord(side->members, st));
+            HALMA_CUDA(cudaStreamWaitEvent(side->s, side->members, 0));
+            HALMA_LAUNCH(gather_kernel<3>, g, 256, 0, side->s, nm, dmem, (GatherSrc<3>{{dvx, dvy, dvz}, {3, 4, 5}}),
+                         g7);
+            HALMA_CUDA(cudaEventRecord(side->vel, side->s));
+        } else {
+            HALMA_LAUNCH(gather_kernel<7>, g, 256, 0, st, nm, dmem,
+                         (GatherSrc<7>{{dx, dy, dz, dvx, dvy, dvz, dm}, {0, 1, 2, 3, 4, 5, 6}}), g7);
+        }
         HALMA_CUDA(cudaMemcpyAsync(h_off.data(), doff, 8ull * (ng + 1), cudaMemcpyDeviceToHost, st));
         HALMA_CUDA(cudaStreamSynchronize(st));
     }
@@ -199,7 +230,7 @@ extern "C" int halma_find_haloes(int64_t n, const double *x, const double *y, co
     if (ng > 0) {
         if (prof.enabled) HALMA_CUDA(cudaEventRecord(ev[2], st));
         HALMA_TRY(unbind_device(nm, (int)ng, doff, h_off.data(), g7, g7 + nm, g7 + 2 * nm, g7 + 3 * nm, g7 + 4 * nm,
-                                g7 + 5 * nm, g7 + 6 * nm, p, bs, nullptr, dhalo, st));
+                                g7 + 5 * nm, g7 + 6 * nm, p, bs, nullptr, dhalo, st, defer_vel ? side->vel : nullptr));
         if (prof.enabled) HALMA_CUDA(cudaEventRecord(ev[3], st));
         HALMA_LAUNCH(scatter_bound_kernel, g, 256, 0, st, nm, dmem, bs, dbnd);
     }

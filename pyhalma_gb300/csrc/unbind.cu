@@ -94,7 +94,13 @@ constexpr int kRedSums = 8;   // M, Mx, My, Mz, Mvx, Mvy, Mvz, count
 // Per member chunk of an active halo (or of every halo with force): FP64 sums over its bound
 // members.  FP64 is slow on this GPU, so the block's partials are combined by a few threads
 // in shared memory rather than by warp trees (fixed association: per thread in member order,
-// then per value four runs of 64 threads, then the four runs in order).
+// then per value four runs of 64 threads, then the four runs in order).  PART selects the
+// sums written: 0 all, 1 mass, mass-weighted positions and count (the velocities are not
+// read), 2 the mass-weighted velocities; each sum is formed the same way in every mode, so
+// modes 1 then 2 write exactly what mode 0 writes.
+__host__ __device__ constexpr bool red_wants(int part, int k) { return part == 0 || (part == 1 ? (k < 4 || k == 7) : (k >= 4 && k < 7)); }
+
+template <int PART>
 __global__ void __launch_bounds__(kSegThreads) ub_reduce_seg_kernel(
     const int64_t *__restrict__ off, const int *__restrict__ cstart, const int *__restrict__ chunk_h,
     const double *__restrict__ x, const double *__restrict__ y, const double *__restrict__ z,
@@ -121,12 +127,12 @@ __global__ void __launch_bounds__(kSegThreads) ub_reduce_seg_kernel(
         const int64_t s = in ? i : b;
         use[j] = in && bound[s];
         f[j][0] = m[s];
-        f[j][1] = x[s];
-        f[j][2] = y[s];
-        f[j][3] = z[s];
-        f[j][4] = vx[s];
-        f[j][5] = vy[s];
-        f[j][6] = vz[s];
+        f[j][1] = red_wants(PART, 1) ? x[s] : 0.0;
+        f[j][2] = red_wants(PART, 2) ? y[s] : 0.0;
+        f[j][3] = red_wants(PART, 3) ? z[s] : 0.0;
+        f[j][4] = red_wants(PART, 4) ? vx[s] : 0.0;
+        f[j][5] = red_wants(PART, 5) ? vy[s] : 0.0;
+        f[j][6] = red_wants(PART, 6) ? vz[s] : 0.0;
     }
 #pragma unroll
     for (int j = 0; j < kSegPer; ++j) {
@@ -134,7 +140,8 @@ __global__ void __launch_bounds__(kSegThreads) ub_reduce_seg_kernel(
         const double mi = f[j][0];
         v[0] += mi;
 #pragma unroll
-        for (int k = 1; k < 7; ++k) v[k] += mi * f[j][k];
+        for (int k = 1; k < 7; ++k)
+            if (red_wants(PART, k)) v[k] += mi * f[j][k];
         ++count;
     }
 #pragma unroll
@@ -153,8 +160,8 @@ __global__ void __launch_bounds__(kSegThreads) ub_reduce_seg_kernel(
     __syncthreads();
     if (threadIdx.x < kRedSums - 1) {
         const int k = threadIdx.x;
-        part[(int64_t)c * kRedSums + k] = ((q4[k][0] + q4[k][1]) + q4[k][2]) + q4[k][3];
-    } else if (threadIdx.x == kRedSums - 1) {
+        if (red_wants(PART, k)) part[(int64_t)c * kRedSums + k] = ((q4[k][0] + q4[k][1]) + q4[k][2]) + q4[k][3];
+    } else if (threadIdx.x == kRedSums - 1 && red_wants(PART, 7)) {
         int tot = 0;
         for (int w = 0; w < kSegThreads / 32; ++w) tot += wcount[w];
         part[(int64_t)c * kRedSums + kRedSums - 1] = (double)tot;
@@ -198,7 +205,8 @@ __global__ void ub_reduce_fin_kernel(int nh, const int *__restrict__ cstart, con
 // First packing, per member chunk: every member is bound before the first pass, so member
 // i of halo h goes to slot i - off[h] of the halo's padded range, re-centred on the halo's
 // centre of mass; the chunk holding the halo's end also writes the padding (zero-mass far
-// points up to the next multiple of 32).
+// points up to the next multiple of 32).  pk == nullptr writes the velocities alone, pv ==
+// nullptr the positions and indices alone.
 template <class V>
 __global__ void __launch_bounds__(kSegThreads) ub_pack_kernel(
     const int64_t *__restrict__ off, const int64_t *__restrict__ poff, const int *__restrict__ cstart,
@@ -214,10 +222,12 @@ __global__ void __launch_bounds__(kSegThreads) ub_pack_kernel(
     const int64_t b = hb + (int64_t)(c - cstart[h]) * kSeg;
     const int64_t e = min(he, b + kSeg);
     for (int64_t i = b + threadIdx.x; i < e; i += kSegThreads) {
-        V r;
-        r.x = x[i] - cx; r.y = y[i] - cy; r.z = z[i] - cz; r.w = m[i];
-        pk[pb + (i - hb)] = r;
-        pidx[pb + (i - hb)] = (int)i;
+        if (pk) {
+            V r;
+            r.x = x[i] - cx; r.y = y[i] - cy; r.z = z[i] - cz; r.w = m[i];
+            pk[pb + (i - hb)] = r;
+            pidx[pb + (i - hb)] = (int)i;
+        }
         // FP32 path: velocity relative to the bulk velocity at packing, and the mass
         if (pv) pv[pb + (i - hb)] = make_float4((float)(vx[i] - v0x), (float)(vy[i] - v0y), (float)(vz[i] - v0z),
                                                  (float)m[i]);
@@ -225,10 +235,12 @@ __global__ void __launch_bounds__(kSegThreads) ub_pack_kernel(
     if (e == he) {
         const int64_t nb = he - hb, npad = (nb + 31) & ~31ll;
         for (int64_t r = nb + threadIdx.x; r < npad; r += kSegThreads) {
-            V f;
-            f.x = f.y = f.z = kFar; f.w = 0;
-            pk[pb + r] = f;
-            pidx[pb + r] = -1;
+            if (pk) {
+                V f;
+                f.x = f.y = f.z = kFar; f.w = 0;
+                pk[pb + r] = f;
+                pidx[pb + r] = -1;
+            }
             if (pv) pv[pb + r] = make_float4(0.f, 0.f, 0.f, 0.f);
         }
     }
@@ -1342,7 +1354,7 @@ int sym_self_potential_device(const float4 *pk, int nb, float eps2, float2 *part
 int unbind_device(int64_t n, int nh, const int64_t *d_off, const int64_t *h_off, const double *x, const double *y,
                   const double *z, const double *vx, const double *vy, const double *vz, const double *m,
                   const halma_unbind_params &p, unsigned char *bound, double *phi_out, double *halo_out,
-                  cudaStream_t st) {
+                  cudaStream_t st, cudaEvent_t vel_ready) {
     const TileTable tab = tile_table();
     const bool f64 = p.precision == HALMA_UNBIND_FP64;
     // source slice length (a multiple of 32); the FP64 path sums a halo in one piece
@@ -1459,11 +1471,20 @@ int unbind_device(int64_t n, int nh, const int64_t *d_off, const int64_t *h_off,
         HALMA_LAUNCH(ub_items_fill_kernel, igrid, 256, 0, rs, nh, icount, ipre, istart, ystart, sstart, sown, cnt);
         return HALMA_OK;
     };
-    // FP64 bound mass, centre and bulk velocity per halo (active ones, or all with force)
-    auto reduce = [&](cudaStream_t rs, int force) -> int {
-        if (nchunks > 0)
-            HALMA_LAUNCH(ub_reduce_seg_kernel, nchunks, kSegThreads, 0, rs, off, dcst, dchh, x, y, z, vx, vy, vz, m,
-                         bound, hs, force, rpart);
+    // FP64 bound mass, centre and bulk velocity per halo (active ones, or all with force);
+    // part as in ub_reduce_seg_kernel (the halo state is final after parts 1 and 2 in turn)
+    auto reduce = [&](cudaStream_t rs, int force, int part = 0) -> int {
+        if (nchunks > 0) {
+            if (part == 1)
+                HALMA_LAUNCH(ub_reduce_seg_kernel<1>, nchunks, kSegThreads, 0, rs, off, dcst, dchh, x, y, z, vx, vy,
+                             vz, m, bound, hs, force, rpart);
+            else if (part == 2)
+                HALMA_LAUNCH(ub_reduce_seg_kernel<2>, nchunks, kSegThreads, 0, rs, off, dcst, dchh, x, y, z, vx, vy,
+                             vz, m, bound, hs, force, rpart);
+            else
+                HALMA_LAUNCH(ub_reduce_seg_kernel<0>, nchunks, kSegThreads, 0, rs, off, dcst, dchh, x, y, z, vx, vy,
+                             vz, m, bound, hs, force, rpart);
+        }
         HALMA_LAUNCH(ub_reduce_fin_kernel, fgrid, 256, 0, rs, nh, dcst, rpart, force, hs);
         return HALMA_OK;
     };
@@ -1490,11 +1511,15 @@ int unbind_device(int64_t n, int nh, const int64_t *d_off, const int64_t *h_off,
         auto record = [&](cudaStream_t rs, int it0, int it1) -> int {
             // first pass: centre of mass and packing into buffer 0; every pass then compacts
             // its survivors into the other buffer and sets the next pass's halo state
+            // With vel_ready, the velocities may still be arriving: the first pass's pair
+            // kernels start from the positions and masses, and the velocity sums and packed
+            // velocities follow once vel_ready has fired (an external wait: a node of the
+            // captured graph), before the first energy kernel.
             if (it0 == 0) {
-                HALMA_TRY(reduce(rs, 0));
+                HALMA_TRY(reduce(rs, 0, vel_ready ? 1 : 0));
                 if (nchunks > 0)
                     HALMA_LAUNCH(ub_pack_kernel<float4>, nchunks, kSegThreads, 0, rs, off, dpoff, dcst, dchh, x, y, z,
-                                 m, vx, vy, vz, hs, pkb[0], pvb[0], pidxb[0]);
+                                 m, vx, vy, vz, hs, pkb[0], vel_ready ? nullptr : pvb[0], pidxb[0]);
             }
             float4 *rk = at<float4>(base, o_rk);
             for (int it = it0; it < it1; ++it) {
@@ -1512,6 +1537,13 @@ int unbind_device(int64_t n, int nh, const int64_t *d_off, const int64_t *h_off,
                 HALMA_LAUNCH(ub_pair_kernel, pgrid, 256, 0, rs, pkb[a], rk, inc, dpoff, dqoff, hs, nh, istart, idesc,
                              cnt, cnt + 1, eps2, slice_len / 32, part2);
                 if (profiling) HALMA_CUDA(cudaEventRecordWithFlags(prof.ev1[it], rs, cudaEventRecordExternal));
+                if (it == 0 && vel_ready) {
+                    HALMA_CUDA(cudaStreamWaitEvent(rs, vel_ready, cudaEventWaitExternal));
+                    HALMA_TRY(reduce(rs, 0, 2));
+                    if (nchunks > 0)
+                        HALMA_LAUNCH(ub_pack_kernel<float4>, nchunks, kSegThreads, 0, rs, off, dpoff, dcst, dchh, x, y,
+                                     z, m, vx, vy, vz, hs, (float4 *)nullptr, pvb[0], (int *)nullptr);
+                }
                 HALMA_LAUNCH(ub_energy_df_kernel, sgrid, kSegThreads, 0, rs, sstart, sown, idesc, cnt + 2, dpoff, dqoff,
                              inc, pidxb[a], pvb[a], part2, phin2, phic2, x, y, z, vx, vy, vz, m, gfac_f, hs, bound,
                              phi_out, keepf, sdf);
@@ -1542,6 +1574,7 @@ int unbind_device(int64_t n, int nh, const int64_t *d_off, const int64_t *h_off,
             key.push_back((uintptr_t)slice_len);
             key.push_back((uintptr_t)incremental);
             key.push_back((uintptr_t)nchunks);
+            key.push_back((uintptr_t)vel_ready);
             for (int c = 0; c < tab.n; ++c) {
                 key.push_back((uintptr_t)tab.upper[c]);
                 key.push_back((uintptr_t)tab.t[c]);

@@ -52,6 +52,7 @@ int sym_self_potential_device(const float4 *pk, int nb, float eps2, float2 *part
 int unbind_device(int64_t n, int nh, const int64_t *d_off, const int64_t *h_off, const double *x,
                   const double *y, const double *z, const double *vx, const double *vy,
                   const double *vz, const double *m, const halma_unbind_params &p,
-                  unsigned char *bound, double *phi_out, double *halo_out, cudaStream_t st);
+                  unsigned char *bound, double *phi_out, double *halo_out, cudaStream_t st,
+                  cudaEvent_t vel_ready = nullptr);
 
 }  // namespace halma

@@ -45,9 +45,11 @@ def test_find_haloes_matches_oracle_composition(cuda):
 
 
 def test_find_haloes_device_arrays_and_capacity(cuda):
-    """The one-call path from device arrays gives what it gives from host arrays; through the
-    C ABI, a halo capacity below the groups found returns HALMA_ERR_CAPACITY with the count set
-    and the labels and bound flags filled (the early label copy is not started then)."""
+    """The one-call path from device arrays gives what it gives from host arrays (where the
+    first pass starts before the velocities have arrived, and a second call replays the
+    captured passes with their wait on the velocities); through the C ABI, a halo capacity
+    below the groups found returns HALMA_ERR_CAPACITY with the count set and the labels and
+    bound flags filled (the early label copy is not started then)."""
     import ctypes
     import torch
     from pyhalma_gb300 import _lib
@@ -62,6 +64,9 @@ def test_find_haloes_device_arrays_and_capacity(cuda):
     assert np.array_equal(dev.members.cpu().numpy(), host.members)
     assert np.array_equal(dev.haloes.cpu().numpy(), host.haloes)
     assert host.n_haloes >= 2
+    again = find_haloes(*cols, 0.0015, minp=50, options=opt)
+    assert np.array_equal(again.bound, host.bound)
+    assert np.array_equal(again.haloes, host.haloes)
     n = s.n
     labels = np.empty(n, dtype=np.int32)
     bound = np.empty(n, dtype=np.uint8)
