@@ -946,127 +946,146 @@ __global__ void __launch_bounds__(kSegThreads) ub_energy_df_kernel(
     const double *__restrict__ vy, const double *__restrict__ vz, const double *__restrict__ m, float gfac,
     const HaloState *__restrict__ hs, unsigned char *__restrict__ bound, double *__restrict__ phi_out,
     unsigned char *__restrict__ keepf, SegDF *__restrict__ seg_sums) {
-    const int seg = blockIdx.x;
-    if (seg >= *nsegs) return;
     __shared__ unsigned char gone[kSeg];
     __shared__ int rlist[kSeg];
     __shared__ float2 se[2][kSegThreads / 32];
     __shared__ int sc[2][kSegThreads / 32];
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const int q = sown[seg];
-    const int h = idesc[q].x;
-    const int nsl = idesc[q].w;   // partial-sum slices written by this pass's pair kernels
-    const int sl = seg - sstart[q];
-    const int nb = hs[h].nb;
-    const float wx = hs[h].wx, wy = hs[h].wy, wz = hs[h].wz;
-    const int64_t pb = poff[h], npad = poff[h + 1] - pb, qb = qoff[h];
-    const int rend = min(nb, (sl + 1) * kSeg);
-    int r[kSegPer];
-    bool ok[kSegPer];
-    float4 u[kSegPer];
-    float2 d[kSegPer];
+    const int nseg_all = *nsegs;
+    for (int seg = blockIdx.x; seg < nseg_all; seg += gridDim.x) {
+        const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+        const int q = sown[seg];
+        const int h = idesc[q].x;
+        const int nsl = idesc[q].w;   // partial-sum slices written by this pass's pair kernels
+        const int sl = seg - sstart[q];
+        const int nb = hs[h].nb;
+        const float wx = hs[h].wx, wy = hs[h].wy, wz = hs[h].wz;
+        const int64_t pb = poff[h], npad = poff[h + 1] - pb, qb = qoff[h];
+        const int rend = min(nb, (sl + 1) * kSeg);
+        int r[kSegPer];
+        bool ok[kSegPer];
+        float4 u[kSegPer];
+        float2 d[kSegPer];
 #pragma unroll
-    for (int j = 0; j < kSegPer; ++j) {
-        r[j] = sl * kSeg + j * kSegThreads + threadIdx.x;
-        ok[j] = r[j] < rend;
-        u[j] = ok[j] ? pv[pb + r[j]] : make_float4(0.f, 0.f, 0.f, 0.f);
-        d[j] = make_float2(0.f, 0.f);
-    }
-    for (int k = 0; k < nsl; ++k)   // slices in order
-#pragma unroll
-        for (int j = 0; j < kSegPer; ++j)
-            if (ok[j]) d[j] = df_add(d[j], part[qb + (int64_t)k * npad + r[j]]);
-    float ek_s = 0.f, ek_c = 0.f, ep_s = 0.f, ep_c = 0.f;
-    int kept = 0, removed = 0;
-#pragma unroll
-    for (int j = 0; j < kSegPer; ++j) {
-        const int slot = j * kSegThreads + threadIdx.x;   // within the segment
-        if (!ok[j]) {
-            gone[slot] = 0;
-            continue;
+        for (int j = 0; j < kSegPer; ++j) {
+            r[j] = sl * kSeg + j * kSegThreads + threadIdx.x;
+            ok[j] = r[j] < rend;
+            u[j] = ok[j] ? pv[pb + r[j]] : make_float4(0.f, 0.f, 0.f, 0.f);
+            d[j] = make_float2(0.f, 0.f);
         }
-        // full pass: the sum itself; incremental pass: previous potential minus the removed
-        // particles' contribution
-        const float2 p = inc ? df_sub(phi_prev[pb + r[j]], d[j]) : d[j];
-        phi_cur[pb + r[j]] = p;
-        const float pf = p.x + p.y;
-        const float dx = u[j].x - wx, dy = u[j].y - wy, dz = u[j].z - wz;
-        const float ek = 0.5f * (dx * dx + dy * dy + dz * dz);
-        const float e = ek - gfac * pf;
-        const bool keep = !(e > 0.f);
-        keepf[pb + r[j]] = keep ? 1 : 0;
-        gone[slot] = keep ? 0 : 1;
-        if (keep) {
-            ++kept;
-            two_sum_acc(ek_s, ek_c, u[j].w * ek);
-            two_sum_acc(ep_s, ep_c, u[j].w * pf);
-            if (phi_out) phi_out[pidx[pb + r[j]]] = df_to_double(p);
-        } else {
-            ++removed;
-            const int i = pidx[pb + r[j]];
-            bound[i] = 0;
-            if (phi_out) phi_out[i] = 0.0;
+        // slices in order, four at a time with all their loads issued before the additions
+        const float2 *pr[kSegPer];
+#pragma unroll
+        for (int j = 0; j < kSegPer; ++j) pr[j] = part + qb + (ok[j] ? r[j] : 0);
+        int k = 0;
+        for (; k + 4 <= nsl; k += 4) {
+            float2 t[4][kSegPer];
+#pragma unroll
+            for (int kk = 0; kk < 4; ++kk)
+#pragma unroll
+                for (int j = 0; j < kSegPer; ++j) t[kk][j] = pr[j][(int64_t)(k + kk) * npad];
+#pragma unroll
+            for (int kk = 0; kk < 4; ++kk)
+#pragma unroll
+                for (int j = 0; j < kSegPer; ++j)
+                    if (ok[j]) d[j] = df_add(d[j], t[kk][j]);
         }
-    }
-    // block sums: counts exactly, energies in double-float (warp tree, then warps in order)
-    float2 ekv = df_warp_sum(df_from_acc(ek_s, ek_c));
-    float2 epv = df_warp_sum(df_from_acc(ep_s, ep_c));
-    int kc = kept, rc = removed;
-    for (int o = 16; o > 0; o >>= 1) {
-        kc += __shfl_down_sync(0xffffffffu, kc, o);
-        rc += __shfl_down_sync(0xffffffffu, rc, o);
-    }
-    if (lane == 0) {
-        se[0][w] = ekv;
-        se[1][w] = epv;
-        sc[0][w] = kc;
-        sc[1][w] = rc;
-    }
-    __syncthreads();
-    int nrem = 0;
-    for (int k = 0; k < kSegThreads / 32; ++k) nrem += sc[1][k];
-    if (w == 0) {
-        // the removed particles in slot order (32 slots per step)
-        int base = 0;
-        if (nrem > 0)
-            for (int s0 = 0; s0 < kSeg; s0 += 32) {
-                const bool g = gone[s0 + lane];
-                const unsigned bal = __ballot_sync(0xffffffffu, g);
-                if (g) rlist[base + __popc(bal & ((1u << lane) - 1u))] = pidx[pb + sl * kSeg + s0 + lane];
-                base += __popc(bal);
+        for (; k < nsl; ++k)
+#pragma unroll
+            for (int j = 0; j < kSegPer; ++j)
+                if (ok[j]) d[j] = df_add(d[j], pr[j][(int64_t)k * npad]);
+        float ek_s = 0.f, ek_c = 0.f, ep_s = 0.f, ep_c = 0.f;
+        int kept = 0, removed = 0;
+#pragma unroll
+        for (int j = 0; j < kSegPer; ++j) {
+            const int slot = j * kSegThreads + threadIdx.x;   // within the segment
+            if (!ok[j]) {
+                gone[slot] = 0;
+                continue;
             }
-        __syncwarp();
-        double a[7] = {0, 0, 0, 0, 0, 0, 0};
-        for (int k = lane; k < nrem; k += 32) {
-            const int i = rlist[k];
-            const double mi = m[i];
-            a[0] += mi;
-            a[1] += mi * x[i];
-            a[2] += mi * y[i];
-            a[3] += mi * z[i];
-            a[4] += mi * vx[i];
-            a[5] += mi * vy[i];
-            a[6] += mi * vz[i];
+            // full pass: the sum itself; incremental pass: previous potential minus the removed
+            // particles' contribution
+            const float2 p = inc ? df_sub(phi_prev[pb + r[j]], d[j]) : d[j];
+            phi_cur[pb + r[j]] = p;
+            const float pf = p.x + p.y;
+            const float dx = u[j].x - wx, dy = u[j].y - wy, dz = u[j].z - wz;
+            const float ek = 0.5f * (dx * dx + dy * dy + dz * dz);
+            const float e = ek - gfac * pf;
+            const bool keep = !(e > 0.f);
+            keepf[pb + r[j]] = keep ? 1 : 0;
+            gone[slot] = keep ? 0 : 1;
+            if (keep) {
+                ++kept;
+                two_sum_acc(ek_s, ek_c, u[j].w * ek);
+                two_sum_acc(ep_s, ep_c, u[j].w * pf);
+                if (phi_out) phi_out[pidx[pb + r[j]]] = df_to_double(p);
+            } else {
+                ++removed;
+                const int i = pidx[pb + r[j]];
+                bound[i] = 0;
+                if (phi_out) phi_out[i] = 0.0;
+            }
         }
-        if (nrem > 0)
-#pragma unroll
-            for (int k = 0; k < 7; ++k) a[k] = warp_sum(a[k]);
+        // block sums: counts exactly, energies in double-float (warp tree, then warps in order)
+        float2 ekv = df_warp_sum(df_from_acc(ek_s, ek_c));
+        float2 epv = df_warp_sum(df_from_acc(ep_s, ep_c));
+        int kc = kept, rc = removed;
+        for (int o = 16; o > 0; o >>= 1) {
+            kc += __shfl_down_sync(0xffffffffu, kc, o);
+            rc += __shfl_down_sync(0xffffffffu, rc, o);
+        }
         if (lane == 0) {
-            SegDF o;
-            o.removed = nrem;
-            o.kept = 0;
-            float2 e0 = make_float2(0.f, 0.f), e1 = make_float2(0.f, 0.f);
-            for (int k = 0; k < kSegThreads / 32; ++k) {
-                o.kept += sc[0][k];
-                e0 = df_add(e0, se[0][k]);
-                e1 = df_add(e1, se[1][k]);
-            }
-            o.ekin = e0;
-            o.epot = e1;
-            o.rm = a[0]; o.rmx = a[1]; o.rmy = a[2]; o.rmz = a[3];
-            o.rmvx = a[4]; o.rmvy = a[5]; o.rmvz = a[6];
-            seg_sums[seg] = o;
+            se[0][w] = ekv;
+            se[1][w] = epv;
+            sc[0][w] = kc;
+            sc[1][w] = rc;
         }
+        __syncthreads();
+        int nrem = 0;
+        for (int k = 0; k < kSegThreads / 32; ++k) nrem += sc[1][k];
+        if (w == 0) {
+            // the removed particles in slot order (32 slots per step)
+            int base = 0;
+            if (nrem > 0)
+                for (int s0 = 0; s0 < kSeg; s0 += 32) {
+                    const bool g = gone[s0 + lane];
+                    const unsigned bal = __ballot_sync(0xffffffffu, g);
+                    if (g) rlist[base + __popc(bal & ((1u << lane) - 1u))] = pidx[pb + sl * kSeg + s0 + lane];
+                    base += __popc(bal);
+                }
+            __syncwarp();
+            double a[7] = {0, 0, 0, 0, 0, 0, 0};
+            for (int k = lane; k < nrem; k += 32) {
+                const int i = rlist[k];
+                const double mi = m[i];
+                a[0] += mi;
+                a[1] += mi * x[i];
+                a[2] += mi * y[i];
+                a[3] += mi * z[i];
+                a[4] += mi * vx[i];
+                a[5] += mi * vy[i];
+                a[6] += mi * vz[i];
+            }
+            if (nrem > 0)
+#pragma unroll
+                for (int k = 0; k < 7; ++k) a[k] = warp_sum(a[k]);
+            if (lane == 0) {
+                SegDF o;
+                o.removed = nrem;
+                o.kept = 0;
+                float2 e0 = make_float2(0.f, 0.f), e1 = make_float2(0.f, 0.f);
+                for (int k = 0; k < kSegThreads / 32; ++k) {
+                    o.kept += sc[0][k];
+                    e0 = df_add(e0, se[0][k]);
+                    e1 = df_add(e1, se[1][k]);
+                }
+                o.ekin = e0;
+                o.epot = e1;
+                o.rm = a[0]; o.rmx = a[1]; o.rmy = a[2]; o.rmz = a[3];
+                o.rmvx = a[4]; o.rmvy = a[5]; o.rmvz = a[6];
+                seg_sums[seg] = o;
+            }
+        }
+        __syncthreads();   // the shared arrays are reused by the next segment
     }
 }
 
@@ -1154,64 +1173,66 @@ __global__ void __launch_bounds__(kSegThreads) ub_compact_df_kernel(
     const float4 *__restrict__ pv_in, const int *__restrict__ pidx_in, const float2 *__restrict__ phi_cur,
     float4 *__restrict__ pk_out, float4 *__restrict__ pv_out, int *__restrict__ pidx_out,
     float2 *__restrict__ phi_next, float4 *__restrict__ removed) {
-    const int seg = blockIdx.x;
-    if (seg >= *nsegs) return;
     __shared__ int wcount[kSegThreads / 32], wrem[kSegThreads / 32];
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const int q = sown[seg];
-    const int h = idesc[q].x;
-    if (!hs[h].active) return;   // converged this pass: its packed slots are not read again
-    const int s0 = sstart[q], sl = seg - s0, nseg = sstart[q + 1] - s0;
-    const int nb = hs[h].nprev;
-    const int64_t pb = poff[h];
-    const int2 pre = seg_pre[seg];
-    int running = pre.x, rrunning = pre.y;
-    const int rend = min(nb, (sl + 1) * kSeg);
-    for (int r0 = sl * kSeg; r0 < rend; r0 += kSegThreads) {
-        const int r = r0 + threadIdx.x;
-        const bool valid = r < rend;
-        const bool keep = valid && keepf[pb + r];
-        const bool gone = valid && !keep;
-        const unsigned bal = __ballot_sync(0xffffffffu, keep);
-        const unsigned bgone = __ballot_sync(0xffffffffu, gone);
-        if (lane == 0) {
-            wcount[w] = __popc(bal);
-            wrem[w] = __popc(bgone);
-        }
-        __syncthreads();
-        int rank = running, rrank = rrunning, tot = 0, trem = 0;
-#pragma unroll
-        for (int k = 0; k < kSegThreads / 32; ++k) {
-            if (k < w) {
-                rank += wcount[k];
-                rrank += wrem[k];
+    const int nseg_all = *nsegs;
+    for (int seg = blockIdx.x; seg < nseg_all; seg += gridDim.x) {
+        const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+        const int q = sown[seg];
+        const int h = idesc[q].x;
+        if (!hs[h].active) continue;   // converged this pass: its packed slots are not read again
+        const int s0 = sstart[q], sl = seg - s0, nseg = sstart[q + 1] - s0;
+        const int nb = hs[h].nprev;
+        const int64_t pb = poff[h];
+        const int2 pre = seg_pre[seg];
+        int running = pre.x, rrunning = pre.y;
+        const int rend = min(nb, (sl + 1) * kSeg);
+        for (int r0 = sl * kSeg; r0 < rend; r0 += kSegThreads) {
+            const int r = r0 + threadIdx.x;
+            const bool valid = r < rend;
+            const bool keep = valid && keepf[pb + r];
+            const bool gone = valid && !keep;
+            const unsigned bal = __ballot_sync(0xffffffffu, keep);
+            const unsigned bgone = __ballot_sync(0xffffffffu, gone);
+            if (lane == 0) {
+                wcount[w] = __popc(bal);
+                wrem[w] = __popc(bgone);
             }
-            tot += wcount[k];
-            trem += wrem[k];
+            __syncthreads();
+            int rank = running, rrank = rrunning, tot = 0, trem = 0;
+#pragma unroll
+            for (int k = 0; k < kSegThreads / 32; ++k) {
+                if (k < w) {
+                    rank += wcount[k];
+                    rrank += wrem[k];
+                }
+                tot += wcount[k];
+                trem += wrem[k];
+            }
+            rank += __popc(bal & ((1u << lane) - 1u));
+            rrank += __popc(bgone & ((1u << lane) - 1u));
+            if (keep) {
+                pk_out[pb + rank] = pk_in[pb + r];
+                pv_out[pb + rank] = pv_in[pb + r];
+                pidx_out[pb + rank] = pidx_in[pb + r];
+                phi_next[pb + rank] = phi_cur[pb + r];
+            } else if (gone) {
+                removed[pb + rrank] = pk_in[pb + r];
+            }
+            running += tot;
+            rrunning += trem;
+            __syncthreads();
         }
-        rank += __popc(bal & ((1u << lane) - 1u));
-        rrank += __popc(bgone & ((1u << lane) - 1u));
-        if (keep) {
-            pk_out[pb + rank] = pk_in[pb + r];
-            pv_out[pb + rank] = pv_in[pb + r];
-            pidx_out[pb + rank] = pidx_in[pb + r];
-            phi_next[pb + rank] = phi_cur[pb + r];
-        } else if (gone) {
-            removed[pb + rrank] = pk_in[pb + r];
+        if (sl == nseg - 1) {   // the halo's last segment pads after the survivors and the removed
+            const float4 f = make_float4(kFar, kFar, kFar, 0.f);
+            const int nkeep = running, nrem = rrunning;
+            for (int r = nkeep + threadIdx.x; r < ((nkeep + 31) & ~31); r += kSegThreads) {
+                pk_out[pb + r] = f;
+                pv_out[pb + r] = make_float4(0.f, 0.f, 0.f, 0.f);
+                pidx_out[pb + r] = -1;
+            }
+            for (int r = nrem + threadIdx.x; r < ((nrem + 31) & ~31); r += kSegThreads) removed[pb + r] = f;
         }
-        running += tot;
-        rrunning += trem;
-        __syncthreads();
-    }
-    if (sl == nseg - 1) {   // the halo's last segment pads after the survivors and the removed
-        const float4 f = make_float4(kFar, kFar, kFar, 0.f);
-        const int nkeep = running, nrem = rrunning;
-        for (int r = nkeep + threadIdx.x; r < ((nkeep + 31) & ~31); r += kSegThreads) {
-            pk_out[pb + r] = f;
-            pv_out[pb + r] = make_float4(0.f, 0.f, 0.f, 0.f);
-            pidx_out[pb + r] = -1;
-        }
-        for (int r = nrem + threadIdx.x; r < ((nrem + 31) & ~31); r += kSegThreads) removed[pb + r] = f;
+        __syncthreads();   // the shared arrays are reused by the next segment
     }
 }
 
@@ -1508,6 +1529,12 @@ int unbind_device(int64_t n, int nh, const int64_t *d_off, const int64_t *h_off,
         HALMA_CUDA(cudaFuncSetAttribute(ub_pair_sym_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSymSmem));
         HALMA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, ub_pair_sym_kernel, 128, kSymSmem));
         const int ygrid = device_sm_count() * std::max(bps, 1);
+        // the end-of-pass kernels loop over the pass's energy segments with one wave of blocks
+        // (a launch of one block per possible segment cost ~30 us even when few were active)
+        HALMA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, ub_energy_df_kernel, kSegThreads, 0));
+        const int egrid = std::min(sgrid, device_sm_count() * std::max(bps, 1));
+        HALMA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, ub_compact_df_kernel, kSegThreads, 0));
+        const int cgrid = std::min(sgrid, device_sm_count() * std::max(bps, 1));
         auto record = [&](cudaStream_t rs, int it0, int it1) -> int {
             // first pass: centre of mass and packing into buffer 0; every pass then compacts
             // its survivors into the other buffer and sets the next pass's halo state
@@ -1544,11 +1571,11 @@ int unbind_device(int64_t n, int nh, const int64_t *d_off, const int64_t *h_off,
                         HALMA_LAUNCH(ub_pack_kernel<float4>, nchunks, kSegThreads, 0, rs, off, dpoff, dcst, dchh, x, y,
                                      z, m, vx, vy, vz, hs, (float4 *)nullptr, pvb[0], (int *)nullptr);
                 }
-                HALMA_LAUNCH(ub_energy_df_kernel, sgrid, kSegThreads, 0, rs, sstart, sown, idesc, cnt + 2, dpoff, dqoff,
+                HALMA_LAUNCH(ub_energy_df_kernel, egrid, kSegThreads, 0, rs, sstart, sown, idesc, cnt + 2, dpoff, dqoff,
                              inc, pidxb[a], pvb[a], part2, phin2, phic2, x, y, z, vx, vy, vz, m, gfac_f, hs, bound,
                              phi_out, keepf, sdf);
                 HALMA_LAUNCH(ub_finalize_df_kernel, fgrid, 256, 0, rs, nh, dorder, sstart, sdf, gfac, hs, segpre);
-                HALMA_LAUNCH(ub_compact_df_kernel, sgrid, kSegThreads, 0, rs, sstart, sown, idesc, cnt + 2, dpoff, hs,
+                HALMA_LAUNCH(ub_compact_df_kernel, cgrid, kSegThreads, 0, rs, sstart, sown, idesc, cnt + 2, dpoff, hs,
                              keepf, segpre, pkb[a], pvb[a], pidxb[a], phic2, pkb[b], pvb[b], pidxb[b], phin2, rk);
             }
             HALMA_CUDA(cudaMemsetAsync(cnt + 6, 0, sizeof(int), rs));
