@@ -388,15 +388,23 @@ __global__ void keys_kernel(const double *__restrict__ x, const double *__restri
 }
 
 // Sorted records, run heads, union-find / label initialisation.
+// Sorted records, cell heads and label slots.  With runstart (sub-cells in the key), the
+// sub-cell runs' starts for the run-head scan (see subrun below) instead of the union-find
+// initialisation, which preunion_kernel then writes.
 __global__ void prep_kernel(int n, int sb, const uint64_t *__restrict__ keys, const int *__restrict__ idx,
                             const float4 *__restrict__ pre, float4 *__restrict__ rec, int *__restrict__ head,
-                            int *__restrict__ parent, unsigned char *__restrict__ has, int *__restrict__ minidx) {
+                            int *__restrict__ parent, unsigned char *__restrict__ has, int *__restrict__ minidx,
+                            int *__restrict__ runstart) {
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
-        const uint64_t key = keys[k] >> sb;
+        const uint64_t full = keys[k], prev = k > 0 ? keys[k - 1] : ~full;
         rec[k] = pre[idx[k]];
-        head[k] = (k == 0 || (keys[k - 1] >> sb) != key) ? 1 : 0;
-        parent[k] = k;
-        has[k] = 0;
+        head[k] = (k == 0 || (prev >> sb) != (full >> sb)) ? 1 : 0;
+        if (runstart) {
+            runstart[k] = (k == 0 || prev != full) ? k : 0;
+        } else {
+            parent[k] = k;
+            has[k] = 0;
+        }
         minidx[k] = INT_MAX;
     }
 }
@@ -404,12 +412,8 @@ __global__ void prep_kernel(int n, int sb, const uint64_t *__restrict__ keys, co
 // Particles with the same full key (cell and 4 x 4 x 4 sub-cell) lie at most sqrt(3)/4 of a
 // cell (0.44 LL) apart, so they are friends whatever the rounding: each such run is joined
 // up front, every member under the run's first sorted position (which keeps "a root is the
-// smallest position of its tree").  runstart[k] = k at a run's first position, else 0; an
-// inclusive max-scan turns it into the run head of every position.
-__global__ void subrun_kernel(int n, const uint64_t *__restrict__ keys, int *__restrict__ runstart) {
-    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x)
-        runstart[k] = (k == 0 || keys[k] != keys[k - 1]) ? k : 0;
-}
+// smallest position of its tree").  runstart[k] = k at a run's first position, else 0
+// (prep_kernel); an inclusive max-scan turns it into the run head of every position.
 
 __global__ void preunion_kernel(int n, const uint64_t *__restrict__ keys, const int *__restrict__ runhead,
                                 int *__restrict__ parent, unsigned char *__restrict__ has) {
@@ -425,12 +429,13 @@ __global__ void preunion_kernel(int n, const uint64_t *__restrict__ keys, const 
 // cell/4) are joined without pair tests when every pair of their points is closer than the
 // linking length: for a sub-cell offset d, the largest distance is sqrt(sum_i (|d_i|+1)^2)/4
 // cells, and offsets with sum_i (|d_i|+1)^2 <= 15 stay below 0.97 LL (the rounding of the
-// sub-cell assignment moves a point by ~1e-9 cells at most).  One warp per dense cell labels
-// its occupied sub-cells with the smallest run head of their component (min-label
-// propagation over those offsets), hooks every run head under its label (a smaller sorted
-// position, so a root stays the smallest position of its tree), marks the particles of
-// multi-particle components as having friends, and records whether the whole cell is one
-// component (conn[c]).  Smaller cells are connected when all their particles share one run.
+// sub-cell assignment moves a point by ~1e-8 cells at most).  One warp per dense cell finds
+// the components of its occupied sub-cells under those offsets (bitmask flood fill, see
+// subcell_dilate), hooks every run head under the smallest run head of its component (a
+// smaller sorted position, so a root stays the smallest position of its tree), marks the
+// particles of multi-particle components as having friends, and records whether the whole
+// cell is one component (conn[c]).  Smaller cells are connected when all their particles
+// share one run.
 constexpr int kDenseMin = 32;
 
 __device__ __forceinline__ int lower_bound_key(const uint64_t *__restrict__ keys, int lo, int hi, uint64_t k) {
@@ -456,88 +461,78 @@ __global__ void small_cell_kernel(const int *__restrict__ ncell_p, const int *__
     }
 }
 
+// Sub-cell sets as 64-bit masks, bit 16 x + 4 y + z for sub-cell (x, y, z).  subcell_dilate
+// adds every sub-cell within the guaranteed-link offsets of the set: the 3 x 3 x 3 cube, and
+// +-2 along one axis with at most one of the other two offsets +-1 ((3,2,2) gives 17 > 15).
+__device__ __forceinline__ unsigned long long subcell_dilate(unsigned long long m) {
+    constexpr unsigned long long Z0 = 0x1111111111111111ull, Z1 = Z0 << 1, Z2 = Z0 << 2, Z3 = Z0 << 3;
+    constexpr unsigned long long Y0 = 0x000F000F000F000Full, Y1 = Y0 << 4, Y2 = Y0 << 8, Y3 = Y0 << 12;
+    const unsigned long long zl = ((m << 1) & ~Z0) | ((m >> 1) & ~Z3);   // z +- 1
+    const unsigned long long yl = ((m << 4) & ~Y0) | ((m >> 4) & ~Y3);   // y +- 1
+    const unsigned long long xl = (m << 16) | (m >> 16);                 // x +- 1
+    const unsigned long long a = m | zl;
+    const unsigned long long b = a | ((a << 4) & ~Y0) | ((a >> 4) & ~Y3);
+    const unsigned long long cube = b | (b << 16) | (b >> 16);
+    const unsigned long long cyz = a | yl, cxz = a | xl, cxy = m | xl | yl;   // plus shapes
+    return cube | (cyz << 32) | (cyz >> 32) | ((cxz << 8) & ~(Y0 | Y1)) | ((cxz >> 8) & ~(Y2 | Y3)) |
+           ((cxy << 2) & ~(Z0 | Z1)) | ((cxy >> 2) & ~(Z2 | Z3));
+}
+
+// Bit of Morton sub-cell code m (x1 y1 z1 x0 y0 z0) in the mask layout.
+__device__ __forceinline__ int subcell_bit(int m) {
+    const int x = (((m >> 5) & 1) << 1) | ((m >> 2) & 1), y = (((m >> 4) & 1) << 1) | ((m >> 1) & 1),
+              z = (((m >> 3) & 1) << 1) | (m & 1);
+    return (x << 4) | (y << 2) | z;
+}
+
 __global__ void __launch_bounds__(256) dense_cell_kernel(const int *__restrict__ ndense_p, const int *__restrict__ dense,
                                                          const int *__restrict__ cell_start,
                                                          const uint64_t *__restrict__ keys, int *__restrict__ parent,
                                                          unsigned char *__restrict__ has, unsigned char *__restrict__ conn) {
-    __shared__ unsigned long long nbmask[64];   // guaranteed-link neighbours of each sub-cell (Morton codes)
-    __shared__ int lab[8][64];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    if (threadIdx.x < 64) {
-        const int m = threadIdx.x;
-        const int sx = (((m >> 5) & 1) << 1) | ((m >> 2) & 1), sy = (((m >> 4) & 1) << 1) | ((m >> 1) & 1),
-                  sz = (((m >> 3) & 1) << 1) | (m & 1);
-        unsigned long long mask = 0;
-        for (int dx = -2; dx <= 2; ++dx)
-            for (int dy = -2; dy <= 2; ++dy)
-                for (int dz = -2; dz <= 2; ++dz) {
-                    const int ax = abs(dx) + 1, ay = abs(dy) + 1, az = abs(dz) + 1;
-                    if ((dx | dy | dz) == 0 || ax * ax + ay * ay + az * az > 15) continue;
-                    const int tx = sx + dx, ty = sy + dy, tz = sz + dz;
-                    if (tx < 0 || tx > 3 || ty < 0 || ty > 3 || tz < 0 || tz > 3) continue;
-                    const int t = ((tx >> 1) << 5) | ((ty >> 1) << 4) | ((tz >> 1) << 3) | ((tx & 1) << 2) |
-                                  ((ty & 1) << 1) | (tz & 1);
-                    mask |= 1ull << t;
-                }
-        nbmask[m] = mask;
-    }
-    __syncthreads();
     const int nd = *ndense_p;
     const int warps = gridDim.x * (blockDim.x >> 5);
+    const int bit0 = subcell_bit(lane), bit1 = subcell_bit(lane + 32);
     for (int di = blockIdx.x * (blockDim.x >> 5) + w; di < nd; di += warps) {
-        {
-            const int c = dense[di];
-            const int cs = cell_start[c], ce = cell_start[c + 1];
-            const uint64_t ck = keys[cs] & ~63ull;   // the cell's key with the sub-cell bits cleared
-            int lo[2], hi[2];
-            bool occ[2];
-            for (int r = 0; r < 2; ++r) {
-                const int m = lane + 32 * r;
-                lo[r] = lower_bound_key(keys, cs, ce, ck | (uint64_t)m);
-                hi[r] = lower_bound_key(keys, lo[r], ce, (ck | (uint64_t)m) + 1);
-                occ[r] = hi[r] > lo[r];
-                lab[w][m] = occ[r] ? lo[r] : INT_MAX;
+        const int c = dense[di];
+        const int cs = cell_start[c], ce = cell_start[c + 1];
+        const uint64_t ck = keys[cs] & ~63ull;   // the cell's key with the sub-cell bits cleared
+        int lo[2], hi[2];
+        bool occ[2];
+        for (int r = 0; r < 2; ++r) {
+            const int m = lane + 32 * r;
+            lo[r] = lower_bound_key(keys, cs, ce, ck | (uint64_t)m);
+            hi[r] = lower_bound_key(keys, lo[r], ce, (ck | (uint64_t)m) + 1);
+            occ[r] = hi[r] > lo[r];
+        }
+        const unsigned long long mine = (occ[0] ? 1ull << bit0 : 0ull) | (occ[1] ? 1ull << bit1 : 0ull);
+        const unsigned long long occm =
+            (unsigned long long)__reduce_or_sync(0xffffffffu, (unsigned)mine) |
+            ((unsigned long long)__reduce_or_sync(0xffffffffu, (unsigned)(mine >> 32)) << 32);
+        unsigned long long rem = occm;
+        bool first = true, one = false;
+        while (rem) {   // one component per round, from its lowest remaining sub-cell (warp-uniform)
+            unsigned long long comp = rem & (~rem + 1ull);
+            for (;;) {
+                const unsigned long long grown = subcell_dilate(comp) & occm;
+                if (grown == comp) break;
+                comp = grown;
             }
-            const unsigned long long occm = (unsigned long long)__ballot_sync(0xffffffffu, occ[0]) |
-                                            ((unsigned long long)__ballot_sync(0xffffffffu, occ[1]) << 32);
-            __syncwarp();
-            for (int round = 0; round < 64; ++round) {   // converges in a few rounds
-                bool changed = false;
-                for (int r = 0; r < 2; ++r) {
-                    const int m = lane + 32 * r;
-                    if (!occ[r]) continue;
-                    int v = lab[w][m];
-                    unsigned long long nb = nbmask[m] & occm;
-                    while (nb) {
-                        const int t = __ffsll((long long)nb) - 1;
-                        nb &= nb - 1;
-                        v = min(v, lab[w][t]);
-                    }
-                    if (v < lab[w][m]) {
-                        lab[w][m] = v;
-                        changed = true;
-                    }
-                }
-                __syncwarp();
-                if (!__any_sync(0xffffffffu, changed)) break;
-            }
-            int mn = INT_MAX;
-            for (int r = 0; r < 2; ++r)
-                if (occ[r]) mn = min(mn, lab[w][lane + 32 * r]);
-            for (int o = 16; o > 0; o >>= 1) mn = min(mn, __shfl_xor_sync(0xffffffffu, mn, o));
-            const bool one = __all_sync(0xffffffffu, (!occ[0] || lab[w][lane] == mn) && (!occ[1] || lab[w][lane + 32] == mn));
+            if (first) one = comp == occm;
+            first = false;
+            rem &= ~comp;
+            const bool in0 = occ[0] && ((comp >> bit0) & 1ull), in1 = occ[1] && ((comp >> bit1) & 1ull);
+            // the component's smallest run head (sorted positions grow with the Morton code)
+            const int L = __reduce_min_sync(0xffffffffu, in0 ? lo[0] : (in1 ? lo[1] : INT_MAX));
+            const bool multi = (comp & (comp - 1ull)) != 0;
             for (int r = 0; r < 2; ++r) {
-                if (!occ[r]) continue;
-                const int m = lane + 32 * r, L = lab[w][m];
+                if (!(r == 0 ? in0 : in1)) continue;
                 if (L != lo[r]) parent[lo[r]] = L;   // run head under the component's smallest run head
-                // the component holds another sub-cell exactly when an occupied sub-cell is
-                // among this one's guaranteed-link neighbours
-                if ((nbmask[m] & occm) != 0 || hi[r] - lo[r] > 1)
+                if (multi || hi[r] - lo[r] > 1)
                     for (int q = lo[r]; q < hi[r]; ++q) has[q] = 1;
             }
-            if (lane == 0) conn[c] = one ? 1 : 0;
-            __syncwarp();
         }
+        if (lane == 0) conn[c] = one ? 1 : 0;
     }
 }
 
@@ -1209,9 +1204,10 @@ int fof_core(int n, const double *x, const double *y, const double *z, FofGeom g
     HALMA_TRY(mark(1));
     HALMA_TRY(sort_pairs_u64_i32(tmp, sort_b, kin, kout, vin, vout, n, end_bit, st));
     HALMA_TRY(mark(2));
-    HALMA_LAUNCH(prep_kernel, g1, 256, 0, st, n, g.sb, kout, vout, pre, rec, head, parent, has, minidx);
-    if (g.sb != 0 && g.lo > 0.f) {   // sub-cells in the key and a positive linking length
-        HALMA_LAUNCH(subrun_kernel, g1, 256, 0, st, n, kout, flag);
+    const bool runs = g.sb != 0 && g.lo > 0.f;   // sub-cells in the key and a positive linking length
+    HALMA_LAUNCH(prep_kernel, g1, 256, 0, st, n, g.sb, kout, vout, pre, rec, head, parent, has, minidx,
+                 runs ? flag : nullptr);
+    if (runs) {
         HALMA_TRY(inclusive_max_i32(tmp, scan_b, flag, root, n, st));
         HALMA_LAUNCH(preunion_kernel, g1, 256, 0, st, n, kout, root, parent, has);
     }
