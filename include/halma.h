@@ -39,7 +39,7 @@
  *   halma_ball_gather             <- halo_gas.py:223-277 st_gas_dm_particles_inside range
  *                                    queries (KDTree.query_ball_point, parallel_inside)
  *   halma_phase_space_clean       <- halo_properties.py:113-278 calc_cell / clean_cell and
- *                                    the driver's loop pyHALMA.py:774-843
+ *                                    the main script's loop pyHALMA.py:774-843
  *   halma_halo_properties         <- halo_properties.py:45-96, 365-515, 607-625, 781-866 and
  *                                    particle_subroutines.f90:12-461 as called at
  *                                    pyHALMA.py:930-1016
@@ -186,13 +186,13 @@ int halma_split_bridges(int64_t n, const double *x, const double *y, const doubl
 /* Phase-space cleaning                                                                 */
 /* ------------------------------------------------------------------------------------ */
 /* pyHALMA's phase-space cleaning for all groups at once: calc_cell / clean_cell
- * (python_scripts/halo_properties.py:113-278) inside the driver's loop over groups
+ * (python_scripts/halo_properties.py:113-278) inside pyHALMA.py's loop over groups
  * (pyHALMA.py:774-843), parameters as read from pyHALMA.dat (pyHALMA.py:71-73, 776). */
 typedef struct {
     double  linking_length;  /* LL: grid cells are 2 LL wide                            */
     double  q_fil;           /* Q_FIL: a particle in a cell of <= q_fil particles drops  */
     double  sig_fil;         /* SIG_FIL: drop at |v - v_cell| >= fac_sig*SIG_FIL*sigma    */
-    int32_t enabled;         /* PSC_FLAG: 0 keeps every particle (the driver's reset)    */
+    int32_t enabled;         /* PSC_FLAG: 0 keeps every particle (pyHALMA.py's reset)     */
     int32_t min_part;        /* min_part_PSC (50): smaller groups keep every particle     */
     int32_t minp;            /* MINP: groups with fewer kept particles are not kept       */
     int32_t max_passes;      /* bound on the sweeps per group (a safety limit)            */
@@ -203,14 +203,14 @@ enum {
     HALMA_PSC_MASS,      /* their mass                                                   */
     HALMA_PSC_RMAX,      /* furthest kept particle from that centre                      */
     HALMA_PSC_NPART,     /* kept particles                                               */
-    HALMA_PSC_NCELL,     /* grid points per axis of the first grid (the driver's n_cell) */
+    HALMA_PSC_NCELL,     /* grid points per axis of the first grid (pyHALMA.py's n_cell)  */
     HALMA_PSC_KEPT,      /* 1 when NPART >= MINP                                         */
     HALMA_PSC_PASSES,    /* sweeps made                                                  */
     HALMA_PSC_NFIELDS
 };
 
 /* Groups as CSR over particle indices (group_offsets[n_groups+1], group_members).  Outputs:
- * control[k] (1 = member k kept, the driver's part_list[control]); which_cell (optional,
+ * control[k] (1 = member k kept, pyHALMA.py's part_list[control]); which_cell (optional,
  * 3 x members: the x, y then z cell of every particle of clean_cell's final grid, group g's
  * first n_which[g] entries from group_offsets[g] on, n_which optional); halo_out
  * (n_groups x HALMA_PSC_NFIELDS).  Like the reference, a sweep after the first marks
@@ -460,7 +460,7 @@ int halma_unbind_batched(int64_t n, int64_t n_haloes, const int64_t *offsets,
 /* ------------------------------------------------------------------------------------ */
 /* One snapshot end to end                                                              */
 /* ------------------------------------------------------------------------------------ */
-/* The driver's star-particle path (pyHALMA.py:543-592 FoF + good_groups, then the per-halo
+/* pyHALMA.py's star-particle path (pyHALMA.py:543-592 FoF + good_groups, then the per-halo
  * unbinding above) in one call: halma_fof -> groups with >= min_members members in the
  * reference order -> halma_unbind_batched over those groups.  Outputs (each optional except
  * n_haloes): labels[n] (FoF labels), bound[n] (1 = member of a kept group that survived the

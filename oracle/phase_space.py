@@ -15,7 +15,7 @@ Restates, group by group:
   grid around the remaining particles while dropped / remaining > 0.1.  Later passes write
   ``control[ip]`` with ``ip`` the position in the *current* list, so (as in the reference)
   they mark entries of the original list by that position;
-* the driver's loop over groups (pyHALMA.py:774-877): initial centre, furthest particle and
+* the main script's loop over groups (pyHALMA.py:774-877): initial centre, furthest particle and
   grid (np.arange(-(r+LL), r+LL, 2LL)), cleaning, ``control`` reset to all ones when
   cleaning is off or the group has fewer than 50 particles, centre / mass / furthest particle
   of the kept particles, groups with at least MINP particles kept, then every array sorted by
@@ -125,7 +125,7 @@ def clean_cell(cx, cy, cz, pl, x, y, z, vx, vy, vz, m, ll, q_fil, sig_fil):
 
 def phase_space_cleaning(groups, st_x, st_y, st_z, st_vx, st_vy, st_vz, st_mass, LL, Q_FIL, SIG_FIL, PSC_FLAG,
                          MINP, min_part_PSC=50):
-    """The driver block: returns dict of the arrays it leaves (sorted by decreasing size)."""
+    """The main script's block: returns dict of the arrays it leaves (sorted by decreasing size)."""
     x, y, z, vx, vy, vz, m = (np.asarray(a, dtype=np.float64) for a in (st_x, st_y, st_z, st_vx, st_vy, st_vz,
                                                                          st_mass))
     keep = {k: [] for k in ("center_x", "center_y", "center_z", "masses", "rmax", "num_particles", "num_cells",

@@ -1,4 +1,4 @@
-"""ORACLE (test infrastructure only): the O(N) per-halo properties of pyHALMA's driver loop
+"""ORACLE (test infrastructure only): the O(N) per-halo properties of pyHALMA's main-script loop
 (pyHALMA.py:930-1016) restated on the CPU.
 
 NumPy FP64 restatements of the numba functions of python_scripts/halo_properties.py (fastmath,

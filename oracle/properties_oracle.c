@@ -2,7 +2,7 @@
  *
  * C restatement of two routines of pyHALMA's fortran_modules/particle_subroutines.f90
  * (gfortran is absent here, so the Fortran cannot be compiled), statement by statement, in
- * the Fortran's precision, run as the driver runs them with one OpenMP thread:
+ * the Fortran's precision, run as the main script runs them with one OpenMP thread:
  *
  *   halo_shape            f90:160-214  FP32 inertia tensor sum_p m r_i r_j / sum m (particle
  *                                      order), DIAGONALISE (f90:12-126, Jacobi rotations in

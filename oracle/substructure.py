@@ -1,6 +1,6 @@
 """ORACLE (test infrastructure only): pyHALMA's substructure block restated on the CPU.
 
-Restates pyHALMA.py:703-766 group by group, exactly as the driver runs it: for sub_LL =
+Restates pyHALMA.py:703-766 group by group, exactly as the main script runs it: for sub_LL =
 LL/DEC_FACTOR, LL/DEC_FACTOR^2, ... while sub_LL > MIN_LL, centre of mass
 (halo_properties.py:26-43) and half-mass radius (halo_properties.py:365-392) of the current
 particle list, FoF of the list at sub_LL (fof.py:87-89, here the C oracle's exact partition),

@@ -241,7 +241,7 @@ def as_host(a, dtype):
 def pinned_empty(shape, dtype):
     """An uninitialised NumPy array in page-locked host memory from torch's caching pinned
     allocator (plain np.empty without torch or a CUDA device).  Device-to-host copies into it
-    are DMA transfers with no CPU memcpy; a pageable destination makes the driver copy through
+    are DMA transfers with no CPU memcpy; a pageable destination makes the CUDA driver copy through
     staging buffers on the host and fault fresh pages in, whose cost depends on the host's
     other load.  The block goes back to torch's cache when the array is released, so repeated
     calls of the same size allocate nothing."""

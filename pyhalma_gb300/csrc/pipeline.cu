@@ -78,7 +78,7 @@ struct OutCopy {
 // `groups` has fired, waiting for the copies to end.  Runs on a helper thread while the
 // calling thread drives the unbinding: a copy to pageable host memory returns only when it is
 // complete.  (Staging them through pinned memory and a CPU memcpy measured far slower: the
-// driver's own pageable path writes fresh pages much faster than a memcpy that faults them in.)
+// CUDA driver's own pageable path writes fresh pages much faster than a memcpy that faults them in.)
 int copy_groups_out(int dev, SideStream *side, const OutCopy *outs, int nout) {
     HALMA_CUDA(cudaSetDevice(dev));
     HALMA_CUDA(cudaStreamWaitEvent(side->s, side->groups, 0));

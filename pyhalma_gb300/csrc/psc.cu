@@ -1,5 +1,5 @@
 // Phase-space cleaning of all FoF groups at once: pyHALMA's calc_cell / clean_cell
-// (python_scripts/halo_properties.py:113-278) inside the driver's loop over groups
+// (python_scripts/halo_properties.py:113-278) inside pyHALMA.py's loop over groups
 // (pyHALMA.py:774-843).
 //
 // Reference, per group (part_list P of N0 particles):
@@ -15,7 +15,7 @@
 //            sweep repeats on a new grid around P[control != 0] (a pass that leaves remaining
 //            == 0 ends the group with zero outputs), fac_sig = max(1, 0.75 fac_sig);
 //   final  = grid and cells of P[control != 0] (their cells are the which_cell output);
-//   driver = control reset to ones when cleaning is off or N0 < min_part; centre, mass and
+//   main script = control reset to ones when cleaning is off or N0 < min_part; centre, mass and
 //            furthest particle of P[control]; the group is kept when it has >= MINP particles.
 //
 // Here every step runs for all groups in a fixed set of launches: a group's state (centre,
@@ -90,10 +90,10 @@ __global__ void psc_fill_kernel(int G, const int64_t *__restrict__ off, int *__r
 }
 
 // One block per group whose mode matches: FP64 centre of mass of the list (zeros when the
-// mass is not positive), furthest particle from it, and the grid around it.  With `driver`
-// the results go to the output row instead of the state.
+// mass is not positive), furthest particle from it, and the grid around it.  For the main
+// script's own step the results go to the output row instead of the state.
 // Centre of mass and furthest particle of every group that sweeps or takes its final step
-// (with all, of every group: the driver's final values).  A group's list is split over up to
+// (with all, of every group: the main script's final values).  A group's list is split over up to
 // S blocks of at least kPscMin entries; each block writes its partial sums, and the last block
 // of the group to finish (a counter per group, no waiting) adds them in block order.  The
 // furthest particle is the square root of the largest squared distance (the square root is
@@ -517,7 +517,7 @@ __global__ void psc_compact_kernel(int64_t n0, int G, const int *__restrict__ fl
         off[h] = goff[h] < n0 ? (int64_t)pos[goff[h]] : total;
 }
 
-// Driver step: control reset to ones when cleaning is off or the group is small.
+// Main-script step: control reset to ones when cleaning is off or the group is small.
 __global__ void psc_reset_kernel(int G, const int64_t *__restrict__ goff, int enabled, int min_part,
                                  unsigned char *__restrict__ control) {
     for (int h = blockIdx.x; h < G; h += gridDim.x) {
@@ -728,7 +728,7 @@ extern "C" int halma_phase_space_clean(int64_t n, const double *x, const double 
         sweeping = hc[0];
         finals = hc[1];
     }
-    // driver step: reset, centre / mass / furthest particle of the kept particles
+    // main-script step: reset, centre / mass / furthest particle of the kept particles
     HALMA_LAUNCH(psc_reset_kernel, gG, 256, 0, st, G, dgoff, p.enabled, p.min_part, dctl);
     HALMA_LAUNCH(psc_flag_kernel, gN, 256, 0, st, N0, dctl, flag);
     HALMA_TRY(exclusive_sum_i32(tmp, scan_b, flag, pos, (int)NL, st));

@@ -197,10 +197,10 @@ def escape_velocity_unbinding_particles(cx, cy, cz, vx, vy, vz, Rmax, part_list,
 
 
 # ---------------------------------------------------------------------------------------
-# the O(N) part of the driver's property loop (pyHALMA.py:930-1016)
+# the O(N) part of the main script's property loop (pyHALMA.py:930-1016)
 # ---------------------------------------------------------------------------------------
 PROP = {k: i for i, k in enumerate(_lib.PROP_FIELDS)}
-# driver array name -> field (pyHALMA.py:945-1013)
+# main-script array name -> field (pyHALMA.py:945-1013)
 DRIVER_NAMES = {"rad05": "r05", "rad05_x": "r05x", "rad05_y": "r05y", "rad05_z": "r05z", "velocities_x": "vx",
                 "velocities_y": "vy", "velocities_z": "vz", "specific_angular_momentum_x": "jx",
                 "specific_angular_momentum_y": "jy", "specific_angular_momentum_z": "jz",
@@ -230,9 +230,9 @@ def halo_property_table(offsets, members, st_x, st_y, st_z, st_vx, st_vy, st_vz,
 
 def property_loop(new_groups, st_x, st_y, st_z, st_vx, st_vy, st_vz, st_mass, center_x, center_y, center_z, masses,
                   rmax, LL):
-    """The O(N) properties the driver's loop computes per halo (pyHALMA.py:930-1016), for all
+    """The O(N) properties the main script's loop computes per halo (pyHALMA.py:930-1016), for all
     haloes at once.  Inputs as the phase-space cleaning leaves them; returns a dict keyed by the
-    driver's array names (rad05, rad05_x, ..., sig_3D, sig_1D_x, vsigma, lambda_ensellem)."""
+    main script's array names (rad05, rad05_x, ..., sig_3D, sig_1D_x, vsigma, lambda_ensellem)."""
     lens = np.fromiter((len(g) for g in new_groups), dtype=np.int64, count=len(new_groups))
     offsets = np.zeros(len(new_groups) + 1, dtype=np.int64)
     np.cumsum(lens, out=offsets[1:])

@@ -1,6 +1,6 @@
 """Phase-space cleaning of FoF groups, backed by the GB300 kernels.
 
-pyHALMA cleans every FoF group in phase space before computing its properties: the driver
+pyHALMA cleans every FoF group in phase space before computing its properties: its main script
 (pyHALMA.py:774-877) calls ``halo_properties.calc_cell`` and ``clean_cell``
 (python_scripts/halo_properties.py:113-278) group by group.  Particles are binned on a grid of
 2*LL cells around the group's centre of mass; a particle is dropped when its cell holds no
@@ -11,7 +11,7 @@ new grid while they drop more than 10 % of the remaining particles.  Small group
 fewer than MINP particles are discarded; the survivors are sorted by decreasing size.
 
 ``phase_space_cleaning`` runs that whole block for all groups at once (C ABI
-``halma_phase_space_clean``) and returns the arrays the driver builds, in its order.  Like the
+``halma_phase_space_clean``) and returns the arrays the main script builds, in its order.  Like the
 reference, sweeps after the first mark particles by their position in the list being swept.
 """
 from __future__ import annotations
@@ -77,7 +77,7 @@ def clean_groups(offsets, members, st_x, st_y, st_z, st_vx, st_vy, st_vz, st_mas
 
 def phase_space_cleaning(groups, st_x, st_y, st_z, st_vx, st_vy, st_vz, st_mass, LL, Q_FIL, SIG_FIL, PSC_FLAG, MINP,
                          min_part_PSC=50):
-    """pyHALMA.py:774-877 for all groups at once.  Returns a dict with the driver's arrays
+    """pyHALMA.py:774-877 for all groups at once.  Returns a dict with the main script's arrays
     after its sort by decreasing size: center_x, center_y, center_z, masses, rmax,
     num_particles, num_cells, new_groups (index arrays), which_x / which_y / which_z (the
     cells of clean_cell's final grid, one int32 array per group)."""
@@ -109,6 +109,6 @@ def phase_space_cleaning(groups, st_x, st_y, st_z, st_vx, st_vy, st_vz, st_mass,
         k = int(n_which[g])
         for a, name in enumerate(("which_x", "which_y", "which_z")):
             out[name].append(which[a, b:b + k].copy())
-    # the driver's sort: np.flip(np.argsort(num_particles)) (pyHALMA.py:863)
+    # the main script's sort: np.flip(np.argsort(num_particles)) (pyHALMA.py:863)
     order = np.flip(np.argsort(np.array(out["num_particles"], dtype=np.int32)))
     return {k: [v[i] for i in order] for k, v in out.items()}

@@ -1,6 +1,6 @@
 """Batched substructure identification (bridge splitting), backed by the GB300 kernels.
 
-pyHALMA splits FoF groups joined by thin bridges in an inline block of its driver
+pyHALMA splits FoF groups joined by thin bridges in an inline block of its main script
 (pyHALMA.py:703-766, parameters MINP_SUB, DEC_FACTOR, MIN_LL, DIST_FACTOR read at
 pyHALMA.py:96-98).  For every group, at sub_LL = LL/DEC_FACTOR, LL/DEC_FACTOR^2, ... while
 sub_LL > MIN_LL, it runs a FoF on the group's particles at sub_LL

@@ -12,7 +12,7 @@ precision="fp32c" — float32 pair terms with compensated summation in one persi
                     work-queue kernel per pass, all passes replayed from one CUDA graph;
 precision="fp64"  — the plain per-halo path: FP64 pair sums, one launch per halo per pass.
 
-``find_haloes`` is the whole star-particle path of the driver (FoF, good_groups, unbinding)
+``find_haloes`` is the whole star-particle path of the main script pyHALMA.py (FoF, good_groups, unbinding)
 in one C-ABI call (``halma_find_haloes``).
 """
 from __future__ import annotations

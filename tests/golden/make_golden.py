@@ -28,11 +28,11 @@ Fixtures written to tests/golden/ (all seeds fixed):
 * halo_props.npz  — reference reductions (halo_properties.py) on a few haloes;
 * rps.npz         — reference ``halo_gas.RPS`` / ``most_bound_particle`` outputs with
   ``np.random.seed`` fixed before each call (pins the sub-sampling and energy logic);
-* substructure.npz — the driver's inline substructure block (pyHALMA.py:703-766) exec'd
+* substructure.npz — the main script's inline substructure block (pyHALMA.py:703-766) exec'd
   from the reference's own source on bridged snapshots (input and output groups stored);
 * ball.npz        — reference ``halo_gas.st_gas_dm_particles_inside`` with its MASCLET AMR
   conversion replaced by a pass-through of gas particles (inputs and the 17 outputs stored);
-* psc.npz         — the driver's phase-space cleaning block (pyHALMA.py:774-877) exec'd from
+* psc.npz         — the main script's phase-space cleaning block (pyHALMA.py:774-877) exec'd from
   the reference's own source on FoF groups of contaminated Plummer snapshots;
 * amr.npz         — reference ``halo_gas.AMRgrid_to_particles`` (with its numba kernel
   patch_to_particles) on synthetic refined patches, several boxes;
@@ -40,7 +40,7 @@ Fixtures written to tests/golden/ (all seeds fixed):
   same AMR grids, DM particles and a stellar halo (two factor_v, two Rmax);
 * properties.npz  — the reference's O(N) per-halo property functions (half-mass radii, bulk
   velocity, angular momentum, Tully-Fisher velocity, kappa_co, shape, sigma_effective,
-  sigma projections) called as the driver's property loop calls them; the f2py routines
+  sigma projections) called as the main script's property loop calls them; the f2py routines
   halo_shape / sigma_projections map onto the C restatement of the Fortran.
 """
 from __future__ import annotations
@@ -307,8 +307,8 @@ def _reference_block(refdir, start_marker, end_marker, extra_lines=1):
 
 
 def substructure_cases(fof, hp, refdir):
-    """The driver's substructure block (pyHALMA.py:703-766) run as written: its source is
-    exec'd with the reference's fof / halo_properties modules, the driver's good_groups and
+    """The main script's substructure block (pyHALMA.py:703-766) run as written: its source is
+    exec'd with the reference's fof / halo_properties modules, the main script's good_groups and
     the FoF groups of a bridged snapshot (after good_groups(MINP), as at pyHALMA.py:592)."""
     block, b0, b1 = _reference_block(refdir, "if SUBSTRUCTURE_FLAG:", "Substructures / Cut FoF bridges")
     gg, _, _ = _reference_block(refdir, "def good_groups(groups, minp):", "def good_groups(groups, minp):")
@@ -347,7 +347,7 @@ def substructure_cases(fof, hp, refdir):
 def ball_cases(hg):
     """The reference's st_gas_dm_particles_inside (halo_gas.py:223-277) run as written, with its
     AMR-grid conversion (halo_gas.py:56-141, needs MASCLET grids) replaced by a pass-through of
-    gas particles; the KD-trees are built as the driver builds them (pyHALMA.py:543-545)."""
+    gas particles; the KD-trees are built as the main script builds them (pyHALMA.py:543-545)."""
     from scipy.spatial import KDTree
     out = {}
     orig = hg.AMRgrid_to_particles
@@ -461,7 +461,7 @@ def escape_cases(hp):
 
 
 def psc_cases(fof, hp, refdir):
-    """The driver's phase-space cleaning block (pyHALMA.py:774-877: calc_cell / clean_cell per
+    """The main script's phase-space cleaning block (pyHALMA.py:774-877: calc_cell / clean_cell per
     group, the reset for small groups, the MINP cut and the sort by size) run as written on the
     FoF groups of contaminated Plummer snapshots."""
     block, b0, b1 = _reference_block(refdir, "print('---> Phase-space cleaning begins <---')",
@@ -503,8 +503,8 @@ def psc_cases(fof, hp, refdir):
 
 
 def property_cases(hp):
-    """The O(N) per-halo properties of the driver's property loop (pyHALMA.py:930-1016), called
-    as the driver calls them, on the groups and centres that phase-space cleaning leaves for a
+    """The O(N) per-halo properties of the main script's property loop (pyHALMA.py:930-1016), called
+    as the main script calls them, on the groups and centres that phase-space cleaning leaves for a
     contaminated Plummer snapshot.  The Fortran routines (halo_shape, sigma_projections) run
     through the reference's Python wrappers on the C restatement of the Fortran."""
     from oracle import phase_space as ops

@@ -96,8 +96,8 @@ def test_dense_lattices_and_random_clusters_property(cuda):
 
 
 def test_far_offsets_and_elongated_boxes(cuda):
-    """Cell keys from one FMA per axis stay exact far from the origin (a cloud 3e4 Mpc away) and
-    on grids millions of cells long on one axis (a chain of particles 0.5-1.2 LL apart)."""
+    """Cell keys stay exact far from the origin (a cloud 3e4 Mpc away) and on grids millions of
+    cells long on one axis (a chain of particles 0.5-1.2 LL apart)."""
     rng = np.random.default_rng(23)
     pts = rng.normal(0, 0.003, (20_000, 3)) + np.array([1.0e4, -2.5e4, 7.5e3])
     lab = fof.fof_labels(pts[:, 0].copy(), pts[:, 1].copy(), pts[:, 2].copy(), 0.0007)
@@ -135,3 +135,22 @@ def test_flat_and_thin_grids(cuda):
         x, y, z = (np.ascontiguousarray(v, dtype=np.float64) for v in (x, y, z))
         lab = fof.fof_labels(x, y, z, ll)
         assert np.array_equal(lab, oracle.fof_labels(x, y, z, ll)), k
+
+
+def test_integer_and_fma_key_maps(cuda):
+    """Both maps from coordinates to quarter cells: the integer one (coordinates and grid within
+    2^37 quarter cells) on a cloud straddling zero with signed zeros, subnormals and points on
+    multiples of the linking length, and the FP64 FMA one on a cloud 1e8 length units from the
+    origin (4e11 quarter cells), each against the oracle."""
+    rng = np.random.default_rng(31)
+    ll = 0.001
+    pts = rng.normal(0, 0.004, (30_000, 3))
+    special = np.array([[0.0, -0.0, 5e-324], [-5e-324, 0.0, -0.0], [2.2e-308, -2.2e-308, 0.0],
+                        [ll, -ll, 0.0], [2 * ll, 0.0, -3 * ll], [-ll, -ll, -ll], [0.5 * ll, 0.5 * ll, 0.0]])
+    grid = np.stack(np.meshgrid(*(np.arange(-4, 5) * ll,) * 3, indexing="ij"), axis=-1).reshape(-1, 3)
+    pts = np.concatenate([pts, special, grid, grid + np.array([ll * (1 + 2 ** -40), 0.0, 0.0])])
+    lab = fof.fof_labels(pts[:, 0].copy(), pts[:, 1].copy(), pts[:, 2].copy(), ll)
+    assert np.array_equal(lab, oracle.fof_labels(pts[:, 0], pts[:, 1], pts[:, 2], ll))
+    far = rng.normal(0, 0.004, (20_000, 3)) + np.array([1.0e8, -3.0e7, 2.0e8])
+    lab = fof.fof_labels(far[:, 0].copy(), far[:, 1].copy(), far[:, 2].copy(), ll)
+    assert np.array_equal(lab, oracle.fof_labels(far[:, 0], far[:, 1], far[:, 2], ll))

@@ -1,4 +1,4 @@
-"""Phase-space cleaning (halo_properties.py:113-278 calc_cell / clean_cell and the driver loop
+"""Phase-space cleaning (halo_properties.py:113-278 calc_cell / clean_cell and the main script's loop
 pyHALMA.py:774-877): the oracle and the CUDA path against the reference's own block (golden
 fixture made by exec'ing its source).
 

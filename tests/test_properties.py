@@ -1,4 +1,4 @@
-"""The O(N) per-halo properties of the driver's property loop (pyHALMA.py:930-1016) against the
+"""The O(N) per-halo properties of the main script's property loop (pyHALMA.py:930-1016) against the
 reference's own functions (golden fixture; the Fortran routines through the reference's
 wrappers on the C restatement of the Fortran) and the oracle.
 
