@@ -139,7 +139,8 @@ int halma_fof_periodic(int64_t n, const double *x, const double *y, const double
 /* Groups in the reference's output order (fof.py:76-77): groups ordered by smallest member,
  * members ascending, only groups with >= min_members members (pyHALMA.py:148-149).
  * members must hold n entries and offsets n+1 entries.  On return *n_groups groups are
- * stored: members[offsets[g] .. offsets[g+1]). */
+ * stored: members[offsets[g] .. offsets[g+1]).  A label outside [-1, n) (checked on the
+ * device, so also for device labels) fails the call with HALMA_ERR_INVALID. */
 int halma_fof_groups(int64_t n, const int32_t *labels, int32_t min_members,
                      int64_t *offsets, int32_t *members, int64_t *n_groups,
                      halma_stream_t stream);
@@ -378,7 +379,8 @@ int halma_potential_grad_f32(int64_t ns, const float *m, const float *sx, const 
 /* Per-halo reductions (FP64)                                                           */
 /* ------------------------------------------------------------------------------------ */
 /* Haloes are CSR segments: halo h owns rows offsets[h] .. offsets[h+1] of the particle
- * arrays (halo-contiguous order).  mask (optional, uint8) selects the particles that take
+ * arrays (halo-contiguous order); the offsets run from 0 to n without decreasing
+ * (HALMA_ERR_INVALID otherwise, before any device work).  mask (optional, uint8) selects the particles that take
  * part.  out is n_haloes x HALMA_RED_NFIELDS doubles, row-major. */
 enum {
     HALMA_RED_MASS = 0,  /* total_mass                                  */

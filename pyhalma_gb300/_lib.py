@@ -238,6 +238,36 @@ def as_host(a, dtype):
     return np.ascontiguousarray(a, dtype=dtype)
 
 
+_TORCH_DTYPE_NAMES = {np.float32: "float32", np.float64: "float64", np.int32: "int32", np.int64: "int64",
+                      np.uint8: "uint8"}
+
+
+def check_arrays(dtype, n, **arrays):
+    """Raise ValueError unless every given array (None entries skipped) is one-dimensional,
+    holds n entries (any number when n is None) and has exactly `dtype`; torch tensors on a
+    CUDA device must also be on the current device.  The library reads n elements of that
+    type through each raw pointer, so an array of another dtype or length would be read
+    past its end."""
+    for name, a in arrays.items():
+        if a is None:
+            continue
+        if _is_torch(a):
+            import torch
+            want = getattr(torch, _TORCH_DTYPE_NAMES[np.dtype(dtype).type])
+            if a.dtype != want:
+                raise ValueError(f"{name} must be a {want} tensor, got {a.dtype}")
+            if a.is_cuda and a.device.index != torch.cuda.current_device():
+                raise ValueError(f"{name} is on {a.device}, not on the current device "
+                                 f"cuda:{torch.cuda.current_device()}")
+        elif not isinstance(a, np.ndarray) or a.dtype != np.dtype(dtype):
+            raise ValueError(f"{name} must be a {np.dtype(dtype).name} array or tensor")
+        shape = tuple(a.shape)
+        if len(shape) != 1:
+            raise ValueError(f"{name} must be one-dimensional, got shape {shape}")
+        if n is not None and shape[0] != n:
+            raise ValueError(f"{name} has {shape[0]} entries, expected {n}")
+
+
 def pinned_empty(shape, dtype):
     """An uninitialised NumPy array in page-locked host memory from torch's caching pinned
     allocator (plain np.empty without torch or a CUDA device).  Device-to-host copies into it

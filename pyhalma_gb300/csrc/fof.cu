@@ -1396,11 +1396,16 @@ namespace {
 
 // Members per label (a label is the smallest index of its group), one atomic per distinct
 // label among the lanes of a warp: group members are often neighbours in index order.
-__global__ void group_count_kernel(int n, const int *__restrict__ labels, int *__restrict__ gsize) {
+__global__ void group_count_kernel(int n, const int *__restrict__ labels, int *__restrict__ gsize,
+                                   int *__restrict__ bad) {
     const int lane = threadIdx.x & 31;
     for (int i0 = blockIdx.x * blockDim.x; i0 < n; i0 += gridDim.x * blockDim.x) {
         const int i = i0 + threadIdx.x;
-        const int l = i < n ? labels[i] : -1;
+        int l = i < n ? labels[i] : -1;
+        if (l < -1 || l >= n) {   // not a particle index: reported, counted nowhere
+            atomicOr(bad, 1);
+            l = -1;
+        }
         const unsigned peers = __match_any_sync(0xffffffffu, l);
         if (l >= 0 && lane == __ffs(peers) - 1) atomicAdd(gsize + l, __popc(peers));
     }
@@ -1414,7 +1419,7 @@ __global__ void group_flag_kernel(int n, const int *__restrict__ labels, const i
                                   long long *__restrict__ flags) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const int l = labels[i];
-        const bool keep = l >= 0 && gsize[l] >= minp;
+        const bool keep = l >= 0 && l < n && gsize[l] >= minp;
         flags[i] = keep ? (1ll | (l == i ? 1ll << 32 : 0ll)) : 0ll;
     }
 }
@@ -1472,7 +1477,7 @@ int fof_groups_device(int n, const int *labels, int minp, int64_t *offsets, int 
     const int g1 = std::min(device_sm_count() * 8, grid_for(n, 256));
     HALMA_CUDA(cudaMemsetAsync(cnt, 0, 64, st));
     HALMA_CUDA(cudaMemsetAsync(gsize, 0, 4ull * n, st));
-    HALMA_LAUNCH(group_count_kernel, g1, 256, 0, st, n, labels, gsize);
+    HALMA_LAUNCH(group_count_kernel, g1, 256, 0, st, n, labels, gsize, cnt);
     HALMA_LAUNCH(group_flag_kernel, g1, 256, 0, st, n, labels, gsize, std::max(minp, 1), flags);
     HALMA_TRY(exclusive_sum_i64(tmp, scan_b, reinterpret_cast<const int64_t *>(flags),
                                 reinterpret_cast<int64_t *>(pre), n, st));
@@ -1480,6 +1485,7 @@ int fof_groups_device(int n, const int *labels, int minp, int64_t *offsets, int 
     int hc[4];
     HALMA_CUDA(cudaMemcpyAsync(hc, cnt, sizeof(hc), cudaMemcpyDeviceToHost, st));
     HALMA_CUDA(cudaStreamSynchronize(st));
+    if (hc[0]) return fail(HALMA_ERR_INVALID, "labels must be particle indices in [0, n) or -1");
     const int ng = hc[2], nm = hc[3];
     if (nm > 0) {
         if (ng > 1)

@@ -6,6 +6,7 @@
 // FP64 distance bits, then by halo id), after which each halo walks its own segment.
 #include <limits.h>
 #include <math.h>
+#include <string.h>
 
 #include "common.cuh"
 #include "sort.cuh"
@@ -473,8 +474,23 @@ extern "C" int halma_halo_reductions(int64_t n, int64_t n_haloes, const int64_t 
     if (n_haloes == 0) return HALMA_OK;
     if (!offsets || !out || (n > 0 && (!x || !y || !z || !vx || !vy || !vz || !m)))
         return fail(HALMA_ERR_INVALID, "null pointer");
-    std::lock_guard<std::mutex> guard(api_mutex());
     cudaStream_t st = (cudaStream_t)stream;
+    // the segments must cover the n rows in order (checked on the host: the kernels size
+    // their chunk table from n, index the rows through the offsets and sort all n rows by
+    // the halo each belongs to)
+    {
+        std::vector<int64_t> h_off(n_haloes + 1);
+        if (is_device_pointer(offsets)) {
+            HALMA_CUDA(cudaMemcpyAsync(h_off.data(), offsets, 8ull * (n_haloes + 1), cudaMemcpyDeviceToHost, st));
+            HALMA_CUDA(cudaStreamSynchronize(st));
+        } else {
+            memcpy(h_off.data(), offsets, 8ull * (n_haloes + 1));
+        }
+        if (h_off[0] != 0 || h_off[n_haloes] != n) return fail(HALMA_ERR_INVALID, "halo offsets must run from 0 to n");
+        for (int64_t h = 0; h < n_haloes; ++h)
+            if (h_off[h + 1] < h_off[h]) return fail(HALMA_ERR_INVALID, "halo offsets must not decrease");
+    }
+    std::lock_guard<std::mutex> guard(api_mutex());
     Stager sg;
     const int64_t *off = nullptr;
     const double *dx = nullptr, *dy = nullptr, *dz = nullptr, *dvx = nullptr, *dvy = nullptr, *dvz = nullptr,

@@ -37,6 +37,7 @@ def fof_labels(x, y, z, linking_length, boxsize=None):
     """
     if _lib._is_torch(x):
         n = int(x.shape[0])
+        _lib.check_arrays(np.float64, n, x=x, y=y, z=z)
         labels = _lib.like(x, (n,), np.int32)
         px, py, pz = x, y, z
     else:
@@ -64,6 +65,7 @@ def fof_groups(labels, min_members=2):
     """Groups as CSR (offsets int64 [G+1], members int32) in the reference order."""
     if _lib._is_torch(labels):
         n = int(labels.shape[0])
+        _lib.check_arrays(np.int32, n, labels=labels)
         offsets = _lib.like(labels, (n + 1,), np.int64)
         members = _lib.like(labels, (max(n, 1),), np.int32)
     else:

@@ -53,6 +53,8 @@ def bf_potential(total_mass, total_x, total_y, total_z, test_x, test_y, test_z, 
     if _lib._is_torch(test_x):
         nt = int(test_x.shape[0])
         ns = int(total_mass.shape[0])
+        _lib.check_arrays(np.float32, ns, total_mass=total_mass, total_x=total_x, total_y=total_y, total_z=total_z)
+        _lib.check_arrays(np.float32, nt, test_x=test_x, test_y=test_y, test_z=test_z)
         out = _lib.like(test_x, (nt,), np.float32)
         args = (total_mass, total_x, total_y, total_z, test_x, test_y, test_z)
     else:
@@ -183,10 +185,12 @@ def balls_inside(x, y, z, cx, cy, cz, R, strict=False):
     if _lib._is_torch(x):
         n = int(x.shape[0])
         px, py, pz = x, y, z
+        _lib.check_arrays(np.float64, n, x=x, y=y, z=z)
         b = tuple(a.to(dtype=x.dtype).reshape(-1).contiguous() for a in (cx, cy, cz, R))
     else:
         px, py, pz = (_lib.as_host(a, np.float64) for a in (x, y, z))
         n = px.shape[0]
+        _lib.check_arrays(np.float64, n, x=px, y=py, z=pz)
         b = tuple(np.atleast_1d(_lib.as_host(a, np.float64)) for a in (cx, cy, cz, R))
     k = int(b[0].shape[0])
     if any(int(a.shape[0]) != k for a in b):

@@ -54,6 +54,12 @@ def halo_reductions(offsets, x, y, z, vx, vy, vz, m, mask=None, about=None):
             about = _lib.as_host(about, np.float64).reshape(nh, N_ABOUT)
     if nh <= 0:
         return out
+    _lib.check_arrays(np.int64, nh + 1, offsets=arrs[0])
+    _lib.check_arrays(np.float64, n, **dict(zip(("x", "y", "z", "vx", "vy", "vz", "m"), arrs[1:])))
+    _lib.check_arrays(np.uint8, n, mask=mask)
+    if about is not None and (tuple(about.shape) != (nh, N_ABOUT) or str(about.dtype) not in ("float64", "torch.float64")
+                              or (_lib._is_torch(about) and not about.is_contiguous())):
+        raise ValueError(f"about must be a contiguous float64 ({nh}, {N_ABOUT}) array")
     st = _lib.lib().halma_halo_reductions(n, nh, *[_lib.ptr(a) for a in arrs], _lib.ptr(mask), _lib.ptr(about),
                                           _lib.ptr(out), _lib.stream_of(*arrs))
     _lib.check(st, "halma_halo_reductions")

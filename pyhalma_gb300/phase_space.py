@@ -30,8 +30,10 @@ def sequential_sums(values, offsets):
     dev = _lib._is_torch(values)
     if dev:
         nseg = int(offsets.shape[0]) - 1
-        out = _lib.like(values, (max(nseg, 0),), np.float64)
         n = int(values.shape[0])
+        _lib.check_arrays(np.float64, n, values=values)
+        _lib.check_arrays(np.int64, None, offsets=offsets)
+        out = _lib.like(values, (max(nseg, 0),), np.float64)
         arrs = (values, offsets)
     else:
         values = _lib.as_host(values, np.float64)

@@ -43,6 +43,8 @@ def fof_segmented_labels(x, y, z, seg_offsets, linking_length):
     if _lib._is_torch(x):
         n = int(x.shape[0])
         ns = int(seg_offsets.shape[0]) - 1
+        _lib.check_arrays(np.float64, n, x=x, y=y, z=z)
+        _lib.check_arrays(np.int64, None, seg_offsets=seg_offsets)
         px, py, pz, off = x, y, z, seg_offsets
         labels = _lib.like(x, (n,), np.int32)
     else:

@@ -71,6 +71,8 @@ def unbind_batched(offsets, x, y, z, vx, vy, vz, m, options: UnbindOptions | Non
         arrs = (offsets,) + tuple(_lib.as_host(a, np.float64) for a in (x, y, z, vx, vy, vz, m))
         n = arrs[1].shape[0]
         nh = offsets.shape[0] - 1
+    _lib.check_arrays(np.int64, None, offsets=arrs[0])
+    _lib.check_arrays(np.float64, n, **dict(zip(("x", "y", "z", "vx", "vy", "vz", "m"), arrs[1:])))
     bound = _lib.like(arrs[1], (n,), np.uint8)
     halo = _lib.like(arrs[1], (max(nh, 0), len(_lib.UB_FIELDS)), np.float64)
     phi = _lib.like(arrs[1], (n,), np.float64) if want_phi else None
@@ -108,6 +110,7 @@ def find_haloes(st_x, st_y, st_z, st_vx, st_vy, st_vz, st_mass, linking_length, 
     else:
         arrs = tuple(_lib.as_host(a, np.float64) for a in (st_x, st_y, st_z, st_vx, st_vy, st_vz, st_mass))
         n = arrs[0].shape[0]
+    _lib.check_arrays(np.float64, n, **dict(zip(("st_x", "st_y", "st_z", "st_vx", "st_vy", "st_vz", "st_mass"), arrs)))
     cap = max(n // max(int(minp), 2) + 1, 1)
     # host outputs in pinned memory: their copies are DMA transfers that overlap the unbinding
     out = _lib.like if dev else (lambda a, shape, dtype: _lib.pinned_empty(shape, dtype))

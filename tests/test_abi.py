@@ -154,3 +154,56 @@ def test_sequential_sum_rejects_bad_arguments():
     assert s(np.array([1, 2, 4], dtype=np.int64)) == _lib.ERR_INVALID             # offsets do not start at 0
     assert L.halma_sequential_sum_f64(4, None, 2, _lib.ptr(np.array([0, 2, 4], dtype=np.int64)), _lib.ptr(out),
                                       None) == _lib.ERR_INVALID
+
+
+def test_halo_reductions_rejects_offsets_outside_the_rows():
+    L = _lib.lib()
+    x = np.zeros(4)
+    out = np.zeros((2, len(_lib.RED_FIELDS)))
+    r = lambda o: L.halma_halo_reductions(4, len(o) - 1, _lib.ptr(o), *[_lib.ptr(x)] * 7, None, None, _lib.ptr(out),
+                                          None)
+    assert r(np.array([0, 2, 5], dtype=np.int64)) == _lib.ERR_INVALID     # past the 4 rows
+    assert r(np.array([0, 3, 2], dtype=np.int64)) == _lib.ERR_INVALID     # decreasing
+    assert r(np.array([1, 2, 4], dtype=np.int64)) == _lib.ERR_INVALID     # does not start at 0
+    assert r(np.array([0, 1, 3], dtype=np.int64)) == _lib.ERR_INVALID     # rows left outside every halo
+    assert b"offsets" in L.halma_last_error()
+
+
+def test_wrappers_check_dtypes_and_lengths_before_the_library_reads():
+    """Raw pointers carry no type: a float32 tensor read as float64, or a short array read to
+    n, would be read past its end.  The Python layer refuses both before any call."""
+    torch = pytest.importorskip("torch")
+    from pyhalma_gb300 import fof, halo_gas, halo_properties, phase_space, substructure, unbinding
+    x64, x32 = torch.zeros(6, dtype=torch.float64), torch.zeros(6, dtype=torch.float32)
+    with pytest.raises(ValueError, match="float64"):
+        fof.fof_labels(x32, x32, x32, 1.0)
+    with pytest.raises(ValueError, match="entries"):
+        fof.fof_labels(x64, x64[:5], x64, 1.0)
+    with pytest.raises(ValueError, match="int32"):
+        fof.fof_groups(torch.zeros(6, dtype=torch.int64))
+    with pytest.raises(ValueError, match="float32"):
+        halo_gas.bf_potential(x64, x64, x64, x64, x32, x32, x32)
+    with pytest.raises(ValueError, match="entries"):
+        halo_gas.bf_potential(x32, x32, x32, x32[:4], x32, x32, x32)
+    with pytest.raises(ValueError, match="float64"):
+        halo_gas.balls_inside(x32, x32, x32, 0.0, 0.0, 0.0, 1.0)
+    with pytest.raises(ValueError, match="entries"):
+        halo_gas.balls_inside(np.zeros(6), np.zeros(5), np.zeros(6), 0.0, 0.0, 0.0, 1.0)
+    off = np.array([0, 6], dtype=np.int64)
+    with pytest.raises(ValueError, match="entries"):
+        unbinding.unbind_batched(off, np.zeros(6), np.zeros(6), np.zeros(5), np.zeros(6), np.zeros(6), np.zeros(6),
+                                 np.ones(6))
+    with pytest.raises(ValueError, match="int64"):
+        unbinding.unbind_batched(off.astype(np.int32), *[x64] * 7)
+    with pytest.raises(ValueError, match="float64"):
+        unbinding.find_haloes(*[x64] * 6, x32, 1.0)
+    with pytest.raises(ValueError, match="entries"):
+        halo_properties.halo_reductions(off, *[np.zeros(6)] * 6, np.zeros(7))
+    with pytest.raises(ValueError, match="mask"):
+        halo_properties.halo_reductions(off, *[np.zeros(6)] * 7, mask=np.ones(5, dtype=np.uint8))
+    with pytest.raises(ValueError, match="about"):
+        halo_properties.halo_reductions(off, *[x64] * 7, about=torch.zeros(8, dtype=torch.float32))
+    with pytest.raises(ValueError, match="float64"):
+        phase_space.sequential_sums(x32, torch.tensor([0, 6]))
+    with pytest.raises(ValueError, match="int64"):
+        substructure.fof_segmented_labels(x64, x64, x64, torch.tensor([0, 6], dtype=torch.int32), 1.0)

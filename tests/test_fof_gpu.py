@@ -154,3 +154,16 @@ def test_integer_and_fma_key_maps(cuda):
     far = rng.normal(0, 0.004, (20_000, 3)) + np.array([1.0e8, -3.0e7, 2.0e8])
     lab = fof.fof_labels(far[:, 0].copy(), far[:, 1].copy(), far[:, 2].copy(), ll)
     assert np.array_equal(lab, oracle.fof_labels(far[:, 0], far[:, 1], far[:, 2], ll))
+
+
+def test_groups_reject_labels_that_are_not_particle_indices(cuda):
+    """Labels index the per-group counters; one outside [-1, n) is refused by the kernel that
+    reads it (host and device labels), and the next call works as before."""
+    import torch
+    for bad in (np.array([0, 0, 5, -1, 2], dtype=np.int32), np.array([0, 0, -2, -1, 2], dtype=np.int32)):
+        with pytest.raises(ValueError, match="labels"):
+            fof.fof_groups(bad)
+        with pytest.raises(ValueError, match="labels"):
+            fof.fof_groups(torch.from_numpy(bad).to(cuda))
+    off, mem = fof.fof_groups(np.array([0, 0, -1, 3, 3, 3], dtype=np.int32))
+    assert off.tolist() == [0, 2, 5] and mem.tolist() == [0, 1, 3, 4, 5]

@@ -105,3 +105,15 @@ def test_half_mass_walk_is_the_sequential_sum(cuda):
         pl = np.arange(off[k], off[k + 1])
         r05 = ref.half_mass_radius(0.0, 0.0, 0.0, about[k][6], pl, x, z0, z0, m)
         assert out[k, 8] == r05, (k, sizes[k // 3], out[k, 8], r05)
+
+
+def test_device_offsets_outside_the_rows_are_refused(cuda):
+    import torch
+    x = torch.zeros(4, dtype=torch.float64, device=cuda)
+    with pytest.raises(ValueError, match="offsets"):
+        hp.halo_reductions(torch.tensor([0, 2, 5], device=cuda), *[x] * 7)
+    with pytest.raises(ValueError, match="offsets"):
+        hp.halo_reductions(torch.tensor([0, 3, 2, 4], device=cuda), *[x] * 7)
+    out = hp.halo_reductions(torch.tensor([0, 1, 4], device=cuda), *[x] * 6, torch.ones(4, dtype=torch.float64,
+                                                                                              device=cuda))
+    assert out[:, 0].cpu().tolist() == [1.0, 3.0]
