@@ -15,6 +15,7 @@ self_offset=0) differentiates the self-potential, autograd summing both contribu
 """
 from __future__ import annotations
 
+import numpy as np
 import torch
 
 from . import _lib
@@ -44,6 +45,8 @@ class SoftenedPotential(torch.autograd.Function):
         for a in args:
             if a.dtype != torch.float32 or not a.is_cuda:
                 raise ValueError("SoftenedPotential takes float32 CUDA tensors")
+        _lib.check_arrays(np.float32, int(args[0].shape[0]), sx=args[0], sy=args[1], sz=args[2], m=args[3])
+        _lib.check_arrays(np.float32, int(args[4].shape[0]), tx=args[4], ty=args[5], tz=args[6])
         ctx.eps = float(eps)
         ctx.self_offset = self_offset
         ctx.save_for_backward(*args)

@@ -226,6 +226,10 @@ def halo_property_table(offsets, members, st_x, st_y, st_z, st_vx, st_vy, st_vz,
     G = offsets.shape[0] - 1
     if centre.shape[0] != G:
         raise ValueError("one centre row (cx, cy, cz, mass, rmax) per group")
+    _lib.check_arrays(np.float64, arrs[0].shape[0], **dict(zip(("st_x", "st_y", "st_z", "st_vx", "st_vy", "st_vz",
+                                                               "st_mass"), arrs)))
+    if G > 0 and not 0 <= offsets[-1] <= members.shape[0]:
+        raise ValueError(f"the offsets cover {offsets[-1]} members, {members.shape[0]} given")
     out = np.zeros((max(G, 1), len(_lib.PROP_FIELDS)), dtype=np.float64)
     if G > 0:
         st = _lib.lib().halma_halo_properties(arrs[0].shape[0], *[_lib.ptr(a) for a in arrs], G, _lib.ptr(offsets),

@@ -63,6 +63,8 @@ def clean_groups(offsets, members, st_x, st_y, st_z, st_vx, st_vy, st_vz, st_mas
         raise ValueError("particle arrays must have the same length")
     G = offsets.shape[0] - 1
     nm = members.shape[0]
+    if G > 0 and not 0 <= offsets[-1] <= nm:
+        raise ValueError(f"the offsets cover {offsets[-1]} members, {nm} given")
     control = np.zeros(max(nm, 1), dtype=np.uint8)
     which = np.zeros((3, max(nm, 1)), dtype=np.int32)
     n_which = np.zeros(max(G, 1), dtype=np.int64)

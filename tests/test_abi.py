@@ -207,3 +207,15 @@ def test_wrappers_check_dtypes_and_lengths_before_the_library_reads():
         phase_space.sequential_sums(x32, torch.tensor([0, 6]))
     with pytest.raises(ValueError, match="int64"):
         substructure.fof_segmented_labels(x64, x64, x64, torch.tensor([0, 6], dtype=torch.int32), 1.0)
+
+
+def test_group_wrappers_check_member_counts():
+    from pyhalma_gb300 import halo_properties, phase_space
+    z = np.zeros(6)
+    off, mem = np.array([0, 4, 9], dtype=np.int64), np.arange(6, dtype=np.int32)
+    with pytest.raises(ValueError, match="members"):
+        phase_space.clean_groups(off, mem, *[z] * 7, 0.001, 1.0, 3.0)
+    with pytest.raises(ValueError, match="members"):
+        halo_properties.halo_property_table(off, mem, *[z] * 7, np.zeros((2, 5)), 0.001)
+    with pytest.raises(ValueError, match="entries"):
+        halo_properties.halo_property_table(off[:2], mem, *[z] * 6, np.zeros(5), np.zeros((1, 5)), 0.001)
