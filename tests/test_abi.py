@@ -219,3 +219,37 @@ def test_group_wrappers_check_member_counts():
         halo_properties.halo_property_table(off, mem, *[z] * 7, np.zeros((2, 5)), 0.001)
     with pytest.raises(ValueError, match="entries"):
         halo_properties.halo_property_table(off[:2], mem, *[z] * 6, np.zeros(5), np.zeros((1, 5)), 0.001)
+
+
+C_CALLER = r"""
+#include <stdio.h>
+#include "halma.h"
+int main(void) {
+    double x[4] = {0, 0, 0, 0};
+    int32_t lab[4];
+    int64_t ng = 0;
+    if (halma_abi_version() != 1) return 1;
+    if (halma_fof(4, x, x, x, -1.0, lab, &ng, NULL) != HALMA_ERR_INVALID) return 2;
+    printf("%s|%s\n", halma_status_string(HALMA_ERR_INVALID), halma_last_error());
+    return 0;
+}
+"""
+
+
+def test_plain_c_caller_compiles_links_and_calls(tmp_path):
+    """The boundary is plain C: a C99 program (-pedantic, no C++ and no CUDA headers) includes
+    halma.h, links the shared library and gets the documented status and message."""
+    import shutil
+    import subprocess
+    gcc = shutil.which("gcc")
+    if gcc is None:
+        pytest.skip("no C compiler")
+    src, exe = tmp_path / "caller.c", tmp_path / "caller"
+    src.write_text(C_CALLER)
+    libdir = os.path.dirname(_lib.LIB_PATH)
+    _lib.lib()
+    subprocess.run([gcc, "-std=c99", "-Wall", "-Wextra", "-pedantic", "-Werror", "-I", os.path.dirname(HEADER),
+                    str(src), "-L", libdir, "-lhalma_gb300", f"-Wl,-rpath,{libdir}", "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True)
+    assert out.returncode == 0, out
+    assert out.stdout.strip() == "invalid argument|linking length must be finite and >= 0"
